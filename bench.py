@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Ray-query benchmark of the GB300 render hot path (rtcIntersect1/rtcOccluded1 contract).
+
+Workload (one "step"): 64 displaced icospheres at subdivision level 6 (5,242,880 triangles) plus a
+2-triangle ground plane; 4,194,304 coherent primary rays (2048 x 2048 pinhole) and 4,194,304 incoherent
+rays (random surface points, cosine directions); closest-hit and any-hit queries of both sets, i.e.
+16,777,216 queries per step.  Rays are re-staged from pristine copies in HBM before each step (the ray
+records are updated in place by the queries).  Inputs (1.2 GB of ray records, 0.4 GB of BVH) are far
+larger than the 129 MB L2, so no extra flush is done.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Prints one JSON line.  `value` is device-timed throughput with rays resident in HBM; `e2e` is the same
+metric through the host-memory C ABI entry points (sel_intersect1M / sel_occluded1M) from pinned host
+buffers, copies included; `cpu_baseline` is the CPU oracle traversal on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+QUERY_BYTES = {"intersect": 56, "occluded": 36}  # algorithmic bytes per query (ray in + result out)
+WORKLOAD = ("ray queries: 64 displaced icospheres (subdivision 6, 5,242,880 triangles) + 200x200 ground plane; "
+            "4,194,304 coherent primary rays (2048x2048 pinhole) + 4,194,304 incoherent surface rays "
+            "(cosine directions); closest-hit + any-hit of each set = 16,777,216 queries per step")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--level", type=int, default=6)
+    p.add_argument("--width", type=int, default=2048)
+    p.add_argument("--cpu-sample", type=int, default=65536, help="rays per query set in each CPU sample step")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        d = json.loads(path.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the query kernels from the committed ncu summary (key=value lines)."""
+    path = ROOT / "profiles" / "query_kernels_dram.txt"
+    out = {}
+    if path.exists():
+        for line in path.read_text().splitlines():
+            if line.startswith("#") or "=" not in line:
+                continue
+            k, v = line.split("=", 1)
+            try:
+                out[k.strip()] = float(v.strip())
+            except ValueError:
+                pass
+    return out
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks/throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline_run(soup, sets, sample: int, steps: int, threads: int):
+    """CPU oracle traversal (binned-SAH BVH + watertight test, all host threads) on a bounded sample."""
+    import oracle
+    import selas_gb300 as sel
+    bvh = oracle.OracleBvh(soup)
+    rng = np.random.default_rng(123)
+    total_q, total_t = 0, 0.0
+    for _ in range(steps):
+        for org, d in sets:
+            pick = rng.choice(org.shape[0], sample, replace=False)
+            rh = sel.make_rayhits(org[pick], d[pick])
+            rs = sel.make_rays(org[pick], d[pick])
+            t0 = time.perf_counter()
+            bvh.intersect(rh, threads)
+            bvh.occluded(rs, threads)
+            total_t += time.perf_counter() - t0
+            total_q += 2 * sample
+    return total_q / total_t / 1e6, total_q, total_t
+
+
+def cpu_desc():
+    try:
+        import platform
+        return f"{platform.machine()} {os.cpu_count()} cores"
+    except Exception:
+        return "unknown"
+
+
+def run_reference(args):
+    """CPU implementation of the path on the host cores (the oracle port: the reference's own Embree/TBB
+    path is a closed Windows/macOS binary)."""
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from selas_gb300 import scenes
+    data, coherent, incoherent = scenes.ray_query_workload(level=args.level, width=args.width, height=args.width)
+    soup = data.soup()
+    threads = os.cpu_count() or 1
+    # warm-up (untimed) then K timed bounded-sample steps
+    cpu_baseline_run(soup, [coherent, incoherent], max(1024, args.cpu_sample // 8), max(1, args.warmup), threads)
+    v, q, t = cpu_baseline_run(soup, [coherent, incoherent], args.cpu_sample, args.steps, threads)
+    line = {
+        "impl": "reference", "metric": "Mrays/s", "value": round(v, 3), "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": f"{args.cpu_sample} rays of each set per step",
+                   "parallelism": "cpu threads"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{q} queries ({args.cpu_sample} rays x 2 sets x closest+any per step, "
+                                   f"{args.steps} steps) on {cpu_desc()}"},
+        "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Embree 3.2 ships only as Windows/macOS binaries in the reference; the CPU oracle port of the "
+                "same query contract (binned-SAH BVH, watertight test) stands in for it",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from selas_gb300._build import build_library
+    build_library()
+    import selas_gb300 as sel
+    from selas_gb300 import scenes
+
+    data, coherent, incoherent = scenes.ray_query_workload(level=args.level, width=args.width, height=args.width)
+    n_co, n_inc = coherent[0].shape[0], incoherent[0].shape[0]
+    dev = sel.Device(local)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    recs = {
+        "co_hit": sel.make_rayhits(*coherent), "inc_hit": sel.make_rayhits(*incoherent),
+        "co_occ": sel.make_rays(*coherent), "inc_occ": sel.make_rays(*incoherent),
+    }
+    pristine = {k: torch.from_numpy(v.view(np.uint8)).cuda() for k, v in recs.items()}
+    work = {k: torch.empty_like(v) for k, v in pristine.items()}
+    counts = {"co_hit": n_co, "inc_hit": n_inc, "co_occ": n_co, "inc_occ": n_inc}
+    kinds = {"co_hit": "intersect", "inc_hit": "intersect", "co_occ": "occluded", "inc_occ": "occluded"}
+    queries_per_step = sum(counts.values())
+
+    def make_scene(kind):
+        sc = sel.Scene(dev, kind)
+        data.attach_to(sc)
+        sc.commit()
+        return sc
+
+    def device_run(sc, steps, warmup, sample_clocks=False):
+        def step(evs):
+            with torch.cuda.stream(stream):
+                for k in work:
+                    work[k].copy_(pristine[k], non_blocking=True)
+                for k in work:
+                    if evs is not None:
+                        evs[k][0].record(stream)
+                    if kinds[k] == "intersect":
+                        sc.intersect_device(work[k].data_ptr(), counts[k], sp)
+                    else:
+                        sc.occluded_device(work[k].data_ptr(), counts[k], sp)
+                    if evs is not None:
+                        evs[k][1].record(stream)
+
+        for _ in range(warmup):
+            step(None)
+        dev.sync(sp)
+        evs_all = []
+        sampler = ClockSampler(local) if sample_clocks else None
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            evs = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for k in work}
+            step(evs)
+            evs_all.append(evs)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        if world > 1:
+            torch.distributed.barrier()
+        dev.sync(sp)
+        ms = t0.elapsed_time(t1)
+        per_kernel = {k: statistics.mean(e[k][0].elapsed_time(e[k][1]) for e in evs_all) for k in work}
+        return ms, per_kernel, clocks
+
+    wide = make_scene(sel.SEL_BVH_WIDE8_Q8)
+    info = wide.info()
+    ms, per_kernel, clocks = device_run(wide, args.steps, args.warmup, sample_clocks=(rank == 0))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * queries_per_step / (ms_step * 1e-3) / 1e6
+
+    # the plain FP32 binary-BVH path on the same workload (the comparison the quantised BVH is held to)
+    binary = make_scene(sel.SEL_BVH_BINARY_FP32)
+    binfo = binary.info()
+    ms_b, per_kernel_b, _ = device_run(binary, max(2, args.steps // 2), 1)
+    plain_value = queries_per_step / (ms_b / max(2, args.steps // 2) * 1e-3) / 1e6
+    binary.release()
+
+    # end to end through the host-memory C ABI (pinned host buffers, copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        pinned = {k: torch.empty(v.nbytes, dtype=torch.uint8, pin_memory=True) for k, v in recs.items()}
+        host = {k: pinned[k].numpy().view(recs[k].dtype) for k in recs}
+        for k in host:
+            np.copyto(host[k], recs[k])
+        lib = sel.lib()
+
+        def e2e_step():
+            el = 0.0
+            for k in host:
+                np.copyto(host[k], recs[k])  # restage outside the timed calls
+                t_0 = time.perf_counter()
+                if kinds[k] == "intersect":
+                    sel.check(lib.sel_intersect1M(wide.handle, host[k].ctypes.data, counts[k], 96))
+                else:
+                    sel.check(lib.sel_occluded1M(wide.handle, host[k].ctypes.data, counts[k], 48))
+                el += time.perf_counter() - t_0
+            return el
+
+        e2e_step()
+        e2e_steps = max(2, min(args.steps, 5))
+        el = sum(e2e_step() for _ in range(e2e_steps))
+        h2d = sum(v.nbytes for v in recs.values())
+        e2e = {"value": round(world * queries_per_step * e2e_steps / el / 1e6, 3), "unit": "Mrays/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
+               "path": "sel_intersect1M / sel_occluded1M from pinned host memory", "steps": e2e_steps}
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    dom = max(per_kernel, key=per_kernel.get)
+    alg_bytes = counts[dom] * QUERY_BYTES[kinds[dom]]
+    achieved = alg_bytes / (per_kernel[dom] * 1e-3) / 1e9
+    traffic = ncu_traffic().get(f"wide8.{dom}")
+    roofline = {"bound": "hbm", "kernel": f"k_{kinds[dom]}<wide8> ({dom})", "achieved": round(achieved, 2),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+                "avg_launch_ms": round(per_kernel[dom], 4)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, q, t = cpu_baseline_run(data.soup(), [coherent, incoherent], args.cpu_sample, 2, threads)
+        cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"{q} queries (2 x {args.cpu_sample} rays of each set, closest+any) on {cpu_desc()}, "
+                         f"{t:.1f} s"}
+
+    per_set = {k: round(counts[k] / (per_kernel[k] * 1e-3) / 1e6, 1) for k in per_kernel}
+    per_set_b = {k: round(counts[k] / (per_kernel_b[k] * 1e-3) / 1e6, 1) for k in per_kernel_b}
+    line = {
+        "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "bvh": "8-wide, 8-bit quantised child bounds",
+                   "l2": "no flush: ray records (1.2 GB) and BVH exceed the 129 MB L2",
+                   "parallelism": f"replicas x{world}", "triangles": int(info.triangle_count),
+                   "bvh_nodes": int(info.node_count), "bvh_depth": int(info.max_depth),
+                   "bvh_device_mb": round(info.device_bytes / 2**20, 1), "bvh_build_ms": round(info.build_ms, 1)},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": 4 * args.steps,
+        "per_set_mrays": per_set,
+        "plain_fp32_binary_bvh": {"value": round(plain_value, 3), "unit": "Mrays/s", "per_set_mrays": per_set_b,
+                                  "bvh_nodes": int(binfo.node_count), "bvh_device_mb": round(binfo.device_bytes / 2**20, 1),
+                                  "speedup_of_quantised_wide": round(value / world / plain_value, 3)},
+    }
+    wide.release()
+    dev.release()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

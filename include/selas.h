@@ -1,0 +1,149 @@
+/*
+ * selas.h - C ABI of the GB300-native Selas render hot path.
+ *
+ * One shared library, libselas_gb300.so, exports every function declared here.  All functions return
+ * an int status (SEL_OK == 0) and never abort; sel_get_last_error() describes the most recent failure
+ * on the calling host thread.  No function takes or returns a PyTorch, CUDA-runtime or C++ type:
+ * device memory is passed as plain pointers and CUDA streams as void*.
+ *
+ * Ray/hit records are byte-identical to Embree 3.2's RTCRay / RTCHit / RTCRayHit
+ * (Middleware/embree-latest/include/embree3/rtcore_ray.h:26-61), so arrays built for rtcIntersect1M /
+ * rtcOccluded1M can be handed to the functions below unchanged.
+ */
+#ifndef SELAS_GB300_H
+#define SELAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Status codes                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+enum {
+    SEL_OK = 0,
+    SEL_ERR_INVALID_ARGUMENT = 1,  /* null handle, bad size or stride, unknown enum value          */
+    SEL_ERR_OUT_OF_MEMORY = 2,     /* device or host allocation failed                             */
+    SEL_ERR_CUDA = 3,              /* a CUDA runtime call failed (text in sel_get_last_error)      */
+    SEL_ERR_INVALID_OPERATION = 4, /* e.g. query on a scene that was never committed               */
+    SEL_ERR_DEVICE_LIMIT = 5       /* a kernel hit its iteration cap or stack limit and stopped    */
+};
+
+/* Mirrors RTC_INVALID_GEOMETRY_ID and RTC_MAX_INSTANCE_LEVEL_COUNT (rtcore_common.h:66,72). */
+#define SEL_INVALID_GEOMETRY_ID ((unsigned int)-1)
+#define SEL_MAX_INSTANCE_LEVEL_COUNT 2
+
+/* Layout of RTCRay (rtcore_ray.h:26-43): 48 bytes, 16-byte aligned. */
+typedef struct __attribute__((aligned(16))) SelRay {
+    float org_x, org_y, org_z;
+    float tnear;
+    float dir_x, dir_y, dir_z;
+    float time;
+    float tfar;
+    unsigned int mask;
+    unsigned int id;
+    unsigned int flags;
+} SelRay;
+
+/* Layout of RTCHit (rtcore_ray.h:46-57): 36 bytes. */
+typedef struct SelHit {
+    float Ng_x, Ng_y, Ng_z;
+    float u, v;
+    unsigned int primID;
+    unsigned int geomID;
+    unsigned int instID[SEL_MAX_INSTANCE_LEVEL_COUNT];
+} SelHit;
+
+/* Layout of RTCRayHit (rtcore_ray.h:59-63): 96 bytes (hit at offset 48). */
+typedef struct SelRayHit {
+    SelRay ray;
+    SelHit hit;
+} SelRayHit;
+
+typedef struct SelDeviceTy* SelDevice; /* replaces RTCDevice (rtcore_device.h) */
+typedef struct SelSceneTy* SelScene;   /* replaces RTCScene  (rtcore_scene.h)  */
+
+/* Acceleration structure built by sel_scene_commit. */
+enum {
+    SEL_BVH_WIDE8_Q8 = 0,    /* 8-wide BVH, child bounds quantised to 8 bits per axis, rounded outward */
+    SEL_BVH_BINARY_FP32 = 1  /* binary BVH with FP32 child bounds: the plain GPU path                   */
+};
+
+typedef struct SelSceneInfo {
+    uint64_t triangle_count;
+    uint64_t node_count;
+    uint64_t device_bytes;     /* nodes + triangles resident in HBM                */
+    uint32_t bvh_kind;
+    uint32_t max_depth;        /* deepest node level (root = 1)                    */
+    double build_ms;           /* host-side SAH build + layout                     */
+    double upload_ms;          /* host -> HBM copy                                 */
+    float bounds_lo[3];
+    float bounds_hi[3];
+} SelSceneInfo;
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Errors                                                                                            */
+/* ------------------------------------------------------------------------------------------------ */
+const char* sel_get_last_error(void);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Device lifetime.  Replaces rtcNewDevice / rtcReleaseDevice (rtcore_device.h; called at           */
+/* Source/Applications/Selas/Source/main.cpp:99).  cuda_device selects the GPU.                      */
+/* ------------------------------------------------------------------------------------------------ */
+int sel_device_new(int cuda_device, SelDevice* out_device);
+int sel_device_release(SelDevice device);
+/* Waits for `stream` and returns SEL_ERR_DEVICE_LIMIT if any kernel of this device raised its error
+ * word since the last call (the word is cleared by the call). */
+int sel_device_sync(SelDevice device, void* stream);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Scene lifetime.  Replaces rtcNewScene, rtcNewGeometry(RTC_GEOMETRY_TYPE_TRIANGLE) +               */
+/* rtcSetSharedGeometryBuffer + rtcAttachGeometryByID, rtcCommitScene and rtcReleaseScene as used in */
+/* Source/Core/SceneLib/ModelResource.cpp:236-297,461-468 and SceneResource.cpp:310-312.            */
+/* ------------------------------------------------------------------------------------------------ */
+int sel_scene_new(SelDevice device, SelScene* out_scene);
+int sel_scene_set_bvh_kind(SelScene scene, int bvh_kind);
+/* vertices: vertex_count records of 3 floats (x,y,z) every vertex_stride_bytes bytes (>= 12);
+ * indices: triangle_count x 3 unsigned ints.  The data is copied; the caller may free it after the
+ * call.  geomID is reported in SelHit.geomID; primID is the triangle's index within this mesh. */
+int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const float* vertices,
+                                   size_t vertex_count, size_t vertex_stride_bytes,
+                                   const unsigned int* indices, size_t triangle_count);
+int sel_scene_commit(SelScene scene);
+int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info);
+int sel_scene_release(SelScene scene);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Ray queries.                                                                                      */
+/* Closest hit: a triangle is hit when the watertight test of Woop, Benthin and Wald (JCGT 2013)     */
+/* accepts it with tnear <= t <= tfar.  Of all hit triangles the one with the smallest t wins; equal */
+/* t is decided by the smaller (geomID, primID).  On a hit tfar, Ng = (v1-v0)x(v2-v0), u, v (so that */
+/* p = (1-u-v)v0 + u v1 + v v2), primID, geomID are written and instID[0..1] are set to             */
+/* SEL_INVALID_GEOMETRY_ID; on a miss the record is left untouched.                                  */
+/* Any hit: tfar is set to -inf when some triangle is hit in [tnear, tfar].                          */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* Host-memory forms.  Replace rtcIntersect1 / rtcOccluded1 (rtcore_scene.h:94,118; called at        */
+/* Source/Applications/Selas/Source/PathTracer.cpp:88,116) and the stream forms rtcIntersect1M /     */
+/* rtcOccluded1M (rtcore_scene.h:106,130).  They copy the records to HBM, trace, copy back and       */
+/* return when the results are in host memory.                                                       */
+int sel_intersect1(SelScene scene, SelRayHit* rayhit);
+int sel_occluded1(SelScene scene, SelRay* ray);
+int sel_intersect1M(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride);
+int sel_occluded1M(SelScene scene, SelRay* rays, unsigned int M, size_t byte_stride);
+
+/* Device-memory forms: d_rayhits / d_rays point to HBM, work is queued on `stream` (void* holding a
+ * cudaStream_t, NULL = default stream) and the call returns without waiting.  Replace the packet
+ * queries rtcIntersect8 / rtcOccluded8 of Source/Applications/Selas/Source/DeferredPathTracer.cpp:191,267
+ * for whole ray batches.  Use sel_device_sync to wait and collect kernel errors. */
+int sel_intersect_device(SelScene scene, SelRayHit* d_rayhits, unsigned int n, void* stream);
+int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SELAS_GB300_H */

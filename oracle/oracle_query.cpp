@@ -1,0 +1,412 @@
+// ORACLE - test infrastructure only.  Nothing in the product links or calls this file; only tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg load liboracle.so, as the checker.
+//
+// CPU restatement of the ray-query contract the reference integrators rely on:
+//   * closest hit  - Embree rtcIntersect1 as called by RayPick, Source/Applications/Selas/Source/PathTracer.cpp:95-139
+//                    (tnear/tfar in, tfar/Ng/u/v/primID/geomID/instID out; geomID stays -1 on a miss);
+//   * any hit      - Embree rtcOccluded1 as called by OcclusionRay, PathTracer.cpp:71-92 (tfar = -inf on a hit).
+// Embree 3.2 itself ships only as a Windows/macOS binary (Middleware/embree-latest), so parity against it
+// is unpinned here; this file pins the contract instead with an independent CPU implementation of the
+// watertight test of Woop, Benthin and Wald (JCGT 2013) and the order-independent tie rule (smallest t,
+// then smallest (geomID, primID)).  Two traversals are provided: brute force over every triangle (the
+// definition) and an SAH BVH of this file's own (for large scenes and for the CPU baseline).
+//
+// Compiled with -ffp-contract=off; every fused multiply-add is an explicit std::fma.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct Ray {
+    float org[3];
+    float tnear;
+    float dir[3];
+    float time;
+    float tfar;
+    uint32_t mask, id, flags;
+};
+struct RayHit {
+    Ray ray;
+    float ng[3];
+    float u, v;
+    uint32_t prim, geom, inst[2];
+    uint32_t pad[3];
+};
+static_assert(sizeof(Ray) == 48, "Ray");
+static_assert(sizeof(RayHit) == 96, "RayHit");
+
+struct Tri {
+    float v[3][3];
+    uint32_t prim, geom;
+};
+
+struct Setup {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+Setup setup(const float* d) {
+    Setup s;
+    const float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+    s.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    s.kx = s.kz == 2 ? 0 : s.kz + 1;
+    s.ky = s.kx == 2 ? 0 : s.kx + 1;
+    if (d[s.kz] < 0.0f) std::swap(s.kx, s.ky);
+    s.sx = d[s.kx] / d[s.kz];
+    s.sy = d[s.ky] / d[s.kz];
+    s.sz = 1.0f / d[s.kz];
+    return s;
+}
+
+bool intersect(const Setup& s, const float* o, const Tri& tri, float tnear, float tfar, float& t, float& u, float& v) {
+    float A[3], B[3], C[3];
+    for (int k = 0; k < 3; ++k) {
+        A[k] = tri.v[0][k] - o[k];
+        B[k] = tri.v[1][k] - o[k];
+        C[k] = tri.v[2][k] - o[k];
+    }
+    const float Ax = std::fma(-s.sx, A[s.kz], A[s.kx]);
+    const float Ay = std::fma(-s.sy, A[s.kz], A[s.ky]);
+    const float Bx = std::fma(-s.sx, B[s.kz], B[s.kx]);
+    const float By = std::fma(-s.sy, B[s.kz], B[s.ky]);
+    const float Cx = std::fma(-s.sx, C[s.kz], C[s.kx]);
+    const float Cy = std::fma(-s.sy, C[s.kz], C[s.ky]);
+    const float cybx = Cy * Bx, aycx = Ay * Cx, byax = By * Ax;
+    float U = std::fma(Cx, By, -cybx);
+    float V = std::fma(Ax, Cy, -aycx);
+    float W = std::fma(Bx, Ay, -byax);
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = float(double(Cx) * double(By) - double(Cy) * double(Bx));
+        V = float(double(Ax) * double(Cy) - double(Ay) * double(Cx));
+        W = float(double(Bx) * double(Ay) - double(By) * double(Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = (U + V) + W;
+    if (det == 0.0f) return false;
+    const float Az = s.sz * A[s.kz], Bz = s.sz * B[s.kz], Cz = s.sz * C[s.kz];
+    const float wcz = W * Cz;
+    const float T = std::fma(U, Az, std::fma(V, Bz, wcz));
+    const float rcp = 1.0f / det;
+    const float tt = T * rcp;
+    if (!(tt >= tnear && tt <= tfar)) return false;
+    t = tt;
+    u = V * rcp;
+    v = W * rcp;
+    return true;
+}
+
+void normal(const Tri& tri, float* ng) {
+    float e1[3], e2[3];
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = tri.v[1][k] - tri.v[0][k];
+        e2[k] = tri.v[2][k] - tri.v[0][k];
+    }
+    const float a = e1[2] * e2[1], b = e1[0] * e2[2], c = e1[1] * e2[0];
+    ng[0] = std::fma(e1[1], e2[2], -a);
+    ng[1] = std::fma(e1[2], e2[0], -b);
+    ng[2] = std::fma(e1[0], e2[1], -c);
+}
+
+uint64_t key_of(const Tri& t) { return (uint64_t(t.geom) << 32) | t.prim; }
+
+struct Best {
+    float t, u, v;
+    int64_t tri = -1;
+    uint64_t key = ~0ull;
+};
+
+// candidate accepted when tnear <= t <= current tfar; ties on t go to the smaller key
+inline void offer(const Setup& s, const Ray& r, const Tri& tri, int64_t index, float& tfar, Best& best) {
+    float t, u, v;
+    if (!intersect(s, r.org, tri, r.tnear, tfar, t, u, v)) return;
+    const uint64_t k = key_of(tri);
+    if (t < tfar || k < best.key) {
+        tfar = t;
+        best.t = t; best.u = u; best.v = v; best.tri = index; best.key = k;
+    }
+}
+
+void write_hit(RayHit& rh, const Tri& tri, const Best& b) {
+    rh.ray.tfar = b.t;
+    normal(tri, rh.ng);
+    rh.u = b.u;
+    rh.v = b.v;
+    rh.prim = tri.prim;
+    rh.geom = tri.geom;
+    rh.inst[0] = rh.inst[1] = 0xffffffffu;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Oracle BVH: binary, binned SAH (16 bins), leaves of <= 4 triangles.
+// ---------------------------------------------------------------------------------------------------
+struct Box {
+    float lo[3], hi[3];
+    void reset() { for (int a = 0; a < 3; ++a) { lo[a] = INFINITY; hi[a] = -INFINITY; } }
+    void grow(const Box& b) { for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], b.lo[a]); hi[a] = std::max(hi[a], b.hi[a]); } }
+    float area() const {
+        if (lo[0] > hi[0]) return 0.0f;
+        const float x = hi[0] - lo[0], y = hi[1] - lo[1], z = hi[2] - lo[2];
+        return 2.0f * (x * y + y * z + z * x);
+    }
+};
+
+struct Node {
+    Box box;
+    int32_t left, right;  // internal: child indices; leaf: left = first, right = -count
+};
+
+struct Bvh {
+    std::vector<Tri> tris;  // reordered to leaf order
+    std::vector<Node> nodes;
+};
+
+struct Item {
+    Box box;
+    float c[3];
+    uint32_t tri;
+};
+
+int build_node(std::vector<Node>& nodes, std::vector<Item>& items, int first, int count) {
+    const int index = int(nodes.size());
+    nodes.push_back(Node());
+    Box box, cb;
+    box.reset();
+    cb.reset();
+    for (int i = first; i < first + count; ++i) {
+        box.grow(items[i].box);
+        for (int a = 0; a < 3; ++a) { cb.lo[a] = std::min(cb.lo[a], items[i].c[a]); cb.hi[a] = std::max(cb.hi[a], items[i].c[a]); }
+    }
+    nodes[index].box = box;
+    int axis = 0;
+    for (int a = 1; a < 3; ++a) if (cb.hi[a] - cb.lo[a] > cb.hi[axis] - cb.lo[axis]) axis = a;
+    if (count <= 4 || !(cb.hi[axis] > cb.lo[axis])) {
+        if (count <= 4) {
+            nodes[index].left = first;
+            nodes[index].right = -count;
+            return index;
+        }
+    }
+    int mid = first + count / 2;
+    if (cb.hi[axis] > cb.lo[axis]) {
+        constexpr int kB = 16;
+        Box bins[kB];
+        int cnt[kB] = {};
+        for (int b = 0; b < kB; ++b) bins[b].reset();
+        const float scale = kB * 0.999999f / (cb.hi[axis] - cb.lo[axis]);
+        for (int i = first; i < first + count; ++i) {
+            int b = std::min(kB - 1, std::max(0, int((items[i].c[axis] - cb.lo[axis]) * scale)));
+            bins[b].grow(items[i].box);
+            cnt[b]++;
+        }
+        float best = INFINITY;
+        int best_b = -1;
+        for (int s = 0; s < kB - 1; ++s) {
+            Box l, r;
+            l.reset(); r.reset();
+            int nl = 0, nr = 0;
+            for (int b = 0; b <= s; ++b) { l.grow(bins[b]); nl += cnt[b]; }
+            for (int b = s + 1; b < kB; ++b) { r.grow(bins[b]); nr += cnt[b]; }
+            if (!nl || !nr) continue;
+            const float c = l.area() * nl + r.area() * nr;
+            if (c < best) { best = c; best_b = s; }
+        }
+        if (best_b >= 0) {
+            auto it = std::partition(items.begin() + first, items.begin() + first + count, [&](const Item& it2) {
+                int b = std::min(kB - 1, std::max(0, int((it2.c[axis] - cb.lo[axis]) * scale)));
+                return b <= best_b;
+            });
+            mid = int(it - items.begin());
+        }
+        if (mid == first || mid == first + count) {
+            mid = first + count / 2;
+            std::nth_element(items.begin() + first, items.begin() + mid, items.begin() + first + count,
+                             [axis](const Item& a, const Item& b) { return a.c[axis] < b.c[axis]; });
+        }
+    }
+    const int l = build_node(nodes, items, first, mid - first);
+    const int r = build_node(nodes, items, mid, first + count - mid);
+    nodes[index].left = l;
+    nodes[index].right = r;
+    return index;
+}
+
+// Slab test in double on boxes padded by 2^-20 of their magnitude; a zero direction component constrains
+// nothing when the origin lies inside the slab and rejects the box otherwise.
+inline bool box_hit(const Box& b, const float* o, const float* dir, float tnear, float tfar, float& tmin) {
+    double t0 = tnear, t1 = tfar;
+    for (int a = 0; a < 3; ++a) {
+        const double pad = std::ldexp(std::max(std::fabs(double(b.lo[a])), std::fabs(double(b.hi[a]))), -20) + 1e-30;
+        const double lo = double(b.lo[a]) - pad, hi = double(b.hi[a]) + pad;
+        if (dir[a] == 0.0f) {
+            if (o[a] < lo || o[a] > hi) return false;
+            continue;
+        }
+        double n = (lo - o[a]) / double(dir[a]);
+        double f = (hi - o[a]) / double(dir[a]);
+        if (n > f) std::swap(n, f);
+        t0 = std::max(t0, n);
+        t1 = std::min(t1, f);
+    }
+    tmin = float(t0);
+    return t0 <= t1;
+}
+
+template <bool kAny>
+bool trace(const Bvh& bvh, const Ray& r, Best& best) {
+    const Setup s = setup(r.dir);
+    const float* inv = r.dir;
+    const float margin = 1.0f / 262144.0f;
+    float tfar = r.tfar;
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const Node& n = bvh.nodes[stack[--sp]];
+        float tmin;
+        if (!box_hit(n.box, r.org, inv, r.tnear - std::fabs(r.tnear) * margin, tfar + std::fabs(tfar) * margin, tmin))
+            continue;
+        if (n.right <= 0) {
+            for (int i = n.left; i < n.left - n.right; ++i) {
+                if (kAny) {
+                    float t, u, v;
+                    if (intersect(s, r.org, bvh.tris[i], r.tnear, r.tfar, t, u, v)) return true;
+                } else {
+                    offer(s, r, bvh.tris[i], i, tfar, best);
+                }
+            }
+            continue;
+        }
+        const Node& l = bvh.nodes[n.left];
+        const Node& rr = bvh.nodes[n.right];
+        float tl, tr;
+        const bool hl = box_hit(l.box, r.org, inv, r.tnear - std::fabs(r.tnear) * margin, tfar + std::fabs(tfar) * margin, tl);
+        const bool hr = box_hit(rr.box, r.org, inv, r.tnear - std::fabs(r.tnear) * margin, tfar + std::fabs(tfar) * margin, tr);
+        if (hl && hr) {
+            if (tl <= tr) { stack[sp++] = n.right; stack[sp++] = n.left; }
+            else { stack[sp++] = n.left; stack[sp++] = n.right; }
+        } else if (hl) {
+            stack[sp++] = n.left;
+        } else if (hr) {
+            stack[sp++] = n.right;
+        }
+        if (sp > 120) break;  // cannot happen for trees built above (depth < 64)
+    }
+    return best.tri >= 0;
+}
+
+std::vector<Tri> make_tris(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n) {
+    std::vector<Tri> tris(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        std::memcpy(tris[size_t(i)].v, verts + 9 * i, 36);
+        tris[size_t(i)].prim = prim[i];
+        tris[size_t(i)].geom = geom[i];
+    }
+    return tris;
+}
+
+template <typename F>
+void parallel_for(int64_t n, int threads, F f) {
+    if (threads <= 1 || n < 256) {
+        for (int64_t i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (;;) {
+                const int64_t start = next.fetch_add(64);
+                if (start >= n) break;
+                const int64_t end = std::min(n, start + 64);
+                for (int64_t i = start; i < end; ++i) f(i);
+            }
+        });
+    for (auto& th : pool) th.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+// verts: n x 9 floats (v0, v1, v2); prim/geom: n ids.  Brute force over every triangle.
+void oracle_intersect_bruteforce(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n,
+                                 void* rayhits, int64_t m, int threads) {
+    const std::vector<Tri> tris = make_tris(verts, prim, geom, n);
+    RayHit* rh = static_cast<RayHit*>(rayhits);
+    parallel_for(m, threads, [&](int64_t i) {
+        RayHit& q = rh[i];
+        const Setup s = setup(q.ray.dir);
+        float tfar = q.ray.tfar;
+        Best best;
+        for (int64_t k = 0; k < n; ++k) offer(s, q.ray, tris[size_t(k)], k, tfar, best);
+        if (best.tri >= 0) write_hit(q, tris[size_t(best.tri)], best);
+    });
+}
+
+void oracle_occluded_bruteforce(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n, void* rays,
+                                int64_t m, int threads) {
+    const std::vector<Tri> tris = make_tris(verts, prim, geom, n);
+    Ray* rs = static_cast<Ray*>(rays);
+    parallel_for(m, threads, [&](int64_t i) {
+        Ray& r = rs[i];
+        const Setup s = setup(r.dir);
+        for (int64_t k = 0; k < n; ++k) {
+            float t, u, v;
+            if (intersect(s, r.org, tris[size_t(k)], r.tnear, r.tfar, t, u, v)) {
+                r.tfar = -INFINITY;
+                return;
+            }
+        }
+    });
+}
+
+void* oracle_bvh_build(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n) {
+    Bvh* bvh = new Bvh();
+    std::vector<Tri> tris = make_tris(verts, prim, geom, n);
+    std::vector<Item> items(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) {
+        Item& it = items[size_t(i)];
+        it.box.reset();
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                it.box.lo[a] = std::min(it.box.lo[a], tris[size_t(i)].v[k][a]);
+                it.box.hi[a] = std::max(it.box.hi[a], tris[size_t(i)].v[k][a]);
+            }
+        for (int a = 0; a < 3; ++a) it.c[a] = 0.5f * (it.box.lo[a] + it.box.hi[a]);
+        it.tri = uint32_t(i);
+    }
+    bvh->nodes.reserve(size_t(2 * n));
+    build_node(bvh->nodes, items, 0, int(n));
+    bvh->tris.resize(size_t(n));
+    for (int64_t i = 0; i < n; ++i) bvh->tris[size_t(i)] = tris[items[size_t(i)].tri];
+    return bvh;
+}
+
+void oracle_bvh_free(void* h) { delete static_cast<Bvh*>(h); }
+
+void oracle_intersect_bvh(void* h, void* rayhits, int64_t m, int threads) {
+    const Bvh& bvh = *static_cast<Bvh*>(h);
+    RayHit* rh = static_cast<RayHit*>(rayhits);
+    parallel_for(m, threads, [&](int64_t i) {
+        Best best;
+        if (trace<false>(bvh, rh[i].ray, best)) write_hit(rh[i], bvh.tris[size_t(best.tri)], best);
+    });
+}
+
+void oracle_occluded_bvh(void* h, void* rays, int64_t m, int threads) {
+    const Bvh& bvh = *static_cast<Bvh*>(h);
+    Ray* rs = static_cast<Ray*>(rays);
+    parallel_for(m, threads, [&](int64_t i) {
+        Best best;
+        if (trace<true>(bvh, rs[i], best)) rs[i].tfar = -INFINITY;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+"""selas_gb300: GB300-native (sm_103a) render hot path of Selas behind a C ABI.
+
+This module is a thin ctypes view of libselas_gb300.so (declared in include/selas.h).  All work happens
+in the CUDA library; there is no Python or CPU fallback: importing the bindings without the built
+library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libselas_gb300.so"
+
+SEL_OK = 0
+SEL_ERR_INVALID_ARGUMENT = 1
+SEL_ERR_OUT_OF_MEMORY = 2
+SEL_ERR_CUDA = 3
+SEL_ERR_INVALID_OPERATION = 4
+SEL_ERR_DEVICE_LIMIT = 5
+
+SEL_BVH_WIDE8_Q8 = 0
+SEL_BVH_BINARY_FP32 = 1
+
+INVALID_ID = 0xFFFFFFFF
+
+# Embree 3.2 RTCRay / RTCRayHit layouts (rtcore_ray.h:26-63)
+RAY_DTYPE = np.dtype({
+    "names": ["org_x", "org_y", "org_z", "tnear", "dir_x", "dir_y", "dir_z", "time", "tfar", "mask", "id", "flags"],
+    "formats": ["<f4"] * 9 + ["<u4"] * 3,
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44],
+    "itemsize": 48,
+})
+RAYHIT_DTYPE = np.dtype({
+    "names": ["org_x", "org_y", "org_z", "tnear", "dir_x", "dir_y", "dir_z", "time", "tfar", "mask", "id", "flags",
+              "Ng_x", "Ng_y", "Ng_z", "u", "v", "primID", "geomID", "instID0", "instID1"],
+    "formats": ["<f4"] * 9 + ["<u4"] * 3 + ["<f4"] * 5 + ["<u4"] * 4,
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 36, 40, 44, 48, 52, 56, 60, 64, 68, 72, 76, 80],
+    "itemsize": 96,
+})
+
+
+class SelError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"selas error {code}: {msg}")
+        self.code = code
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("triangle_count", ctypes.c_uint64), ("node_count", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_uint64), ("bvh_kind", ctypes.c_uint32), ("max_depth", ctypes.c_uint32),
+                ("build_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
+                ("bounds_lo", ctypes.c_float * 3), ("bounds_hi", ctypes.c_float * 3)]
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_u = ctypes.c_uint
+_sz = ctypes.c_size_t
+
+# name -> argtypes; every function returns int except sel_get_last_error
+_SIGNATURES = {
+    "sel_device_new": [_i, ctypes.POINTER(_vp)],
+    "sel_device_release": [_vp],
+    "sel_device_sync": [_vp, _vp],
+    "sel_scene_new": [_vp, ctypes.POINTER(_vp)],
+    "sel_scene_set_bvh_kind": [_vp, _i],
+    "sel_scene_attach_triangle_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
+    "sel_scene_commit": [_vp],
+    "sel_scene_get_info": [_vp, ctypes.POINTER(SceneInfo)],
+    "sel_scene_release": [_vp],
+    "sel_intersect1": [_vp, _vp],
+    "sel_occluded1": [_vp, _vp],
+    "sel_intersect1M": [_vp, _vp, _u, _sz],
+    "sel_occluded1M": [_vp, _vp, _u, _sz],
+    "sel_intersect_device": [_vp, _vp, _u, _vp],
+    "sel_occluded_device": [_vp, _vp, _u, _vp],
+}
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libselas_gb300.so; raises when it has not been built (run __graft_entry__.build())."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        handle = ctypes.CDLL(str(LIB_PATH))
+        handle.sel_get_last_error.restype = ctypes.c_char_p
+        handle.sel_get_last_error.argtypes = []
+        for name, args in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        _lib = handle
+    return _lib
+
+
+def register_signatures(table: dict) -> None:
+    """Lets sibling modules add entry points of the same library."""
+    _SIGNATURES.update(table)
+    if _lib is not None:
+        for name, args in table.items():
+            fn = getattr(_lib, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+
+
+def check(rc: int) -> None:
+    if rc != SEL_OK:
+        raise SelError(rc, lib().sel_get_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Device:
+    """Owns one CUDA device context view (sel_device_new / sel_device_release)."""
+
+    def __init__(self, cuda_device: int = 0):
+        h = _vp()
+        check(lib().sel_device_new(cuda_device, ctypes.byref(h)))
+        self.handle = h
+
+    def sync(self, stream: int | None = None) -> None:
+        check(lib().sel_device_sync(self.handle, stream))
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().sel_device_release(self.handle))
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.release()
+
+
+class Scene:
+    """Triangle scene behind the rtcIntersect1 / rtcOccluded1 contract."""
+
+    def __init__(self, device: Device, bvh_kind: int = SEL_BVH_WIDE8_Q8):
+        h = _vp()
+        check(lib().sel_scene_new(device.handle, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+        check(lib().sel_scene_set_bvh_kind(h, bvh_kind))
+
+    def attach_triangle_mesh(self, geom_id: int, vertices: np.ndarray, indices: np.ndarray) -> None:
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
+        check(lib().sel_scene_attach_triangle_mesh(self.handle, geom_id, _ptr(v), v.shape[0], 12, _ptr(idx),
+                                                   idx.shape[0]))
+
+    def commit(self) -> None:
+        check(lib().sel_scene_commit(self.handle))
+
+    def info(self) -> SceneInfo:
+        out = SceneInfo()
+        check(lib().sel_scene_get_info(self.handle, ctypes.byref(out)))
+        return out
+
+    def intersect1M(self, rayhits: np.ndarray) -> None:
+        assert rayhits.dtype == RAYHIT_DTYPE and rayhits.flags.c_contiguous
+        check(lib().sel_intersect1M(self.handle, _ptr(rayhits), rayhits.shape[0], 96))
+
+    def occluded1M(self, rays: np.ndarray) -> None:
+        assert rays.dtype == RAY_DTYPE and rays.flags.c_contiguous
+        check(lib().sel_occluded1M(self.handle, _ptr(rays), rays.shape[0], 48))
+
+    def intersect_device(self, d_ptr: int, n: int, stream: int | None = None) -> None:
+        check(lib().sel_intersect_device(self.handle, d_ptr, n, stream))
+
+    def occluded_device(self, d_ptr: int, n: int, stream: int | None = None) -> None:
+        check(lib().sel_occluded_device(self.handle, d_ptr, n, stream))
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().sel_scene_release(self.handle))
+            self.handle = None
+
+
+def make_rayhits(org: np.ndarray, dirs: np.ndarray, tnear=0.0, tfar=np.inf) -> np.ndarray:
+    """Fills RTCRayHit records the way RayPick does (PathTracer.cpp:100-116): ids invalid, mask/flags 0."""
+    n = org.shape[0]
+    r = np.zeros(n, dtype=RAYHIT_DTYPE)
+    r["org_x"], r["org_y"], r["org_z"] = org[:, 0], org[:, 1], org[:, 2]
+    r["dir_x"], r["dir_y"], r["dir_z"] = dirs[:, 0], dirs[:, 1], dirs[:, 2]
+    r["tnear"] = tnear
+    r["tfar"] = tfar
+    r["mask"] = 0xFFFFFFFF
+    for f in ("primID", "geomID", "instID0", "instID1"):
+        r[f] = INVALID_ID
+    return r
+
+
+def make_rays(org: np.ndarray, dirs: np.ndarray, tnear=0.0, tfar=np.inf) -> np.ndarray:
+    n = org.shape[0]
+    r = np.zeros(n, dtype=RAY_DTYPE)
+    r["org_x"], r["org_y"], r["org_z"] = org[:, 0], org[:, 1], org[:, 2]
+    r["dir_x"], r["dir_y"], r["dir_z"] = dirs[:, 0], dirs[:, 1], dirs[:, 2]
+    r["tnear"] = tnear
+    r["tfar"] = tfar
+    r["mask"] = 0xFFFFFFFF
+    return r

@@ -1,0 +1,324 @@
+// C ABI: device and scene lifetime plus the ray-query entry points declared in include/selas.h.
+// Status codes instead of exceptions; the message of the last failure is kept per host thread.
+#include <chrono>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "capi_internal.h"
+#include "query.h"
+
+using sel::BuiltBvh;
+using sel::DeviceBvh;
+using sel::MeshInput;
+
+namespace sel {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(SEL_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int set_device(SelDeviceTy* dev) {
+    cudaError_t e = cudaSetDevice(dev->cuda_device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return SEL_OK;
+}
+
+int ensure_scratch(SelSceneTy* sc, size_t bytes) {
+    if (sc->scratch_bytes >= bytes) return SEL_OK;
+    if (sc->scratch) cudaFree(sc->scratch);
+    sc->scratch = nullptr;
+    sc->scratch_bytes = 0;
+    cudaError_t e = cudaMalloc(&sc->scratch, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(query staging)");
+    sc->scratch_bytes = bytes;
+    return SEL_OK;
+}
+
+int read_error_word(SelDeviceTy* dev, cudaStream_t s) {
+    uint32_t word = 0;
+    cudaError_t e = cudaMemcpyAsync(&word, dev->d_err, sizeof(word), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "reading device error word");
+    if (word) {
+        cudaMemsetAsync(dev->d_err, 0, sizeof(uint32_t), s);
+        cudaStreamSynchronize(s);
+        return fail(SEL_ERR_DEVICE_LIMIT, word & 2u ? "traversal stack overflow" : "kernel iteration cap reached");
+    }
+    return SEL_OK;
+}
+
+DeviceBvh device_bvh(const SelSceneTy* sc) {
+    DeviceBvh b;
+    b.kind = sc->info.bvh_kind;
+    b.nodes = sc->d_nodes;
+    b.tris = static_cast<const float4*>(sc->d_tris);
+    b.tri_count = uint32_t(sc->info.triangle_count);
+    return b;
+}
+
+}  // namespace sel
+
+using namespace sel;
+
+extern "C" {
+
+const char* sel_get_last_error(void) { return g_last_error.c_str(); }
+
+int sel_device_new(int cuda_device, SelDevice* out_device) {
+    if (!out_device) return fail(SEL_ERR_INVALID_ARGUMENT, "out_device is null");
+    *out_device = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (cuda_device < 0 || cuda_device >= count) return fail(SEL_ERR_INVALID_ARGUMENT, "no such CUDA device");
+    SelDeviceTy* dev = new (std::nothrow) SelDeviceTy();
+    if (!dev) return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    dev->cuda_device = cuda_device;
+    if (int rc = set_device(dev)) { delete dev; return rc; }
+    e = cudaStreamCreateWithFlags(&dev->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&dev->d_err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(dev->d_err, 0, sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        if (dev->stream) cudaStreamDestroy(dev->stream);
+        if (dev->d_err) cudaFree(dev->d_err);
+        delete dev;
+        return cuda_fail(e, "device setup");
+    }
+    *out_device = dev;
+    return SEL_OK;
+}
+
+int sel_device_release(SelDevice device) {
+    if (!device) return fail(SEL_ERR_INVALID_ARGUMENT, "device is null");
+    set_device(device);
+    cudaStreamSynchronize(device->stream);
+    cudaStreamDestroy(device->stream);
+    cudaFree(device->d_err);
+    delete device;
+    return SEL_OK;
+}
+
+int sel_device_sync(SelDevice device, void* stream) {
+    if (!device) return fail(SEL_ERR_INVALID_ARGUMENT, "device is null");
+    if (int rc = set_device(device)) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    std::lock_guard<std::mutex> lock(device->mu);
+    return read_error_word(device, device->stream);
+}
+
+int sel_scene_new(SelDevice device, SelScene* out_scene) {
+    if (!device || !out_scene) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    SelSceneTy* sc = new (std::nothrow) SelSceneTy();
+    if (!sc) return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    sc->dev = device;
+    *out_scene = sc;
+    return SEL_OK;
+}
+
+int sel_scene_set_bvh_kind(SelScene scene, int bvh_kind) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (bvh_kind != SEL_BVH_WIDE8_Q8 && bvh_kind != SEL_BVH_BINARY_FP32)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "unknown BVH kind");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    scene->kind = bvh_kind;
+    return SEL_OK;
+}
+
+int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const float* vertices, size_t vertex_count,
+                                   size_t vertex_stride_bytes, const unsigned int* indices, size_t triangle_count) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if ((vertex_count && !vertices) || (triangle_count && !indices))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "null buffer");
+    if (vertex_stride_bytes < 12 || vertex_stride_bytes % 4)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "vertex stride must be >= 12 and a multiple of 4");
+    if (geomID == SEL_INVALID_GEOMETRY_ID) return fail(SEL_ERR_INVALID_ARGUMENT, "invalid geomID");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    for (const MeshInput& m : scene->meshes)
+        if (m.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
+    MeshInput m;
+    m.geomID = geomID;
+    try {
+        m.vertices.resize(vertex_count * 3);
+        const char* vb = reinterpret_cast<const char*>(vertices);
+        for (size_t i = 0; i < vertex_count; ++i) std::memcpy(&m.vertices[3 * i], vb + i * vertex_stride_bytes, 12);
+        m.indices.assign(indices, indices + triangle_count * 3);
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    for (uint32_t idx : m.indices)
+        if (idx >= vertex_count) return fail(SEL_ERR_INVALID_ARGUMENT, "triangle index out of range");
+    scene->meshes.push_back(std::move(m));
+    scene->committed = false;
+    return SEL_OK;
+}
+
+int sel_scene_commit(SelScene scene) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    BuiltBvh built;
+    auto t0 = std::chrono::steady_clock::now();
+    std::string err;
+    try {
+        err = build_bvh(scene->meshes, scene->kind, built);
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed during BVH build");
+    }
+    if (!err.empty()) return fail(SEL_ERR_INVALID_OPERATION, err);
+    auto t1 = std::chrono::steady_clock::now();
+    const void* nodes_src = scene->kind == SEL_BVH_WIDE8_Q8 ? static_cast<const void*>(built.wide.data())
+                                                            : static_cast<const void*>(built.binary.data());
+    const size_t node_count = scene->kind == SEL_BVH_WIDE8_Q8 ? built.wide.size() : built.binary.size();
+    const size_t node_bytes = node_count * (scene->kind == SEL_BVH_WIDE8_Q8 ? sizeof(WideNode) : sizeof(BinaryNode));
+    const size_t tri_bytes = built.tris.size() * sizeof(TriRecord);
+    if (scene->d_nodes) cudaFree(scene->d_nodes);
+    if (scene->d_tris) cudaFree(scene->d_tris);
+    scene->d_nodes = scene->d_tris = nullptr;
+    cudaError_t e = cudaMalloc(&scene->d_nodes, node_bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&scene->d_tris, tri_bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scene)");
+    e = cudaMemcpy(scene->d_nodes, nodes_src, node_bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(scene->d_tris, built.tris.data(), tri_bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(scene)");
+    auto t2 = std::chrono::steady_clock::now();
+    SelSceneInfo& info = scene->info;
+    std::memset(&info, 0, sizeof(info));
+    info.triangle_count = built.tris.size();
+    info.node_count = node_count;
+    info.device_bytes = node_bytes + tri_bytes;
+    info.bvh_kind = uint32_t(scene->kind);
+    info.max_depth = built.max_depth;
+    info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    info.upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    for (int a = 0; a < 3; ++a) { info.bounds_lo[a] = built.lo[a]; info.bounds_hi[a] = built.hi[a]; }
+    scene->committed = true;
+    return SEL_OK;
+}
+
+int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info) {
+    if (!scene || !out_info) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    *out_info = scene->info;
+    return SEL_OK;
+}
+
+int sel_scene_release(SelScene scene) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    set_device(scene->dev);
+    cudaStreamSynchronize(scene->dev->stream);
+    if (scene->d_nodes) cudaFree(scene->d_nodes);
+    if (scene->d_tris) cudaFree(scene->d_tris);
+    if (scene->scratch) cudaFree(scene->scratch);
+    delete scene;
+    return SEL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------
+// Queries
+// ---------------------------------------------------------------------------------------------------
+static int check_query(SelScene scene) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    return SEL_OK;
+}
+
+template <typename Rec, bool kHit>
+static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_stride) {
+    if (int rc = check_query(scene)) return rc;
+    if (M == 0) return SEL_OK;
+    if (!recs) return fail(SEL_ERR_INVALID_ARGUMENT, "ray buffer is null");
+    if (byte_stride < sizeof(Rec)) return fail(SEL_ERR_INVALID_ARGUMENT, "byte_stride smaller than the record");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    SelDeviceTy* dev = scene->dev;
+    std::lock_guard<std::mutex> dlock(dev->mu);
+    const size_t bytes = size_t(M) * sizeof(Rec);
+    if (int rc = ensure_scratch(scene, bytes)) return rc;
+    cudaStream_t s = dev->stream;
+    cudaError_t e;
+    std::vector<Rec> packed;
+    const bool dense = byte_stride == sizeof(Rec);
+    if (dense) {
+        e = cudaMemcpyAsync(scene->scratch, recs, bytes, cudaMemcpyHostToDevice, s);
+    } else {
+        packed.resize(M);
+        const char* src = reinterpret_cast<const char*>(recs);
+        for (unsigned i = 0; i < M; ++i) std::memcpy(&packed[i], src + size_t(i) * byte_stride, sizeof(Rec));
+        e = cudaMemcpyAsync(scene->scratch, packed.data(), bytes, cudaMemcpyHostToDevice, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(rays to device)");
+    if (kHit)
+        e = launch_intersect(device_bvh(scene), static_cast<SelRayHit*>(scene->scratch), M, dev->d_err, s);
+    else
+        e = launch_occluded(device_bvh(scene), static_cast<SelRay*>(scene->scratch), M, dev->d_err, s);
+    if (e != cudaSuccess) return cuda_fail(e, "query launch");
+    if (dense) {
+        e = cudaMemcpyAsync(recs, scene->scratch, bytes, cudaMemcpyDeviceToHost, s);
+    } else {
+        e = cudaMemcpyAsync(packed.data(), scene->scratch, bytes, cudaMemcpyDeviceToHost, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(rays to host)");
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "query");
+    if (!dense) {
+        char* dst = reinterpret_cast<char*>(recs);
+        for (unsigned i = 0; i < M; ++i) std::memcpy(dst + size_t(i) * byte_stride, &packed[i], sizeof(Rec));
+    }
+    return read_error_word(dev, s);
+}
+
+extern "C" {
+
+int sel_intersect1(SelScene scene, SelRayHit* rayhit) {
+    return host_query<SelRayHit, true>(scene, rayhit, 1, sizeof(SelRayHit));
+}
+
+int sel_occluded1(SelScene scene, SelRay* ray) { return host_query<SelRay, false>(scene, ray, 1, sizeof(SelRay)); }
+
+int sel_intersect1M(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride) {
+    return host_query<SelRayHit, true>(scene, rayhits, M, byte_stride);
+}
+
+int sel_occluded1M(SelScene scene, SelRay* rays, unsigned int M, size_t byte_stride) {
+    return host_query<SelRay, false>(scene, rays, M, byte_stride);
+}
+
+int sel_intersect_device(SelScene scene, SelRayHit* d_rayhits, unsigned int n, void* stream) {
+    if (int rc = check_query(scene)) return rc;
+    if (n == 0) return SEL_OK;
+    if (!d_rayhits || (reinterpret_cast<uintptr_t>(d_rayhits) & 15u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_rayhits must be a 16-byte aligned device pointer");
+    if (int rc = set_device(scene->dev)) return rc;
+    cudaError_t e = launch_intersect(device_bvh(scene), d_rayhits, n, scene->dev->d_err, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "intersect launch");
+    return SEL_OK;
+}
+
+int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* stream) {
+    if (int rc = check_query(scene)) return rc;
+    if (n == 0) return SEL_OK;
+    if (!d_rays || (reinterpret_cast<uintptr_t>(d_rays) & 15u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_rays must be a 16-byte aligned device pointer");
+    if (int rc = set_device(scene->dev)) return rc;
+    cudaError_t e = launch_occluded(device_bvh(scene), d_rays, n, scene->dev->d_err, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "occluded launch");
+    return SEL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,21 @@
+// Launchers for the ray-query kernels (query.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sel_internal.h"
+
+namespace sel {
+
+// A committed acceleration structure resident in HBM.
+struct DeviceBvh {
+    int kind = SEL_BVH_WIDE8_Q8;
+    const void* nodes = nullptr;   // WideNode[] or BinaryNode[]
+    const float4* tris = nullptr;  // TriRecord[] as 3 x float4
+    uint32_t tri_count = 0;
+};
+
+cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);
+cudaError_t launch_occluded(const DeviceBvh& bvh, SelRay* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);
+
+}  // namespace sel

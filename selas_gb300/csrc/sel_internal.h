@@ -1,0 +1,83 @@
+// Internal declarations shared by the host-side builder (bvh_build.cpp) and the CUDA translation units.
+// Nothing here crosses the C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/selas.h"
+
+namespace sel {
+
+// ---------------------------------------------------------------------------------------------------
+// Acceleration-structure layouts in HBM
+// ---------------------------------------------------------------------------------------------------
+
+// Triangle record, 48 bytes = 3 x float4, in the leaf order of the BVH that references it.
+//   v0.xyz, w = primID (bits)      v1.xyz, w = geomID (bits)      v2.xyz, w = 0
+struct TriRecord {
+    float v0[3]; uint32_t prim;
+    float v1[3]; uint32_t geom;
+    float v2[3]; uint32_t pad;
+};
+static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
+
+// 8-wide node with child boxes quantised to 8 bits per axis (80 bytes = 5 x uint4).
+//   origin p (float3), per-axis exponent byte e (scale = 2^(e-127)), internal-child mask imask,
+//   child_base (index of the first internal child; internal children are contiguous in slot order),
+//   tri_base (index of the first triangle; leaf children are contiguous),
+//   meta[8]: leaf slot -> (count << 5) | offset, count in 1..3, offset in 0..23; 0 for internal/empty,
+//   qlo/qhi[axis][8]: child box = p + scale * q, rounded outward when built.
+struct WideNode {
+    float p[3];
+    uint8_t e[3];
+    uint8_t imask;
+    uint32_t child_base;
+    uint32_t tri_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8];
+    uint8_t qhi[3][8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
+
+// Binary node with FP32 child boxes (64 bytes = 4 x float4):
+//   [c0.lo.x c0.hi.x c0.lo.y c0.hi.y] [c1.lo.x c1.hi.x c1.lo.y c1.hi.y] [c0.lo.z c0.hi.z c1.lo.z c1.hi.z]
+//   [ref0 ref1 count0 count1]: ref >= 0 and count == 0 -> internal node index; count > 0 -> leaf of
+//   `count` triangles starting at triangle index ref.
+struct BinaryNode {
+    float c0x[2], c0y[2];
+    float c1x[2], c1y[2];
+    float c0z[2], c1z[2];
+    int32_t ref[2];
+    int32_t count[2];
+};
+static_assert(sizeof(BinaryNode) == 64, "BinaryNode must be 64 bytes");
+
+// ---------------------------------------------------------------------------------------------------
+// Host-side build
+// ---------------------------------------------------------------------------------------------------
+struct MeshInput {
+    uint32_t geomID;
+    std::vector<float> vertices;   // xyz packed
+    std::vector<uint32_t> indices; // 3 per triangle
+};
+
+struct BuiltBvh {
+    int kind = SEL_BVH_WIDE8_Q8;
+    std::vector<WideNode> wide;
+    std::vector<BinaryNode> binary;
+    std::vector<TriRecord> tris;
+    uint32_t max_depth = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// Returns an empty string on success or an error message.
+std::string build_bvh(const std::vector<MeshInput>& meshes, int kind, BuiltBvh& out);
+
+// Traversal stack capacities (entries per thread); the builder rejects trees deeper than these.
+constexpr int kWideStack = 32;
+constexpr int kBinaryStack = 64;
+
+}  // namespace sel

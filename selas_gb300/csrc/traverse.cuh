@@ -1,0 +1,312 @@
+// Device-side ray queries: watertight ray/triangle test and traversal of the two BVH layouts.
+//
+// The query contract is the one Embree gives rtcIntersect1 / rtcOccluded1
+// (Middleware/embree-latest/include/embree3/rtcore_scene.h:94,118; used by
+// Source/Applications/Selas/Source/PathTracer.cpp:71-139).  Intersection follows Woop, Benthin and
+// Wald, "Watertight Ray/Triangle Intersection", JCGT 2(1) 2013, with every rounding step written out
+// (fmaf / __fmul_rn / __fadd_rn) so that the CPU oracle, written independently with the same rounding
+// steps, reproduces t, u, v bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sel_internal.h"
+
+namespace sel {
+
+constexpr uint32_t kIterationCap = 1u << 22;  // node visits + triangle tests per ray before giving up
+constexpr uint32_t kErrIterationCap = 1u;
+constexpr uint32_t kErrStackOverflow = 2u;
+constexpr float kBoxMargin = 1.0f / 1048576.0f;  // relative widening of the ray interval for box tests
+
+__device__ __forceinline__ float pick3(int k, float x, float y, float z) { return k == 0 ? x : (k == 1 ? y : z); }
+
+struct Watertight {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+// kz = dominant axis of |d| (ties resolved x, then y, then z); kx, ky follow cyclically and are swapped
+// when d[kz] < 0 to keep the winding.
+__device__ __forceinline__ Watertight watertight_setup(float dx, float dy, float dz) {
+    Watertight w;
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    w.kz = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    w.kx = w.kz == 2 ? 0 : w.kz + 1;
+    w.ky = w.kx == 2 ? 0 : w.kx + 1;
+    const float dkz = pick3(w.kz, dx, dy, dz);
+    if (dkz < 0.0f) { int t = w.kx; w.kx = w.ky; w.ky = t; }
+    const float dkx = pick3(w.kx, dx, dy, dz), dky = pick3(w.ky, dx, dy, dz);
+    w.sx = __fdiv_rn(dkx, dkz);
+    w.sy = __fdiv_rn(dky, dkz);
+    w.sz = __frcp_rn(dkz);
+    return w;
+}
+
+// Returns true and t/u/v when the triangle is hit with tnear <= t <= tfar.
+__device__ __forceinline__ bool watertight_intersect(const Watertight& w, float ox, float oy, float oz, const float4& p0,
+                                                     const float4& p1, const float4& p2, float tnear, float tfar,
+                                                     float& t, float& u, float& v) {
+    const float a0 = __fsub_rn(p0.x, ox), a1 = __fsub_rn(p0.y, oy), a2 = __fsub_rn(p0.z, oz);
+    const float b0 = __fsub_rn(p1.x, ox), b1 = __fsub_rn(p1.y, oy), b2 = __fsub_rn(p1.z, oz);
+    const float c0 = __fsub_rn(p2.x, ox), c1 = __fsub_rn(p2.y, oy), c2 = __fsub_rn(p2.z, oz);
+    const float Akz = pick3(w.kz, a0, a1, a2), Bkz = pick3(w.kz, b0, b1, b2), Ckz = pick3(w.kz, c0, c1, c2);
+    const float Ax = fmaf(-w.sx, Akz, pick3(w.kx, a0, a1, a2));
+    const float Ay = fmaf(-w.sy, Akz, pick3(w.ky, a0, a1, a2));
+    const float Bx = fmaf(-w.sx, Bkz, pick3(w.kx, b0, b1, b2));
+    const float By = fmaf(-w.sy, Bkz, pick3(w.ky, b0, b1, b2));
+    const float Cx = fmaf(-w.sx, Ckz, pick3(w.kx, c0, c1, c2));
+    const float Cy = fmaf(-w.sy, Ckz, pick3(w.ky, c0, c1, c2));
+    float U = fmaf(Cx, By, -__fmul_rn(Cy, Bx));
+    float V = fmaf(Ax, Cy, -__fmul_rn(Ay, Cx));
+    float W = fmaf(Bx, Ay, -__fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        // Edge case: redo the 2D edge functions exactly (products of floats are exact in double).
+        U = (float)__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx));
+        V = (float)__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx));
+        W = (float)__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = __fadd_rn(__fadd_rn(U, V), W);
+    if (det == 0.0f) return false;
+    const float Az = __fmul_rn(w.sz, Akz), Bz = __fmul_rn(w.sz, Bkz), Cz = __fmul_rn(w.sz, Ckz);
+    const float T = fmaf(U, Az, fmaf(V, Bz, __fmul_rn(W, Cz)));
+    const float rcp = __frcp_rn(det);
+    const float tt = __fmul_rn(T, rcp);
+    if (!(tt >= tnear && tt <= tfar)) return false;
+    t = tt;
+    u = __fmul_rn(V, rcp);
+    v = __fmul_rn(W, rcp);
+    return true;
+}
+
+// Geometric normal (v1 - v0) x (v2 - v0) with explicit rounding.
+__device__ __forceinline__ float3 triangle_ng(const float4& p0, const float4& p1, const float4& p2) {
+    const float e1x = __fsub_rn(p1.x, p0.x), e1y = __fsub_rn(p1.y, p0.y), e1z = __fsub_rn(p1.z, p0.z);
+    const float e2x = __fsub_rn(p2.x, p0.x), e2y = __fsub_rn(p2.y, p0.y), e2z = __fsub_rn(p2.z, p0.z);
+    return make_float3(fmaf(e1y, e2z, -__fmul_rn(e1z, e2y)), fmaf(e1z, e2x, -__fmul_rn(e1x, e2z)),
+                       fmaf(e1x, e2y, -__fmul_rn(e1y, e2x)));
+}
+
+__device__ __forceinline__ float safe_rcp(float d) {
+    return __frcp_rn(fabsf(d) > 1e-30f ? d : copysignf(1e-30f, d));
+}
+
+struct QueryRay {
+    float ox, oy, oz, dx, dy, dz, tnear, tfar;
+};
+
+struct QueryHit {
+    float t, u, v;
+    uint32_t tri;  // index into the triangle array in leaf order (0xffffffff: no hit)
+};
+
+__device__ __forceinline__ uint64_t tri_key(const float4& p0, const float4& p1) {
+    return (uint64_t(__float_as_uint(p1.w)) << 32) | uint64_t(__float_as_uint(p0.w));
+}
+
+__device__ __forceinline__ float byte_as_float(uint32_t word, int byte) {
+    return __uint2float_rn((word >> (8 * byte)) & 0xffu);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// 8-wide quantised BVH.  Node groups on the stack are (child_base, hit bits 24..31 | imask bits 0..7);
+// hit bit 24 + (slot ^ octant) so that the lowest set bit is the nearest child for this ray octant.
+// `stack` points at this thread's first entry; entries are `stride` uint2 apart (shared memory).
+// Returns true on a hit (any-hit: as soon as one is found).
+// ---------------------------------------------------------------------------------------------------
+template <bool kAnyHit>
+__device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                           const QueryRay& r, QueryHit& hit, uint2* stack, int stride,
+                                           uint32_t& status) {
+    const Watertight wt = watertight_setup(r.dx, r.dy, r.dz);
+    const float ix = safe_rcp(r.dx), iy = safe_rcp(r.dy), iz = safe_rcp(r.dz);
+    const uint32_t oct = (ix < 0.0f ? 4u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 1u : 0u);
+    const float tnear_box = r.tnear - fabsf(r.tnear) * kBoxMargin;
+    float tfar = r.tfar;
+    float tfar_box = tfar + fabsf(tfar) * kBoxMargin;
+    uint64_t best_key = ~0ull;
+    bool found = false;
+    hit.tri = 0xffffffffu;
+
+    uint2 group = make_uint2(0u, (1u << (24 + oct)) | 1u);
+    int sp = 0;
+    uint32_t iters = 0;
+    for (;;) {
+        uint32_t tmask = 0, tbase = 0;
+        if (group.y & 0xff000000u) {
+            const int b = __ffs(group.y >> 24) - 1;
+            group.y &= ~(1u << (24 + b));
+            const uint32_t slot = uint32_t(b) ^ oct;
+            const uint32_t idx = group.x + __popc(group.y & ((1u << slot) - 1u));
+            if (group.y & 0xff000000u) {
+                if (sp >= kWideStack) { status |= kErrStackOverflow; break; }
+                stack[sp * stride] = group;
+                ++sp;
+            }
+            const uint4* np = nodes + size_t(idx) * 5;
+            const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+            const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y), pz = __uint_as_float(n0.z);
+            const float sxs = __fmul_rn(__uint_as_float((n0.w & 0xffu) << 23), ix);
+            const float sys = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xffu) << 23), iy);
+            const float szs = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xffu) << 23), iz);
+            const float oxa = __fmul_rn(__fsub_rn(px, r.ox), ix);
+            const float oya = __fmul_rn(__fsub_rn(py, r.oy), iy);
+            const float oza = __fmul_rn(__fsub_rn(pz, r.oz), iz);
+            const uint32_t imask = n0.w >> 24;
+            // near/far plane words per axis (lo when the inverse direction is positive)
+            const uint32_t nx0 = ix >= 0.0f ? n2.x : n3.z, nx1 = ix >= 0.0f ? n2.y : n3.w;
+            const uint32_t fx0 = ix >= 0.0f ? n3.z : n2.x, fx1 = ix >= 0.0f ? n3.w : n2.y;
+            const uint32_t ny0 = iy >= 0.0f ? n2.z : n4.x, ny1 = iy >= 0.0f ? n2.w : n4.y;
+            const uint32_t fy0 = iy >= 0.0f ? n4.x : n2.z, fy1 = iy >= 0.0f ? n4.y : n2.w;
+            const uint32_t nz0 = iz >= 0.0f ? n3.x : n4.z, nz1 = iz >= 0.0f ? n3.y : n4.w;
+            const uint32_t fz0 = iz >= 0.0f ? n4.z : n3.x, fz1 = iz >= 0.0f ? n4.w : n3.y;
+            uint32_t new_hits = 0;
+#pragma unroll
+            for (int s = 0; s < 8; ++s) {
+                const int byte = s & 3;
+                const uint32_t wnx = s < 4 ? nx0 : nx1, wfx = s < 4 ? fx0 : fx1;
+                const uint32_t wny = s < 4 ? ny0 : ny1, wfy = s < 4 ? fy0 : fy1;
+                const uint32_t wnz = s < 4 ? nz0 : nz1, wfz = s < 4 ? fz0 : fz1;
+                const float tnx = fmaf(byte_as_float(wnx, byte), sxs, oxa);
+                const float tfx = fmaf(byte_as_float(wfx, byte), sxs, oxa);
+                const float tny = fmaf(byte_as_float(wny, byte), sys, oya);
+                const float tfy = fmaf(byte_as_float(wfy, byte), sys, oya);
+                const float tnz = fmaf(byte_as_float(wnz, byte), szs, oza);
+                const float tfz = fmaf(byte_as_float(wfz, byte), szs, oza);
+                const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tnear_box));
+                const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_box));
+                if (tmin <= tmax) {
+                    if ((imask >> s) & 1u) {
+                        new_hits |= 1u << (s ^ oct);
+                    } else {
+                        const uint32_t meta = ((s < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
+                        const uint32_t cnt = meta >> 5;
+                        tmask |= ((1u << cnt) - 1u) << (meta & 31u);
+                    }
+                }
+            }
+            group = make_uint2(n1.x, (new_hits << 24) | imask);
+            tbase = n1.y;
+        }
+        while (tmask) {
+            if (++iters > kIterationCap) { status |= kErrIterationCap; return found; }
+            const int b = __ffs(tmask) - 1;
+            tmask &= tmask - 1u;
+            const uint32_t ti = tbase + uint32_t(b);
+            const float4* tp = tris + size_t(ti) * 3;
+            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+            float t, u, v;
+            if (watertight_intersect(wt, r.ox, r.oy, r.oz, p0, p1, p2, r.tnear, tfar, t, u, v)) {
+                if (kAnyHit) {
+                    hit.t = t; hit.u = u; hit.v = v; hit.tri = ti;
+                    return true;
+                }
+                const uint64_t key = tri_key(p0, p1);
+                if (t < tfar || key < best_key) {
+                    tfar = t;
+                    tfar_box = tfar + fabsf(tfar) * kBoxMargin;
+                    best_key = key;
+                    hit.t = t; hit.u = u; hit.v = v; hit.tri = ti;
+                    found = true;
+                }
+            }
+        }
+        if (!(group.y & 0xff000000u)) {
+            if (sp == 0) break;
+            --sp;
+            group = stack[sp * stride];
+        }
+        if (++iters > kIterationCap) { status |= kErrIterationCap; break; }
+    }
+    return found;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Binary FP32 BVH (the plain GPU path): classic stack traversal, nearer child first.
+// `stack` points at this thread's first int entry; entries are `stride` ints apart.
+// ---------------------------------------------------------------------------------------------------
+template <bool kAnyHit>
+__device__ __forceinline__ bool trace_binary(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                             const QueryRay& r, QueryHit& hit, int* stack, int stride,
+                                             uint32_t& status) {
+    const Watertight wt = watertight_setup(r.dx, r.dy, r.dz);
+    const float ix = safe_rcp(r.dx), iy = safe_rcp(r.dy), iz = safe_rcp(r.dz);
+    const float oix = __fmul_rn(r.ox, ix), oiy = __fmul_rn(r.oy, iy), oiz = __fmul_rn(r.oz, iz);
+    const float tnear_box = r.tnear - fabsf(r.tnear) * kBoxMargin;
+    float tfar = r.tfar;
+    float tfar_box = tfar + fabsf(tfar) * kBoxMargin;
+    uint64_t best_key = ~0ull;
+    bool found = false;
+    hit.tri = 0xffffffffu;
+    const bool nx = ix < 0.0f, ny = iy < 0.0f, nz = iz < 0.0f;
+
+    int node = 0;
+    int sp = 0;
+    uint32_t iters = 0;
+    for (;;) {
+        if (++iters > kIterationCap) { status |= kErrIterationCap; break; }
+        const float4* np = nodes + size_t(node) * 4;
+        const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+        const int4 refs = __ldg(reinterpret_cast<const int4*>(np + 3));
+        // child 0
+        const float t0nx = fmaf(nx ? a.y : a.x, ix, -oix), t0fx = fmaf(nx ? a.x : a.y, ix, -oix);
+        const float t0ny = fmaf(ny ? a.w : a.z, iy, -oiy), t0fy = fmaf(ny ? a.z : a.w, iy, -oiy);
+        const float t0nz = fmaf(nz ? c.y : c.x, iz, -oiz), t0fz = fmaf(nz ? c.x : c.y, iz, -oiz);
+        const float t1nx = fmaf(nx ? b.y : b.x, ix, -oix), t1fx = fmaf(nx ? b.x : b.y, ix, -oix);
+        const float t1ny = fmaf(ny ? b.w : b.z, iy, -oiy), t1fy = fmaf(ny ? b.z : b.w, iy, -oiy);
+        const float t1nz = fmaf(nz ? c.w : c.z, iz, -oiz), t1fz = fmaf(nz ? c.z : c.w, iz, -oiz);
+        const float tmin0 = fmaxf(fmaxf(t0nx, t0ny), fmaxf(t0nz, tnear_box));
+        const float tmax0 = fminf(fminf(t0fx, t0fy), fminf(t0fz, tfar_box));
+        const float tmin1 = fmaxf(fmaxf(t1nx, t1ny), fmaxf(t1nz, tnear_box));
+        const float tmax1 = fminf(fminf(t1fx, t1fy), fminf(t1fz, tfar_box));
+        bool h0 = tmin0 <= tmax0 && refs.z >= 0;
+        bool h1 = tmin1 <= tmax1 && refs.w >= 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const bool hk = k == 0 ? h0 : h1;
+            const int cnt = k == 0 ? refs.z : refs.w;
+            if (!hk || cnt <= 0) continue;
+            const int first = k == 0 ? refs.x : refs.y;
+            for (int i = 0; i < cnt; ++i) {
+                const float4* tp = tris + size_t(first + i) * 3;
+                const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                float t, u, v;
+                if (watertight_intersect(wt, r.ox, r.oy, r.oz, p0, p1, p2, r.tnear, tfar, t, u, v)) {
+                    if (kAnyHit) {
+                        hit.t = t; hit.u = u; hit.v = v; hit.tri = uint32_t(first + i);
+                        return true;
+                    }
+                    const uint64_t key = tri_key(p0, p1);
+                    if (t < tfar || key < best_key) {
+                        tfar = t;
+                        tfar_box = tfar + fabsf(tfar) * kBoxMargin;
+                        best_key = key;
+                        hit.t = t; hit.u = u; hit.v = v; hit.tri = uint32_t(first + i);
+                        found = true;
+                    }
+                }
+            }
+            if (k == 0) h0 = false; else h1 = false;
+        }
+        if (h0 && h1) {
+            const bool first0 = tmin0 <= tmin1;
+            if (sp >= kBinaryStack) { status |= kErrStackOverflow; break; }
+            stack[sp * stride] = first0 ? refs.y : refs.x;
+            ++sp;
+            node = first0 ? refs.x : refs.y;
+        } else if (h0) {
+            node = refs.x;
+        } else if (h1) {
+            node = refs.y;
+        } else {
+            if (sp == 0) break;
+            --sp;
+            node = stack[sp * stride];
+        }
+    }
+    return found;
+}
+
+}  // namespace sel

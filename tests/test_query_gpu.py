@@ -1,0 +1,155 @@
+"""GPU parity of the ray queries (C ABI -> sm_103a kernels) against the CPU oracle.
+
+Closest-hit records (t, u, v, Ng, primID, geomID, instID) and any-hit bits must be bit-exact: both sides
+implement the same watertight test with the same rounding steps and the same order-independent tie rule.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import selas_gb300 as sel
+from conftest import HIT_FIELDS, assert_hits_equal
+from edge_scenes import grid_rays, grid_scene, segment_rayhits, segment_rays
+from selas_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+KINDS = [sel.SEL_BVH_WIDE8_Q8, sel.SEL_BVH_BINARY_FP32]
+
+
+def _scene(device, data, kind):
+    sc = sel.Scene(device, kind)
+    data.attach_to(sc)
+    sc.commit()
+    return sc
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_small_scene_matches_bruteforce(device, kind):
+    data = scenes.displaced_icospheres(count=5, level=3, seed=11)
+    soup = data.soup()
+    sc = _scene(device, data, kind)
+    cam = scenes.camera_basis([0.0, 70.0, -170.0], [0.0, 40.0, 0.0], [0.0, 1.0, 0.0], 60.0, 96, 96)
+    for org, d in (scenes.primary_rays(cam), scenes.surface_rays(data, 8000, seed=5)):
+        got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+        sc.intersect1M(got)
+        oracle.intersect_bruteforce(soup, want)
+        assert (want["geomID"] != sel.INVALID_ID).sum() > 500
+        assert_hits_equal(got, want)
+        rg, rw = sel.make_rays(org, d), sel.make_rays(org, d)
+        sc.occluded1M(rg)
+        oracle.occluded_bruteforce(soup, rw)
+        assert_hits_equal(rg, rw, fields=("tfar",))
+    sc.release()
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_edge_cases_match_bruteforce(device, kind):
+    data = grid_scene()
+    soup = data.soup()
+    sc = _scene(device, data, kind)
+    org, d, _ = grid_rays()
+    got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+    sc.intersect1M(got)
+    oracle.intersect_bruteforce(soup, want)
+    assert_hits_equal(got, want)
+    for make, query, ref in ((segment_rayhits, sc.intersect1M, oracle.intersect_bruteforce),
+                             (segment_rays, sc.occluded1M, oracle.occluded_bruteforce)):
+        g, w = make(), make()
+        query(g)
+        ref(soup, w)
+        assert_hits_equal(g, w, fields=HIT_FIELDS if g.dtype == sel.RAYHIT_DTYPE else ("tfar",))
+    # empty batches are no-ops
+    sc.intersect1M(sel.make_rayhits(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32)))
+    sc.release()
+
+
+def test_single_ray_and_strided_forms(device):
+    data = scenes.displaced_icospheres(count=3, level=2, seed=3)
+    soup = data.soup()
+    sc = _scene(device, data, sel.SEL_BVH_WIDE8_Q8)
+    org, d = scenes.surface_rays(data, 300, seed=9)
+    want = sel.make_rayhits(org, d)
+    oracle.intersect_bruteforce(soup, want)
+    # one record at a time (rtcIntersect1 form)
+    lib = sel.lib()
+    one = sel.make_rayhits(org[:40], d[:40])
+    for i in range(40):
+        rec = one[i:i + 1].copy()
+        sel.check(lib.sel_intersect1(sc.handle, rec.ctypes.data))
+        one[i] = rec[0]
+    assert_hits_equal(one, want[:40])
+    # strided records (128-byte stride, as a caller embedding RTCRayHit in a larger struct would pass)
+    wide = np.zeros(300, dtype=np.dtype({"names": ["rh"], "formats": [sel.RAYHIT_DTYPE], "offsets": [0],
+                                         "itemsize": 128}))
+    wide["rh"] = sel.make_rayhits(org, d)
+    sel.check(lib.sel_intersect1M(sc.handle, wide.ctypes.data, 300, 128))
+    assert_hits_equal(wide["rh"], want)
+    sc.release()
+
+
+def test_device_forms_and_errors(device):
+    torch = pytest.importorskip("torch")
+    data = scenes.displaced_icospheres(count=3, level=3, seed=4)
+    sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8)
+    data.attach_to(sc)
+    rh = sel.make_rayhits(*scenes.surface_rays(data, 1000, seed=2))
+    with pytest.raises(sel.SelError) as e:
+        sc.intersect1M(rh.copy())
+    assert e.value.code == sel.SEL_ERR_INVALID_OPERATION
+    sc.commit()
+    host = rh.copy()
+    sc.intersect1M(host)
+    buf = torch.from_numpy(rh.view(np.uint8).copy()).cuda()
+    stream = torch.cuda.Stream()
+    sc.intersect_device(buf.data_ptr(), rh.shape[0], stream.cuda_stream)
+    device.sync(stream.cuda_stream)
+    dev_res = buf.cpu().numpy().view(sel.RAYHIT_DTYPE)
+    assert_hits_equal(dev_res, host)
+    with pytest.raises(sel.SelError) as e:
+        sc.intersect_device(buf.data_ptr() + 4, 10, None)
+    assert e.value.code == sel.SEL_ERR_INVALID_ARGUMENT
+    sc.release()
+
+
+@pytest.fixture(scope="module")
+def full_workload():
+    data, (co, cd), (io, idr) = scenes.ray_query_workload(level=6)
+    return data, (co, cd), (io, idr)
+
+
+def _trace_device(sc, org, d, any_hit=False):
+    import torch
+    recs = (sel.make_rays if any_hit else sel.make_rayhits)(org, d)
+    buf = torch.from_numpy(recs.view(np.uint8)).cuda()
+    (sc.occluded_device if any_hit else sc.intersect_device)(buf.data_ptr(), recs.shape[0], None)
+    sc.device.sync(None)
+    return buf.cpu().numpy().view(recs.dtype)
+
+
+def test_full_size_workload(device, full_workload):
+    """5.24 M triangles, 4 M coherent + 4 M incoherent rays: both BVH layouts agree on every record at full
+    size, a 40 k-ray sample of each set is bit-exact against the oracle BVH, and any-hit bits equal
+    closest-hit existence."""
+    pytest.importorskip("torch")
+    data, coherent, incoherent = full_workload
+    soup = data.soup()
+    wide = _scene(device, data, sel.SEL_BVH_WIDE8_Q8)
+    binary = _scene(device, data, sel.SEL_BVH_BINARY_FP32)
+    info = wide.info()
+    assert info.triangle_count == data.triangle_count
+    obvh = oracle.OracleBvh(soup)
+    rng = np.random.default_rng(1)
+    for org, d in (coherent, incoherent):
+        a = _trace_device(wide, org, d)
+        b = _trace_device(binary, org, d)
+        assert_hits_equal(a, b)
+        hit = a["geomID"] != sel.INVALID_ID
+        assert hit.mean() > 0.05
+        occ = _trace_device(wide, org, d, any_hit=True)
+        assert np.array_equal(np.isneginf(occ["tfar"]), hit)
+        pick = rng.choice(org.shape[0], 40000, replace=False)
+        want = sel.make_rayhits(org[pick], d[pick])
+        obvh.intersect(want)
+        assert_hits_equal(a[pick], want)
+    wide.release()
+    binary.release()
