@@ -40,12 +40,12 @@ WORKLOAD = ("ray queries: 64 displaced icospheres (subdivision 6, 5,242,880 tria
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--level", type=int, default=6)
     p.add_argument("--width", type=int, default=2048)
-    p.add_argument("--cpu-sample", type=int, default=65536, help="rays per query set in each CPU sample step")
+    p.add_argument("--cpu-sample", type=int, default=2097152, help="rays per query set in each CPU sample step")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -326,9 +326,9 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, q, t = cpu_baseline_run(data.soup(), [coherent, incoherent], args.cpu_sample, 2, threads)
+        v, q, t = cpu_baseline_run(data.soup(), [coherent, incoherent], args.cpu_sample, 4, threads)
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": f"{q} queries (2 x {args.cpu_sample} rays of each set, closest+any) on {cpu_desc()}, "
+               "sample": f"{q} queries (4 x {args.cpu_sample} rays of each set, closest+any) on {cpu_desc()}, "
                          f"{t:.1f} s"}
 
     per_set = {k: round(counts[k] / (per_kernel[k] * 1e-3) / 1e6, 1) for k in per_kernel}

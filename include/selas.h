@@ -142,6 +142,42 @@ int sel_occluded1M(SelScene scene, SelRay* rays, unsigned int M, size_t byte_str
 int sel_intersect_device(SelScene scene, SelRayHit* d_rayhits, unsigned int n, void* stream);
 int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* stream);
 
+/* ------------------------------------------------------------------------------------------------ */
+/* BSDF evaluation and sampling (device memory, asynchronous on `stream`).                           */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* Shader kinds: ShaderType (Source/Core/SceneLib/ModelResource.h:27-34). */
+enum { SEL_SHADER_DISNEY_THIN = 0, SEL_SHADER_DISNEY_SOLID = 1, SEL_SHADER_DIRAC_TRANSPARENT = 2 };
+/* Event flags: SurfaceEventFlags (Source/Core/Shading/Scattering.h:12-17). */
+enum { SEL_EVENT_SCATTER = 1, SEL_EVENT_TRANSMISSION = 2, SEL_EVENT_DIRAC = 4 };
+
+/* A shading point: the fields of SurfaceParameters (Source/Core/Shading/SurfaceParameters.h:15-48) that
+ * the BSDF reads.  tangent/normal/bitangent are the world-space rows of tangentToWorld (worldToTangent is
+ * their transpose); baseColor is linear; diffTrans is the halved value CalculateSurfaceParams stores.
+ * 128 bytes. */
+typedef struct SelSurface {
+    float tangent[3], normal[3], bitangent[3];
+    float baseColor[3];
+    float transmittanceColor[3];
+    float sheen, sheenTint, clearcoat, clearcoatGloss;
+    float metallic, specTrans, diffTrans, flatness;
+    float anisotropic, relativeIOR, specularTint, roughness;
+    float scatterDistance, ior;
+    int32_t shader;
+    float pad[2];
+} SelSurface;
+
+/* EvaluateBsdf (Source/Core/Shading/SurfaceScattering.h:16): for each i, wo[i] (toward the viewer) and
+ * wi[i] (toward the light) are 3 floats; out[5*i..] = f.x f.y f.z forwardPdfW reversePdfW, where f already
+ * includes |cos(theta_i)| as in the reference. */
+int sel_bsdf_evaluate_device(const SelSurface* d_surfaces, const float* d_wo, const float* d_wi, unsigned int n,
+                             float* d_out, void* stream);
+/* SampleBsdfFunction (Source/Core/Shading/SurfaceScattering.h:15) with the sampler's uniforms given
+ * explicitly: u[4*i..4*i+3] are consumed in the order the reference draws them.  out[16*i..] = success
+ * flags reflectance[3] wi[3] forwardPdfW reversePdfW mediumPhase extinction[3] uniformsUsed 0. */
+int sel_bsdf_sample_device(const SelSurface* d_surfaces, const float* d_wo, const float* d_u, unsigned int n,
+                           float* d_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,70 +31,76 @@ __device__ __forceinline__ void store_hit(SelRayHit* rh, const float4* __restric
     reinterpret_cast<uint32_t*>(base)[20] = SEL_INVALID_GEOMETRY_ID;
 }
 
-template <int kKind>
-__global__ void __launch_bounds__(kQueryBlock) k_intersect(const void* __restrict__ nodes,
-                                                           const float4* __restrict__ tris, SelRayHit* rays,
-                                                           uint32_t n, uint32_t* err) {
-    __shared__ uint2 stack_mem[kKind == SEL_BVH_WIDE8_Q8 ? kWideStack * kQueryBlock : kBinaryStack * kQueryBlock / 2];
+// 8-wide traversal: one thread per ray over the whole batch, 8 resident 128-thread blocks per SM
+// (64 registers, 24 KB of shared-memory stacks per block).  A sweep of persistent variants that refill
+// finished lanes from per-warp ray blocks was slower on both coherent and incoherent rays (lanes lose
+// the lockstep that makes node fetches shared), so the hardware block scheduler does the balancing.
+constexpr int kWideBlocksPerSm = 8;
+
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm)
+    k_query_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris, float4* rays,
+                 uint32_t record_float4s, uint32_t n, uint32_t* err) {
+    __shared__ uint2 stack_mem[kWideStack * kQueryBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const QueryRay r = load_ray(reinterpret_cast<const float4*>(rays + i));
     QueryHit h;
     uint32_t status = 0;
-    bool found;
-    if (kKind == SEL_BVH_WIDE8_Q8) {
-        found = trace_wide<false>(static_cast<const uint4*>(nodes), tris, r, h, stack_mem + threadIdx.x, kQueryBlock,
-                                  status);
-    } else {
-        found = trace_binary<false>(static_cast<const float4*>(nodes), tris, r, h,
-                                    reinterpret_cast<int*>(stack_mem) + threadIdx.x, kQueryBlock, status);
-    }
+    const bool found = trace_wide<kAnyHit>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
+                                           stack_mem + threadIdx.x, kQueryBlock, status);
     if (status) atomicOr(err, status);
-    if (found) store_hit(rays + i, tris, h);
+    if (found) {
+        if (kAnyHit)
+            reinterpret_cast<float*>(rays + size_t(i) * record_float4s)[8] = -__int_as_float(0x7f800000);
+        else
+            store_hit(reinterpret_cast<SelRayHit*>(rays + size_t(i) * record_float4s), tris, h);
+    }
 }
 
-template <int kKind>
-__global__ void __launch_bounds__(kQueryBlock) k_occluded(const void* __restrict__ nodes,
-                                                          const float4* __restrict__ tris, SelRay* rays, uint32_t n,
-                                                          uint32_t* err) {
-    __shared__ uint2 stack_mem[kKind == SEL_BVH_WIDE8_Q8 ? kWideStack * kQueryBlock : kBinaryStack * kQueryBlock / 2];
+// Plain binary FP32 path: one thread per ray, launched over the whole batch.
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kQueryBlock) k_query_binary(const float4* __restrict__ nodes,
+                                                              const float4* __restrict__ tris, float4* rays,
+                                                              uint32_t record_float4s, uint32_t n, uint32_t* err) {
+    __shared__ int stack_mem[kBinaryStack * kQueryBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const QueryRay r = load_ray(reinterpret_cast<const float4*>(rays + i));
+    const QueryRay r = load_ray(rays + size_t(i) * record_float4s);
     QueryHit h;
     uint32_t status = 0;
-    bool found;
-    if (kKind == SEL_BVH_WIDE8_Q8) {
-        found = trace_wide<true>(static_cast<const uint4*>(nodes), tris, r, h, stack_mem + threadIdx.x, kQueryBlock,
-                                 status);
-    } else {
-        found = trace_binary<true>(static_cast<const float4*>(nodes), tris, r, h,
-                                   reinterpret_cast<int*>(stack_mem) + threadIdx.x, kQueryBlock, status);
-    }
+    const bool found = trace_binary<kAnyHit>(nodes, tris, r, h, stack_mem + threadIdx.x, kQueryBlock, status);
     if (status) atomicOr(err, status);
-    if (found) rays[i].tfar = -__int_as_float(0x7f800000);
+    if (found) {
+        if (kAnyHit)
+            reinterpret_cast<float*>(rays + size_t(i) * record_float4s)[8] = -__int_as_float(0x7f800000);
+        else
+            store_hit(reinterpret_cast<SelRayHit*>(rays + size_t(i) * record_float4s), tris, h);
+    }
+}
+
+template <bool kAnyHit>
+cudaError_t launch_query(const DeviceBvh& bvh, float4* d_rays, uint32_t record_float4s, uint32_t n, uint32_t* d_err,
+                         cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const dim3 grid((n + kQueryBlock - 1) / kQueryBlock);
+    if (bvh.kind == SEL_BVH_WIDE8_Q8) {
+        k_query_wide<kAnyHit><<<grid, kQueryBlock, 0, s>>>(static_cast<const uint4*>(bvh.nodes), bvh.tris, d_rays,
+                                                           record_float4s, n, d_err);
+    } else {
+        k_query_binary<kAnyHit><<<grid, kQueryBlock, 0, s>>>(static_cast<const float4*>(bvh.nodes), bvh.tris, d_rays,
+                                                             record_float4s, n, d_err);
+    }
+    return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    const dim3 grid((n + kQueryBlock - 1) / kQueryBlock);
-    if (bvh.kind == SEL_BVH_WIDE8_Q8)
-        k_intersect<SEL_BVH_WIDE8_Q8><<<grid, kQueryBlock, 0, s>>>(bvh.nodes, bvh.tris, d_rays, n, d_err);
-    else
-        k_intersect<SEL_BVH_BINARY_FP32><<<grid, kQueryBlock, 0, s>>>(bvh.nodes, bvh.tris, d_rays, n, d_err);
-    return cudaGetLastError();
+    return launch_query<false>(bvh, reinterpret_cast<float4*>(d_rays), sizeof(SelRayHit) / 16, n, d_err, s);
 }
 
 cudaError_t launch_occluded(const DeviceBvh& bvh, SelRay* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    const dim3 grid((n + kQueryBlock - 1) / kQueryBlock);
-    if (bvh.kind == SEL_BVH_WIDE8_Q8)
-        k_occluded<SEL_BVH_WIDE8_Q8><<<grid, kQueryBlock, 0, s>>>(bvh.nodes, bvh.tris, d_rays, n, d_err);
-    else
-        k_occluded<SEL_BVH_BINARY_FP32><<<grid, kQueryBlock, 0, s>>>(bvh.nodes, bvh.tris, d_rays, n, d_err);
-    return cudaGetLastError();
+    return launch_query<true>(bvh, reinterpret_cast<float4*>(d_rays), sizeof(SelRay) / 16, n, d_err, s);
 }
 
 }  // namespace sel

@@ -77,7 +77,7 @@ struct BuiltBvh {
 std::string build_bvh(const std::vector<MeshInput>& meshes, int kind, BuiltBvh& out);
 
 // Traversal stack capacities (entries per thread); the builder rejects trees deeper than these.
-constexpr int kWideStack = 32;
+constexpr int kWideStack = 24;
 constexpr int kBinaryStack = 64;
 
 }  // namespace sel

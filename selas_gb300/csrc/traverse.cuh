@@ -113,114 +113,135 @@ __device__ __forceinline__ float byte_as_float(uint32_t word, int byte) {
 // ---------------------------------------------------------------------------------------------------
 // 8-wide quantised BVH.  Node groups on the stack are (child_base, hit bits 24..31 | imask bits 0..7);
 // hit bit 24 + (slot ^ octant) so that the lowest set bit is the nearest child for this ray octant.
-// `stack` points at this thread's first entry; entries are `stride` uint2 apart (shared memory).
-// Returns true on a hit (any-hit: as soon as one is found).
+// The traversal is written as a resumable per-ray state plus one step (one node visit and the triangles
+// it exposes), so that persistent kernels can refill finished lanes with new rays between steps.
 // ---------------------------------------------------------------------------------------------------
+struct WideState {
+    float ox, oy, oz, dx, dy, dz;
+    float tnear, tfar;  // tfar shrinks to the closest hit found so far
+    float ix, iy, iz;
+    Watertight wt;
+    uint32_t oct;
+    uint2 group;
+    int sp;
+    uint32_t iters;
+    uint64_t best_key;
+    QueryHit hit;
+};
+
+__device__ __forceinline__ void wide_init(WideState& s, const QueryRay& r) {
+    s.ox = r.ox; s.oy = r.oy; s.oz = r.oz;
+    s.dx = r.dx; s.dy = r.dy; s.dz = r.dz;
+    s.tnear = r.tnear;
+    s.tfar = r.tfar;
+    s.wt = watertight_setup(r.dx, r.dy, r.dz);
+    s.ix = safe_rcp(r.dx); s.iy = safe_rcp(r.dy); s.iz = safe_rcp(r.dz);
+    s.oct = (s.ix < 0.0f ? 4u : 0u) | (s.iy < 0.0f ? 2u : 0u) | (s.iz < 0.0f ? 1u : 0u);
+    s.group = make_uint2(0u, (1u << (24 + s.oct)) | 1u);
+    s.sp = 0;
+    s.iters = 0;
+    s.best_key = ~0ull;
+    s.hit.tri = 0xffffffffu;
+}
+
+// q as float: 0x4B0000qq is 2^23 + q exactly, the subtraction is exact as well.
+__device__ __forceinline__ float qbyte(uint32_t word, uint32_t byte) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | byte)) - 8388608.0f;
+}
+
+// One traversal step.  Returns true when the ray is finished (any-hit: on the first hit).
+template <bool kAnyHit>
+__device__ __forceinline__ bool wide_step(WideState& s, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                          uint2* stack, int stride, uint32_t& status) {
+    uint32_t tmask = 0, tbase = 0;
+    if (s.group.y & 0xff000000u) {
+        const int b = __ffs(s.group.y >> 24) - 1;
+        s.group.y &= ~(1u << (24 + b));
+        const uint32_t slot = uint32_t(b) ^ s.oct;
+        const uint32_t idx = s.group.x + __popc(s.group.y & ((1u << slot) - 1u));
+        if (s.group.y & 0xff000000u) {
+            if (s.sp >= kWideStack) { status |= kErrStackOverflow; return true; }
+            stack[s.sp * stride] = s.group;
+            ++s.sp;
+        }
+        const uint4* np = nodes + size_t(idx) * 5;
+        const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+        const float sxs = __fmul_rn(__uint_as_float((n0.w & 0xffu) << 23), s.ix);
+        const float sys = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xffu) << 23), s.iy);
+        const float szs = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xffu) << 23), s.iz);
+        const float oxa = __fmul_rn(__fsub_rn(__uint_as_float(n0.x), s.ox), s.ix);
+        const float oya = __fmul_rn(__fsub_rn(__uint_as_float(n0.y), s.oy), s.iy);
+        const float oza = __fmul_rn(__fsub_rn(__uint_as_float(n0.z), s.oz), s.iz);
+        const uint32_t imask = n0.w >> 24;
+        const float tnear_box = s.tnear - fabsf(s.tnear) * kBoxMargin;
+        const float tfar_box = s.tfar + fabsf(s.tfar) * kBoxMargin;
+        const bool px = s.ix >= 0.0f, py = s.iy >= 0.0f, pz = s.iz >= 0.0f;
+        const uint32_t nx0 = px ? n2.x : n3.z, nx1 = px ? n2.y : n3.w, fx0 = px ? n3.z : n2.x, fx1 = px ? n3.w : n2.y;
+        const uint32_t ny0 = py ? n2.z : n4.x, ny1 = py ? n2.w : n4.y, fy0 = py ? n4.x : n2.z, fy1 = py ? n4.y : n2.w;
+        const uint32_t nz0 = pz ? n3.x : n4.z, nz1 = pz ? n3.y : n4.w, fz0 = pz ? n4.z : n3.x, fz1 = pz ? n4.w : n3.y;
+        uint32_t new_hits = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const uint32_t byte = uint32_t(c & 3);
+            const float tnx = fmaf(qbyte(c < 4 ? nx0 : nx1, byte), sxs, oxa);
+            const float tfx = fmaf(qbyte(c < 4 ? fx0 : fx1, byte), sxs, oxa);
+            const float tny = fmaf(qbyte(c < 4 ? ny0 : ny1, byte), sys, oya);
+            const float tfy = fmaf(qbyte(c < 4 ? fy0 : fy1, byte), sys, oya);
+            const float tnz = fmaf(qbyte(c < 4 ? nz0 : nz1, byte), szs, oza);
+            const float tfz = fmaf(qbyte(c < 4 ? fz0 : fz1, byte), szs, oza);
+            const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tnear_box));
+            const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_box));
+            if (tmin <= tmax) {
+                if ((imask >> c) & 1u) {
+                    new_hits |= 1u << (uint32_t(c) ^ s.oct);
+                } else {
+                    const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
+                    tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+                }
+            }
+        }
+        s.group = make_uint2(n1.x, (new_hits << 24) | imask);
+        tbase = n1.y;
+    }
+    while (tmask) {
+        const int b = __ffs(tmask) - 1;
+        tmask &= tmask - 1u;
+        const uint32_t ti = tbase + uint32_t(b);
+        const float4* tp = tris + size_t(ti) * 3;
+        const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+        float t, u, v;
+        if (watertight_intersect(s.wt, s.ox, s.oy, s.oz, p0, p1, p2, s.tnear, s.tfar, t, u, v)) {
+            if (kAnyHit) {
+                s.hit.t = t; s.hit.u = u; s.hit.v = v; s.hit.tri = ti;
+                return true;
+            }
+            const uint64_t key = tri_key(p0, p1);
+            if (t < s.tfar || key < s.best_key) {
+                s.tfar = t;
+                s.best_key = key;
+                s.hit.t = t; s.hit.u = u; s.hit.v = v; s.hit.tri = ti;
+            }
+        }
+    }
+    if (++s.iters > kIterationCap) { status |= kErrIterationCap; return true; }
+    if (!(s.group.y & 0xff000000u)) {
+        if (s.sp == 0) return true;
+        --s.sp;
+        s.group = stack[s.sp * stride];
+    }
+    return false;
+}
+
+// Whole-ray form (one thread, one ray).
 template <bool kAnyHit>
 __device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                            const QueryRay& r, QueryHit& hit, uint2* stack, int stride,
                                            uint32_t& status) {
-    const Watertight wt = watertight_setup(r.dx, r.dy, r.dz);
-    const float ix = safe_rcp(r.dx), iy = safe_rcp(r.dy), iz = safe_rcp(r.dz);
-    const uint32_t oct = (ix < 0.0f ? 4u : 0u) | (iy < 0.0f ? 2u : 0u) | (iz < 0.0f ? 1u : 0u);
-    const float tnear_box = r.tnear - fabsf(r.tnear) * kBoxMargin;
-    float tfar = r.tfar;
-    float tfar_box = tfar + fabsf(tfar) * kBoxMargin;
-    uint64_t best_key = ~0ull;
-    bool found = false;
-    hit.tri = 0xffffffffu;
-
-    uint2 group = make_uint2(0u, (1u << (24 + oct)) | 1u);
-    int sp = 0;
-    uint32_t iters = 0;
-    for (;;) {
-        uint32_t tmask = 0, tbase = 0;
-        if (group.y & 0xff000000u) {
-            const int b = __ffs(group.y >> 24) - 1;
-            group.y &= ~(1u << (24 + b));
-            const uint32_t slot = uint32_t(b) ^ oct;
-            const uint32_t idx = group.x + __popc(group.y & ((1u << slot) - 1u));
-            if (group.y & 0xff000000u) {
-                if (sp >= kWideStack) { status |= kErrStackOverflow; break; }
-                stack[sp * stride] = group;
-                ++sp;
-            }
-            const uint4* np = nodes + size_t(idx) * 5;
-            const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
-            const float px = __uint_as_float(n0.x), py = __uint_as_float(n0.y), pz = __uint_as_float(n0.z);
-            const float sxs = __fmul_rn(__uint_as_float((n0.w & 0xffu) << 23), ix);
-            const float sys = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xffu) << 23), iy);
-            const float szs = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xffu) << 23), iz);
-            const float oxa = __fmul_rn(__fsub_rn(px, r.ox), ix);
-            const float oya = __fmul_rn(__fsub_rn(py, r.oy), iy);
-            const float oza = __fmul_rn(__fsub_rn(pz, r.oz), iz);
-            const uint32_t imask = n0.w >> 24;
-            // near/far plane words per axis (lo when the inverse direction is positive)
-            const uint32_t nx0 = ix >= 0.0f ? n2.x : n3.z, nx1 = ix >= 0.0f ? n2.y : n3.w;
-            const uint32_t fx0 = ix >= 0.0f ? n3.z : n2.x, fx1 = ix >= 0.0f ? n3.w : n2.y;
-            const uint32_t ny0 = iy >= 0.0f ? n2.z : n4.x, ny1 = iy >= 0.0f ? n2.w : n4.y;
-            const uint32_t fy0 = iy >= 0.0f ? n4.x : n2.z, fy1 = iy >= 0.0f ? n4.y : n2.w;
-            const uint32_t nz0 = iz >= 0.0f ? n3.x : n4.z, nz1 = iz >= 0.0f ? n3.y : n4.w;
-            const uint32_t fz0 = iz >= 0.0f ? n4.z : n3.x, fz1 = iz >= 0.0f ? n4.w : n3.y;
-            uint32_t new_hits = 0;
-#pragma unroll
-            for (int s = 0; s < 8; ++s) {
-                const int byte = s & 3;
-                const uint32_t wnx = s < 4 ? nx0 : nx1, wfx = s < 4 ? fx0 : fx1;
-                const uint32_t wny = s < 4 ? ny0 : ny1, wfy = s < 4 ? fy0 : fy1;
-                const uint32_t wnz = s < 4 ? nz0 : nz1, wfz = s < 4 ? fz0 : fz1;
-                const float tnx = fmaf(byte_as_float(wnx, byte), sxs, oxa);
-                const float tfx = fmaf(byte_as_float(wfx, byte), sxs, oxa);
-                const float tny = fmaf(byte_as_float(wny, byte), sys, oya);
-                const float tfy = fmaf(byte_as_float(wfy, byte), sys, oya);
-                const float tnz = fmaf(byte_as_float(wnz, byte), szs, oza);
-                const float tfz = fmaf(byte_as_float(wfz, byte), szs, oza);
-                const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tnear_box));
-                const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_box));
-                if (tmin <= tmax) {
-                    if ((imask >> s) & 1u) {
-                        new_hits |= 1u << (s ^ oct);
-                    } else {
-                        const uint32_t meta = ((s < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
-                        const uint32_t cnt = meta >> 5;
-                        tmask |= ((1u << cnt) - 1u) << (meta & 31u);
-                    }
-                }
-            }
-            group = make_uint2(n1.x, (new_hits << 24) | imask);
-            tbase = n1.y;
-        }
-        while (tmask) {
-            if (++iters > kIterationCap) { status |= kErrIterationCap; return found; }
-            const int b = __ffs(tmask) - 1;
-            tmask &= tmask - 1u;
-            const uint32_t ti = tbase + uint32_t(b);
-            const float4* tp = tris + size_t(ti) * 3;
-            const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-            float t, u, v;
-            if (watertight_intersect(wt, r.ox, r.oy, r.oz, p0, p1, p2, r.tnear, tfar, t, u, v)) {
-                if (kAnyHit) {
-                    hit.t = t; hit.u = u; hit.v = v; hit.tri = ti;
-                    return true;
-                }
-                const uint64_t key = tri_key(p0, p1);
-                if (t < tfar || key < best_key) {
-                    tfar = t;
-                    tfar_box = tfar + fabsf(tfar) * kBoxMargin;
-                    best_key = key;
-                    hit.t = t; hit.u = u; hit.v = v; hit.tri = ti;
-                    found = true;
-                }
-            }
-        }
-        if (!(group.y & 0xff000000u)) {
-            if (sp == 0) break;
-            --sp;
-            group = stack[sp * stride];
-        }
-        if (++iters > kIterationCap) { status |= kErrIterationCap; break; }
-    }
-    return found;
+    WideState s;
+    wide_init(s, r);
+    while (!wide_step<kAnyHit>(s, nodes, tris, stack, stride, status)) {}
+    hit = s.hit;
+    return s.hit.tri != 0xffffffffu;
 }
 
 // ---------------------------------------------------------------------------------------------------

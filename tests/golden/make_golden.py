@@ -1,0 +1,113 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own code.
+
+Run on a machine with the reference checkout (it loads oracle/_ref/*.so, built from the reference sources
+by oracle/ref/build_ref.py):
+
+    python tests/golden/make_golden.py
+
+bsdf_golden.npz  - seeded (surface, wo, wi) tuples -> EvaluateBsdf (f, forwardPdfW, reversePdfW) and
+                   seeded (surface, wo, 4 uniforms) tuples -> SampleBsdfFunction results, computed by
+                   Source/Core/Shading/SurfaceScattering.cpp:18-60 -> Disney.cpp / DiracTransparent.cpp.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+OUT = Path(__file__).resolve().parent
+
+SHADER_THIN, SHADER_SOLID, SHADER_DIRAC = 0, 1, 2
+
+
+def random_frames(rng, n):
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    helper = np.where(np.abs(nrm[:, :1]) < 0.9, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
+    t = np.cross(helper, nrm)
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    b = np.cross(nrm, t)
+    return t, nrm, b
+
+
+def random_dirs(rng, n, nrm, upper_frac):
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    up = np.sum(d * nrm, axis=1) >= 0
+    want_up = rng.random(n) < upper_frac
+    flip = up != want_up
+    d[flip] *= -1
+    return d
+
+
+def random_surfaces(rng, n, allow_dirac=True):
+    t, nrm, b = random_frames(rng, n)
+    s = np.zeros((n, 32), np.float64)
+    s[:, 0:3], s[:, 3:6], s[:, 6:9] = t, nrm, b
+    s[:, 9:12] = rng.uniform(0.02, 1.0, (n, 3))
+    s[:, 12:15] = rng.uniform(0.0, 1.0, (n, 3))
+
+    def sparse(p_zero, lo=0.0, hi=1.0):
+        v = rng.uniform(lo, hi, n)
+        v[rng.random(n) < p_zero] = 0.0
+        return v
+
+    s[:, 15] = sparse(0.5)                      # sheen
+    s[:, 16] = rng.random(n)                    # sheenTint
+    s[:, 17] = sparse(0.5)                      # clearcoat
+    s[:, 18] = rng.random(n)                    # clearcoatGloss
+    met = rng.random(n)
+    r = rng.random(n)
+    met[r < 0.4] = 0.0
+    met[(r >= 0.4) & (r < 0.6)] = 1.0
+    s[:, 19] = met                              # metallic
+    s[:, 20] = sparse(0.5)                      # specTrans
+    s[:, 21] = sparse(0.5, 0.0, 0.5)            # diffTrans (already halved, as SurfaceParameters holds it)
+    s[:, 22] = rng.random(n)                    # flatness
+    s[:, 23] = sparse(0.5)                      # anisotropic
+    ior = rng.uniform(1.1, 2.5, n)
+    s[:, 28] = ior
+    s[:, 24] = np.where(rng.random(n) < 0.5, 1.0 / ior, ior)  # relativeIOR
+    s[:, 25] = rng.random(n)                    # specularTint
+    rough = rng.uniform(0.01, 1.0, n)
+    rough[rng.random(n) < 0.05] = 0.005
+    s[:, 26] = rough                            # roughness
+    s[:, 27] = rng.uniform(0.1, 2.0, n)         # scatterDistance
+    sh = rng.random(n)
+    s[:, 29] = np.where(sh < 0.7, SHADER_SOLID, SHADER_THIN)
+    if allow_dirac:
+        s[sh >= 0.92, 29] = SHADER_DIRAC
+    return s.astype(np.float32)
+
+
+def make_bsdf(n_eval=3000, n_sample=3000, seed=0x5E1A5B5D):
+    lib = ctypes.CDLL(str(ROOT / "oracle" / "_ref" / "libref_bsdf.so"))
+    vp = ctypes.c_void_p
+    lib.ref_bsdf_evaluate.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    lib.ref_bsdf_sample.argtypes = [vp, vp, vp, ctypes.c_int, vp]
+    rng = np.random.default_rng(seed)
+
+    surf_e = random_surfaces(rng, n_eval, allow_dirac=False)
+    wo_e = random_dirs(rng, n_eval, surf_e[:, 3:6].astype(np.float64), 0.8).astype(np.float32)
+    wi_e = random_dirs(rng, n_eval, surf_e[:, 3:6].astype(np.float64), 0.7).astype(np.float32)
+    out_e = np.zeros((n_eval, 5), np.float32)
+    lib.ref_bsdf_evaluate(surf_e.ctypes.data, wo_e.ctypes.data, wi_e.ctypes.data, n_eval, out_e.ctypes.data)
+
+    surf_s = random_surfaces(rng, n_sample, allow_dirac=True)
+    wo_s = random_dirs(rng, n_sample, surf_s[:, 3:6].astype(np.float64), 0.8).astype(np.float32)
+    u_s = rng.random((n_sample, 4)).astype(np.float32)
+    out_s = np.zeros((n_sample, 16), np.float32)
+    lib.ref_bsdf_sample(surf_s.ctypes.data, wo_s.ctypes.data, u_s.ctypes.data, n_sample, out_s.ctypes.data)
+
+    np.savez_compressed(OUT / "bsdf_golden.npz", surf_e=surf_e, wo_e=wo_e, wi_e=wi_e, out_e=out_e,
+                        surf_s=surf_s, wo_s=wo_s, u_s=u_s, out_s=out_s)
+    print("bsdf_golden.npz:", n_eval, "eval,", n_sample, "sample tuples;",
+          "nonzero f:", int((out_e[:, :3].sum(1) > 0).sum()), "successful samples:", int(out_s[:, 0].sum()))
+
+
+if __name__ == "__main__":
+    make_bsdf()
