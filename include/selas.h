@@ -178,6 +178,74 @@ int sel_bsdf_evaluate_device(const SelSurface* d_surfaces, const float* d_wo, co
 int sel_bsdf_sample_device(const SelSurface* d_surfaces, const float* d_wo, const float* d_u, unsigned int n,
                            float* d_out, void* stream);
 
+/* ------------------------------------------------------------------------------------------------ */
+/* Shading data of a scene.                                                                          */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* The MaterialResourceData fields the renderer reads (Source/Core/SceneLib/ModelResource.h:68-88), with
+ * the scalar attributes in eMaterialProperty order (Source/Core/BuildCommon/ImportMaterial.cpp:36-52).
+ * baseColor is as authored: shading raises it to the power 2.2 (Shading/SurfaceParameters.cpp:210-212).
+ * The transparent flag is derived as the reference's build step does (BuildCommon/BuildModel.cpp:60-65). */
+typedef struct SelMaterial {
+    int32_t shader;
+    uint32_t lightSetIndex;
+    float baseColor[3];
+    float transmittanceColor[3];
+    float metallic, specularTint, roughness, anisotropic, sheen, sheenTint, clearcoat, clearcoatGloss;
+    float specTrans, diffuseTrans, flatness, ior, scatterDistance;
+    uint32_t usesPtex;   /* 1: base colour from the geometry's per-face Ptex texels */
+} SelMaterial;
+
+/* Fills the reference's default material (CreateDefaultMaterial, SceneLib/ModelResource.cpp:203-211). */
+int sel_material_defaults(SelMaterial* out);
+/* Material of geometry geomID (geomID < 65536); geometries without one use the default material. */
+int sel_scene_set_material(SelScene scene, unsigned int geomID, const SelMaterial* material);
+
+/* SceneLight (SceneLib/SceneResource.h) as the lighting code reads it: quad centre, facing direction,
+ * full edge vectors x and z, emitted radiance (AreaLighting.cpp:113-153). */
+typedef struct SelQuadLight {
+    float position[3];
+    float direction[3];
+    float x[3];
+    float z[3];
+    float radiance[3];
+} SelQuadLight;
+int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const SelQuadLight* light);
+/* backgroundIntensity (default 1, BuildCommon/CSceneBuildProcessor.cpp:59). */
+int sel_scene_set_background(SelScene scene, float r, float g, float b);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Integrator entry points.                                                                          */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* CameraSettings (GeometryLib/Camera.h:13-21: position, lookAt, up, horizontal fovDegrees) and the
+ * viewport InitializeRayCastCamera receives (GeometryLib/Camera.cpp:89-115). */
+typedef struct SelCamera {
+    float position[3];
+    float lookAt[3];
+    float up[3];
+    float fovDegrees;
+    uint32_t width, height;
+} SelCamera;
+
+typedef struct SelPtSettings {
+    uint32_t samplesPerPixel;  /* PathsPerPixel_ (PathTracer.cpp:45) */
+    uint32_t maxBounces;       /* MaxBounceCount_ (PathTracer.cpp:42) */
+    uint64_t seed;             /* PCG32 seed; path k uses stream k */
+    uint32_t pathsInFlight;    /* wavefront batch (0 = 4,194,304) */
+    uint32_t reserved;
+} SelPtSettings;
+
+/* PathTracer::GenerateImage (Source/Applications/Selas/Source/PathTracer.h:20-21): renders the scene
+ * with the wavefront path tracer and writes the two framebuffer layers, already scaled by 1/spp
+ * (FrameBuffer_Scale, PathTracer.cpp:346), to out_layers: [2][height][width][3] floats in host memory.
+ * Layer 0 is the first-bounce BSDF sample weight, layer 1 the radiance estimate.  Accumulation is FP64. */
+int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, float* out_layers);
+/* Device form: adds the un-normalised FP64 sums into d_accum ([2][height][width][3] doubles in HBM) on
+ * `stream` and returns without waiting. */
+int sel_pt_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,13 +30,13 @@ def lib() -> ctypes.CDLL:
             "oracle_bvh_free": ([_vp], None),
             "oracle_intersect_bvh": ([_vp, _vp, _i64, _i], None),
             "oracle_occluded_bvh": ([_vp, _vp, _i64, _i], None),
+            "oracle_bsdf_evaluate": ([_vp, _vp, _vp, _i64, _vp], None),
+            "oracle_bsdf_sample": ([_vp, _vp, _vp, _i64, _vp], None),
+            "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
+                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.c_uint64, _i, _i, _vp], None),
         }
         for name, (args, res) in sig.items():
-            fn = getattr(_lib, name)
-            fn.argtypes = args
-            fn.restype = res
-        extra = getattr(__import__(__name__), "_extra_signatures", {})
-        for name, (args, res) in extra.items():
             fn = getattr(_lib, name)
             fn.argtypes = args
             fn.restype = res
@@ -80,3 +80,45 @@ class OracleBvh:
         if getattr(self, "handle", None) and _lib is not None:
             _lib.oracle_bvh_free(self.handle)
             self.handle = None
+
+
+def surface_records(surf: np.ndarray) -> np.ndarray:
+    """Golden-fixture surfaces keep the shader as a float; SelSurface records hold it as int32 bits."""
+    out = np.ascontiguousarray(surf, np.float32).copy()
+    out[:, 29] = out[:, 29].astype(np.int32).view(np.float32)
+    return out
+
+
+def bsdf_evaluate(surf, wo, wi):
+    s = surface_records(surf)
+    wo, wi = np.ascontiguousarray(wo, np.float32), np.ascontiguousarray(wi, np.float32)
+    out = np.zeros((s.shape[0], 5), np.float32)
+    lib().oracle_bsdf_evaluate(_p(s), _p(wo), _p(wi), s.shape[0], _p(out))
+    return out
+
+
+def bsdf_sample(surf, wo, u):
+    s = surface_records(surf)
+    wo, u = np.ascontiguousarray(wo, np.float32), np.ascontiguousarray(u, np.float32)
+    out = np.zeros((s.shape[0], 16), np.float32)
+    lib().oracle_bsdf_sample(_p(s), _p(wo), _p(u), s.shape[0], _p(out))
+    return out
+
+
+def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, seed=0x5E1A5000, rng="pcg",
+              nthreads=None):
+    """CPU oracle path tracer (oracle_pt.cpp): FP64 per-pixel sums over passes [pass_begin, pass_end),
+    shape (2, height, width, 3)."""
+    from selas_gb300.scenes import light_records, material_records
+    verts, prim, geom = render_scene.geometry.soup()
+    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    lights, sets = light_records(render_scene.lights)
+    bg = np.array(render_scene.background, np.float32)
+    c = render_scene.camera
+    cam = np.array(list(c["position"]) + list(c["look_at"]) + list(c["up"]) + [c["fov_degrees"]], np.float32)
+    out = np.zeros((2, height, width, 3), np.float64)
+    L = lib()
+    L.oracle_pt_render(_p(verts), _p(prim), _p(geom), verts.shape[0], _p(mats), mats.shape[0], _p(lights),
+                       lights.shape[0], _p(sets), sets.shape[0], _p(bg), _p(cam), width, height, pass_begin, pass_end,
+                       max_bounces, seed, 0 if rng == "pcg" else 1, nthreads or threads(), _p(out))
+    return out

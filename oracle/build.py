@@ -18,7 +18,8 @@ LIB = HERE / "liboracle.so"
 
 def build_oracle(force: bool = False) -> Path:
     srcs = sorted(HERE.glob("*.cpp"))
-    if not force and LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in srcs):
+    deps = srcs + sorted(HERE.glob("*.h"))
+    if not force and LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in deps):
         return LIB
     tmp = LIB.with_suffix(".so.tmp")
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",

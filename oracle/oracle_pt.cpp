@@ -1,0 +1,360 @@
+// ORACLE - test infrastructure only (see oracle_query.cpp).
+//
+// CPU restatement of the reference unidirectional path tracer, one path at a time:
+//   EvaluatePath       Source/Applications/Selas/Source/PathTracer.cpp:142-258
+//   RayPick            PathTracer.cpp:95-139 (tnear 0, error bound 32 * 1.19209e-07 * max(|p|, t))
+//   OcclusionRay       PathTracer.cpp:71-92  (origin offset 0.1 * error, tnear = error)
+//   JitteredCameraRay  Source/Core/GeometryLib/Camera.cpp:56-74; InitializeRayCastCamera :89-115
+//   NextEventEstimation / SampleRectangleLightSolidAngle  Source/Core/Shading/AreaLighting.cpp:113-153,353-373
+//   RectangleLightSampler  Source/Core/GeometryLib/RectangulerLightSampler.cpp:17-97
+//   CalculateSurfaceParams Source/Core/Shading/SurfaceParameters.cpp:144-247 (no normals/tangents/uvs)
+//   Isotropic media        Source/Core/Shading/IsotropicScattering.cpp, VolumetricScattering.cpp
+// Random numbers: either PCG32 with one stream per path (stream = pass * W * H + pixel, the sampling the
+// GPU path tracer uses) or MT19937 as the reference's CSampler draws them (Random.cpp:46-49), one engine
+// per pixel.  Each path's two layers are summed in float as the reference's Ld[] (PathTracer.cpp:144-257)
+// and the per-pixel sums are kept in double.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "oracle_bsdf.h"
+#include "oracle_query.h"
+
+using orc::V3;
+
+namespace {
+
+const float kPi = 3.141592653589793f;
+
+struct Rng {
+    bool pcg = true;
+    uint64_t state = 0, inc = 1;
+    std::mt19937 mt;
+    uint32_t next_u32() {
+        const uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        const uint32_t xs = uint32_t(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = uint32_t(old >> 59u);
+        return (xs >> rot) | (xs << ((32u - rot) & 31u));
+    }
+    void seed_pcg(uint64_t seed, uint64_t stream) {
+        pcg = true;
+        state = 0;
+        inc = (stream << 1u) | 1u;
+        next_u32();
+        state += seed;
+        next_u32();
+    }
+    float uniform() {
+        if (pcg) return float(next_u32() >> 8) * (1.0f / 16777216.0f);
+        return float(mt()) / float(0xFFFFFFFFu);
+    }
+};
+
+struct Camera {
+    V3 x, y, z, pos;
+    float w, h;
+};
+
+Camera make_camera(const float* c, uint32_t width, uint32_t height) {
+    // c: position[3] lookAt[3] up[3] fovDegrees
+    Camera cam;
+    const float widthf = float(width), heightf = float(height);
+    const float aspect = widthf / heightf;
+    const float hfov = c[9] * (kPi / 180.0f);
+    const float hlen = std::tan(hfov * 0.5f);
+    const float vfov = 2.0f * std::atan(hlen / aspect);
+    const float vlen = std::tan(vfov * 0.5f);
+    V3 pos(c[0], c[1], c[2]), look(c[3], c[4], c[5]), up(c[6], c[7], c[8]);
+    V3 fwd = orc::Norm(look - pos);
+    V3 right = orc::Norm(orc::Cross(up, fwd));
+    cam.x = hlen * right;
+    cam.y = vlen * orc::Cross(fwd, right);
+    cam.z = fwd;
+    cam.pos = pos;
+    cam.w = widthf;
+    cam.h = heightf;
+    return cam;
+}
+
+struct Light {
+    V3 pos, dir, x, z, radiance;
+};
+
+struct Material {
+    int shader;
+    uint32_t flags, light_set;
+    float base[3], trans[3];
+    float sheen, sheenTint, clearcoat, clearcoatGloss, metallic, specTrans, diffTrans, flatness;
+    float anisotropic, specularTint, roughness, scatterDistance, ior;
+};
+
+Material read_material(const float* r) {
+    Material m;
+    int32_t sh;
+    uint32_t fl, ls;
+    std::memcpy(&sh, r + 0, 4);
+    std::memcpy(&fl, r + 1, 4);
+    std::memcpy(&ls, r + 2, 4);
+    m.shader = sh;
+    m.flags = fl;
+    m.light_set = ls;
+    for (int i = 0; i < 3; ++i) { m.base[i] = r[4 + i]; m.trans[i] = r[7 + i]; }
+    m.sheen = r[10]; m.sheenTint = r[11]; m.clearcoat = r[12]; m.clearcoatGloss = r[13];
+    m.metallic = r[14]; m.specTrans = r[15]; m.diffTrans = r[16]; m.flatness = r[17];
+    m.anisotropic = r[18]; m.specularTint = r[19]; m.roughness = r[20]; m.scatterDistance = r[21]; m.ior = r[22];
+    return m;
+}
+
+float Sat(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+// SampleRectangleLightSolidAngle (AreaLighting.cpp:113-153) with the sampler of RectangulerLightSampler.cpp.
+void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad, float& dist, float& pdfw) {
+    V3 s = L.pos - 0.5f * L.x - 0.5f * L.z;
+    const float exl = orc::Len(L.x), eyl = orc::Len(L.z);
+    V3 X = L.x * (1.0f / exl), Y = L.z * (1.0f / eyl), Z = orc::Cross(X, Y);
+    V3 d = s - p;
+    float z0 = orc::Dot(d, Z);
+    if (z0 > 0) { Z = -1.0f * Z; z0 *= -1; }
+    const float z0sq = z0 * z0, x0 = orc::Dot(d, X), y0 = orc::Dot(d, Y);
+    const float x1 = x0 + exl, y1 = y0 + eyl, y0sq = y0 * y0, y1sq = y1 * y1;
+    V3 v00(x0, y0, z0), v01(x0, y1, z0), v10(x1, y0, z0), v11(x1, y1, z0);
+    V3 n0 = orc::Norm(orc::Cross(v00, v10)), n1 = orc::Norm(orc::Cross(v10, v11));
+    V3 n2 = orc::Norm(orc::Cross(v11, v01)), n3 = orc::Norm(orc::Cross(v01, v00));
+    const float g0 = std::acos(-orc::Dot(n0, n1)), g1 = std::acos(-orc::Dot(n1, n2));
+    const float g2 = std::acos(-orc::Dot(n2, n3)), g3 = std::acos(-orc::Dot(n3, n0));
+    const float b0 = n0.z, b1 = n2.z, b0sq = b0 * b0;
+    const float k = 2 * kPi - g2 - g3;
+    const float S = g0 + g1 - k;
+    const float pdf = 1.0f / S;
+    // SampleRectangleLight
+    const float au = u * S + k;
+    const float fu = (std::cos(au) * b0 - b1) / std::sin(au);
+    float cu = 1 / std::sqrt(fu * fu + b0sq) * (fu > 0 ? +1 : -1);
+    cu = std::min(std::max(cu, -1.0f), 1.0f);
+    float xu = -(cu * z0) / std::sqrt(1 - cu * cu);
+    xu = std::min(std::max(xu, x0), x1);
+    const float dd = std::sqrt(xu * xu + z0sq);
+    const float h0 = y0 / std::sqrt(dd * dd + y0sq);
+    const float h1 = y1 / std::sqrt(dd * dd + y1sq);
+    const float hv = h0 + v * (h1 - h0), hv2 = hv * hv;
+    const float yv = (hv2 < 1 - 1e-10f) ? (hv * dd) / std::sqrt(1 - hv2) : y1;
+    V3 lp = p + xu * X + yv * Y + z0 * Z;
+    V3 ul = lp - p;
+    const float d2 = orc::Dot(ul, ul);
+    const float di = std::sqrt(d2);
+    V3 l = (1.0f / di) * ul;
+    const float area = orc::Dot(L.dir, -1.0f * l) / d2;
+    if (area > 0) {
+        dir = l;
+        dist = di;
+        rad = L.radiance * (area * orc::Dot(n, l));
+        pdfw = pdf * area;
+    } else {
+        dir = V3(0.0f);
+        dist = 0;
+        rad = V3(0.0f);
+        pdfw = 1.0f;
+    }
+}
+
+struct Scene {
+    const void* bvh;
+    std::vector<Material> materials;
+    std::vector<Light> lights;
+    std::vector<uint32_t> set_first, set_count;
+    V3 background;
+};
+
+V3 offset(V3 p, V3 n, float err, V3 dir, float scale) {
+    const float side = orc::Dot(dir, n) < 0.0f ? -1.0f : 1.0f;
+    return p + (side * err * scale) * n;
+}
+
+// EvaluatePath (PathTracer.cpp:142-258); returns both layers.
+void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounces, V3& ld0, V3& ld1) {
+    ld0 = V3(0.0f);
+    ld1 = V3(0.0f);
+    V3 thr(1.0f);
+    int phase = 0;
+    V3 ext(0.0f);
+    uint32_t bounce = 0;
+    while (bounce < max_bounces) {
+        float tfar = 3.402823466e+38f;
+        if (phase == 1) {  // Isotropic::SampleDistance
+            const float ps = ext.x + ext.y + ext.z;
+            const float pr = ext.x / ps, pg = ext.y / ps;
+            float c;
+            const float r0 = rng.uniform();
+            if (r0 < pr) c = ext.x;
+            else if (r0 < pr + pg) c = ext.y;
+            else c = ext.z;
+            tfar = -std::log(rng.uniform()) / c;
+        }
+        orq::Hit h;
+        const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
+        const bool hit = orq::closest(sc.bvh, o, d, 0.0f, tfar, h);
+        float ray_distance = tfar;
+        V3 pos;
+        if (hit) {
+            pos = V3(org.x + h.t * dir.x, org.y + h.t * dir.y, org.z + h.t * dir.z);
+            ray_distance = orc::Len(pos - org);
+        }
+        if (phase == 1)
+            thr = thr * V3(std::exp(-ext.x * ray_distance), std::exp(-ext.y * ray_distance), std::exp(-ext.z * ray_distance));
+        if (hit) {
+            const Material& m = sc.materials[h.geom < sc.materials.size() ? h.geom : 0];
+            const float err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(pos.x), std::fabs(pos.y)),
+                                                              std::max(std::fabs(pos.z), h.t));
+            orc::Surf s;
+            const V3 n = orc::Norm(V3(h.ng[0], h.ng[1], h.ng[2]));
+            V3 t, b;
+            if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
+            else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
+            b = orc::Cross(n, t);
+            s.t = t; s.n = n; s.b = b;
+            s.baseColor = V3(std::pow(m.base[0], 2.2f), std::pow(m.base[1], 2.2f), std::pow(m.base[2], 2.2f));
+            s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
+            s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
+            s.specTrans = Sat(m.specTrans); s.diffTrans = m.diffTrans * 0.5f; s.flatness = m.flatness;
+            s.anisotropic = m.anisotropic; s.specularTint = m.specularTint; s.roughness = m.roughness;
+            s.metallic = Sat(m.metallic); s.scatterDistance = m.scatterDistance; s.ior = m.ior; s.shader = m.shader;
+            const V3 view = -1.0f * dir;
+            s.relativeIOR = ((m.flags & 1u) && orc::Dot(view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
+            // next-event estimation
+            V3 ldir, lrad(0.0f);
+            float ldist = 0, lpdf = 1;
+            if (m.light_set < sc.set_count.size() && sc.set_count[m.light_set] > 0) {
+                const uint32_t cnt = sc.set_count[m.light_set];
+                const float p0 = rng.uniform();
+                uint32_t li = uint32_t(p0 * float(cnt));
+                li = std::min(li, cnt - 1);
+                const float u = rng.uniform(), v = rng.uniform();
+                sample_light(sc.lights[sc.set_first[m.light_set] + li], pos, n, u, v, ldir, lrad, ldist, lpdf);
+                lpdf *= 1.0f / float(cnt);
+            }
+            if (orc::Dot(lrad, V3(1.0f)) > 0) {
+                float fp, rp;
+                const V3 refl = orc::bsdf_evaluate(s, view, ldir, fp, rp);
+                if (orc::Dot(refl, V3(1.0f)) > 0) {
+                    const V3 so = offset(pos, n, err, ldir, 0.1f);
+                    const float soa[3] = {so.x, so.y, so.z}, lda[3] = {ldir.x, ldir.y, ldir.z};
+                    if (!orq::occluded(sc.bvh, soa, lda, err, ldist)) ld1 = ld1 + refl * lrad * (1.0f / lpdf) * thr;
+                }
+            }
+            // BSDF sample: uniforms drawn lazily, in order
+            float u4[4];
+            Rng ahead = rng;
+            for (int k = 0; k < 4; ++k) u4[k] = ahead.uniform();
+            int used = 0;
+            orc::Sample bs;
+            const bool ok = orc::bsdf_sample(s, view, u4, used, bs);
+            for (int k = 0; k < used; ++k) rng.uniform();
+            if (!ok) break;
+            if (bs.flags == 2u) {
+                if (phase == 0) { phase = bs.phase; ext = bs.ext; }
+                else { phase = 0; ext = V3(0.0f); }
+            }
+            thr = 1.0f * thr * bs.refl;
+            org = offset(pos, n, err, bs.wi, 1.0f);
+            dir = bs.wi;
+            if (bounce == 0) ld0 = bs.refl;
+        } else if (phase != 0) {
+            org = org + ray_distance * dir;
+            const float r0 = rng.uniform(), r1 = rng.uniform();
+            const float uu = 2.0f * r1 - 1.0f;
+            const float nn = std::sqrt(std::max(0.0f, 1.0f - uu * uu));
+            const float th = 2.0f * kPi * r0;
+            dir = V3(nn * std::cos(th), uu, nn * std::sin(th));
+        } else {
+            ld1 = ld1 + sc.background * thr;
+            break;
+        }
+        ++bounce;
+        if (bounce > 8) {
+            const float cp = std::max(std::max(thr.x, thr.y), thr.z);
+            if (rng.uniform() > cp) break;
+            thr = thr * (1.0f / cp);
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// verts/prim/geom: triangle soup; materials: n_materials x 32 words (MaterialDev layout, indexed by geomID);
+// lights: n_lights x 15 floats (position, direction, x, z, radiance); sets: n_sets x 2 (first, count);
+// camera: position[3] lookAt[3] up[3] fovDegrees; out: [2][height][width][3] doubles (sums over the paths
+// of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the GPU); 1: MT19937 per pixel.
+void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
+                      const float* materials, int n_materials, const float* lights, int n_lights,
+                      const uint32_t* sets, int n_sets, const float* background, const float* camera,
+                      uint32_t width, uint32_t height, uint32_t pass_begin, uint32_t pass_end, uint32_t max_bounces,
+                      uint64_t seed, int rng_mode, int threads, double* out) {
+    Scene sc;
+    sc.bvh = orq::build(verts, prim, geom, ntri);
+    for (int i = 0; i < n_materials; ++i) sc.materials.push_back(read_material(materials + 32 * i));
+    for (int i = 0; i < n_lights; ++i) {
+        const float* l = lights + 15 * i;
+        Light L;
+        L.pos = V3(l[0], l[1], l[2]);
+        L.dir = V3(l[3], l[4], l[5]);
+        L.x = V3(l[6], l[7], l[8]);
+        L.z = V3(l[9], l[10], l[11]);
+        L.radiance = V3(l[12], l[13], l[14]);
+        sc.lights.push_back(L);
+    }
+    for (int i = 0; i < n_sets; ++i) {
+        sc.set_first.push_back(sets[2 * i]);
+        sc.set_count.push_back(sets[2 * i + 1]);
+    }
+    sc.background = V3(background[0], background[1], background[2]);
+    const Camera cam = make_camera(camera, width, height);
+    const uint32_t npix = width * height;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const uint32_t pix0 = next.fetch_add(16);
+            if (pix0 >= npix) break;
+            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
+                const uint32_t y = pixel / width, x = pixel - y * width;
+                Rng rng;
+                if (rng_mode == 1) {
+                    rng.pcg = false;
+                    rng.mt.seed(uint32_t(seed) + pixel);
+                }
+                double acc[6] = {0, 0, 0, 0, 0, 0};
+                for (uint32_t pass = pass_begin; pass < pass_end; ++pass) {
+                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(pass) * npix + pixel);
+                    const float vx = float(x) + rng.uniform();
+                    const float vy = float(y) + rng.uniform();
+                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
+                    const float cy = 1.0f - 2.0f * vy / cam.h;
+                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
+                    V3 l0, l1;
+                    evaluate_path(sc, rng, cam.pos, d, max_bounces, l0, l1);
+                    acc[0] += l0.x; acc[1] += l0.y; acc[2] += l0.z;
+                    acc[3] += l1.x; acc[4] += l1.y; acc[5] += l1.z;
+                }
+                for (int c = 0; c < 3; ++c) {
+                    out[size_t(pixel) * 3 + c] += acc[c];
+                    out[(size_t(npix) + pixel) * 3 + c] += acc[3 + c];
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    const int nt = std::max(1, threads);
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+    orq::release(const_cast<void*>(sc.bvh));
+}
+
+}  // extern "C"

@@ -410,3 +410,48 @@ void oracle_occluded_bvh(void* h, void* rays, int64_t m, int threads) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------
+// Entry points for the oracle integrators (oracle_query.h).
+// ---------------------------------------------------------------------------------------------------
+#include "oracle_query.h"
+
+namespace orq {
+
+void* build(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n) {
+    return oracle_bvh_build(verts, prim, geom, n);
+}
+
+bool closest(const void* h, const float* org, const float* dir, float tnear, float tfar, Hit& out) {
+    const Bvh& bvh = *static_cast<const Bvh*>(h);
+    Ray r;
+    std::memcpy(r.org, org, 12);
+    std::memcpy(r.dir, dir, 12);
+    r.tnear = tnear;
+    r.tfar = tfar;
+    Best best;
+    if (!trace<false>(bvh, r, best)) return false;
+    const Tri& t = bvh.tris[size_t(best.tri)];
+    out.t = best.t;
+    out.u = best.u;
+    out.v = best.v;
+    normal(t, out.ng);
+    out.prim = t.prim;
+    out.geom = t.geom;
+    return true;
+}
+
+void release(void* h) { oracle_bvh_free(h); }
+
+bool occluded(const void* h, const float* org, const float* dir, float tnear, float tfar) {
+    const Bvh& bvh = *static_cast<const Bvh*>(h);
+    Ray r;
+    std::memcpy(r.org, org, 12);
+    std::memcpy(r.dir, dir, 12);
+    r.tnear = tnear;
+    r.tfar = tfar;
+    Best best;
+    return trace<true>(bvh, r, best);
+}
+
+}  // namespace orq

@@ -207,3 +207,101 @@ def make_rays(org: np.ndarray, dirs: np.ndarray, tnear=0.0, tfar=np.inf) -> np.n
     r["tfar"] = tfar
     r["mask"] = 0xFFFFFFFF
     return r
+
+
+# ---------------------------------------------------------------------------------------------------
+# Shading data and the path tracer (include/selas.h: SelMaterial, SelQuadLight, SelCamera, SelPtSettings)
+# ---------------------------------------------------------------------------------------------------
+_f3 = ctypes.c_float * 3
+
+
+class SelMaterial(ctypes.Structure):
+    _fields_ = [("shader", ctypes.c_int32), ("lightSetIndex", ctypes.c_uint32), ("baseColor", _f3),
+                ("transmittanceColor", _f3)] + [(n, ctypes.c_float) for n in (
+                    "metallic", "specularTint", "roughness", "anisotropic", "sheen", "sheenTint", "clearcoat",
+                    "clearcoatGloss", "specTrans", "diffuseTrans", "flatness", "ior", "scatterDistance")] + [
+                ("usesPtex", ctypes.c_uint32)]
+
+
+class SelQuadLight(ctypes.Structure):
+    _fields_ = [("position", _f3), ("direction", _f3), ("x", _f3), ("z", _f3), ("radiance", _f3)]
+
+
+class SelCamera(ctypes.Structure):
+    _fields_ = [("position", _f3), ("lookAt", _f3), ("up", _f3), ("fovDegrees", ctypes.c_float),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class SelPtSettings(ctypes.Structure):
+    _fields_ = [("samplesPerPixel", ctypes.c_uint32), ("maxBounces", ctypes.c_uint32), ("seed", ctypes.c_uint64),
+                ("pathsInFlight", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+SEL_SHADER_DISNEY_THIN, SEL_SHADER_DISNEY_SOLID, SEL_SHADER_DIRAC_TRANSPARENT = 0, 1, 2
+
+register_signatures({
+    "sel_bsdf_evaluate_device": [_vp, _vp, _vp, _u, _vp, _vp],
+    "sel_bsdf_sample_device": [_vp, _vp, _vp, _u, _vp, _vp],
+    "sel_material_defaults": [ctypes.POINTER(SelMaterial)],
+    "sel_scene_set_material": [_vp, _u, ctypes.POINTER(SelMaterial)],
+    "sel_scene_add_quad_light": [_vp, _u, ctypes.POINTER(SelQuadLight)],
+    "sel_scene_set_background": [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float],
+    "sel_pt_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
+    "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
+})
+
+
+def material(**kw) -> SelMaterial:
+    """SelMaterial starting from the reference default material, fields overridden by keyword."""
+    m = SelMaterial()
+    check(lib().sel_material_defaults(ctypes.byref(m)))
+    for k, v in kw.items():
+        if isinstance(getattr(m, k), ctypes.Array):
+            getattr(m, k)[:] = list(v)
+        else:
+            setattr(m, k, v)
+    return m
+
+
+def camera(position, look_at, up, fov_degrees, width, height) -> SelCamera:
+    c = SelCamera()
+    c.position[:] = list(position)
+    c.lookAt[:] = list(look_at)
+    c.up[:] = list(up)
+    c.fovDegrees = fov_degrees
+    c.width, c.height = width, height
+    return c
+
+
+def pt_settings(spp, max_bounces=8, seed=0x5E1A5000, paths_in_flight=0) -> SelPtSettings:
+    s = SelPtSettings()
+    s.samplesPerPixel, s.maxBounces, s.seed, s.pathsInFlight = spp, max_bounces, seed, paths_in_flight
+    return s
+
+
+def _scene_set_material(self, geom_id: int, m: SelMaterial) -> None:
+    check(lib().sel_scene_set_material(self.handle, geom_id, ctypes.byref(m)))
+
+
+def _scene_add_quad_light(self, light_set: int, position, direction, x, z, radiance) -> None:
+    q = SelQuadLight()
+    q.position[:], q.direction[:], q.x[:], q.z[:], q.radiance[:] = (list(position), list(direction), list(x),
+                                                                     list(z), list(radiance))
+    check(lib().sel_scene_add_quad_light(self.handle, light_set, ctypes.byref(q)))
+
+
+def _scene_set_background(self, rgb) -> None:
+    check(lib().sel_scene_set_background(self.handle, *map(float, rgb)))
+
+
+def _scene_pt_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> np.ndarray:
+    """PathTracer::GenerateImage: (2, height, width, 3) float32 layers, scaled by 1/spp."""
+    out = np.zeros((2, cam.height, cam.width, 3), np.float32)
+    check(lib().sel_pt_generate_image(self.handle, ctypes.byref(cam), ctypes.byref(settings), out.ctypes.data))
+    return out
+
+
+Scene.set_material = _scene_set_material
+Scene.add_quad_light = _scene_add_quad_light
+Scene.set_background = _scene_set_background
+Scene.pt_generate_image = _scene_pt_generate_image

@@ -1,6 +1,7 @@
 // C ABI: device and scene lifetime plus the ray-query entry points declared in include/selas.h.
 // Status codes instead of exceptions; the message of the last failure is kept per host thread.
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -10,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "capi_internal.h"
+#include "pt.h"
 #include "query.h"
 
 using sel::BuiltBvh;
@@ -220,9 +222,9 @@ int sel_scene_release(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     set_device(scene->dev);
     cudaStreamSynchronize(scene->dev->stream);
-    if (scene->d_nodes) cudaFree(scene->d_nodes);
-    if (scene->d_tris) cudaFree(scene->d_tris);
-    if (scene->scratch) cudaFree(scene->scratch);
+    for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
+                    scene->d_light_sets, scene->pt_block, scene->d_accum})
+        if (p) cudaFree(p);
     delete scene;
     return SEL_OK;
 }
@@ -322,3 +324,44 @@ int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* st
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------
+// Camera set-up on the host (compiled without contraction so the CPU oracle, which restates the same
+// steps, derives a bit-identical basis): InitializeRayCastCamera (GeometryLib/Camera.cpp:89-115).
+// ---------------------------------------------------------------------------------------------------
+namespace sel {
+
+void init_camera(const SelCamera& c, PtCamera& out) {
+    auto sub = [](const float* a, const float* b, float* o) { for (int i = 0; i < 3; ++i) o[i] = a[i] - b[i]; };
+    auto norm = [](float* v) {
+        const float il = 1.0f / std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        for (int i = 0; i < 3; ++i) v[i] = v[i] * il;
+    };
+    auto cross = [](const float* a, const float* b, float* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    const float widthf = float(c.width), heightf = float(c.height);
+    const float aspect = widthf / heightf;
+    const float hfov = c.fovDegrees * (3.141592653589793f / 180.0f);
+    const float hlen = std::tan(hfov * 0.5f);
+    const float vfov = 2.0f * std::atan(hlen / aspect);
+    const float vlen = std::tan(vfov * 0.5f);
+    float fwd[3], right[3], upv[3];
+    sub(c.lookAt, c.position, fwd);
+    norm(fwd);
+    cross(c.up, fwd, right);
+    norm(right);
+    cross(fwd, right, upv);
+    for (int i = 0; i < 3; ++i) {
+        out.x[i] = hlen * right[i];
+        out.y[i] = vlen * upv[i];
+        out.z[i] = fwd[i];
+        out.position[i] = c.position[i];
+    }
+    out.width = c.width;
+    out.height = c.height;
+}
+
+}  // namespace sel

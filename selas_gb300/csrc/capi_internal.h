@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include "scene_types.h"
 #include "sel_internal.h"
 
 struct SelDeviceTy {
@@ -26,11 +27,27 @@ struct SelSceneTy {
     SelSceneInfo info{};
     void* scratch = nullptr;  // staging buffer of the host-memory query forms
     size_t scratch_bytes = 0;
+
+    // shading data (materials indexed by geomID, quad-light sets, background) and its HBM copies
+    std::vector<sel::MaterialDev> materials;
+    std::vector<std::vector<sel::QuadLight>> light_sets;
+    float background[3] = {1.0f, 1.0f, 1.0f};  // backgroundIntensity default (CSceneBuildProcessor.cpp:59)
+    bool shading_dirty = true;
+    void* d_materials = nullptr;
+    void* d_lights = nullptr;
+    void* d_light_sets = nullptr;
+    // path-tracer scratch: path state for `pt_capacity` paths and the FP64 accumulator
+    void* pt_block = nullptr;
+    uint32_t pt_capacity = 0;
+    void* d_accum = nullptr;
+    size_t accum_bytes = 0;
     std::mutex mu;
 };
 
 namespace sel {
 struct DeviceBvh;
+struct PtCamera;
+void init_camera(const SelCamera& c, PtCamera& out);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 int set_device(SelDeviceTy* dev);

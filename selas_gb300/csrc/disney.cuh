@@ -8,7 +8,8 @@
 //   * the scalar Schlick term is Lerp(1, SchlickWeight(cos), r0) (Fresnel.cpp:26-29);
 //   * the lobe after diffuse is always specular transmission (Disney.cpp:639-642);
 //   * spec-transmission and diffuse sampling do not renormalise the tangent-space view vector
-//     (Disney.cpp:349, 464) while the other paths do.
+//     (Disney.cpp:349, 464) while the other paths do;
+//   * the medium extinction is s * scatterDistance (see extinction() below).
 // Tangent space is y-up: (t, n, b) = (x, y, z) (MathLib/Trigonometric.h:49-108).
 #pragma once
 
@@ -243,9 +244,11 @@ SEL_HD float diffuse_eval(const Surface& s, float3 wo, float3 wm, float3 wi, boo
     const float ss = lerpf(1.0f, hk, thin ? s.flatness : 0.0f);
     return kInvPi * (retro + ss * (1.0f - 0.5f * fl) * (1.0f - 0.5f * fv));
 }
+// CalculateExtinction (Disney.cpp:337-343) writes 1.0f / (s * d), but the reference's operator/(float,
+// float3) returns rhs / lhs (MathLib/FloatFuncs.h:147-151), so the value it produces is s * d.
 SEL_HD float3 extinction(float3 a, float dist) {
     const float3 s = f3(1.9f) - a + 3.5f * (a - f3(0.8f)) * (a - f3(0.8f));
-    return f3(1.0f) / (s * dist);
+    return s * dist;
 }
 
 // EvaluateDisney (Disney.cpp:525-614); v = toward the viewer, l = toward the light, world space.

@@ -1,0 +1,402 @@
+// Wavefront unidirectional path tracer: the GB300 form of PathTracer::GenerateImage / EvaluatePath
+// (Source/Applications/Selas/Source/PathTracer.cpp:142-258, 261-349).
+//
+// Per batch of paths: generate -> for each bounce: extend (closest hit) -> shade (surface setup, quad-light
+// NEE, BSDF sampling, Russian roulette) -> shadow (any hit).  Queues hold path slots; appends are
+// warp-aggregated (one atomic per warp).  Contributions go straight into an FP64 per-pixel accumulator
+// (layer 0: first-bounce reflectance, layer 1: radiance, as the reference's two framebuffer layers), so
+// the path state carries no per-path radiance.  Every path draws from its own PCG32 stream (stream id =
+// global path index), consumed in the order the reference consumes its sampler: jitter x/y; per bounce
+// [distance in a medium: 2], light pick + 2 for the light, BSDF lobe + 2..3, [medium scatter: 2],
+// [Russian roulette after bounce 8: 1].
+#include "pt.h"
+
+#include <cstring>
+
+#include "capi_internal.h"
+#include "shading.cuh"
+#include "traverse.cuh"
+
+namespace sel {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr float kFloatMax = 3.402823466e+38f;  // FloatMax_ (SystemLib/BasicTypes.h:31)
+
+struct PtParams {
+    const uint4* nodes;
+    const float4* tris;
+    const MaterialDev* materials;
+    uint32_t material_count;
+    const QuadLight* lights;
+    const uint2* light_sets;  // (first light, count) per set
+    uint32_t light_set_count;
+    float3 background;
+    CameraDev cam;
+    uint32_t width, height;
+    uint64_t seed;
+    uint64_t first_path;
+    uint32_t batch;
+    uint32_t max_bounces;
+    double* accum;  // [2][height*width][3]
+    PtState st;
+    uint32_t* err;
+};
+
+// Warp-aggregated append: returns this lane's slot in a queue whose length lives at *count.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
+    const uint32_t mask = __ballot_sync(__activemask(), want);
+    if (!want) return 0xffffffffu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void accumulate(double* accum, uint32_t npix, int layer, uint32_t pixel, float3 c) {
+    double* p = accum + (size_t(layer) * npix + pixel) * 3;
+    atomicAdd(p, double(c.x));
+    atomicAdd(p + 1, double(c.y));
+    atomicAdd(p + 2, double(c.z));
+}
+
+__device__ __forceinline__ Pcg32 load_rng(const PtState& st, uint32_t slot) {
+    Pcg32 r;
+    r.state = st.rng[slot];
+    r.inc = (uint64_t(st.path_id[slot]) << 1u) | 1u;
+    return r;
+}
+
+__global__ void k_reset(uint32_t* counters, uint32_t first_queue_count) {
+    if (threadIdx.x < kPtCounters) counters[threadIdx.x] = threadIdx.x == 0 ? first_queue_count : 0u;
+}
+
+__global__ void k_bounce_reset(uint32_t* counters, int next) {
+    // next queue length, shadow queue length and both fetch cursors restart each bounce
+    if (threadIdx.x == 0) {
+        counters[next] = 0u;
+        counters[2] = 0u;
+        counters[3] = 0u;
+        counters[4] = 0u;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
+    const uint32_t npix = P.width * P.height;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.batch; s += gridDim.x * blockDim.x) {
+        const uint64_t path = P.first_path + s;
+        const uint32_t pixel = uint32_t(path % npix);
+        Pcg32 rng = pcg_seed(P.seed, path);
+        const uint32_t y = pixel / P.width, x = pixel - y * P.width;
+        const float vx = float(x) + pcg_float(rng);  // JitteredCameraRay (Camera.cpp:63-74)
+        const float vy = float(y) + pcg_float(rng);
+        const float3 d = camera_direction(P.cam, vx, vy);
+        P.st.ray_o[s] = make_float4(P.cam.position.x, P.cam.position.y, P.cam.position.z, 0.0f);
+        P.st.ray_d[s] = make_float4(d.x, d.y, d.z, kFloatMax);
+        P.st.thr[s] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // w = isDeltaOnly
+        P.st.medium[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // x = phase (0 vacuum, 1 isotropic)
+        P.st.pixel[s] = pixel;
+        P.st.path_id[s] = uint32_t(path);
+        P.st.rng[s] = rng.state;
+        P.st.queue[0][s] = s;
+    }
+}
+
+// Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
+// so expensive and cheap rays balance across the GPU.
+__global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
+    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    const uint32_t n = P.st.counters[cur];
+    const uint32_t* queue = P.st.queue[cur];
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if ((threadIdx.x & 31u) == 0) base = atomicAdd(&P.st.counters[3], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t e = base + (threadIdx.x & 31u);
+        if (e < n) {
+            const uint32_t s = queue[e];
+            const float4 o = P.st.ray_o[s], d = P.st.ray_d[s];
+            const float4 med = P.st.medium[s];
+            float tfar = kFloatMax;
+            if (med.x != 0.0f) {
+                // Isotropic::SampleDistance (Shading/IsotropicScattering.cpp:18-47)
+                Pcg32 rng = load_rng(P.st, s);
+                const float ps = med.y + med.z + med.w;
+                const float pr = med.y / ps, pg = med.z / ps, pb = med.w / ps;
+                float c, p;
+                const float r0 = pcg_float(rng);
+                if (r0 < pr) { c = med.y; p = pr; }
+                else if (r0 < pr + pg) { c = med.z; p = pg; }
+                else { c = med.w; p = pb; }
+                (void)p;
+                tfar = -logf(pcg_float(rng)) / c;
+                P.st.rng[s] = rng.state;
+            }
+            QueryRay q;
+            q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
+            q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = tfar;
+            QueryHit h;
+            const bool found = trace_wide<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status);
+            P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+        }
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+__global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce) {
+    const uint32_t n = P.st.counters[cur];
+    const uint32_t npix = P.width * P.height;
+    const int next = cur ^ 1;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        bool cont = false, shadow = false;
+        uint32_t s = 0;
+        float4 sh_o = make_float4(0, 0, 0, 0), sh_d = sh_o, sh_c = sh_o;
+        if (valid) {
+            s = P.st.queue[cur][e];
+            const float4 o4 = P.st.ray_o[s], d4 = P.st.ray_d[s];
+            const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
+            float4 thr4 = P.st.thr[s];
+            float3 thr = f3(thr4.x, thr4.y, thr4.z);
+            float4 med = P.st.medium[s];
+            const float4 hit = P.st.hit[s];
+            const uint32_t tri = __float_as_uint(hit.w);
+            const uint32_t pixel = P.st.pixel[s];
+            Pcg32 rng = load_rng(P.st, s);
+            float ray_distance = hit.x;
+            float3 pos = f3(0.0f);
+            if (tri != 0xffffffffu) {
+                pos = f3(o.x + hit.x * d.x, o.y + hit.x * d.y, o.z + hit.x * d.z);
+                ray_distance = length(pos - o);
+            }
+            if (med.x != 0.0f) {  // Isotropic::Transmission
+                thr = thr * f3(expf(-med.y * ray_distance), expf(-med.z * ray_distance), expf(-med.w * ray_distance));
+            }
+            bool alive = true;
+            if (tri != 0xffffffffu) {
+                const float4* tp = P.tris + size_t(tri) * 3;
+                const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                const float3 ng = triangle_ng(p0, p1, p2);
+                const uint32_t geom = __float_as_uint(p1.w);
+                const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+                // RayPick error bound (PathTracer.cpp:134-136)
+                const float err = 32.0f * 1.19209e-07f *
+                                  fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
+                const Surface sf = make_surface(m, ng, -d, ld3(m.base_color));
+                // Next-event estimation to the surface's light set (AreaLighting.cpp:353-373)
+                LightSample ls;
+                ls.radiance = f3(0.0f);
+                if (m.light_set < P.light_set_count) {
+                    const uint2 set = P.light_sets[m.light_set];
+                    if (set.y > 0) {
+                        const float p0u = pcg_float(rng);
+                        uint32_t li = uint32_t(p0u * float(set.y));
+                        li = li < set.y ? li : set.y - 1;
+                        const float u = pcg_float(rng), v = pcg_float(rng);
+                        sample_quad_light(P.lights[set.x + li], pos, sf.n, u, v, ls);
+                        ls.pdf *= 1.0f / float(set.y);
+                    }
+                }
+                if (dot(ls.radiance, f3(1.0f)) > 0.0f) {
+                    float fpdf, rpdf;
+                    const float3 refl = bsdf_evaluate(sf, -d, ls.direction, fpdf, rpdf);
+                    if (dot(refl, f3(1.0f)) > 0.0f) {
+                        // OcclusionRay (PathTracer.cpp:71-92): origin offset 0.1 * error, tnear = error
+                        const float3 so = offset_origin(pos, sf.n, err, ls.direction, 0.1f);
+                        const float3 c = refl * ls.radiance * (1.0f / ls.pdf) * thr;
+                        sh_o = make_float4(so.x, so.y, so.z, err);
+                        sh_d = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.distance);
+                        sh_c = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
+                        shadow = true;
+                    }
+                }
+                // BSDF sampling: draw ahead from a copy of the stream, then advance by what was used
+                float u4[4];
+                Pcg32 ahead = rng;
+                for (int k = 0; k < 4; ++k) u4[k] = pcg_float(ahead);
+                int used = 0;
+                BsdfSampleOut bs;
+                const bool ok = bsdf_sample(sf, -d, u4, used, bs);
+                for (int k = 0; k < used; ++k) pcg_next(rng);
+                if (!ok) {
+                    alive = false;
+                } else {
+                    if (!(bs.flags & kDiracEvent)) thr4.w = 0.0f;
+                    if (bs.flags == kTransmissionEvent) {
+                        if (med.x == 0.0f) med = make_float4(float(bs.medium_phase), bs.extinction.x, bs.extinction.y, bs.extinction.z);
+                        else med = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    }
+                    thr = 1.0f * thr * bs.reflectance;
+                    const float3 no = offset_origin(pos, sf.n, err, bs.wi, 1.0f);
+                    P.st.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
+                    P.st.ray_d[s] = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, kFloatMax);
+                    if (bounce == 0) accumulate(P.accum, npix, 0, pixel, bs.reflectance);
+                }
+            } else if (med.x != 0.0f) {
+                // scatter inside the medium: Isotropic::SampleScatterDirection -> CSampler::UniformSphere
+                const float3 no = o + ray_distance * d;
+                const float r0 = pcg_float(rng), r1 = pcg_float(rng);
+                const float uu = 2.0f * r1 - 1.0f;
+                const float nn = sqrtf(fmaxf(0.0f, 1.0f - uu * uu));
+                const float th = kTwoPi * r0;
+                const float3 nd = f3(nn * cosf(th), uu, nn * sinf(th));
+                P.st.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
+                P.st.ray_d[s] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
+            } else {
+                // miss: background (EvaluateBackground / EvaluateBackgroundMiss without an IBL)
+                accumulate(P.accum, npix, 1, pixel, P.background * thr);
+                alive = false;
+            }
+            if (alive) {
+                const uint32_t nb = bounce + 1;
+                if (nb > 8) {  // Russian roulette (PathTracer.cpp:248-254)
+                    const float cp = fmaxf(fmaxf(thr.x, thr.y), thr.z);
+                    if (pcg_float(rng) > cp) alive = false;
+                    else thr = thr * (1.0f / cp);
+                }
+                cont = alive && nb < P.max_bounces;
+            }
+            P.st.thr[s] = make_float4(thr.x, thr.y, thr.z, thr4.w);
+            P.st.medium[s] = med;
+            P.st.rng[s] = rng.state;
+        }
+        const uint32_t qslot = warp_append(&P.st.counters[next], cont);
+        if (cont) P.st.queue[next][qslot] = s;
+        const uint32_t sslot = warp_append(&P.st.counters[2], shadow);
+        if (shadow) {
+            P.st.sh_o[sslot] = sh_o;
+            P.st.sh_d[sslot] = sh_d;
+            P.st.sh_c[sslot] = sh_c;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
+    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    const uint32_t n = P.st.counters[2];
+    const uint32_t npix = P.width * P.height;
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if ((threadIdx.x & 31u) == 0) base = atomicAdd(&P.st.counters[4], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t e = base + (threadIdx.x & 31u);
+        if (e < n) {
+            const float4 o = P.st.sh_o[e], d = P.st.sh_d[e];
+            QueryRay q;
+            q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
+            q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
+            QueryHit h;
+            if (!trace_wide<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status)) {
+                const float4 c = P.st.sh_c[e];
+                accumulate(P.accum, npix, 1, __float_as_uint(c.w), f3(c.x, c.y, c.z));
+            }
+        }
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+__global__ void k_resolve(const double* accum, uint32_t count, double scale, float* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        out[i] = float(accum[i] * scale);
+}
+
+int grid_for(int sm_count, int blocks_per_sm) { return sm_count * blocks_per_sm; }
+
+}  // namespace
+
+// Carves the path state of `paths` slots out of one device block (the caller owns the block).
+PtState pt_state_carve(void* block, uint32_t paths) {
+    char* p = static_cast<char*>(block);
+    PtState st;
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    st.ray_o = reinterpret_cast<float4*>(take(16ull * paths));
+    st.ray_d = reinterpret_cast<float4*>(take(16ull * paths));
+    st.thr = reinterpret_cast<float4*>(take(16ull * paths));
+    st.medium = reinterpret_cast<float4*>(take(16ull * paths));
+    st.hit = reinterpret_cast<float4*>(take(16ull * paths));
+    st.pixel = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.path_id = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.rng = reinterpret_cast<uint64_t*>(take(8ull * paths));
+    st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.sh_o = reinterpret_cast<float4*>(take(16ull * paths));
+    st.sh_d = reinterpret_cast<float4*>(take(16ull * paths));
+    st.sh_c = reinterpret_cast<float4*>(take(16ull * paths));
+    st.counters = reinterpret_cast<uint32_t*>(take(64 * sizeof(uint32_t)));
+    st.capacity = paths;
+    return st;
+}
+
+size_t pt_state_block_bytes(uint32_t paths) {
+    // each carve is rounded up to 256 bytes
+    auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
+    return r(16ull * paths) * 9 + r(4ull * paths) * 4 + r(8ull * paths) + r(64 * sizeof(uint32_t));
+}
+
+cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
+                      uint32_t* d_err, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    PtParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.nodes = sc.nodes;
+    P.tris = sc.tris;
+    P.materials = sc.materials;
+    P.material_count = sc.material_count;
+    P.lights = sc.lights;
+    P.light_sets = sc.light_sets;
+    P.light_set_count = sc.light_set_count;
+    P.background = make_float3(sc.background[0], sc.background[1], sc.background[2]);
+    P.cam.x = make_float3(cam.x[0], cam.x[1], cam.x[2]);
+    P.cam.y = make_float3(cam.y[0], cam.y[1], cam.y[2]);
+    P.cam.z = make_float3(cam.z[0], cam.z[1], cam.z[2]);
+    P.cam.position = make_float3(cam.position[0], cam.position[1], cam.position[2]);
+    P.cam.width = float(cam.width);
+    P.cam.height = float(cam.height);
+    P.width = cam.width;
+    P.height = cam.height;
+    P.seed = set.seed;
+    P.max_bounces = set.max_bounces;
+    P.accum = d_accum;
+    P.st = st;
+    P.err = d_err;
+    const uint64_t total = uint64_t(cam.width) * cam.height * set.spp;
+    const int trace_grid = grid_for(sms, 8);
+    const int shade_grid = grid_for(sms, 8);
+    for (uint64_t first = 0; first < total; first += st.capacity) {
+        const uint32_t batch = uint32_t(total - first < st.capacity ? total - first : st.capacity);
+        P.first_path = first;
+        P.batch = batch;
+        k_reset<<<1, 32, 0, stream>>>(st.counters, batch);
+        k_generate<<<(batch + kBlock - 1) / kBlock, kBlock, 0, stream>>>(P);
+        for (uint32_t b = 0; b < set.max_bounces; ++b) {
+            const int cur = int(b & 1u);
+            k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
+            k_extend<<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            k_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur, b);
+            k_shadow<<<trace_grid, kBlock, 0, stream>>>(P);
+        }
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {
+    k_resolve<<<1024, 256, 0, stream>>>(d_accum, values, scale, d_out);
+    return cudaGetLastError();
+}
+
+}  // namespace sel

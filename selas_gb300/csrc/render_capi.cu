@@ -1,0 +1,232 @@
+// C ABI of the scene shading data and of the path-tracer entry points (include/selas.h).
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "capi_internal.h"
+#include "pt.h"
+
+using namespace sel;
+
+namespace {
+
+constexpr uint32_t kMaxGeom = 65536;
+constexpr uint32_t kDefaultPathsInFlight = 1u << 22;
+
+MaterialDev to_device(const SelMaterial& m) {
+    MaterialDev d;
+    std::memset(&d, 0, sizeof(d));
+    d.shader = m.shader;
+    d.light_set = m.lightSetIndex;
+    for (int i = 0; i < 3; ++i) {
+        d.base_color[i] = m.baseColor[i];
+        d.transmittance_color[i] = m.transmittanceColor[i];
+    }
+    d.metallic = m.metallic;
+    d.specular_tint = m.specularTint;
+    d.roughness = m.roughness;
+    d.anisotropic = m.anisotropic;
+    d.sheen = m.sheen;
+    d.sheen_tint = m.sheenTint;
+    d.clearcoat = m.clearcoat;
+    d.clearcoat_gloss = m.clearcoatGloss;
+    d.spec_trans = m.specTrans;
+    d.diffuse_trans = m.diffuseTrans;
+    d.flatness = m.flatness;
+    d.ior = m.ior;
+    d.scatter_distance = m.scatterDistance;
+    if (m.shader == SEL_SHADER_DISNEY_SOLID && (m.diffuseTrans > 0.0f || m.specTrans > 0.0f))
+        d.flags |= kMaterialTransparent;
+    if (m.usesPtex) d.flags |= kMaterialUsesPtex;
+    return d;
+}
+
+SelMaterial default_material() {
+    SelMaterial m;
+    std::memset(&m, 0, sizeof(m));
+    m.shader = SEL_SHADER_DISNEY_SOLID;
+    m.baseColor[0] = m.baseColor[1] = m.baseColor[2] = 0.6f;
+    m.ior = 1.5f;
+    return m;
+}
+
+template <typename T>
+int upload(void*& dst, const T* src, size_t count) {
+    if (dst) cudaFree(dst);
+    dst = nullptr;
+    const size_t bytes = count ? count * sizeof(T) : sizeof(T);
+    cudaError_t e = cudaMalloc(&dst, bytes);
+    if (e == cudaSuccess && count) e = cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? SEL_OK : cuda_fail(e, "uploading shading data");
+}
+
+int sync_shading(SelSceneTy* sc) {
+    if (!sc->shading_dirty) return SEL_OK;
+    uint32_t max_geom = 0;
+    for (const MeshInput& m : sc->meshes) max_geom = m.geomID + 1 > max_geom ? m.geomID + 1 : max_geom;
+    if (max_geom > kMaxGeom) return fail(SEL_ERR_INVALID_OPERATION, "rendering needs geomIDs below 65536");
+    std::vector<MaterialDev> mats(max_geom ? max_geom : 1, to_device(default_material()));
+    for (size_t i = 0; i < sc->materials.size() && i < mats.size(); ++i)
+        if (sc->materials[i].shader >= 0) mats[i] = sc->materials[i];
+    std::vector<QuadLight> lights;
+    std::vector<uint2> sets;
+    for (const auto& set : sc->light_sets) {
+        sets.push_back(make_uint2(uint32_t(lights.size()), uint32_t(set.size())));
+        lights.insert(lights.end(), set.begin(), set.end());
+    }
+    if (int rc = upload(sc->d_materials, mats.data(), mats.size())) return rc;
+    if (int rc = upload(sc->d_lights, lights.data(), lights.size())) return rc;
+    if (int rc = upload(sc->d_light_sets, sets.data(), sets.size())) return rc;
+    sc->shading_dirty = false;
+    return SEL_OK;
+}
+
+int ensure_pt_state(SelSceneTy* sc, uint32_t paths) {
+    if (sc->pt_block && sc->pt_capacity == paths) return SEL_OK;
+    if (sc->pt_block) cudaFree(sc->pt_block);
+    sc->pt_block = nullptr;
+    sc->pt_capacity = 0;
+    cudaError_t e = cudaMalloc(&sc->pt_block, pt_state_block_bytes(paths));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(path state)");
+    sc->pt_capacity = paths;
+    return SEL_OK;
+}
+
+int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings) {
+    if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    if (scene->info.bvh_kind != SEL_BVH_WIDE8_Q8)
+        return fail(SEL_ERR_INVALID_OPERATION, "the renderer traverses the 8-wide BVH: commit with SEL_BVH_WIDE8_Q8");
+    if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
+    if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "fovDegrees must lie in (0, 180)");
+    if (settings->samplesPerPixel == 0) return fail(SEL_ERR_INVALID_ARGUMENT, "samplesPerPixel must be > 0");
+    const uint64_t total = uint64_t(camera->width) * camera->height * settings->samplesPerPixel;
+    if (total >= (uint64_t(1) << 32)) return fail(SEL_ERR_INVALID_ARGUMENT, "width * height * spp must be < 2^32");
+    return SEL_OK;
+}
+
+int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& settings, double* d_accum,
+                  cudaStream_t stream) {
+    if (int rc = sync_shading(sc)) return rc;
+    const uint64_t total = uint64_t(camera.width) * camera.height * settings.samplesPerPixel;
+    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight : kDefaultPathsInFlight;
+    if (uint64_t(cap) > total) cap = uint32_t(total);
+    if (int rc = ensure_pt_state(sc, cap)) return rc;
+    PtScene ps;
+    ps.nodes = static_cast<const uint4*>(sc->d_nodes);
+    ps.tris = static_cast<const float4*>(sc->d_tris);
+    ps.materials = static_cast<const MaterialDev*>(sc->d_materials);
+    uint32_t max_geom = 0;
+    for (const MeshInput& m : sc->meshes) max_geom = m.geomID + 1 > max_geom ? m.geomID + 1 : max_geom;
+    ps.material_count = max_geom ? max_geom : 1;
+    ps.lights = static_cast<const QuadLight*>(sc->d_lights);
+    ps.light_sets = static_cast<const uint2*>(sc->d_light_sets);
+    ps.light_set_count = uint32_t(sc->light_sets.size());
+    for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
+    PtCamera cam;
+    init_camera(camera, cam);
+    PtSettings set;
+    set.spp = settings.samplesPerPixel;
+    set.max_bounces = settings.maxBounces;
+    set.seed = settings.seed;
+    const PtState st = pt_state_carve(sc->pt_block, cap);
+    cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream);
+    return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int sel_material_defaults(SelMaterial* out) {
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    *out = default_material();
+    return SEL_OK;
+}
+
+int sel_scene_set_material(SelScene scene, unsigned int geomID, const SelMaterial* material) {
+    if (!scene || !material) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
+    if (material->shader < SEL_SHADER_DISNEY_THIN || material->shader > SEL_SHADER_DIRAC_TRANSPARENT)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "unknown shader");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (scene->materials.size() <= geomID) {
+        MaterialDev unset;
+        std::memset(&unset, 0, sizeof(unset));
+        unset.shader = -1;
+        scene->materials.resize(geomID + 1, unset);
+    }
+    scene->materials[geomID] = to_device(*material);
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const SelQuadLight* light) {
+    if (!scene || !light) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (lightSetIndex >= 4096) return fail(SEL_ERR_INVALID_ARGUMENT, "lightSetIndex must be below 4096");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (scene->light_sets.size() <= lightSetIndex) scene->light_sets.resize(lightSetIndex + 1);
+    QuadLight q;
+    q.position = make_float3(light->position[0], light->position[1], light->position[2]);
+    q.direction = make_float3(light->direction[0], light->direction[1], light->direction[2]);
+    q.x = make_float3(light->x[0], light->x[1], light->x[2]);
+    q.z = make_float3(light->z[0], light->z[1], light->z[2]);
+    q.radiance = make_float3(light->radiance[0], light->radiance[1], light->radiance[2]);
+    scene->light_sets[lightSetIndex].push_back(q);
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_set_background(SelScene scene, float r, float g, float b) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    scene->background[0] = r;
+    scene->background[1] = g;
+    scene->background[2] = b;
+    return SEL_OK;
+}
+
+int sel_pt_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
+                         void* stream) {
+    if (int rc = check_render_args(scene, camera, settings)) return rc;
+    if (!d_accum || (reinterpret_cast<uintptr_t>(d_accum) & 7u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_accum must be an 8-byte aligned device pointer");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    return render_device(scene, *camera, *settings, d_accum, static_cast<cudaStream_t>(stream));
+}
+
+int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, float* out_layers) {
+    if (int rc = check_render_args(scene, camera, settings)) return rc;
+    if (!out_layers) return fail(SEL_ERR_INVALID_ARGUMENT, "out_layers is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    SelDeviceTy* dev = scene->dev;
+    std::lock_guard<std::mutex> dlock(dev->mu);
+    cudaStream_t s = dev->stream;
+    const uint32_t values = 2u * camera->width * camera->height * 3u;
+    const size_t accum_bytes = size_t(values) * sizeof(double);
+    const size_t need = accum_bytes + size_t(values) * sizeof(float);
+    if (scene->accum_bytes < need) {
+        if (scene->d_accum) cudaFree(scene->d_accum);
+        scene->d_accum = nullptr;
+        scene->accum_bytes = 0;
+        cudaError_t e = cudaMalloc(&scene->d_accum, need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(accumulator)");
+        scene->accum_bytes = need;
+    }
+    double* acc = static_cast<double*>(scene->d_accum);
+    float* res = reinterpret_cast<float*>(static_cast<char*>(scene->d_accum) + accum_bytes);
+    cudaError_t e = cudaMemsetAsync(acc, 0, accum_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(accumulator)");
+    if (int rc = render_device(scene, *camera, *settings, acc, s)) return rc;
+    e = pt_resolve(acc, values, 1.0 / double(settings->samplesPerPixel), res, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_layers, res, size_t(values) * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "path tracer");
+    return read_error_word(dev, s);
+}
+
+}  // extern "C"

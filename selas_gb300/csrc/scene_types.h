@@ -1,0 +1,34 @@
+// Scene records shared by host set-up code and the render kernels (plain data, no device code).
+#pragma once
+
+#include <cstdint>
+
+#include <vector_types.h>
+
+namespace sel {
+
+// SceneLight as NextEventEstimation reads it (SceneLib/SceneResource.h; AreaLighting.cpp:113-153):
+// centre, facing direction, full edge vectors x and z, emitted radiance.
+struct QuadLight {
+    float3 position, direction, x, z, radiance;
+};
+
+// Per-geometry material record in HBM (128 bytes): the MaterialResourceData fields the shading reads
+// (SceneLib/ModelResource.h:68-88) plus the geometry's light set and Ptex face range.
+struct MaterialDev {
+    int shader;
+    uint32_t flags;      // kMaterialTransparent | kMaterialUsesPtex
+    uint32_t light_set;
+    uint32_t ptex_base;  // first face of this geometry in the packed Ptex face table
+    float base_color[3];
+    float transmittance_color[3];
+    float sheen, sheen_tint, clearcoat, clearcoat_gloss, metallic, spec_trans, diffuse_trans, flatness;
+    float anisotropic, specular_tint, roughness, scatter_distance, ior;
+    float pad[9];
+};
+static_assert(sizeof(MaterialDev) == 128, "MaterialDev must be 128 bytes");
+
+constexpr uint32_t kMaterialTransparent = 1u;  // DisneySolid with diffTrans or specTrans (BuildModel.cpp:60-65)
+constexpr uint32_t kMaterialUsesPtex = 2u;
+
+}  // namespace sel

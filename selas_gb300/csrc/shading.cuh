@@ -1,0 +1,189 @@
+// Device-side pieces of the path tracer around the BSDF: random numbers, the reference camera model,
+// quad-light next-event estimation and surface setup from a hit.
+#pragma once
+
+#include <cstdint>
+
+#include "disney.cuh"
+#include "scene_types.h"
+#include "vecmath.cuh"
+
+namespace sel {
+
+// ---------------------------------------------------------------------------------------------------
+// PCG32 (O'Neill 2014, "PCG: A family of simple fast space-efficient statistically good algorithms for
+// random number generation"): 64-bit LCG state, XSH-RR output; one stream per path.  Uniform floats are
+// the top 24 bits scaled to [0, 1).
+// ---------------------------------------------------------------------------------------------------
+struct Pcg32 {
+    uint64_t state, inc;
+};
+
+SEL_HD uint32_t pcg_next(Pcg32& r) {
+    const uint64_t old = r.state;
+    r.state = old * 6364136223846793005ull + r.inc;
+    const uint32_t xs = uint32_t(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = uint32_t(old >> 59u);
+    return (xs >> rot) | (xs << ((32u - rot) & 31u));
+}
+SEL_HD Pcg32 pcg_seed(uint64_t seed, uint64_t stream) {
+    Pcg32 r;
+    r.state = 0;
+    r.inc = (stream << 1u) | 1u;
+    pcg_next(r);
+    r.state += seed;
+    pcg_next(r);
+    return r;
+}
+SEL_HD float pcg_float(Pcg32& r) { return float(pcg_next(r) >> 8) * (1.0f / 16777216.0f); }
+
+// ---------------------------------------------------------------------------------------------------
+// Camera: RayCastCameraSettings (GeometryLib/Camera.h:24-42) and ImageToWorldDirection
+// (GeometryLib/Camera.cpp:56-60).
+// ---------------------------------------------------------------------------------------------------
+struct CameraDev {
+    float3 x, y, z, position;
+    float width, height;
+};
+
+SEL_HD float3 camera_direction(const CameraDev& c, float px, float py) {
+    const float cx = (px / c.width) * 2.0f - 1.0f;
+    const float cy = 1.0f - 2.0f * py / c.height;
+    return normalize(c.z - cx * c.x + cy * c.y);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Quad lights: SceneLight fields as NextEventEstimation reads them (Shading/AreaLighting.cpp:113-153,
+// 353-373) and the spherical-rectangle sampler of Urena, Fajardo and King (EGSR 2013) as restated in
+// GeometryLib/RectangulerLightSampler.cpp:17-97.
+// ---------------------------------------------------------------------------------------------------
+struct RectSampler {
+    float3 o, x, y, z;
+    float z0, z0sq, x0, y0, y0sq, x1, y1, y1sq, b0, b1, b0sq, k, S;
+};
+
+SEL_HD void rect_init(float3 s, float3 ex, float3 ey, float3 o, RectSampler& r) {
+    r.o = o;
+    const float exl = length(ex), eyl = length(ey);
+    r.x = ex * (1.0f / exl);
+    r.y = ey * (1.0f / eyl);
+    r.z = cross(r.x, r.y);
+    const float3 d = s - o;
+    r.z0 = dot(d, r.z);
+    if (r.z0 > 0.0f) {
+        r.z = -r.z;
+        r.z0 *= -1.0f;
+    }
+    r.z0sq = r.z0 * r.z0;
+    r.x0 = dot(d, r.x);
+    r.y0 = dot(d, r.y);
+    r.x1 = r.x0 + exl;
+    r.y1 = r.y0 + eyl;
+    r.y0sq = r.y0 * r.y0;
+    r.y1sq = r.y1 * r.y1;
+    const float3 v00 = f3(r.x0, r.y0, r.z0), v01 = f3(r.x0, r.y1, r.z0);
+    const float3 v10 = f3(r.x1, r.y0, r.z0), v11 = f3(r.x1, r.y1, r.z0);
+    const float3 n0 = normalize(cross(v00, v10)), n1 = normalize(cross(v10, v11));
+    const float3 n2 = normalize(cross(v11, v01)), n3 = normalize(cross(v01, v00));
+    const float g0 = acosf(-dot(n0, n1)), g1 = acosf(-dot(n1, n2));
+    const float g2 = acosf(-dot(n2, n3)), g3 = acosf(-dot(n3, n0));
+    r.b0 = n0.z;
+    r.b1 = n2.z;
+    r.b0sq = r.b0 * r.b0;
+    r.k = 2.0f * kPi - g2 - g3;
+    r.S = g0 + g1 - r.k;
+}
+
+SEL_HD float3 rect_sample(const RectSampler& r, float u, float v) {
+    const float au = u * r.S + r.k;
+    const float fu = (cosf(au) * r.b0 - r.b1) / sinf(au);
+    float cu = 1.0f / sqrtf(fu * fu + r.b0sq) * (fu > 0.0f ? 1.0f : -1.0f);
+    cu = clampf(cu, -1.0f, 1.0f);
+    float xu = -(cu * r.z0) / sqrtf(1.0f - cu * cu);
+    xu = clampf(xu, r.x0, r.x1);
+    const float d = sqrtf(xu * xu + r.z0sq);
+    const float h0 = r.y0 / sqrtf(d * d + r.y0sq);
+    const float h1 = r.y1 / sqrtf(d * d + r.y1sq);
+    const float hv = h0 + v * (h1 - h0), hv2 = hv * hv;
+    const float yv = (hv2 < 1.0f - 1e-10f) ? (hv * d) / sqrtf(1.0f - hv2) : r.y1;  // SmallFloatEpsilon_
+    return r.o + xu * r.x + yv * r.y + r.z0 * r.z;
+}
+
+struct LightSample {
+    float3 direction, radiance;
+    float distance, pdf;
+};
+
+// SampleRectangleLightSolidAngle (AreaLighting.cpp:113-153): radiance already carries cos(theta_light)/d^2
+// and cos(theta_surface) (as the reference computes it), pdf is (1/solid angle) * cos(theta_light)/d^2.
+SEL_HD void sample_quad_light(const QuadLight& L, float3 p, float3 n, float u, float v, LightSample& s) {
+    const float3 corner = L.position - 0.5f * L.x - 0.5f * L.z;
+    RectSampler r;
+    rect_init(corner, L.x, L.z, p, r);
+    const float pdf = 1.0f / r.S;
+    const float3 lp = rect_sample(r, u, v);
+    const float3 ul = lp - p;
+    const float d2 = dot(ul, ul);
+    const float d = sqrtf(d2);
+    const float3 l = (1.0f / d) * ul;
+    const float area = dot(L.direction, -l) / d2;
+    if (area > 0.0f) {
+        s.direction = l;
+        s.distance = d;
+        s.radiance = L.radiance * (area * dot(n, l));
+        s.pdf = pdf * area;
+    } else {
+        s.direction = f3(0.0f);
+        s.distance = 0.0f;
+        s.radiance = f3(0.0f);
+        s.pdf = 1.0f;
+    }
+}
+
+// MakeOrthogonalCoordinateSystem (GeometryLib/CoordinateSystem.h:14-21)
+SEL_HD void orthonormal_basis(float3 v1, float3& v2, float3& v3) {
+    if (fabsf(v1.x) > fabsf(v1.y))
+        v2 = f3(-v1.z, 0.0f, v1.x) * (1.0f / sqrtf(v1.x * v1.x + v1.z * v1.z));
+    else
+        v2 = f3(0.0f, v1.z, -v1.y) * (1.0f / sqrtf(v1.y * v1.y + v1.z * v1.z));
+    v3 = cross(v1, v2);
+}
+
+
+// CalculateSurfaceParams (Shading/SurfaceParameters.cpp:144-247) for meshes without shading normals,
+// tangents or uvs: frame from the normalised geometric normal, base colour raised to the power 2.2.
+SEL_HD Surface make_surface(const MaterialDev& m, float3 ng, float3 view, float3 base_color_authored) {
+    Surface s;
+    const float3 n = normalize(ng);
+    float3 t, b;
+    orthonormal_basis(n, t, b);
+    s.t = t;
+    s.n = n;
+    s.b = b;
+    s.base_color = pow3(base_color_authored, 2.2f);
+    s.transmittance_color = ld3(m.transmittance_color);
+    s.sheen = m.sheen;
+    s.sheen_tint = m.sheen_tint;
+    s.clearcoat = m.clearcoat;
+    s.clearcoat_gloss = m.clearcoat_gloss;
+    s.spec_trans = saturate(m.spec_trans);
+    s.diff_trans = m.diffuse_trans * 0.5f;
+    s.flatness = m.flatness;
+    s.anisotropic = m.anisotropic;
+    s.specular_tint = m.specular_tint;
+    s.roughness = m.roughness;
+    s.metallic = saturate(m.metallic);
+    s.scatter_distance = m.scatter_distance;
+    s.ior = m.ior;
+    s.shader = m.shader;
+    s.relative_ior = ((m.flags & kMaterialTransparent) && dot(view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
+    return s;
+}
+
+// OffsetRayOrigin (SurfaceParameters.cpp:403-408)
+SEL_HD float3 offset_origin(float3 p, float3 n, float error, float3 dir, float scale) {
+    const float side = dot(dir, n) < 0.0f ? -1.0f : 1.0f;
+    return p + (side * error * scale) * n;
+}
+
+}  // namespace sel

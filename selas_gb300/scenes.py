@@ -179,3 +179,111 @@ def ray_query_workload(level: int = 6, width: int = 2048, height: int = 2048, in
     n_inc = incoherent if incoherent is not None else width * height
     io, idir = surface_rays(scene, n_inc, seed=seed + 1)
     return scene, (co, cd), (io, idir)
+
+
+# ---------------------------------------------------------------------------------------------------
+# Render scenes: geometry + per-geometry materials + quad lights + camera
+# ---------------------------------------------------------------------------------------------------
+@dataclass
+class RenderScene:
+    geometry: TriangleScene
+    materials: dict = field(default_factory=dict)   # geomID -> dict of SelMaterial fields
+    lights: list = field(default_factory=list)      # (light set, dict(position, direction, x, z, radiance))
+    background: tuple = (0.0, 0.0, 0.0)
+    camera: dict = field(default_factory=dict)      # position, look_at, up, fov_degrees
+
+    def build(self, sel_module, device, bvh_kind=0):
+        """Creates and commits a selas_gb300 Scene with this content."""
+        sc = sel_module.Scene(device, bvh_kind)
+        self.geometry.attach_to(sc)
+        for gid, m in self.materials.items():
+            sc.set_material(gid, sel_module.material(**m))
+        for ls, l in self.lights:
+            sc.add_quad_light(ls, l["position"], l["direction"], l["x"], l["z"], l["radiance"])
+        sc.set_background(self.background)
+        sc.commit()
+        return sc
+
+    def sel_camera(self, sel_module, width, height):
+        c = self.camera
+        return sel_module.camera(c["position"], c["look_at"], c["up"], c["fov_degrees"], width, height)
+
+
+def _quad(p0, p1, p2, p3):
+    v = np.array([p0, p1, p2, p3], np.float32)
+    return v, np.array([[0, 1, 2], [0, 2, 3]], np.uint32)
+
+
+def _box(centre, size, angle_deg):
+    sx, sy, sz = size
+    c = np.array(centre, np.float64)
+    corners = np.array([[x, y, z] for y in (0.0, sy) for z in (-sz / 2, sz / 2) for x in (-sx / 2, sx / 2)])
+    a = np.deg2rad(angle_deg)
+    rot = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+    v = (corners @ rot.T) + np.array([c[0], 0.0, c[2]])
+    # corner index = 4*y + 2*z + x
+    faces = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    idx = []
+    for a_, b_, c_, d_ in faces:
+        idx += [[a_, b_, c_], [a_, c_, d_]]
+    return v.astype(np.float32), np.array(idx, np.uint32)
+
+
+def cornell_box(background=(0.0, 0.0, 0.0)) -> RenderScene:
+    """Cornell-style box: 5 axis-aligned quads of side 556, boxes 165 and 330 tall rotated -18 / +18
+    degrees about y, a 130 x 105 quad light of radiance (17, 12, 4) just under the ceiling (lights are not
+    geometry in the reference: NEE only).  Disney solid, roughness 0.5, metallic 0, ior 1.5, 34 triangles."""
+    s = 556.0
+    g = TriangleScene()
+    g.add(0, *_quad([0, 0, 0], [0, 0, s], [s, 0, s], [s, 0, 0]))          # floor (normal +y)
+    g.add(1, *_quad([0, s, 0], [s, s, 0], [s, s, s], [0, s, s]))          # ceiling (normal -y)
+    g.add(2, *_quad([0, 0, s], [0, s, s], [s, s, s], [s, 0, s]))          # back wall (normal -z)
+    g.add(3, *_quad([s, 0, 0], [s, 0, s], [s, s, s], [s, s, 0]))          # left wall, red (normal -x)
+    g.add(4, *_quad([0, 0, 0], [0, s, 0], [0, s, s], [0, 0, s]))          # right wall, green (normal +x)
+    g.add(5, *_box([185.0, 0.0, 169.0], (165.0, 165.0, 165.0), -18.0))   # short box
+    g.add(6, *_box([368.0, 0.0, 351.0], (165.0, 330.0, 165.0), 18.0))    # tall box
+    base = dict(shader=1, lightSetIndex=0, roughness=0.5, metallic=0.0, ior=1.5)
+    grey, red, green = (0.73, 0.73, 0.73), (0.65, 0.05, 0.05), (0.12, 0.45, 0.15)
+    mats = {gid: dict(base, baseColor=grey) for gid in (0, 1, 2, 5, 6)}
+    mats[3] = dict(base, baseColor=red)
+    mats[4] = dict(base, baseColor=green)
+    light = dict(position=(278.0, 554.0, 279.5), direction=(0.0, -1.0, 0.0), x=(130.0, 0.0, 0.0),
+                 z=(0.0, 0.0, 105.0), radiance=(17.0, 12.0, 4.0))
+    cam = dict(position=(278.0, 273.0, -800.0), look_at=(278.0, 273.0, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=39.3)
+    return RenderScene(g, mats, [(0, light)], tuple(background), cam)
+
+
+def material_records(materials: dict, count: int) -> np.ndarray:
+    """Per-geomID 32-word material records (the renderer's HBM layout) for the CPU oracle; geometries
+    without a material get the reference default (CreateDefaultMaterial, ModelResource.cpp:203-211)."""
+    recs = np.zeros((count, 32), np.float32)
+    words = recs.view(np.uint32)
+    defaults = dict(shader=1, lightSetIndex=0, baseColor=(0.6, 0.6, 0.6), transmittanceColor=(0, 0, 0), metallic=0.0,
+                    specularTint=0.0, roughness=0.0, anisotropic=0.0, sheen=0.0, sheenTint=0.0, clearcoat=0.0,
+                    clearcoatGloss=0.0, specTrans=0.0, diffuseTrans=0.0, flatness=0.0, ior=1.5, scatterDistance=0.0,
+                    usesPtex=0)
+    for gid in range(count):
+        m = dict(defaults, **materials.get(gid, {}))
+        transparent = m["shader"] == 1 and (m["diffuseTrans"] > 0 or m["specTrans"] > 0)
+        words[gid, 0] = np.uint32(np.int32(m["shader"]).view(np.uint32))
+        words[gid, 1] = (1 if transparent else 0) | (2 if m["usesPtex"] else 0)
+        words[gid, 2] = m["lightSetIndex"]
+        recs[gid, 4:7] = m["baseColor"]
+        recs[gid, 7:10] = m["transmittanceColor"]
+        for i, k in enumerate(("sheen", "sheenTint", "clearcoat", "clearcoatGloss", "metallic", "specTrans",
+                               "diffuseTrans", "flatness", "anisotropic", "specularTint", "roughness",
+                               "scatterDistance", "ior")):
+            recs[gid, 10 + i] = m[k]
+    return recs
+
+
+def light_records(lights: list):
+    """(lights n x 15 floats, sets n_sets x 2 (first, count)) grouped by light set."""
+    n_sets = 1 + max((ls for ls, _ in lights), default=-1)
+    grouped = [[l for ls, l in lights if ls == k] for k in range(n_sets)]
+    flat, sets = [], []
+    for group in grouped:
+        sets.append((len(flat), len(group)))
+        for l in group:
+            flat.append(list(l["position"]) + list(l["direction"]) + list(l["x"]) + list(l["z"]) + list(l["radiance"]))
+    return (np.array(flat, np.float32).reshape(-1, 15), np.array(sets, np.uint32).reshape(-1, 2))

@@ -8,6 +8,9 @@ by oracle/ref/build_ref.py):
 bsdf_golden.npz  - seeded (surface, wo, wi) tuples -> EvaluateBsdf (f, forwardPdfW, reversePdfW) and
                    seeded (surface, wo, 4 uniforms) tuples -> SampleBsdfFunction results, computed by
                    Source/Core/Shading/SurfaceScattering.cpp:18-60 -> Disney.cpp / DiracTransparent.cpp.
+cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
+                   from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp); the image the
+                   path tracers' rMSE is measured against.  Needs only the oracle (python ... cornell).
 """
 from __future__ import annotations
 
@@ -109,5 +112,22 @@ def make_bsdf(n_eval=3000, n_sample=3000, seed=0x5E1A5B5D):
           "nonzero f:", int((out_e[:, :3].sum(1) > 0).sum()), "successful samples:", int(out_s[:, 0].sum()))
 
 
+def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
+    import oracle
+    from selas_gb300 import scenes
+    rs = scenes.cornell_box()
+    img = np.zeros((2, size, size, 3), np.float64)
+    step = 256
+    for p in range(0, spp, step):
+        img += oracle.pt_render(rs, size, size, p, min(spp, p + step), max_bounces=8, seed=seed, rng="mt")
+    img /= spp
+    np.savez_compressed(OUT / "cornell_64_ref.npz", image=img.astype(np.float32), spp=spp, seed=seed)
+    print("cornell_64_ref.npz: mean radiance", img[1].mean(axis=(0, 1)))
+
+
 if __name__ == "__main__":
-    make_bsdf()
+    what = sys.argv[1:] or ["bsdf", "cornell"]
+    if "bsdf" in what:
+        make_bsdf()
+    if "cornell" in what:
+        make_cornell()
