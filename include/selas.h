@@ -215,6 +215,34 @@ int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const S
 int sel_scene_set_background(SelScene scene, float r, float g, float b);
 
 /* ------------------------------------------------------------------------------------------------ */
+/* Ptex per-face textures.                                                                           */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* One triangle face of a Ptex texture (Ptex FaceInfo, Middleware/ptex/Include/Ptexture.h:228-300):
+ * square resolution 2^log2 (all faces of a mesh share it), offset of its texels in the texel array (in
+ * texels), neighbouring face across edge i (edge i runs from vertex i to vertex i+1; -1 = boundary) and
+ * the neighbour's edge id for that edge.  32 bytes. */
+typedef struct SelPtexFace {
+    int32_t log2;
+    uint32_t offset;
+    int32_t adjfaces[3];
+    int32_t adjedges[3];
+} SelPtexFace;
+
+/* PtexFilter::getFilter(f_bspline) + eval on a triangle texture as CalculateSurfaceParams calls it
+ * (Source/Core/Shading/SurfaceParameters.cpp:196-206: faceid = primId, u/v = barycentrics, widths 0):
+ * d_texels holds half-float RGB texels, d_queries n x (face id as int32 bits, u, v), d_out n x 3 floats
+ * (rows of invalid face ids are left untouched).  Device memory, asynchronous on `stream`. */
+int sel_ptex_filter_device(SelDevice device, const SelPtexFace* d_faces, unsigned int nfaces, const uint16_t* d_texels,
+                           const float* d_queries, unsigned int n, float* d_out, void* stream);
+
+/* Binds a Ptex texture to geometry geomID (replaces TextureCache::FetchPtex of the per-mesh .ptx,
+ * Source/Core/TextureLib/TextureCache.cpp:168-185): face_count must equal the geometry's triangle count;
+ * materials with usesPtex take their base colour from it.  Host arrays, copied. */
+int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* faces, size_t face_count,
+                       const uint16_t* texels, size_t texel_count);
+
+/* ------------------------------------------------------------------------------------------------ */
 /* Integrator entry points.                                                                          */
 /* ------------------------------------------------------------------------------------------------ */
 

@@ -32,9 +32,10 @@ def lib() -> ctypes.CDLL:
             "oracle_occluded_bvh": ([_vp, _vp, _i64, _i], None),
             "oracle_bsdf_evaluate": ([_vp, _vp, _vp, _i64, _vp], None),
             "oracle_bsdf_sample": ([_vp, _vp, _vp, _i64, _vp], None),
+            "oracle_ptex_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
             "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
-                                  ctypes.c_uint64, _i, _i, _vp], None),
+                                  ctypes.c_uint64, _i, _i, _vp, _i, _vp, _vp], None),
         }
         for name, (args, res) in sig.items():
             fn = getattr(_lib, name)
@@ -112,6 +113,7 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
     from selas_gb300.scenes import light_records, material_records
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    rows, texels = render_scene.ptex_tables(mats)
     lights, sets = light_records(render_scene.lights)
     bg = np.array(render_scene.background, np.float32)
     c = render_scene.camera
@@ -120,5 +122,16 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
     L = lib()
     L.oracle_pt_render(_p(verts), _p(prim), _p(geom), verts.shape[0], _p(mats), mats.shape[0], _p(lights),
                        lights.shape[0], _p(sets), sets.shape[0], _p(bg), _p(cam), width, height, pass_begin, pass_end,
-                       max_bounces, seed, 0 if rng == "pcg" else 1, nthreads or threads(), _p(out))
+                       max_bounces, seed, 0 if rng == "pcg" else 1, nthreads or threads(), _p(rows), rows.shape[0],
+                       _p(texels), _p(out))
+    return out
+
+
+def ptex_eval(faces, texels_u16, queries):
+    """Oracle Ptex triangle filter (oracle_ptex.cpp): queries (n, 3) = (face bits, u, v) -> (n, 3)."""
+    faces = np.ascontiguousarray(faces, np.int32)
+    texels_u16 = np.ascontiguousarray(texels_u16, np.uint16)
+    queries = np.ascontiguousarray(queries, np.float32)
+    out = np.zeros((queries.shape[0], 3), np.float32)
+    lib().oracle_ptex_eval(_p(faces), faces.shape[0], _p(texels_u16), _p(queries), queries.shape[0], _p(out))
     return out

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "oracle_bsdf.h"
+#include "oracle_ptex.h"
 #include "oracle_query.h"
 
 using orc::V3;
@@ -89,7 +90,7 @@ struct Light {
 
 struct Material {
     int shader;
-    uint32_t flags, light_set;
+    uint32_t flags, light_set, ptex_base;
     float base[3], trans[3];
     float sheen, sheenTint, clearcoat, clearcoatGloss, metallic, specTrans, diffTrans, flatness;
     float anisotropic, specularTint, roughness, scatterDistance, ior;
@@ -105,6 +106,7 @@ Material read_material(const float* r) {
     m.shader = sh;
     m.flags = fl;
     m.light_set = ls;
+    std::memcpy(&m.ptex_base, r + 3, 4);
     for (int i = 0; i < 3; ++i) { m.base[i] = r[4 + i]; m.trans[i] = r[7 + i]; }
     m.sheen = r[10]; m.sheenTint = r[11]; m.clearcoat = r[12]; m.clearcoatGloss = r[13];
     m.metallic = r[14]; m.specTrans = r[15]; m.diffTrans = r[16]; m.flatness = r[17];
@@ -166,6 +168,7 @@ void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad
 
 struct Scene {
     const void* bvh;
+    const orp::Texture* ptex = nullptr;
     std::vector<Material> materials;
     std::vector<Light> lights;
     std::vector<uint32_t> set_first, set_count;
@@ -219,7 +222,9 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
             else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
             b = orc::Cross(n, t);
             s.t = t; s.n = n; s.b = b;
-            s.baseColor = V3(std::pow(m.base[0], 2.2f), std::pow(m.base[1], 2.2f), std::pow(m.base[2], 2.2f));
+            float base[3] = {m.base[0], m.base[1], m.base[2]};
+            if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+            s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
             s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
             s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
             s.specTrans = Sat(m.specTrans); s.diffTrans = m.diffTrans * 0.5f; s.flatness = m.flatness;
@@ -291,15 +296,20 @@ extern "C" {
 
 // verts/prim/geom: triangle soup; materials: n_materials x 32 words (MaterialDev layout, indexed by geomID);
 // lights: n_lights x 15 floats (position, direction, x, z, radiance); sets: n_sets x 2 (first, count);
-// camera: position[3] lookAt[3] up[3] fovDegrees; out: [2][height][width][3] doubles (sums over the paths
-// of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the GPU); 1: MT19937 per pixel.
+// camera: position[3] lookAt[3] up[3] fovDegrees; ptex_rows/ptex_texels: the combined Ptex face table of
+// all textured geometries (material word 3 = that geometry's first face); out: [2][height][width][3]
+// doubles (sums over the paths of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the
+// GPU); 1: MT19937 per pixel.
 void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
                       const float* materials, int n_materials, const float* lights, int n_lights,
                       const uint32_t* sets, int n_sets, const float* background, const float* camera,
                       uint32_t width, uint32_t height, uint32_t pass_begin, uint32_t pass_end, uint32_t max_bounces,
-                      uint64_t seed, int rng_mode, int threads, double* out) {
+                      uint64_t seed, int rng_mode, int threads, const int32_t* ptex_rows, int ptex_faces,
+                      const uint16_t* ptex_texels, double* out) {
     Scene sc;
     sc.bvh = orq::build(verts, prim, geom, ntri);
+    orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
+    sc.ptex = tex;
     for (int i = 0; i < n_materials; ++i) sc.materials.push_back(read_material(materials + 32 * i));
     for (int i = 0; i < n_lights; ++i) {
         const float* l = lights + 15 * i;
@@ -355,6 +365,7 @@ void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* 
     for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
     for (auto& th : pool) th.join();
     orq::release(const_cast<void*>(sc.bvh));
+    delete tex;
 }
 
 }  // extern "C"

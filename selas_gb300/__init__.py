@@ -247,6 +247,8 @@ register_signatures({
     "sel_scene_add_quad_light": [_vp, _u, ctypes.POINTER(SelQuadLight)],
     "sel_scene_set_background": [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float],
     "sel_pt_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
+    "sel_ptex_filter_device": [_vp, _vp, _u, _vp, _vp, _u, _vp, _vp],
+    "sel_scene_set_ptex": [_vp, _u, _vp, _sz, _vp, _sz],
     "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
 })
 
@@ -301,6 +303,14 @@ def _scene_pt_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> n
     return out
 
 
+def _scene_set_ptex(self, geom_id: int, rows: np.ndarray, texels: np.ndarray) -> None:
+    """Binds per-face Ptex texels (rows: (n, 8) int32 SelPtexFace records; texels: float16 RGB)."""
+    r = np.ascontiguousarray(rows, np.int32)
+    t = np.ascontiguousarray(np.asarray(texels, np.float16).view(np.uint16))
+    check(lib().sel_scene_set_ptex(self.handle, geom_id, r.ctypes.data, r.shape[0], t.ctypes.data, t.size))
+
+
+Scene.set_ptex = _scene_set_ptex
 Scene.set_material = _scene_set_material
 Scene.add_quad_light = _scene_add_quad_light
 Scene.set_background = _scene_set_background

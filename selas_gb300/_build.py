@@ -60,7 +60,9 @@ def build_library(force: bool = False, jobs: int | None = None) -> Path:
         obj = OBJ / (src.stem + ".cu.o")
         objs.append(obj)
         if force or _stale(src, obj, newest):
-            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
+            # -fmad=false: no implicit multiply-add contraction, so FP32 shading rounds like the
+            # reference's (uncontracted) CPU build; traversal spells out its fmaf / __fmul_rn steps.
+            cmds.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr", "-fmad=false",
                          "-Xcompiler", "-fPIC", *inc, "-c", str(src), "-o", str(obj)])
     for src in sorted(CSRC.glob("*.cpp")):
         obj = OBJ / (src.stem + ".cpp.o")

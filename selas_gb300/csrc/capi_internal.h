@@ -33,6 +33,15 @@ struct SelSceneTy {
     std::vector<std::vector<sel::QuadLight>> light_sets;
     float background[3] = {1.0f, 1.0f, 1.0f};  // backgroundIntensity default (CSceneBuildProcessor.cpp:59)
     bool shading_dirty = true;
+    struct PtexBinding {
+        uint32_t geomID;
+        std::vector<SelPtexFace> faces;
+        std::vector<uint16_t> texels;
+    };
+    std::vector<PtexBinding> ptex;
+    void* d_ptex_faces = nullptr;
+    void* d_ptex_texels = nullptr;
+    uint32_t ptex_face_count = 0;
     void* d_materials = nullptr;
     void* d_lights = nullptr;
     void* d_light_sets = nullptr;

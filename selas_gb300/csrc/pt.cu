@@ -14,6 +14,7 @@
 #include <cstring>
 
 #include "capi_internal.h"
+#include "ptex.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
 
@@ -32,6 +33,9 @@ struct PtParams {
     const QuadLight* lights;
     const uint2* light_sets;  // (first light, count) per set
     uint32_t light_set_count;
+    const PtexFace* ptex_faces;
+    const __half* ptex_texels;
+    uint32_t ptex_face_count;
     float3 background;
     CameraDev cam;
     uint32_t width, height;
@@ -189,7 +193,15 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 // RayPick error bound (PathTracer.cpp:134-136)
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
-                const Surface sf = make_surface(m, ng, -d, ld3(m.base_color));
+                float3 base = ld3(m.base_color);
+                if (m.flags & kMaterialUsesPtex) {
+                    // per-face Ptex base colour at the hit's barycentrics (SurfaceParameters.cpp:196-206)
+                    uint32_t pstatus = 0;
+                    ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels,
+                              int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z, base, pstatus);
+                    if (pstatus) atomicOr(P.err, pstatus);
+                }
+                const Surface sf = make_surface(m, ng, -d, base);
                 // Next-event estimation to the surface's light set (AreaLighting.cpp:353-373)
                 LightSample ls;
                 ls.radiance = f3(0.0f);
@@ -360,6 +372,9 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     P.lights = sc.lights;
     P.light_sets = sc.light_sets;
     P.light_set_count = sc.light_set_count;
+    P.ptex_faces = static_cast<const PtexFace*>(sc.ptex_faces);
+    P.ptex_texels = static_cast<const __half*>(sc.ptex_texels);
+    P.ptex_face_count = sc.ptex_face_count;
     P.background = make_float3(sc.background[0], sc.background[1], sc.background[2]);
     P.cam.x = make_float3(cam.x[0], cam.x[1], cam.x[2]);
     P.cam.y = make_float3(cam.y[0], cam.y[1], cam.y[2]);

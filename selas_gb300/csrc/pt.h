@@ -39,6 +39,9 @@ struct PtScene {
     const QuadLight* lights;
     const uint2* light_sets;
     uint32_t light_set_count;
+    const void* ptex_faces;   // PtexFace[] of all bound geometries
+    const void* ptex_texels;  // half RGB
+    uint32_t ptex_face_count;
     float background[3];
 };
 

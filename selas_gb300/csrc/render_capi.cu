@@ -74,6 +74,29 @@ int sync_shading(SelSceneTy* sc) {
         sets.push_back(make_uint2(uint32_t(lights.size()), uint32_t(set.size())));
         lights.insert(lights.end(), set.begin(), set.end());
     }
+    // Ptex: one face table for all bound geometries, adjacency and texel offsets rebased
+    std::vector<SelPtexFace> faces;
+    std::vector<uint16_t> texels;
+    for (const auto& pb : sc->ptex) {
+        const uint32_t face_base = uint32_t(faces.size());
+        const uint32_t texel_base = uint32_t(texels.size() / 3);
+        for (SelPtexFace f : pb.faces) {
+            f.offset += texel_base;
+            for (int e = 0; e < 3; ++e)
+                if (f.adjfaces[e] >= 0) f.adjfaces[e] += int32_t(face_base);
+            faces.push_back(f);
+        }
+        texels.insert(texels.end(), pb.texels.begin(), pb.texels.end());
+        if (pb.geomID < mats.size()) mats[pb.geomID].ptex_base = face_base;
+    }
+    for (auto& m : mats) {
+        bool bound = false;
+        for (const auto& pb : sc->ptex) bound |= (&m - mats.data()) == ptrdiff_t(pb.geomID);
+        if (!bound) m.flags &= ~kMaterialUsesPtex;  // no texture bound: keep the material's base colour
+    }
+    if (int rc = upload(sc->d_ptex_faces, faces.data(), faces.size())) return rc;
+    if (int rc = upload(sc->d_ptex_texels, texels.data(), texels.size())) return rc;
+    sc->ptex_face_count = uint32_t(faces.size());
     if (int rc = upload(sc->d_materials, mats.data(), mats.size())) return rc;
     if (int rc = upload(sc->d_lights, lights.data(), lights.size())) return rc;
     if (int rc = upload(sc->d_light_sets, sets.data(), sets.size())) return rc;
@@ -124,6 +147,9 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     ps.lights = static_cast<const QuadLight*>(sc->d_lights);
     ps.light_sets = static_cast<const uint2*>(sc->d_light_sets);
     ps.light_set_count = uint32_t(sc->light_sets.size());
+    ps.ptex_faces = sc->d_ptex_faces;
+    ps.ptex_texels = sc->d_ptex_texels;
+    ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
     PtCamera cam;
     init_camera(camera, cam);
@@ -175,6 +201,43 @@ int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const S
     q.z = make_float3(light->z[0], light->z[1], light->z[2]);
     q.radiance = make_float3(light->radiance[0], light->radiance[1], light->radiance[2]);
     scene->light_sets[lightSetIndex].push_back(q);
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* faces, size_t face_count,
+                       const uint16_t* texels, size_t texel_count) {
+    if (!scene || (face_count && !faces) || (texel_count && !texels)) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    const MeshInput* mesh = nullptr;
+    for (const MeshInput& m : scene->meshes)
+        if (m.geomID == geomID) mesh = &m;
+    if (!mesh) return fail(SEL_ERR_INVALID_ARGUMENT, "no geometry with this geomID");
+    if (face_count != mesh->indices.size() / 3)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "face_count must equal the geometry's triangle count");
+    for (size_t i = 0; i < face_count; ++i) {
+        const SelPtexFace& f = faces[i];
+        if (f.log2 < 0 || f.log2 > 12) return fail(SEL_ERR_INVALID_ARGUMENT, "face log2 resolution out of range");
+        const uint64_t need = uint64_t(f.offset) + (uint64_t(1) << (2 * f.log2));
+        if (need * 3 > texel_count) return fail(SEL_ERR_INVALID_ARGUMENT, "face texels exceed the texel array");
+        if (f.log2 != faces[0].log2) return fail(SEL_ERR_INVALID_ARGUMENT, "all faces must share one resolution");
+        for (int e = 0; e < 3; ++e) {
+            if (f.adjfaces[e] >= int64_t(face_count) || f.adjfaces[e] < -1 || f.adjedges[e] < 0 || f.adjedges[e] > 2)
+                return fail(SEL_ERR_INVALID_ARGUMENT, "adjacency out of range");
+        }
+    }
+    SelSceneTy::PtexBinding pb;
+    pb.geomID = geomID;
+    pb.faces.assign(faces, faces + face_count);
+    pb.texels.assign(texels, texels + texel_count);
+    for (auto& existing : scene->ptex)
+        if (existing.geomID == geomID) {
+            existing = std::move(pb);
+            scene->shading_dirty = true;
+            return SEL_OK;
+        }
+    scene->ptex.push_back(std::move(pb));
     scene->shading_dirty = true;
     return SEL_OK;
 }

@@ -191,6 +191,27 @@ class RenderScene:
     lights: list = field(default_factory=list)      # (light set, dict(position, direction, x, z, radiance))
     background: tuple = (0.0, 0.0, 0.0)
     camera: dict = field(default_factory=dict)      # position, look_at, up, fov_degrees
+    ptex: dict = field(default_factory=dict)        # geomID -> (face rows (n, 8) int32, texels float16)
+
+    def ptex_tables(self, material_recs=None):
+        """Combined face table (rows rebased) and texels of all textured geometries, in geomID order; writes
+        each geometry's first face into word 3 of its material record when given."""
+        rows, texels, base_face, base_texel = [], [], 0, 0
+        for gid in sorted(self.ptex):
+            r, t = self.ptex[gid]
+            r = np.array(r, np.int32, copy=True)
+            r[:, 1] += base_texel
+            adj = r[:, 2:5]
+            adj[adj >= 0] += base_face
+            rows.append(r)
+            texels.append(np.asarray(t, np.float16).view(np.uint16))
+            if material_recs is not None and gid < material_recs.shape[0]:
+                material_recs.view(np.uint32)[gid, 3] = base_face
+            base_face += r.shape[0]
+            base_texel += t.size // 3
+        if not rows:
+            return np.zeros((0, 8), np.int32), np.zeros(3, np.uint16)
+        return np.ascontiguousarray(np.concatenate(rows)), np.ascontiguousarray(np.concatenate(texels))
 
     def build(self, sel_module, device, bvh_kind=0):
         """Creates and commits a selas_gb300 Scene with this content."""
@@ -201,6 +222,9 @@ class RenderScene:
         for ls, l in self.lights:
             sc.add_quad_light(ls, l["position"], l["direction"], l["x"], l["z"], l["radiance"])
         sc.set_background(self.background)
+        for gid in sorted(self.ptex):
+            rows, tex = self.ptex[gid]
+            sc.set_ptex(gid, rows, tex)
         sc.commit()
         return sc
 
@@ -287,3 +311,86 @@ def light_records(lights: list):
         for l in group:
             flat.append(list(l["position"]) + list(l["direction"]) + list(l["x"]) + list(l["z"]) + list(l["radiance"]))
     return (np.array(flat, np.float32).reshape(-1, 15), np.array(sets, np.uint32).reshape(-1, 2))
+
+
+# ---------------------------------------------------------------------------------------------------
+# Per-face textures (Ptex model: one square texel block per triangle plus edge adjacency)
+# ---------------------------------------------------------------------------------------------------
+def triangle_adjacency(faces: np.ndarray):
+    """Ptex FaceInfo adjacency of a triangle mesh: edge i of a face runs from vertex i to vertex i+1;
+    adj[f, i] = neighbouring face across that edge (-1 on a boundary), adjedge[f, i] = the neighbour's edge
+    index for the same edge."""
+    f = np.asarray(faces, np.int64)
+    n = f.shape[0]
+    a = np.concatenate([f[:, 0], f[:, 1], f[:, 2]])
+    b = np.concatenate([f[:, 1], f[:, 2], f[:, 0]])
+    face_of = np.tile(np.arange(n), 3)
+    edge_of = np.repeat(np.arange(3), n)
+    lo, hi = np.minimum(a, b), np.maximum(a, b)
+    key = lo * (int(f.max()) + 1) + hi
+    order = np.argsort(key, kind="stable")
+    ks = key[order]
+    adj = np.full((n, 3), -1, np.int32)
+    adjedge = np.zeros((n, 3), np.int32)
+    same = np.nonzero(ks[1:] == ks[:-1])[0]
+    for i in same:  # manifold edges appear exactly twice
+        p, q = order[i], order[i + 1]
+        if i + 2 < ks.size and ks[i + 2] == ks[i]:
+            continue
+        if i > 0 and ks[i - 1] == ks[i]:
+            continue
+        adj[face_of[p], edge_of[p]] = face_of[q]
+        adjedge[face_of[p], edge_of[p]] = edge_of[q]
+        adj[face_of[q], edge_of[q]] = face_of[p]
+        adjedge[face_of[q], edge_of[q]] = edge_of[p]
+    return adj, adjedge
+
+
+def value_noise_texels(n_faces: int, log2: int, seed: int, lattice: int = 4, lo: float = 0.1, hi: float = 0.9):
+    """Per-face value noise: a lattice x lattice grid of seeded RGB values, bilinearly interpolated to
+    2^log2 x 2^log2 texels, stored as float16 (face-major, row-major, RGB interleaved)."""
+    rng = np.random.default_rng(seed)
+    res = 1 << log2
+    grid = rng.uniform(lo, hi, size=(n_faces, lattice, lattice, 3))
+    t = (np.arange(res) + 0.5) / res * (lattice - 1)
+    i0 = np.minimum(np.floor(t).astype(int), lattice - 2)
+    fr = t - i0
+    rows = grid[:, i0, :, :] * (1 - fr)[None, :, None, None] + grid[:, i0 + 1, :, :] * fr[None, :, None, None]
+    tex = rows[:, :, i0, :] * (1 - fr)[None, None, :, None] + rows[:, :, i0 + 1, :] * fr[None, None, :, None]
+    return tex.astype(np.float16).reshape(-1)
+
+
+def ptex_faces(faces: np.ndarray, log2: int):
+    """Face table rows (log2, texel offset, adj0..2, adjedge0..2) as int32, one per triangle."""
+    n = faces.shape[0]
+    adj, adjedge = triangle_adjacency(faces)
+    table = np.zeros((n, 8), np.int32)
+    table[:, 0] = log2
+    table[:, 1] = np.arange(n, dtype=np.int64) * (1 << (2 * log2))
+    table[:, 2:5] = adj
+    table[:, 5:8] = adjedge
+    return table
+
+
+def textured_spheres(count: int = 6, level: int = 3, log2: int = 4, seed: int = 0x5E1A5F00) -> RenderScene:
+    """A few displaced icospheres with per-face Ptex value-noise base colour (16 x 16 FP16 RGB by default)
+    on a grey floor, under one 2 x 2 quad light and a dim background."""
+    rng = np.random.default_rng(seed)
+    unit_v, f = icosphere(level)
+    g = TriangleScene()
+    mats, ptex = {}, {}
+    for i in range(count):
+        centre = np.array([rng.uniform(-4, 4), rng.uniform(1.0, 2.5), rng.uniform(-2, 2)])
+        radius = rng.uniform(0.6, 1.2)
+        disp = 1.0 + 0.1 * value_noise_dirs(unit_v, rng)
+        g.add(i, (centre + unit_v * (radius * disp)[:, None]).astype(np.float32), f.astype(np.uint32))
+        mats[i] = dict(shader=1, lightSetIndex=0, roughness=float(rng.uniform(0.05, 1.0)),
+                       metallic=float(rng.random() < 0.3), ior=1.5, usesPtex=1)
+        ptex[i] = (ptex_faces(f, log2), value_noise_texels(f.shape[0], log2, seed + 17 * i))
+    floor = np.array([[-20, 0, -20], [-20, 0, 20], [20, 0, 20], [20, 0, -20]], np.float32)
+    g.add(count, floor, np.array([[0, 1, 2], [0, 2, 3]], np.uint32))
+    mats[count] = dict(shader=1, lightSetIndex=0, baseColor=(0.6, 0.6, 0.6), roughness=0.7, ior=1.5)
+    light = dict(position=(0.0, 6.0, 0.0), direction=(0.0, -1.0, 0.0), x=(2.0, 0.0, 0.0), z=(0.0, 0.0, 2.0),
+                 radiance=(30.0, 28.0, 25.0))
+    cam = dict(position=(0.0, 3.0, -11.0), look_at=(0.0, 1.5, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=55.0)
+    return RenderScene(g, mats, [(0, light)], (0.05, 0.05, 0.08), cam, ptex)

@@ -8,6 +8,10 @@ by oracle/ref/build_ref.py):
 bsdf_golden.npz  - seeded (surface, wo, wi) tuples -> EvaluateBsdf (f, forwardPdfW, reversePdfW) and
                    seeded (surface, wo, 4 uniforms) tuples -> SampleBsdfFunction results, computed by
                    Source/Core/Shading/SurfaceScattering.cpp:18-60 -> Disney.cpp / DiracTransparent.cpp.
+ptex_golden.npz  - a triangle mesh (icosphere, 320 faces) with 16 x 16 half-float RGB value-noise texels per
+                   face and Ptex adjacency, written with the vendored Ptex 2.2 writer and filtered by its
+                   PtexTriangleFilter (getFilter(f_bspline), zero widths, as SurfaceParameters.cpp:196-206)
+                   at seeded (face, u, v) queries including edges, corners and out-of-range faces.
 cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
                    from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp); the image the
                    path tracers' rMSE is measured against.  Needs only the oracle (python ... cornell).
@@ -112,6 +116,44 @@ def make_bsdf(n_eval=3000, n_sample=3000, seed=0x5E1A5B5D):
           "nonzero f:", int((out_e[:, :3].sum(1) > 0).sum()), "successful samples:", int(out_s[:, 0].sum()))
 
 
+def make_ptex(seed=0x5E1A5E7E, n_random=6000):
+    import tempfile
+    from selas_gb300 import scenes
+    lib = ctypes.CDLL(str(ROOT / "oracle" / "_ref" / "libref_ptex.so"))
+    vp = ctypes.c_void_p
+    lib.ref_ptex_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, vp]
+    lib.ref_ptex_eval.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, vp]
+    _, tris = scenes.icosphere(2)
+    faces = scenes.ptex_faces(tris, 4)
+    texels = scenes.value_noise_texels(tris.shape[0], 4, seed)
+    tex_u16 = np.ascontiguousarray(texels.view(np.uint16))
+    rng = np.random.default_rng(seed)
+    nf = tris.shape[0]
+    f = rng.integers(0, nf, n_random)
+    a, b = rng.random(n_random), rng.random(n_random)
+    flip = a + b > 1
+    a[flip], b[flip] = 1 - a[flip], 1 - b[flip]
+    q = [np.stack([f, a, b], 1)]
+    special = []
+    for face in rng.integers(0, nf, 40):
+        for u, v in ((0, 0), (1, 0), (0, 1), (0.5, 0), (0, 0.5), (0.5, 0.5), (1e-4, 0.3), (0.3, 1e-4),
+                     (0.4999, 0.4999), (1.2, -0.1), (0.02, 0.97)):
+            special.append((face, u, v))
+    special += [(-1, 0.3, 0.3), (nf, 0.3, 0.3)]
+    q.append(np.array(special, np.float64))
+    q = np.concatenate(q)
+    queries = np.zeros((q.shape[0], 3), np.float32)
+    queries[:, 0] = q[:, 0].astype(np.int32).view(np.float32)
+    queries[:, 1:] = q[:, 1:]
+    out = np.zeros((q.shape[0], 3), np.float32)
+    with tempfile.TemporaryDirectory() as d:
+        path = (Path(d) / "noise.ptx").as_posix().encode()
+        assert lib.ref_ptex_write(path, faces.ctypes.data, nf, tex_u16.ctypes.data) == 0
+        assert lib.ref_ptex_eval(path, queries.ctypes.data, queries.shape[0], out.ctypes.data) == 0
+    np.savez_compressed(OUT / "ptex_golden.npz", faces=faces, texels=tex_u16, queries=queries, out=out)
+    print("ptex_golden.npz:", queries.shape[0], "queries over", nf, "faces")
+
+
 def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
     import oracle
     from selas_gb300 import scenes
@@ -126,8 +168,10 @@ def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["bsdf", "cornell"]
+    what = sys.argv[1:] or ["bsdf", "ptex", "cornell"]
     if "bsdf" in what:
         make_bsdf()
+    if "ptex" in what:
+        make_ptex()
     if "cornell" in what:
         make_cornell()
