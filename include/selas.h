@@ -135,6 +135,18 @@ int sel_occluded1(SelScene scene, SelRay* ray);
 int sel_intersect1M(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride);
 int sel_occluded1M(SelScene scene, SelRay* rays, unsigned int M, size_t byte_stride);
 
+/* Same closest-hit query as sel_intersect1M for callers that must not allocate GPU memory: a host
+ * application that owns the GPU's memory through its own pool (a plugin inside a renderer or engine),
+ * a real-time loop that cannot risk the device synchronisation cudaMalloc/cudaFree may cause, or code
+ * with every byte of HBM budgeted up front.  It has no counterpart in the reference.  The call allocates
+ * nothing: it stages records in one fixed array of 65536 SelRayHit records (6 MiB) that every GPU
+ * loading the library holds until exit, and rejects M > 65536 with SEL_ERR_INVALID_ARGUMENT.  The first
+ * call on a device looks up that array's device address; make that first call before any stream capture.
+ * All calls share the array (its contents are whatever the last call left; every call overwrites the
+ * records it uses first).  Calls through one SelDevice are serialised; calls through different SelDevice
+ * handles on the same GPU that overlap on the GPU race on the array. */
+int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride);
+
 /* Device-memory forms: d_rayhits / d_rays point to HBM, work is queued on `stream` (void* holding a
  * cudaStream_t, NULL = default stream) and the call returns without waiting.  Replace the packet
  * queries rtcIntersect8 / rtcOccluded8 of Source/Applications/Selas/Source/DeferredPathTracer.cpp:191,267
