@@ -35,7 +35,10 @@ def lib() -> ctypes.CDLL:
             "oracle_ptex_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
             "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
-                                  ctypes.c_uint64, _i, _i, _vp, _i, _vp, _vp], None),
+                                  ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
+            "oracle_vcm_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, ctypes.c_uint32, ctypes.c_uint32,
+                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_uint64, _i, _vp, _i, _vp, _i, _i, _vp], None),
         }
         for name, (args, res) in sig.items():
             fn = getattr(_lib, name)
@@ -106,8 +109,21 @@ def bsdf_sample(surf, wo, u):
     return out
 
 
+class consistent_lambert:
+    """Context manager: the oracle's BSDF is an opaque Lambert with exact sampling weights while inside
+    (oracle_bsdf.cpp, g_consistent_lambert), for checking that the integrators' estimators agree."""
+
+    def __enter__(self):
+        lib().oracle_set_consistent_lambert(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_consistent_lambert(0)
+        return False
+
+
 def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, seed=0x5E1A5000, rng="pcg",
-              nthreads=None):
+              nthreads=None, physical_nee=False):
     """CPU oracle path tracer (oracle_pt.cpp): FP64 per-pixel sums over passes [pass_begin, pass_end),
     shape (2, height, width, 3)."""
     from selas_gb300.scenes import light_records, material_records
@@ -123,7 +139,7 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
     L.oracle_pt_render(_p(verts), _p(prim), _p(geom), verts.shape[0], _p(mats), mats.shape[0], _p(lights),
                        lights.shape[0], _p(sets), sets.shape[0], _p(bg), _p(cam), width, height, pass_begin, pass_end,
                        max_bounces, seed, 0 if rng == "pcg" else 1, nthreads or threads(), _p(rows), rows.shape[0],
-                       _p(texels), _p(out))
+                       _p(texels), int(physical_nee), _p(out))
     return out
 
 
@@ -134,4 +150,27 @@ def ptex_eval(faces, texels_u16, queries):
     queries = np.ascontiguousarray(queries, np.float32)
     out = np.zeros((queries.shape[0], 3), np.float32)
     lib().oracle_ptex_eval(_p(faces), faces.shape[0], _p(texels_u16), _p(queries), queries.shape[0], _p(out))
+    return out
+
+
+def vcm_render(render_scene, width, height, iter_begin, iter_end, max_len=10, radius0=None, alpha=0.75,
+               seed=0x5E1A5000, nthreads=None, merging=True, strategies=15):
+    """CPU oracle VCM (oracle_vcm.cpp): FP64 per-pixel sums over iterations [iter_begin, iter_end), shape
+    (height, width, 3).  radius0 defaults to 0.0025 x the scene's bounding-sphere radius (VCM.cpp:778 with
+    VcmRadiusFactor_ = 0.0025), the sphere taken about the bounding box (radius = half its diagonal)."""
+    from selas_gb300.scenes import light_records, material_records
+    verts, prim, geom = render_scene.geometry.soup()
+    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    rows, texels = render_scene.ptex_tables(mats)
+    lights, sets = light_records(render_scene.lights)
+    lights0 = np.ascontiguousarray(lights[sets[0, 0]:sets[0, 0] + sets[0, 1]]) if sets.shape[0] else lights[:0]
+    if radius0 is None:
+        lo, hi = render_scene.geometry.bounds()
+        radius0 = 0.0025 * 0.5 * float(np.linalg.norm(hi - lo))
+    c = render_scene.camera
+    cam = np.array(list(c["position"]) + list(c["look_at"]) + list(c["up"]) + [c["fov_degrees"]], np.float32)
+    out = np.zeros((height, width, 3), np.float64)
+    lib().oracle_vcm_render(_p(verts), _p(prim), _p(geom), verts.shape[0], _p(mats), mats.shape[0], _p(lights0),
+                            lights0.shape[0], _p(cam), width, height, iter_begin, iter_end, max_len, radius0, alpha,
+                            seed, nthreads or threads(), _p(rows), rows.shape[0], _p(texels), int(merging), int(strategies), _p(out))
     return out

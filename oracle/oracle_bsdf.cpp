@@ -9,6 +9,8 @@
 
 #include "oracle_bsdf.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -387,8 +389,37 @@ Surf surf_from_record(const float* r) {
     return s;
 }
 
+// Test switch: a BSDF whose sampling weights are exactly f * cos / density (opaque Lambert with albedo
+// baseColor, cosine sampling, pdf cos / pi).  The reference Disney model is not of that kind (its diffuse
+// sample weight is baseColor * f_d and its diffuse pdf is |cos| rather than |cos| / pi, Disney.cpp:466-519),
+// so different estimators of the same path converge to different images on it; the integrators' estimator
+// bookkeeping is checked on this one, where every unbiased estimator converges to the same image.
+std::atomic<int> g_consistent_lambert{0};
+
+static V3 EvalLambert(const Surf& s, V3 v, V3 l, float& fwd, float& rev) {
+    const float cl = Dot(s.n, l), cv = Dot(s.n, v);
+    if (cl * cv <= 0.0f) return V3(0.0f);
+    fwd = std::fabs(cl) * float(1.0 / M_PI);
+    rev = std::fabs(cv) * float(1.0 / M_PI);
+    return s.baseColor * fwd;
+}
+
+static bool SampLambert(const Surf& s, V3 v, Uniforms& un, Sample& o) {
+    const float r0 = un.next(), r1 = un.next();
+    const float r = std::sqrt(r0), ph = float(2.0 * M_PI) * r1, ct = std::sqrt(std::max(0.0f, 1.0f - r0));
+    const float side = Dot(s.n, v) < 0.0f ? -1.0f : 1.0f;
+    o.wi = Norm(r * std::cos(ph) * s.t + (side * ct) * s.n + r * std::sin(ph) * s.b);
+    if (!(ct > 0.0f)) return false;
+    o.refl = s.baseColor;
+    o.fwd = ct * float(1.0 / M_PI);
+    o.rev = std::fabs(Dot(s.n, v)) * float(1.0 / M_PI);
+    o.flags = 1;
+    return true;
+}
+
 V3 bsdf_evaluate(const Surf& s, V3 v, V3 l, float& fwd, float& rev) {
     fwd = rev = 0.0f;
+    if (g_consistent_lambert.load(std::memory_order_relaxed) && s.shader != 2) return EvalLambert(s, v, l, fwd, rev);
     if (s.shader == 0) return EvalDisney(s, v, l, true, fwd, rev);
     if (s.shader == 1) return EvalDisney(s, v, l, false, fwd, rev);
     return V3(0.0f);
@@ -398,7 +429,8 @@ bool bsdf_sample(const Surf& s, V3 v, const float* u, int& used, Sample& o) {
     o = Sample();
     Uniforms un{u, used};
     bool ok = false;
-    if (s.shader == 0) ok = SampDisney(s, v, true, un, o);
+    if (g_consistent_lambert.load(std::memory_order_relaxed) && s.shader != 2) ok = SampLambert(s, v, un, o);
+    else if (s.shader == 0) ok = SampDisney(s, v, true, un, o);
     else if (s.shader == 1) ok = SampDisney(s, v, false, un, o);
     else if (s.shader == 2) ok = SampDirac(s, v, un, o);
     used = un.used;
@@ -408,6 +440,8 @@ bool bsdf_sample(const Surf& s, V3 v, const float* u, int& used, Sample& o) {
 }  // namespace orc
 
 extern "C" {
+
+void oracle_set_consistent_lambert(int on) { orc::g_consistent_lambert.store(on); }
 
 // surf: 32-word SelSurface records (shader as int32 bits); out as sel_bsdf_evaluate_device.
 void oracle_bsdf_evaluate(const float* surf, const float* wo, const float* wi, int64_t n, float* out) {

@@ -117,7 +117,8 @@ Material read_material(const float* r) {
 float Sat(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
 
 // SampleRectangleLightSolidAngle (AreaLighting.cpp:113-153) with the sampler of RectangulerLightSampler.cpp.
-void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad, float& dist, float& pdfw) {
+void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad, float& dist, float& pdfw,
+                  bool physical) {
     V3 s = L.pos - 0.5f * L.x - 0.5f * L.z;
     const float exl = orc::Len(L.x), eyl = orc::Len(L.z);
     V3 X = L.x * (1.0f / exl), Y = L.z * (1.0f / eyl), Z = orc::Cross(X, Y);
@@ -156,7 +157,7 @@ void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad
     if (area > 0) {
         dir = l;
         dist = di;
-        rad = L.radiance * (area * orc::Dot(n, l));
+        rad = L.radiance * (physical ? area : area * orc::Dot(n, l));
         pdfw = pdf * area;
     } else {
         dir = V3(0.0f);
@@ -169,6 +170,7 @@ void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad
 struct Scene {
     const void* bvh;
     const orp::Texture* ptex = nullptr;
+    bool physical_nee = false;
     std::vector<Material> materials;
     std::vector<Light> lights;
     std::vector<uint32_t> set_first, set_count;
@@ -241,7 +243,8 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
                 uint32_t li = uint32_t(p0 * float(cnt));
                 li = std::min(li, cnt - 1);
                 const float u = rng.uniform(), v = rng.uniform();
-                sample_light(sc.lights[sc.set_first[m.light_set] + li], pos, n, u, v, ldir, lrad, ldist, lpdf);
+                sample_light(sc.lights[sc.set_first[m.light_set] + li], pos, n, u, v, ldir, lrad, ldist, lpdf,
+                             sc.physical_nee);
                 lpdf *= 1.0f / float(cnt);
             }
             if (orc::Dot(lrad, V3(1.0f)) > 0) {
@@ -299,14 +302,17 @@ extern "C" {
 // camera: position[3] lookAt[3] up[3] fovDegrees; ptex_rows/ptex_texels: the combined Ptex face table of
 // all textured geometries (material word 3 = that geometry's first face); out: [2][height][width][3]
 // doubles (sums over the paths of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the
-// GPU); 1: MT19937 per pixel.
+// GPU); 1: MT19937 per pixel.  physical_nee drops the extra cos(theta_surface) factor that the reference's
+// SampleRectangleLightSolidAngle puts into the NEE radiance (AreaLighting.cpp:140-146), giving the
+// physically correct estimator that other integrators (VCM) converge to.
 void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
                       const float* materials, int n_materials, const float* lights, int n_lights,
                       const uint32_t* sets, int n_sets, const float* background, const float* camera,
                       uint32_t width, uint32_t height, uint32_t pass_begin, uint32_t pass_end, uint32_t max_bounces,
                       uint64_t seed, int rng_mode, int threads, const int32_t* ptex_rows, int ptex_faces,
-                      const uint16_t* ptex_texels, double* out) {
+                      const uint16_t* ptex_texels, int physical_nee, double* out) {
     Scene sc;
+    sc.physical_nee = physical_nee != 0;
     sc.bvh = orq::build(verts, prim, geom, ntri);
     orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
     sc.ptex = tex;
