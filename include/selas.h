@@ -286,6 +286,30 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
 int sel_pt_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
                          void* stream);
 
+/* Vertex connection and merging: VCM::GenerateImage (Source/Applications/Selas/Source/VCM.h:18,
+ * VCM.cpp:751-808, commented out in the reference and restated from the VCM technical report it cites).
+ * A pass traces width * height light paths (from light set 0) and as many camera paths; the pass index
+ * i = firstPass + k sets the merge radius r0 / (i + 1)^((1 - alpha) / 2) (VCMCommon.cpp:91-112) and the
+ * random streams, so a render split over several calls equals one call over all its passes. */
+typedef struct SelVcmSettings {
+    uint32_t passes;          /* iterations (the reference integrates for IntegrationSeconds_ = 30 s) */
+    uint32_t firstPass;       /* global index of the first pass */
+    uint32_t maxPathLength;   /* path segments, 2..32 (MaxBounceCount_ = 10, VCMCommon.cpp:24) */
+    uint32_t disableMerging;  /* nonzero: bidirectional path tracing (no merge term or merge weights) */
+    uint64_t seed;            /* PCG32 seed */
+    float radius;             /* r0; 0 = VcmRadiusFactor_ (0.0025) x the bounding-sphere radius of the
+                                 scene bounds (half their diagonal), as VCM.cpp:778 */
+    float radiusAlpha;        /* VcmRadiusAlpha_ = 0.75 (VCMCommon.cpp:30) */
+} SelVcmSettings;
+
+int sel_vcm_settings_defaults(SelVcmSettings* out);
+/* Renders and writes the mean over the passes, [height][width][3] floats in host memory (FP64 sums). */
+int sel_vcm_generate_image(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, float* out_rgb);
+/* Device form: adds the per-pass sums into d_accum ([height][width][3] doubles in HBM) on `stream` and
+ * returns without waiting. */
+int sel_vcm_render_device(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, double* d_accum,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

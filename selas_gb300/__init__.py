@@ -237,6 +237,12 @@ class SelPtSettings(ctypes.Structure):
                 ("pathsInFlight", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class SelVcmSettings(ctypes.Structure):
+    _fields_ = [("passes", ctypes.c_uint32), ("firstPass", ctypes.c_uint32), ("maxPathLength", ctypes.c_uint32),
+                ("disableMerging", ctypes.c_uint32), ("seed", ctypes.c_uint64), ("radius", ctypes.c_float),
+                ("radiusAlpha", ctypes.c_float)]
+
+
 SEL_SHADER_DISNEY_THIN, SEL_SHADER_DISNEY_SOLID, SEL_SHADER_DIRAC_TRANSPARENT = 0, 1, 2
 
 register_signatures({
@@ -250,6 +256,9 @@ register_signatures({
     "sel_ptex_filter_device": [_vp, _vp, _u, _vp, _vp, _u, _vp, _vp],
     "sel_scene_set_ptex": [_vp, _u, _vp, _sz, _vp, _sz],
     "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
+    "sel_vcm_settings_defaults": [ctypes.POINTER(SelVcmSettings)],
+    "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
+    "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
 })
 
 
@@ -281,6 +290,17 @@ def pt_settings(spp, max_bounces=8, seed=0x5E1A5000, paths_in_flight=0) -> SelPt
     return s
 
 
+def vcm_settings(passes, max_path_length=10, seed=0x5E1A5000, first_pass=0, merging=True, radius=0.0,
+                 radius_alpha=0.75) -> SelVcmSettings:
+    """SelVcmSettings; radius 0 selects the reference's default (0.0025 x the bounding-sphere radius)."""
+    s = SelVcmSettings()
+    check(lib().sel_vcm_settings_defaults(ctypes.byref(s)))
+    s.passes, s.maxPathLength, s.seed, s.firstPass = passes, max_path_length, seed, first_pass
+    s.disableMerging = 0 if merging else 1
+    s.radius, s.radiusAlpha = radius, radius_alpha
+    return s
+
+
 def _scene_set_material(self, geom_id: int, m: SelMaterial) -> None:
     check(lib().sel_scene_set_material(self.handle, geom_id, ctypes.byref(m)))
 
@@ -303,6 +323,13 @@ def _scene_pt_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> n
     return out
 
 
+def _scene_vcm_generate_image(self, cam: SelCamera, settings: SelVcmSettings) -> np.ndarray:
+    """VCM::GenerateImage: (height, width, 3) float32, the mean over the passes."""
+    out = np.zeros((cam.height, cam.width, 3), np.float32)
+    check(lib().sel_vcm_generate_image(self.handle, ctypes.byref(cam), ctypes.byref(settings), out.ctypes.data))
+    return out
+
+
 def _scene_set_ptex(self, geom_id: int, rows: np.ndarray, texels: np.ndarray) -> None:
     """Binds per-face Ptex texels (rows: (n, 8) int32 SelPtexFace records; texels: float16 RGB)."""
     r = np.ascontiguousarray(rows, np.int32)
@@ -315,3 +342,4 @@ Scene.set_material = _scene_set_material
 Scene.add_quad_light = _scene_add_quad_light
 Scene.set_background = _scene_set_background
 Scene.pt_generate_image = _scene_pt_generate_image
+Scene.vcm_generate_image = _scene_vcm_generate_image

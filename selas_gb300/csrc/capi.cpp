@@ -223,7 +223,8 @@ int sel_scene_release(SelScene scene) {
     set_device(scene->dev);
     cudaStreamSynchronize(scene->dev->stream);
     for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
-                    scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels})
+                    scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
+                    scene->vcm_block})
         if (p) cudaFree(p);
     delete scene;
     return SEL_OK;

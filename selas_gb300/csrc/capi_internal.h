@@ -50,6 +50,9 @@ struct SelSceneTy {
     uint32_t pt_capacity = 0;
     void* d_accum = nullptr;
     size_t accum_bytes = 0;
+    // VCM scratch: light vertices, hash grid and constants table for `vcm_paths` paths per pass
+    void* vcm_block = nullptr;
+    uint32_t vcm_paths = 0, vcm_len = 0, vcm_passes = 0;
     std::mutex mu;
 };
 

@@ -3,8 +3,11 @@
 #include <mutex>
 #include <new>
 
+#include <cmath>
+
 #include "capi_internal.h"
 #include "pt.h"
+#include "vcm.h"
 
 using namespace sel;
 
@@ -130,13 +133,7 @@ int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettin
     return SEL_OK;
 }
 
-int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& settings, double* d_accum,
-                  cudaStream_t stream) {
-    if (int rc = sync_shading(sc)) return rc;
-    const uint64_t total = uint64_t(camera.width) * camera.height * settings.samplesPerPixel;
-    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight : kDefaultPathsInFlight;
-    if (uint64_t(cap) > total) cap = uint32_t(total);
-    if (int rc = ensure_pt_state(sc, cap)) return rc;
+PtScene scene_view(const SelSceneTy* sc) {
     PtScene ps;
     ps.nodes = static_cast<const uint4*>(sc->d_nodes);
     ps.tris = static_cast<const float4*>(sc->d_tris);
@@ -151,6 +148,17 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     ps.ptex_texels = sc->d_ptex_texels;
     ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
+    return ps;
+}
+
+int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& settings, double* d_accum,
+                  cudaStream_t stream) {
+    if (int rc = sync_shading(sc)) return rc;
+    const uint64_t total = uint64_t(camera.width) * camera.height * settings.samplesPerPixel;
+    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight : kDefaultPathsInFlight;
+    if (uint64_t(cap) > total) cap = uint32_t(total);
+    if (int rc = ensure_pt_state(sc, cap)) return rc;
+    const PtScene ps = scene_view(sc);
     PtCamera cam;
     init_camera(camera, cam);
     PtSettings set;
@@ -160,6 +168,120 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     const PtState st = pt_state_carve(sc->pt_block, cap);
     cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
+}
+
+constexpr uint32_t kVcmChunk = 1024;  // passes per constants table
+
+SelVcmSettings default_vcm_settings() {
+    SelVcmSettings s;
+    std::memset(&s, 0, sizeof(s));
+    s.passes = 1;
+    s.maxPathLength = 10;      // MaxBounceCount_ (VCMCommon.cpp:24)
+    s.seed = 1;
+    s.radius = 0.0f;           // VcmRadiusFactor_ x bounding-sphere radius
+    s.radiusAlpha = 0.75f;     // VcmRadiusAlpha_ (VCMCommon.cpp:30)
+    return s;
+}
+
+int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings) {
+    if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    if (scene->info.bvh_kind != SEL_BVH_WIDE8_Q8)
+        return fail(SEL_ERR_INVALID_OPERATION, "the renderer traverses the 8-wide BVH: commit with SEL_BVH_WIDE8_Q8");
+    if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
+    if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "fovDegrees must lie in (0, 180)");
+    if (settings->passes == 0) return fail(SEL_ERR_INVALID_ARGUMENT, "passes must be > 0");
+    if (settings->maxPathLength < 2 || settings->maxPathLength > 32)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "maxPathLength must lie in 2..32");
+    if (!(settings->radius >= 0.0f) || !std::isfinite(settings->radius))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "radius must be finite and >= 0");
+    if (!(settings->radiusAlpha > 0.0f && settings->radiusAlpha <= 1.0f))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "radiusAlpha must lie in (0, 1]");
+    const uint64_t paths = uint64_t(camera->width) * camera->height;
+    // random streams (2 * pass + 1) * N + p and slot indices p * (maxPathLength - 1) + k stay 32/64-bit exact
+    if (paths * (settings->maxPathLength - 1) >= (uint64_t(1) << 31))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "width * height * (maxPathLength - 1) must be below 2^31");
+    if (uint64_t(settings->firstPass) + settings->passes > (uint64_t(1) << 31))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "firstPass + passes must be below 2^31");
+    return SEL_OK;
+}
+
+int ensure_vcm_state(SelSceneTy* sc, uint32_t paths, uint32_t max_len) {
+    if (sc->vcm_block && sc->vcm_paths == paths && sc->vcm_len == max_len) return SEL_OK;
+    if (sc->vcm_block) cudaFree(sc->vcm_block);
+    sc->vcm_block = nullptr;
+    sc->vcm_paths = sc->vcm_len = sc->vcm_passes = 0;
+    cudaError_t e = cudaMalloc(&sc->vcm_block, vcm_state_block_bytes(paths, max_len, kVcmChunk));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(VCM state)");
+    sc->vcm_paths = paths;
+    sc->vcm_len = max_len;
+    sc->vcm_passes = kVcmChunk;
+    return SEL_OK;
+}
+
+// Per-pass constants (CalculateIterationConstants, VCMCommon.cpp:91-112, with vcCount = 1): the float
+// expressions of the CPU restatement, so that both compute the same radius and weights.
+void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c) {
+    const float pi = 3.141592653589793f;
+    c.radius = radius0 / std::pow(float(pass + 1), 0.5f * (1.0f - alpha));
+    c.radius2 = c.radius * c.radius;
+    c.n_paths = float(paths);
+    const float eta = pi * c.radius2 * c.n_paths;
+    c.vm_weight = merging ? eta : 0.0f;
+    c.vc_weight = 1.0f / eta;
+    c.vm_norm = 1.0f / eta;
+    c.pass = pass;
+    c.pad = 0;
+}
+
+int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSettings& settings, double* d_accum,
+                      cudaStream_t stream) {
+    if (int rc = sync_shading(sc)) return rc;
+    const uint32_t paths = camera.width * camera.height;
+    if (int rc = ensure_vcm_state(sc, paths, settings.maxPathLength)) return rc;
+    float radius0 = settings.radius;
+    if (radius0 == 0.0f) {
+        float d2 = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            const float e = sc->info.bounds_hi[a] - sc->info.bounds_lo[a];
+            d2 += e * e;
+        }
+        radius0 = 0.0025f * (0.5f * std::sqrt(d2));  // VcmRadiusFactor_ * boundingSphere.w (VCM.cpp:778)
+        if (!(radius0 > 0.0f)) radius0 = 1e-3f;
+    }
+    VcmCamera cam;
+    init_camera(camera, cam.cam);
+    const float hlen = std::tan(camera.fovDegrees * (3.141592653589793f / 180.0f) * 0.5f);
+    cam.image_plane = float(camera.width) / (2.0f * hlen);
+    VcmSettings set;
+    set.max_len = settings.maxPathLength;
+    set.seed = settings.seed;
+    set.merging = settings.disableMerging ? 0 : 1;
+    set.light_first = 0;
+    set.light_count = 0;
+    if (!sc->light_sets.empty()) {
+        set.light_count = uint32_t(sc->light_sets[0].size());
+    }
+    const PtScene ps = scene_view(sc);
+    const VcmState st = vcm_state_carve(sc->vcm_block, paths, settings.maxPathLength, kVcmChunk);
+    std::vector<VcmConsts> consts;
+    for (uint32_t done = 0; done < settings.passes;) {
+        const uint32_t n = std::min(kVcmChunk, settings.passes - done);
+        consts.resize(n);
+        for (uint32_t k = 0; k < n; ++k)
+            vcm_constants(radius0, settings.radiusAlpha, paths, set.merging != 0, settings.firstPass + done + k, consts[k]);
+        cudaError_t e = vcm_render(ps, cam, set, consts.data(), n, st, d_accum, sc->dev->d_err, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "VCM launch");
+        // the constants table is read by the passes just queued: wait before it is refilled
+        if (done + n < settings.passes) {
+            e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) return cuda_fail(e, "VCM");
+        }
+        done += n;
+    }
+    return SEL_OK;
 }
 
 }  // namespace
@@ -289,6 +411,53 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
     if (e == cudaSuccess) e = cudaMemcpyAsync(out_layers, res, size_t(values) * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "path tracer");
+    return read_error_word(dev, s);
+}
+
+int sel_vcm_settings_defaults(SelVcmSettings* out) {
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    *out = default_vcm_settings();
+    return SEL_OK;
+}
+
+int sel_vcm_render_device(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, double* d_accum,
+                          void* stream) {
+    if (int rc = check_vcm_args(scene, camera, settings)) return rc;
+    if (!d_accum || (reinterpret_cast<uintptr_t>(d_accum) & 7u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_accum must be an 8-byte aligned device pointer");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    return vcm_render_device(scene, *camera, *settings, d_accum, static_cast<cudaStream_t>(stream));
+}
+
+int sel_vcm_generate_image(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, float* out_rgb) {
+    if (int rc = check_vcm_args(scene, camera, settings)) return rc;
+    if (!out_rgb) return fail(SEL_ERR_INVALID_ARGUMENT, "out_rgb is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    SelDeviceTy* dev = scene->dev;
+    std::lock_guard<std::mutex> dlock(dev->mu);
+    cudaStream_t s = dev->stream;
+    const uint32_t values = camera->width * camera->height * 3u;
+    const size_t accum_bytes = size_t(values) * sizeof(double);
+    const size_t need = accum_bytes + size_t(values) * sizeof(float);
+    if (scene->accum_bytes < need) {
+        if (scene->d_accum) cudaFree(scene->d_accum);
+        scene->d_accum = nullptr;
+        scene->accum_bytes = 0;
+        cudaError_t e = cudaMalloc(&scene->d_accum, need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(accumulator)");
+        scene->accum_bytes = need;
+    }
+    double* acc = static_cast<double*>(scene->d_accum);
+    float* res = reinterpret_cast<float*>(static_cast<char*>(scene->d_accum) + accum_bytes);
+    cudaError_t e = cudaMemsetAsync(acc, 0, accum_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(accumulator)");
+    if (int rc = vcm_render_device(scene, *camera, *settings, acc, s)) return rc;
+    e = pt_resolve(acc, values, 1.0 / double(settings->passes), res, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_rgb, res, size_t(values) * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "VCM");
     return read_error_word(dev, s);
 }
 

@@ -151,16 +151,15 @@ SEL_HD void orthonormal_basis(float3 v1, float3& v2, float3& v3) {
 
 
 // CalculateSurfaceParams (Shading/SurfaceParameters.cpp:144-247) for meshes without shading normals,
-// tangents or uvs: frame from the normalised geometric normal, base colour raised to the power 2.2.
-SEL_HD Surface make_surface(const MaterialDev& m, float3 ng, float3 view, float3 base_color_authored) {
+// tangents or uvs, from the unit geometric normal n and the linear base colour.
+SEL_HD Surface make_surface_linear(const MaterialDev& m, float3 n, float3 view, float3 base_color_linear) {
     Surface s;
-    const float3 n = normalize(ng);
     float3 t, b;
     orthonormal_basis(n, t, b);
     s.t = t;
     s.n = n;
     s.b = b;
-    s.base_color = pow3(base_color_authored, 2.2f);
+    s.base_color = base_color_linear;
     s.transmittance_color = ld3(m.transmittance_color);
     s.sheen = m.sheen;
     s.sheen_tint = m.sheen_tint;
@@ -178,6 +177,17 @@ SEL_HD Surface make_surface(const MaterialDev& m, float3 ng, float3 view, float3
     s.shader = m.shader;
     s.relative_ior = ((m.flags & kMaterialTransparent) && dot(view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
     return s;
+}
+
+// The same from a hit: frame from the normalised geometric normal, authored base colour raised to the
+// power 2.2.
+SEL_HD Surface make_surface(const MaterialDev& m, float3 ng, float3 view, float3 base_color_authored) {
+    return make_surface_linear(m, normalize(ng), view, pow3(base_color_authored, 2.2f));
+}
+
+// ContinuationProbability (SurfaceParameters.cpp:420-424)
+SEL_HD float continuation_probability(const Surface& s) {
+    return saturate(fmaxf(fmaxf(s.base_color.x, s.base_color.y), s.base_color.z));
 }
 
 // OffsetRayOrigin (SurfaceParameters.cpp:403-408)

@@ -1,0 +1,826 @@
+// Vertex connection and merging (Georgiev, Krivanek, Davidovic, Slusallek, "Implementing Vertex
+// Connection and Merging", 2012 technical report), the integrator of the reference's VCM.cpp:171-666 with
+// VCMCommon.cpp:37-112 and VCMHashGrid.cpp:15-155, on the reference's scene model: quad lights of light
+// set 0 that light sub-paths start from and next-event estimation samples, and that camera and BSDF rays do
+// not hit (so the emitter-hit strategy has weight zero: dVC = dVM = 0 at the emitter).
+//
+// One pass = N = width * height light paths and N camera paths:
+//   k_light     one thread per light path: emission, closest hits, a stored vertex per non-Dirac hit (fixed
+//               slots, max_len - 1 per path), light tracing to the camera (occlusion ray, FP64 splat), BSDF
+//               scattering.  The reference BSDF is not reciprocal, so every evaluation is oriented
+//               f(v = camera side, l = light side) and a light sub-path's sampled weight is corrected by
+//               f(d, view) / f(view, d) (VCM.cpp:304-319,387 orient the connections the same way).
+//   grid        bounds of the stored vertices (widened by the radius), compaction in path order, a stable
+//               LSD radix sort of (cell, slot) pairs by cell and per-cell ranges: the vertices of a cell
+//               are visited in path order, as a sequential counting sort (VCMHashGrid.cpp:48-96) leaves them.
+//   k_camera    one thread per camera path: closest hits; per non-Dirac vertex next-event estimation, a
+//               connection to every vertex of the light path with the same index, and merging with the
+//               vertices in the 2x2x2 cells around it (VCMHashGrid.cpp:107-155); BSDF scattering.
+//
+// Random numbers: PCG32, stream (2 * pass) * N + p for light path p and (2 * pass + 1) * N + p for
+// camera path p, consumed as: light [light pick, u, v, r0, r1], per bounce [4 drawn ahead for the BSDF
+// sample, advanced by the number used, Russian roulette]; camera [jitter x, y], per vertex [light pick, u,
+// v], [BSDF sample], [Russian roulette].
+#include "vcm.h"
+
+#include <algorithm>
+#include <cstring>
+
+#include "capi_internal.h"
+#include "ptex.cuh"
+#include "shading.cuh"
+#include "traverse.cuh"
+
+namespace sel {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr float kFloatMax = 3.402823466e+38f;
+constexpr int kScanTile = 2048;  // 256 threads x 8
+constexpr int kSortTile = 4096;  // 256 threads x 16
+constexpr int kBoundsBlocks = 256;
+
+struct VcmParams {
+    const uint4* nodes;
+    const float4* tris;
+    const MaterialDev* materials;
+    uint32_t material_count;
+    const QuadLight* lights;  // light set 0
+    uint32_t light_count;
+    const PtexFace* ptex_faces;
+    const __half* ptex_texels;
+    uint32_t ptex_face_count;
+    CameraDev cam;
+    float image_plane;
+    uint32_t width, height, npaths, max_len, slots;
+    uint64_t seed;
+    int merging;
+    double* accum;
+    VcmState st;
+    const uint32_t* sorted_index;  // vertex slots sorted by cell (the last radix pass's output)
+    uint32_t* err;
+};
+
+// A shading point of a sub-path.
+struct VHit {
+    float3 pos, n, view;
+    float err, cont;
+    Surface s;
+    uint32_t mat;
+    bool delta, transparent;
+};
+
+struct PathState {
+    float3 org, dir, thr;
+    float dvcm, dvc, dvm;
+    uint32_t len;
+};
+
+// Stored light vertex: 80 bytes.
+struct LightVertex {
+    float3 pos, n, view, thr, base;
+    float dvcm, dvc, dvm;
+    uint32_t len, mat;
+};
+
+__device__ __forceinline__ void store_vertex(float4* v, const VHit& h, const PathState& st) {
+    v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, __uint_as_float(st.len));
+    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(h.mat));
+    v[2] = make_float4(h.view.x, h.view.y, h.view.z, st.dvcm);
+    v[3] = make_float4(st.thr.x, st.thr.y, st.thr.z, st.dvc);
+    v[4] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, st.dvm);
+}
+
+__device__ __forceinline__ LightVertex load_vertex(const float4* v) {
+    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4];
+    LightVertex lv;
+    lv.pos = f3(a.x, a.y, a.z);
+    lv.len = __float_as_uint(a.w);
+    lv.n = f3(b.x, b.y, b.z);
+    lv.mat = __float_as_uint(b.w);
+    lv.view = f3(c.x, c.y, c.z);
+    lv.dvcm = c.w;
+    lv.thr = f3(d.x, d.y, d.z);
+    lv.dvc = d.w;
+    lv.base = f3(e.x, e.y, e.z);
+    lv.dvm = e.w;
+    return lv;
+}
+
+// Closest hit from org along dir and the surface there (CalculateSurfaceParams as the path tracer uses it).
+__device__ bool vcm_hit(const VcmParams& P, float3 org, float3 dir, VHit& h, uint2* stack, uint32_t& status) {
+    QueryRay q;
+    q.ox = org.x; q.oy = org.y; q.oz = org.z; q.tnear = 0.0f;
+    q.dx = dir.x; q.dy = dir.y; q.dz = dir.z; q.tfar = kFloatMax;
+    QueryHit qh;
+    if (!trace_wide<false>(P.nodes, P.tris, q, qh, stack, kBlock, status)) return false;
+    const float4* tp = P.tris + size_t(qh.tri) * 3;
+    const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+    const uint32_t geom = __float_as_uint(p1.w);
+    const uint32_t mi = geom < P.material_count ? geom : 0;
+    const MaterialDev& m = P.materials[mi];
+    h.pos = f3(org.x + qh.t * dir.x, org.y + qh.t * dir.y, org.z + qh.t * dir.z);
+    h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), qh.t));
+    float3 base = ld3(m.base_color);
+    if (m.flags & kMaterialUsesPtex) {
+        uint32_t pstatus = 0;
+        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
+                  qh.u, qh.v, base, pstatus);
+        status |= pstatus;
+    }
+    h.view = -dir;
+    h.s = make_surface(m, triangle_ng(p0, p1, p2), h.view, base);
+    h.n = h.s.n;
+    h.cont = continuation_probability(h.s);
+    h.mat = mi;
+    h.delta = m.shader == kDiracTransparent;
+    h.transparent = (m.flags & kMaterialTransparent) != 0u;
+    return true;
+}
+
+// Visibility of a segment from a hit: origin offset 0.1 x the hit's error bound, tnear = the error bound
+// (OcclusionRay, PathTracer.cpp:71-92).
+__device__ __forceinline__ bool visible(const VcmParams& P, const VHit& h, float3 dir, float tfar, uint2* stack,
+                                        uint32_t& status) {
+    const float3 o = offset_origin(h.pos, h.n, h.err, dir, 0.1f);
+    QueryRay q;
+    q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = h.err;
+    q.dx = dir.x; q.dy = dir.y; q.dz = dir.z; q.tfar = tfar;
+    QueryHit qh;
+    return !trace_wide<true>(P.nodes, P.tris, q, qh, stack, kBlock, status);
+}
+
+__device__ __forceinline__ bool nonzero(float3 a) { return a.x != 0.0f || a.y != 0.0f || a.z != 0.0f; }
+
+// BSDF sampling, Russian roulette and the partial MIS weights (VCM.cpp:412-444; tech report eq. 38-40).
+__device__ bool scatter(Pcg32& rng, const VHit& h, const VcmConsts& c, PathState& st, bool light_path) {
+    float u4[4];
+    Pcg32 ahead = rng;
+    for (int k = 0; k < 4; ++k) u4[k] = pcg_float(ahead);
+    int used = 0;
+    BsdfSampleOut bs;
+    const bool ok = bsdf_sample(h.s, h.view, u4, used, bs);
+    for (int k = 0; k < used; ++k) pcg_next(rng);
+    if (!ok) return false;
+    if (!nonzero(bs.reflectance)) return false;
+    if (pcg_float(rng) > h.cont) return false;
+    float3 weight = bs.reflectance;
+    if (light_path && !h.delta && !(bs.flags & kDiracEvent)) {
+        float a0, a1, b0, b1;
+        const float3 adj = bsdf_evaluate(h.s, bs.wi, h.view, a0, a1);  // f(d, view) |cos view|
+        const float3 fw = bsdf_evaluate(h.s, h.view, bs.wi, b0, b1);   // f(view, d) |cos d|
+        const float cv = fabsf(dot(h.n, h.view)), cd = fabsf(dot(h.n, bs.wi));
+        const float k = cv > 0.0f ? cd / cv : 0.0f;
+        weight.x = (adj.x > 0.0f && fw.x > 0.0f) ? bs.reflectance.x * (adj.x * k / fw.x) : bs.reflectance.x;
+        weight.y = (adj.y > 0.0f && fw.y > 0.0f) ? bs.reflectance.y * (adj.y * k / fw.y) : bs.reflectance.y;
+        weight.z = (adj.z > 0.0f && fw.z > 0.0f) ? bs.reflectance.z * (adj.z * k / fw.z) : bs.reflectance.z;
+    }
+    const float fwd = bs.forward_pdf * h.cont, rev = bs.reverse_pdf * h.cont;
+    const float cos_out = fabsf(dot(bs.wi, h.n));
+    if (h.delta) {
+        st.dvcm = 0.0f;
+        st.dvc *= cos_out;
+        st.dvm *= cos_out;
+    } else {
+        st.dvc = (cos_out / fwd) * (st.dvc * rev + st.dvcm + c.vm_weight);
+        st.dvm = (cos_out / fwd) * (st.dvm * rev + st.dvcm * c.vc_weight + 1.0f);
+        st.dvcm = 1.0f / fwd;
+    }
+    st.thr = st.thr * weight * (1.0f / h.cont);
+    st.org = offset_origin(h.pos, h.n, h.err, bs.wi, 1.0f);
+    st.dir = bs.wi;
+    st.len += 1;
+    return true;
+}
+
+// World position -> pixel, the inverse of ImageToWorldDirection (GeometryLib/Camera.cpp:56-60).
+__device__ __forceinline__ bool to_pixel(const CameraDev& cam, float3 p, int& px, int& py) {
+    const float3 d = p - cam.position;
+    const float dz = dot(d, cam.z);
+    if (dz <= 0.0f) return false;
+    const float cx = -dot(d, cam.x) / (dz * dot(cam.x, cam.x));
+    const float cy = dot(d, cam.y) / (dz * dot(cam.y, cam.y));
+    const float fx = (cx + 1.0f) * 0.5f * cam.width, fy = (1.0f - cy) * 0.5f * cam.height;
+    if (!(fx >= 0.0f && fx < cam.width && fy >= 0.0f && fy < cam.height)) return false;
+    px = int(fx);
+    py = int(fy);
+    return true;
+}
+
+__device__ __forceinline__ void splat(double* accum, uint32_t pixel, float3 c) {
+    double* p = accum + size_t(pixel) * 3;
+    atomicAdd(p, double(c.x));
+    atomicAdd(p + 1, double(c.y));
+    atomicAdd(p + 2, double(c.z));
+}
+
+// Light sub-paths (GenerateLightSample + EvaluateLightPaths, VCM.cpp:493-561; VCMCommon.cpp:37-62 for an
+// area emitter: uniform point on the quad, cosine-weighted direction about its facing direction).
+__global__ void __launch_bounds__(kBlock) k_light(VcmParams P) {
+    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    uint2* stack = stack_mem + threadIdx.x;
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t N = P.npaths;
+    uint32_t status = 0;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+        uint32_t stored = 0;
+        float4* slots = P.st.verts + size_t(p) * P.slots * 5;
+        if (P.light_count > 0) {
+            Pcg32 rng = pcg_seed(P.seed, (uint64_t(c.pass) * 2 + 0) * N + p);
+            const float pick = pcg_float(rng);
+            uint32_t li = uint32_t(pick * float(P.light_count));
+            li = li < P.light_count - 1 ? li : P.light_count - 1;
+            const QuadLight L = P.lights[li];
+            const float u = pcg_float(rng), v = pcg_float(rng);
+            const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+            const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+            const float3 ln = normalize(L.direction);
+            float3 lt, lb;
+            orthonormal_basis(ln, lt, lb);
+            const float r0 = pcg_float(rng), r1 = pcg_float(rng);
+            const float rr = sqrtf(r0), ph = 2.0f * kPi * r1;
+            const float cosl = sqrtf(fmaxf(0.0f, 1.0f - r0));
+            const float3 dir = normalize(rr * cosf(ph) * lt + cosl * ln + rr * sinf(ph) * lb);
+            if (cosl > 0.0f) {
+                const float light_pick = 1.0f / float(P.light_count);
+                const float emission_pdf = pdf_a * cosl / kPi * light_pick;
+                const float direct_pdf_a = pdf_a * light_pick;
+                PathState st;
+                st.org = lp;
+                st.dir = dir;
+                st.thr = L.radiance * (cosl / emission_pdf);
+                st.dvcm = direct_pdf_a / emission_pdf;
+                st.dvc = 0.0f;
+                st.dvm = 0.0f;
+                st.len = 1;
+                while (st.len + 2 <= P.max_len + 1) {
+                    VHit h;
+                    if (!vcm_hit(P, st.org, st.dir, h, stack, status)) break;
+                    const float3 seg = h.pos - st.org;
+                    const float d2 = dot(seg, seg);
+                    const float cos_in = fabsf(dot(h.n, h.view));
+                    st.dvcm *= d2;
+                    st.dvcm *= 1.0f / cos_in;
+                    st.dvc *= 1.0f / cos_in;
+                    st.dvm *= 1.0f / cos_in;
+                    if (!h.delta) {
+                        store_vertex(slots + size_t(stored) * 5, h, st);
+                        ++stored;
+                        // light tracing: connect to the camera (ConnectLightPathToCamera, VCM.cpp:190-233;
+                        // tech report sec. 5.3)
+                        int px, py;
+                        if (st.len + 1 <= P.max_len && to_pixel(P.cam, h.pos, px, py)) {
+                            float3 to_cam = P.cam.position - h.pos;
+                            const float dist2 = dot(to_cam, to_cam);
+                            const float dist = sqrtf(dist2);
+                            to_cam = to_cam * (1.0f / dist);
+                            const float cos_cam = dot(P.cam.z, -to_cam);
+                            float cam_side_pdf, light_side_pdf;
+                            const float3 fa = bsdf_evaluate(h.s, to_cam, h.view, cam_side_pdf, light_side_pdf);
+                            const float cos_view = fabsf(dot(h.n, h.view));
+                            const float3 f = cos_view > 0.0f ? fa * (fabsf(dot(h.n, to_cam)) / cos_view) : f3(0.0f);
+                            float rev = cam_side_pdf;
+                            if (nonzero(f) && cos_cam > 0.0f) {
+                                rev *= h.cont;
+                                const float ip = P.image_plane / cos_cam;
+                                const float img_to_solid = ip * ip / cos_cam;
+                                const float cos_surf = fabsf(dot(h.n, to_cam));
+                                const float camera_pdf_a = img_to_solid * cos_surf / dist2;
+                                const float w_light = (camera_pdf_a / c.n_paths) * (c.vm_weight + st.dvcm + st.dvc * rev);
+                                const float mis = 1.0f / (w_light + 1.0f);
+                                const float3 contrib = (mis * img_to_solid / (c.n_paths * dist2)) * (st.thr * f);
+                                if (visible(P, h, to_cam, dist * (1.0f - 1e-4f), stack, status))
+                                    splat(P.accum, uint32_t(py) * P.width + uint32_t(px), contrib);
+                            }
+                        }
+                    }
+                    if (st.len + 2 > P.max_len) break;
+                    if (!scatter(rng, h, c, st, true)) break;
+                }
+            }
+        }
+        P.st.vcount[p] = stored;
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Hash grid (VCMHashGrid.cpp:48-96): bounds, compaction, radix sort by cell, cell ranges.
+// ---------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, uint32_t cells) {
+    const uint32_t ux = uint32_t(x), uy = uint32_t(y), uz = uint32_t(z);
+    return ((ux * 73856093u) ^ (uy * 19349663u) ^ (uz * 83492791u)) % cells;
+}
+
+// Bounds of all stored vertices: per-block partials (min x y z, max x y z), then one block reduces them,
+// widens the box by the radius (the correction VCMHashGrid.cpp:69-72 leaves commented out: without it a
+// vertex on a bounding plane of the vertex set fails the range test about half the time) and writes the
+// grid header.
+__global__ void __launch_bounds__(256) k_bounds(VcmParams P) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.npaths; p += gridDim.x * blockDim.x) {
+        const uint32_t n = P.st.vcount[p];
+        const float4* v = P.st.verts + size_t(p) * P.slots * 5;
+        for (uint32_t k = 0; k < n; ++k) {
+            const float4 a = v[size_t(k) * 5];
+            mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
+            mx[0] = fmaxf(mx[0], a.x); mx[1] = fmaxf(mx[1], a.y); mx[2] = fmaxf(mx[2], a.z);
+        }
+    }
+    __shared__ float red[6][8];
+    for (int i = 0; i < 3; ++i) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[i] = fminf(mn[i], __shfl_xor_sync(0xffffffffu, mn[i], o));
+            mx[i] = fmaxf(mx[i], __shfl_xor_sync(0xffffffffu, mx[i], o));
+        }
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int i = 0; i < 3; ++i) { red[i][w] = mn[i]; red[3 + i][w] = mx[i]; }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        float r = red[threadIdx.x][0];
+        for (int k = 1; k < 8; ++k) r = threadIdx.x < 3 ? fminf(r, red[threadIdx.x][k]) : fmaxf(r, red[threadIdx.x][k]);
+        P.st.bounds_part[blockIdx.x * 6 + threadIdx.x] = r;
+    }
+}
+
+__global__ void k_bounds_final(VcmParams P, int parts) {
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    if (threadIdx.x < 6) {
+        float r = P.st.bounds_part[threadIdx.x];
+        for (int k = 1; k < parts; ++k) {
+            const float x = P.st.bounds_part[k * 6 + threadIdx.x];
+            r = threadIdx.x < 3 ? fminf(r, x) : fmaxf(r, x);
+        }
+        P.st.grid[threadIdx.x] = threadIdx.x < 3 ? r - c.radius : r + c.radius;
+    }
+    if (threadIdx.x == 0) {
+        P.st.grid[6] = 1.0f / (2.0f * c.radius);
+        P.st.grid[7] = c.radius * c.radius;
+        P.st.grid[9] = __uint_as_float(P.npaths);
+    }
+}
+
+// Exclusive scan of n u32 values, three kernels: tile sums, scan of the tile sums (one block), tiles.
+__device__ __forceinline__ uint32_t block_exclusive_scan_256(uint32_t x, uint32_t* warp_sums, uint32_t& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = x;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_sums[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t s = lane < 8 ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < 8) warp_sums[lane] = s;  // inclusive
+    }
+    __syncthreads();
+    total = warp_sums[7];
+    const uint32_t before = w > 0 ? warp_sums[w - 1] : 0u;
+    __syncthreads();
+    return before + inc - x;
+}
+
+__global__ void __launch_bounds__(256) k_scan_tiles(const uint32_t* in, uint32_t n, uint32_t* tile_sums) {
+    const size_t base = size_t(blockIdx.x) * kScanTile;
+    uint32_t s = 0;
+    for (int k = 0; k < kScanTile / 256; ++k) {
+        const size_t i = base + size_t(k) * 256 + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ uint32_t ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int k = 0; k < 8; ++k) t += ws[k];
+        tile_sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_scan_top(uint32_t* tile_sums, uint32_t ntiles) {
+    __shared__ uint32_t ws[8];
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < ntiles; base += 256) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t x = i < ntiles ? tile_sums[i] : 0u;
+        uint32_t total;
+        const uint32_t ex = block_exclusive_scan_256(x, ws, total);
+        if (i < ntiles) tile_sums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+// out[0..n) = exclusive scan of in, out[n] = total.  in and out may alias.
+__global__ void __launch_bounds__(256) k_scan_apply(const uint32_t* in, uint32_t n, const uint32_t* tile_sums,
+                                                    uint32_t* out, uint32_t ntiles) {
+    __shared__ uint32_t tile[kScanTile];
+    __shared__ uint32_t ws[8];
+    const size_t base = size_t(blockIdx.x) * kScanTile;
+    for (int k = 0; k < kScanTile / 256; ++k) {
+        const size_t i = base + size_t(k) * 256 + threadIdx.x;
+        tile[k * 256 + threadIdx.x] = i < n ? in[i] : 0u;
+    }
+    __syncthreads();
+    constexpr int kPer = kScanTile / 256;
+    uint32_t loc[kPer];
+    uint32_t s = 0;
+    for (int k = 0; k < kPer; ++k) {
+        loc[k] = tile[threadIdx.x * kPer + k];
+        s += loc[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan_256(s, ws, total) + tile_sums[blockIdx.x];
+    for (int k = 0; k < kPer; ++k) {
+        tile[threadIdx.x * kPer + k] = run;
+        run += loc[k];
+    }
+    __syncthreads();
+    for (int k = 0; k < kScanTile / 256; ++k) {
+        const size_t i = base + size_t(k) * 256 + threadIdx.x;
+        if (i < n) out[i] = tile[k * 256 + threadIdx.x];
+    }
+    if (blockIdx.x == ntiles - 1 && threadIdx.x == 0) out[n] = tile_sums[blockIdx.x] + total;
+}
+
+void scan_exclusive(const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* tmp, cudaStream_t s) {
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<ntiles, 256, 0, s>>>(in, n, tmp);
+    k_scan_top<<<1, 256, 0, s>>>(tmp, ntiles);
+    k_scan_apply<<<ntiles, 256, 0, s>>>(in, n, tmp, out, ntiles);
+}
+
+__device__ __forceinline__ uint32_t cell_of(const float* grid, float3 p, uint32_t cells) {
+    const float inv = grid[6];
+    const float3 f = p - f3(grid[0], grid[1], grid[2]);
+    return cell_hash(int(floorf(inv * f.x)), int(floorf(inv * f.y)), int(floorf(inv * f.z)), cells);
+}
+
+// Compacted (cell, slot) pairs in path order, and the number of vertices per cell.
+__global__ void __launch_bounds__(256) k_keys(VcmParams P) {
+    const uint32_t cells = P.npaths;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.npaths; p += gridDim.x * blockDim.x) {
+        const uint32_t n = P.st.vcount[p], at = P.st.vpos[p];
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t slot = p * P.slots + k;
+            const float4 a = P.st.verts[size_t(slot) * 5];
+            const uint32_t cell = cell_of(P.st.grid, f3(a.x, a.y, a.z), cells);
+            P.st.keys[0][at + k] = cell;
+            P.st.vals[0][at + k] = slot;
+            atomicAdd(&P.st.cell_count[cell], 1u);
+        }
+    }
+}
+
+// One pass of a stable LSD radix sort, 8-bit digits, tiles of kSortTile keys.
+__global__ void __launch_bounds__(256) k_radix_hist(const uint32_t* keys, const uint32_t* total_ptr, int shift,
+                                                    uint32_t* hist, uint32_t ntiles) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t total = *total_ptr;
+    const size_t base = size_t(blockIdx.x) * kSortTile;
+    for (int k = 0; k < kSortTile / 256; ++k) {
+        const size_t i = base + size_t(k) * 256 + threadIdx.x;
+        if (i < total) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[size_t(threadIdx.x) * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t* keys_in, const uint32_t* vals_in,
+                                                       uint32_t* keys_out, uint32_t* vals_out,
+                                                       const uint32_t* total_ptr, int shift, const uint32_t* offsets,
+                                                       uint32_t ntiles) {
+    __shared__ uint32_t tile_base[256];
+    __shared__ uint32_t chunk_count[256];
+    __shared__ uint32_t warp_hist[8][256];
+    const uint32_t total = *total_ptr;
+    tile_base[threadIdx.x] = offsets[size_t(threadIdx.x) * ntiles + blockIdx.x];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const size_t base = size_t(blockIdx.x) * kSortTile;
+    for (int chunk = 0; chunk < kSortTile / 256; ++chunk) {
+        for (int k = 0; k < 8; ++k) warp_hist[k][threadIdx.x] = 0;
+        __syncthreads();
+        const size_t i = base + size_t(chunk) * 256 + threadIdx.x;
+        const bool valid = i < total;
+        const uint32_t key = valid ? keys_in[i] : 0u;
+        const uint32_t digit = (key >> shift) & 255u;
+        // lanes with the same digit, in lane order; invalid lanes match nobody
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? digit : 256u + uint32_t(lane));
+        const uint32_t rank = __popc(peers & lt_mask);
+        if (valid && rank == 0) warp_hist[w][digit] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = 0;
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t cnt = warp_hist[k][threadIdx.x];
+                warp_hist[k][threadIdx.x] = run;
+                run += cnt;
+            }
+            chunk_count[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t dst = tile_base[digit] + warp_hist[w][digit] + rank;
+            keys_out[dst] = key;
+            vals_out[dst] = vals_in[i];
+        }
+        __syncthreads();
+        tile_base[threadIdx.x] += chunk_count[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Camera sub-paths (GenerateCameraPaths + EvaluateCameraPaths, VCM.cpp:563-666).
+// ---------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_camera(VcmParams P) {
+    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    uint2* stack = stack_mem + threadIdx.x;
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t N = P.npaths;
+    const float* grid = P.st.grid;
+    const uint32_t total_vertices = P.st.vpos[N];
+    const float3 glo = f3(grid[0], grid[1], grid[2]), ghi = f3(grid[3], grid[4], grid[5]);
+    const float ginv = grid[6], gr2 = grid[7];
+    const uint32_t* cell_start = P.st.cell_start;
+    uint32_t status = 0;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+        Pcg32 rng = pcg_seed(P.seed, (uint64_t(c.pass) * 2 + 1) * N + p);
+        const uint32_t y = p / P.width, x = p - y * P.width;
+        const float vx = float(x) + pcg_float(rng), vy = float(y) + pcg_float(rng);
+        const float3 d = camera_direction(P.cam, vx, vy);
+        const float cos_cam = dot(P.cam.z, d);
+        const float ip = P.image_plane / cos_cam;
+        const float camera_pdf_w = ip * ip / cos_cam;
+        PathState st;
+        st.org = P.cam.position;
+        st.dir = d;
+        st.thr = f3(1.0f);
+        st.dvcm = c.n_paths / camera_pdf_w;
+        st.dvc = 0.0f;
+        st.dvm = 0.0f;
+        st.len = 1;
+        float3 color = f3(0.0f);
+        const uint32_t lcount = P.st.vcount[p];
+        const float4* lslots = P.st.verts + size_t(p) * P.slots * 5;
+        for (;;) {
+            VHit h;
+            if (!vcm_hit(P, st.org, st.dir, h, stack, status)) break;
+            const float3 seg = h.pos - st.org;
+            const float d2 = dot(seg, seg);
+            const float cos_in = fabsf(dot(h.n, h.view));
+            st.dvcm *= d2;
+            st.dvcm *= 1.0f / cos_in;
+            st.dvc *= 1.0f / cos_in;
+            st.dvm *= 1.0f / cos_in;
+            if (!h.delta) {
+                // next-event estimation to light set 0 (tech report sec. 5.4)
+                if (st.len + 1 <= P.max_len && P.light_count > 0) {
+                    const float pick = pcg_float(rng);
+                    uint32_t li = uint32_t(pick * float(P.light_count));
+                    li = li < P.light_count - 1 ? li : P.light_count - 1;
+                    const QuadLight L = P.lights[li];
+                    const float u = pcg_float(rng), v = pcg_float(rng);
+                    const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                    const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                    float3 to_l = lp - h.pos;
+                    const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
+                    to_l = to_l * (1.0f / dl);
+                    const float cos_light = dot(normalize(L.direction), -to_l);
+                    if (cos_light > 0.0f) {
+                        float fwd, rev;
+                        const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                        if (nonzero(f)) {
+                            rev *= h.cont;
+                            const float light_pick = 1.0f / float(P.light_count);
+                            const float direct_pdf_w = pdf_a * dl2 / cos_light;
+                            const float emission_pdf_w = pdf_a * cos_light / kPi;
+                            const float cos_to_light = fabsf(dot(h.n, to_l));
+                            const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
+                                                   (c.vm_weight + st.dvcm + st.dvc * rev);
+                            const float mis = 1.0f / (1.0f + w_camera);
+                            const float3 contrib = (mis / (light_pick * direct_pdf_w)) * (L.radiance * f);
+                            if (visible(P, h, to_l, dl * (1.0f - 1e-4f), stack, status)) color = color + st.thr * contrib;
+                        }
+                    }
+                }
+                // vertex connection to the vertices of light path p (ConnectPathVertices, VCM.cpp:293-359)
+                for (uint32_t k = 0; k < lcount; ++k) {
+                    const LightVertex lv = load_vertex(lslots + size_t(k) * 5);
+                    if (lv.len + 1 + st.len > P.max_len) break;
+                    float3 dir = lv.pos - h.pos;
+                    const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
+                    dir = dir * (1.0f / dist);
+                    float cfwd, crev, lfwd, lrev;
+                    const float3 cf = bsdf_evaluate(h.s, h.view, dir, cfwd, crev);
+                    if (!nonzero(cf)) continue;
+                    const MaterialDev& lm = P.materials[lv.mat];
+                    const Surface ls = make_surface_linear(lm, lv.n, lv.view, lv.base);
+                    const float lcont = continuation_probability(ls);
+                    const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
+                    const float lcos_view = fabsf(dot(lv.n, lv.view));
+                    const float3 lf = lcos_view > 0.0f ? lfa * (fabsf(dot(lv.n, dir)) / lcos_view) : f3(0.0f);
+                    if (!nonzero(lf)) continue;
+                    cfwd *= h.cont; crev *= h.cont;
+                    lfwd *= lcont; lrev *= lcont;
+                    const float cos_cam_v = fabsf(dot(dir, h.n));
+                    const float cos_light_v = fabsf(dot(-dir, lv.n));
+                    const float cam_pdf_a = cfwd * cos_light_v / dist2;
+                    const float light_pdf_a = lfwd * cos_cam_v / dist2;
+                    const float w_light = cam_pdf_a * (c.vm_weight + lv.dvcm + lv.dvc * lrev);
+                    const float w_camera = light_pdf_a * (c.vm_weight + st.dvcm + st.dvc * crev);
+                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                    const float3 contrib = (mis / dist2) * (cf * lf);
+                    const float bias = 0.1f * h.err;
+                    if (visible(P, h, dir, dist - 16.0f * bias, stack, status)) color = color + st.thr * lv.thr * contrib;
+                }
+                // vertex merging (MergeVertices + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155)
+                float3 merged = f3(0.0f);
+                const float3 dmin = h.pos - glo, dmax = ghi - h.pos;
+                if (P.merging && total_vertices > 0 && dmin.x >= 0.0f && dmin.y >= 0.0f && dmin.z >= 0.0f &&
+                    dmax.x >= 0.0f && dmax.y >= 0.0f && dmax.z >= 0.0f) {
+                    const uint32_t* idx = P.sorted_index;
+                    const float3 cp = ginv * dmin;
+                    const float fx = floorf(cp.x), fy = floorf(cp.y), fz = floorf(cp.z);
+                    const int x0 = int(fx) - (cp.x - fx < 0.5f ? 1 : 0);
+                    const int y0 = int(fy) - (cp.y - fy < 0.5f ? 1 : 0);
+                    const int z0 = int(fz) - (cp.z - fz < 0.5f ? 1 : 0);
+                    for (int dz = 0; dz <= 1; ++dz)
+                        for (int dy = 0; dy <= 1; ++dy)
+                            for (int dx = 0; dx <= 1; ++dx) {
+                                const uint32_t cell = cell_hash(x0 + dx, y0 + dy, z0 + dz, N);
+                                const uint32_t b = cell_start[cell], e = cell_start[cell + 1];
+                                for (uint32_t k = b; k < e; ++k) {
+                                    const float4* vp = P.st.verts + size_t(idx[k]) * 5;
+                                    const float4 a = vp[0];
+                                    const float3 dd = h.pos - f3(a.x, a.y, a.z);
+                                    if (dot(dd, dd) > gr2) continue;
+                                    const LightVertex lv = load_vertex(vp);
+                                    if (st.len + lv.len > P.max_len) continue;
+                                    const MaterialDev& lm = P.materials[lv.mat];
+                                    // the reference merges only between surfaces of the same transparency
+                                    // (VCM.cpp:372-375)
+                                    if (h.transparent != ((lm.flags & kMaterialTransparent) != 0u)) continue;
+                                    float fwd, rev;
+                                    const float3 fc = bsdf_evaluate(h.s, h.view, lv.view, fwd, rev);
+                                    const float cosl = fabsf(dot(h.n, lv.view));
+                                    if (!nonzero(fc) || cosl == 0.0f) continue;
+                                    const float lcont = saturate(max3(lv.base));
+                                    fwd *= h.cont;
+                                    rev *= lcont;
+                                    const float w_light = lv.dvcm * c.vc_weight + lv.dvm * fwd;
+                                    const float w_camera = st.dvcm * c.vc_weight + st.dvm * rev;
+                                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                                    merged = merged + (mis / cosl) * (fc * lv.thr);
+                                }
+                            }
+                }
+                color = color + c.vm_norm * (st.thr * merged);
+            }
+            if (st.len >= P.max_len) break;
+            if (!scatter(rng, h, c, st, false)) break;
+        }
+        double* px = P.accum + size_t(p) * 3;
+        px[0] += double(color.x);
+        px[1] += double(color.y);
+        px[2] += double(color.z);
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+__global__ void k_pass_end(uint32_t* iter) {
+    if (threadIdx.x == 0) *iter += 1u;
+}
+
+}  // namespace
+
+VcmState vcm_state_carve(void* block, uint32_t paths, uint32_t max_len, uint32_t passes) {
+    char* p = static_cast<char*>(block);
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    const uint32_t slots = max_len - 1;
+    const size_t nv = size_t(paths) * slots;
+    const uint32_t ntiles = uint32_t((nv + kSortTile - 1) / kSortTile);
+    const size_t scan_n = std::max<size_t>(std::max<size_t>(paths + 1, size_t(256) * ntiles), 1);
+    VcmState st;
+    st.verts = reinterpret_cast<float4*>(take(80 * nv));
+    st.vcount = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.vpos = reinterpret_cast<uint32_t*>(take(4ull * (paths + 1)));
+    for (int k = 0; k < 2; ++k) {
+        st.keys[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
+        st.vals[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
+    }
+    st.cell_count = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.cell_start = reinterpret_cast<uint32_t*>(take(4ull * (paths + 1)));
+    st.hist = reinterpret_cast<uint32_t*>(take(4ull * 256 * ntiles));
+    st.hist_off = reinterpret_cast<uint32_t*>(take(4ull * (256 * size_t(ntiles) + 1)));
+    st.scan_tmp = reinterpret_cast<uint32_t*>(take(4 * ((scan_n + kScanTile - 1) / kScanTile + 1)));
+    st.bounds_part = reinterpret_cast<float*>(take(4 * 6 * kBoundsBlocks));
+    st.grid = reinterpret_cast<float*>(take(4 * 16));
+    st.iter = reinterpret_cast<uint32_t*>(take(4 * 4));
+    st.consts = reinterpret_cast<VcmConsts*>(take(sizeof(VcmConsts) * passes));
+    st.paths = paths;
+    st.slots_per_path = slots;
+    st.consts_capacity = passes;
+    return st;
+}
+
+size_t vcm_state_block_bytes(uint32_t paths, uint32_t max_len, uint32_t passes) {
+    auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t nv = size_t(paths) * (max_len - 1);
+    const size_t ntiles = (nv + kSortTile - 1) / kSortTile;
+    const size_t scan_n = std::max<size_t>(std::max<size_t>(paths + 1, 256 * ntiles), 1);
+    return r(80 * nv) + r(4ull * paths) + r(4ull * (paths + 1)) + 4 * r(4 * nv) + r(4ull * paths) +
+           r(4ull * (paths + 1)) + r(4 * 256 * ntiles) + r(4 * (256 * ntiles + 1)) +
+           r(4 * ((scan_n + kScanTile - 1) / kScanTile + 1)) + r(4 * 6 * kBoundsBlocks) + r(4 * 16) + r(4 * 4) +
+           r(sizeof(VcmConsts) * passes);
+}
+
+cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
+                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    VcmParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.nodes = sc.nodes;
+    P.tris = sc.tris;
+    P.materials = sc.materials;
+    P.material_count = sc.material_count;
+    P.lights = sc.lights;
+    P.light_count = 0;
+    P.ptex_faces = static_cast<const PtexFace*>(sc.ptex_faces);
+    P.ptex_texels = static_cast<const __half*>(sc.ptex_texels);
+    P.ptex_face_count = sc.ptex_face_count;
+    P.cam.x = make_float3(cam.cam.x[0], cam.cam.x[1], cam.cam.x[2]);
+    P.cam.y = make_float3(cam.cam.y[0], cam.cam.y[1], cam.cam.y[2]);
+    P.cam.z = make_float3(cam.cam.z[0], cam.cam.z[1], cam.cam.z[2]);
+    P.cam.position = make_float3(cam.cam.position[0], cam.cam.position[1], cam.cam.position[2]);
+    P.cam.width = float(cam.cam.width);
+    P.cam.height = float(cam.cam.height);
+    P.image_plane = cam.image_plane;
+    P.width = cam.cam.width;
+    P.height = cam.cam.height;
+    P.npaths = st.paths;
+    P.max_len = set.max_len;
+    P.slots = st.slots_per_path;
+    P.seed = set.seed;
+    P.merging = set.merging;
+    P.accum = d_accum;
+    P.st = st;
+    P.err = d_err;
+    P.lights = sc.lights + set.light_first;
+    P.light_count = set.light_count;
+
+    cudaError_t e = cudaMemcpyAsync(st.consts, host_consts, sizeof(VcmConsts) * passes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(st.iter, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    const uint32_t N = st.paths;
+    const size_t nv = size_t(N) * st.slots_per_path;
+    const uint32_t ntiles = uint32_t((nv + kSortTile - 1) / kSortTile);
+    int bits = 0;
+    while (bits < 32 && (uint64_t(N - 1) >> bits) != 0) ++bits;  // cells = N: keys below N
+    const int radix_passes = (bits + 7) / 8;
+    const int path_grid = sms * 8;
+    const uint32_t list_grid = std::min<uint32_t>((N + 255) / 256, uint32_t(sms) * 16);
+    int cur = 0;
+    for (int r = 0; r < radix_passes; ++r) cur ^= 1;
+    P.sorted_index = st.vals[cur];
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        k_light<<<path_grid, kBlock, 0, stream>>>(P);
+        k_bounds<<<kBoundsBlocks, 256, 0, stream>>>(P);
+        k_bounds_final<<<1, 32, 0, stream>>>(P, kBoundsBlocks);
+        scan_exclusive(st.vcount, N, st.vpos, st.scan_tmp, stream);
+        cudaMemsetAsync(st.cell_count, 0, sizeof(uint32_t) * N, stream);
+        k_keys<<<list_grid, 256, 0, stream>>>(P);
+        scan_exclusive(st.cell_count, N, st.cell_start, st.scan_tmp, stream);
+        int from = 0;
+        for (int r = 0; r < radix_passes; ++r) {
+            k_radix_hist<<<ntiles, 256, 0, stream>>>(st.keys[from], st.vpos + N, 8 * r, st.hist, ntiles);
+            scan_exclusive(st.hist, 256 * ntiles, st.hist_off, st.scan_tmp, stream);
+            k_radix_scatter<<<ntiles, 256, 0, stream>>>(st.keys[from], st.vals[from], st.keys[from ^ 1], st.vals[from ^ 1],
+                                                        st.vpos + N, 8 * r, st.hist_off, ntiles);
+            from ^= 1;
+        }
+        k_camera<<<path_grid, kBlock, 0, stream>>>(P);
+        k_pass_end<<<1, 32, 0, stream>>>(st.iter);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace sel

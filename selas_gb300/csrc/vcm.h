@@ -1,0 +1,65 @@
+// Host interface of the vertex connection and merging integrator (vcm.cu).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "pt.h"
+
+namespace sel {
+
+// Per-pass constants (VCMCommon.cpp:91-112), computed on the host for a range of passes so that every
+// pass launches the same kernels with the same arguments (a pass reads its row through a device counter).
+struct VcmConsts {
+    float radius, radius2;
+    float vm_weight;  // pi r^2 N without merging turned off, else 0
+    float vc_weight;  // 1 / (pi r^2 N)
+    float vm_norm;    // 1 / (pi r^2 N)
+    float n_paths;
+    uint32_t pass;    // global pass index: random streams and the radius schedule
+    uint32_t pad;
+};
+
+struct VcmSettings {
+    uint32_t max_len;  // maximum path length in segments (MaxBounceCount_)
+    uint64_t seed;
+    int merging;       // 0: bidirectional path tracing (no merge term, no merge weights)
+    uint32_t light_first, light_count;  // light set 0 within the scene's light array
+};
+
+// Device scratch of one VCM pass for `paths` light and camera paths (paths = width * height).
+struct VcmState {
+    float4* verts;        // light vertices, 5 x float4 each, max_len - 1 slots per light path
+    uint32_t* vcount;     // stored vertices per light path
+    uint32_t* vpos;       // exclusive scan of vcount (+ total)
+    uint32_t* keys[2];    // radix-sort ping-pong: cell of each stored vertex
+    uint32_t* vals[2];    // ... and its slot
+    uint32_t* cell_count; // vertices per cell
+    uint32_t* cell_start; // exclusive scan of cell_count (+ total)
+    uint32_t* hist;       // radix digit counts per tile (digit-major)
+    uint32_t* hist_off;   // their exclusive scan
+    uint32_t* scan_tmp;   // tile sums of the scans
+    float* bounds_part;   // per-block bound partials
+    float* grid;          // lo[3], hi[3], inv_cell, radius2, vertex total (bits), cells (bits)
+    uint32_t* iter;       // current row of the constants table
+    VcmConsts* consts;    // constants table
+    uint32_t paths, slots_per_path, consts_capacity;
+};
+
+size_t vcm_state_block_bytes(uint32_t paths, uint32_t max_len, uint32_t passes);
+VcmState vcm_state_carve(void* block, uint32_t paths, uint32_t max_len, uint32_t passes);
+
+// Camera model of the light-tracing strategy: the pixel-area image-plane distance width / (2 tan(fov/2)).
+struct VcmCamera {
+    PtCamera cam;
+    float image_plane;
+};
+
+// Runs passes [first, first + passes).  Accumulates into d_accum ([height][width][3] doubles) the sum of
+// the passes' images.
+cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
+                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream);
+
+}  // namespace sel

@@ -15,6 +15,10 @@ ptex_golden.npz  - a triangle mesh (icosphere, 320 faces) with 16 x 16 half-floa
 cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
                    from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp); the image the
                    path tracers' rMSE is measured against.  Needs only the oracle (python ... cornell).
+cornell_vcm_64_ref.npz - the FP64 high-pass vertex connection and merging image of the Cornell scene (64 x 64,
+                   4096 passes, path length 10, the default radius) from the oracle VCM (oracle/oracle_vcm.cpp);
+                   the image the VCM integrators' rMSE is measured against.  Needs only the oracle
+                   (python ... vcm).
 """
 from __future__ import annotations
 
@@ -167,11 +171,27 @@ def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
     print("cornell_64_ref.npz: mean radiance", img[1].mean(axis=(0, 1)))
 
 
+def make_cornell_vcm(passes=4096, size=64, max_len=10, seed=0x5E1A5C0C):
+    import oracle
+    from selas_gb300 import scenes
+    rs = scenes.cornell_box()
+    img = np.zeros((size, size, 3), np.float64)
+    step = 256
+    for p in range(0, passes, step):
+        img += oracle.vcm_render(rs, size, size, p, min(passes, p + step), max_len=max_len, seed=seed)
+    img /= passes
+    np.savez_compressed(OUT / "cornell_vcm_64_ref.npz", image=img.astype(np.float32), passes=passes, seed=seed,
+                        max_len=max_len)
+    print("cornell_vcm_64_ref.npz: mean radiance", img.mean(axis=(0, 1)))
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["bsdf", "ptex", "cornell"]
+    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm"]
     if "bsdf" in what:
         make_bsdf()
     if "ptex" in what:
         make_ptex()
     if "cornell" in what:
         make_cornell()
+    if "vcm" in what:
+        make_cornell_vcm()

@@ -57,3 +57,13 @@ def test_no_gpu_reports_an_error_instead_of_aborting(lib):
     h = ctypes.c_void_p()
     rc = lib.sel_device_new(0, ctypes.byref(h))
     assert rc != 0 and not h.value
+
+
+def test_vcm_settings_defaults_and_layout(lib):
+    import selas_gb300 as sel
+    assert ctypes.sizeof(sel.SelVcmSettings) == 32
+    s = sel.vcm_settings(7)
+    assert (s.passes, s.maxPathLength, s.disableMerging) == (7, 10, 0)
+    assert s.radiusAlpha == pytest.approx(0.75) and s.radius == 0.0
+    assert lib.sel_vcm_settings_defaults(None) == sel.SEL_ERR_INVALID_ARGUMENT
+    assert lib.sel_vcm_generate_image(None, None, None, None) == sel.SEL_ERR_INVALID_ARGUMENT

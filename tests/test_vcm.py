@@ -5,6 +5,8 @@ VCM, bidirectional path tracing and each strategy alone must converge to the ora
 The reference Disney BSDF is not of that kind (its diffuse sample weight and pdf differ from f * cos /
 density by a factor pi, Disney.cpp:466-519), so on it VCM converges to its own image, the FP64 oracle VCM.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -72,3 +74,73 @@ def test_oracle_vcm_without_merging_is_bpt_at_zero_radius_weight(cornell):
     a = oracle.vcm_render(cornell, SIZE, SIZE, 0, it, max_len=4, merging=True) / it
     b = oracle.vcm_render(cornell, SIZE, SIZE, 0, it, max_len=4, merging=False) / it
     np.testing.assert_allclose(_mean(a), _mean(b), rtol=0.01)
+
+
+# ---------------------------------------------------------------------------------------------------
+# GPU integrator (sel_vcm_generate_image) against the oracle
+# ---------------------------------------------------------------------------------------------------
+VCM_REF = Path(__file__).resolve().parent / "golden" / "cornell_vcm_64_ref.npz"
+SEED = 0x5E1A5000
+R0 = 1.25  # explicit initial radius, exact in float32, given to both implementations
+RATIO = 1.05
+
+
+def rmse(img, ref):
+    return float(np.sqrt(np.mean((img - ref) ** 2)) / np.mean(ref))
+
+
+def _gpu_vcm(device, rs, size, passes, seed=SEED, max_len=10, merging=True, radius=R0, first_pass=0):
+    import selas_gb300 as sel
+    sc = rs.build(sel, device)
+    cam = rs.sel_camera(sel, size, size)
+    img = sc.vcm_generate_image(cam, sel.vcm_settings(passes, max_len, seed, first_pass, merging, radius))
+    sc.release()
+    return img.astype(np.float64)
+
+
+def _same_paths(g, c):
+    rel = np.abs(g - c) / np.maximum(np.abs(c), 1e-3 * c.mean())
+    assert np.median(rel) < 1e-4, np.median(rel)
+    assert (rel < 1e-2).mean() > 0.97, (rel < 1e-2).mean()
+    assert abs(g.mean() / c.mean() - 1.0) < 5e-3, (g.mean(), c.mean())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("merging", [True, False])
+def test_gpu_vcm_traces_the_oracles_paths(device, cornell, merging):
+    """Same PCG32 streams: the GPU passes trace the oracle's light and camera paths, so the images agree
+    pixel by pixel up to FP32 rounding (and the rare path whose Russian roulette or lobe choice flips)."""
+    passes, size = 4, 48
+    gpu = _gpu_vcm(device, cornell, size, passes, merging=merging)
+    cpu = oracle.vcm_render(cornell, size, size, 0, passes, max_len=10, radius0=R0, seed=SEED, merging=merging) / passes
+    _same_paths(gpu, cpu)
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_passes_split_over_calls(device, cornell):
+    a = _gpu_vcm(device, cornell, 32, 3, first_pass=0)
+    b = _gpu_vcm(device, cornell, 32, 3, first_pass=3)
+    whole = _gpu_vcm(device, cornell, 32, 6)
+    np.testing.assert_allclose((a + b) / 2, whole, rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_rmse_within_ratio_of_oracle(device, cornell):
+    """rMSE against the FP64 high-pass oracle VCM image at equal passes, averaged over independent seeds,
+    within 1.05x that of the CPU oracle (default radius: 0.0025 x the bounding-sphere radius)."""
+    ref = np.load(VCM_REF)["image"].astype(np.float64)
+    passes = 16
+    e_gpu = np.mean([rmse(_gpu_vcm(device, cornell, 64, passes, seed=s, radius=0.0), ref) for s in (11, 12, 13, 14)])
+    e_cpu = np.mean([rmse(oracle.vcm_render(cornell, 64, 64, 0, passes, max_len=10, seed=s) / passes, ref)
+                     for s in (21, 22, 23, 24)])
+    print(f"VCM rmse gpu {e_gpu:.5f} oracle {e_cpu:.5f} ratio {e_gpu / e_cpu:.4f}")
+    assert e_gpu <= RATIO * e_cpu
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_full_size(device, cornell):
+    """1280 x 720 (the VCM configuration's viewport), path length 10: finite, non-negative, and its mean equals
+    the converged oracle image's mean within the statistical error."""
+    ref = np.load(VCM_REF)["image"].astype(np.float64)
+    img = _gpu_vcm(device, cornell, 720, 8, radius=0.0)
+    assert np.isfinite(img).all() and (img >= 0).all()
