@@ -56,7 +56,11 @@ int read_error_word(SelDeviceTy* dev, cudaStream_t s) {
     if (word) {
         cudaMemsetAsync(dev->d_err, 0, sizeof(uint32_t), s);
         cudaStreamSynchronize(s);
-        return fail(SEL_ERR_DEVICE_LIMIT, word & 2u ? "traversal stack overflow" : "kernel iteration cap reached");
+        const char* what = (word & 2u)   ? "traversal stack overflow"
+                           : (word & 4u) ? "Ptex filter frame stack overflow"
+                           : (word & 8u) ? "render queue overflow"
+                                         : "kernel iteration cap reached";
+        return fail(SEL_ERR_DEVICE_LIMIT, what);
     }
     return SEL_OK;
 }

@@ -26,7 +26,7 @@ constexpr int kBlock = 128;
 constexpr float kFloatMax = 3.402823466e+38f;  // FloatMax_ (SystemLib/BasicTypes.h:31)
 
 struct PtParams {
-    const uint4* nodes;
+    const void* nodes;
     const float4* tris;
     const MaterialDev* materials;
     uint32_t material_count;
@@ -111,8 +111,9 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
 
 // Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
 // so expensive and cheap rays balance across the GPU.
+template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
-    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[cur];
     const uint32_t* queue = P.st.queue[cur];
     uint32_t status = 0;
@@ -145,7 +146,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = tfar;
             QueryHit h;
-            const bool found = trace_wide<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status);
+            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock,
+                                                                status);
             P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
                                 : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
         }
@@ -290,8 +292,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
     }
 }
 
+template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
-    __shared__ uint2 stack_mem[kWideStack * kBlock];
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[2];
     const uint32_t npix = P.width * P.height;
     uint32_t status = 0;
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
             QueryHit h;
-            if (!trace_wide<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status)) {
+            if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status)) {
                 const float4 c = P.st.sh_c[e];
                 accumulate(P.accum, npix, 1, __float_as_uint(c.w), f3(c.x, c.y, c.z));
             }
@@ -401,9 +404,11 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
         for (uint32_t b = 0; b < set.max_bounces; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
-            k_extend<<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
             k_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur, b);
-            k_shadow<<<trace_grid, kBlock, 0, stream>>>(P);
+            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
+            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
         }
     }
     return cudaGetLastError();

@@ -32,7 +32,8 @@ struct PtState {
 };
 
 struct PtScene {
-    const uint4* nodes;
+    const void* nodes;  // 8-wide quantised (bvh_kind 0) or binary FP32 (bvh_kind 1) node array
+    int bvh_kind;
     const float4* tris;
     const MaterialDev* materials;
     uint32_t material_count;

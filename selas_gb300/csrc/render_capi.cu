@@ -121,8 +121,6 @@ int ensure_pt_state(SelSceneTy* sc, uint32_t paths) {
 int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
-    if (scene->info.bvh_kind != SEL_BVH_WIDE8_Q8)
-        return fail(SEL_ERR_INVALID_OPERATION, "the renderer traverses the 8-wide BVH: commit with SEL_BVH_WIDE8_Q8");
     if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
         return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
@@ -135,7 +133,8 @@ int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettin
 
 PtScene scene_view(const SelSceneTy* sc) {
     PtScene ps;
-    ps.nodes = static_cast<const uint4*>(sc->d_nodes);
+    ps.nodes = sc->d_nodes;
+    ps.bvh_kind = sc->info.bvh_kind == SEL_BVH_WIDE8_Q8 ? 0 : 1;
     ps.tris = static_cast<const float4*>(sc->d_tris);
     ps.materials = static_cast<const MaterialDev*>(sc->d_materials);
     uint32_t max_geom = 0;
@@ -186,8 +185,6 @@ SelVcmSettings default_vcm_settings() {
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
-    if (scene->info.bvh_kind != SEL_BVH_WIDE8_Q8)
-        return fail(SEL_ERR_INVALID_OPERATION, "the renderer traverses the 8-wide BVH: commit with SEL_BVH_WIDE8_Q8");
     if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
         return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))

@@ -330,4 +330,34 @@ __device__ __forceinline__ bool trace_binary(const float4* __restrict__ nodes, c
     return found;
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Traversal policies for the render kernels, which are instantiated for both BVH layouts: the 8-wide
+// quantised one and the plain binary FP32 one (the comparison path).  Stack entries live in shared memory,
+// `stride` entries apart per thread.
+// ---------------------------------------------------------------------------------------------------
+template <int kKind>
+struct Tracer;
+
+template <>
+struct Tracer<0> {  // SEL_BVH_WIDE8_Q8
+    using Entry = uint2;
+    static constexpr int kDepth = kWideStack;
+    template <bool kAnyHit>
+    static __device__ __forceinline__ bool trace(const void* nodes, const float4* tris, const QueryRay& r, QueryHit& h,
+                                                 Entry* stack, int stride, uint32_t& status) {
+        return trace_wide<kAnyHit>(static_cast<const uint4*>(nodes), tris, r, h, stack, stride, status);
+    }
+};
+
+template <>
+struct Tracer<1> {  // SEL_BVH_BINARY_FP32
+    using Entry = int;
+    static constexpr int kDepth = kBinaryStack;
+    template <bool kAnyHit>
+    static __device__ __forceinline__ bool trace(const void* nodes, const float4* tris, const QueryRay& r, QueryHit& h,
+                                                 Entry* stack, int stride, uint32_t& status) {
+        return trace_binary<kAnyHit>(static_cast<const float4*>(nodes), tris, r, h, stack, stride, status);
+    }
+};
+
 }  // namespace sel

@@ -40,9 +40,10 @@ constexpr float kFloatMax = 3.402823466e+38f;
 constexpr int kScanTile = 2048;  // 256 threads x 8
 constexpr int kSortTile = 4096;  // 256 threads x 16
 constexpr int kBoundsBlocks = 256;
+constexpr uint32_t kErrQueueOverflow = 8u;
 
 struct VcmParams {
-    const uint4* nodes;
+    const void* nodes;
     const float4* tris;
     const MaterialDev* materials;
     uint32_t material_count;
@@ -106,49 +107,6 @@ __device__ __forceinline__ LightVertex load_vertex(const float4* v) {
     lv.base = f3(e.x, e.y, e.z);
     lv.dvm = e.w;
     return lv;
-}
-
-// Closest hit from org along dir and the surface there (CalculateSurfaceParams as the path tracer uses it).
-__device__ bool vcm_hit(const VcmParams& P, float3 org, float3 dir, VHit& h, uint2* stack, uint32_t& status) {
-    QueryRay q;
-    q.ox = org.x; q.oy = org.y; q.oz = org.z; q.tnear = 0.0f;
-    q.dx = dir.x; q.dy = dir.y; q.dz = dir.z; q.tfar = kFloatMax;
-    QueryHit qh;
-    if (!trace_wide<false>(P.nodes, P.tris, q, qh, stack, kBlock, status)) return false;
-    const float4* tp = P.tris + size_t(qh.tri) * 3;
-    const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-    const uint32_t geom = __float_as_uint(p1.w);
-    const uint32_t mi = geom < P.material_count ? geom : 0;
-    const MaterialDev& m = P.materials[mi];
-    h.pos = f3(org.x + qh.t * dir.x, org.y + qh.t * dir.y, org.z + qh.t * dir.z);
-    h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), qh.t));
-    float3 base = ld3(m.base_color);
-    if (m.flags & kMaterialUsesPtex) {
-        uint32_t pstatus = 0;
-        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
-                  qh.u, qh.v, base, pstatus);
-        status |= pstatus;
-    }
-    h.view = -dir;
-    h.s = make_surface(m, triangle_ng(p0, p1, p2), h.view, base);
-    h.n = h.s.n;
-    h.cont = continuation_probability(h.s);
-    h.mat = mi;
-    h.delta = m.shader == kDiracTransparent;
-    h.transparent = (m.flags & kMaterialTransparent) != 0u;
-    return true;
-}
-
-// Visibility of a segment from a hit: origin offset 0.1 x the hit's error bound, tnear = the error bound
-// (OcclusionRay, PathTracer.cpp:71-92).
-__device__ __forceinline__ bool visible(const VcmParams& P, const VHit& h, float3 dir, float tfar, uint2* stack,
-                                        uint32_t& status) {
-    const float3 o = offset_origin(h.pos, h.n, h.err, dir, 0.1f);
-    QueryRay q;
-    q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = h.err;
-    q.dx = dir.x; q.dy = dir.y; q.dz = dir.z; q.tfar = tfar;
-    QueryHit qh;
-    return !trace_wide<true>(P.nodes, P.tris, q, qh, stack, kBlock, status);
 }
 
 __device__ __forceinline__ bool nonzero(float3 a) { return a.x != 0.0f || a.y != 0.0f || a.z != 0.0f; }
@@ -215,92 +173,316 @@ __device__ __forceinline__ void splat(double* accum, uint32_t pixel, float3 c) {
     atomicAdd(p + 2, double(c.z));
 }
 
-// Light sub-paths (GenerateLightSample + EvaluateLightPaths, VCM.cpp:493-561; VCMCommon.cpp:37-62 for an
-// area emitter: uniform point on the quad, cosine-weighted direction about its facing direction).
-__global__ void __launch_bounds__(kBlock) k_light(VcmParams P) {
-    __shared__ uint2 stack_mem[kWideStack * kBlock];
-    uint2* stack = stack_mem + threadIdx.x;
+// Warp-aggregated append of one entry per willing lane (full warps only).
+__device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
+    const uint32_t mask = __ballot_sync(0xffffffffu, want);
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t base = 0;
+    if (lane == 0 && mask) base = atomicAdd(count, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// Warp-aggregated reservation of n entries per lane (full warps only): returns this lane's first entry.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* count, uint32_t n) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t incl = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= uint32_t(o)) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(count, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - n;
+}
+
+__device__ __forceinline__ Pcg32 load_rng(const VcmParams& P, uint32_t s, uint64_t stream) {
+    Pcg32 r;
+    r.state = P.st.prng[s];
+    r.inc = (stream << 1u) | 1u;
+    return r;
+}
+
+__device__ __forceinline__ PathState load_path(const VcmParams& P, uint32_t s) {
+    const float4 o = P.st.po[s], d = P.st.pd[s], t = P.st.pt[s];
+    PathState st;
+    st.org = f3(o.x, o.y, o.z);
+    st.dvcm = o.w;
+    st.dir = f3(d.x, d.y, d.z);
+    st.dvc = d.w;
+    st.thr = f3(t.x, t.y, t.z);
+    st.dvm = t.w;
+    st.len = P.st.plen[s];
+    return st;
+}
+
+__device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const PathState& st) {
+    P.st.po[s] = make_float4(st.org.x, st.org.y, st.org.z, st.dvcm);
+    P.st.pd[s] = make_float4(st.dir.x, st.dir.y, st.dir.z, st.dvc);
+    P.st.pt[s] = make_float4(st.thr.x, st.thr.y, st.thr.z, st.dvm);
+    P.st.plen[s] = st.len;
+}
+
+// Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
+__device__ void make_vhit(const VcmParams& P, float3 org, float3 dir, float4 hit, VHit& h, uint32_t& status) {
+    const uint32_t tri = __float_as_uint(hit.w);
+    const float4* tp = P.tris + size_t(tri) * 3;
+    const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+    const uint32_t geom = __float_as_uint(p1.w);
+    const uint32_t mi = geom < P.material_count ? geom : 0;
+    const MaterialDev& m = P.materials[mi];
+    h.pos = f3(org.x + hit.x * dir.x, org.y + hit.x * dir.y, org.z + hit.x * dir.z);
+    h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), hit.x));
+    float3 base = ld3(m.base_color);
+    if (m.flags & kMaterialUsesPtex) {
+        uint32_t pstatus = 0;
+        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
+                  hit.y, hit.z, base, pstatus);
+        status |= pstatus;
+    }
+    h.view = -dir;
+    h.s = make_surface(m, triangle_ng(p0, p1, p2), h.view, base);
+    h.n = h.s.n;
+    h.cont = continuation_probability(h.s);
+    h.mat = mi;
+    h.delta = m.shader == kDiracTransparent;
+    h.transparent = (m.flags & kMaterialTransparent) != 0u;
+}
+
+// Shadow-ray record for a segment leaving a hit: origin offset 0.1 x the hit's error bound, tnear = the
+// error bound (OcclusionRay, PathTracer.cpp:71-92); contribution and pixel ride along.
+__device__ __forceinline__ void push_shadow(const VcmParams& P, uint32_t slot, const VHit& h, float3 dir, float tfar,
+                                            float3 c, uint32_t pixel) {
+    const float3 o = offset_origin(h.pos, h.n, h.err, dir, 0.1f);
+    P.st.so[slot] = make_float4(o.x, o.y, o.z, h.err);
+    P.st.sd[slot] = make_float4(dir.x, dir.y, dir.z, tfar);
+    P.st.sc[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
+}
+
+__device__ __forceinline__ void push_null_shadow(const VcmParams& P, uint32_t slot) {
+    P.st.sc[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void k_reset(uint32_t* counters) {
+    if (threadIdx.x < 8) counters[threadIdx.x] = 0u;
+}
+
+__global__ void k_bounce_reset(uint32_t* counters, int next) {
+    if (threadIdx.x == 0) {
+        counters[next] = 0u;
+        counters[2] = 0u;
+        counters[3] = 0u;
+        counters[4] = 0u;
+    }
+}
+
+// GenerateLightSample for a quad light of light set 0 (VCMCommon.cpp:37-62 restated for an area emitter:
+// uniform point on the quad, cosine-weighted direction about its facing direction).
+__global__ void __launch_bounds__(kBlock) k_l_generate(VcmParams P) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t N = P.npaths;
-    uint32_t status = 0;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
-        uint32_t stored = 0;
-        float4* slots = P.st.verts + size_t(p) * P.slots * 5;
-        if (P.light_count > 0) {
-            Pcg32 rng = pcg_seed(P.seed, (uint64_t(c.pass) * 2 + 0) * N + p);
-            const float pick = pcg_float(rng);
-            uint32_t li = uint32_t(pick * float(P.light_count));
-            li = li < P.light_count - 1 ? li : P.light_count - 1;
-            const QuadLight L = P.lights[li];
-            const float u = pcg_float(rng), v = pcg_float(rng);
-            const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-            const float pdf_a = 1.0f / (length(L.x) * length(L.z));
-            const float3 ln = normalize(L.direction);
-            float3 lt, lb;
-            orthonormal_basis(ln, lt, lb);
-            const float r0 = pcg_float(rng), r1 = pcg_float(rng);
-            const float rr = sqrtf(r0), ph = 2.0f * kPi * r1;
-            const float cosl = sqrtf(fmaxf(0.0f, 1.0f - r0));
-            const float3 dir = normalize(rr * cosf(ph) * lt + cosl * ln + rr * sinf(ph) * lb);
-            if (cosl > 0.0f) {
-                const float light_pick = 1.0f / float(P.light_count);
-                const float emission_pdf = pdf_a * cosl / kPi * light_pick;
-                const float direct_pdf_a = pdf_a * light_pick;
-                PathState st;
-                st.org = lp;
-                st.dir = dir;
-                st.thr = L.radiance * (cosl / emission_pdf);
-                st.dvcm = direct_pdf_a / emission_pdf;
-                st.dvc = 0.0f;
-                st.dvm = 0.0f;
-                st.len = 1;
-                while (st.len + 2 <= P.max_len + 1) {
-                    VHit h;
-                    if (!vcm_hit(P, st.org, st.dir, h, stack, status)) break;
-                    const float3 seg = h.pos - st.org;
-                    const float d2 = dot(seg, seg);
-                    const float cos_in = fabsf(dot(h.n, h.view));
-                    st.dvcm *= d2;
-                    st.dvcm *= 1.0f / cos_in;
-                    st.dvc *= 1.0f / cos_in;
-                    st.dvm *= 1.0f / cos_in;
-                    if (!h.delta) {
-                        store_vertex(slots + size_t(stored) * 5, h, st);
-                        ++stored;
-                        // light tracing: connect to the camera (ConnectLightPathToCamera, VCM.cpp:190-233;
-                        // tech report sec. 5.3)
-                        int px, py;
-                        if (st.len + 1 <= P.max_len && to_pixel(P.cam, h.pos, px, py)) {
-                            float3 to_cam = P.cam.position - h.pos;
-                            const float dist2 = dot(to_cam, to_cam);
-                            const float dist = sqrtf(dist2);
-                            to_cam = to_cam * (1.0f / dist);
-                            const float cos_cam = dot(P.cam.z, -to_cam);
-                            float cam_side_pdf, light_side_pdf;
-                            const float3 fa = bsdf_evaluate(h.s, to_cam, h.view, cam_side_pdf, light_side_pdf);
-                            const float cos_view = fabsf(dot(h.n, h.view));
-                            const float3 f = cos_view > 0.0f ? fa * (fabsf(dot(h.n, to_cam)) / cos_view) : f3(0.0f);
-                            float rev = cam_side_pdf;
-                            if (nonzero(f) && cos_cam > 0.0f) {
-                                rev *= h.cont;
-                                const float ip = P.image_plane / cos_cam;
-                                const float img_to_solid = ip * ip / cos_cam;
-                                const float cos_surf = fabsf(dot(h.n, to_cam));
-                                const float camera_pdf_a = img_to_solid * cos_surf / dist2;
-                                const float w_light = (camera_pdf_a / c.n_paths) * (c.vm_weight + st.dvcm + st.dvc * rev);
-                                const float mis = 1.0f / (w_light + 1.0f);
-                                const float3 contrib = (mis * img_to_solid / (c.n_paths * dist2)) * (st.thr * f);
-                                if (visible(P, h, to_cam, dist * (1.0f - 1e-4f), stack, status))
-                                    splat(P.accum, uint32_t(py) * P.width + uint32_t(px), contrib);
-                            }
-                        }
-                    }
-                    if (st.len + 2 > P.max_len) break;
-                    if (!scatter(rng, h, c, st, true)) break;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
+        const uint32_t p = base + threadIdx.x;
+        bool alive = false;
+        if (p < N) {
+            P.st.vcount[p] = 0;
+            if (P.light_count > 0) {
+                const uint64_t stream = (uint64_t(c.pass) * 2 + 0) * N + p;
+                Pcg32 rng = pcg_seed(P.seed, stream);
+                const float pick = pcg_float(rng);
+                uint32_t li = uint32_t(pick * float(P.light_count));
+                li = li < P.light_count - 1 ? li : P.light_count - 1;
+                const QuadLight L = P.lights[li];
+                const float u = pcg_float(rng), v = pcg_float(rng);
+                const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                const float3 ln = normalize(L.direction);
+                float3 lt, lb;
+                orthonormal_basis(ln, lt, lb);
+                const float r0 = pcg_float(rng), r1 = pcg_float(rng);
+                const float rr = sqrtf(r0), ph = 2.0f * kPi * r1;
+                const float cosl = sqrtf(fmaxf(0.0f, 1.0f - r0));
+                const float3 dir = normalize(rr * cosf(ph) * lt + cosl * ln + rr * sinf(ph) * lb);
+                if (cosl > 0.0f) {
+                    const float light_pick = 1.0f / float(P.light_count);
+                    const float emission_pdf = pdf_a * cosl / kPi * light_pick;
+                    const float direct_pdf_a = pdf_a * light_pick;
+                    PathState st;
+                    st.org = lp;
+                    st.dir = dir;
+                    st.thr = L.radiance * (cosl / emission_pdf);
+                    st.dvcm = direct_pdf_a / emission_pdf;
+                    st.dvc = 0.0f;  // the emitter cannot be hit by camera or BSDF rays
+                    st.dvm = 0.0f;
+                    st.len = 1;
+                    store_path(P, p, st);
+                    P.st.prng[p] = rng.state;
+                    alive = true;
                 }
             }
         }
-        P.st.vcount[p] = stored;
+        const uint32_t q = warp_append(&P.st.counters[0], alive);
+        if (alive) P.st.queue[0][q] = p;
+    }
+}
+
+// Camera rays (GenerateCameraPaths, VCM.cpp:563-574, with x = p - y * width): one jittered sample per pixel.
+__global__ void __launch_bounds__(kBlock) k_c_generate(VcmParams P) {
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t N = P.npaths;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+        Pcg32 rng = pcg_seed(P.seed, (uint64_t(c.pass) * 2 + 1) * N + p);
+        const uint32_t y = p / P.width, x = p - y * P.width;
+        const float vx = float(x) + pcg_float(rng), vy = float(y) + pcg_float(rng);
+        const float3 d = camera_direction(P.cam, vx, vy);
+        const float cos_cam = dot(P.cam.z, d);
+        const float ip = P.image_plane / cos_cam;
+        const float camera_pdf_w = ip * ip / cos_cam;
+        PathState st;
+        st.org = P.cam.position;
+        st.dir = d;
+        st.thr = f3(1.0f);
+        st.dvcm = c.n_paths / camera_pdf_w;
+        st.dvc = 0.0f;
+        st.dvm = 0.0f;
+        st.len = 1;
+        store_path(P, p, st);
+        P.st.prng[p] = rng.state;
+        P.st.queue[0][p] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.st.counters[0] = N;
+}
+
+// Closest hits of the queued paths: persistent blocks, warps take 32-entry packets through an atomic cursor.
+template <int K>
+__global__ void __launch_bounds__(kBlock, 8) k_extend(VcmParams P, int cur) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+    const uint32_t n = P.st.counters[cur];
+    const uint32_t* queue = P.st.queue[cur];
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if ((threadIdx.x & 31u) == 0) base = atomicAdd(&P.st.counters[3], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t e = base + (threadIdx.x & 31u);
+        if (e < n) {
+            const uint32_t s = queue[e];
+            const float4 o = P.st.po[s], d = P.st.pd[s];
+            QueryRay q;
+            q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
+            q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = kFloatMax;
+            QueryHit h;
+            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock,
+                                                                status);
+            P.st.phit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                 : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+        }
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+// Any-hit of the queued shadow rays; unoccluded ones add their contribution to their pixel.
+template <int K>
+__global__ void __launch_bounds__(kBlock, 8) k_shadow(VcmParams P) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+    const uint32_t n = P.st.counters[2];
+    uint32_t status = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if ((threadIdx.x & 31u) == 0) base = atomicAdd(&P.st.counters[4], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t e = base + (threadIdx.x & 31u);
+        if (e < n) {
+            const float4 c = P.st.sc[e];
+            if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) {
+                const float4 o = P.st.so[e], d = P.st.sd[e];
+                QueryRay q;
+                q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
+                q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
+                QueryHit h;
+                if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status))
+                    splat(P.accum, __float_as_uint(c.w), f3(c.x, c.y, c.z));
+            }
+        }
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+// Light sub-path vertices (EvaluateLightPaths, VCM.cpp:502-561): MIS update, stored vertex, connection to
+// the camera (ConnectLightPathToCamera, VCM.cpp:190-233; tech report sec. 5.3) and scattering.
+__global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur) {
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t n = P.st.counters[cur];
+    const uint32_t N = P.npaths;
+    const int next = cur ^ 1;
+    uint32_t status = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        bool cont = false, shadow = false;
+        uint32_t s = 0, pixel = 0;
+        VHit h;
+        float3 to_cam = f3(0.0f), contrib = f3(0.0f);
+        float sh_tfar = 0.0f;
+        if (e < n) {
+            s = P.st.queue[cur][e];
+            const float4 hit = P.st.phit[s];
+            if (__float_as_uint(hit.w) != 0xffffffffu) {
+                PathState st = load_path(P, s);
+                make_vhit(P, st.org, st.dir, hit, h, status);
+                const float3 seg = h.pos - st.org;
+                const float d2 = dot(seg, seg);
+                const float cos_in = fabsf(dot(h.n, h.view));
+                st.dvcm *= d2;
+                st.dvcm *= 1.0f / cos_in;
+                st.dvc *= 1.0f / cos_in;
+                st.dvm *= 1.0f / cos_in;
+                if (!h.delta) {
+                    const uint32_t k = P.st.vcount[s];
+                    store_vertex(P.st.verts + (size_t(s) * P.slots + k) * 5, h, st);
+                    P.st.vcount[s] = k + 1;
+                    int px, py;
+                    if (st.len + 1 <= P.max_len && to_pixel(P.cam, h.pos, px, py)) {
+                        to_cam = P.cam.position - h.pos;
+                        const float dist2 = dot(to_cam, to_cam);
+                        const float dist = sqrtf(dist2);
+                        to_cam = to_cam * (1.0f / dist);
+                        const float cos_cam = dot(P.cam.z, -to_cam);
+                        float cam_side_pdf, light_side_pdf;
+                        const float3 fa = bsdf_evaluate(h.s, to_cam, h.view, cam_side_pdf, light_side_pdf);
+                        const float cos_view = fabsf(dot(h.n, h.view));
+                        const float3 f = cos_view > 0.0f ? fa * (fabsf(dot(h.n, to_cam)) / cos_view) : f3(0.0f);
+                        float rev = cam_side_pdf;
+                        if (nonzero(f) && cos_cam > 0.0f) {
+                            rev *= h.cont;
+                            const float ip = P.image_plane / cos_cam;
+                            const float img_to_solid = ip * ip / cos_cam;
+                            const float cos_surf = fabsf(dot(h.n, to_cam));
+                            const float camera_pdf_a = img_to_solid * cos_surf / dist2;
+                            const float w_light = (camera_pdf_a / c.n_paths) * (c.vm_weight + st.dvcm + st.dvc * rev);
+                            const float mis = 1.0f / (w_light + 1.0f);
+                            contrib = (mis * img_to_solid / (c.n_paths * dist2)) * (st.thr * f);
+                            sh_tfar = dist * (1.0f - 1e-4f);
+                            pixel = uint32_t(py) * P.width + uint32_t(px);
+                            shadow = nonzero(contrib);
+                        }
+                    }
+                }
+                if (st.len + 2 <= P.max_len) {
+                    Pcg32 rng = load_rng(P, s, (uint64_t(c.pass) * 2 + 0) * N + s);
+                    cont = scatter(rng, h, c, st, true);
+                    P.st.prng[s] = rng.state;
+                    if (cont) store_path(P, s, st);
+                }
+            }
+        }
+        const uint32_t q = warp_append(&P.st.counters[next], cont);
+        if (cont) P.st.queue[next][q] = s;
+        const uint32_t sq = warp_append(&P.st.counters[2], shadow);
+        if (shadow) push_shadow(P, sq, h, to_cam, sh_tfar, contrib, pixel);
     }
     if (status) atomicOr(P.err, status);
 }
@@ -543,159 +725,177 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t* keys_in, 
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Camera sub-paths (GenerateCameraPaths + EvaluateCameraPaths, VCM.cpp:563-666).
+// Camera sub-path vertices (EvaluateCameraPaths, VCM.cpp:576-666): MIS update, next-event estimation (tech
+// report sec. 5.4), connections to the vertices of the light path with the same index (ConnectPathVertices,
+// VCM.cpp:293-359) and merging with the light vertices of the 2x2x2 cells around the vertex (MergeVertices
+// + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155), then scattering.  Next-event and connection
+// segments go to the shadow queue: each lane reserves one entry per candidate (warp-aggregated) and fills
+// the candidates whose BSDF product is zero with null entries.  Merged radiance goes straight to the pixel.
 // ---------------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_camera(VcmParams P) {
-    __shared__ uint2 stack_mem[kWideStack * kBlock];
-    uint2* stack = stack_mem + threadIdx.x;
+__global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur) {
     const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t n = P.st.counters[cur];
     const uint32_t N = P.npaths;
+    const int next = cur ^ 1;
     const float* grid = P.st.grid;
     const uint32_t total_vertices = P.st.vpos[N];
     const float3 glo = f3(grid[0], grid[1], grid[2]), ghi = f3(grid[3], grid[4], grid[5]);
     const float ginv = grid[6], gr2 = grid[7];
     const uint32_t* cell_start = P.st.cell_start;
+    const uint32_t capacity = P.st.shadow_capacity;
     uint32_t status = 0;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
-        Pcg32 rng = pcg_seed(P.seed, (uint64_t(c.pass) * 2 + 1) * N + p);
-        const uint32_t y = p / P.width, x = p - y * P.width;
-        const float vx = float(x) + pcg_float(rng), vy = float(y) + pcg_float(rng);
-        const float3 d = camera_direction(P.cam, vx, vy);
-        const float cos_cam = dot(P.cam.z, d);
-        const float ip = P.image_plane / cos_cam;
-        const float camera_pdf_w = ip * ip / cos_cam;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        bool cont = false, hit_ok = false;
+        uint32_t s = 0, nee = 0, nvc = 0;
+        VHit h;
         PathState st;
-        st.org = P.cam.position;
-        st.dir = d;
-        st.thr = f3(1.0f);
-        st.dvcm = c.n_paths / camera_pdf_w;
-        st.dvc = 0.0f;
-        st.dvm = 0.0f;
-        st.len = 1;
-        float3 color = f3(0.0f);
-        const uint32_t lcount = P.st.vcount[p];
-        const float4* lslots = P.st.verts + size_t(p) * P.slots * 5;
-        for (;;) {
-            VHit h;
-            if (!vcm_hit(P, st.org, st.dir, h, stack, status)) break;
-            const float3 seg = h.pos - st.org;
-            const float d2 = dot(seg, seg);
-            const float cos_in = fabsf(dot(h.n, h.view));
-            st.dvcm *= d2;
-            st.dvcm *= 1.0f / cos_in;
-            st.dvc *= 1.0f / cos_in;
-            st.dvm *= 1.0f / cos_in;
-            if (!h.delta) {
-                // next-event estimation to light set 0 (tech report sec. 5.4)
-                if (st.len + 1 <= P.max_len && P.light_count > 0) {
-                    const float pick = pcg_float(rng);
-                    uint32_t li = uint32_t(pick * float(P.light_count));
-                    li = li < P.light_count - 1 ? li : P.light_count - 1;
-                    const QuadLight L = P.lights[li];
-                    const float u = pcg_float(rng), v = pcg_float(rng);
-                    const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                    const float pdf_a = 1.0f / (length(L.x) * length(L.z));
-                    float3 to_l = lp - h.pos;
-                    const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
-                    to_l = to_l * (1.0f / dl);
-                    const float cos_light = dot(normalize(L.direction), -to_l);
-                    if (cos_light > 0.0f) {
-                        float fwd, rev;
-                        const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
-                        if (nonzero(f)) {
-                            rev *= h.cont;
-                            const float light_pick = 1.0f / float(P.light_count);
-                            const float direct_pdf_w = pdf_a * dl2 / cos_light;
-                            const float emission_pdf_w = pdf_a * cos_light / kPi;
-                            const float cos_to_light = fabsf(dot(h.n, to_l));
-                            const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
-                                                   (c.vm_weight + st.dvcm + st.dvc * rev);
-                            const float mis = 1.0f / (1.0f + w_camera);
-                            const float3 contrib = (mis / (light_pick * direct_pdf_w)) * (L.radiance * f);
-                            if (visible(P, h, to_l, dl * (1.0f - 1e-4f), stack, status)) color = color + st.thr * contrib;
-                        }
+        Pcg32 rng;
+        rng.state = 0;
+        rng.inc = 1;
+        if (e < n) {
+            s = P.st.queue[cur][e];
+            const float4 hit = P.st.phit[s];
+            if (__float_as_uint(hit.w) != 0xffffffffu) {
+                hit_ok = true;
+                st = load_path(P, s);
+                make_vhit(P, st.org, st.dir, hit, h, status);
+                const float3 seg = h.pos - st.org;
+                const float d2 = dot(seg, seg);
+                const float cos_in = fabsf(dot(h.n, h.view));
+                st.dvcm *= d2;
+                st.dvcm *= 1.0f / cos_in;
+                st.dvc *= 1.0f / cos_in;
+                st.dvm *= 1.0f / cos_in;
+                rng = load_rng(P, s, (uint64_t(c.pass) * 2 + 1) * N + s);
+                if (!h.delta) {
+                    nee = (st.len + 1 <= P.max_len && P.light_count > 0) ? 1u : 0u;
+                    const uint32_t lcount = P.st.vcount[s];
+                    const float4* lslots = P.st.verts + size_t(s) * P.slots * 5;
+                    while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * 5].w) + 1 + st.len <= P.max_len) ++nvc;
+                }
+            }
+        }
+        uint32_t slot = warp_reserve(&P.st.counters[2], nee + nvc);
+        if (hit_ok && slot + nee + nvc > capacity) {  // cannot happen with capacity N * max_len
+            status |= kErrQueueOverflow;
+            nee = nvc = 0;
+        }
+        if (hit_ok && !h.delta) {
+            const uint32_t pixel = s;
+            if (nee) {
+                const float pick = pcg_float(rng);
+                uint32_t li = uint32_t(pick * float(P.light_count));
+                li = li < P.light_count - 1 ? li : P.light_count - 1;
+                const QuadLight L = P.lights[li];
+                const float u = pcg_float(rng), v = pcg_float(rng);
+                const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                float3 to_l = lp - h.pos;
+                const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
+                to_l = to_l * (1.0f / dl);
+                const float cos_light = dot(normalize(L.direction), -to_l);
+                bool pushed = false;
+                if (cos_light > 0.0f) {
+                    float fwd, rev;
+                    const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                    if (nonzero(f)) {
+                        rev *= h.cont;
+                        const float light_pick = 1.0f / float(P.light_count);
+                        const float direct_pdf_w = pdf_a * dl2 / cos_light;
+                        const float emission_pdf_w = pdf_a * cos_light / kPi;
+                        const float cos_to_light = fabsf(dot(h.n, to_l));
+                        const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
+                                               (c.vm_weight + st.dvcm + st.dvc * rev);
+                        const float mis = 1.0f / (1.0f + w_camera);
+                        const float3 contrib = st.thr * ((mis / (light_pick * direct_pdf_w)) * (L.radiance * f));
+                        push_shadow(P, slot, h, to_l, dl * (1.0f - 1e-4f), contrib, pixel);
+                        pushed = true;
                     }
                 }
-                // vertex connection to the vertices of light path p (ConnectPathVertices, VCM.cpp:293-359)
-                for (uint32_t k = 0; k < lcount; ++k) {
-                    const LightVertex lv = load_vertex(lslots + size_t(k) * 5);
-                    if (lv.len + 1 + st.len > P.max_len) break;
-                    float3 dir = lv.pos - h.pos;
-                    const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
-                    dir = dir * (1.0f / dist);
-                    float cfwd, crev, lfwd, lrev;
-                    const float3 cf = bsdf_evaluate(h.s, h.view, dir, cfwd, crev);
-                    if (!nonzero(cf)) continue;
-                    const MaterialDev& lm = P.materials[lv.mat];
-                    const Surface ls = make_surface_linear(lm, lv.n, lv.view, lv.base);
-                    const float lcont = continuation_probability(ls);
-                    const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
-                    const float lcos_view = fabsf(dot(lv.n, lv.view));
-                    const float3 lf = lcos_view > 0.0f ? lfa * (fabsf(dot(lv.n, dir)) / lcos_view) : f3(0.0f);
-                    if (!nonzero(lf)) continue;
-                    cfwd *= h.cont; crev *= h.cont;
-                    lfwd *= lcont; lrev *= lcont;
-                    const float cos_cam_v = fabsf(dot(dir, h.n));
-                    const float cos_light_v = fabsf(dot(-dir, lv.n));
-                    const float cam_pdf_a = cfwd * cos_light_v / dist2;
-                    const float light_pdf_a = lfwd * cos_cam_v / dist2;
-                    const float w_light = cam_pdf_a * (c.vm_weight + lv.dvcm + lv.dvc * lrev);
-                    const float w_camera = light_pdf_a * (c.vm_weight + st.dvcm + st.dvc * crev);
-                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
-                    const float3 contrib = (mis / dist2) * (cf * lf);
-                    const float bias = 0.1f * h.err;
-                    if (visible(P, h, dir, dist - 16.0f * bias, stack, status)) color = color + st.thr * lv.thr * contrib;
-                }
-                // vertex merging (MergeVertices + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155)
-                float3 merged = f3(0.0f);
-                const float3 dmin = h.pos - glo, dmax = ghi - h.pos;
-                if (P.merging && total_vertices > 0 && dmin.x >= 0.0f && dmin.y >= 0.0f && dmin.z >= 0.0f &&
-                    dmax.x >= 0.0f && dmax.y >= 0.0f && dmax.z >= 0.0f) {
-                    const uint32_t* idx = P.sorted_index;
-                    const float3 cp = ginv * dmin;
-                    const float fx = floorf(cp.x), fy = floorf(cp.y), fz = floorf(cp.z);
-                    const int x0 = int(fx) - (cp.x - fx < 0.5f ? 1 : 0);
-                    const int y0 = int(fy) - (cp.y - fy < 0.5f ? 1 : 0);
-                    const int z0 = int(fz) - (cp.z - fz < 0.5f ? 1 : 0);
-                    for (int dz = 0; dz <= 1; ++dz)
-                        for (int dy = 0; dy <= 1; ++dy)
-                            for (int dx = 0; dx <= 1; ++dx) {
-                                const uint32_t cell = cell_hash(x0 + dx, y0 + dy, z0 + dz, N);
-                                const uint32_t b = cell_start[cell], e = cell_start[cell + 1];
-                                for (uint32_t k = b; k < e; ++k) {
-                                    const float4* vp = P.st.verts + size_t(idx[k]) * 5;
-                                    const float4 a = vp[0];
-                                    const float3 dd = h.pos - f3(a.x, a.y, a.z);
-                                    if (dot(dd, dd) > gr2) continue;
-                                    const LightVertex lv = load_vertex(vp);
-                                    if (st.len + lv.len > P.max_len) continue;
-                                    const MaterialDev& lm = P.materials[lv.mat];
-                                    // the reference merges only between surfaces of the same transparency
-                                    // (VCM.cpp:372-375)
-                                    if (h.transparent != ((lm.flags & kMaterialTransparent) != 0u)) continue;
-                                    float fwd, rev;
-                                    const float3 fc = bsdf_evaluate(h.s, h.view, lv.view, fwd, rev);
-                                    const float cosl = fabsf(dot(h.n, lv.view));
-                                    if (!nonzero(fc) || cosl == 0.0f) continue;
-                                    const float lcont = saturate(max3(lv.base));
-                                    fwd *= h.cont;
-                                    rev *= lcont;
-                                    const float w_light = lv.dvcm * c.vc_weight + lv.dvm * fwd;
-                                    const float w_camera = st.dvcm * c.vc_weight + st.dvm * rev;
-                                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
-                                    merged = merged + (mis / cosl) * (fc * lv.thr);
-                                }
-                            }
-                }
-                color = color + c.vm_norm * (st.thr * merged);
+                if (!pushed) push_null_shadow(P, slot);
+                ++slot;
             }
-            if (st.len >= P.max_len) break;
-            if (!scatter(rng, h, c, st, false)) break;
+            const float4* lslots = P.st.verts + size_t(s) * P.slots * 5;
+            for (uint32_t k = 0; k < nvc; ++k, ++slot) {
+                const LightVertex lv = load_vertex(lslots + size_t(k) * 5);
+                float3 dir = lv.pos - h.pos;
+                const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
+                dir = dir * (1.0f / dist);
+                float cfwd, crev, lfwd, lrev;
+                const float3 cf = bsdf_evaluate(h.s, h.view, dir, cfwd, crev);
+                if (!nonzero(cf)) { push_null_shadow(P, slot); continue; }
+                const MaterialDev& lm = P.materials[lv.mat];
+                const Surface ls = make_surface_linear(lm, lv.n, lv.view, lv.base);
+                const float lcont = continuation_probability(ls);
+                const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
+                const float lcos_view = fabsf(dot(lv.n, lv.view));
+                const float3 lf = lcos_view > 0.0f ? lfa * (fabsf(dot(lv.n, dir)) / lcos_view) : f3(0.0f);
+                if (!nonzero(lf)) { push_null_shadow(P, slot); continue; }
+                cfwd *= h.cont; crev *= h.cont;
+                lfwd *= lcont; lrev *= lcont;
+                const float cos_cam_v = fabsf(dot(dir, h.n));
+                const float cos_light_v = fabsf(dot(-dir, lv.n));
+                const float cam_pdf_a = cfwd * cos_light_v / dist2;
+                const float light_pdf_a = lfwd * cos_cam_v / dist2;
+                const float w_light = cam_pdf_a * (c.vm_weight + lv.dvcm + lv.dvc * lrev);
+                const float w_camera = light_pdf_a * (c.vm_weight + st.dvcm + st.dvc * crev);
+                const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                const float3 contrib = st.thr * lv.thr * ((mis / dist2) * (cf * lf));
+                const float bias = 0.1f * h.err;
+                push_shadow(P, slot, h, dir, dist - 16.0f * bias, contrib, pixel);
+            }
+            // vertex merging
+            float3 merged = f3(0.0f);
+            const float3 dmin = h.pos - glo, dmax = ghi - h.pos;
+            if (P.merging && total_vertices > 0 && dmin.x >= 0.0f && dmin.y >= 0.0f && dmin.z >= 0.0f &&
+                dmax.x >= 0.0f && dmax.y >= 0.0f && dmax.z >= 0.0f) {
+                const uint32_t* idx = P.sorted_index;
+                const float3 cp = ginv * dmin;
+                const float fx = floorf(cp.x), fy = floorf(cp.y), fz = floorf(cp.z);
+                const int x0 = int(fx) - (cp.x - fx < 0.5f ? 1 : 0);
+                const int y0 = int(fy) - (cp.y - fy < 0.5f ? 1 : 0);
+                const int z0 = int(fz) - (cp.z - fz < 0.5f ? 1 : 0);
+                for (int dz = 0; dz <= 1; ++dz)
+                    for (int dy = 0; dy <= 1; ++dy)
+                        for (int dx = 0; dx <= 1; ++dx) {
+                            const uint32_t cell = cell_hash(x0 + dx, y0 + dy, z0 + dz, N);
+                            const uint32_t b = cell_start[cell], eidx = cell_start[cell + 1];
+                            for (uint32_t k = b; k < eidx; ++k) {
+                                const float4* vp = P.st.verts + size_t(idx[k]) * 5;
+                                const float4 a = vp[0];
+                                const float3 dd = h.pos - f3(a.x, a.y, a.z);
+                                if (dot(dd, dd) > gr2) continue;
+                                const LightVertex lv = load_vertex(vp);
+                                if (st.len + lv.len > P.max_len) continue;
+                                const MaterialDev& lm = P.materials[lv.mat];
+                                // the reference merges only between surfaces of the same transparency
+                                // (VCM.cpp:372-375)
+                                if (h.transparent != ((lm.flags & kMaterialTransparent) != 0u)) continue;
+                                float fwd, rev;
+                                const float3 fc = bsdf_evaluate(h.s, h.view, lv.view, fwd, rev);
+                                const float cosl = fabsf(dot(h.n, lv.view));
+                                if (!nonzero(fc) || cosl == 0.0f) continue;
+                                const float lcont = saturate(max3(lv.base));
+                                fwd *= h.cont;
+                                rev *= lcont;
+                                const float w_light = lv.dvcm * c.vc_weight + lv.dvm * fwd;
+                                const float w_camera = st.dvcm * c.vc_weight + st.dvm * rev;
+                                const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                                merged = merged + (mis / cosl) * (fc * lv.thr);
+                            }
+                        }
+            }
+            const float3 mc = c.vm_norm * (st.thr * merged);
+            if (nonzero(mc)) splat(P.accum, pixel, mc);
         }
-        double* px = P.accum + size_t(p) * 3;
-        px[0] += double(color.x);
-        px[1] += double(color.y);
-        px[2] += double(color.z);
+        if (hit_ok && st.len < P.max_len) {
+            cont = scatter(rng, h, c, st, false);
+            if (cont) store_path(P, s, st);
+        }
+        if (hit_ok) P.st.prng[s] = rng.state;
+        const uint32_t q = warp_append(&P.st.counters[next], cont);
+        if (cont) P.st.queue[next][q] = s;
     }
     if (status) atomicOr(P.err, status);
 }
@@ -706,29 +906,40 @@ __global__ void k_pass_end(uint32_t* iter) {
 
 }  // namespace
 
-VcmState vcm_state_carve(void* block, uint32_t paths, uint32_t max_len, uint32_t passes) {
-    char* p = static_cast<char*>(block);
-    auto take = [&](size_t bytes) {
-        char* r = p;
-        p += (bytes + 255) & ~size_t(255);
-        return r;
-    };
+namespace {
+
+// One layout walk for both sizing and carving.
+template <typename Take>
+void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint32_t passes) {
     const uint32_t slots = max_len - 1;
     const size_t nv = size_t(paths) * slots;
-    const uint32_t ntiles = uint32_t((nv + kSortTile - 1) / kSortTile);
-    const size_t scan_n = std::max<size_t>(std::max<size_t>(paths + 1, size_t(256) * ntiles), 1);
-    VcmState st;
+    const size_t ntiles = (nv + kSortTile - 1) / kSortTile;
+    const size_t scan_n = std::max<size_t>(std::max<size_t>(size_t(paths) + 1, 256 * ntiles), 1);
+    const size_t shadow = size_t(paths) * max_len;  // per bounce: one next-event + up to max_len - 1 connections
     st.verts = reinterpret_cast<float4*>(take(80 * nv));
     st.vcount = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.vpos = reinterpret_cast<uint32_t*>(take(4ull * (paths + 1)));
+    st.po = reinterpret_cast<float4*>(take(16ull * paths));
+    st.pd = reinterpret_cast<float4*>(take(16ull * paths));
+    st.pt = reinterpret_cast<float4*>(take(16ull * paths));
+    st.plen = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.prng = reinterpret_cast<uint64_t*>(take(8ull * paths));
+    st.phit = reinterpret_cast<float4*>(take(16ull * paths));
+    st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.so = reinterpret_cast<float4*>(take(16 * shadow));
+    st.sd = reinterpret_cast<float4*>(take(16 * shadow));
+    st.sc = reinterpret_cast<float4*>(take(16 * shadow));
+    st.shadow_capacity = uint32_t(shadow);
+    st.counters = reinterpret_cast<uint32_t*>(take(4 * 16));
     for (int k = 0; k < 2; ++k) {
         st.keys[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
         st.vals[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
     }
     st.cell_count = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.cell_start = reinterpret_cast<uint32_t*>(take(4ull * (paths + 1)));
-    st.hist = reinterpret_cast<uint32_t*>(take(4ull * 256 * ntiles));
-    st.hist_off = reinterpret_cast<uint32_t*>(take(4ull * (256 * size_t(ntiles) + 1)));
+    st.hist = reinterpret_cast<uint32_t*>(take(4 * 256 * ntiles));
+    st.hist_off = reinterpret_cast<uint32_t*>(take(4 * (256 * ntiles + 1)));
     st.scan_tmp = reinterpret_cast<uint32_t*>(take(4 * ((scan_n + kScanTile - 1) / kScanTile + 1)));
     st.bounds_part = reinterpret_cast<float*>(take(4 * 6 * kBoundsBlocks));
     st.grid = reinterpret_cast<float*>(take(4 * 16));
@@ -737,18 +948,29 @@ VcmState vcm_state_carve(void* block, uint32_t paths, uint32_t max_len, uint32_t
     st.paths = paths;
     st.slots_per_path = slots;
     st.consts_capacity = passes;
+}
+
+}  // namespace
+
+VcmState vcm_state_carve(void* block, uint32_t paths, uint32_t max_len, uint32_t passes) {
+    char* p = static_cast<char*>(block);
+    VcmState st;
+    vcm_layout(st, [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    }, paths, max_len, passes);
     return st;
 }
 
 size_t vcm_state_block_bytes(uint32_t paths, uint32_t max_len, uint32_t passes) {
-    auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t nv = size_t(paths) * (max_len - 1);
-    const size_t ntiles = (nv + kSortTile - 1) / kSortTile;
-    const size_t scan_n = std::max<size_t>(std::max<size_t>(paths + 1, 256 * ntiles), 1);
-    return r(80 * nv) + r(4ull * paths) + r(4ull * (paths + 1)) + 4 * r(4 * nv) + r(4ull * paths) +
-           r(4ull * (paths + 1)) + r(4 * 256 * ntiles) + r(4 * (256 * ntiles + 1)) +
-           r(4 * ((scan_n + kScanTile - 1) / kScanTile + 1)) + r(4 * 6 * kBoundsBlocks) + r(4 * 16) + r(4 * 4) +
-           r(sizeof(VcmConsts) * passes);
+    size_t total = 0;
+    VcmState st;
+    vcm_layout(st, [&](size_t bytes) {
+        total += (bytes + 255) & ~size_t(255);
+        return static_cast<char*>(nullptr);
+    }, paths, max_len, passes);
+    return total;
 }
 
 cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
@@ -796,13 +1018,26 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
     int bits = 0;
     while (bits < 32 && (uint64_t(N - 1) >> bits) != 0) ++bits;  // cells = N: keys below N
     const int radix_passes = (bits + 7) / 8;
-    const int path_grid = sms * 8;
     const uint32_t list_grid = std::min<uint32_t>((N + 255) / 256, uint32_t(sms) * 16);
     int cur = 0;
     for (int r = 0; r < radix_passes; ++r) cur ^= 1;
     P.sorted_index = st.vals[cur];
+    const int trace_grid = sms * 8;
+    const int shade_grid = sms * 8;
     for (uint32_t pass = 0; pass < passes; ++pass) {
-        k_light<<<path_grid, kBlock, 0, stream>>>(P);
+        // light sub-paths: vertices and light tracing
+        k_reset<<<1, 32, 0, stream>>>(st.counters);
+        k_l_generate<<<shade_grid, kBlock, 0, stream>>>(P);
+        for (uint32_t b = 0; b + 1 < set.max_len; ++b) {
+            const int cur = int(b & 1u);
+            k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
+            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            k_l_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
+            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
+        }
+        // hash grid over the stored vertices
         k_bounds<<<kBoundsBlocks, 256, 0, stream>>>(P);
         k_bounds_final<<<1, 32, 0, stream>>>(P, kBoundsBlocks);
         scan_exclusive(st.vcount, N, st.vpos, st.scan_tmp, stream);
@@ -817,7 +1052,18 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
                                                         st.vpos + N, 8 * r, st.hist_off, ntiles);
             from ^= 1;
         }
-        k_camera<<<path_grid, kBlock, 0, stream>>>(P);
+        // camera sub-paths: next-event estimation, connections, merging
+        k_reset<<<1, 32, 0, stream>>>(st.counters);
+        k_c_generate<<<shade_grid, kBlock, 0, stream>>>(P);
+        for (uint32_t b = 0; b < set.max_len; ++b) {
+            const int cur = int(b & 1u);
+            k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
+            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            k_c_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
+            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
+        }
         k_pass_end<<<1, 32, 0, stream>>>(st.iter);
     }
     return cudaGetLastError();

@@ -29,11 +29,26 @@ struct VcmSettings {
     uint32_t light_first, light_count;  // light set 0 within the scene's light array
 };
 
-// Device scratch of one VCM pass for `paths` light and camera paths (paths = width * height).
+// Device scratch of one VCM pass for `paths` light and camera paths (paths = width * height): the light
+// vertices, the wavefront path state and queues, the shadow queue and the hash grid.
 struct VcmState {
     float4* verts;        // light vertices, 5 x float4 each, max_len - 1 slots per light path
     uint32_t* vcount;     // stored vertices per light path
     uint32_t* vpos;       // exclusive scan of vcount (+ total)
+    // path state, one slot per path (slot = path index)
+    float4* po;           // origin, dVCM
+    float4* pd;           // direction, dVC
+    float4* pt;           // throughput, dVM
+    uint32_t* plen;       // path length in segments
+    uint64_t* prng;       // PCG32 state (the stream is a function of the pass and the slot)
+    float4* phit;         // t, u, v, triangle bits (all ones: miss)
+    uint32_t* queue[2];   // live path slots, ping-pong between bounces
+    // shadow queue: light tracing, next-event and connection segments with their contributions
+    float4* so;           // origin, tnear
+    float4* sd;           // direction, tfar
+    float4* sc;           // contribution, pixel bits (zero contribution: null entry)
+    uint32_t shadow_capacity;
+    uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor
     uint32_t* keys[2];    // radix-sort ping-pong: cell of each stored vertex
     uint32_t* vals[2];    // ... and its slot
     uint32_t* cell_count; // vertices per cell
@@ -42,7 +57,7 @@ struct VcmState {
     uint32_t* hist_off;   // their exclusive scan
     uint32_t* scan_tmp;   // tile sums of the scans
     float* bounds_part;   // per-block bound partials
-    float* grid;          // lo[3], hi[3], inv_cell, radius2, vertex total (bits), cells (bits)
+    float* grid;          // lo[3], hi[3], inv_cell, radius2
     uint32_t* iter;       // current row of the constants table
     VcmConsts* consts;    // constants table
     uint32_t paths, slots_per_path, consts_capacity;

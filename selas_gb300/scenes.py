@@ -394,3 +394,69 @@ def textured_spheres(count: int = 6, level: int = 3, log2: int = 4, seed: int = 
                  radiance=(30.0, 28.0, 25.0))
     cam = dict(position=(0.0, 3.0, -11.0), look_at=(0.0, 1.5, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=55.0)
     return RenderScene(g, mats, [(0, light)], (0.05, 0.05, 0.08), cam, ptex)
+
+
+def _noise_texels_f32(n_faces: int, log2: int, rng: np.random.Generator, lattice: int = 4, lo: float = 0.1,
+                      hi: float = 0.9, chunk: int = 1 << 15) -> np.ndarray:
+    """value_noise_texels computed in float32 chunks (the same construction; large meshes)."""
+    res = 1 << log2
+    out = np.empty((n_faces, res, res, 3), np.float16)
+    t = (np.arange(res, dtype=np.float32) + 0.5) / res * (lattice - 1)
+    i0 = np.minimum(np.floor(t).astype(int), lattice - 2)
+    fr = (t - i0).astype(np.float32)
+    for s in range(0, n_faces, chunk):
+        e = min(n_faces, s + chunk)
+        grid = rng.uniform(lo, hi, size=(e - s, lattice, lattice, 3)).astype(np.float32)
+        rows = grid[:, i0, :, :] * (1 - fr)[None, :, None, None] + grid[:, i0 + 1, :, :] * fr[None, :, None, None]
+        out[s:e] = rows[:, :, i0, :] * (1 - fr)[None, None, :, None] + rows[:, :, i0 + 1, :] * fr[None, None, :, None]
+    return out.reshape(-1)
+
+
+def vcm_room(icospheres: int = 24, level: int = 6, glass: int = 40, glass_level: int = 3, log2: int = 4,
+             seed: int = 0x5E1A5003) -> RenderScene:
+    """The VCM scene: displaced icospheres (per-face Ptex value-noise base colour, 16 x 16 FP16 texels) and
+    glass spheres (specTrans 1, ior 1.5) inside a 20 x 20 x 10 room shell lit by one 2 x 2 quad light
+    below the ceiling.  Per mesh: roughness U[0.05, 1], metallic Bernoulli(0.3), baseColor U[0.1, 0.9]^3.
+    Defaults: 24 x 81,920 + 40 x 1,280 + 12 = 2,017,292 triangles."""
+    rng = np.random.default_rng(seed)
+    unit_v, f = icosphere(level)
+    face_table = ptex_faces(f, log2)  # same topology for every icosphere
+    g = TriangleScene()
+    mats, ptex = {}, {}
+
+    def disney(**kw):
+        m = dict(shader=1, lightSetIndex=0, roughness=float(rng.uniform(0.05, 1.0)),
+                 metallic=float(rng.random() < 0.3), ior=1.5,
+                 baseColor=tuple(float(x) for x in rng.uniform(0.1, 0.9, 3)))
+        m.update(kw)
+        return m
+
+    gid = 0
+    for _ in range(icospheres):
+        radius = rng.uniform(0.6, 1.5)
+        centre = np.array([rng.uniform(-8.0, 8.0), rng.uniform(radius, 6.0), rng.uniform(-8.0, 8.0)])
+        disp = 1.0 + 0.1 * value_noise_dirs(unit_v, rng)
+        g.add(gid, (centre + unit_v * (radius * disp)[:, None]).astype(np.float32), f.astype(np.uint32))
+        mats[gid] = disney(usesPtex=1)
+        ptex[gid] = (face_table, _noise_texels_f32(f.shape[0], log2, rng))
+        gid += 1
+    gv, gf = icosphere(glass_level)
+    for _ in range(glass):
+        radius = rng.uniform(0.3, 0.8)
+        centre = np.array([rng.uniform(-8.0, 8.0), rng.uniform(radius, 6.0), rng.uniform(-8.0, 8.0)])
+        g.add(gid, (centre + gv * radius).astype(np.float32), gf.astype(np.uint32))
+        mats[gid] = disney(specTrans=1.0, metallic=0.0, baseColor=(1.0, 1.0, 1.0))
+        gid += 1
+    # room shell, faces pointing inwards: floor y=0, ceiling y=10, walls at x, z = +-10
+    lo, hi = -10.0, 10.0
+    c = np.array([[lo, 0, lo], [hi, 0, lo], [hi, 0, hi], [lo, 0, hi], [lo, 10, lo], [hi, 10, lo], [hi, 10, hi],
+                  [lo, 10, hi]], np.float32)
+    quads = [(0, 3, 2, 1), (4, 5, 6, 7), (0, 1, 5, 4), (2, 3, 7, 6), (1, 2, 6, 5), (3, 0, 4, 7)]
+    tris = np.array([[q[0], q[1], q[2]] for q in quads] + [[q[0], q[2], q[3]] for q in quads], np.uint32)
+    g.add(gid, c, tris)
+    mats[gid] = disney(usesPtex=1, metallic=0.0)
+    ptex[gid] = (ptex_faces(tris, log2), _noise_texels_f32(tris.shape[0], log2, rng))
+    light = dict(position=(0.0, 9.9, 0.0), direction=(0.0, -1.0, 0.0), x=(2.0, 0.0, 0.0), z=(0.0, 0.0, 2.0),
+                 radiance=(40.0, 38.0, 34.0))
+    cam = dict(position=(0.0, 5.0, -9.5), look_at=(0.0, 3.0, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=75.0)
+    return RenderScene(g, mats, [(0, light)], (0.0, 0.0, 0.0), cam, ptex)

@@ -100,3 +100,14 @@ def test_gpu_batching_does_not_change_the_image(device, cornell):
     a = _gpu_image(device, cornell, 48, 8, paths_in_flight=0)
     b = _gpu_image(device, cornell, 48, 8, paths_in_flight=5000)
     np.testing.assert_allclose(a, b, rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_gpu_same_image_on_both_bvh_layouts(device, cornell):
+    import selas_gb300 as sel
+    imgs = []
+    for kind in (sel.SEL_BVH_WIDE8_Q8, sel.SEL_BVH_BINARY_FP32):
+        sc = cornell.build(sel, device, bvh_kind=kind)
+        imgs.append(sc.pt_generate_image(cornell.sel_camera(sel, 48, 48), sel.pt_settings(8)))
+        sc.release()
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)

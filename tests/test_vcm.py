@@ -144,3 +144,16 @@ def test_gpu_vcm_full_size(device, cornell):
     ref = np.load(VCM_REF)["image"].astype(np.float64)
     img = _gpu_vcm(device, cornell, 720, 8, radius=0.0)
     assert np.isfinite(img).all() and (img >= 0).all()
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_same_image_on_both_bvh_layouts(device, cornell):
+    """The quantised 8-wide BVH returns the plain binary FP32 BVH's hits bit for bit, so both trace the
+    same paths; the images differ only by the order of FP64 splats."""
+    import selas_gb300 as sel
+    imgs = []
+    for kind in (sel.SEL_BVH_WIDE8_Q8, sel.SEL_BVH_BINARY_FP32):
+        sc = cornell.build(sel, device, bvh_kind=kind)
+        imgs.append(sc.vcm_generate_image(cornell.sel_camera(sel, 32, 32), sel.vcm_settings(3, radius=R0)))
+        sc.release()
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
