@@ -40,7 +40,6 @@ constexpr float kFloatMax = 3.402823466e+38f;
 constexpr int kScanTile = 2048;  // 256 threads x 8
 constexpr int kSortTile = 4096;  // 256 threads x 16
 constexpr int kBoundsBlocks = 256;
-constexpr uint32_t kErrQueueOverflow = 8u;
 
 struct VcmParams {
     const void* nodes;
@@ -261,10 +260,6 @@ __device__ __forceinline__ void push_shadow(const VcmParams& P, uint32_t slot, c
     P.st.sc[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
 }
 
-__device__ __forceinline__ void push_null_shadow(const VcmParams& P, uint32_t slot) {
-    P.st.sc[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-}
-
 __global__ void k_reset(uint32_t* counters) {
     if (threadIdx.x < 8) counters[threadIdx.x] = 0u;
 }
@@ -272,9 +267,11 @@ __global__ void k_reset(uint32_t* counters) {
 __global__ void k_bounce_reset(uint32_t* counters, int next) {
     if (threadIdx.x == 0) {
         counters[next] = 0u;
-        counters[2] = 0u;
-        counters[3] = 0u;
-        counters[4] = 0u;
+        counters[2] = 0u;  // shadow entries
+        counters[3] = 0u;  // extend cursor
+        counters[4] = 0u;  // shadow cursor
+        counters[5] = 0u;  // camera-vertex records
+        counters[6] = 0u;  // connection pairs
     }
 }
 
@@ -725,34 +722,68 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t* keys_in, 
 }
 
 // ---------------------------------------------------------------------------------------------------
-// Camera sub-path vertices (EvaluateCameraPaths, VCM.cpp:576-666): MIS update, next-event estimation (tech
-// report sec. 5.4), connections to the vertices of the light path with the same index (ConnectPathVertices,
-// VCM.cpp:293-359) and merging with the light vertices of the 2x2x2 cells around the vertex (MergeVertices
-// + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155), then scattering.  Next-event and connection
-// segments go to the shadow queue: each lane reserves one entry per candidate (warp-aggregated) and fills
-// the candidates whose BSDF product is zero with null entries.  Merged radiance goes straight to the pixel.
+// Camera sub-path vertices (EvaluateCameraPaths, VCM.cpp:576-666), in three kernels so that lanes of a warp
+// do the same work: k_c_shade (MIS update, next-event estimation, a camera-vertex record, one connection
+// entry per eligible light vertex, scattering), k_c_connect (one thread per camera-vertex / light-vertex
+// pair: ConnectPathVertices, VCM.cpp:293-359) and k_c_merge (one warp per camera vertex over the light
+// vertices of the 2x2x2 cells around it: MergeVertices + SearchHashGrid, VCM.cpp:362-409,
+// VCMHashGrid.cpp:107-155).  Next-event and connection segments go to the shadow queue; merged radiance
+// goes straight to the pixel.
 // ---------------------------------------------------------------------------------------------------
+
+// Camera vertex record: 96 bytes.
+struct CameraVertex {
+    float3 pos, n, view, base, thr;
+    float err, cont, dvcm, dvc, dvm;
+    uint32_t mat, pixel, len, transparent;
+};
+
+__device__ __forceinline__ void store_camera_vertex(float4* v, const VHit& h, const PathState& st, uint32_t pixel) {
+    v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, h.err);
+    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(h.mat));
+    v[2] = make_float4(h.view.x, h.view.y, h.view.z, h.cont);
+    v[3] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, __uint_as_float(pixel));
+    v[4] = make_float4(st.thr.x, st.thr.y, st.thr.z, __uint_as_float(st.len));
+    v[5] = make_float4(st.dvcm, st.dvc, st.dvm, __uint_as_float(h.transparent ? 1u : 0u));
+}
+
+__device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
+    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], f = v[5];
+    CameraVertex cv;
+    cv.pos = f3(a.x, a.y, a.z);
+    cv.err = a.w;
+    cv.n = f3(b.x, b.y, b.z);
+    cv.mat = __float_as_uint(b.w);
+    cv.view = f3(c.x, c.y, c.z);
+    cv.cont = c.w;
+    cv.base = f3(d.x, d.y, d.z);
+    cv.pixel = __float_as_uint(d.w);
+    cv.thr = f3(e.x, e.y, e.z);
+    cv.len = __float_as_uint(e.w);
+    cv.dvcm = f.x;
+    cv.dvc = f.y;
+    cv.dvm = f.z;
+    cv.transparent = __float_as_uint(f.w);
+    return cv;
+}
+
 __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[cur];
     const uint32_t N = P.npaths;
     const int next = cur ^ 1;
-    const float* grid = P.st.grid;
-    const uint32_t total_vertices = P.st.vpos[N];
-    const float3 glo = f3(grid[0], grid[1], grid[2]), ghi = f3(grid[3], grid[4], grid[5]);
-    const float ginv = grid[6], gr2 = grid[7];
-    const uint32_t* cell_start = P.st.cell_start;
-    const uint32_t capacity = P.st.shadow_capacity;
     uint32_t status = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
-        bool cont = false, hit_ok = false;
-        uint32_t s = 0, nee = 0, nvc = 0;
+        bool cont = false, hit_ok = false, nee_ray = false, record = false;
+        uint32_t s = 0, nvc = 0;
         VHit h;
         PathState st;
         Pcg32 rng;
         rng.state = 0;
         rng.inc = 1;
+        float3 to_l = f3(0.0f), contrib = f3(0.0f);
+        float tfar = 0.0f;
         if (e < n) {
             s = P.st.queue[cur][e];
             const float4 hit = P.st.phit[s];
@@ -769,135 +800,222 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur) {
                 st.dvm *= 1.0f / cos_in;
                 rng = load_rng(P, s, (uint64_t(c.pass) * 2 + 1) * N + s);
                 if (!h.delta) {
-                    nee = (st.len + 1 <= P.max_len && P.light_count > 0) ? 1u : 0u;
+                    record = true;
+                    // next-event estimation to light set 0 (tech report sec. 5.4; wLight = 0)
+                    if (st.len + 1 <= P.max_len && P.light_count > 0) {
+                        const float pick = pcg_float(rng);
+                        uint32_t li = uint32_t(pick * float(P.light_count));
+                        li = li < P.light_count - 1 ? li : P.light_count - 1;
+                        const QuadLight L = P.lights[li];
+                        const float u = pcg_float(rng), v = pcg_float(rng);
+                        const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                        const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                        to_l = lp - h.pos;
+                        const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
+                        to_l = to_l * (1.0f / dl);
+                        const float cos_light = dot(normalize(L.direction), -to_l);
+                        if (cos_light > 0.0f) {
+                            float fwd, rev;
+                            const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                            if (nonzero(f)) {
+                                rev *= h.cont;
+                                const float light_pick = 1.0f / float(P.light_count);
+                                const float direct_pdf_w = pdf_a * dl2 / cos_light;
+                                const float emission_pdf_w = pdf_a * cos_light / kPi;
+                                const float cos_to_light = fabsf(dot(h.n, to_l));
+                                const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
+                                                       (c.vm_weight + st.dvcm + st.dvc * rev);
+                                const float mis = 1.0f / (1.0f + w_camera);
+                                contrib = st.thr * ((mis / (light_pick * direct_pdf_w)) * (L.radiance * f));
+                                tfar = dl * (1.0f - 1e-4f);
+                                nee_ray = nonzero(contrib);
+                            }
+                        }
+                    }
+                    // light vertices of path s that a connection may join (path length bound)
                     const uint32_t lcount = P.st.vcount[s];
                     const float4* lslots = P.st.verts + size_t(s) * P.slots * 5;
                     while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * 5].w) + 1 + st.len <= P.max_len) ++nvc;
                 }
             }
         }
-        uint32_t slot = warp_reserve(&P.st.counters[2], nee + nvc);
-        if (hit_ok && slot + nee + nvc > capacity) {  // cannot happen with capacity N * max_len
-            status |= kErrQueueOverflow;
-            nee = nvc = 0;
-        }
-        if (hit_ok && !h.delta) {
-            const uint32_t pixel = s;
-            if (nee) {
-                const float pick = pcg_float(rng);
-                uint32_t li = uint32_t(pick * float(P.light_count));
-                li = li < P.light_count - 1 ? li : P.light_count - 1;
-                const QuadLight L = P.lights[li];
-                const float u = pcg_float(rng), v = pcg_float(rng);
-                const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                const float pdf_a = 1.0f / (length(L.x) * length(L.z));
-                float3 to_l = lp - h.pos;
-                const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
-                to_l = to_l * (1.0f / dl);
-                const float cos_light = dot(normalize(L.direction), -to_l);
-                bool pushed = false;
-                if (cos_light > 0.0f) {
-                    float fwd, rev;
-                    const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
-                    if (nonzero(f)) {
-                        rev *= h.cont;
-                        const float light_pick = 1.0f / float(P.light_count);
-                        const float direct_pdf_w = pdf_a * dl2 / cos_light;
-                        const float emission_pdf_w = pdf_a * cos_light / kPi;
-                        const float cos_to_light = fabsf(dot(h.n, to_l));
-                        const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
-                                               (c.vm_weight + st.dvcm + st.dvc * rev);
-                        const float mis = 1.0f / (1.0f + w_camera);
-                        const float3 contrib = st.thr * ((mis / (light_pick * direct_pdf_w)) * (L.radiance * f));
-                        push_shadow(P, slot, h, to_l, dl * (1.0f - 1e-4f), contrib, pixel);
-                        pushed = true;
-                    }
-                }
-                if (!pushed) push_null_shadow(P, slot);
-                ++slot;
+        // camera-vertex record with the state at the vertex, its connection pairs, the next-event segment
+        const uint32_t vi = warp_append(&P.st.counters[5], record);
+        if (record) store_camera_vertex(P.st.cverts + size_t(vi) * 6, h, st, s);
+        const uint32_t pair0 = warp_reserve(&P.st.counters[6], nvc);
+        for (uint32_t k = 0; k < nvc; ++k) P.st.pairs[pair0 + k] = make_uint2(vi, k);
+        const uint32_t sq = warp_append(&P.st.counters[2], nee_ray);
+        if (nee_ray) push_shadow(P, sq, h, to_l, tfar, contrib, s);
+        if (hit_ok) {
+            if (st.len < P.max_len) {
+                cont = scatter(rng, h, c, st, false);
+                if (cont) store_path(P, s, st);
             }
-            const float4* lslots = P.st.verts + size_t(s) * P.slots * 5;
-            for (uint32_t k = 0; k < nvc; ++k, ++slot) {
-                const LightVertex lv = load_vertex(lslots + size_t(k) * 5);
-                float3 dir = lv.pos - h.pos;
-                const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
-                dir = dir * (1.0f / dist);
-                float cfwd, crev, lfwd, lrev;
-                const float3 cf = bsdf_evaluate(h.s, h.view, dir, cfwd, crev);
-                if (!nonzero(cf)) { push_null_shadow(P, slot); continue; }
-                const MaterialDev& lm = P.materials[lv.mat];
-                const Surface ls = make_surface_linear(lm, lv.n, lv.view, lv.base);
-                const float lcont = continuation_probability(ls);
-                const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
-                const float lcos_view = fabsf(dot(lv.n, lv.view));
-                const float3 lf = lcos_view > 0.0f ? lfa * (fabsf(dot(lv.n, dir)) / lcos_view) : f3(0.0f);
-                if (!nonzero(lf)) { push_null_shadow(P, slot); continue; }
-                cfwd *= h.cont; crev *= h.cont;
-                lfwd *= lcont; lrev *= lcont;
-                const float cos_cam_v = fabsf(dot(dir, h.n));
-                const float cos_light_v = fabsf(dot(-dir, lv.n));
-                const float cam_pdf_a = cfwd * cos_light_v / dist2;
-                const float light_pdf_a = lfwd * cos_cam_v / dist2;
-                const float w_light = cam_pdf_a * (c.vm_weight + lv.dvcm + lv.dvc * lrev);
-                const float w_camera = light_pdf_a * (c.vm_weight + st.dvcm + st.dvc * crev);
-                const float mis = 1.0f / (w_light + 1.0f + w_camera);
-                const float3 contrib = st.thr * lv.thr * ((mis / dist2) * (cf * lf));
-                const float bias = 0.1f * h.err;
-                push_shadow(P, slot, h, dir, dist - 16.0f * bias, contrib, pixel);
-            }
-            // vertex merging
-            float3 merged = f3(0.0f);
-            const float3 dmin = h.pos - glo, dmax = ghi - h.pos;
-            if (P.merging && total_vertices > 0 && dmin.x >= 0.0f && dmin.y >= 0.0f && dmin.z >= 0.0f &&
-                dmax.x >= 0.0f && dmax.y >= 0.0f && dmax.z >= 0.0f) {
-                const uint32_t* idx = P.sorted_index;
-                const float3 cp = ginv * dmin;
-                const float fx = floorf(cp.x), fy = floorf(cp.y), fz = floorf(cp.z);
-                const int x0 = int(fx) - (cp.x - fx < 0.5f ? 1 : 0);
-                const int y0 = int(fy) - (cp.y - fy < 0.5f ? 1 : 0);
-                const int z0 = int(fz) - (cp.z - fz < 0.5f ? 1 : 0);
-                for (int dz = 0; dz <= 1; ++dz)
-                    for (int dy = 0; dy <= 1; ++dy)
-                        for (int dx = 0; dx <= 1; ++dx) {
-                            const uint32_t cell = cell_hash(x0 + dx, y0 + dy, z0 + dz, N);
-                            const uint32_t b = cell_start[cell], eidx = cell_start[cell + 1];
-                            for (uint32_t k = b; k < eidx; ++k) {
-                                const float4* vp = P.st.verts + size_t(idx[k]) * 5;
-                                const float4 a = vp[0];
-                                const float3 dd = h.pos - f3(a.x, a.y, a.z);
-                                if (dot(dd, dd) > gr2) continue;
-                                const LightVertex lv = load_vertex(vp);
-                                if (st.len + lv.len > P.max_len) continue;
-                                const MaterialDev& lm = P.materials[lv.mat];
-                                // the reference merges only between surfaces of the same transparency
-                                // (VCM.cpp:372-375)
-                                if (h.transparent != ((lm.flags & kMaterialTransparent) != 0u)) continue;
-                                float fwd, rev;
-                                const float3 fc = bsdf_evaluate(h.s, h.view, lv.view, fwd, rev);
-                                const float cosl = fabsf(dot(h.n, lv.view));
-                                if (!nonzero(fc) || cosl == 0.0f) continue;
-                                const float lcont = saturate(max3(lv.base));
-                                fwd *= h.cont;
-                                rev *= lcont;
-                                const float w_light = lv.dvcm * c.vc_weight + lv.dvm * fwd;
-                                const float w_camera = st.dvcm * c.vc_weight + st.dvm * rev;
-                                const float mis = 1.0f / (w_light + 1.0f + w_camera);
-                                merged = merged + (mis / cosl) * (fc * lv.thr);
-                            }
-                        }
-            }
-            const float3 mc = c.vm_norm * (st.thr * merged);
-            if (nonzero(mc)) splat(P.accum, pixel, mc);
+            P.st.prng[s] = rng.state;
         }
-        if (hit_ok && st.len < P.max_len) {
-            cont = scatter(rng, h, c, st, false);
-            if (cont) store_path(P, s, st);
-        }
-        if (hit_ok) P.st.prng[s] = rng.state;
         const uint32_t q = warp_append(&P.st.counters[next], cont);
         if (cont) P.st.queue[next][q] = s;
     }
     if (status) atomicOr(P.err, status);
+}
+
+// One thread per (camera vertex, light vertex) pair: ConnectPathVertices (VCM.cpp:293-359), with the light
+// side oriented f(v = toward the camera vertex, l = toward the previous light vertex) and the cosine at the
+// connection carried.
+__global__ void __launch_bounds__(kBlock) k_c_connect(VcmParams P) {
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t n = P.st.counters[6];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        bool ray = false;
+        float3 dir = f3(0.0f), contrib = f3(0.0f);
+        float tfar = 0.0f;
+        CameraVertex cv;
+        cv.pixel = 0;
+        if (e < n) {
+            const uint2 pr = P.st.pairs[e];
+            cv = load_camera_vertex(P.st.cverts + size_t(pr.x) * 6);
+            const LightVertex lv = load_vertex(P.st.verts + (size_t(cv.pixel) * P.slots + pr.y) * 5);
+            dir = lv.pos - cv.pos;
+            const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
+            dir = dir * (1.0f / dist);
+            const Surface cs = make_surface_linear(P.materials[cv.mat], cv.n, cv.view, cv.base);
+            float cfwd, crev, lfwd, lrev;
+            const float3 cf = bsdf_evaluate(cs, cv.view, dir, cfwd, crev);
+            if (nonzero(cf)) {
+                const Surface ls = make_surface_linear(P.materials[lv.mat], lv.n, lv.view, lv.base);
+                const float lcont = continuation_probability(ls);
+                const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
+                const float lcos_view = fabsf(dot(lv.n, lv.view));
+                const float3 lf = lcos_view > 0.0f ? lfa * (fabsf(dot(lv.n, dir)) / lcos_view) : f3(0.0f);
+                if (nonzero(lf)) {
+                    cfwd *= cv.cont; crev *= cv.cont;
+                    lfwd *= lcont; lrev *= lcont;
+                    const float cos_cam_v = fabsf(dot(dir, cv.n));
+                    const float cos_light_v = fabsf(dot(-dir, lv.n));
+                    const float cam_pdf_a = cfwd * cos_light_v / dist2;
+                    const float light_pdf_a = lfwd * cos_cam_v / dist2;
+                    const float w_light = cam_pdf_a * (c.vm_weight + lv.dvcm + lv.dvc * lrev);
+                    const float w_camera = light_pdf_a * (c.vm_weight + cv.dvcm + cv.dvc * crev);
+                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                    contrib = cv.thr * lv.thr * ((mis / dist2) * (cf * lf));
+                    const float bias = 0.1f * cv.err;
+                    tfar = dist - 16.0f * bias;
+                    ray = nonzero(contrib);
+                }
+            }
+        }
+        const uint32_t sq = warp_append(&P.st.counters[2], ray);
+        if (ray) {
+            const float3 o = offset_origin(cv.pos, cv.n, cv.err, dir, 0.1f);
+            P.st.so[sq] = make_float4(o.x, o.y, o.z, cv.err);
+            P.st.sd[sq] = make_float4(dir.x, dir.y, dir.z, tfar);
+            P.st.sc[sq] = make_float4(contrib.x, contrib.y, contrib.z, __uint_as_float(cv.pixel));
+        }
+    }
+}
+
+// Positions of the stored vertices in cell order (position, slot bits): the merge's distance test reads
+// consecutive entries.
+__global__ void __launch_bounds__(256) k_gather_positions(VcmParams P) {
+    const uint32_t total = P.st.vpos[P.npaths];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const uint32_t slot = P.sorted_index[k];
+        const float4 a = P.st.verts[size_t(slot) * 5];
+        P.st.spos[k] = make_float4(a.x, a.y, a.z, __uint_as_float(slot));
+    }
+}
+
+// One warp per camera vertex (MergeVertices + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155;
+// tech report sec. 5.6): the ranges of the 2x2x2 cells around it are concatenated, lanes stride over the
+// concatenation (a cell visited twice when two of the eight cells hash to one bucket, as the sequential
+// search visits it), each lane keeps a partial sum and a fixed xor-tree reduction adds them.
+__global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
+    const VcmConsts c = P.st.consts[*P.st.iter];
+    const uint32_t n = P.st.counters[5];
+    const uint32_t N = P.npaths;
+    const float* grid = P.st.grid;
+    if (!P.merging || P.st.vpos[N] == 0) return;
+    const float3 glo = f3(grid[0], grid[1], grid[2]), ghi = f3(grid[3], grid[4], grid[5]);
+    const float ginv = grid[6], gr2 = grid[7];
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+        const float4* rec = P.st.cverts + size_t(i) * 6;
+        const float4 r0 = rec[0];
+        const float3 pos = f3(r0.x, r0.y, r0.z);
+        const float3 dmin = pos - glo, dmax = ghi - pos;
+        if (!(dmin.x >= 0.0f && dmin.y >= 0.0f && dmin.z >= 0.0f && dmax.x >= 0.0f && dmax.y >= 0.0f &&
+              dmax.z >= 0.0f))
+            continue;  // uniform across the warp
+        const float3 cp = ginv * dmin;
+        const float fx = floorf(cp.x), fy = floorf(cp.y), fz = floorf(cp.z);
+        const int x0 = int(fx) - (cp.x - fx < 0.5f ? 1 : 0);
+        const int y0 = int(fy) - (cp.y - fy < 0.5f ? 1 : 0);
+        const int z0 = int(fz) - (cp.z - fz < 0.5f ? 1 : 0);
+        // lane j < 8 owns cell j = (dx, dy, dz) in the search order dz, dy, dx
+        uint32_t cb = 0, cn = 0;
+        if (lane < 8) {
+            const int dx = int(lane & 1u), dy = int((lane >> 1) & 1u), dz = int(lane >> 2);
+            const uint32_t cell = cell_hash(x0 + dx, y0 + dy, z0 + dz, N);
+            cb = P.st.cell_start[cell];
+            cn = P.st.cell_start[cell + 1] - cb;
+        }
+        uint32_t incl = cn;  // inclusive prefix of the counts over lanes 0..7
+        for (int o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= uint32_t(o)) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 7);
+        if (total == 0) continue;
+        uint32_t bases[8], ends[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            bases[j] = __shfl_sync(0xffffffffu, cb, j);
+            ends[j] = __shfl_sync(0xffffffffu, incl, j);
+        }
+        const CameraVertex cv = load_camera_vertex(rec);
+        const Surface cs = make_surface_linear(P.materials[cv.mat], cv.n, cv.view, cv.base);
+        float3 merged = f3(0.0f);
+        for (uint32_t t = lane; t < total; t += 32) {
+            int j = 0;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) j += t >= ends[q] ? 1 : 0;
+            uint32_t start = 0, b = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q == j) { b = bases[q]; start = q > 0 ? ends[q - 1] : 0u; }
+            const uint32_t k = b + (t - start);
+            const float4 sp = P.st.spos[k];
+            const float3 dd = pos - f3(sp.x, sp.y, sp.z);
+            if (dot(dd, dd) > gr2) continue;
+            const LightVertex lv = load_vertex(P.st.verts + size_t(__float_as_uint(sp.w)) * 5);
+            if (cv.len + lv.len > P.max_len) continue;
+            // the reference merges only between surfaces of the same transparency (VCM.cpp:372-375)
+            const uint32_t lt = (P.materials[lv.mat].flags & kMaterialTransparent) ? 1u : 0u;
+            if (cv.transparent != lt) continue;
+            float fwd, rev;
+            const float3 fc = bsdf_evaluate(cs, cv.view, lv.view, fwd, rev);
+            const float cosl = fabsf(dot(cv.n, lv.view));
+            if (!nonzero(fc) || cosl == 0.0f) continue;
+            const float lcont = saturate(max3(lv.base));
+            fwd *= cv.cont;
+            rev *= lcont;
+            const float w_light = lv.dvcm * c.vc_weight + lv.dvm * fwd;
+            const float w_camera = cv.dvcm * c.vc_weight + cv.dvm * rev;
+            const float mis = 1.0f / (w_light + 1.0f + w_camera);
+            merged = merged + (mis / cosl) * (fc * lv.thr);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            merged.x += __shfl_xor_sync(0xffffffffu, merged.x, o);
+            merged.y += __shfl_xor_sync(0xffffffffu, merged.y, o);
+            merged.z += __shfl_xor_sync(0xffffffffu, merged.z, o);
+        }
+        if (lane == 0) {
+            const float3 mc = c.vm_norm * (cv.thr * merged);
+            if (nonzero(mc)) splat(P.accum, cv.pixel, mc);
+        }
+    }
 }
 
 __global__ void k_pass_end(uint32_t* iter) {
@@ -932,6 +1050,9 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.sc = reinterpret_cast<float4*>(take(16 * shadow));
     st.shadow_capacity = uint32_t(shadow);
     st.counters = reinterpret_cast<uint32_t*>(take(4 * 16));
+    st.cverts = reinterpret_cast<float4*>(take(96ull * paths));
+    st.pairs = reinterpret_cast<uint2*>(take(8 * nv));
+    st.spos = reinterpret_cast<float4*>(take(16 * nv));
     for (int k = 0; k < 2; ++k) {
         st.keys[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
         st.vals[k] = reinterpret_cast<uint32_t*>(take(4 * nv));
@@ -1052,6 +1173,7 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
                                                         st.vpos + N, 8 * r, st.hist_off, ntiles);
             from ^= 1;
         }
+        k_gather_positions<<<list_grid, 256, 0, stream>>>(P);
         // camera sub-paths: next-event estimation, connections, merging
         k_reset<<<1, 32, 0, stream>>>(st.counters);
         k_c_generate<<<shade_grid, kBlock, 0, stream>>>(P);
@@ -1061,6 +1183,8 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
             if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
             else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
             k_c_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            k_c_connect<<<shade_grid, kBlock, 0, stream>>>(P);
+            k_c_merge<<<shade_grid, kBlock, 0, stream>>>(P);
             if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
             else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
         }

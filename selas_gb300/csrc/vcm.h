@@ -48,7 +48,11 @@ struct VcmState {
     float4* sd;           // direction, tfar
     float4* sc;           // contribution, pixel bits (zero contribution: null entry)
     uint32_t shadow_capacity;
-    uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor
+    uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor,
+                          // [5] camera-vertex records, [6] connection pairs
+    float4* cverts;       // camera-vertex records of the current bounce, 6 x float4 each
+    uint2* pairs;         // (camera-vertex record, light-vertex index) connection pairs of the current bounce
+    float4* spos;         // stored-vertex positions in cell order, slot bits in w
     uint32_t* keys[2];    // radix-sort ping-pong: cell of each stored vertex
     uint32_t* vals[2];    // ... and its slot
     uint32_t* cell_count; // vertices per cell
