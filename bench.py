@@ -48,6 +48,8 @@ def parse_args():
     p.add_argument("--cpu-sample", type=int, default=2097152, help="rays per query set in each CPU sample step")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-render", action="store_true", help="skip the path-tracer and VCM measurements")
+    p.add_argument("--vcm-passes", type=int, default=256, help="VCM iterations timed on the quantised BVH")
     return p.parse_args()
 
 
@@ -187,6 +189,75 @@ def run_reference(args):
                 "same query contract (binned-SAH BVH, watertight test) stands in for it",
     }
     print(json.dumps(line), flush=True)
+
+
+def render_metrics(sel, scenes, dev, stream, args):
+    """Integrator throughput on both BVH layouts (they return identical hits, so both trace the same paths
+    and reach the same image rMSE): the Cornell path tracer (512 x 512, 64 spp, depth 8) and VCM on the room
+    scene (1280 x 720, length 10, r0 = 0.003 x the scene diagonal, alpha 0.75)."""
+    import ctypes
+
+    import torch
+    lib = sel.lib()
+    sp = stream.cuda_stream
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    out = {}
+    cornell = scenes.cornell_box()
+    pt = {}
+    for kind, name in ((sel.SEL_BVH_WIDE8_Q8, "quantised_wide8"), (sel.SEL_BVH_BINARY_FP32, "plain_fp32_binary")):
+        sc = cornell.build(sel, dev, bvh_kind=kind)
+        cam = cornell.sel_camera(sel, 512, 512)
+        acc = torch.zeros((2, 512, 512, 3), dtype=torch.float64, device="cuda")
+        st = sel.pt_settings(64, 8)
+        ms = timed(lambda: sel.check(lib.sel_pt_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(st),
+                                                                acc.data_ptr(), sp)), 3)
+        pt[name] = {"ms_per_image": round(ms, 3), "paths_per_s": round(512 * 512 * 64 / (ms * 1e-3), 1)}
+        sc.release()
+    pt["speedup_of_quantised_wide"] = round(pt["quantised_wide8"]["paths_per_s"] / pt["plain_fp32_binary"]["paths_per_s"], 3)
+    out["pt"] = {"workload": "Cornell box, 512x512, 64 spp, max depth 8, one jittered PCG32 sample per pass", **pt}
+
+    t0 = time.time()
+    room = scenes.vcm_room()
+    gen_s = time.time() - t0
+    lo, hi = room.geometry.bounds()
+    r0 = 0.003 * float(np.linalg.norm(hi - lo))
+    w, h = 1280, 720
+    vcm = {}
+    for kind, name, passes in ((sel.SEL_BVH_WIDE8_Q8, "quantised_wide8", args.vcm_passes),
+                               (sel.SEL_BVH_BINARY_FP32, "plain_fp32_binary", max(1, args.vcm_passes // 4))):
+        t0 = time.time()
+        sc = room.build(sel, dev, bvh_kind=kind)
+        build_s = time.time() - t0
+        cam = room.sel_camera(sel, w, h)
+        acc = torch.zeros((h, w, 3), dtype=torch.float64, device="cuda")
+        warm = sel.vcm_settings(1, 10, radius=r0)
+        sel.check(lib.sel_vcm_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(warm), acc.data_ptr(), sp))
+        st = sel.vcm_settings(passes, 10, radius=r0)
+        ms = timed(lambda: sel.check(lib.sel_vcm_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(st),
+                                                                 acc.data_ptr(), sp)), 1) if passes else 0.0
+        dev.sync(sp)
+        vcm[name] = {"passes": passes, "ms_per_pass": round(ms / passes, 3),
+                     "paths_per_s": round(2 * w * h * passes / (ms * 1e-3), 1), "scene_upload_and_build_s": round(build_s, 2)}
+        sc.release()
+    vcm["speedup_of_quantised_wide"] = round(vcm["quantised_wide8"]["paths_per_s"] / vcm["plain_fp32_binary"]["paths_per_s"], 3)
+    out["vcm"] = {"workload": f"room 20x20x10 with {room.geometry.triangle_count} triangles (24 displaced icospheres "
+                              f"with 16x16 FP16 Ptex per face, 40 glass spheres), 1280x720, max path length 10, "
+                              f"r0 {r0:.4f} (0.003 x diagonal), alpha 0.75",
+                  "paths": "light + camera sub-paths (2 x 1280 x 720 per pass)", "scene_generation_s": round(gen_s, 1),
+                  **vcm}
+    out["equal_rmse"] = "both layouts return identical hits, so they trace the same paths (tests: same image)"
+    return out
 
 
 def run_ours(args):
@@ -331,6 +402,13 @@ def run_ours(args):
                "sample": f"{q} queries (4 x {args.cpu_sample} rays of each set, closest+any) on {cpu_desc()}, "
                          f"{t:.1f} s"}
 
+    render = None
+    if not args.no_render and rank == 0:
+        for k in list(work):  # release the ray sets first
+            del work[k], pristine[k]
+        torch.cuda.empty_cache()
+        render = render_metrics(sel, scenes, dev, stream, args)
+
     per_set = {k: round(counts[k] / (per_kernel[k] * 1e-3) / 1e6, 1) for k in per_kernel}
     per_set_b = {k: round(counts[k] / (per_kernel_b[k] * 1e-3) / 1e6, 1) for k in per_kernel_b}
     line = {
@@ -348,6 +426,7 @@ def run_ours(args):
         "clocks": clocks,
         "gpu_launches": 4 * args.steps,
         "per_set_mrays": per_set,
+        "render": render,
         "plain_fp32_binary_bvh": {"value": round(plain_value, 3), "unit": "Mrays/s", "per_set_mrays": per_set_b,
                                   "bvh_nodes": int(binfo.node_count), "bvh_device_mb": round(binfo.device_bytes / 2**20, 1),
                                   "speedup_of_quantised_wide": round(value / world / plain_value, 3)},
