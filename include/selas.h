@@ -99,6 +99,13 @@ int sel_device_release(SelDevice device);
  * word since the last call (the word is cleared by the call). */
 int sel_device_sync(SelDevice device, void* stream);
 
+/* Device options (no reference counterpart: tuning switches of this implementation). */
+enum {
+    SEL_OPTION_GRAPH_REPLAY = 1  /* 1 (default): the integrators capture one path batch / VCM pass as a CUDA
+                                    graph per argument set and replay it; 0: launch kernel by kernel */
+};
+int sel_device_set_option(SelDevice device, int option, int value);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Scene lifetime.  Replaces rtcNewScene, rtcNewGeometry(RTC_GEOMETRY_TYPE_TRIANGLE) +               */
 /* rtcSetSharedGeometryBuffer + rtcAttachGeometryByID, rtcCommitScene and rtcReleaseScene as used in */

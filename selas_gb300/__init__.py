@@ -21,6 +21,7 @@ SEL_ERR_CUDA = 3
 SEL_ERR_INVALID_OPERATION = 4
 SEL_ERR_DEVICE_LIMIT = 5
 
+SEL_OPTION_GRAPH_REPLAY = 1
 SEL_BVH_WIDE8_Q8 = 0
 SEL_BVH_BINARY_FP32 = 1
 
@@ -127,6 +128,9 @@ class Device:
 
     def sync(self, stream: int | None = None) -> None:
         check(lib().sel_device_sync(self.handle, stream))
+
+    def set_option(self, option: int, value: int) -> None:
+        check(lib().sel_device_set_option(self.handle, option, value))
 
     def release(self) -> None:
         if self.handle:
@@ -257,6 +261,7 @@ register_signatures({
     "sel_scene_set_ptex": [_vp, _u, _vp, _sz, _vp, _sz],
     "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
     "sel_vcm_settings_defaults": [ctypes.POINTER(SelVcmSettings)],
+    "sel_device_set_option": [_vp, ctypes.c_int, ctypes.c_int],
     "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
     "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
 })

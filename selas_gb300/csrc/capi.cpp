@@ -222,6 +222,18 @@ int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info) {
     return SEL_OK;
 }
 
+int sel_device_set_option(SelDevice device, int option, int value) {
+    if (!device) return fail(SEL_ERR_INVALID_ARGUMENT, "device is null");
+    std::lock_guard<std::mutex> lock(device->mu);
+    switch (option) {
+        case SEL_OPTION_GRAPH_REPLAY:
+            device->graph_replay = value != 0;
+            return SEL_OK;
+        default:
+            return fail(SEL_ERR_INVALID_ARGUMENT, "unknown option");
+    }
+}
+
 int sel_scene_release(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     set_device(scene->dev);

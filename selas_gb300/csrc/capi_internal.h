@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include "graph.h"
 #include "scene_types.h"
 #include "sel_internal.h"
 
@@ -14,6 +15,7 @@ struct SelDeviceTy {
     int cuda_device = 0;
     cudaStream_t stream = nullptr;  // internal stream for the host-memory entry points
     uint32_t* d_err = nullptr;      // kernel error word (iteration cap / stack overflow bits)
+    bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     std::mutex mu;
 };
 
@@ -53,6 +55,8 @@ struct SelSceneTy {
     // VCM scratch: light vertices, hash grid and constants table for `vcm_paths` paths per pass
     void* vcm_block = nullptr;
     uint32_t vcm_paths = 0, vcm_len = 0, vcm_passes = 0;
+    // captured per-batch / per-pass launch graphs of the integrators
+    sel::GraphCache pt_graph, vcm_graph;
     std::mutex mu;
 };
 

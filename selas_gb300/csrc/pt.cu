@@ -14,6 +14,7 @@
 #include <cstring>
 
 #include "capi_internal.h"
+#include "graph.h"
 #include "ptex.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
@@ -40,8 +41,7 @@ struct PtParams {
     CameraDev cam;
     uint32_t width, height;
     uint64_t seed;
-    uint64_t first_path;
-    uint32_t batch;
+    uint64_t total;  // paths of the whole render (width * height * spp)
     uint32_t max_bounces;
     double* accum;  // [2][height*width][3]
     PtState st;
@@ -74,8 +74,18 @@ __device__ __forceinline__ Pcg32 load_rng(const PtState& st, uint32_t slot) {
     return r;
 }
 
-__global__ void k_reset(uint32_t* counters, uint32_t first_queue_count) {
-    if (threadIdx.x < kPtCounters) counters[threadIdx.x] = threadIdx.x == 0 ? first_queue_count : 0u;
+// Batch set-up from the device-resident first path of the batch: every batch launches the same kernels with
+// the same arguments, so one batch can be captured as a graph and replayed.
+__global__ void k_batch_begin(PtParams P) {
+    const uint64_t first = *P.st.first;
+    const uint64_t left = P.total > first ? P.total - first : 0;
+    const uint32_t batch = uint32_t(left < P.st.capacity ? left : P.st.capacity);
+    if (threadIdx.x < kPtCounters) P.st.counters[threadIdx.x] = threadIdx.x == 0 ? batch : 0u;
+    if (threadIdx.x == kPtCounters) P.st.counters[kPtCounters] = batch;
+}
+
+__global__ void k_batch_end(PtParams P) {
+    if (threadIdx.x == 0) *P.st.first += P.st.capacity;
 }
 
 __global__ void k_bounce_reset(uint32_t* counters, int next) {
@@ -90,8 +100,10 @@ __global__ void k_bounce_reset(uint32_t* counters, int next) {
 
 __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
     const uint32_t npix = P.width * P.height;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < P.batch; s += gridDim.x * blockDim.x) {
-        const uint64_t path = P.first_path + s;
+    const uint32_t batch = P.st.counters[kPtCounters];
+    const uint64_t first = *P.st.first;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < batch; s += gridDim.x * blockDim.x) {
+        const uint64_t path = first + s;
         const uint32_t pixel = uint32_t(path % npix);
         Pcg32 rng = pcg_seed(P.seed, path);
         const uint32_t y = pixel / P.width, x = pixel - y * P.width;
@@ -351,6 +363,7 @@ PtState pt_state_carve(void* block, uint32_t paths) {
     st.sh_d = reinterpret_cast<float4*>(take(16ull * paths));
     st.sh_c = reinterpret_cast<float4*>(take(16ull * paths));
     st.counters = reinterpret_cast<uint32_t*>(take(64 * sizeof(uint32_t)));
+    st.first = reinterpret_cast<uint64_t*>(st.counters + 16);
     st.capacity = paths;
     return st;
 }
@@ -362,7 +375,7 @@ size_t pt_state_block_bytes(uint32_t paths) {
 }
 
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
-                      uint32_t* d_err, cudaStream_t stream) {
+                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -393,14 +406,13 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     P.st = st;
     P.err = d_err;
     const uint64_t total = uint64_t(cam.width) * cam.height * set.spp;
+    P.total = total;
     const int trace_grid = grid_for(sms, 8);
     const int shade_grid = grid_for(sms, 8);
-    for (uint64_t first = 0; first < total; first += st.capacity) {
-        const uint32_t batch = uint32_t(total - first < st.capacity ? total - first : st.capacity);
-        P.first_path = first;
-        P.batch = batch;
-        k_reset<<<1, 32, 0, stream>>>(st.counters, batch);
-        k_generate<<<(batch + kBlock - 1) / kBlock, kBlock, 0, stream>>>(P);
+    const int gen_grid = int((st.capacity + kBlock - 1) / kBlock);
+    auto enqueue = [&](cudaStream_t stream) {
+        k_batch_begin<<<1, 32, 0, stream>>>(P);
+        k_generate<<<gen_grid, kBlock, 0, stream>>>(P);
         for (uint32_t b = 0; b < set.max_bounces; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
@@ -410,8 +422,22 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
             if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
             else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
         }
-    }
-    return cudaGetLastError();
+        k_batch_end<<<1, 32, 0, stream>>>(P);
+    };
+    cudaError_t e = cudaMemsetAsync(st.first, 0, sizeof(uint64_t), stream);
+    if (e != cudaSuccess) return e;
+    const uint64_t batches = (total + st.capacity - 1) / st.capacity;
+    struct Key {
+        PtParams P;
+        int kind, sms;
+        uint32_t max_bounces;
+    } key;
+    std::memset(&key, 0, sizeof(key));
+    std::memcpy(&key.P, &P, sizeof(P));
+    key.kind = sc.bvh_kind;
+    key.sms = sms;
+    key.max_bounces = set.max_bounces;
+    return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -6,12 +6,15 @@
 
 #include <cuda_runtime.h>
 
+#include "graph.h"
+
 namespace sel {
 
 struct MaterialDev;
 struct QuadLight;
 
-constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors
+constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
+                                // [8] holds the current batch size
 
 // Device-resident path state (structure of arrays), carved from one allocation.
 struct PtState {
@@ -28,6 +31,7 @@ struct PtState {
     float4* sh_d;     // direction, tfar
     float4* sh_c;     // contribution, pixel (bits)
     uint32_t* counters;
+    uint64_t* first;  // first path of the current batch (device-resident, inside the counters block)
     uint32_t capacity;
 };
 
@@ -60,8 +64,9 @@ struct PtSettings {
 
 size_t pt_state_block_bytes(uint32_t paths);
 PtState pt_state_carve(void* block, uint32_t paths);
+// With `graphs`, one batch of paths is captured as a CUDA graph (once per argument set) and replayed per batch.
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
-                      uint32_t* d_err, cudaStream_t stream);
+                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs);
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream);
 
 }  // namespace sel

@@ -165,7 +165,8 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     set.max_bounces = settings.maxBounces;
     set.seed = settings.seed;
     const PtState st = pt_state_carve(sc->pt_block, cap);
-    cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream);
+    cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream,
+                              sc->dev->graph_replay ? &sc->pt_graph : nullptr);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
 }
 
@@ -269,7 +270,8 @@ int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSetti
         consts.resize(n);
         for (uint32_t k = 0; k < n; ++k)
             vcm_constants(radius0, settings.radiusAlpha, paths, set.merging != 0, settings.firstPass + done + k, consts[k]);
-        cudaError_t e = vcm_render(ps, cam, set, consts.data(), n, st, d_accum, sc->dev->d_err, stream);
+        cudaError_t e = vcm_render(ps, cam, set, consts.data(), n, st, d_accum, sc->dev->d_err, stream,
+                                   sc->dev->graph_replay ? &sc->vcm_graph : nullptr);
         if (e != cudaSuccess) return cuda_fail(e, "VCM launch");
         // the constants table is read by the passes just queued: wait before it is refilled
         if (done + n < settings.passes) {

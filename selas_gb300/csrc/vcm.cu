@@ -27,6 +27,7 @@
 #include <cstring>
 
 #include "capi_internal.h"
+#include "graph.h"
 #include "ptex.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
@@ -1095,7 +1096,8 @@ size_t vcm_state_block_bytes(uint32_t paths, uint32_t max_len, uint32_t passes) 
 }
 
 cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
-                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream) {
+                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
+                       GraphCache* graphs) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1145,7 +1147,8 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
     P.sorted_index = st.vals[cur];
     const int trace_grid = sms * 8;
     const int shade_grid = sms * 8;
-    for (uint32_t pass = 0; pass < passes; ++pass) {
+    // one pass; identical launches every pass (the pass reads its constants through st.iter)
+    auto enqueue = [&](cudaStream_t stream) {
         // light sub-paths: vertices and light tracing
         k_reset<<<1, 32, 0, stream>>>(st.counters);
         k_l_generate<<<shade_grid, kBlock, 0, stream>>>(P);
@@ -1189,8 +1192,17 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
             else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
         }
         k_pass_end<<<1, 32, 0, stream>>>(st.iter);
-    }
-    return cudaGetLastError();
+    };
+    struct Key {
+        VcmParams P;
+        int kind, sms, radix_passes;
+    } key;
+    std::memset(&key, 0, sizeof(key));
+    std::memcpy(&key.P, &P, sizeof(P));
+    key.kind = sc.bvh_kind;
+    key.sms = sms;
+    key.radix_passes = radix_passes;
+    return replay(graphs, &key, sizeof(key), stream, passes, enqueue);
 }
 
 }  // namespace sel

@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include "graph.h"
 #include "pt.h"
 
 namespace sel {
@@ -78,7 +79,9 @@ struct VcmCamera {
 
 // Runs passes [first, first + passes).  Accumulates into d_accum ([height][width][3] doubles) the sum of
 // the passes' images.
+// With `graphs`, one pass is captured as a CUDA graph (once per argument set) and replayed per pass.
 cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
-                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream);
+                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
+                       GraphCache* graphs);
 
 }  // namespace sel

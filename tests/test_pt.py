@@ -111,3 +111,16 @@ def test_gpu_same_image_on_both_bvh_layouts(device, cornell):
         imgs.append(sc.pt_generate_image(cornell.sel_camera(sel, 48, 48), sel.pt_settings(8)))
         sc.release()
     np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_graph_replay_matches_direct_launches(device, cornell):
+    """Batches replayed from one captured CUDA graph (here 12 batches of 2,000 paths) give the image of
+    kernel-by-kernel launches."""
+    import selas_gb300 as sel
+    imgs = []
+    for replay in (1, 0):
+        device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, replay)
+        imgs.append(_gpu_image(device, cornell, 40, 15, paths_in_flight=2000))
+    device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)

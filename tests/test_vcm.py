@@ -157,3 +157,15 @@ def test_gpu_vcm_same_image_on_both_bvh_layouts(device, cornell):
         imgs.append(sc.vcm_generate_image(cornell.sel_camera(sel, 32, 32), sel.vcm_settings(3, radius=R0)))
         sc.release()
     np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_graph_replay_matches_direct_launches(device, cornell):
+    """Passes replayed from one captured CUDA graph give the image of kernel-by-kernel launches."""
+    import selas_gb300 as sel
+    imgs = []
+    for replay in (1, 0):
+        device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, replay)
+        imgs.append(_gpu_vcm(device, cornell, 40, 5))
+    device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
