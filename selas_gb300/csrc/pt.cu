@@ -1,6 +1,11 @@
 // Wavefront unidirectional path tracer: the GB300 form of PathTracer::GenerateImage / EvaluatePath
 // (Source/Applications/Selas/Source/PathTracer.cpp:142-258, 261-349).
 //
+// The wavefront is shared by up to kMaxPtJobs render jobs (scene, camera, spp, seed, accumulator) held in a
+// device-resident job table: a batch takes up to `quota` paths from each job, every path carries its job
+// slot, and each kernel reads the job's scene, camera and accumulator through it.  A single render is the
+// one-job case.
+//
 // Per batch of paths: generate -> for each bounce: extend (closest hit) -> shade (surface setup, quad-light
 // NEE, BSDF sampling, Russian roulette) -> shadow (any hit).  Queues hold path slots; appends are
 // warp-aggregated (one atomic per warp).  Contributions go straight into an FP64 per-pixel accumulator
@@ -27,26 +32,20 @@ constexpr int kBlock = 128;
 constexpr float kFloatMax = 3.402823466e+38f;  // FloatMax_ (SystemLib/BasicTypes.h:31)
 
 struct PtParams {
-    const void* nodes;
-    const float4* tris;
-    const MaterialDev* materials;
-    uint32_t material_count;
-    const QuadLight* lights;
-    const uint2* light_sets;  // (first light, count) per set
-    uint32_t light_set_count;
-    const PtexFace* ptex_faces;
-    const __half* ptex_texels;
-    uint32_t ptex_face_count;
-    float3 background;
-    CameraDev cam;
-    uint32_t width, height;
-    uint64_t seed;
-    uint64_t total;  // paths of the whole render (width * height * spp)
-    uint32_t max_bounces;
-    double* accum;  // [2][height*width][3]
     PtState st;
     uint32_t* err;
 };
+
+__device__ __forceinline__ CameraDev camera_of(const PtCamera& c) {
+    CameraDev d;
+    d.x = make_float3(c.x[0], c.x[1], c.x[2]);
+    d.y = make_float3(c.y[0], c.y[1], c.y[2]);
+    d.z = make_float3(c.z[0], c.z[1], c.z[2]);
+    d.position = make_float3(c.position[0], c.position[1], c.position[2]);
+    d.width = float(c.width);
+    d.height = float(c.height);
+    return d;
+}
 
 // Warp-aggregated append: returns this lane's slot in a queue whose length lives at *count.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* count, bool want) {
@@ -70,22 +69,40 @@ __device__ __forceinline__ void accumulate(double* accum, uint32_t npix, int lay
 __device__ __forceinline__ Pcg32 load_rng(const PtState& st, uint32_t slot) {
     Pcg32 r;
     r.state = st.rng[slot];
-    r.inc = (uint64_t(st.path_id[slot]) << 1u) | 1u;
+    r.inc = (st.path_id[slot] << 1u) | 1u;
     return r;
 }
 
-// Batch set-up from the device-resident first path of the batch: every batch launches the same kernels with
-// the same arguments, so one batch can be captured as a graph and replayed.
+// Batch set-up: each job slot contributes min(paths left, quota) paths; counts, prefix and the batch size are
+// derived here from the device-resident control block, so every batch launches the same kernels with the
+// same arguments and one batch can be captured as a graph and replayed.
 __global__ void k_batch_begin(PtParams P) {
-    const uint64_t first = *P.st.first;
-    const uint64_t left = P.total > first ? P.total - first : 0;
-    const uint32_t batch = uint32_t(left < P.st.capacity ? left : P.st.capacity);
-    if (threadIdx.x < kPtCounters) P.st.counters[threadIdx.x] = threadIdx.x == 0 ? batch : 0u;
-    if (threadIdx.x == kPtCounters) P.st.counters[kPtCounters] = batch;
+    PtControl& c = *P.st.control;
+    const uint32_t lane = threadIdx.x;  // one warp
+    uint32_t cnt = 0;
+    if (lane < c.njobs && lane < kMaxPtJobs) {
+        const uint64_t total = P.st.jobs[lane].total, next = c.next[lane];
+        const uint64_t left = total > next ? total - next : 0;
+        cnt = uint32_t(left < c.quota[lane] ? left : c.quota[lane]);
+    }
+    uint32_t incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= uint32_t(o)) incl += y;
+    }
+    const uint32_t batch = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane < kMaxPtJobs) {
+        c.count[lane] = cnt;
+        c.prefix[lane] = incl - cnt;
+    }
+    if (lane == 0) c.prefix[kMaxPtJobs] = batch;
+    if (lane < kPtCounters) P.st.counters[lane] = lane == 0 ? batch : 0u;
+    if (lane == kPtCounters) P.st.counters[kPtCounters] = batch;
 }
 
 __global__ void k_batch_end(PtParams P) {
-    if (threadIdx.x == 0) *P.st.first += P.st.capacity;
+    PtControl& c = *P.st.control;
+    if (threadIdx.x < kMaxPtJobs) c.next[threadIdx.x] += c.count[threadIdx.x];
 }
 
 __global__ void k_bounce_reset(uint32_t* counters, int next) {
@@ -99,23 +116,30 @@ __global__ void k_bounce_reset(uint32_t* counters, int next) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
-    const uint32_t npix = P.width * P.height;
+    const PtControl& c = *P.st.control;
     const uint32_t batch = P.st.counters[kPtCounters];
-    const uint64_t first = *P.st.first;
+    const uint32_t njobs = c.njobs < kMaxPtJobs ? c.njobs : kMaxPtJobs;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < batch; s += gridDim.x * blockDim.x) {
-        const uint64_t path = first + s;
+        uint32_t j = 0;
+        while (j + 1 < njobs && s >= c.prefix[j + 1]) ++j;
+        const PtJob& J = P.st.jobs[j];
+        const uint64_t path = c.next[j] + (s - c.prefix[j]);
+        const uint32_t width = J.cam.width;
+        const uint32_t npix = width * J.cam.height;
         const uint32_t pixel = uint32_t(path % npix);
-        Pcg32 rng = pcg_seed(P.seed, path);
-        const uint32_t y = pixel / P.width, x = pixel - y * P.width;
+        Pcg32 rng = pcg_seed(J.seed, path);
+        const uint32_t y = pixel / width, x = pixel - y * width;
         const float vx = float(x) + pcg_float(rng);  // JitteredCameraRay (Camera.cpp:63-74)
         const float vy = float(y) + pcg_float(rng);
-        const float3 d = camera_direction(P.cam, vx, vy);
-        P.st.ray_o[s] = make_float4(P.cam.position.x, P.cam.position.y, P.cam.position.z, 0.0f);
+        const CameraDev cam = camera_of(J.cam);
+        const float3 d = camera_direction(cam, vx, vy);
+        P.st.ray_o[s] = make_float4(cam.position.x, cam.position.y, cam.position.z, 0.0f);
         P.st.ray_d[s] = make_float4(d.x, d.y, d.z, kFloatMax);
         P.st.thr[s] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);  // w = isDeltaOnly
         P.st.medium[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // x = phase (0 vacuum, 1 isotropic)
         P.st.pixel[s] = pixel;
-        P.st.path_id[s] = uint32_t(path);
+        P.st.job[s] = j;
+        P.st.path_id[s] = path;
         P.st.rng[s] = rng.state;
         P.st.queue[0][s] = s;
     }
@@ -127,6 +151,7 @@ template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     const uint32_t* queue = P.st.queue[cur];
     uint32_t status = 0;
     for (;;) {
@@ -158,7 +183,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = tfar;
             QueryHit h;
-            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock,
+            const PtScene& sc = P.st.jobs[P.st.job[s]].scene;
+            const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x, kBlock,
                                                                 status);
             P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
                                 : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
@@ -169,7 +195,6 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
 
 __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce) {
     const uint32_t n = P.st.counters[cur];
-    const uint32_t npix = P.width * P.height;
     const int next = cur ^ 1;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
@@ -179,6 +204,10 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
         float4 sh_o = make_float4(0, 0, 0, 0), sh_d = sh_o, sh_c = sh_o;
         if (valid) {
             s = P.st.queue[cur][e];
+            const uint32_t job = P.st.job[s];
+            const PtJob& J = P.st.jobs[job];
+            const PtScene& S = J.scene;
+            const uint32_t npix = J.cam.width * J.cam.height;
             const float4 o4 = P.st.ray_o[s], d4 = P.st.ray_d[s];
             const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
             float4 thr4 = P.st.thr[s];
@@ -199,11 +228,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
             }
             bool alive = true;
             if (tri != 0xffffffffu) {
-                const float4* tp = P.tris + size_t(tri) * 3;
+                const float4* tp = S.tris + size_t(tri) * 3;
                 const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
                 const float3 ng = triangle_ng(p0, p1, p2);
                 const uint32_t geom = __float_as_uint(p1.w);
-                const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+                const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
                 // RayPick error bound (PathTracer.cpp:134-136)
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
@@ -211,22 +240,23 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 if (m.flags & kMaterialUsesPtex) {
                     // per-face Ptex base colour at the hit's barycentrics (SurfaceParameters.cpp:196-206)
                     uint32_t pstatus = 0;
-                    ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels,
-                              int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z, base, pstatus);
+                    ptex_eval(static_cast<const PtexFace*>(S.ptex_faces), int(S.ptex_face_count),
+                              static_cast<const __half*>(S.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                              hit.z, base, pstatus);
                     if (pstatus) atomicOr(P.err, pstatus);
                 }
                 const Surface sf = make_surface(m, ng, -d, base);
                 // Next-event estimation to the surface's light set (AreaLighting.cpp:353-373)
                 LightSample ls;
                 ls.radiance = f3(0.0f);
-                if (m.light_set < P.light_set_count) {
-                    const uint2 set = P.light_sets[m.light_set];
+                if (m.light_set < S.light_set_count) {
+                    const uint2 set = S.light_sets[m.light_set];
                     if (set.y > 0) {
                         const float p0u = pcg_float(rng);
                         uint32_t li = uint32_t(p0u * float(set.y));
                         li = li < set.y ? li : set.y - 1;
                         const float u = pcg_float(rng), v = pcg_float(rng);
-                        sample_quad_light(P.lights[set.x + li], pos, sf.n, u, v, ls);
+                        sample_quad_light(S.lights[set.x + li], pos, sf.n, u, v, ls);
                         ls.pdf *= 1.0f / float(set.y);
                     }
                 }
@@ -239,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                         const float3 c = refl * ls.radiance * (1.0f / ls.pdf) * thr;
                         sh_o = make_float4(so.x, so.y, so.z, err);
                         sh_d = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.distance);
-                        sh_c = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
+                        sh_c = make_float4(c.x, c.y, c.z, __uint_as_float((job << 28) | pixel));
                         shadow = true;
                     }
                 }
@@ -263,7 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                     const float3 no = offset_origin(pos, sf.n, err, bs.wi, 1.0f);
                     P.st.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
                     P.st.ray_d[s] = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, kFloatMax);
-                    if (bounce == 0) accumulate(P.accum, npix, 0, pixel, bs.reflectance);
+                    if (bounce == 0) accumulate(J.accum, npix, 0, pixel, bs.reflectance);
                 }
             } else if (med.x != 0.0f) {
                 // scatter inside the medium: Isotropic::SampleScatterDirection -> CSampler::UniformSphere
@@ -277,7 +307,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 P.st.ray_d[s] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
             } else {
                 // miss: background (EvaluateBackground / EvaluateBackgroundMiss without an IBL)
-                accumulate(P.accum, npix, 1, pixel, P.background * thr);
+                accumulate(J.accum, npix, 1, pixel, f3(S.background[0], S.background[1], S.background[2]) * thr);
                 alive = false;
             }
             if (alive) {
@@ -287,7 +317,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                     if (pcg_float(rng) > cp) alive = false;
                     else thr = thr * (1.0f / cp);
                 }
-                cont = alive && nb < P.max_bounces;
+                cont = alive && nb < J.max_bounces;
             }
             P.st.thr[s] = make_float4(thr.x, thr.y, thr.z, thr4.w);
             P.st.medium[s] = med;
@@ -308,7 +338,7 @@ template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[2];
-    const uint32_t npix = P.width * P.height;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     uint32_t status = 0;
     for (;;) {
         uint32_t base = 0;
@@ -318,14 +348,16 @@ __global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
         const uint32_t e = base + (threadIdx.x & 31u);
         if (e < n) {
             const float4 o = P.st.sh_o[e], d = P.st.sh_d[e];
+            const float4 c = P.st.sh_c[e];
+            const uint32_t tag = __float_as_uint(c.w);
+            const PtJob& J = P.st.jobs[tag >> 28];
             QueryRay q;
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
             QueryHit h;
-            if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status)) {
-                const float4 c = P.st.sh_c[e];
-                accumulate(P.accum, npix, 1, __float_as_uint(c.w), f3(c.x, c.y, c.z));
-            }
+            if (!Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, kBlock,
+                                                 status))
+                accumulate(J.accum, J.cam.width * J.cam.height, 1, tag & 0x0fffffffu, f3(c.x, c.y, c.z));
         }
     }
     if (status) atomicOr(P.err, status);
@@ -341,21 +373,17 @@ int grid_for(int sm_count, int blocks_per_sm) { return sm_count * blocks_per_sm;
 }  // namespace
 
 // Carves the path state of `paths` slots out of one device block (the caller owns the block).
-PtState pt_state_carve(void* block, uint32_t paths) {
-    char* p = static_cast<char*>(block);
-    PtState st;
-    auto take = [&](size_t bytes) {
-        char* r = p;
-        p += (bytes + 255) & ~size_t(255);
-        return r;
-    };
+namespace {
+template <typename Take>
+void pt_layout(PtState& st, Take take, uint32_t paths) {
     st.ray_o = reinterpret_cast<float4*>(take(16ull * paths));
     st.ray_d = reinterpret_cast<float4*>(take(16ull * paths));
     st.thr = reinterpret_cast<float4*>(take(16ull * paths));
     st.medium = reinterpret_cast<float4*>(take(16ull * paths));
     st.hit = reinterpret_cast<float4*>(take(16ull * paths));
     st.pixel = reinterpret_cast<uint32_t*>(take(4ull * paths));
-    st.path_id = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.job = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.path_id = reinterpret_cast<uint64_t*>(take(8ull * paths));
     st.rng = reinterpret_cast<uint64_t*>(take(8ull * paths));
     st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
@@ -363,81 +391,92 @@ PtState pt_state_carve(void* block, uint32_t paths) {
     st.sh_d = reinterpret_cast<float4*>(take(16ull * paths));
     st.sh_c = reinterpret_cast<float4*>(take(16ull * paths));
     st.counters = reinterpret_cast<uint32_t*>(take(64 * sizeof(uint32_t)));
-    st.first = reinterpret_cast<uint64_t*>(st.counters + 16);
+    st.rays = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+    st.control = reinterpret_cast<PtControl*>(take(sizeof(PtControl)));
+    st.jobs = reinterpret_cast<PtJob*>(take(sizeof(PtJob) * kMaxPtJobs));
     st.capacity = paths;
+}
+}  // namespace
+
+PtState pt_state_carve(void* block, uint32_t paths) {
+    char* p = static_cast<char*>(block);
+    PtState st;
+    pt_layout(st, [&](size_t bytes) {
+        char* r = p;
+        p += (bytes + 255) & ~size_t(255);
+        return r;
+    }, paths);
     return st;
 }
 
 size_t pt_state_block_bytes(uint32_t paths) {
-    // each carve is rounded up to 256 bytes
-    auto r = [](size_t b) { return (b + 255) & ~size_t(255); };
-    return r(16ull * paths) * 9 + r(4ull * paths) * 4 + r(8ull * paths) + r(64 * sizeof(uint32_t));
+    size_t total = 0;
+    PtState st;
+    pt_layout(st, [&](size_t bytes) {
+        total += (bytes + 255) & ~size_t(255);
+        return static_cast<char*>(nullptr);
+    }, paths);
+    return total;
 }
 
-cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
-                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs) {
+cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, uint32_t* d_err, uint64_t batches,
+                           cudaStream_t stream, GraphCache* graphs) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     PtParams P;
     std::memset(&P, 0, sizeof(P));
-    P.nodes = sc.nodes;
-    P.tris = sc.tris;
-    P.materials = sc.materials;
-    P.material_count = sc.material_count;
-    P.lights = sc.lights;
-    P.light_sets = sc.light_sets;
-    P.light_set_count = sc.light_set_count;
-    P.ptex_faces = static_cast<const PtexFace*>(sc.ptex_faces);
-    P.ptex_texels = static_cast<const __half*>(sc.ptex_texels);
-    P.ptex_face_count = sc.ptex_face_count;
-    P.background = make_float3(sc.background[0], sc.background[1], sc.background[2]);
-    P.cam.x = make_float3(cam.x[0], cam.x[1], cam.x[2]);
-    P.cam.y = make_float3(cam.y[0], cam.y[1], cam.y[2]);
-    P.cam.z = make_float3(cam.z[0], cam.z[1], cam.z[2]);
-    P.cam.position = make_float3(cam.position[0], cam.position[1], cam.position[2]);
-    P.cam.width = float(cam.width);
-    P.cam.height = float(cam.height);
-    P.width = cam.width;
-    P.height = cam.height;
-    P.seed = set.seed;
-    P.max_bounces = set.max_bounces;
-    P.accum = d_accum;
     P.st = st;
     P.err = d_err;
-    const uint64_t total = uint64_t(cam.width) * cam.height * set.spp;
-    P.total = total;
     const int trace_grid = grid_for(sms, 8);
     const int shade_grid = grid_for(sms, 8);
     const int gen_grid = int((st.capacity + kBlock - 1) / kBlock);
-    auto enqueue = [&](cudaStream_t stream) {
-        k_batch_begin<<<1, 32, 0, stream>>>(P);
-        k_generate<<<gen_grid, kBlock, 0, stream>>>(P);
-        for (uint32_t b = 0; b < set.max_bounces; ++b) {
+    auto enqueue = [&](cudaStream_t s) {
+        k_batch_begin<<<1, 32, 0, s>>>(P);
+        k_generate<<<gen_grid, kBlock, 0, s>>>(P);
+        for (uint32_t b = 0; b < bounces; ++b) {
             const int cur = int(b & 1u);
-            k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
-            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            k_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur, b);
-            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
-            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
+            k_bounce_reset<<<1, 32, 0, s>>>(st.counters, cur ^ 1);
+            if (bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, s>>>(P, cur);
+            else k_extend<1><<<trace_grid, kBlock, 0, s>>>(P, cur);
+            k_shade<<<shade_grid, kBlock, 0, s>>>(P, cur, b);
+            if (bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, s>>>(P);
+            else k_shadow<1><<<trace_grid, kBlock, 0, s>>>(P);
         }
-        k_batch_end<<<1, 32, 0, stream>>>(P);
+        k_batch_end<<<1, 32, 0, s>>>(P);
     };
-    cudaError_t e = cudaMemsetAsync(st.first, 0, sizeof(uint64_t), stream);
-    if (e != cudaSuccess) return e;
-    const uint64_t batches = (total + st.capacity - 1) / st.capacity;
     struct Key {
         PtParams P;
         int kind, sms;
-        uint32_t max_bounces;
+        uint32_t bounces;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
-    key.kind = sc.bvh_kind;
+    key.kind = bvh_kind;
     key.sms = sms;
-    key.max_bounces = set.max_bounces;
+    key.bounces = bounces;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
+}
+
+cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
+                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs) {
+    PtJob job;
+    std::memset(&job, 0, sizeof(job));
+    job.scene = sc;
+    job.cam = cam;
+    job.max_bounces = set.max_bounces;
+    job.seed = set.seed;
+    job.total = uint64_t(cam.width) * cam.height * set.spp;
+    job.accum = d_accum;
+    PtControl ctl;
+    std::memset(&ctl, 0, sizeof(ctl));
+    ctl.quota[0] = st.capacity;
+    ctl.njobs = 1;
+    cudaError_t e = cudaMemcpyAsync(st.jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st.control, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
+    return pt_run_batches(sc.bvh_kind, set.max_bounces, st, d_err, batches, stream, graphs);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

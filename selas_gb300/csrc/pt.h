@@ -15,26 +15,9 @@ struct QuadLight;
 
 constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
                                 // [8] holds the current batch size
+constexpr int kMaxPtJobs = 16;  // jobs sharing one wavefront (shadow records pack the job in 4 bits)
 
-// Device-resident path state (structure of arrays), carved from one allocation.
-struct PtState {
-    float4* ray_o;    // origin, tnear
-    float4* ray_d;    // direction, tfar
-    float4* thr;      // throughput, isDeltaOnly
-    float4* medium;   // phase (0 vacuum / 1 isotropic), extinction
-    float4* hit;      // t, u, v, triangle (bits; all ones = miss)
-    uint32_t* pixel;
-    uint32_t* path_id;
-    uint64_t* rng;
-    uint32_t* queue[2];
-    float4* sh_o;     // shadow rays: origin, tnear
-    float4* sh_d;     // direction, tfar
-    float4* sh_c;     // contribution, pixel (bits)
-    uint32_t* counters;
-    uint64_t* first;  // first path of the current batch (device-resident, inside the counters block)
-    uint32_t capacity;
-};
-
+// Scene view the integrators read.
 struct PtScene {
     const void* nodes;  // 8-wide quantised (bvh_kind 0) or binary FP32 (bvh_kind 1) node array
     int bvh_kind;
@@ -62,9 +45,60 @@ struct PtSettings {
     uint64_t seed;
 };
 
+// One render job of the shared wavefront (an entry of the device-resident job table).
+struct PtJob {
+    PtScene scene;
+    PtCamera cam;
+    uint32_t max_bounces;
+    uint32_t pad;
+    uint64_t seed;
+    uint64_t total;  // paths of the job: width * height * spp
+    double* accum;   // [2][height][width][3]
+};
+
+// Device-resident batch control: which paths of each job the next batch takes.  The host writes `next`
+// and `quota` when a job enters a slot; k_batch_begin derives count and prefix, k_batch_end advances next.
+struct PtControl {
+    uint64_t next[kMaxPtJobs];   // paths of the job already issued
+    uint32_t quota[kMaxPtJobs];  // paths of the job a batch may take (0: slot idle)
+    uint32_t count[kMaxPtJobs];  // paths of the job in the current batch
+    uint32_t prefix[kMaxPtJobs + 1];
+    uint32_t njobs;              // slots in use: 0..njobs-1
+    uint32_t pad[2];
+};
+
+// Device-resident path state (structure of arrays), carved from one allocation.
+struct PtState {
+    float4* ray_o;    // origin, tnear
+    float4* ray_d;    // direction, tfar
+    float4* thr;      // throughput, isDeltaOnly
+    float4* medium;   // phase (0 vacuum / 1 isotropic), extinction
+    float4* hit;      // t, u, v, triangle (bits; all ones = miss)
+    uint32_t* pixel;
+    uint32_t* job;    // job slot of the path
+    uint64_t* path_id;  // index of the path within its job (its PCG32 stream)
+    uint64_t* rng;
+    uint32_t* queue[2];
+    float4* sh_o;     // shadow rays: origin, tnear
+    float4* sh_d;     // direction, tfar
+    float4* sh_c;     // contribution, (job << 28 | pixel) bits
+    uint32_t* counters;
+    unsigned long long* rays;  // rays traced (closest + any hit), a running total
+    PtControl* control;
+    PtJob* jobs;      // job table (kMaxPtJobs entries)
+    uint32_t capacity;
+};
+
 size_t pt_state_block_bytes(uint32_t paths);
 PtState pt_state_carve(void* block, uint32_t paths);
-// With `graphs`, one batch of paths is captured as a CUDA graph (once per argument set) and replayed per batch.
+
+// Launches `batches` batches of the shared wavefront over the jobs in st.jobs / st.control (uploaded by the
+// caller).  `bounces` is the number of extend/shade/shadow rounds per batch (the largest max_bounces of the
+// jobs).  With `graphs`, one batch is captured as a CUDA graph and replayed.
+cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, uint32_t* d_err, uint64_t batches,
+                           cudaStream_t stream, GraphCache* graphs);
+
+// Single render (PathTracer::GenerateImage): one job, batches until all its paths are done.
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
                       uint32_t* d_err, cudaStream_t stream, GraphCache* graphs);
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream);
