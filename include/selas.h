@@ -317,6 +317,70 @@ int sel_vcm_generate_image(SelScene scene, const SelCamera* camera, const SelVcm
 int sel_vcm_render_device(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, double* d_accum,
                           void* stream);
 
+/* ------------------------------------------------------------------------------------------------ */
+/* Render server (no reference counterpart: the reference renders one image per process,            */
+/* main.cpp:120-123).  Jobs of differing scene, resolution, spp and integrator are admitted while   */
+/* device memory (a byte budget) and job slots allow, and their work overlaps on the GPU: path-tracer */
+/* jobs share the wavefront launches (a batch takes a fair share of paths from every admitted job),  */
+/* VCM jobs advance one pass per round on their own streams.  Scenes stay resident; each job holds   */
+/* its accumulator (and VCM state) from admission to completion.  A job's image does not depend on    */
+/* the other jobs: its paths use the same random streams alone and in a mix.                         */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct SelServerTy* SelServer;
+
+enum { SEL_INTEGRATOR_PT = 0, SEL_INTEGRATOR_VCM = 1 };
+
+typedef struct SelServerConfig {
+    uint64_t hbm_budget_bytes;  /* device bytes admitted jobs may hold (0: free HBM minus the reserve)  */
+    uint64_t hbm_reserve_bytes; /* left free when hbm_budget_bytes is 0 (default 2 GiB)                */
+    uint32_t max_jobs;          /* jobs admitted at once, 1..16 (default 16)                           */
+    uint32_t paths_in_flight;   /* shared path-tracer wavefront capacity (default 4,194,304)           */
+    uint32_t max_bounces;       /* bounce rounds of a shared batch; path-tracer jobs may ask for at most
+                                   this many (default 8)                                               */
+    uint32_t reserved;
+} SelServerConfig;
+
+typedef struct SelJob {
+    SelScene scene;             /* committed with SEL_BVH_WIDE8_Q8; must outlive the job               */
+    SelCamera camera;
+    uint32_t integrator;        /* SEL_INTEGRATOR_PT or SEL_INTEGRATOR_VCM                              */
+    uint32_t reserved;
+    SelPtSettings pt;           /* used by SEL_INTEGRATOR_PT (pathsInFlight is ignored)                 */
+    SelVcmSettings vcm;         /* used by SEL_INTEGRATOR_VCM                                           */
+} SelJob;
+
+typedef struct SelJobStats {
+    double queue_ms;            /* submit -> admission                                                  */
+    double run_ms;              /* admission -> result in host memory                                   */
+    double latency_ms;          /* submit -> result in host memory                                      */
+    uint64_t device_bytes;      /* device memory the job held                                           */
+    int32_t status;             /* SEL_OK or the error the job ended with                                */
+    uint32_t reserved;
+} SelJobStats;
+
+typedef struct SelServerStats {
+    uint64_t submitted, completed;
+    uint64_t rays;              /* closest-hit + any-hit rays traced by finished work                    */
+    uint64_t peak_jobs;         /* most jobs admitted at once                                           */
+    uint64_t peak_bytes;        /* most device bytes held by admitted jobs at once                      */
+    uint64_t graph_captures;    /* shared path-tracer batches captured as CUDA graphs                   */
+} SelServerStats;
+
+int sel_server_config_defaults(SelServerConfig* out);
+int sel_server_new(SelDevice device, const SelServerConfig* config, SelServer* out_server);
+/* Queues a job and returns at once with its id.  The result size is sel_server_result_floats. */
+int sel_server_submit(SelServer server, const SelJob* job, uint64_t* out_job_id);
+int sel_server_result_floats(const SelJob* job, size_t* out_floats);
+/* done = 1 when the job's result is in host memory. */
+int sel_server_poll(SelServer server, uint64_t job_id, int* out_done);
+/* Blocks until the job is done, copies its image (path tracer: the two layers [2][H][W][3] scaled by
+ * 1/spp; VCM: [H][W][3], the mean over the passes) to out (out_floats >= the result size) and its
+ * statistics to stats (may be null), and forgets the job.  Returns the job's status. */
+int sel_server_wait(SelServer server, uint64_t job_id, float* out, size_t out_floats, SelJobStats* stats);
+int sel_server_stats(SelServer server, SelServerStats* out);
+/* Finishes every queued job, then stops the server. */
+int sel_server_release(SelServer server);
+
 #ifdef __cplusplus
 }
 #endif

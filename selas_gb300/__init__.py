@@ -348,3 +348,102 @@ Scene.add_quad_light = _scene_add_quad_light
 Scene.set_background = _scene_set_background
 Scene.pt_generate_image = _scene_pt_generate_image
 Scene.vcm_generate_image = _scene_vcm_generate_image
+
+
+# ---------------------------------------------------------------------------------------------------
+# Render server (include/selas.h: sel_server_*)
+# ---------------------------------------------------------------------------------------------------
+SEL_INTEGRATOR_PT, SEL_INTEGRATOR_VCM = 0, 1
+
+
+class SelServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("hbm_reserve_bytes", ctypes.c_uint64),
+                ("max_jobs", ctypes.c_uint32), ("paths_in_flight", ctypes.c_uint32), ("max_bounces", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class SelJob(ctypes.Structure):
+    _fields_ = [("scene", _vp), ("camera", SelCamera), ("integrator", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("pt", SelPtSettings), ("vcm", SelVcmSettings)]
+
+
+class SelJobStats(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("device_bytes", ctypes.c_uint64), ("status", ctypes.c_int32), ("reserved", ctypes.c_uint32)]
+
+
+class SelServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in ("submitted", "completed", "rays", "peak_jobs", "peak_bytes",
+                                                "graph_captures")]
+
+
+register_signatures({
+    "sel_server_config_defaults": [ctypes.POINTER(SelServerConfig)],
+    "sel_server_new": [_vp, ctypes.POINTER(SelServerConfig), ctypes.POINTER(_vp)],
+    "sel_server_submit": [_vp, ctypes.POINTER(SelJob), ctypes.POINTER(ctypes.c_uint64)],
+    "sel_server_result_floats": [ctypes.POINTER(SelJob), ctypes.POINTER(_sz)],
+    "sel_server_poll": [_vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int)],
+    "sel_server_wait": [_vp, ctypes.c_uint64, _vp, _sz, ctypes.POINTER(SelJobStats)],
+    "sel_server_stats": [_vp, ctypes.POINTER(SelServerStats)],
+    "sel_server_release": [_vp],
+})
+
+
+def server_config(**kw) -> SelServerConfig:
+    c = SelServerConfig()
+    check(lib().sel_server_config_defaults(ctypes.byref(c)))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def pt_job(scene, cam: SelCamera, settings: SelPtSettings) -> SelJob:
+    j = SelJob()
+    j.scene, j.camera, j.integrator, j.pt = scene.handle, cam, SEL_INTEGRATOR_PT, settings
+    return j
+
+
+def vcm_job(scene, cam: SelCamera, settings: SelVcmSettings) -> SelJob:
+    j = SelJob()
+    j.scene, j.camera, j.integrator, j.vcm = scene.handle, cam, SEL_INTEGRATOR_VCM, settings
+    return j
+
+
+class Server:
+    """Continuous-batching render server (sel_server_*): submit() returns a job id at once, wait() returns
+    the image (path tracer: (2, H, W, 3) layers; VCM: (H, W, 3)) and the job's SelJobStats."""
+
+    def __init__(self, device: Device, config: SelServerConfig | None = None):
+        h = _vp()
+        check(lib().sel_server_new(device.handle, ctypes.byref(config) if config is not None else None,
+                                   ctypes.byref(h)))
+        self.handle = h
+        self._shapes = {}
+
+    def submit(self, job: SelJob) -> int:
+        jid = ctypes.c_uint64()
+        check(lib().sel_server_submit(self.handle, ctypes.byref(job), ctypes.byref(jid)))
+        w, h = job.camera.width, job.camera.height
+        self._shapes[jid.value] = (2, h, w, 3) if job.integrator == SEL_INTEGRATOR_PT else (h, w, 3)
+        return jid.value
+
+    def done(self, job_id: int) -> bool:
+        d = ctypes.c_int()
+        check(lib().sel_server_poll(self.handle, job_id, ctypes.byref(d)))
+        return bool(d.value)
+
+    def wait(self, job_id: int):
+        out = np.zeros(self._shapes.pop(job_id), np.float32)
+        st = SelJobStats()
+        check(lib().sel_server_wait(self.handle, job_id, out.ctypes.data, out.size, ctypes.byref(st)))
+        return out, st
+
+    def stats(self) -> SelServerStats:
+        s = SelServerStats()
+        check(lib().sel_server_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    def release(self) -> None:
+        if self.handle:
+            check(lib().sel_server_release(self.handle))
+            self.handle = None

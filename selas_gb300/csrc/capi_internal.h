@@ -63,6 +63,17 @@ struct SelSceneTy {
 namespace sel {
 struct DeviceBvh;
 struct PtCamera;
+struct PtScene;
+struct VcmConsts;
+struct VcmSettings;
+// render_capi.cu
+int sync_shading(SelSceneTy* sc);              // uploads materials, lights and Ptex when they changed
+PtScene scene_view(const SelSceneTy* sc);       // device pointers of a committed, synced scene
+float vcm_default_radius(const SelSceneTy* sc);
+void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c);
+void vcm_lights(const SelSceneTy* sc, VcmSettings& set);
+int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
+int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings);
 void init_camera(const SelCamera& c, PtCamera& out);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);

@@ -63,6 +63,10 @@ int upload(void*& dst, const T* src, size_t count) {
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "uploading shading data");
 }
 
+}  // namespace
+
+namespace sel {
+
 int sync_shading(SelSceneTy* sc) {
     if (!sc->shading_dirty) return SEL_OK;
     uint32_t max_geom = 0;
@@ -107,6 +111,10 @@ int sync_shading(SelSceneTy* sc) {
     return SEL_OK;
 }
 
+}  // namespace sel
+
+namespace {
+
 int ensure_pt_state(SelSceneTy* sc, uint32_t paths) {
     if (sc->pt_block && sc->pt_capacity == paths) return SEL_OK;
     if (sc->pt_block) cudaFree(sc->pt_block);
@@ -117,6 +125,10 @@ int ensure_pt_state(SelSceneTy* sc, uint32_t paths) {
     sc->pt_capacity = paths;
     return SEL_OK;
 }
+
+}  // namespace
+
+namespace sel {
 
 int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
@@ -130,6 +142,14 @@ int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettin
     if (total >= (uint64_t(1) << 32)) return fail(SEL_ERR_INVALID_ARGUMENT, "width * height * spp must be < 2^32");
     return SEL_OK;
 }
+
+}  // namespace sel
+
+namespace {
+
+}  // namespace
+
+namespace sel {
 
 PtScene scene_view(const SelSceneTy* sc) {
     PtScene ps;
@@ -149,6 +169,43 @@ PtScene scene_view(const SelSceneTy* sc) {
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
     return ps;
 }
+
+// Default initial merge radius: VcmRadiusFactor_ (0.0025) x the bounding-sphere radius of the scene bounds
+// (VCM.cpp:778), the sphere taken about the bounding box.
+float vcm_default_radius(const SelSceneTy* sc) {
+    float d2 = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        const float e = sc->info.bounds_hi[a] - sc->info.bounds_lo[a];
+        d2 += e * e;
+    }
+    const float r = 0.0025f * (0.5f * std::sqrt(d2));
+    return r > 0.0f ? r : 1e-3f;
+}
+
+// Per-pass constants (CalculateIterationConstants, VCMCommon.cpp:91-112, with vcCount = 1): the float
+// expressions of the CPU restatement, so that both compute the same radius and weights.
+void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c) {
+    const float pi = 3.141592653589793f;
+    c.radius = radius0 / std::pow(float(pass + 1), 0.5f * (1.0f - alpha));
+    c.radius2 = c.radius * c.radius;
+    c.n_paths = float(paths);
+    const float eta = pi * c.radius2 * c.n_paths;
+    c.vm_weight = merging ? eta : 0.0f;
+    c.vc_weight = 1.0f / eta;
+    c.vm_norm = 1.0f / eta;
+    c.pass = pass;
+    c.pad = 0;
+}
+
+// Light set 0 of the scene as the VCM light source.
+void vcm_lights(const SelSceneTy* sc, VcmSettings& set) {
+    set.light_first = 0;
+    set.light_count = sc->light_sets.empty() ? 0u : uint32_t(sc->light_sets[0].size());
+}
+
+}  // namespace sel
+
+namespace {
 
 int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& settings, double* d_accum,
                   cudaStream_t stream) {
@@ -183,6 +240,10 @@ SelVcmSettings default_vcm_settings() {
     return s;
 }
 
+}  // namespace
+
+namespace sel {
+
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
@@ -206,6 +267,10 @@ int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings
     return SEL_OK;
 }
 
+}  // namespace sel
+
+namespace {
+
 int ensure_vcm_state(SelSceneTy* sc, uint32_t paths, uint32_t max_len) {
     if (sc->vcm_block && sc->vcm_paths == paths && sc->vcm_len == max_len) return SEL_OK;
     if (sc->vcm_block) cudaFree(sc->vcm_block);
@@ -219,36 +284,12 @@ int ensure_vcm_state(SelSceneTy* sc, uint32_t paths, uint32_t max_len) {
     return SEL_OK;
 }
 
-// Per-pass constants (CalculateIterationConstants, VCMCommon.cpp:91-112, with vcCount = 1): the float
-// expressions of the CPU restatement, so that both compute the same radius and weights.
-void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c) {
-    const float pi = 3.141592653589793f;
-    c.radius = radius0 / std::pow(float(pass + 1), 0.5f * (1.0f - alpha));
-    c.radius2 = c.radius * c.radius;
-    c.n_paths = float(paths);
-    const float eta = pi * c.radius2 * c.n_paths;
-    c.vm_weight = merging ? eta : 0.0f;
-    c.vc_weight = 1.0f / eta;
-    c.vm_norm = 1.0f / eta;
-    c.pass = pass;
-    c.pad = 0;
-}
-
 int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSettings& settings, double* d_accum,
                       cudaStream_t stream) {
     if (int rc = sync_shading(sc)) return rc;
     const uint32_t paths = camera.width * camera.height;
     if (int rc = ensure_vcm_state(sc, paths, settings.maxPathLength)) return rc;
-    float radius0 = settings.radius;
-    if (radius0 == 0.0f) {
-        float d2 = 0.0f;
-        for (int a = 0; a < 3; ++a) {
-            const float e = sc->info.bounds_hi[a] - sc->info.bounds_lo[a];
-            d2 += e * e;
-        }
-        radius0 = 0.0025f * (0.5f * std::sqrt(d2));  // VcmRadiusFactor_ * boundingSphere.w (VCM.cpp:778)
-        if (!(radius0 > 0.0f)) radius0 = 1e-3f;
-    }
+    const float radius0 = settings.radius != 0.0f ? settings.radius : vcm_default_radius(sc);
     VcmCamera cam;
     init_camera(camera, cam.cam);
     const float hlen = std::tan(camera.fovDegrees * (3.141592653589793f / 180.0f) * 0.5f);
@@ -257,11 +298,7 @@ int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSetti
     set.max_len = settings.maxPathLength;
     set.seed = settings.seed;
     set.merging = settings.disableMerging ? 0 : 1;
-    set.light_first = 0;
-    set.light_count = 0;
-    if (!sc->light_sets.empty()) {
-        set.light_count = uint32_t(sc->light_sets[0].size());
-    }
+    vcm_lights(sc, set);
     const PtScene ps = scene_view(sc);
     const VcmState st = vcm_state_carve(sc->vcm_block, paths, settings.maxPathLength, kVcmChunk);
     std::vector<VcmConsts> consts;

@@ -358,6 +358,7 @@ template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_extend(VcmParams P, int cur) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     const uint32_t* queue = P.st.queue[cur];
     uint32_t status = 0;
     for (;;) {
@@ -387,6 +388,7 @@ template <int K>
 __global__ void __launch_bounds__(kBlock, 8) k_shadow(VcmParams P) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
     const uint32_t n = P.st.counters[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     uint32_t status = 0;
     for (;;) {
         uint32_t base = 0;
@@ -1051,6 +1053,7 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.sc = reinterpret_cast<float4*>(take(16 * shadow));
     st.shadow_capacity = uint32_t(shadow);
     st.counters = reinterpret_cast<uint32_t*>(take(4 * 16));
+    st.rays = reinterpret_cast<unsigned long long*>(take(8));
     st.cverts = reinterpret_cast<float4*>(take(96ull * paths));
     st.pairs = reinterpret_cast<uint2*>(take(8 * nv));
     st.spos = reinterpret_cast<float4*>(take(16 * nv));
@@ -1095,9 +1098,17 @@ size_t vcm_state_block_bytes(uint32_t paths, uint32_t max_len, uint32_t passes) 
     return total;
 }
 
-cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
-                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
-                       GraphCache* graphs) {
+cudaError_t vcm_upload_constants(const VcmState& st, const VcmConsts* host_consts, uint32_t passes,
+                                 cudaStream_t stream) {
+    if (passes > st.consts_capacity) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(st.consts, host_consts, sizeof(VcmConsts) * passes, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(st.iter, 0, sizeof(uint32_t), stream);
+    return e;
+}
+
+cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, uint32_t passes,
+                           const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
+                           GraphCache* graphs) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1132,9 +1143,6 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
     P.lights = sc.lights + set.light_first;
     P.light_count = set.light_count;
 
-    cudaError_t e = cudaMemcpyAsync(st.consts, host_consts, sizeof(VcmConsts) * passes, cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(st.iter, 0, sizeof(uint32_t), stream);
-    if (e != cudaSuccess) return e;
     const uint32_t N = st.paths;
     const size_t nv = size_t(N) * st.slots_per_path;
     const uint32_t ntiles = uint32_t((nv + kSortTile - 1) / kSortTile);
@@ -1203,6 +1211,14 @@ cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSetting
     key.sms = sms;
     key.radix_passes = radix_passes;
     return replay(graphs, &key, sizeof(key), stream, passes, enqueue);
+}
+
+cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
+                       uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
+                       GraphCache* graphs) {
+    cudaError_t e = vcm_upload_constants(st, host_consts, passes, stream);
+    if (e != cudaSuccess) return e;
+    return vcm_run_passes(sc, cam, set, passes, st, d_accum, d_err, stream, graphs);
 }
 
 }  // namespace sel

@@ -51,6 +51,7 @@ struct VcmState {
     uint32_t shadow_capacity;
     uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor,
                           // [5] camera-vertex records, [6] connection pairs
+    unsigned long long* rays;  // rays traced (closest + any hit), a running total
     float4* cverts;       // camera-vertex records of the current bounce, 6 x float4 each
     uint2* pairs;         // (camera-vertex record, light-vertex index) connection pairs of the current bounce
     float4* spos;         // stored-vertex positions in cell order, slot bits in w
@@ -79,7 +80,16 @@ struct VcmCamera {
 
 // Runs passes [first, first + passes).  Accumulates into d_accum ([height][width][3] doubles) the sum of
 // the passes' images.
-// With `graphs`, one pass is captured as a CUDA graph (once per argument set) and replayed per pass.
+// Copies the constants of `passes` passes to the device table and restarts its row counter.
+cudaError_t vcm_upload_constants(const VcmState& st, const VcmConsts* host_consts, uint32_t passes,
+                                 cudaStream_t stream);
+// Launches `passes` passes continuing from the current row of the constants table.  With `graphs`, one pass
+// is captured as a CUDA graph (once per argument set) and replayed per pass.
+cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, uint32_t passes,
+                           const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
+                           GraphCache* graphs);
+// Upload + run.
+
 cudaError_t vcm_render(const PtScene& sc, const VcmCamera& cam, const VcmSettings& set, const VcmConsts* host_consts,
                        uint32_t passes, const VcmState& st, double* d_accum, uint32_t* d_err, cudaStream_t stream,
                        GraphCache* graphs);

@@ -67,3 +67,16 @@ def test_vcm_settings_defaults_and_layout(lib):
     assert s.radiusAlpha == pytest.approx(0.75) and s.radius == 0.0
     assert lib.sel_vcm_settings_defaults(None) == sel.SEL_ERR_INVALID_ARGUMENT
     assert lib.sel_vcm_generate_image(None, None, None, None) == sel.SEL_ERR_INVALID_ARGUMENT
+
+
+def test_server_records_and_defaults(lib):
+    import selas_gb300 as sel
+    assert ctypes.sizeof(sel.SelJob) == 120 and ctypes.sizeof(sel.SelServerConfig) == 32
+    c = sel.server_config()
+    assert (c.max_jobs, c.paths_in_flight, c.max_bounces) == (16, 1 << 22, 8)
+    assert c.hbm_reserve_bytes == 2 << 30
+    assert lib.sel_server_new(None, None, None) == sel.SEL_ERR_INVALID_ARGUMENT
+    j = sel.SelJob()
+    j.camera.width, j.camera.height, j.integrator = 10, 6, sel.SEL_INTEGRATOR_PT
+    n = ctypes.c_size_t()
+    assert lib.sel_server_result_floats(ctypes.byref(j), ctypes.byref(n)) == 0 and n.value == 360
