@@ -50,6 +50,8 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the path-tracer and VCM measurements")
     p.add_argument("--vcm-passes", type=int, default=256, help="VCM iterations timed on the quantised BVH")
+    p.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving stream (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream, jobs/s")
     return p.parse_args()
 
 
@@ -191,7 +193,93 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def render_metrics(sel, scenes, dev, stream, args):
+def serve_metrics(sel, scenes, dev, room, args):
+    """Render-serving stream: jobs with Poisson arrivals, each with a scene drawn from {Cornell, the
+    ray-query icospheres, the VCM room} (resident in HBM), a resolution from {256x256, 512x512, 1024x768,
+    1920x1080}, spp (path tracer) or passes (VCM) from {16, 64, 256}, an integrator from {path tracer, VCM}
+    and a seeded camera yaw.  Served: submitted at their arrival times to the render server (quantised BVH,
+    shared graph-replayed batches, overlapping VCM jobs).  Serial plain path: the same jobs one after
+    another through sel_pt_generate_image / sel_vcm_generate_image on the binary FP32 BVH with kernel-by-
+    kernel launches; its latencies replay the same arrivals through a FIFO with the measured service times."""
+    rng = np.random.default_rng(0x5E1A5005)
+    defs = {"cornell": scenes.cornell_box(), "icospheres": scenes.icosphere_field(), "room": room}
+    names = list(defs)
+    res = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
+    jobs, t = [], 0.0
+    for _ in range(args.serve_jobs):
+        t += rng.exponential(1.0 / args.serve_rate)
+        jobs.append(dict(t=t, scene=names[rng.integers(3)], res=res[rng.integers(4)], spp=int([16, 64, 256][rng.integers(3)]),
+                         integrator=int(rng.integers(2)), yaw=float(rng.uniform(-0.35, 0.35)),
+                         seed=int(rng.integers(1 << 31))))
+    wide = {k: v.build(sel, dev) for k, v in defs.items()}
+
+    def make(j, built):
+        rs = defs[j["scene"]]
+        c = scenes.orbit_camera(rs.camera, j["yaw"])
+        cam = sel.camera(c["position"], c["look_at"], c["up"], c["fov_degrees"], *j["res"])
+        if j["integrator"] == 0:
+            return sel.pt_job(built[j["scene"]], cam, sel.pt_settings(j["spp"], 8, j["seed"])), cam
+        return sel.vcm_job(built[j["scene"]], cam, sel.vcm_settings(j["spp"], 10, j["seed"])), cam
+
+    paths = sum(j["res"][0] * j["res"][1] * j["spp"] * (1 if j["integrator"] == 0 else 2) for j in jobs)
+    # served
+    srv = sel.Server(dev)
+    t0 = time.perf_counter()
+    ids = []
+    for j in jobs:
+        delay = t0 + j["t"] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(make(j, wide)[0]))
+    served = [srv.wait(i) for i in ids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.release()
+    lat = np.array([s.latency_ms for _, s in served])
+    for sc in wide.values():
+        sc.release()
+    # serial plain path: binary FP32 BVH, no graph replay, one job at a time
+    plain = {k: v.build(sel, dev, bvh_kind=sel.SEL_BVH_BINARY_FP32) for k, v in defs.items()}
+    dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 0)
+    service = []
+    for j in jobs:
+        job, cam = make(j, plain)
+        t1 = time.perf_counter()
+        if j["integrator"] == 0:
+            plain[j["scene"]].pt_generate_image(cam, job.pt)
+        else:
+            plain[j["scene"]].vcm_generate_image(cam, job.vcm)
+        service.append(time.perf_counter() - t1)
+    dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
+    for sc in plain.values():
+        sc.release()
+    finish, lat_serial = 0.0, []
+    for j, sv in zip(jobs, service):
+        finish = max(finish, j["t"]) + sv
+        lat_serial.append(1e3 * (finish - j["t"]))
+    lat_serial = np.array(lat_serial)
+    served_wall = wall
+    return {
+        "workload": f"{len(jobs)} jobs, Poisson arrivals at {args.serve_rate} jobs/s; scene from {{Cornell, ray-query "
+                    f"icospheres, VCM room}}, resolution from {{256x256, 512x512, 1024x768, 1920x1080}}, spp/passes from "
+                    f"{{16, 64, 256}}, integrator from {{path tracer, VCM}}, seeded camera yaw",
+        "jobs_pt": sum(1 for j in jobs if j["integrator"] == 0), "jobs_vcm": sum(1 for j in jobs if j["integrator"] == 1),
+        "served": {"p50_latency_ms": round(float(np.percentile(lat, 50)), 1),
+                   "p99_latency_ms": round(float(np.percentile(lat, 99)), 1),
+                   "makespan_s": round(served_wall, 3), "jobs_per_s": round(len(jobs) / served_wall, 3),
+                   "paths_per_s": round(paths / served_wall, 1), "mrays_per_s": round(st.rays / served_wall / 1e6, 1),
+                   "rays": int(st.rays), "peak_jobs": int(st.peak_jobs), "peak_device_gb": round(st.peak_bytes / 1e9, 2)},
+        "serial_plain": {"p50_latency_ms": round(float(np.percentile(lat_serial, 50)), 1),
+                         "p99_latency_ms": round(float(np.percentile(lat_serial, 99)), 1),
+                         "makespan_s": round(finish, 3), "busy_s": round(sum(service), 3),
+                         "jobs_per_s": round(len(jobs) / finish, 3), "paths_per_s": round(paths / finish, 1),
+                         "mrays_per_s": round(st.rays / finish / 1e6, 1)},
+        "throughput_ratio_served_vs_serial_plain": round(finish / served_wall, 3),
+        "rays_note": "both forms trace the same paths (identical hits, same streams), so they trace the same rays",
+    }
+
+
+def render_metrics(sel, scenes, dev, stream, args, room=None):
     """Integrator throughput on both BVH layouts (they return identical hits, so both trace the same paths
     and reach the same image rMSE): the Cornell path tracer (512 x 512, 64 spp, depth 8) and VCM on the room
     scene (1280 x 720, length 10, r0 = 0.003 x the scene diagonal, alpha 0.75)."""
@@ -228,7 +316,7 @@ def render_metrics(sel, scenes, dev, stream, args):
     out["pt"] = {"workload": "Cornell box, 512x512, 64 spp, max depth 8, one jittered PCG32 sample per pass", **pt}
 
     t0 = time.time()
-    room = scenes.vcm_room()
+    room = room if room is not None else scenes.vcm_room()
     gen_s = time.time() - t0
     lo, hi = room.geometry.bounds()
     r0 = 0.003 * float(np.linalg.norm(hi - lo))
@@ -407,7 +495,13 @@ def run_ours(args):
         for k in list(work):  # release the ray sets first
             del work[k], pristine[k]
         torch.cuda.empty_cache()
-        render = render_metrics(sel, scenes, dev, stream, args)
+        t_gen = time.time()
+        room = scenes.vcm_room()
+        room_gen_s = time.time() - t_gen
+        render = render_metrics(sel, scenes, dev, stream, args, room)
+        render["vcm"]["scene_generation_s"] = round(room_gen_s, 1)
+        if args.serve_jobs > 0:
+            render["serving"] = serve_metrics(sel, scenes, dev, room, args)
 
     per_set = {k: round(counts[k] / (per_kernel[k] * 1e-3) / 1e6, 1) for k in per_kernel}
     per_set_b = {k: round(counts[k] / (per_kernel_b[k] * 1e-3) / 1e6, 1) for k in per_kernel_b}

@@ -10,6 +10,8 @@
 //           the batch (water-filling of the capacity over the paths each job has left); the batch is a
 //           replayed CUDA graph, the job table and quotas go up from pinned buffers (two rounds in flight);
 //   VCM     one pass of every admitted VCM job on the job's own stream (at most two passes queued per job);
+//           streams carry CUDA priorities, highest for the shared path-tracer batches and then by a VCM job's
+//           work (pixels x passes, smaller first), so short jobs are not held behind long passes;
 //   retire  jobs whose last work finished: resolve, copy the image to host memory, free the device memory.
 // A path's random stream depends only on its job and index, so a job renders the same image alone and in
 // any mix (up to the order of FP64 additions).
@@ -103,6 +105,7 @@ struct SelServerTy {
     unsigned long long* h_rays = nullptr;  // pinned scratch for counter reads
     uint64_t vcm_rays = 0;
     uint64_t held_bytes = 0;
+    int prio_least = 0, prio_greatest = 0;  // cudaDeviceGetStreamPriorityRange
     SelServerStats stats{};
 };
 
@@ -143,7 +146,14 @@ bool admit_one(SelServerTy* S, Job* j) {
     if (!budget_allows(S, j->bytes)) return false;
     cudaStream_t s = S->pt_stream;
     if (d.integrator == SEL_INTEGRATOR_VCM) {
-        if (cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+        // priority by work: one level per factor 16 of pixels x passes above 2^20, the largest jobs lowest
+        const double work = double(d.camera.width) * d.camera.height * d.vcm.passes;
+        int level = 0;
+        for (double w = work; w > double(1 << 20) && level < 8; w /= 16.0) ++level;
+        int prio = S->prio_greatest + 1 + level;  // numerically larger = lower priority
+        if (prio > S->prio_least) prio = S->prio_least;
+        if (prio < S->prio_greatest) prio = S->prio_greatest;
+        if (cudaStreamCreateWithPriority(&j->stream, cudaStreamNonBlocking, prio) != cudaSuccess) return false;
         s = j->stream;
     }
     j->alloc_stream = s;
@@ -280,11 +290,22 @@ bool pt_round(SelServerTy* S) {
     return true;
 }
 
-// One pass of every admitted VCM job that has passes left and fewer than kRing passes queued.
+// One pass of the admitted VCM jobs with the least work left (pixels x passes, shortest first) whose pixels
+// together stay within the wavefront capacity, each only while it has fewer than kRing passes queued.  The
+// job with the least work always advances; the others wait for the GPU the shorter jobs leave.
 bool vcm_round(SelServerTy* S, const std::vector<Job*>& act) {
+    std::vector<std::pair<double, Job*>> order;
+    for (Job* j : act)
+        if (j->desc.integrator == SEL_INTEGRATOR_VCM && j->passes_issued < j->passes)
+            order.push_back({double(j->desc.camera.width) * j->desc.camera.height * (j->passes - j->passes_issued), j});
+    std::sort(order.begin(), order.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
     bool queued = false;
-    for (Job* j : act) {
-        if (j->desc.integrator != SEL_INTEGRATOR_VCM || j->passes_issued >= j->passes) continue;
+    uint64_t pixels = 0;
+    for (size_t r = 0; r < order.size(); ++r) {
+        Job* j = order[r].second;
+        const uint64_t px = uint64_t(j->desc.camera.width) * j->desc.camera.height;
+        if (r > 0 && pixels + px > S->cfg.paths_in_flight) break;
+        pixels += px;
         const int par = int(j->passes_issued % kRing);
         if (j->passes_issued >= uint32_t(kRing) && cudaEventQuery(j->pass_ev[par]) == cudaErrorNotReady) continue;
         cudaError_t e = vcm_run_passes(j->scene, j->vcam, j->vset, 1, j->vst, j->accum, S->dev->d_err, j->stream,
@@ -396,7 +417,8 @@ int sel_server_new(SelDevice device, const SelServerConfig* config, SelServer* o
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(server path state)");
     S->pst = pt_state_carve(S->pt_block, cfg.paths_in_flight);
     e = cudaMemset(S->pst.rays, 0, sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->pt_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&S->prio_least, &S->prio_greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&S->pt_stream, cudaStreamNonBlocking, S->prio_greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->retire_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_jobs, sizeof(PtJob) * kMaxPtJobs * kRing);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_ctl, sizeof(PtControl) * kRing);

@@ -129,6 +129,17 @@ struct WideState {
     QueryHit hit;
 };
 
+// A ray that no triangle can hit under the watertight test: a non-finite origin or direction component
+// (NaN arithmetic rejects every triangle) or a zero direction (no dominant axis).  Traversing it would be
+// worse than useless: with NaN slab distances fminf/fmaxf keep the interval bounds and every box is
+// entered, so one such ray walks the whole tree.  The traversals return "no hit" for it at once, which is
+// what the full walk returns.
+__device__ __forceinline__ bool ray_untraceable(const QueryRay& r) {
+    const bool finite = isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz) && isfinite(r.dx) && isfinite(r.dy) &&
+                        isfinite(r.dz);
+    return !finite || (r.dx == 0.0f && r.dy == 0.0f && r.dz == 0.0f);
+}
+
 __device__ __forceinline__ void wide_init(WideState& s, const QueryRay& r) {
     s.ox = r.ox; s.oy = r.oy; s.oz = r.oz;
     s.dx = r.dx; s.dy = r.dy; s.dz = r.dz;
@@ -237,6 +248,10 @@ template <bool kAnyHit>
 __device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                            const QueryRay& r, QueryHit& hit, uint2* stack, int stride,
                                            uint32_t& status) {
+    if (ray_untraceable(r)) {
+        hit.tri = 0xffffffffu;
+        return false;
+    }
     WideState s;
     wide_init(s, r);
     while (!wide_step<kAnyHit>(s, nodes, tris, stack, stride, status)) {}
@@ -252,6 +267,10 @@ template <bool kAnyHit>
 __device__ __forceinline__ bool trace_binary(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                              const QueryRay& r, QueryHit& hit, int* stack, int stride,
                                              uint32_t& status) {
+    if (ray_untraceable(r)) {
+        hit.tri = 0xffffffffu;
+        return false;
+    }
     const Watertight wt = watertight_setup(r.dx, r.dy, r.dz);
     const float ix = safe_rcp(r.dx), iy = safe_rcp(r.dy), iz = safe_rcp(r.dz);
     const float oix = __fmul_rn(r.ox, ix), oiy = __fmul_rn(r.oy, iy), oiz = __fmul_rn(r.oz, iz);

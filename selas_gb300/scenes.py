@@ -460,3 +460,24 @@ def vcm_room(icospheres: int = 24, level: int = 6, glass: int = 40, glass_level:
                  radiance=(40.0, 38.0, 34.0))
     cam = dict(position=(0.0, 5.0, -9.5), look_at=(0.0, 3.0, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=75.0)
     return RenderScene(g, mats, [(0, light)], (0.0, 0.0, 0.0), cam, ptex)
+
+
+def icosphere_field(level: int = 6, seed: int = 0x5E1A5001) -> RenderScene:
+    """The ray-query geometry (64 displaced icospheres over a 200 x 200 ground plane) as a render scene:
+    grey Disney surfaces (roughness 0.5) under one 80 x 80 quad light, the ray-query camera."""
+    g = displaced_icospheres(level=level, seed=seed)
+    mats = {gid: dict(shader=1, lightSetIndex=0, roughness=0.5, ior=1.5, baseColor=(0.6, 0.6, 0.6))
+            for gid, _, _ in g.meshes}
+    light = dict(position=(0.0, 150.0, 0.0), direction=(0.0, -1.0, 0.0), x=(80.0, 0.0, 0.0), z=(0.0, 0.0, 80.0),
+                 radiance=(6.0, 6.0, 6.0))
+    cam = dict(position=(0.0, 70.0, -170.0), look_at=(0.0, 40.0, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=60.0)
+    return RenderScene(g, mats, [(0, light)], (0.05, 0.05, 0.05), cam, {})
+
+
+def orbit_camera(camera: dict, yaw: float) -> dict:
+    """The camera turned by `yaw` radians about the vertical axis through its look-at point."""
+    p, c = np.asarray(camera["position"], np.float64), np.asarray(camera["look_at"], np.float64)
+    d = p - c
+    cs, sn = np.cos(yaw), np.sin(yaw)
+    q = c + np.array([cs * d[0] + sn * d[2], d[1], -sn * d[0] + cs * d[2]])
+    return {**camera, "position": tuple(float(x) for x in q)}

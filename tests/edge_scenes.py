@@ -68,3 +68,13 @@ def segment_rays():
     r = make_rays(org, d)
     r["tnear"], r["tfar"] = tn, tf
     return r
+
+
+def untraceable_rays():
+    """Rays no triangle can hit under the watertight test: NaN or infinite origin or direction components,
+    a zero direction; each aimed (where finite) at the scene so that a broken guard would show up as hits."""
+    nan, inf = np.float32(np.nan), np.float32(np.inf)
+    org = np.array([[nan, 40, -170], [0, 40, -170], [inf, 40, -170], [0, 40, -170], [0, -inf, 0], [0, 40, -170],
+                    [0, 40, -170]], np.float32)
+    d = np.array([[0, 0, 1], [0, nan, 1], [0, 0, 1], [0, 0, inf], [0, 1, 0], [0, 0, 0], [-inf, 0, 1]], np.float32)
+    return org, d

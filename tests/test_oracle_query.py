@@ -4,7 +4,7 @@ import numpy as np
 
 import oracle
 from conftest import assert_hits_equal
-from edge_scenes import grid_rays, grid_scene, segment_rayhits, segment_rays
+from edge_scenes import grid_rays, grid_scene, segment_rayhits, segment_rays, untraceable_rays
 from selas_gb300 import INVALID_ID, make_rayhits, make_rays, scenes
 
 
@@ -82,3 +82,17 @@ def test_closed_mesh_never_leaks():
     a = make_rayhits(org, d)
     oracle.OracleBvh(s.soup()).intersect(a)
     assert (a["geomID"] == 0).all()
+
+
+def test_untraceable_rays_never_hit():
+    """The brute-force definition rejects rays with non-finite components or a zero direction (the GPU
+    traversals return the same miss without walking the tree)."""
+    data = scenes.displaced_icospheres(count=5, level=3, seed=11)
+    org, d = untraceable_rays()
+    rh = make_rayhits(org, d)
+    oracle.intersect_bruteforce(data.soup(), rh)
+    assert (rh["geomID"] == INVALID_ID).all()
+    r = make_rays(org, d)
+    before = r["tfar"].copy()
+    oracle.occluded_bruteforce(data.soup(), r)
+    assert np.array_equal(r["tfar"], before)  # never set to -inf (the any-hit mark)

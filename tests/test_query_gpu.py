@@ -9,7 +9,7 @@ import pytest
 import oracle
 import selas_gb300 as sel
 from conftest import HIT_FIELDS, assert_hits_equal
-from edge_scenes import grid_rays, grid_scene, segment_rayhits, segment_rays
+from edge_scenes import grid_rays, grid_scene, segment_rayhits, segment_rays, untraceable_rays
 from selas_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
@@ -153,3 +153,21 @@ def test_full_size_workload(device, full_workload):
         assert_hits_equal(a[pick], want)
     wide.release()
     binary.release()
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_untraceable_rays_miss_like_the_bruteforce_definition(device, kind):
+    data = scenes.displaced_icospheres(count=5, level=3, seed=11)
+    soup = data.soup()
+    sc = _scene(device, data, kind)
+    org, d = untraceable_rays()
+    got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+    sc.intersect1M(got)
+    oracle.intersect_bruteforce(soup, want)
+    assert (want["geomID"] == sel.INVALID_ID).all()
+    assert_hits_equal(got, want)
+    rg, rw = sel.make_rays(org, d), sel.make_rays(org, d)
+    sc.occluded1M(rg)
+    oracle.occluded_bruteforce(soup, rw)
+    assert_hits_equal(rg, rw, fields=("tfar",))
+    sc.release()
