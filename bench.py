@@ -213,6 +213,11 @@ def serve_metrics(sel, scenes, dev, room, args):
                          seed=int(rng.integers(1 << 31))))
     wide = {k: v.build(sel, dev) for k, v in defs.items()}
 
+    def warm(built):  # materials, lights and texels go to HBM on first use: keep that out of the timings
+        for k, sc in built.items():
+            sc.pt_generate_image(defs[k].sel_camera(sel, 8, 8), sel.pt_settings(1, 1))
+    warm(wide)
+
     def make(j, built):
         rs = defs[j["scene"]]
         c = scenes.orbit_camera(rs.camera, j["yaw"])
@@ -240,6 +245,7 @@ def serve_metrics(sel, scenes, dev, room, args):
         sc.release()
     # serial plain path: binary FP32 BVH, no graph replay, one job at a time
     plain = {k: v.build(sel, dev, bvh_kind=sel.SEL_BVH_BINARY_FP32) for k, v in defs.items()}
+    warm(plain)
     dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 0)
     service = []
     for j in jobs:
