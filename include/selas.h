@@ -113,6 +113,13 @@ int sel_device_set_option(SelDevice device, int option, int value);
 /* ------------------------------------------------------------------------------------------------ */
 int sel_scene_new(SelDevice device, SelScene* out_scene);
 int sel_scene_set_bvh_kind(SelScene scene, int bvh_kind);
+
+/* Where sel_scene_commit builds the BVH (no reference counterpart: Embree builds on the host with TBB).
+ * SEL_BUILD_DEVICE (the default) builds the 8-wide layout with GPU kernels (binned SAH, collapse,
+ * quantisation); the binary layout is always built on the host.  Results of queries do not depend on the
+ * builder. */
+enum { SEL_BUILD_HOST = 0, SEL_BUILD_DEVICE = 1 };
+int sel_scene_set_build_mode(SelScene scene, int build_mode);
 /* vertices: vertex_count records of 3 floats (x,y,z) every vertex_stride_bytes bytes (>= 12);
  * indices: triangle_count x 3 unsigned ints.  The data is copied; the caller may free it after the
  * call.  geomID is reported in SelHit.geomID; primID is the triangle's index within this mesh. */

@@ -22,6 +22,7 @@ SEL_ERR_INVALID_OPERATION = 4
 SEL_ERR_DEVICE_LIMIT = 5
 
 SEL_OPTION_GRAPH_REPLAY = 1
+SEL_BUILD_HOST, SEL_BUILD_DEVICE = 0, 1
 SEL_BVH_WIDE8_Q8 = 0
 SEL_BVH_BINARY_FP32 = 1
 
@@ -147,9 +148,11 @@ class Device:
 class Scene:
     """Triangle scene behind the rtcIntersect1 / rtcOccluded1 contract."""
 
-    def __init__(self, device: Device, bvh_kind: int = SEL_BVH_WIDE8_Q8):
+    def __init__(self, device: Device, bvh_kind: int = SEL_BVH_WIDE8_Q8, build_mode: int | None = None):
         h = _vp()
         check(lib().sel_scene_new(device.handle, ctypes.byref(h)))
+        if build_mode is not None:
+            check(lib().sel_scene_set_build_mode(h, build_mode))
         self.handle = h
         self.device = device
         check(lib().sel_scene_set_bvh_kind(h, bvh_kind))
@@ -262,6 +265,7 @@ register_signatures({
     "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
     "sel_vcm_settings_defaults": [ctypes.POINTER(SelVcmSettings)],
     "sel_device_set_option": [_vp, ctypes.c_int, ctypes.c_int],
+    "sel_scene_set_build_mode": [_vp, ctypes.c_int],
     "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
     "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
 })

@@ -172,10 +172,45 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
     return SEL_OK;
 }
 
+int sel_scene_set_build_mode(SelScene scene, int build_mode) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (build_mode != SEL_BUILD_HOST && build_mode != SEL_BUILD_DEVICE)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "unknown build mode");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    scene->build_mode = build_mode;
+    return SEL_OK;
+}
+
 int sel_scene_commit(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     std::lock_guard<std::mutex> lock(scene->mu);
     if (int rc = set_device(scene->dev)) return rc;
+    if (scene->kind == SEL_BVH_WIDE8_Q8 && scene->build_mode == SEL_BUILD_DEVICE) {
+        DeviceBuild db;
+        std::string derr;
+        try {
+            derr = build_wide_device(scene->meshes, db);
+        } catch (const std::bad_alloc&) {
+            return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed during BVH build");
+        }
+        if (!derr.empty()) return fail(SEL_ERR_INVALID_OPERATION, derr);
+        if (scene->d_nodes) cudaFree(scene->d_nodes);
+        if (scene->d_tris) cudaFree(scene->d_tris);
+        scene->d_nodes = db.d_nodes;
+        scene->d_tris = db.d_tris;
+        SelSceneInfo& info = scene->info;
+        std::memset(&info, 0, sizeof(info));
+        info.triangle_count = db.tri_count;
+        info.node_count = db.node_count;
+        info.device_bytes = uint64_t(db.node_count) * sizeof(WideNode) + uint64_t(db.tri_count) * sizeof(TriRecord);
+        info.bvh_kind = SEL_BVH_WIDE8_Q8;
+        info.max_depth = db.max_depth;
+        info.build_ms = db.build_ms;
+        info.upload_ms = 0.0;
+        for (int a = 0; a < 3; ++a) { info.bounds_lo[a] = db.lo[a]; info.bounds_hi[a] = db.hi[a]; }
+        scene->committed = true;
+        return SEL_OK;
+    }
     BuiltBvh built;
     auto t0 = std::chrono::steady_clock::now();
     std::string err;

@@ -22,6 +22,7 @@ struct SelDeviceTy {
 struct SelSceneTy {
     SelDeviceTy* dev = nullptr;
     int kind = SEL_BVH_WIDE8_Q8;
+    int build_mode = SEL_BUILD_DEVICE;  // 8-wide layout built by GPU kernels (binary: always host)
     std::vector<sel::MeshInput> meshes;
     bool committed = false;
     void* d_nodes = nullptr;

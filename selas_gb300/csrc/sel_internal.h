@@ -76,6 +76,17 @@ struct BuiltBvh {
 // Returns an empty string on success or an error message.
 std::string build_bvh(const std::vector<MeshInput>& meshes, int kind, BuiltBvh& out);
 
+// The 8-wide quantised BVH built on the current CUDA device (bvh_device.cu): node and triangle arrays in
+// device memory, handed to the caller (cudaFree).
+struct DeviceBuild {
+    void* d_nodes = nullptr;  // WideNode[node_count]
+    void* d_tris = nullptr;   // TriRecord[tri_count], leaf order
+    uint32_t node_count = 0, tri_count = 0, max_depth = 0, binary_depth = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    double build_ms = 0.0;    // upload of the triangles + all build kernels
+};
+std::string build_wide_device(const std::vector<MeshInput>& meshes, DeviceBuild& out);
+
 // Traversal stack capacities (entries per thread); the builder rejects trees deeper than these.
 constexpr int kWideStack = 24;
 constexpr int kBinaryStack = 64;

@@ -213,9 +213,9 @@ class RenderScene:
             return np.zeros((0, 8), np.int32), np.zeros(3, np.uint16)
         return np.ascontiguousarray(np.concatenate(rows)), np.ascontiguousarray(np.concatenate(texels))
 
-    def build(self, sel_module, device, bvh_kind=0):
+    def build(self, sel_module, device, bvh_kind=0, build_mode=None):
         """Creates and commits a selas_gb300 Scene with this content."""
-        sc = sel_module.Scene(device, bvh_kind)
+        sc = sel_module.Scene(device, bvh_kind, build_mode)
         self.geometry.attach_to(sc)
         for gid, m in self.materials.items():
             sc.set_material(gid, sel_module.material(**m))

@@ -171,3 +171,64 @@ def test_untraceable_rays_miss_like_the_bruteforce_definition(device, kind):
     oracle.occluded_bruteforce(soup, rw)
     assert_hits_equal(rg, rw, fields=("tfar",))
     sc.release()
+
+
+@pytest.mark.parametrize("n_spheres,level", [(1, 0), (3, 2), (8, 4)])
+def test_device_built_bvh_matches_bruteforce(device, n_spheres, level):
+    """The 8-wide BVH built by the GPU kernels (SEL_BUILD_DEVICE) answers every query as the definition does,
+    from a 20-triangle scene (one warp builds the whole tree) to 80 k triangles (large-task levels first)."""
+    data = scenes.displaced_icospheres(count=n_spheres, level=level, seed=31)
+    soup = data.soup()
+    sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8, sel.SEL_BUILD_DEVICE)
+    data.attach_to(sc)
+    sc.commit()
+    info = sc.info()
+    assert info.triangle_count == soup[0].shape[0] and info.node_count >= 1
+    cam = scenes.camera_basis([0.0, 70.0, -170.0], [0.0, 40.0, 0.0], [0.0, 1.0, 0.0], 60.0, 64, 64)
+    for org, d in (scenes.primary_rays(cam), scenes.surface_rays(data, 6000, seed=6)):
+        got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+        sc.intersect1M(got)
+        oracle.intersect_bruteforce(soup, want)
+        assert_hits_equal(got, want)
+        rg, rw = sel.make_rays(org, d), sel.make_rays(org, d)
+        sc.occluded1M(rg)
+        oracle.occluded_bruteforce(soup, rw)
+        assert_hits_equal(rg, rw, fields=("tfar",))
+    sc.release()
+
+
+def test_device_built_bvh_on_the_edge_grid(device):
+    data = grid_scene()
+    soup = data.soup()
+    sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8, sel.SEL_BUILD_DEVICE)
+    data.attach_to(sc)
+    sc.commit()
+    org, d, _ = grid_rays()
+    got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+    sc.intersect1M(got)
+    oracle.intersect_bruteforce(soup, want)
+    assert_hits_equal(got, want)
+    sc.release()
+
+
+def test_device_built_bvh_full_size(device, full_workload):
+    """5,242,882 triangles: device build against the host build on a million rays of each set (both are
+    checked against the definition elsewhere; here they must agree bit for bit)."""
+    data, coherent, incoherent = full_workload
+    built = {}
+    for mode in (sel.SEL_BUILD_HOST, sel.SEL_BUILD_DEVICE):
+        sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8, mode)
+        data.attach_to(sc)
+        sc.commit()
+        built[mode] = sc
+    info_h, info_d = built[0].info(), built[1].info()
+    print(f"host build {info_h.build_ms:.1f} ms, device build {info_d.build_ms:.1f} ms; nodes {info_h.node_count} / "
+          f"{info_d.node_count}; depth {info_h.max_depth} / {info_d.max_depth}")
+    for org, d in (coherent, incoherent):
+        n = min(org.shape[0], 1 << 20)
+        a, b = sel.make_rayhits(org[:n], d[:n]), sel.make_rayhits(org[:n], d[:n])
+        built[0].intersect1M(a)
+        built[1].intersect1M(b)
+        assert_hits_equal(b, a)
+    for sc in built.values():
+        sc.release()
