@@ -6,9 +6,10 @@
 //   admit   pending jobs in arrival order while a job slot and the device-byte budget allow; a job's
 //           accumulator (and VCM state) is allocated with the stream-ordered allocator, so admission and
 //           retirement never synchronise the device;
-//   PT      one batch of the shared path-tracer wavefront: every admitted path-tracer job gets a share of
-//           the batch (water-filling of the capacity over the paths each job has left); the batch is a
-//           replayed CUDA graph, the job table and quotas go up from pinned buffers (two rounds in flight);
+//   PT      one batch of the shared path-tracer wavefront, filled shortest-remaining-work first and one scene
+//           at a time (the job with the fewest paths left, the other jobs on its scene, then the rest); the
+//           batch is a replayed CUDA graph, the job table and quotas go up from pinned buffers (two rounds in
+//           flight);
 //   VCM     one pass of every admitted VCM job on the job's own stream (at most two passes queued per job);
 //           streams carry CUDA priorities, highest for the shared path-tracer batches and then by a VCM job's
 //           work (pixels x passes, smaller first), so short jobs are not held behind long passes;
@@ -243,7 +244,9 @@ bool pt_round(SelServerTy* S) {
     PtControl& c = S->h_ctl[par];
     std::memset(&c, 0, sizeof(c));
     PtJob* table = S->h_jobs + size_t(par) * kMaxPtJobs;
-    // water-filling: jobs with few paths left take what they need, the rest share the remainder evenly
+    // shortest remaining work first, one scene at a time: the batch takes the paths of the job with the
+    // fewest left, then of the other jobs on the same scene, and only then fills up from other scenes,
+    // so a batch's traversal mostly stays in one scene's BVH and textures
     std::vector<std::pair<uint64_t, int>> left;
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
@@ -251,12 +254,15 @@ bool pt_round(SelServerTy* S) {
     }
     std::sort(left.begin(), left.end());
     uint64_t cap = S->pst.capacity;
-    for (size_t i = 0; i < left.size(); ++i) {
-        const uint64_t share = cap / (left.size() - i);
-        const uint64_t q = std::min(left[i].first, share);
-        c.quota[left[i].second] = uint32_t(q);
-        cap -= q;
-    }
+    const SelSceneTy* lead = S->slots[left.front().second]->desc.scene;
+    for (int pass = 0; pass < 2 && cap > 0; ++pass)
+        for (const auto& lk : left) {
+            const bool same = S->slots[lk.second]->desc.scene == lead;
+            if ((pass == 0) != same || cap == 0) continue;
+            const uint64_t q = std::min(lk.first, cap);
+            c.quota[lk.second] = uint32_t(q);
+            cap -= q;
+        }
     c.njobs = uint32_t(njobs);
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
