@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--vcm-passes", type=int, default=256, help="VCM iterations timed on the quantised BVH")
     p.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving stream (0: skip)")
     p.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream, jobs/s")
+    p.add_argument("--profile-case", choices=["query", "build", "pt", "vcm", "all"],
+                   help="run one bounded case for an ncu capture (no timing, no JSON line) and exit")
     return p.parse_args()
 
 
@@ -283,6 +285,46 @@ def serve_metrics(sel, scenes, dev, room, args):
         "throughput_ratio_served_vs_serial_plain": round(finish / served_wall, 3),
         "rays_note": "both forms trace the same paths (identical hits, same streams), so they trace the same rays",
     }
+
+
+def profile_case(case):
+    """Bounded workloads sized for ncu captures (a few GB on the device at most): ray queries on the 5.24 M-
+    triangle scene (1,048,576 coherent and incoherent rays, closest + any hit), two device BVH builds of
+    that scene, and the path tracer (4 spp) and VCM (2 passes) on the room with 8 textured icospheres at
+    640 x 360."""
+    from selas_gb300._build import build_library
+    build_library()
+    import selas_gb300 as sel
+    from selas_gb300 import scenes
+    dev = sel.Device(0)
+    if case in ("query", "all"):
+        data, co, inc = scenes.ray_query_workload(level=6, width=1024, height=1024, incoherent=1 << 20)
+        sc = sel.Scene(dev, sel.SEL_BVH_WIDE8_Q8)
+        data.attach_to(sc)
+        sc.commit()
+        for org, d in (co, inc):
+            sc.intersect1M(sel.make_rayhits(org, d))
+            sc.occluded1M(sel.make_rays(org, d))
+        sc.release()
+    if case in ("build", "all"):
+        data = scenes.displaced_icospheres(level=6)
+        for _ in range(2):
+            sc = sel.Scene(dev, sel.SEL_BVH_WIDE8_Q8, sel.SEL_BUILD_DEVICE)
+            data.attach_to(sc)
+            sc.commit()
+            sc.release()
+    if case in ("pt", "vcm", "all"):
+        room = scenes.vcm_room(icospheres=8)
+        sc = room.build(sel, dev)
+        cam = room.sel_camera(sel, 640, 360)
+        if case in ("pt", "all"):
+            sc.pt_generate_image(cam, sel.pt_settings(2, 8))
+            sc.pt_generate_image(cam, sel.pt_settings(4, 8))
+        if case in ("vcm", "all"):
+            lo, hi = room.geometry.bounds()
+            sc.vcm_generate_image(cam, sel.vcm_settings(2, 10, radius=0.003 * float(np.linalg.norm(hi - lo))))
+        sc.release()
+    dev.release()
 
 
 def render_metrics(sel, scenes, dev, stream, args, room=None):
@@ -541,6 +583,9 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
