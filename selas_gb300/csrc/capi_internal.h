@@ -45,6 +45,7 @@ struct SelSceneTy {
     void* d_ptex_faces = nullptr;
     void* d_ptex_texels = nullptr;
     uint32_t ptex_face_count = 0;
+    uint32_t sort_hint = 0;  // Ptex materials or more than one material class among the meshes
     void* d_materials = nullptr;
     void* d_lights = nullptr;
     void* d_light_sets = nullptr;

@@ -193,7 +193,89 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
     if (status) atomicOr(P.err, status);
 }
 
-__global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce) {
+// Material class of a queued path's hit: 0 miss; else 1 + shader * 4 + 2 (Ptex) + 1 (transparent).  Paths
+// are counting-sorted by class before shading, so a warp shades one kind of surface.
+__device__ __forceinline__ uint32_t material_class(const PtParams& P, uint32_t s) {
+    const uint32_t tri = __float_as_uint(P.st.hit[s].w);
+    if (tri == 0xffffffffu) return 0u;
+    const PtScene& S = P.st.jobs[P.st.job[s]].scene;
+    const uint32_t geom = __float_as_uint(__ldg(S.tris + size_t(tri) * 3 + 1).w);
+    const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
+    const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
+    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+}
+
+__global__ void k_class_reset(uint32_t* counters) {
+    if (threadIdx.x < 2 * kPtClasses) counters[32 + threadIdx.x] = 0u;
+}
+
+__global__ void __launch_bounds__(kBlock) k_classify(PtParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t c = valid ? material_class(P, P.st.queue[cur][e]) : 0xffu;
+        if (valid) P.st.cls[e] = c;
+        const uint32_t peers = __match_any_sync(0xffffffffu, c);
+        const uint32_t lane = threadIdx.x & 31u;
+        if (valid && (__ffs(peers) - 1) == int(lane)) atomicAdd(&P.st.counters[32 + c], __popc(peers));
+    }
+}
+
+__global__ void k_class_offsets(uint32_t* counters) {
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int c = 0; c < kPtClasses; ++c) {
+            counters[48 + c] = run;
+            run += counters[32 + c];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t c = valid ? P.st.cls[e] : 0xffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, c);
+        const uint32_t lane = threadIdx.x & 31u;
+        const int leader = __ffs(peers) - 1;
+        uint32_t at = 0;
+        if (valid && leader == int(lane)) at = atomicAdd(&P.st.counters[48 + c], __popc(peers));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (valid) P.st.queue_sorted[at + __popc(peers & ((1u << lane) - 1u))] = P.st.queue[cur][e];
+    }
+}
+
+// Ptex base colour of the sorted paths whose hit material is textured (SurfaceParameters.cpp:196-206): a
+// kernel of its own keeps the filter's code out of the shading kernel.
+__global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    uint32_t status = 0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint32_t s = P.st.queue_sorted[e];
+        const float4 hit = P.st.hit[s];
+        const uint32_t tri = __float_as_uint(hit.w);
+        if (tri == 0xffffffffu) continue;
+        const PtScene& S = P.st.jobs[P.st.job[s]].scene;
+        const float4* tp = S.tris + size_t(tri) * 3;
+        const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1);
+        const uint32_t geom = __float_as_uint(p1.w);
+        const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
+        if (!(m.flags & kMaterialUsesPtex)) continue;
+        float3 base = ld3(m.base_color);
+        uint32_t pstatus = 0;
+        ptex_eval(static_cast<const PtexFace*>(S.ptex_faces), int(S.ptex_face_count),
+                  static_cast<const __half*>(S.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z,
+                  base, pstatus);
+        status |= pstatus;
+        P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+__global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     const int next = cur ^ 1;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -203,7 +285,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
         uint32_t s = 0;
         float4 sh_o = make_float4(0, 0, 0, 0), sh_d = sh_o, sh_c = sh_o;
         if (valid) {
-            s = P.st.queue[cur][e];
+            s = in_queue[e];
             const uint32_t job = P.st.job[s];
             const PtJob& J = P.st.jobs[job];
             const PtScene& S = J.scene;
@@ -237,13 +319,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
                 float3 base = ld3(m.base_color);
-                if (m.flags & kMaterialUsesPtex) {
-                    // per-face Ptex base colour at the hit's barycentrics (SurfaceParameters.cpp:196-206)
-                    uint32_t pstatus = 0;
-                    ptex_eval(static_cast<const PtexFace*>(S.ptex_faces), int(S.ptex_face_count),
-                              static_cast<const __half*>(S.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
-                              hit.z, base, pstatus);
-                    if (pstatus) atomicOr(P.err, pstatus);
+                if (m.flags & kMaterialUsesPtex) {  // filtered by k_texture for this hit
+                    const float4 b = P.st.base[s];
+                    base = f3(b.x, b.y, b.z);
                 }
                 const Surface sf = make_surface(m, ng, -d, base);
                 // Next-event estimation to the surface's light set (AreaLighting.cpp:353-373)
@@ -387,6 +465,9 @@ void pt_layout(PtState& st, Take take, uint32_t paths) {
     st.rng = reinterpret_cast<uint64_t*>(take(8ull * paths));
     st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.queue_sorted = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.cls = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.base = reinterpret_cast<float4*>(take(16ull * paths));
     st.sh_o = reinterpret_cast<float4*>(take(16ull * paths));
     st.sh_d = reinterpret_cast<float4*>(take(16ull * paths));
     st.sh_c = reinterpret_cast<float4*>(take(16ull * paths));
@@ -419,8 +500,8 @@ size_t pt_state_block_bytes(uint32_t paths) {
     return total;
 }
 
-cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, uint32_t* d_err, uint64_t batches,
-                           cudaStream_t stream, GraphCache* graphs) {
+cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -439,7 +520,14 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, ui
             k_bounce_reset<<<1, 32, 0, s>>>(st.counters, cur ^ 1);
             if (bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, s>>>(P, cur);
             else k_extend<1><<<trace_grid, kBlock, 0, s>>>(P, cur);
-            k_shade<<<shade_grid, kBlock, 0, s>>>(P, cur, b);
+            if (sort) {
+                k_class_reset<<<1, 32, 0, s>>>(st.counters);
+                k_classify<<<shade_grid, kBlock, 0, s>>>(P, cur);
+                k_class_offsets<<<1, 32, 0, s>>>(st.counters);
+                k_class_scatter<<<shade_grid, kBlock, 0, s>>>(P, cur);
+                k_texture<<<shade_grid, kBlock, 0, s>>>(P, cur);
+            }
+            k_shade<<<shade_grid, kBlock, 0, s>>>(P, cur, b, sort ? st.queue_sorted : st.queue[cur]);
             if (bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, s>>>(P);
             else k_shadow<1><<<trace_grid, kBlock, 0, s>>>(P);
         }
@@ -448,13 +536,14 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, ui
     struct Key {
         PtParams P;
         int kind, sms;
-        uint32_t bounces;
+        uint32_t bounces, sort;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
     key.kind = bvh_kind;
     key.sms = sms;
     key.bounces = bounces;
+    key.sort = sort ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -476,7 +565,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     if (e == cudaSuccess) e = cudaMemcpyAsync(st.control, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
-    return pt_run_batches(sc.bvh_kind, set.max_bounces, st, d_err, batches, stream, graphs);
+    return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

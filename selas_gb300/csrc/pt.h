@@ -14,7 +14,9 @@ struct MaterialDev;
 struct QuadLight;
 
 constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
-                                // [8] holds the current batch size
+                                // [8] holds the current batch size, [32..47] material-class counts,
+                                // [48..63] their scatter cursors
+constexpr int kPtClasses = 16;
 constexpr int kMaxPtJobs = 16;  // jobs sharing one wavefront (shadow records pack the job in 4 bits)
 
 // Scene view the integrators read.
@@ -31,6 +33,7 @@ struct PtScene {
     const void* ptex_texels;  // half RGB
     uint32_t ptex_face_count;
     float background[3];
+    uint32_t sort_hint;  // 1: the scene has Ptex materials or several material classes (sort before shading)
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.
@@ -79,6 +82,9 @@ struct PtState {
     uint64_t* path_id;  // index of the path within its job (its PCG32 stream)
     uint64_t* rng;
     uint32_t* queue[2];
+    uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort)
+    uint32_t* cls;    // material class of each current queue entry
+    float4* base;     // Ptex base colour (authored, before the 2.2 power) of the path's current hit
     float4* sh_o;     // shadow rays: origin, tnear
     float4* sh_d;     // direction, tfar
     float4* sh_c;     // contribution, (job << 28 | pixel) bits
@@ -95,8 +101,10 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // Launches `batches` batches of the shared wavefront over the jobs in st.jobs / st.control (uploaded by the
 // caller).  `bounces` is the number of extend/shade/shadow rounds per batch (the largest max_bounces of the
 // jobs).  With `graphs`, one batch is captured as a CUDA graph and replayed.
-cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, const PtState& st, uint32_t* d_err, uint64_t batches,
-                           cudaStream_t stream, GraphCache* graphs);
+// `sort`: order each bounce's queue by material class and filter Ptex in a kernel of its own before shading
+// (required when a job's scene uses Ptex).
+cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs);
 
 // Single render (PathTracer::GenerateImage): one job, batches until all its paths are done.
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,

@@ -101,6 +101,18 @@ int sync_shading(SelSceneTy* sc) {
         for (const auto& pb : sc->ptex) bound |= (&m - mats.data()) == ptrdiff_t(pb.geomID);
         if (!bound) m.flags &= ~kMaterialUsesPtex;  // no texture bound: keep the material's base colour
     }
+    // material classes of the attached meshes (shader x Ptex x transparency, as the path tracer sorts them)
+    {
+        uint32_t seen = 0;
+        for (const MeshInput& mi : sc->meshes) {
+            const MaterialDev& m = mats[mi.geomID < mats.size() ? mi.geomID : 0];
+            const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
+            seen |= 1u << (shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u));
+        }
+        bool ptex = false;
+        for (const auto& m : mats) ptex |= (m.flags & kMaterialUsesPtex) != 0;
+        sc->sort_hint = (ptex || __builtin_popcount(seen) > 1) ? 1u : 0u;
+    }
     if (int rc = upload(sc->d_ptex_faces, faces.data(), faces.size())) return rc;
     if (int rc = upload(sc->d_ptex_texels, texels.data(), texels.size())) return rc;
     sc->ptex_face_count = uint32_t(faces.size());
@@ -167,6 +179,7 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.ptex_texels = sc->d_ptex_texels;
     ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
+    ps.sort_hint = sc->sort_hint;
     return ps;
 }
 

@@ -279,7 +279,10 @@ bool pt_round(SelServerTy* S) {
     }
     cudaMemcpyAsync(S->pst.jobs, table, sizeof(PtJob) * kMaxPtJobs, cudaMemcpyHostToDevice, S->pt_stream);
     cudaMemcpyAsync(S->pst.control, &c, sizeof(PtControl), cudaMemcpyHostToDevice, S->pt_stream);
-    cudaError_t e = pt_run_batches(0, S->cfg.max_bounces, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph);
+    bool sort = false;
+    for (int k = 0; k < kMaxPtJobs; ++k)
+        if (S->slots[k]) sort |= S->slots[k]->scene.sort_hint != 0;
+    cudaError_t e = pt_run_batches(0, S->cfg.max_bounces, sort, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph);
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
         if (!j || c.quota[k] == 0) continue;
