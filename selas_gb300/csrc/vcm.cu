@@ -835,10 +835,12 @@ __global__ void __launch_bounds__(256) k_gather_positions(VcmParams P) {
 }
 
 // One warp per camera vertex (MergeVertices + SearchHashGrid, VCM.cpp:362-409, VCMHashGrid.cpp:107-155;
-// tech report sec. 5.6): the ranges of the 2x2x2 cells around it are concatenated, lanes stride over the
-// concatenation (a cell visited twice when two of the eight cells hash to one bucket, as the sequential
-// search visits it), each lane keeps a partial sum and a fixed xor-tree reduction adds them.
+// tech report sec. 5.6): the ranges of the 2x2x2 cells around it are concatenated (a cell visited twice
+// when two of the eight cells hash to one bucket, as the sequential search visits it), lanes test the
+// concatenation against the radius and compact the hits, all lanes evaluate the compacted candidates,
+// each keeps a partial sum and a fixed xor-tree reduction adds them.
 __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
+    __shared__ uint32_t mbuf[kBlock / 32][64];  // per warp: candidates inside the radius, awaiting evaluation
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[5];
     const uint32_t N = P.npaths;
@@ -885,27 +887,22 @@ __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
         const CameraVertex cv = load_camera_vertex(rec);
         const Surface cs = make_surface_linear(P.materials[cv.mat], cv.n, cv.view, cv.base);
         float3 merged = f3(0.0f);
-        for (uint32_t t = lane; t < total; t += 32) {
-            int j = 0;
-#pragma unroll
-            for (int q = 0; q < 7; ++q) j += t >= ends[q] ? 1 : 0;
-            uint32_t start = 0, b = 0;
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (q == j) { b = bases[q]; start = q > 0 ? ends[q - 1] : 0u; }
-            const uint32_t k = b + (t - start);
-            const float4 sp = P.st.spos[k];
-            const float3 dd = pos - f3(sp.x, sp.y, sp.z);
-            if (dot(dd, dd) > gr2) continue;
-            const LightVertex lv = load_vertex(P.st.verts + size_t(__float_as_uint(sp.w)) * 5);
-            if (cv.len + lv.len > P.max_len) continue;
+        // two phases so that the BSDF work runs on full warps: lanes test 32 candidates at a time against
+        // the radius and append the ones inside to the warp's buffer; every 32 buffered candidates are
+        // evaluated by all lanes together
+        uint32_t* buf = mbuf[threadIdx.x >> 5];
+        uint32_t pending = 0;
+        const uint32_t below = (1u << lane) - 1u;
+        auto evaluate = [&](uint32_t vslot) {
+            const LightVertex lv = load_vertex(P.st.verts + size_t(vslot) * 5);
+            if (cv.len + lv.len > P.max_len) return;
             // the reference merges only between surfaces of the same transparency (VCM.cpp:372-375)
             const uint32_t lt = (P.materials[lv.mat].flags & kMaterialTransparent) ? 1u : 0u;
-            if (cv.transparent != lt) continue;
+            if (cv.transparent != lt) return;
             float fwd, rev;
             const float3 fc = bsdf_evaluate(cs, cv.view, lv.view, fwd, rev);
             const float cosl = fabsf(dot(cv.n, lv.view));
-            if (!nonzero(fc) || cosl == 0.0f) continue;
+            if (!nonzero(fc) || cosl == 0.0f) return;
             const float lcont = saturate(max3(lv.base));
             fwd *= cv.cont;
             rev *= lcont;
@@ -913,7 +910,41 @@ __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
             const float w_camera = cv.dvcm * c.vc_weight + cv.dvm * rev;
             const float mis = 1.0f / (w_light + 1.0f + w_camera);
             merged = merged + (mis / cosl) * (fc * lv.thr);
+        };
+        for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            bool in = false;
+            uint32_t vslot = 0;
+            if (t < total) {
+                int j = 0;
+#pragma unroll
+                for (int q = 0; q < 7; ++q) j += t >= ends[q] ? 1 : 0;
+                uint32_t start = 0, b = 0;
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q == j) { b = bases[q]; start = q > 0 ? ends[q - 1] : 0u; }
+                const float4 sp = P.st.spos[b + (t - start)];
+                const float3 dd = pos - f3(sp.x, sp.y, sp.z);
+                in = dot(dd, dd) <= gr2;
+                vslot = __float_as_uint(sp.w);
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, in);
+            if (in) buf[pending + __popc(m & below)] = vslot;
+            pending += __popc(m);
+            __syncwarp();
+            if (pending >= 32) {
+                evaluate(buf[lane]);
+                __syncwarp();
+                const uint32_t rest = pending - 32;
+                const uint32_t v = lane < rest ? buf[32 + lane] : 0u;
+                __syncwarp();
+                if (lane < rest) buf[lane] = v;
+                __syncwarp();
+                pending = rest;
+            }
         }
+        if (lane < pending) evaluate(buf[lane]);
+        __syncwarp();
         for (int o = 16; o > 0; o >>= 1) {
             merged.x += __shfl_xor_sync(0xffffffffu, merged.x, o);
             merged.y += __shfl_xor_sync(0xffffffffu, merged.y, o);
