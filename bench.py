@@ -525,7 +525,8 @@ def run_ours(args):
     alg_bytes = counts[dom] * QUERY_BYTES[kinds[dom]]
     achieved = alg_bytes / (per_kernel[dom] * 1e-3) / 1e9
     traffic = ncu_traffic().get(f"wide8.{dom}")
-    roofline = {"bound": "hbm", "kernel": f"k_{kinds[dom]}<wide8> ({dom})", "achieved": round(achieved, 2),
+    kname = "k_query_wide<closest>" if kinds[dom] == "intersect" else "k_query_wide<any>"
+    roofline = {"bound": "hbm", "kernel": f"{kname} ({dom})", "achieved": round(achieved, 2),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
                 "avg_launch_ms": round(per_kernel[dom], 4)}
