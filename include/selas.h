@@ -120,6 +120,8 @@ int sel_scene_set_bvh_kind(SelScene scene, int bvh_kind);
  * builder. */
 enum { SEL_BUILD_HOST = 0, SEL_BUILD_DEVICE = 1 };
 int sel_scene_set_build_mode(SelScene scene, int build_mode);
+/* Triangles per leaf of the device-built 8-wide layout, 1..4 (default 3; the host builder uses 3). */
+int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size);
 /* vertices: vertex_count records of 3 floats (x,y,z) every vertex_stride_bytes bytes (>= 12);
  * indices: triangle_count x 3 unsigned ints.  The data is copied; the caller may free it after the
  * call.  geomID is reported in SelHit.geomID; primID is the triangle's index within this mesh. */
@@ -286,8 +288,8 @@ typedef struct SelPtSettings {
     uint32_t samplesPerPixel;  /* PathsPerPixel_ (PathTracer.cpp:45) */
     uint32_t maxBounces;       /* MaxBounceCount_ (PathTracer.cpp:42) */
     uint64_t seed;             /* PCG32 seed; path k uses stream k */
-    uint32_t pathsInFlight;    /* wavefront batch (0 = 4,194,304) */
-    uint32_t reserved;
+    uint32_t pathsInFlight;    /* wavefront batch (0 = the scene's tuned value, else 4,194,304) */
+    uint32_t traceBlockSize;   /* threads per traversal block: 128 or 256 (0 = the scene's tuned value, else 128) */
 } SelPtSettings;
 
 /* PathTracer::GenerateImage (Source/Applications/Selas/Source/PathTracer.h:20-21): renders the scene
@@ -299,6 +301,24 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
  * `stream` and returns without waiting. */
 int sel_pt_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
                          void* stream);
+
+/* Autotuner (no reference counterpart).  Renders the given path-tracer workload (timed with CUDA events,
+ * after one untimed render per configuration) over BVH layout and leaf size {8-wide quantised with 2, 3, 4
+ * triangles per leaf; binary FP32}, wavefront capacity {1,048,576; 4,194,304; 8,388,608 paths} and traversal
+ * block size {128, 256 (8-wide only)}; rebuilds the scene with the fastest layout and keeps the fastest
+ * capacity and block size as its defaults (used when SelPtSettings leaves them 0).  Images do not depend on
+ * any of these choices. */
+typedef struct SelTuneTrial {
+    uint32_t bvh_kind, leaf_size, paths_in_flight, trace_block;
+    double ms;  /* one render */
+} SelTuneTrial;
+typedef struct SelTuneResult {
+    SelTuneTrial best;
+    uint32_t trials;
+    uint32_t reserved;
+    SelTuneTrial trial[32];
+} SelTuneResult;
+int sel_scene_autotune(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, SelTuneResult* out);
 
 /* Vertex connection and merging: VCM::GenerateImage (Source/Applications/Selas/Source/VCM.h:18,
  * VCM.cpp:751-808, commented out in the reference and restated from the VCM technical report it cites).

@@ -241,7 +241,7 @@ class SelCamera(ctypes.Structure):
 
 class SelPtSettings(ctypes.Structure):
     _fields_ = [("samplesPerPixel", ctypes.c_uint32), ("maxBounces", ctypes.c_uint32), ("seed", ctypes.c_uint64),
-                ("pathsInFlight", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("pathsInFlight", ctypes.c_uint32), ("traceBlockSize", ctypes.c_uint32)]
 
 
 class SelVcmSettings(ctypes.Structure):
@@ -451,3 +451,38 @@ class Server:
         if self.handle:
             check(lib().sel_server_release(self.handle))
             self.handle = None
+
+
+# ---------------------------------------------------------------------------------------------------
+# Autotuner (include/selas.h: sel_scene_autotune)
+# ---------------------------------------------------------------------------------------------------
+class SelTuneTrial(ctypes.Structure):
+    _fields_ = [("bvh_kind", ctypes.c_uint32), ("leaf_size", ctypes.c_uint32), ("paths_in_flight", ctypes.c_uint32),
+                ("trace_block", ctypes.c_uint32), ("ms", ctypes.c_double)]
+
+
+class SelTuneResult(ctypes.Structure):
+    _fields_ = [("best", SelTuneTrial), ("trials", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("trial", SelTuneTrial * 32)]
+
+
+register_signatures({
+    "sel_scene_set_leaf_size": [_vp, _u],
+    "sel_scene_autotune": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), ctypes.POINTER(SelTuneResult)],
+})
+
+
+def _scene_autotune(self, cam: SelCamera, settings: SelPtSettings) -> SelTuneResult:
+    """sel_scene_autotune: times the workload over BVH layout / leaf size / capacity / block size, keeps the
+    fastest on the scene and returns every trial."""
+    r = SelTuneResult()
+    check(lib().sel_scene_autotune(self.handle, ctypes.byref(cam), ctypes.byref(settings), ctypes.byref(r)))
+    return r
+
+
+def _scene_set_leaf_size(self, n: int) -> None:
+    check(lib().sel_scene_set_leaf_size(self.handle, n))
+
+
+Scene.autotune = _scene_autotune
+Scene.set_leaf_size = _scene_set_leaf_size

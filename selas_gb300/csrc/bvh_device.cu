@@ -1,7 +1,7 @@
 // Device SAH-binned BVH builder: the 8-wide quantised layout of bvh_build.cpp built on the GPU.
 //
 // Same method as the host builder (binned SAH after Wald 2007, 32 bins per axis, leaves of at most 3
-// triangles, object-median splits beyond depth 40, greedy collapse to 8 children by largest surface area,
+// triangles by default (1..4 selectable), object-median splits beyond depth 40, greedy collapse to 8 children by largest surface area,
 // octant slot assignment and outward 8-bit child-box quantisation after Ylitie, Karras and Laine 2017),
 // organised for the GPU:
 //   1. one thread per triangle: bounds, centroid (box centre, as the host builder);
@@ -28,7 +28,7 @@ namespace sel {
 namespace {
 
 constexpr int kBinsD = 32;
-constexpr uint32_t kMaxLeafD = 3;
+constexpr uint32_t kMaxLeafLimit = 4;  // 8 leaf slots x 4 triangles fit the 5-bit leaf offsets of WideNode
 constexpr int kMedianDepthD = 40;
 constexpr uint32_t kSmall = 1024;   // subtrees at or below this many triangles are built by one warp
 constexpr int kWarpStack = 32;
@@ -65,6 +65,7 @@ struct Build {
     uint32_t* counters;   // [0] next large tasks, [1] small tasks, [2] max large count, [3] depth, [4] error
     int* scene_box;       // 6 ordered ints
     uint32_t n;
+    uint32_t max_leaf;    // triangles per leaf, 1..kMaxLeafLimit
 };
 
 __global__ void k_init_counters(Build B) {
@@ -415,7 +416,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(Build B) {
             split_axis = uint32_t(axis);
             const bool degenerate = !(v[9 + axis] > v[6 + axis]);
             if (!leaf && (degenerate || int(depth) >= kMedianDepthD)) {
-                leaf = count <= kMaxLeafD;  // otherwise split by position
+                leaf = count <= B.max_leaf;  // otherwise split by position
             } else if (!leaf) {
                 for (int i = lane; i < 3 * kBinsD * 7; i += 32) {
                     const int q = i % 7;
@@ -468,7 +469,7 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(Build B) {
                 const float parent = box_area(make_float3(v[0], v[1], v[2]), make_float3(v[3], v[4], v[5]));
                 const float leaf_cost = parent * float(count);
                 const float split_cost = parent + best;
-                if (count <= kMaxLeafD && (best_axis < 0 || split_cost >= leaf_cost)) {
+                if (count <= B.max_leaf && (best_axis < 0 || split_cost >= leaf_cost)) {
                     leaf = true;
                 } else if (best_axis >= 0) {
                     mode = 0;
@@ -717,7 +718,8 @@ cudaError_t dalloc(T*& p, size_t count) {
 
 }  // namespace
 
-std::string build_wide_device(const std::vector<MeshInput>& meshes, DeviceBuild& out) {
+std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max_leaf, DeviceBuild& out) {
+    if (max_leaf < 1 || max_leaf > kMaxLeafLimit) return "leaf size must lie in 1..4";
     std::vector<TriRecord> soup;
     size_t total = 0;
     for (const MeshInput& m : meshes) total += m.indices.size() / 3;
@@ -754,6 +756,7 @@ std::string build_wide_device(const std::vector<MeshInput>& meshes, DeviceBuild&
     Build B;
     std::memset(&B, 0, sizeof(B));
     B.n = n;
+    B.max_leaf = max_leaf;
     const uint32_t max_large = n / kSmall + 2;
     const size_t max_nodes = 2 * size_t(n);
     std::vector<void*> owned;

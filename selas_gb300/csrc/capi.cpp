@@ -181,6 +181,14 @@ int sel_scene_set_build_mode(SelScene scene, int build_mode) {
     return SEL_OK;
 }
 
+int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (leaf_size < 1 || leaf_size > 4) return fail(SEL_ERR_INVALID_ARGUMENT, "leaf_size must lie in 1..4");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    scene->leaf_size = leaf_size;
+    return SEL_OK;
+}
+
 int sel_scene_commit(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     std::lock_guard<std::mutex> lock(scene->mu);
@@ -189,7 +197,7 @@ int sel_scene_commit(SelScene scene) {
         DeviceBuild db;
         std::string derr;
         try {
-            derr = build_wide_device(scene->meshes, db);
+            derr = build_wide_device(scene->meshes, scene->leaf_size, db);
         } catch (const std::bad_alloc&) {
             return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed during BVH build");
         }

@@ -23,6 +23,9 @@ struct SelSceneTy {
     SelDeviceTy* dev = nullptr;
     int kind = SEL_BVH_WIDE8_Q8;
     int build_mode = SEL_BUILD_DEVICE;  // 8-wide layout built by GPU kernels (binary: always host)
+    uint32_t leaf_size = 3;             // triangles per leaf of the device-built 8-wide layout
+    uint32_t tuned_paths_in_flight = 0; // sel_scene_autotune's choices (0: built-in defaults)
+    uint32_t tuned_trace_block = 0;
     std::vector<sel::MeshInput> meshes;
     bool committed = false;
     void* d_nodes = nullptr;

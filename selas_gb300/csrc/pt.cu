@@ -147,9 +147,9 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
 
 // Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
 // so expensive and cheap rays balance across the GPU.
-template <int K>
-__global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+template <int K, int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_extend(PtParams P, int cur) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     const uint32_t* queue = P.st.queue[cur];
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(PtParams P, int cur) {
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = tfar;
             QueryHit h;
             const PtScene& sc = P.st.jobs[P.st.job[s]].scene;
-            const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x, kBlock,
+            const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x, B,
                                                                 status);
             P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
                                 : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
@@ -412,9 +412,9 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
     }
 }
 
-template <int K>
-__global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+template <int K, int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_shadow(PtParams P) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     uint32_t status = 0;
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_shadow(PtParams P) {
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
             QueryHit h;
-            if (!Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, kBlock,
+            if (!Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, B,
                                                  status))
                 accumulate(J.accum, J.cam.width * J.cam.height, 1, tag & 0x0fffffffu, f3(c.x, c.y, c.z));
         }
@@ -501,7 +501,10 @@ size_t pt_state_block_bytes(uint32_t paths) {
 }
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
-                           uint64_t batches, cudaStream_t stream, GraphCache* graphs) {
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block) {
+    // 256-thread traversal blocks only for the 8-wide layout (its 24-entry stack then fills the 48 KB of
+    // static shared memory; the binary layout's 64-entry stack would not fit)
+    const int tb = (trace_block == 256 && bvh_kind == 0) ? 256 : 128;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -509,7 +512,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     std::memset(&P, 0, sizeof(P));
     P.st = st;
     P.err = d_err;
-    const int trace_grid = grid_for(sms, 8);
+    const int trace_grid = grid_for(sms, 1024 / tb);
     const int shade_grid = grid_for(sms, 8);
     const int gen_grid = int((st.capacity + kBlock - 1) / kBlock);
     auto enqueue = [&](cudaStream_t s) {
@@ -518,8 +521,9 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         for (uint32_t b = 0; b < bounces; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, s>>>(st.counters, cur ^ 1);
-            if (bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, s>>>(P, cur);
-            else k_extend<1><<<trace_grid, kBlock, 0, s>>>(P, cur);
+            if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
+            else if (bvh_kind == 0) k_extend<0, 128><<<trace_grid, tb, 0, s>>>(P, cur);
+            else k_extend<1, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             if (sort) {
                 k_class_reset<<<1, 32, 0, s>>>(st.counters);
                 k_classify<<<shade_grid, kBlock, 0, s>>>(P, cur);
@@ -528,8 +532,9 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
                 k_texture<<<shade_grid, kBlock, 0, s>>>(P, cur);
             }
             k_shade<<<shade_grid, kBlock, 0, s>>>(P, cur, b, sort ? st.queue_sorted : st.queue[cur]);
-            if (bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, s>>>(P);
-            else k_shadow<1><<<trace_grid, kBlock, 0, s>>>(P);
+            if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
+            else if (bvh_kind == 0) k_shadow<0, 128><<<trace_grid, tb, 0, s>>>(P);
+            else k_shadow<1, 128><<<trace_grid, tb, 0, s>>>(P);
         }
         k_batch_end<<<1, 32, 0, s>>>(P);
     };
@@ -537,6 +542,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         PtParams P;
         int kind, sms;
         uint32_t bounces, sort;
+        int tb;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -544,11 +550,12 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.sms = sms;
     key.bounces = bounces;
     key.sort = sort ? 1u : 0u;
+    key.tb = tb;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
-                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs) {
+                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs, int trace_block) {
     PtJob job;
     std::memset(&job, 0, sizeof(job));
     job.scene = sc;
@@ -565,7 +572,8 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     if (e == cudaSuccess) e = cudaMemcpyAsync(st.control, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
-    return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs);
+    return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
+                          trace_block);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -103,12 +103,13 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // jobs).  With `graphs`, one batch is captured as a CUDA graph and replayed.
 // `sort`: order each bounce's queue by material class and filter Ptex in a kernel of its own before shading
 // (required when a job's scene uses Ptex).
+// `trace_block`: threads per block of the traversal kernels (128, or 256 with the 8-wide layout).
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
-                           uint64_t batches, cudaStream_t stream, GraphCache* graphs);
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128);
 
 // Single render (PathTracer::GenerateImage): one job, batches until all its paths are done.
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
-                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs);
+                      uint32_t* d_err, cudaStream_t stream, GraphCache* graphs, int trace_block = 128);
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream);
 
 }  // namespace sel

@@ -150,6 +150,8 @@ int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettin
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
         return fail(SEL_ERR_INVALID_ARGUMENT, "fovDegrees must lie in (0, 180)");
     if (settings->samplesPerPixel == 0) return fail(SEL_ERR_INVALID_ARGUMENT, "samplesPerPixel must be > 0");
+    if (settings->traceBlockSize != 0 && settings->traceBlockSize != 128 && settings->traceBlockSize != 256)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "traceBlockSize must be 0, 128 or 256");
     const uint64_t total = uint64_t(camera->width) * camera->height * settings->samplesPerPixel;
     if (total >= (uint64_t(1) << 32)) return fail(SEL_ERR_INVALID_ARGUMENT, "width * height * spp must be < 2^32");
     return SEL_OK;
@@ -224,7 +226,8 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
                   cudaStream_t stream) {
     if (int rc = sync_shading(sc)) return rc;
     const uint64_t total = uint64_t(camera.width) * camera.height * settings.samplesPerPixel;
-    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight : kDefaultPathsInFlight;
+    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight
+                   : (sc->tuned_paths_in_flight ? sc->tuned_paths_in_flight : kDefaultPathsInFlight);
     if (uint64_t(cap) > total) cap = uint32_t(total);
     if (int rc = ensure_pt_state(sc, cap)) return rc;
     const PtScene ps = scene_view(sc);
@@ -235,8 +238,10 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     set.max_bounces = settings.maxBounces;
     set.seed = settings.seed;
     const PtState st = pt_state_carve(sc->pt_block, cap);
+    const int block = int(settings.traceBlockSize ? settings.traceBlockSize
+                                                  : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream,
-                              sc->dev->graph_replay ? &sc->pt_graph : nullptr);
+                              sc->dev->graph_replay ? &sc->pt_graph : nullptr, block);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
 }
 
@@ -508,6 +513,86 @@ int sel_vcm_generate_image(SelScene scene, const SelCamera* camera, const SelVcm
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "VCM");
     return read_error_word(dev, s);
+}
+
+int sel_scene_autotune(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, SelTuneResult* out) {
+    if (int rc = check_render_args(scene, camera, settings)) return rc;
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    std::memset(out, 0, sizeof(*out));
+    if (int rc = set_device(scene->dev)) return rc;
+    struct Layout {
+        int kind;
+        uint32_t leaf;
+    };
+    const Layout layouts[] = {{SEL_BVH_WIDE8_Q8, 2}, {SEL_BVH_WIDE8_Q8, 3}, {SEL_BVH_WIDE8_Q8, 4}, {SEL_BVH_BINARY_FP32, 3}};
+    const uint32_t capacities[] = {1u << 20, 1u << 22, 1u << 23};
+    const int blocks[] = {128, 256};
+    const size_t values = 2ull * camera->width * camera->height * 3;
+    double* acc = nullptr;
+    cudaStream_t s = scene->dev->stream;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaError_t e = cudaMalloc(&acc, values * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev1);
+    if (e != cudaSuccess) {
+        if (acc) cudaFree(acc);
+        return cuda_fail(e, "autotune set-up");
+    }
+    const int kind0 = scene->kind;
+    const uint32_t leaf0 = scene->leaf_size;
+    SelTuneTrial best;
+    std::memset(&best, 0, sizeof(best));
+    best.ms = 1e300;
+    int rc = SEL_OK;
+    for (const Layout& L : layouts) {
+        {
+            std::lock_guard<std::mutex> lock(scene->mu);
+            scene->kind = L.kind;
+            scene->leaf_size = L.leaf;
+        }
+        if (sel_scene_commit(scene) != SEL_OK) continue;  // e.g. a tree deeper than a traversal stack
+        for (uint32_t cap : capacities)
+            for (int block : blocks) {
+                if (block == 256 && L.kind != SEL_BVH_WIDE8_Q8) continue;
+                SelPtSettings st = *settings;
+                st.pathsInFlight = cap;
+                st.traceBlockSize = uint32_t(block);
+                rc = sel_pt_render_device(scene, camera, &st, acc, s);  // untimed: builds state and graph
+                if (rc == SEL_OK) rc = sel_device_sync(scene->dev, s);
+                if (rc != SEL_OK) break;
+                cudaEventRecord(ev0, s);
+                rc = sel_pt_render_device(scene, camera, &st, acc, s);
+                cudaEventRecord(ev1, s);
+                if (rc == SEL_OK) rc = sel_device_sync(scene->dev, s);
+                if (rc != SEL_OK) break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev0, ev1);
+                SelTuneTrial t;
+                t.bvh_kind = uint32_t(L.kind);
+                t.leaf_size = L.leaf;
+                t.paths_in_flight = cap;
+                t.trace_block = uint32_t(block);
+                t.ms = ms;
+                if (out->trials < 32) out->trial[out->trials++] = t;
+                if (t.ms < best.ms) best = t;
+            }
+        if (rc != SEL_OK) break;
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaFree(acc);
+    {
+        std::lock_guard<std::mutex> lock(scene->mu);
+        scene->kind = best.ms < 1e300 ? int(best.bvh_kind) : kind0;
+        scene->leaf_size = best.ms < 1e300 ? best.leaf_size : leaf0;
+        scene->tuned_paths_in_flight = best.ms < 1e300 ? best.paths_in_flight : 0;
+        scene->tuned_trace_block = best.ms < 1e300 ? best.trace_block : 0;
+    }
+    const int rc_commit = sel_scene_commit(scene);
+    if (rc != SEL_OK) return rc;
+    if (rc_commit != SEL_OK) return rc_commit;
+    out->best = best;
+    return SEL_OK;
 }
 
 }  // extern "C"

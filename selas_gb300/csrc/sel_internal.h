@@ -85,7 +85,7 @@ struct DeviceBuild {
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     double build_ms = 0.0;    // upload of the triangles + all build kernels
 };
-std::string build_wide_device(const std::vector<MeshInput>& meshes, DeviceBuild& out);
+std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max_leaf, DeviceBuild& out);
 
 // Traversal stack capacities (entries per thread); the builder rejects trees deeper than these.
 constexpr int kWideStack = 24;

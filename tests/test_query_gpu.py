@@ -173,13 +173,14 @@ def test_untraceable_rays_miss_like_the_bruteforce_definition(device, kind):
     sc.release()
 
 
-@pytest.mark.parametrize("n_spheres,level", [(1, 0), (3, 2), (8, 4)])
-def test_device_built_bvh_matches_bruteforce(device, n_spheres, level):
+@pytest.mark.parametrize("n_spheres,level,leaf", [(1, 0, 3), (3, 2, 3), (8, 4, 3), (8, 4, 1), (8, 4, 2), (8, 4, 4)])
+def test_device_built_bvh_matches_bruteforce(device, n_spheres, level, leaf):
     """The 8-wide BVH built by the GPU kernels (SEL_BUILD_DEVICE) answers every query as the definition does,
     from a 20-triangle scene (one warp builds the whole tree) to 80 k triangles (large-task levels first)."""
     data = scenes.displaced_icospheres(count=n_spheres, level=level, seed=31)
     soup = data.soup()
     sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8, sel.SEL_BUILD_DEVICE)
+    sc.set_leaf_size(leaf)
     data.attach_to(sc)
     sc.commit()
     info = sc.info()
