@@ -387,6 +387,27 @@ def render_metrics(sel, scenes, dev, stream, args, room=None):
                      "paths_per_s": round(2 * w * h * passes / (ms * 1e-3), 1), "scene_upload_and_build_s": round(build_s, 2)}
         sc.release()
     vcm["speedup_of_quantised_wide"] = round(vcm["quantised_wide8"]["paths_per_s"] / vcm["plain_fp32_binary"]["paths_per_s"], 3)
+
+    # autotuner on the room's path-tracer workload: default configuration against the tuned one
+    sc = room.build(sel, dev)
+    cam = room.sel_camera(sel, 512, 512)
+    acc = torch.zeros((2, 512, 512, 3), dtype=torch.float64, device="cuda")
+    st = sel.pt_settings(16, 8)
+    render = lambda: sel.check(lib.sel_pt_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(st), acc.data_ptr(), sp))
+    default_ms = timed(render, 3)
+    t0 = time.time()
+    res = sc.autotune(cam, st)
+    tune_s = time.time() - t0
+    tuned_ms = timed(render, 3)
+    b = res.best
+    out["autotune"] = {"workload": "room path tracer, 512x512, 16 spp, depth 8",
+                       "space": "8-wide leaf {2,3,4} | binary; capacity {1M, 4M, 8M} paths; traversal block {128, 256}",
+                       "trials": int(res.trials), "tuning_s": round(tune_s, 2),
+                       "best": {"bvh": "8-wide quantised" if b.bvh_kind == 0 else "binary FP32", "leaf": int(b.leaf_size),
+                                "paths_in_flight": int(b.paths_in_flight), "trace_block": int(b.trace_block)},
+                       "default_ms": round(default_ms, 3), "tuned_ms": round(tuned_ms, 3),
+                       "speedup": round(default_ms / tuned_ms, 3)}
+    sc.release()
     out["vcm"] = {"workload": f"room 20x20x10 with {room.geometry.triangle_count} triangles (24 displaced icospheres "
                               f"with 16x16 FP16 Ptex per face, 40 glass spheres), 1280x720, max path length 10, "
                               f"r0 {r0:.4f} (0.003 x diagonal), alpha 0.75",
