@@ -302,6 +302,20 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
 int sel_pt_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
                          void* stream);
 
+/* DeferredPathTracer::GenerateImage (Source/Applications/Selas/Source/DeferredPathTracer.h:20-21, the
+ * integrator main.cpp:121 runs): samplesPerPixel = m * m correlated multi-jittered samples per pixel (m = 4,
+ * SamplesPerPixelX_ x SamplesPerPixelY_, in the reference; samplesPerPixel must be a square, m <= 256), quad-light
+ * and background next-event estimation, balance-heuristic MIS against the background and Russian roulette
+ * from 7 tracked bounces.  The reference has no bounce limit: maxBounces caps the segments of a path (1..1024;
+ * sel_deferred_settings_defaults gives 64).  Writes the one framebuffer layer scaled by 1/spp (FrameBuffer_Scale,
+ * DeferredPathTracer.cpp:465) to out_rgb: [height][width][3] floats in host memory.  Accumulation is FP64. */
+int sel_deferred_settings_defaults(SelPtSettings* out);
+int sel_deferred_generate_image(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, float* out_rgb);
+/* Device form: adds the un-normalised FP64 sums into d_accum ([height][width][3] doubles in HBM) on `stream` and
+ * returns without waiting. */
+int sel_deferred_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
+                               void* stream);
+
 /* Autotuner (no reference counterpart).  Renders the given path-tracer workload (timed with CUDA events,
  * after one untimed render per configuration) over BVH layout and leaf size {8-wide quantised with 2, 3, 4
  * triangles per leaf; binary FP32}, wavefront capacity {1,048,576; 4,194,304; 8,388,608 paths} and traversal
@@ -355,24 +369,24 @@ int sel_vcm_render_device(SelScene scene, const SelCamera* camera, const SelVcmS
 /* ------------------------------------------------------------------------------------------------ */
 typedef struct SelServerTy* SelServer;
 
-enum { SEL_INTEGRATOR_PT = 0, SEL_INTEGRATOR_VCM = 1 };
+enum { SEL_INTEGRATOR_PT = 0, SEL_INTEGRATOR_VCM = 1, SEL_INTEGRATOR_DEFERRED = 2 };
 
 typedef struct SelServerConfig {
     uint64_t hbm_budget_bytes;  /* device bytes admitted jobs may hold (0: free HBM minus the reserve)  */
     uint64_t hbm_reserve_bytes; /* left free when hbm_budget_bytes is 0 (default 2 GiB)                */
     uint32_t max_jobs;          /* jobs admitted at once, 1..16 (default 16)                           */
     uint32_t paths_in_flight;   /* shared path-tracer wavefront capacity (default 4,194,304)           */
-    uint32_t max_bounces;       /* bounce rounds of a shared batch; path-tracer jobs may ask for at most
-                                   this many (default 8)                                               */
+    uint32_t max_bounces;       /* 1..64: path-tracer and deferred jobs may ask for at most this many
+                                   bounces (default 8); a batch runs the most its jobs ask for         */
     uint32_t reserved;
 } SelServerConfig;
 
 typedef struct SelJob {
     SelScene scene;             /* committed with SEL_BVH_WIDE8_Q8; must outlive the job               */
     SelCamera camera;
-    uint32_t integrator;        /* SEL_INTEGRATOR_PT or SEL_INTEGRATOR_VCM                              */
+    uint32_t integrator;        /* SEL_INTEGRATOR_PT, SEL_INTEGRATOR_VCM or SEL_INTEGRATOR_DEFERRED      */
     uint32_t reserved;
-    SelPtSettings pt;           /* used by SEL_INTEGRATOR_PT (pathsInFlight is ignored)                 */
+    SelPtSettings pt;           /* used by SEL_INTEGRATOR_PT and _DEFERRED (pathsInFlight is ignored)   */
     SelVcmSettings vcm;         /* used by SEL_INTEGRATOR_VCM                                           */
 } SelJob;
 
@@ -401,7 +415,7 @@ int sel_server_result_floats(const SelJob* job, size_t* out_floats);
 /* done = 1 when the job's result is in host memory. */
 int sel_server_poll(SelServer server, uint64_t job_id, int* out_done);
 /* Blocks until the job is done, copies its image (path tracer: the two layers [2][H][W][3] scaled by
- * 1/spp; VCM: [H][W][3], the mean over the passes) to out (out_floats >= the result size) and its
+ * 1/spp; deferred path tracer: [H][W][3] scaled by 1/spp; VCM: [H][W][3], the mean over the passes) to out (out_floats >= the result size) and its
  * statistics to stats (may be null), and forgets the job.  Returns the job's status. */
 int sel_server_wait(SelServer server, uint64_t job_id, float* out, size_t out_floats, SelJobStats* stats);
 int sel_server_stats(SelServer server, SelServerStats* out);

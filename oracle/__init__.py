@@ -36,6 +36,10 @@ def lib() -> ctypes.CDLL:
             "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
+            "oracle_deferred_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
+                                        ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_uint32, ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
+            "oracle_cmj": ([_i, _i, _i, _vp], None),
             "oracle_vcm_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_uint64, _i, _vp, _i, _vp, _i, _i, _vp], None),
@@ -141,6 +145,36 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
                        max_bounces, seed, 0 if rng == "pcg" else 1, nthreads or threads(), _p(rows), rows.shape[0],
                        _p(texels), int(physical_nee), _p(out))
     return out
+
+
+def deferred_render(render_scene, width, height, sample_begin, sample_end, samples_per_axis=4, max_bounces=64,
+                    seed=0x5E1A5000, nthreads=None, physical_nee=False, rng="pcg"):
+    """CPU oracle deferred path tracer (oracle_pt.cpp): FP64 per-pixel sums over correlated multi-jittered
+    samples [sample_begin, sample_end) of samples_per_axis^2 per pixel, shape (height, width, 3).  rng "pcg":
+    the GPU's streams; "mt": MT19937 per pixel as the reference's sampler."""
+    from selas_gb300.scenes import light_records, material_records
+    verts, prim, geom = render_scene.geometry.soup()
+    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    rows, texels = render_scene.ptex_tables(mats)
+    lights, sets = light_records(render_scene.lights)
+    bg = np.array(render_scene.background, np.float32)
+    c = render_scene.camera
+    cam = np.array(list(c["position"]) + list(c["look_at"]) + list(c["up"]) + [c["fov_degrees"]], np.float32)
+    out = np.zeros((height, width, 3), np.float64)
+    lib().oracle_deferred_render(_p(verts), _p(prim), _p(geom), verts.shape[0], _p(mats), mats.shape[0], _p(lights),
+                                 lights.shape[0], _p(sets), sets.shape[0], _p(bg), _p(cam), width, height,
+                                 samples_per_axis, sample_begin, sample_end, max_bounces, seed,
+                                 0 if rng == "pcg" else 1, nthreads or threads(),
+                                 _p(rows), rows.shape[0], _p(texels), int(physical_nee), _p(out))
+    return out
+
+
+def cmj(m, p, n=None):
+    """Correlated multi-jittered points s = 0..n-1 (default m * m) of an m x m pattern decorrelated by p."""
+    n = m * m if n is None else n
+    xy = np.zeros((n, 2), np.float32)
+    lib().oracle_cmj(m, p, n, _p(xy))
+    return xy
 
 
 def ptex_eval(faces, texels_u16, queries):

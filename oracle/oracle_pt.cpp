@@ -9,6 +9,11 @@
 //   RectangleLightSampler  Source/Core/GeometryLib/RectangulerLightSampler.cpp:17-97
 //   CalculateSurfaceParams Source/Core/Shading/SurfaceParameters.cpp:144-247 (no normals/tangents/uvs)
 //   Isotropic media        Source/Core/Shading/IsotropicScattering.cpp, VolumetricScattering.cpp
+// The deferred path tracer (Source/Applications/Selas/Source/DeferredPathTracer.cpp:61-148, 151-279,
+// 349-380, 433-472) is restated by deferred_path / oracle_deferred_render: 4 x 4 correlated multi-jittered
+// primary samples (Kensler 2013), quad-light next-event estimation with weight 1 and background sampling
+// with the balance heuristic, shadow rays from tnear 0, no bounce limit (paths end by Russian roulette from
+// 7 tracked bounces, or at a given cap), no participating media, one output layer.
 // Random numbers: either PCG32 with one stream per path (stream = pass * W * H + pixel, the sampling the
 // GPU path tracer uses) or MT19937 as the reference's CSampler draws them (Random.cpp:46-49), one engine
 // per pixel.  Each path's two layers are summed in float as the reference's Ld[] (PathTracer.cpp:144-257)
@@ -182,6 +187,38 @@ V3 offset(V3 p, V3 n, float err, V3 dir, float scale) {
     return p + (side * err * scale) * n;
 }
 
+// CalculateSurfaceParams (SurfaceParameters.cpp:144-247) for meshes without normals, tangents or uvs.
+struct SurfHit {
+    const Material* m;
+    float err;
+    orc::Surf s;
+    V3 n, view;
+};
+
+void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) {
+    const Material& m = sc.materials[h.geom < sc.materials.size() ? h.geom : 0];
+    o.m = &m;
+    o.err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(pos.x), std::fabs(pos.y)), std::max(std::fabs(pos.z), h.t));
+    orc::Surf& s = o.s;
+    const V3 n = orc::Norm(V3(h.ng[0], h.ng[1], h.ng[2]));
+    V3 t, b;
+    if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
+    else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
+    b = orc::Cross(n, t);
+    s.t = t; s.n = n; s.b = b;
+    float base[3] = {m.base[0], m.base[1], m.base[2]};
+    if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
+    s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
+    s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
+    s.specTrans = Sat(m.specTrans); s.diffTrans = m.diffTrans * 0.5f; s.flatness = m.flatness;
+    s.anisotropic = m.anisotropic; s.specularTint = m.specularTint; s.roughness = m.roughness;
+    s.metallic = Sat(m.metallic); s.scatterDistance = m.scatterDistance; s.ior = m.ior; s.shader = m.shader;
+    o.view = -1.0f * dir;
+    s.relativeIOR = ((m.flags & 1u) && orc::Dot(o.view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
+    o.n = n;
+}
+
 // EvaluatePath (PathTracer.cpp:142-258); returns both layers.
 void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounces, V3& ld0, V3& ld1) {
     ld0 = V3(0.0f);
@@ -214,26 +251,13 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
         if (phase == 1)
             thr = thr * V3(std::exp(-ext.x * ray_distance), std::exp(-ext.y * ray_distance), std::exp(-ext.z * ray_distance));
         if (hit) {
-            const Material& m = sc.materials[h.geom < sc.materials.size() ? h.geom : 0];
-            const float err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(pos.x), std::fabs(pos.y)),
-                                                              std::max(std::fabs(pos.z), h.t));
-            orc::Surf s;
-            const V3 n = orc::Norm(V3(h.ng[0], h.ng[1], h.ng[2]));
-            V3 t, b;
-            if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
-            else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
-            b = orc::Cross(n, t);
-            s.t = t; s.n = n; s.b = b;
-            float base[3] = {m.base[0], m.base[1], m.base[2]};
-            if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
-            s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
-            s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
-            s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
-            s.specTrans = Sat(m.specTrans); s.diffTrans = m.diffTrans * 0.5f; s.flatness = m.flatness;
-            s.anisotropic = m.anisotropic; s.specularTint = m.specularTint; s.roughness = m.roughness;
-            s.metallic = Sat(m.metallic); s.scatterDistance = m.scatterDistance; s.ior = m.ior; s.shader = m.shader;
-            const V3 view = -1.0f * dir;
-            s.relativeIOR = ((m.flags & 1u) && orc::Dot(view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
+            SurfHit sh;
+            surface_at(sc, h, pos, dir, sh);
+            const Material& m = *sh.m;
+            const float err = sh.err;
+            const orc::Surf& s = sh.s;
+            const V3 n = sh.n;
+            const V3 view = sh.view;
             // next-event estimation
             V3 ldir, lrad(0.0f);
             float ldist = 0, lpdf = 1;
@@ -293,25 +317,155 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
     }
 }
 
+// Correlated multi-jittered sampling: A. Kensler, "Correlated Multi-Jittered Sampling", Pixar Technical Memo
+// 13-01 (2013), the published hash constants and steps that Source/Core/MathLib/CorrelatedMultiJitter.cpp:12-62
+// uses.  cmj_permute is a bijection of [0, 2^k) walked until it lands below l (at most 2^k steps).
+uint32_t cmj_permute(uint32_t i, uint32_t l, uint32_t p) {
+    uint32_t w = l - 1;
+    for (int sh = 1; sh <= 16; sh <<= 1) w |= w >> sh;
+    do {
+        i ^= p;
+        i *= 0xe170893du;
+        i ^= p >> 16;
+        i ^= (i & w) >> 4;
+        i ^= p >> 8;
+        i *= 0x0929eb3fu;
+        i ^= p >> 23;
+        i ^= (i & w) >> 1;
+        i *= 1u | p >> 27;
+        i *= 0x6935fa69u;
+        i ^= (i & w) >> 11;
+        i *= 0x74dcb303u;
+        i ^= (i & w) >> 2;
+        i *= 0x9e501cc3u;
+        i ^= (i & w) >> 2;
+        i *= 0xc860a3dfu;
+        i &= w;
+        i ^= i >> 5;
+    } while (i >= l);
+    return (i + p) % l;
+}
+
+float cmj_float(uint32_t i, uint32_t p) {
+    i ^= p;
+    i ^= i >> 17;
+    i ^= i >> 10;
+    i *= 0xb36534e5u;
+    i ^= i >> 12;
+    i ^= i >> 21;
+    i *= 0x93fc4795u;
+    i ^= 0xdf6e307fu;
+    i ^= i >> 17;
+    i *= 1u | p >> 18;
+    return float(i) * (1.0f / 4294967808.0f);
+}
+
+// Sample s of an m x n pattern decorrelated by p: a point of [0,1)^2.
+void cmj(int32_t s, int32_t m, int32_t n, int32_t p, float& x, float& y) {
+    const uint32_t up = uint32_t(p);
+    const int32_t sx = int32_t(cmj_permute(uint32_t(s % m), uint32_t(m), up * 0xa511e9b3u));
+    const int32_t sy = int32_t(cmj_permute(uint32_t(s / m), uint32_t(n), up * 0x63d83595u));
+    const float jx = cmj_float(uint32_t(s), up * 0xa399d265u);
+    const float jy = cmj_float(uint32_t(s), up * 0x711ad6a5u);
+    x = (float(s % m) + (float(sy) + jx) / float(n)) / float(m);
+    y = (float(s / m) + (float(sx) + jy) / float(m)) / float(n);
+}
+
+void add(double* acc, V3 c) {
+    acc[0] += c.x;
+    acc[1] += c.y;
+    acc[2] += c.z;
+}
+
+// One path of the deferred path tracer (DeferredPathTracer.cpp:61-148 shading, 151-230 extension rays,
+// 234-279 shadow rays), contributions added to acc as the reference writes them one by one.  Per hit the
+// sampler gives: light pick + 2 for the light, 2 for the background direction (drawn whatever the
+// background), the BSDF's lobe + 2..3, and one for Russian roulette once 7 bounces are tracked.  The
+// reference has no bounce limit; max_bounces caps the segments of a path.
+void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounces, double* acc) {
+    const float kInv4Pi = 1.0f / (4.0f * kPi);
+    V3 thr(1.0f);
+    for (uint32_t bounce = 0; bounce < max_bounces; ++bounce) {
+        orq::Hit h;
+        const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
+        if (!orq::closest(sc.bvh, o, d, 0.0f, 3.402823466e+38f, h)) {
+            add(acc, sc.background * thr);
+            break;
+        }
+        const V3 pos(org.x + h.t * dir.x, org.y + h.t * dir.y, org.z + h.t * dir.z);
+        SurfHit sh;
+        surface_at(sc, h, pos, dir, sh);
+        const Material& m = *sh.m;
+        // quad light (NextEventEstimation), weight 1
+        V3 ldir, lrad(0.0f);
+        float ldist = 0, lpdf = 1;
+        if (m.light_set < sc.set_count.size() && sc.set_count[m.light_set] > 0) {
+            const uint32_t cnt = sc.set_count[m.light_set];
+            const float p0 = rng.uniform();
+            const uint32_t li = std::min(uint32_t(p0 * float(cnt)), cnt - 1);
+            const float u = rng.uniform(), v = rng.uniform();
+            sample_light(sc.lights[sc.set_first[m.light_set] + li], pos, sh.n, u, v, ldir, lrad, ldist, lpdf,
+                         sc.physical_nee);
+            lpdf *= 1.0f / float(cnt);
+        }
+        if (orc::Dot(lrad, V3(1.0f)) > 0) {
+            float fp, rp;
+            const V3 refl = orc::bsdf_evaluate(sh.s, sh.view, ldir, fp, rp);
+            const V3 sample = 1.0f * refl * lrad * (1.0f / lpdf);
+            if (orc::Dot(sample, V3(1.0f)) > 0) {
+                const V3 so = offset(pos, sh.n, sh.err, ldir, 0.1f);
+                const float soa[3] = {so.x, so.y, so.z}, lda[3] = {ldir.x, ldir.y, ldir.z};
+                if (!orq::occluded(sc.bvh, soa, lda, 0.0f, ldist)) add(acc, sample * thr);
+            }
+        }
+        // background (SampleBackground -> BackgroundLightSample, AreaLighting.cpp:334-350: uniform sphere
+        // direction, density recorded as 1), balance heuristic against the BSDF's density
+        const float r0 = rng.uniform(), r1 = rng.uniform();
+        const float uu = 2.0f * r1 - 1.0f;
+        const float nn = std::sqrt(std::max(0.0f, 1.0f - uu * uu));
+        const float th = 2.0f * kPi * r0;
+        const V3 sdir(nn * std::cos(th), uu, nn * std::sin(th));
+        if (orc::Dot(sc.background, V3(1.0f)) > 0) {
+            float fp, rp;
+            const V3 refl = orc::bsdf_evaluate(sh.s, sh.view, sdir, fp, rp);
+            const float mis = 1.0f / (1.0f + fp);
+            const V3 sample = mis * refl * sc.background * (1.0f / 1.0f);
+            if (orc::Dot(sample, V3(1.0f)) > 0) {
+                const V3 so = offset(pos, sh.n, sh.err, sdir, 0.1f);
+                const float soa[3] = {so.x, so.y, so.z}, sda[3] = {sdir.x, sdir.y, sdir.z};
+                if (!orq::occluded(sc.bvh, soa, sda, 0.0f, 1e36f)) add(acc, sample * thr);
+            }
+        }
+        // BSDF sample, weighted against the background density 1 / (4 pi)
+        float u4[4];
+        Rng ahead = rng;
+        for (int k = 0; k < 4; ++k) u4[k] = ahead.uniform();
+        int used = 0;
+        orc::Sample bs;
+        const bool ok = orc::bsdf_sample(sh.s, sh.view, u4, used, bs);
+        for (int k = 0; k < used; ++k) rng.uniform();
+        if (!ok) break;
+        const float mis = bs.fwd / (bs.fwd + kInv4Pi);
+        V3 t = mis * thr * bs.refl;
+        if (orc::Dot(t, t) == 0.0f) break;
+        if (bounce >= 7) {  // Russian roulette once MaxTrackedBounces_ = 7 bounces are tracked
+            const float cp = std::max(std::max(t.x, t.y), t.z);
+            if (rng.uniform() >= cp) break;
+            t = t * (1.0f / cp);
+        }
+        thr = t;
+        org = offset(pos, sh.n, sh.err, bs.wi, 1.0f);
+        dir = bs.wi;
+    }
+}
+
 }  // namespace
 
-extern "C" {
-
-// verts/prim/geom: triangle soup; materials: n_materials x 32 words (MaterialDev layout, indexed by geomID);
-// lights: n_lights x 15 floats (position, direction, x, z, radiance); sets: n_sets x 2 (first, count);
-// camera: position[3] lookAt[3] up[3] fovDegrees; ptex_rows/ptex_texels: the combined Ptex face table of
-// all textured geometries (material word 3 = that geometry's first face); out: [2][height][width][3]
-// doubles (sums over the paths of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the
-// GPU); 1: MT19937 per pixel.  physical_nee drops the extra cos(theta_surface) factor that the reference's
-// SampleRectangleLightSolidAngle puts into the NEE radiance (AreaLighting.cpp:140-146), giving the
-// physically correct estimator that other integrators (VCM) converge to.
-void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
-                      const float* materials, int n_materials, const float* lights, int n_lights,
-                      const uint32_t* sets, int n_sets, const float* background, const float* camera,
-                      uint32_t width, uint32_t height, uint32_t pass_begin, uint32_t pass_end, uint32_t max_bounces,
-                      uint64_t seed, int rng_mode, int threads, const int32_t* ptex_rows, int ptex_faces,
-                      const uint16_t* ptex_texels, int physical_nee, double* out) {
-    Scene sc;
+// Scene tables of the oracle renderers' common arguments; returns the Ptex texture to delete.
+static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
+                         const float* materials, int n_materials, const float* lights, int n_lights,
+                         const uint32_t* sets, int n_sets, const float* background, const int32_t* ptex_rows,
+                         int ptex_faces, const uint16_t* ptex_texels, int physical_nee) {
     sc.physical_nee = physical_nee != 0;
     sc.bvh = orq::build(verts, prim, geom, ntri);
     orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
@@ -332,6 +486,28 @@ void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* 
         sc.set_count.push_back(sets[2 * i + 1]);
     }
     sc.background = V3(background[0], background[1], background[2]);
+    return tex;
+}
+
+extern "C" {
+
+// verts/prim/geom: triangle soup; materials: n_materials x 32 words (MaterialDev layout, indexed by geomID);
+// lights: n_lights x 15 floats (position, direction, x, z, radiance); sets: n_sets x 2 (first, count);
+// camera: position[3] lookAt[3] up[3] fovDegrees; ptex_rows/ptex_texels: the combined Ptex face table of
+// all textured geometries (material word 3 = that geometry's first face); out: [2][height][width][3]
+// doubles (sums over the paths of passes [pass_begin, pass_end)).  rng_mode 0: PCG32 streams (as the
+// GPU); 1: MT19937 per pixel.  physical_nee drops the extra cos(theta_surface) factor that the reference's
+// SampleRectangleLightSolidAngle puts into the NEE radiance (AreaLighting.cpp:140-146), giving the
+// physically correct estimator that other integrators (VCM) converge to.
+void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
+                      const float* materials, int n_materials, const float* lights, int n_lights,
+                      const uint32_t* sets, int n_sets, const float* background, const float* camera,
+                      uint32_t width, uint32_t height, uint32_t pass_begin, uint32_t pass_end, uint32_t max_bounces,
+                      uint64_t seed, int rng_mode, int threads, const int32_t* ptex_rows, int ptex_faces,
+                      const uint16_t* ptex_texels, int physical_nee, double* out) {
+    Scene sc;
+    orp::Texture* tex = load_scene(sc, verts, prim, geom, ntri, materials, n_materials, lights, n_lights, sets, n_sets,
+                                   background, ptex_rows, ptex_faces, ptex_texels, physical_nee);
     const Camera cam = make_camera(camera, width, height);
     const uint32_t npix = width * height;
     std::atomic<uint32_t> next{0};
@@ -372,6 +548,70 @@ void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* 
     for (auto& th : pool) th.join();
     orq::release(const_cast<void*>(sc.bvh));
     delete tex;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// DeferredPathTracer::GenerateImage (DeferredPathTracer.cpp:433-472) over samples [sample_begin, sample_end) of
+// each pixel's samples_per_axis^2 correlated multi-jittered samples (SamplesPerPixelX_ = SamplesPerPixelY_ = 4
+// in the reference; sample s of pixel p jitters by CorrelatedMultiJitter(s, m, m, p), Camera.cpp:77-86).
+// rng_mode 0: PCG32 stream s * width * height + p per path (as the GPU); 1: one MT19937 engine per pixel
+// seeded seed + p, drawn as the reference's CSampler (Random.cpp:46-49) over the pixel's samples in order.
+// Arguments as oracle_pt_render; out: [height][width][3]
+// doubles, the un-normalised sums (the reference scales by 1 / (m * m)).
+void oracle_deferred_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
+                            const float* materials, int n_materials, const float* lights, int n_lights,
+                            const uint32_t* sets, int n_sets, const float* background, const float* camera,
+                            uint32_t width, uint32_t height, uint32_t samples_per_axis, uint32_t sample_begin,
+                            uint32_t sample_end, uint32_t max_bounces, uint64_t seed, int rng_mode, int threads,
+                            const int32_t* ptex_rows, int ptex_faces, const uint16_t* ptex_texels, int physical_nee,
+                            double* out) {
+    Scene sc;
+    orp::Texture* tex = load_scene(sc, verts, prim, geom, ntri, materials, n_materials, lights, n_lights, sets, n_sets,
+                                   background, ptex_rows, ptex_faces, ptex_texels, physical_nee);
+    const Camera cam = make_camera(camera, width, height);
+    const uint32_t npix = width * height;
+    const int32_t m = int32_t(samples_per_axis);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const uint32_t pix0 = next.fetch_add(16);
+            if (pix0 >= npix) break;
+            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
+                const uint32_t y = pixel / width, x = pixel - y * width;
+                double acc[3] = {0, 0, 0};
+                Rng rng;
+                if (rng_mode == 1) {
+                    rng.pcg = false;
+                    rng.mt.seed(uint32_t(seed) + pixel);
+                }
+                for (uint32_t smp = sample_begin; smp < sample_end; ++smp) {
+                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(smp) * npix + pixel);
+                    float jx, jy;
+                    cmj(int32_t(smp), m, m, int32_t(pixel), jx, jy);
+                    const float vx = float(x) + jx, vy = float(y) + jy;
+                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
+                    const float cy = 1.0f - 2.0f * vy / cam.h;
+                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
+                    deferred_path(sc, rng, cam.pos, d, max_bounces, acc);
+                }
+                for (int c = 0; c < 3; ++c) out[size_t(pixel) * 3 + c] += acc[c];
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    const int nt = std::max(1, threads);
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+    orq::release(const_cast<void*>(sc.bvh));
+    delete tex;
+}
+
+// Correlated multi-jittered sample points (for tests): n samples s = 0..n-1 of an m x m pattern with p.
+void oracle_cmj(int32_t m, int32_t p, int32_t n, float* xy) {
+    for (int32_t s = 0; s < n; ++s) cmj(s, m, m, p, xy[2 * s], xy[2 * s + 1]);
 }
 
 }  // extern "C"

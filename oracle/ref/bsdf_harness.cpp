@@ -11,7 +11,10 @@
 // Surface records are 32 floats: t[3] n[3] b[3] baseColor[3] transmittanceColor[3] sheen sheenTint
 // clearcoat clearcoatGloss metallic specTrans diffTrans flatness anisotropic relativeIOR specularTint
 // roughness scatterDistance ior shader(as float) pad pad.
+//
+// ref_cmj exposes CorrelatedMultiJitter (Source/Core/MathLib/CorrelatedMultiJitter.cpp:53-62), reference code.
 
+#include "MathLib/CorrelatedMultiJitter.h"
 #include "MathLib/FloatFuncs.h"
 #include "MathLib/Sampler.h"
 #include "Shading/Scattering.h"
@@ -113,6 +116,15 @@ void ref_bsdf_sample(const float* surf, const float* wo, const float* u, int n, 
         o[13] = bs.medium.extinction.z;
         o[14] = float(g_used);
         o[15] = 0.0f;
+    }
+}
+
+// xy: n points s = 0..n-1 of CorrelatedMultiJitter(s, m, m, p)
+void ref_cmj(int m, int p, int n, float* xy) {
+    for (int s = 0; s < n; ++s) {
+        const float2 r = CorrelatedMultiJitter(s, m, m, p);
+        xy[2 * s] = r.x;
+        xy[2 * s + 1] = r.y;
     }
 }
 

@@ -6,7 +6,8 @@ are git-ignored.  Only the machine that has the checkout builds these, to genera
 under tests/golden/ (tests/golden/make_golden.py).
 
   libref_bsdf.so  - Source/Core/Shading/{Disney,Ggx,Fresnel,SurfaceScattering,Lambert,DiracTransparent}.cpp
-                    + Source/Core/MathLib/{FloatFuncs,FloatStructs,Trigonometric}.cpp + bsdf_harness.cpp
+                    + Source/Core/MathLib/{FloatFuncs,FloatStructs,Trigonometric,CorrelatedMultiJitter}.cpp
+                    + bsdf_harness.cpp
   libref_ptex.so  - Middleware/ptex/Include/Ptex*.cpp (vendored Ptex 2.2, minus the half-table generator)
                     + ptex_harness.cpp, linked with the system zlib
 """
@@ -48,7 +49,8 @@ def build_bsdf(force=False):
     core = REFERENCE / "Source" / "Core"
     srcs = [core / "Shading" / f"{n}.cpp" for n in ("Disney", "Ggx", "Fresnel", "SurfaceScattering", "Lambert",
                                                      "DiracTransparent")]
-    srcs += [core / "MathLib" / f"{n}.cpp" for n in ("FloatFuncs", "FloatStructs", "Trigonometric")]
+    srcs += [core / "MathLib" / f"{n}.cpp" for n in ("FloatFuncs", "FloatStructs", "Trigonometric",
+                                                     "CorrelatedMultiJitter")]
     srcs += [HERE / "bsdf_harness.cpp"]
     inc = [f"-I{core}", f"-I{REFERENCE / 'Middleware'}", f"-I{REFERENCE / 'Middleware' / 'embree-latest' / 'include'}"]
     objs = _compile(srcs, SELAS_FLAGS + inc, OUT / "obj_bsdf")

@@ -268,6 +268,9 @@ register_signatures({
     "sel_scene_set_build_mode": [_vp, ctypes.c_int],
     "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
     "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
+    "sel_deferred_settings_defaults": [ctypes.POINTER(SelPtSettings)],
+    "sel_deferred_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
+    "sel_deferred_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
 })
 
 
@@ -296,6 +299,16 @@ def camera(position, look_at, up, fov_degrees, width, height) -> SelCamera:
 def pt_settings(spp, max_bounces=8, seed=0x5E1A5000, paths_in_flight=0) -> SelPtSettings:
     s = SelPtSettings()
     s.samplesPerPixel, s.maxBounces, s.seed, s.pathsInFlight = spp, max_bounces, seed, paths_in_flight
+    return s
+
+
+def deferred_settings(samples_per_axis=4, max_bounces=64, seed=0x5E1A5000, paths_in_flight=0) -> SelPtSettings:
+    """SelPtSettings of the deferred path tracer: samples_per_axis^2 correlated multi-jittered samples per
+    pixel (4 x 4 in the reference), at most max_bounces segments per path."""
+    s = SelPtSettings()
+    check(lib().sel_deferred_settings_defaults(ctypes.byref(s)))
+    s.samplesPerPixel, s.maxBounces = samples_per_axis * samples_per_axis, max_bounces
+    s.seed, s.pathsInFlight = seed, paths_in_flight
     return s
 
 
@@ -332,6 +345,13 @@ def _scene_pt_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> n
     return out
 
 
+def _scene_deferred_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> np.ndarray:
+    """DeferredPathTracer::GenerateImage: (height, width, 3) float32, scaled by 1/spp."""
+    out = np.zeros((cam.height, cam.width, 3), np.float32)
+    check(lib().sel_deferred_generate_image(self.handle, ctypes.byref(cam), ctypes.byref(settings), out.ctypes.data))
+    return out
+
+
 def _scene_vcm_generate_image(self, cam: SelCamera, settings: SelVcmSettings) -> np.ndarray:
     """VCM::GenerateImage: (height, width, 3) float32, the mean over the passes."""
     out = np.zeros((cam.height, cam.width, 3), np.float32)
@@ -352,12 +372,13 @@ Scene.add_quad_light = _scene_add_quad_light
 Scene.set_background = _scene_set_background
 Scene.pt_generate_image = _scene_pt_generate_image
 Scene.vcm_generate_image = _scene_vcm_generate_image
+Scene.deferred_generate_image = _scene_deferred_generate_image
 
 
 # ---------------------------------------------------------------------------------------------------
 # Render server (include/selas.h: sel_server_*)
 # ---------------------------------------------------------------------------------------------------
-SEL_INTEGRATOR_PT, SEL_INTEGRATOR_VCM = 0, 1
+SEL_INTEGRATOR_PT, SEL_INTEGRATOR_VCM, SEL_INTEGRATOR_DEFERRED = 0, 1, 2
 
 
 class SelServerConfig(ctypes.Structure):
@@ -404,6 +425,12 @@ def server_config(**kw) -> SelServerConfig:
 def pt_job(scene, cam: SelCamera, settings: SelPtSettings) -> SelJob:
     j = SelJob()
     j.scene, j.camera, j.integrator, j.pt = scene.handle, cam, SEL_INTEGRATOR_PT, settings
+    return j
+
+
+def deferred_job(scene, cam: SelCamera, settings: SelPtSettings) -> SelJob:
+    j = SelJob()
+    j.scene, j.camera, j.integrator, j.pt = scene.handle, cam, SEL_INTEGRATOR_DEFERRED, settings
     return j
 
 

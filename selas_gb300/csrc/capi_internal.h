@@ -78,6 +78,9 @@ float vcm_default_radius(const SelSceneTy* sc);
 void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c);
 void vcm_lights(const SelSceneTy* sc, VcmSettings& set);
 int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
+// Deferred path tracer: check_render_args plus samplesPerPixel = m * m (m <= 256) and maxBounces 1..1024.
+int check_deferred_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
+uint32_t deferred_axis(const SelPtSettings& settings);
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings);
 void init_camera(const SelCamera& c, PtCamera& out);
 int fail(int code, const std::string& msg);

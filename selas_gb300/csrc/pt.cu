@@ -14,11 +14,20 @@
 // global path index), consumed in the order the reference consumes its sampler: jitter x/y; per bounce
 // [distance in a medium: 2], light pick + 2 for the light, BSDF lobe + 2..3, [medium scatter: 2],
 // [Russian roulette after bounce 8: 1].
+//
+// A job may instead run the deferred path tracer (DeferredPathTracer.cpp:61-148, 151-279, 349-380): sample s of
+// pixel p jitters by the correlated multi-jittered point cmj_point(s, m, m, p) (path index s * W * H + p, no
+// draws), and per hit the stream gives light pick + 2, 2 for a background direction (drawn whatever the
+// background), BSDF lobe + 2..3 and, from the 7th bounce on, one for Russian roulette.  Its shading emits up to
+// two shadow rays (quad light with weight 1; background with the balance heuristic), both from tnear 0, and
+// weights the BSDF continuation by the balance heuristic against the background density 1 / (4 pi).  Such a
+// job accumulates one layer (radiance).
 #include "pt.h"
 
 #include <cstring>
 
 #include "capi_internal.h"
+#include "cmj.cuh"
 #include "graph.h"
 #include "ptex.cuh"
 #include "shading.cuh"
@@ -129,8 +138,16 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
         const uint32_t pixel = uint32_t(path % npix);
         Pcg32 rng = pcg_seed(J.seed, path);
         const uint32_t y = pixel / width, x = pixel - y * width;
-        const float vx = float(x) + pcg_float(rng);  // JitteredCameraRay (Camera.cpp:63-74)
-        const float vy = float(y) + pcg_float(rng);
+        float vx, vy;
+        if (J.mode == kPtModeDeferred) {  // JitteredCameraRay(camera, x, y, s, m, m, index) (Camera.cpp:77-86)
+            const int32_t m = int32_t(J.samples_per_axis);
+            const float2 j = cmj_point(int32_t(path / npix), m, m, int32_t(pixel));
+            vx = float(x) + j.x;
+            vy = float(y) + j.y;
+        } else {  // JitteredCameraRay (Camera.cpp:63-74)
+            vx = float(x) + pcg_float(rng);
+            vy = float(y) + pcg_float(rng);
+        }
         const CameraDev cam = camera_of(J.cam);
         const float3 d = camera_direction(cam, vx, vy);
         P.st.ray_o[s] = make_float4(cam.position.x, cam.position.y, cam.position.z, 0.0f);
@@ -275,21 +292,26 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
     if (status) atomicOr(P.err, status);
 }
 
+// kModes: bit 0 path-tracer jobs, bit 1 deferred jobs in the batch (a single-mode batch compiles the other
+// integrator out of the kernel).
+template <uint32_t kModes>
 __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     const int next = cur ^ 1;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
         const bool valid = e < n;
-        bool cont = false, shadow = false;
+        bool cont = false, shadow = false, shadow2 = false;
         uint32_t s = 0;
         float4 sh_o = make_float4(0, 0, 0, 0), sh_d = sh_o, sh_c = sh_o;
+        float4 sh2_o = sh_o, sh2_d = sh_o, sh2_c = sh_o;  // deferred: the background's shadow ray
         if (valid) {
             s = in_queue[e];
             const uint32_t job = P.st.job[s];
             const PtJob& J = P.st.jobs[job];
             const PtScene& S = J.scene;
             const uint32_t npix = J.cam.width * J.cam.height;
+            const bool deferred = kModes == 2u || (kModes == 3u && J.mode == kPtModeDeferred);
             const float4 o4 = P.st.ray_o[s], d4 = P.st.ray_d[s];
             const float3 o = f3(o4.x, o4.y, o4.z), d = f3(d4.x, d4.y, d4.z);
             float4 thr4 = P.st.thr[s];
@@ -338,17 +360,54 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                         ls.pdf *= 1.0f / float(set.y);
                     }
                 }
+                const uint32_t tag = (job << 28) | pixel;
                 if (dot(ls.radiance, f3(1.0f)) > 0.0f) {
                     float fpdf, rpdf;
                     const float3 refl = bsdf_evaluate(sf, -d, ls.direction, fpdf, rpdf);
-                    if (dot(refl, f3(1.0f)) > 0.0f) {
+                    if (deferred) {
+                        // weight 1 (DeferredPathTracer.cpp:65-88); the shadow ray starts at tnear 0
+                        const float3 smp = 1.0f * refl * ls.radiance * (1.0f / ls.pdf);
+                        if (dot(smp, f3(1.0f)) > 0.0f) {
+                            const float3 so = offset_origin(pos, sf.n, err, ls.direction, 0.1f);
+                            const float3 c = smp * thr;
+                            sh_o = make_float4(so.x, so.y, so.z, 0.0f);
+                            sh_d = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.distance);
+                            sh_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
+                            shadow = true;
+                        }
+                    } else if (dot(refl, f3(1.0f)) > 0.0f) {
                         // OcclusionRay (PathTracer.cpp:71-92): origin offset 0.1 * error, tnear = error
                         const float3 so = offset_origin(pos, sf.n, err, ls.direction, 0.1f);
                         const float3 c = refl * ls.radiance * (1.0f / ls.pdf) * thr;
                         sh_o = make_float4(so.x, so.y, so.z, err);
                         sh_d = make_float4(ls.direction.x, ls.direction.y, ls.direction.z, ls.distance);
-                        sh_c = make_float4(c.x, c.y, c.z, __uint_as_float((job << 28) | pixel));
+                        sh_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
                         shadow = true;
+                    }
+                }
+                if (deferred) {
+                    // SampleBackground -> BackgroundLightSample (AreaLighting.cpp:334-350): a uniform sphere
+                    // direction whose density is recorded as 1, at distance 1e36; balance heuristic against the
+                    // BSDF's density (DeferredPathTracer.cpp:90-111)
+                    const float r0 = pcg_float(rng), r1 = pcg_float(rng);
+                    const float uu = 2.0f * r1 - 1.0f;
+                    const float nn = sqrtf(fmaxf(0.0f, 1.0f - uu * uu));
+                    const float th = kTwoPi * r0;
+                    const float3 sdir = f3(nn * cosf(th), uu, nn * sinf(th));
+                    const float3 bg = f3(S.background[0], S.background[1], S.background[2]);
+                    if (dot(bg, f3(1.0f)) > 0.0f) {
+                        float fpdf, rpdf;
+                        const float3 refl = bsdf_evaluate(sf, -d, sdir, fpdf, rpdf);
+                        const float mis = (1.0f * 1.0f) / (1.0f * 1.0f + 1.0f * fpdf);
+                        const float3 smp = mis * refl * bg * (1.0f / 1.0f);
+                        if (dot(smp, f3(1.0f)) > 0.0f) {
+                            const float3 so = offset_origin(pos, sf.n, err, sdir, 0.1f);
+                            const float3 c = smp * thr;
+                            sh2_o = make_float4(so.x, so.y, so.z, 0.0f);
+                            sh2_d = make_float4(sdir.x, sdir.y, sdir.z, 1e36f);
+                            sh2_c = make_float4(c.x, c.y, c.z, __uint_as_float(tag));
+                            shadow2 = true;
+                        }
                     }
                 }
                 // BSDF sampling: draw ahead from a copy of the stream, then advance by what was used
@@ -361,6 +420,18 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 for (int k = 0; k < used; ++k) pcg_next(rng);
                 if (!ok) {
                     alive = false;
+                } else if (deferred) {
+                    // balance heuristic against the background density (BackgroundLightingPdf = 1 / (4 pi))
+                    const float mis = (1.0f * bs.forward_pdf) / (1.0f * bs.forward_pdf + 1.0f * kInv4Pi);
+                    const float3 t = mis * thr * bs.reflectance;
+                    if (dot(t, t) == 0.0f) {
+                        alive = false;
+                    } else {
+                        thr = t;
+                        const float3 no = offset_origin(pos, sf.n, err, bs.wi, 1.0f);
+                        P.st.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
+                        P.st.ray_d[s] = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, kFloatMax);
+                    }
                 } else {
                     if (!(bs.flags & kDiracEvent)) thr4.w = 0.0f;
                     if (bs.flags == kTransmissionEvent) {
@@ -373,7 +444,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                     P.st.ray_d[s] = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, kFloatMax);
                     if (bounce == 0) accumulate(J.accum, npix, 0, pixel, bs.reflectance);
                 }
-            } else if (med.x != 0.0f) {
+            } else if (!deferred && med.x != 0.0f) {
                 // scatter inside the medium: Isotropic::SampleScatterDirection -> CSampler::UniformSphere
                 const float3 no = o + ray_distance * d;
                 const float r0 = pcg_float(rng), r1 = pcg_float(rng);
@@ -385,12 +456,19 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 P.st.ray_d[s] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
             } else {
                 // miss: background (EvaluateBackground / EvaluateBackgroundMiss without an IBL)
-                accumulate(J.accum, npix, 1, pixel, f3(S.background[0], S.background[1], S.background[2]) * thr);
+                accumulate(J.accum, npix, deferred ? 0 : 1, pixel,
+                           f3(S.background[0], S.background[1], S.background[2]) * thr);
                 alive = false;
             }
             if (alive) {
                 const uint32_t nb = bounce + 1;
-                if (nb > 8) {  // Russian roulette (PathTracer.cpp:248-254)
+                if (deferred) {
+                    if (bounce >= 7) {  // Russian roulette once MaxTrackedBounces_ = 7 are tracked
+                        const float cp = fmaxf(fmaxf(thr.x, thr.y), thr.z);
+                        if (pcg_float(rng) >= cp) alive = false;
+                        else thr = thr * (1.0f / cp);
+                    }
+                } else if (nb > 8) {  // Russian roulette (PathTracer.cpp:248-254)
                     const float cp = fmaxf(fmaxf(thr.x, thr.y), thr.z);
                     if (pcg_float(rng) > cp) alive = false;
                     else thr = thr * (1.0f / cp);
@@ -408,6 +486,14 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
             P.st.sh_o[sslot] = sh_o;
             P.st.sh_d[sslot] = sh_d;
             P.st.sh_c[sslot] = sh_c;
+        }
+        if ((kModes & 2u) && __any_sync(0xffffffffu, shadow2)) {  // the queue holds 2 records per path
+            const uint32_t s2 = warp_append(&P.st.counters[2], shadow2);
+            if (shadow2) {
+                P.st.sh_o[s2] = sh2_o;
+                P.st.sh_d[s2] = sh2_d;
+                P.st.sh_c[s2] = sh2_c;
+            }
         }
     }
 }
@@ -435,7 +521,8 @@ __global__ void __launch_bounds__(B, 1024 / B) k_shadow(PtParams P) {
             QueryHit h;
             if (!Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, B,
                                                  status))
-                accumulate(J.accum, J.cam.width * J.cam.height, 1, tag & 0x0fffffffu, f3(c.x, c.y, c.z));
+                accumulate(J.accum, J.cam.width * J.cam.height, J.mode == kPtModeDeferred ? 0 : 1, tag & 0x0fffffffu,
+                           f3(c.x, c.y, c.z));
         }
     }
     if (status) atomicOr(P.err, status);
@@ -468,9 +555,9 @@ void pt_layout(PtState& st, Take take, uint32_t paths) {
     st.queue_sorted = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.cls = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.base = reinterpret_cast<float4*>(take(16ull * paths));
-    st.sh_o = reinterpret_cast<float4*>(take(16ull * paths));
-    st.sh_d = reinterpret_cast<float4*>(take(16ull * paths));
-    st.sh_c = reinterpret_cast<float4*>(take(16ull * paths));
+    st.sh_o = reinterpret_cast<float4*>(take(32ull * paths));
+    st.sh_d = reinterpret_cast<float4*>(take(32ull * paths));
+    st.sh_c = reinterpret_cast<float4*>(take(32ull * paths));
     st.counters = reinterpret_cast<uint32_t*>(take(64 * sizeof(uint32_t)));
     st.rays = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
     st.control = reinterpret_cast<PtControl*>(take(sizeof(PtControl)));
@@ -501,7 +588,7 @@ size_t pt_state_block_bytes(uint32_t paths) {
 }
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
-                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block) {
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes) {
     // 256-thread traversal blocks only for the 8-wide layout (its 24-entry stack then fills the 48 KB of
     // static shared memory; the binary layout's 64-entry stack would not fit)
     const int tb = (trace_block == 256 && bvh_kind == 0) ? 256 : 128;
@@ -531,7 +618,10 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
                 k_class_scatter<<<shade_grid, kBlock, 0, s>>>(P, cur);
                 k_texture<<<shade_grid, kBlock, 0, s>>>(P, cur);
             }
-            k_shade<<<shade_grid, kBlock, 0, s>>>(P, cur, b, sort ? st.queue_sorted : st.queue[cur]);
+            const uint32_t* q = sort ? st.queue_sorted : st.queue[cur];
+            if (modes == 2u) k_shade<2><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+            else if (modes == 3u) k_shade<3><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+            else k_shade<1><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
             if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0) k_shadow<0, 128><<<trace_grid, tb, 0, s>>>(P);
             else k_shadow<1, 128><<<trace_grid, tb, 0, s>>>(P);
@@ -543,6 +633,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
+        uint32_t modes;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -551,6 +642,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.bounces = bounces;
     key.sort = sort ? 1u : 0u;
     key.tb = tb;
+    key.modes = modes;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -561,6 +653,8 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     job.scene = sc;
     job.cam = cam;
     job.max_bounces = set.max_bounces;
+    job.mode = set.mode;
+    job.samples_per_axis = set.samples_per_axis;
     job.seed = set.seed;
     job.total = uint64_t(cam.width) * cam.height * set.spp;
     job.accum = d_accum;
@@ -573,7 +667,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     if (e != cudaSuccess) return e;
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
-                          trace_block);
+                          trace_block, set.mode == kPtModeDeferred ? 2u : 1u);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

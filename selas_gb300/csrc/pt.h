@@ -42,10 +42,15 @@ struct PtCamera {
     uint32_t width, height;
 };
 
+// Integrator of a job: PathTracer::EvaluatePath, or DeferredPathTracer (DeferredPathTracer.cpp:61-148).
+enum : uint32_t { kPtModePath = 0, kPtModeDeferred = 1 };
+
 struct PtSettings {
-    uint32_t spp;
-    uint32_t max_bounces;
+    uint32_t spp;          // kPtModeDeferred: samples_per_axis^2
+    uint32_t max_bounces;  // kPtModeDeferred: cap on path segments (the reference has none)
     uint64_t seed;
+    uint32_t mode;
+    uint32_t samples_per_axis;  // kPtModeDeferred: correlated multi-jittered pattern m x m
 };
 
 // One render job of the shared wavefront (an entry of the device-resident job table).
@@ -53,10 +58,12 @@ struct PtJob {
     PtScene scene;
     PtCamera cam;
     uint32_t max_bounces;
+    uint32_t mode;              // kPtModePath / kPtModeDeferred
+    uint32_t samples_per_axis;  // kPtModeDeferred
     uint32_t pad;
     uint64_t seed;
     uint64_t total;  // paths of the job: width * height * spp
-    double* accum;   // [2][height][width][3]
+    double* accum;   // kPtModePath: [2][height][width][3]; kPtModeDeferred: [height][width][3]
 };
 
 // Device-resident batch control: which paths of each job the next batch takes.  The host writes `next`
@@ -85,7 +92,7 @@ struct PtState {
     uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort)
     uint32_t* cls;    // material class of each current queue entry
     float4* base;     // Ptex base colour (authored, before the 2.2 power) of the path's current hit
-    float4* sh_o;     // shadow rays: origin, tnear
+    float4* sh_o;     // shadow rays (2 per path slot): origin, tnear
     float4* sh_d;     // direction, tfar
     float4* sh_c;     // contribution, (job << 28 | pixel) bits
     uint32_t* counters;
@@ -104,10 +111,13 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // `sort`: order each bounce's queue by material class and filter Ptex in a kernel of its own before shading
 // (required when a job's scene uses Ptex).
 // `trace_block`: threads per block of the traversal kernels (128, or 256 with the 8-wide layout).
+// `modes`: integrators of the jobs, bit 0 kPtModePath, bit 1 kPtModeDeferred.
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
-                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128);
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128,
+                           uint32_t modes = 1u);
 
-// Single render (PathTracer::GenerateImage): one job, batches until all its paths are done.
+// Single render (PathTracer::GenerateImage, or DeferredPathTracer::GenerateImage with set.mode =
+// kPtModeDeferred): one job, batches until all its paths are done.
 cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& set, const PtState& st, double* d_accum,
                       uint32_t* d_err, cudaStream_t stream, GraphCache* graphs, int trace_block = 128);
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream);

@@ -157,6 +157,22 @@ int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettin
     return SEL_OK;
 }
 
+// Samples per axis of a deferred render (samplesPerPixel = m * m), or 0 when the settings are invalid.
+uint32_t deferred_axis(const SelPtSettings& settings) {
+    uint32_t m = 1;
+    while (m * m < settings.samplesPerPixel && m < 256) ++m;
+    return m * m == settings.samplesPerPixel ? m : 0u;
+}
+
+int check_deferred_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings) {
+    if (int rc = check_render_args(scene, camera, settings)) return rc;
+    if (deferred_axis(*settings) == 0)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "samplesPerPixel must be m * m with 1 <= m <= 256");
+    if (settings->maxBounces == 0 || settings->maxBounces > 1024)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "maxBounces must lie in 1..1024");
+    return SEL_OK;
+}
+
 }  // namespace sel
 
 namespace {
@@ -223,7 +239,7 @@ void vcm_lights(const SelSceneTy* sc, VcmSettings& set) {
 namespace {
 
 int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& settings, double* d_accum,
-                  cudaStream_t stream) {
+                  cudaStream_t stream, uint32_t mode = kPtModePath) {
     if (int rc = sync_shading(sc)) return rc;
     const uint64_t total = uint64_t(camera.width) * camera.height * settings.samplesPerPixel;
     uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight
@@ -237,6 +253,8 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     set.spp = settings.samplesPerPixel;
     set.max_bounces = settings.maxBounces;
     set.seed = settings.seed;
+    set.mode = mode;
+    set.samples_per_axis = mode == kPtModeDeferred ? deferred_axis(settings) : 0u;
     const PtState st = pt_state_carve(sc->pt_block, cap);
     const int block = int(settings.traceBlockSize ? settings.traceBlockSize
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
@@ -465,6 +483,56 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
     if (e == cudaSuccess) e = cudaMemcpyAsync(out_layers, res, size_t(values) * sizeof(float), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "path tracer");
+    return read_error_word(dev, s);
+}
+
+int sel_deferred_settings_defaults(SelPtSettings* out) {
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    std::memset(out, 0, sizeof(*out));
+    out->samplesPerPixel = 16;  // SamplesPerPixelX_ x SamplesPerPixelY_ (DeferredPathTracer.cpp:40-41)
+    out->maxBounces = 64;
+    out->seed = 1;
+    return SEL_OK;
+}
+
+int sel_deferred_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
+                               void* stream) {
+    if (int rc = check_deferred_args(scene, camera, settings)) return rc;
+    if (!d_accum || (reinterpret_cast<uintptr_t>(d_accum) & 7u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_accum must be an 8-byte aligned device pointer");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    return render_device(scene, *camera, *settings, d_accum, static_cast<cudaStream_t>(stream), kPtModeDeferred);
+}
+
+int sel_deferred_generate_image(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, float* out_rgb) {
+    if (int rc = check_deferred_args(scene, camera, settings)) return rc;
+    if (!out_rgb) return fail(SEL_ERR_INVALID_ARGUMENT, "out_rgb is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    SelDeviceTy* dev = scene->dev;
+    std::lock_guard<std::mutex> dlock(dev->mu);
+    cudaStream_t s = dev->stream;
+    const uint32_t values = camera->width * camera->height * 3u;
+    const size_t accum_bytes = size_t(values) * sizeof(double);
+    const size_t need = accum_bytes + size_t(values) * sizeof(float);
+    if (scene->accum_bytes < need) {
+        if (scene->d_accum) cudaFree(scene->d_accum);
+        scene->d_accum = nullptr;
+        scene->accum_bytes = 0;
+        cudaError_t e = cudaMalloc(&scene->d_accum, need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(accumulator)");
+        scene->accum_bytes = need;
+    }
+    double* acc = static_cast<double*>(scene->d_accum);
+    float* res = reinterpret_cast<float*>(static_cast<char*>(scene->d_accum) + accum_bytes);
+    cudaError_t e = cudaMemsetAsync(acc, 0, accum_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(accumulator)");
+    if (int rc = render_device(scene, *camera, *settings, acc, s, kPtModeDeferred)) return rc;
+    e = pt_resolve(acc, values, 1.0 / double(settings->samplesPerPixel), res, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_rgb, res, size_t(values) * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "deferred path tracer");
     return read_error_word(dev, s);
 }
 

@@ -76,7 +76,7 @@ struct Job {
 
 size_t result_floats(const SelJob& j) {
     const size_t px = size_t(j.camera.width) * j.camera.height;
-    return j.integrator == SEL_INTEGRATOR_PT ? 2 * px * 3 : px * 3;
+    return j.integrator == SEL_INTEGRATOR_PT ? 2 * px * 3 : px * 3;  // deferred and VCM: one layer
 }
 
 }  // namespace
@@ -139,7 +139,7 @@ bool budget_allows(SelServerTy* S, size_t need) {
 bool admit_one(SelServerTy* S, Job* j) {
     const SelJob& d = j->desc;
     int slot = -1;
-    if (d.integrator == SEL_INTEGRATOR_PT) {
+    if (d.integrator != SEL_INTEGRATOR_VCM) {
         for (int k = 0; k < kMaxPtJobs; ++k)
             if (!S->slots[k]) { slot = k; break; }
         if (slot < 0) return false;
@@ -174,7 +174,7 @@ bool admit_one(SelServerTy* S, Job* j) {
     cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming);
     SelSceneTy* sc = d.scene;
     j->scene = scene_view(sc);
-    if (d.integrator == SEL_INTEGRATOR_PT) {
+    if (d.integrator != SEL_INTEGRATOR_VCM) {
         j->slot = slot;
         S->slots[slot] = j;
         j->total = uint64_t(d.camera.width) * d.camera.height * d.pt.samplesPerPixel;
@@ -264,6 +264,7 @@ bool pt_round(SelServerTy* S) {
             cap -= q;
         }
     c.njobs = uint32_t(njobs);
+    uint32_t bounces = 1;
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
         std::memset(&table[k], 0, sizeof(PtJob));
@@ -273,16 +274,27 @@ bool pt_round(SelServerTy* S) {
         t.scene = j->scene;
         init_camera(j->desc.camera, t.cam);
         t.max_bounces = j->desc.pt.maxBounces;
+        if (j->desc.integrator == SEL_INTEGRATOR_DEFERRED) {
+            t.mode = kPtModeDeferred;
+            t.samples_per_axis = deferred_axis(j->desc.pt);
+        }
         t.seed = j->desc.pt.seed;
+        bounces = std::max(bounces, t.max_bounces);
         t.total = j->total;
         t.accum = j->accum;
     }
     cudaMemcpyAsync(S->pst.jobs, table, sizeof(PtJob) * kMaxPtJobs, cudaMemcpyHostToDevice, S->pt_stream);
     cudaMemcpyAsync(S->pst.control, &c, sizeof(PtControl), cudaMemcpyHostToDevice, S->pt_stream);
     bool sort = false;
+    uint32_t modes = 0;
     for (int k = 0; k < kMaxPtJobs; ++k)
-        if (S->slots[k]) sort |= S->slots[k]->scene.sort_hint != 0;
-    cudaError_t e = pt_run_batches(0, S->cfg.max_bounces, sort, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph);
+        if (S->slots[k]) {
+            sort |= S->slots[k]->scene.sort_hint != 0;
+            modes |= S->slots[k]->desc.integrator == SEL_INTEGRATOR_DEFERRED ? 2u : 1u;
+        }
+    // rounds per batch: the largest maxBounces of the jobs in the slots (at most config.max_bounces)
+    cudaError_t e = pt_run_batches(0, bounces, sort, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph, 128,
+                                   modes);
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
         if (!j || c.quota[k] == 0) continue;
@@ -452,8 +464,10 @@ int sel_server_result_floats(const SelJob* job, size_t* out_floats) {
 int sel_server_submit(SelServer server, const SelJob* job, uint64_t* out_job_id) {
     if (!server || !job || !out_job_id) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     SelSceneTy* sc = job->scene;
-    if (job->integrator == SEL_INTEGRATOR_PT) {
-        if (int rc = check_render_args(sc, &job->camera, &job->pt)) return rc;
+    if (job->integrator == SEL_INTEGRATOR_PT || job->integrator == SEL_INTEGRATOR_DEFERRED) {
+        if (int rc = job->integrator == SEL_INTEGRATOR_PT ? check_render_args(sc, &job->camera, &job->pt)
+                                                          : check_deferred_args(sc, &job->camera, &job->pt))
+            return rc;
         if (sc->info.bvh_kind != SEL_BVH_WIDE8_Q8)
             return fail(SEL_ERR_INVALID_OPERATION, "served path-tracer jobs need SEL_BVH_WIDE8_Q8 scenes");
         if (job->pt.maxBounces == 0 || job->pt.maxBounces > server->cfg.max_bounces)

@@ -13,12 +13,20 @@ ptex_golden.npz  - a triangle mesh (icosphere, 320 faces) with 16 x 16 half-floa
                    PtexTriangleFilter (getFilter(f_bspline), zero widths, as SurfaceParameters.cpp:196-206)
                    at seeded (face, u, v) queries including edges, corners and out-of-range faces.
 cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
-                   from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp); the image the
+                   from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp; each 256-spp chunk
+                   with seeds of its own); the image the
                    path tracers' rMSE is measured against.  Needs only the oracle (python ... cornell).
 cornell_vcm_64_ref.npz - the FP64 high-pass vertex connection and merging image of the Cornell scene (64 x 64,
                    4096 passes, path length 10, the default radius) from the oracle VCM (oracle/oracle_vcm.cpp);
                    the image the VCM integrators' rMSE is measured against.  Needs only the oracle
                    (python ... vcm).
+cmj_golden.npz   - correlated multi-jittered points CorrelatedMultiJitter(s, m, m, p) of the reference
+                   (Source/Core/MathLib/CorrelatedMultiJitter.cpp, compiled into oracle/_ref/libref_bsdf.so)
+                   for pattern sizes 1..16 and seeded decorrelation values p.
+cornell_deferred_64_ref.npz - the FP64 image of the Cornell scene (64 x 64) from the oracle deferred path
+                   tracer (oracle/oracle_pt.cpp) with a 64 x 64 correlated multi-jittered pattern (4096 spp),
+                   MT19937 sampling (each 256-sample chunk with seeds of its own) and a 64-segment cap; the image the deferred integrators' rMSE is measured against.
+                   Needs only the oracle (python ... deferred).
 """
 from __future__ import annotations
 
@@ -165,7 +173,9 @@ def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
     img = np.zeros((2, size, size, 3), np.float64)
     step = 256
     for p in range(0, spp, step):
-        img += oracle.pt_render(rs, size, size, p, min(spp, p + step), max_bounces=8, seed=seed, rng="mt")
+        # MT19937 engines are seeded per call (seed + pixel): each chunk takes seeds of its own
+        img += oracle.pt_render(rs, size, size, p, min(spp, p + step), max_bounces=8, seed=seed + (p // step) * 65536,
+                                rng="mt")
     img /= spp
     np.savez_compressed(OUT / "cornell_64_ref.npz", image=img.astype(np.float32), spp=spp, seed=seed)
     print("cornell_64_ref.npz: mean radiance", img[1].mean(axis=(0, 1)))
@@ -185,8 +195,43 @@ def make_cornell_vcm(passes=4096, size=64, max_len=10, seed=0x5E1A5C0C):
     print("cornell_vcm_64_ref.npz: mean radiance", img.mean(axis=(0, 1)))
 
 
+def make_cmj(seed=0x5E1ACC17):
+    lib = ctypes.CDLL(str(ROOT / "oracle" / "_ref" / "libref_bsdf.so"))
+    lib.ref_cmj.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    rng = np.random.default_rng(seed)
+    ps = [0, 1, 7, 4095, 65535, (1 << 20) + 3, (1 << 31) - 1] + [int(x) for x in rng.integers(0, 1 << 31, 9)]
+    ms, pv, pts = [], [], []
+    for m in (1, 2, 3, 4, 5, 7, 8, 16):
+        for p in ps:
+            xy = np.zeros((m * m, 2), np.float32)
+            lib.ref_cmj(m, p, m * m, xy.ctypes.data)
+            ms.append(m)
+            pv.append(p)
+            pts.append(xy)
+    offs = np.cumsum([0] + [x.shape[0] for x in pts]).astype(np.int64)
+    np.savez_compressed(OUT / "cmj_golden.npz", m=np.array(ms, np.int32), p=np.array(pv, np.int64), offsets=offs,
+                        points=np.concatenate(pts))
+    print("cmj_golden.npz:", len(ms), "patterns")
+
+
+def make_cornell_deferred(axis=64, size=64, max_bounces=64, seed=0x5E1A5C0D):
+    import oracle
+    from selas_gb300 import scenes
+    rs = scenes.cornell_box()
+    img = np.zeros((size, size, 3), np.float64)
+    spp = axis * axis
+    step = 256
+    for p in range(0, spp, step):
+        img += oracle.deferred_render(rs, size, size, p, min(spp, p + step), samples_per_axis=axis,
+                                      max_bounces=max_bounces, seed=seed + (p // step) * 65536, rng="mt")
+    img /= spp
+    np.savez_compressed(OUT / "cornell_deferred_64_ref.npz", image=img.astype(np.float32), spp=spp, seed=seed,
+                        max_bounces=max_bounces)
+    print("cornell_deferred_64_ref.npz: mean radiance", img.mean(axis=(0, 1)))
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm"]
+    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm", "cmj", "deferred"]
     if "bsdf" in what:
         make_bsdf()
     if "ptex" in what:
@@ -195,3 +240,7 @@ if __name__ == "__main__":
         make_cornell()
     if "vcm" in what:
         make_cornell_vcm()
+    if "cmj" in what:
+        make_cmj()
+    if "deferred" in what:
+        make_cornell_deferred()

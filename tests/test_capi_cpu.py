@@ -69,6 +69,20 @@ def test_vcm_settings_defaults_and_layout(lib):
     assert lib.sel_vcm_generate_image(None, None, None, None) == sel.SEL_ERR_INVALID_ARGUMENT
 
 
+def test_deferred_settings_defaults(lib):
+    import selas_gb300 as sel
+    s = sel.SelPtSettings()
+    assert lib.sel_deferred_settings_defaults(ctypes.byref(s)) == 0
+    assert (s.samplesPerPixel, s.maxBounces, s.pathsInFlight, s.traceBlockSize) == (16, 64, 0, 0)
+    assert sel.deferred_settings(5, 12).samplesPerPixel == 25
+    assert lib.sel_deferred_settings_defaults(None) == sel.SEL_ERR_INVALID_ARGUMENT
+    assert lib.sel_deferred_generate_image(None, None, None, None) == sel.SEL_ERR_INVALID_ARGUMENT
+    j = sel.SelJob()
+    j.camera.width, j.camera.height, j.integrator = 10, 6, sel.SEL_INTEGRATOR_DEFERRED
+    n = ctypes.c_size_t()
+    assert lib.sel_server_result_floats(ctypes.byref(j), ctypes.byref(n)) == 0 and n.value == 180
+
+
 def test_server_records_and_defaults(lib):
     import selas_gb300 as sel
     assert ctypes.sizeof(sel.SelJob) == 120 and ctypes.sizeof(sel.SelServerConfig) == 32

@@ -1,4 +1,4 @@
-"""Render server (sel_server_*): continuous batching of path-tracer and VCM jobs.  A job's image must not
+"""Render server (sel_server_*): continuous batching of path-tracer, deferred path-tracer and VCM jobs.  A job's image must not
 depend on what else runs: the same as alone, in a mix of other scenes, resolutions and integrators, and as
 the single-render entry points give it (same random streams; only the order of FP64 additions differs)."""
 import ctypes
@@ -30,6 +30,8 @@ def _jobs(scene_set):
         sel.pt_job(s_sc, spheres.sel_camera(sel, 80, 60), sel.pt_settings(8, 6, seed=13)),
         sel.vcm_job(c_sc, cornell.sel_camera(sel, 32, 32), sel.vcm_settings(3, 10, seed=14)),
         sel.pt_job(c_sc, cornell.sel_camera(sel, 40, 40), sel.pt_settings(32, 8, seed=15)),
+        sel.deferred_job(s_sc, spheres.sel_camera(sel, 56, 40), sel.deferred_settings(3, 8, seed=16)),
+        sel.deferred_job(c_sc, cornell.sel_camera(sel, 48, 48), sel.deferred_settings(4, 6, seed=17)),
     ]
 
 
@@ -62,6 +64,11 @@ def test_served_images_equal_the_single_render_entry_points(device, scene_set):
         c_sc.pt_generate_image(cornell.sel_camera(sel, 64, 64), sel.pt_settings(16, 8, seed=11)),
         s_sc.vcm_generate_image(spheres.sel_camera(sel, 48, 32), sel.vcm_settings(4, 8, seed=12)),
         s_sc.pt_generate_image(spheres.sel_camera(sel, 80, 60), sel.pt_settings(8, 6, seed=13)),
+    ]
+    served = served[:3] + served[5:]
+    direct += [
+        s_sc.deferred_generate_image(spheres.sel_camera(sel, 56, 40), sel.deferred_settings(3, 8, seed=16)),
+        c_sc.deferred_generate_image(cornell.sel_camera(sel, 48, 48), sel.deferred_settings(4, 6, seed=17)),
     ]
     for s, d in zip(served, direct):
         np.testing.assert_allclose(s, d, **TOL)
