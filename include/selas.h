@@ -128,6 +128,18 @@ int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size);
 int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const float* vertices,
                                    size_t vertex_count, size_t vertex_stride_bytes,
                                    const unsigned int* indices, size_t triangle_count);
+/* Instances, two levels at most (RTC_MAX_INSTANCE_LEVEL_COUNT = 2): rtcNewGeometry(RTC_GEOMETRY_TYPE_INSTANCE)
+ * + rtcSetGeometryInstancedScene + rtcSetGeometryTransform(RTC_FORMAT_FLOAT4X4_COLUMN_MAJOR) +
+ * rtcAttachGeometryByID (SubsceneResource.cpp:63-79), and the subscene-instance user geometry whose callbacks
+ * transform the ray into the subscene (SceneResource.cpp:73-187).  Attaches `instanced`, a committed scene of
+ * the 8-wide layout, to `scene` under instID (unique among the scene's geomIDs and instIDs) with the affine
+ * localToWorld (16 floats, column-major, last row 0 0 0 1).  Queries report, for a hit inside instances,
+ * instID[0] = the outermost instance's id and instID[1] = the next one's (SEL_INVALID_GEOMETRY_ID where there
+ * is none), geomID / primID of the hit mesh within its scene, Ng in that mesh's object space (untransformed,
+ * as Embree reports it) and t in the world ray's parametrisation.  `instanced` must stay committed and alive
+ * while `scene` uses it (releasing it fails while a committed scene instances it); committing it again
+ * requires committing `scene` again.  Scenes with instances use the SEL_BVH_WIDE8_Q8 layout. */
+int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld);
 int sel_scene_commit(SelScene scene);
 int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info);
 int sel_scene_release(SelScene scene);

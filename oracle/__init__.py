@@ -40,6 +40,9 @@ def lib() -> ctypes.CDLL:
                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                         ctypes.c_uint32, ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
             "oracle_cmj": ([_i, _i, _i, _vp], None),
+            "oracle_instanced_query": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i, _i],
+                                       None),
+            "oracle_affine_inverse": ([_vp, _vp], _i),
             "oracle_vcm_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_uint64, _i, _vp, _i, _vp, _i, _i, _vp], None),
@@ -175,6 +178,44 @@ def cmj(m, p, n=None):
     xy = np.zeros((n, 2), np.float32)
     lib().oracle_cmj(m, p, n, _p(xy))
     return xy
+
+
+def affine_inverse(l2w_rows):
+    """World-to-local rows (3 x 4 float32) of a local-to-world affine (3 x 4 rows), as instances use them."""
+    a = np.ascontiguousarray(np.asarray(l2w_rows, np.float32)[:3, :4])
+    out = np.zeros((3, 4), np.float32)
+    if not lib().oracle_affine_inverse(_p(a), _p(out)):
+        raise ValueError("singular transform")
+    return out
+
+
+def instanced_query(scenes, top, rays, any_hit=False, nthreads=None):
+    """Brute-force queries of an instanced scene graph, in place.  scenes: list of dicts with "meshes"
+    [(geom_id, vertices (n, 3), indices (m, 3))] and "instances" [(inst_id, scene index, local-to-world 3 x 4
+    or 4 x 4)]; rays: SelRayHit records (closest hit) or SelRay records (any hit)."""
+    verts, prim, geom, owner = [], [], [], []
+    w2l, ids, holder, proto = [], [], [], []
+    for si, sc in enumerate(scenes):
+        for gid, v, idx in sc.get("meshes", []):
+            v = np.asarray(v, np.float32).reshape(-1, 3)
+            idx = np.asarray(idx, np.int64).reshape(-1, 3)
+            verts.append(v[idx].reshape(-1, 9))
+            prim.append(np.arange(idx.shape[0], dtype=np.uint32))
+            geom.append(np.full(idx.shape[0], gid, np.uint32))
+            owner.append(np.full(idx.shape[0], si, np.uint32))
+        for iid, pi, m in sc.get("instances", []):
+            w2l.append(affine_inverse(np.asarray(m, np.float32)[:3, :4]).reshape(12))
+            ids.append(iid)
+            holder.append(si)
+            proto.append(pi)
+    cat = lambda xs, dt, shape: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(shape, dt)
+    V, P, G, O = cat(verts, np.float32, (0, 9)), cat(prim, np.uint32, 0), cat(geom, np.uint32, 0), cat(owner, np.uint32, 0)
+    W = np.ascontiguousarray(np.array(w2l, np.float32).reshape(-1, 12))
+    I = np.array(ids, np.uint32)
+    H = np.array(holder, np.uint32)
+    Q = np.array(proto, np.uint32)
+    lib().oracle_instanced_query(len(scenes), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(W), _p(I), _p(H), _p(Q),
+                                 W.shape[0], top, _p(rays), rays.shape[0], int(any_hit), nthreads or threads())
 
 
 def ptex_eval(faces, texels_u16, queries):

@@ -11,6 +11,11 @@
 // then smallest (geomID, primID)).  Two traversals are provided: brute force over every triangle (the
 // definition) and an SAH BVH of this file's own (for large scenes and for the CPU baseline).
 //
+// Instanced scenes (two levels, as the reference's subscene instances of model instances,
+// Source/Core/SceneLib/SceneResource.cpp:73-187 and SubsceneResource.cpp:63-79) are restated by brute force:
+// the ray is carried into each instance by its world-to-local rows (fma chains), t stays in the world ray's
+// parametrisation, and ties on t go to the smaller (instID[0], instID[1], geomID, primID).
+//
 // Compiled with -ffp-contract=off; every fused multiply-add is an explicit std::fma.
 
 #include <algorithm>
@@ -301,6 +306,61 @@ bool trace(const Bvh& bvh, const Ray& r, Best& best) {
     return best.tri >= 0;
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Instanced scenes, brute force
+// ---------------------------------------------------------------------------------------------------
+struct OInst {
+    float w2l[12];
+    uint32_t id, proto;
+};
+struct OScene {
+    std::vector<Tri> tris;
+    std::vector<OInst> insts;
+};
+struct IBest {
+    float t = 0, u = 0, v = 0;
+    const Tri* tri = nullptr;
+    uint64_t inst = ~0ull, key = ~0ull;
+};
+
+void xpoint(const float* m, const float* p, float* o) {
+    for (int r = 0; r < 3; ++r) o[r] = std::fma(m[4 * r], p[0], std::fma(m[4 * r + 1], p[1], std::fma(m[4 * r + 2], p[2], m[4 * r + 3])));
+}
+void xvector(const float* m, const float* d, float* o) {
+    for (int r = 0; r < 3; ++r) o[r] = std::fma(m[4 * r], d[0], std::fma(m[4 * r + 1], d[1], m[4 * r + 2] * d[2]));
+}
+bool untraceable(const float* o, const float* d) {
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(o[k]) || !std::isfinite(d[k])) return true;
+    return d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f;
+}
+
+// Returns true when an any-hit query found a hit.
+bool brute_instanced(const std::vector<OScene>& S, uint32_t s, const float* o, const float* d, float tnear, float& tfar,
+                     uint64_t cur, int level, IBest& best, bool any) {
+    const Setup st = setup(d);
+    for (const Tri& tri : S[s].tris) {
+        float t, u, v;
+        if (!intersect(st, o, tri, tnear, tfar, t, u, v)) continue;
+        if (any) return true;
+        const uint64_t k = key_of(tri);
+        if (t < tfar || cur < best.inst || (cur == best.inst && k < best.key)) {
+            tfar = t;
+            best.t = t; best.u = u; best.v = v; best.tri = &tri; best.inst = cur; best.key = k;
+        }
+    }
+    for (const OInst& in : S[s].insts) {
+        if (level >= 2) continue;
+        float o2[3], d2[3];
+        xpoint(in.w2l, o, o2);
+        xvector(in.w2l, d, d2);
+        if (untraceable(o2, d2)) continue;
+        const uint64_t ci = level == 0 ? ((uint64_t(in.id) << 32) | 0xffffffffull) : ((cur & 0xffffffff00000000ull) | in.id);
+        if (brute_instanced(S, in.proto, o2, d2, tnear, tfar, ci, level + 1, best, any)) return true;
+    }
+    return false;
+}
+
 std::vector<Tri> make_tris(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t n) {
     std::vector<Tri> tris(static_cast<size_t>(n));
     for (int64_t i = 0; i < n; ++i) {
@@ -398,6 +458,68 @@ void oracle_intersect_bvh(void* h, void* rayhits, int64_t m, int threads) {
         Best best;
         if (trace<false>(bvh, rh[i].ray, best)) write_hit(rh[i], bvh.tris[size_t(best.tri)], best);
     });
+}
+
+// Instanced scenes.  Triangles: verts (ntri x 9), prim, geom and the scene each belongs to (tri_scene);
+// instances: w2l rows (ninst x 12), instID, the scene holding the instance and the instanced scene; `top` is
+// the scene queried.  any_hit = 0: rayhits are SelRayHit records (Ng in the hit mesh's object space); else
+// SelRay records (tfar = -inf on a hit).
+void oracle_instanced_query(int n_scenes, const float* verts, const uint32_t* prim, const uint32_t* geom,
+                            const uint32_t* tri_scene, int64_t ntri, const float* w2l, const uint32_t* inst_id,
+                            const uint32_t* inst_scene, const uint32_t* inst_proto, int64_t ninst, int top, void* rays,
+                            int64_t m, int any_hit, int threads) {
+    std::vector<OScene> S(size_t(std::max(n_scenes, 1)));
+    const std::vector<Tri> tris = make_tris(verts, prim, geom, ntri);
+    for (int64_t i = 0; i < ntri; ++i) S[tri_scene[i]].tris.push_back(tris[size_t(i)]);
+    for (int64_t i = 0; i < ninst; ++i) {
+        OInst in;
+        std::memcpy(in.w2l, w2l + 12 * i, 48);
+        in.id = inst_id[i];
+        in.proto = inst_proto[i];
+        S[inst_scene[i]].insts.push_back(in);
+    }
+    parallel_for(m, threads, [&](int64_t i) {
+        Ray& r = any_hit ? static_cast<Ray*>(rays)[i] : static_cast<RayHit*>(rays)[i].ray;
+        if (untraceable(r.org, r.dir)) return;
+        float tfar = r.tfar;
+        IBest best;
+        const bool hit = brute_instanced(S, uint32_t(top), r.org, r.dir, r.tnear, tfar, ~0ull, 0, best, any_hit != 0);
+        if (any_hit) {
+            if (hit) r.tfar = -INFINITY;
+            return;
+        }
+        if (!best.tri) return;
+        RayHit& rh = static_cast<RayHit*>(rays)[i];
+        Best b;
+        b.t = best.t; b.u = best.u; b.v = best.v;
+        write_hit(rh, *best.tri, b);
+        rh.inst[0] = uint32_t(best.inst >> 32);
+        rh.inst[1] = uint32_t(best.inst);
+    });
+}
+
+// World-to-local rows of an affine local-to-world (rows): cofactor inverse and -inv . t in double, rounded
+// to float (the product's instance transform, restated).  Returns 0 when singular or not finite.
+int oracle_affine_inverse(const float* l2w, float* w2l) {
+    const double a00 = l2w[0], a01 = l2w[1], a02 = l2w[2], t0 = l2w[3];
+    const double a10 = l2w[4], a11 = l2w[5], a12 = l2w[6], t1 = l2w[7];
+    const double a20 = l2w[8], a21 = l2w[9], a22 = l2w[10], t2 = l2w[11];
+    const double cof[3][3] = {{a11 * a22 - a12 * a21, a12 * a20 - a10 * a22, a10 * a21 - a11 * a20},
+                              {a02 * a21 - a01 * a22, a00 * a22 - a02 * a20, a01 * a20 - a00 * a21},
+                              {a01 * a12 - a02 * a11, a02 * a10 - a00 * a12, a00 * a11 - a01 * a10}};
+    const double det = a00 * cof[0][0] + a01 * cof[0][1] + a02 * cof[0][2];
+    if (!(det != 0.0) || !std::isfinite(det)) return 0;
+    for (int r = 0; r < 3; ++r) {
+        const double i0 = cof[0][r] / det, i1 = cof[1][r] / det, i2 = cof[2][r] / det;
+        const double tr = -(i0 * t0 + i1 * t1 + i2 * t2);
+        w2l[4 * r] = float(i0);
+        w2l[4 * r + 1] = float(i1);
+        w2l[4 * r + 2] = float(i2);
+        w2l[4 * r + 3] = float(tr);
+    }
+    for (int k = 0; k < 12; ++k)
+        if (!std::isfinite(w2l[k])) return 0;
+    return 1;
 }
 
 void oracle_occluded_bvh(void* h, void* rays, int64_t m, int threads) {

@@ -72,6 +72,7 @@ _SIGNATURES = {
     "sel_scene_set_bvh_kind": [_vp, _i],
     "sel_scene_attach_triangle_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
     "sel_scene_commit": [_vp],
+    "sel_scene_attach_instance": [_vp, _u, _vp, _vp],
     "sel_scene_get_info": [_vp, ctypes.POINTER(SceneInfo)],
     "sel_scene_release": [_vp],
     "sel_intersect1": [_vp, _vp],
@@ -162,6 +163,15 @@ class Scene:
         idx = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
         check(lib().sel_scene_attach_triangle_mesh(self.handle, geom_id, _ptr(v), v.shape[0], 12, _ptr(idx),
                                                    idx.shape[0]))
+
+    def attach_instance(self, inst_id: int, instanced: "Scene", local_to_world) -> None:
+        """Instance of a committed scene; local_to_world: 4 x 4 (or 3 x 4) affine matrix, row-major maths
+        convention (points are columns), passed to the C ABI column-major."""
+        m = np.eye(4, dtype=np.float64)
+        a = np.asarray(local_to_world, dtype=np.float64)
+        m[:a.shape[0], :] = a
+        cm = np.ascontiguousarray(m.T.astype(np.float32)).reshape(16)
+        check(lib().sel_scene_attach_instance(self.handle, inst_id, instanced.handle, _ptr(cm)))
 
     def commit(self) -> None:
         check(lib().sel_scene_commit(self.handle))

@@ -56,10 +56,11 @@ int read_error_word(SelDeviceTy* dev, cudaStream_t s) {
     if (word) {
         cudaMemsetAsync(dev->d_err, 0, sizeof(uint32_t), s);
         cudaStreamSynchronize(s);
-        const char* what = (word & 2u)   ? "traversal stack overflow"
-                           : (word & 4u) ? "Ptex filter frame stack overflow"
-                           : (word & 8u) ? "render queue overflow"
-                                         : "kernel iteration cap reached";
+        const char* what = (word & 2u)    ? "traversal stack overflow"
+                           : (word & 4u)  ? "Ptex filter frame stack overflow"
+                           : (word & 8u)  ? "render queue overflow"
+                           : (word & 16u) ? "instances nested deeper than two levels"
+                                          : "kernel iteration cap reached";
         return fail(SEL_ERR_DEVICE_LIMIT, what);
     }
     return SEL_OK;
@@ -71,7 +72,16 @@ DeviceBvh device_bvh(const SelSceneTy* sc) {
     b.nodes = sc->d_nodes;
     b.tris = static_cast<const float4*>(sc->d_tris);
     b.tri_count = uint32_t(sc->info.triangle_count);
+    b.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     return b;
+}
+
+bool instances_fresh(const SelSceneTy* sc) {
+    for (const auto& r : sc->referenced) {
+        if (!r.first->committed || r.first->generation != r.second) return false;
+        if (!instances_fresh(r.first)) return false;
+    }
+    return true;
 }
 
 }  // namespace sel
@@ -151,10 +161,12 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
         return fail(SEL_ERR_INVALID_ARGUMENT, "null buffer");
     if (vertex_stride_bytes < 12 || vertex_stride_bytes % 4)
         return fail(SEL_ERR_INVALID_ARGUMENT, "vertex stride must be >= 12 and a multiple of 4");
-    if (geomID == SEL_INVALID_GEOMETRY_ID) return fail(SEL_ERR_INVALID_ARGUMENT, "invalid geomID");
+    if (geomID >= kInstanceGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 0xFFFFFFFE");
     std::lock_guard<std::mutex> lock(scene->mu);
     for (const MeshInput& m : scene->meshes)
         if (m.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
+    for (const SelSceneTy::InstanceInput& ii : scene->instances)
+        if (ii.instID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already used by an instance");
     MeshInput m;
     m.geomID = geomID;
     try {
@@ -168,6 +180,32 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
     for (uint32_t idx : m.indices)
         if (idx >= vertex_count) return fail(SEL_ERR_INVALID_ARGUMENT, "triangle index out of range");
     scene->meshes.push_back(std::move(m));
+    scene->committed = false;
+    return SEL_OK;
+}
+
+int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld) {
+    if (!scene || !instanced || !localToWorld) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (instanced == scene) return fail(SEL_ERR_INVALID_ARGUMENT, "a scene cannot instance itself");
+    if (instanced->dev != scene->dev) return fail(SEL_ERR_INVALID_ARGUMENT, "scenes of different devices");
+    if (instID >= kInstanceGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "instID must be below 0xFFFFFFFE");
+    const float* m = localToWorld;  // column-major 4 x 4: element (row r, column c) at m[4 c + r]
+    for (int k = 0; k < 16; ++k)
+        if (!std::isfinite(m[k])) return fail(SEL_ERR_INVALID_ARGUMENT, "non-finite transform");
+    if (m[3] != 0.0f || m[7] != 0.0f || m[11] != 0.0f || m[15] != 1.0f)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "localToWorld must be affine (last row 0 0 0 1)");
+    SelSceneTy::InstanceInput ii;
+    ii.instID = instID;
+    ii.scene = instanced;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) ii.l2w[4 * r + c] = m[4 * c + r];
+    if (!affine_inverse(ii.l2w, ii.w2l)) return fail(SEL_ERR_INVALID_ARGUMENT, "localToWorld is singular");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    for (const MeshInput& mi : scene->meshes)
+        if (mi.geomID == instID) return fail(SEL_ERR_INVALID_ARGUMENT, "instID already used by a mesh");
+    for (const SelSceneTy::InstanceInput& o : scene->instances)
+        if (o.instID == instID) return fail(SEL_ERR_INVALID_ARGUMENT, "instID already attached");
+    scene->instances.push_back(ii);
     scene->committed = false;
     return SEL_OK;
 }
@@ -189,10 +227,139 @@ int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size) {
     return SEL_OK;
 }
 
-int sel_scene_commit(SelScene scene) {
+}  // extern "C"
+
+namespace {
+
+// World box of an instance: the instanced scene's bounds transformed corner by corner in double, rounded
+// outward and padded by 2^-16 of its magnitude and extent, so that the box holds every point the object-space
+// test can hit despite the rounding of the two transforms.
+void instance_box(const SelSceneTy::InstanceInput& ii, float lo[3], float hi[3]) {
+    const SelSceneInfo& pi = ii.scene->info;
+    double blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < 8; ++k) {
+        const double p[3] = {(k & 1) ? pi.bounds_hi[0] : pi.bounds_lo[0], (k & 2) ? pi.bounds_hi[1] : pi.bounds_lo[1],
+                             (k & 4) ? pi.bounds_hi[2] : pi.bounds_lo[2]};
+        for (int r = 0; r < 3; ++r) {
+            const double w = double(ii.l2w[4 * r]) * p[0] + double(ii.l2w[4 * r + 1]) * p[1] +
+                             double(ii.l2w[4 * r + 2]) * p[2] + double(ii.l2w[4 * r + 3]);
+            blo[r] = std::min(blo[r], w);
+            bhi[r] = std::max(bhi[r], w);
+        }
+    }
+    for (int r = 0; r < 3; ++r) {
+        const double pad = (std::max(std::fabs(blo[r]), std::fabs(bhi[r])) + (bhi[r] - blo[r])) * std::ldexp(1.0, -16) +
+                           std::ldexp(1.0, -100);
+        lo[r] = std::nextafter(float(blo[r] - pad), -INFINITY);
+        hi[r] = std::nextafter(float(bhi[r] + pad), INFINITY);
+    }
+}
+
+// Checks the instances of a scene about to be committed and appends the leaf records that stand for them (a
+// mesh of geomID kInstanceGeom whose triangle i spans instance i's world box).
+int prepare_instances(SelSceneTy* scene, MeshInput& mesh, uint32_t& levels, uint32_t& below) {
+    levels = 0;
+    below = 0;
+    mesh.geomID = kInstanceGeom;
+    mesh.vertices.clear();
+    mesh.indices.clear();
+    if (scene->kind != SEL_BVH_WIDE8_Q8)
+        return fail(SEL_ERR_INVALID_OPERATION, "scenes with instances need the SEL_BVH_WIDE8_Q8 layout");
+    for (size_t i = 0; i < scene->instances.size(); ++i) {
+        const SelSceneTy::InstanceInput& ii = scene->instances[i];
+        SelSceneTy* p = ii.scene;
+        if (!p->committed) return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene is not committed");
+        if (p->info.bvh_kind != SEL_BVH_WIDE8_Q8)
+            return fail(SEL_ERR_INVALID_OPERATION, "instanced scenes need the SEL_BVH_WIDE8_Q8 layout");
+        if (p->inst_levels >= 2) return fail(SEL_ERR_INVALID_OPERATION, "instances nest at most two levels");
+        if (!instances_fresh(p)) return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene is out of date");
+        levels = std::max(levels, 1u + p->inst_levels);
+        below = std::max(below, p->stack_need);
+        float lo[3], hi[3];
+        instance_box(ii, lo, hi);
+        const uint32_t v = uint32_t(mesh.vertices.size() / 3);
+        mesh.vertices.insert(mesh.vertices.end(), {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]});
+        mesh.indices.insert(mesh.indices.end(), {v, v + 1, v});
+    }
+    return SEL_OK;
+}
+
+// After a successful build: the instance table, the nesting bounds and the references of a scene.
+int finish_instances(SelSceneTy* scene, uint32_t levels, uint32_t below) {
+    if (scene->d_insts) cudaFree(scene->d_insts);
+    scene->d_insts = nullptr;
+    const size_t n = scene->instances.size();
+    scene->stack_need = scene->info.max_depth + (n ? 2u + below : 0u);
+    if (n && scene->stack_need > uint32_t(kInstStack))
+        return fail(SEL_ERR_INVALID_OPERATION, "instance nesting too deep for the traversal stack");
+    std::vector<InstanceRecord> recs(n);
+    for (size_t i = 0; i < n; ++i) {
+        const SelSceneTy::InstanceInput& ii = scene->instances[i];
+        InstanceRecord& r = recs[i];
+        std::memset(&r, 0, sizeof(r));
+        std::memcpy(r.w2l, ii.w2l, sizeof(r.w2l));
+        std::memcpy(r.l2w, ii.l2w, sizeof(r.l2w));
+        r.nodes = ii.scene->d_nodes;
+        r.tris = ii.scene->d_tris;
+        r.insts = static_cast<const InstanceRecord*>(ii.scene->d_insts);
+        r.shading = nullptr;
+        r.instID = ii.instID;
+    }
+    if (n) {
+        cudaError_t e = cudaMalloc(&scene->d_insts, n * sizeof(InstanceRecord));
+        if (e == cudaSuccess) e = cudaMemcpy(scene->d_insts, recs.data(), n * sizeof(InstanceRecord), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "instance table");
+        scene->info.triangle_count -= n;
+        scene->info.device_bytes += n * sizeof(InstanceRecord);
+    }
+    scene->inst_levels = levels;
+    for (auto& r : scene->referenced) --r.first->instanced_by;
+    scene->referenced.clear();
+    for (const SelSceneTy::InstanceInput& ii : scene->instances) {
+        bool seen = false;
+        for (const auto& r : scene->referenced) seen |= r.first == ii.scene;
+        if (seen) continue;
+        scene->referenced.push_back({ii.scene, ii.scene->generation});
+        ++ii.scene->instanced_by;
+    }
+    return SEL_OK;
+}
+
+int commit_geometry(SelSceneTy* scene);
+
+}  // namespace
+
+extern "C" int sel_scene_commit(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     std::lock_guard<std::mutex> lock(scene->mu);
     if (int rc = set_device(scene->dev)) return rc;
+    uint32_t levels = 0, below = 0;
+    const bool has_instances = !scene->instances.empty();
+    if (has_instances) {
+        MeshInput mesh;
+        try {
+            if (int rc = prepare_instances(scene, mesh, levels, below)) return rc;
+        } catch (const std::bad_alloc&) {
+            return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+        }
+        scene->meshes.push_back(std::move(mesh));  // the instance records, for the duration of the build
+    }
+    scene->committed = false;
+    int rc = commit_geometry(scene);
+    if (has_instances) scene->meshes.pop_back();
+    if (rc == SEL_OK) rc = finish_instances(scene, levels, below);
+    if (rc != SEL_OK) {
+        scene->committed = false;
+        return rc;
+    }
+    ++scene->generation;
+    scene->committed = true;
+    return SEL_OK;
+}
+
+namespace {
+
+int commit_geometry(SelSceneTy* scene) {
     if (scene->kind == SEL_BVH_WIDE8_Q8 && scene->build_mode == SEL_BUILD_DEVICE) {
         DeviceBuild db;
         std::string derr;
@@ -216,7 +383,6 @@ int sel_scene_commit(SelScene scene) {
         info.build_ms = db.build_ms;
         info.upload_ms = 0.0;
         for (int a = 0; a < 3; ++a) { info.bounds_lo[a] = db.lo[a]; info.bounds_hi[a] = db.hi[a]; }
-        scene->committed = true;
         return SEL_OK;
     }
     BuiltBvh built;
@@ -254,9 +420,12 @@ int sel_scene_commit(SelScene scene) {
     info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
     info.upload_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
     for (int a = 0; a < 3; ++a) { info.bounds_lo[a] = built.lo[a]; info.bounds_hi[a] = built.hi[a]; }
-    scene->committed = true;
     return SEL_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info) {
     if (!scene || !out_info) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
@@ -279,11 +448,14 @@ int sel_device_set_option(SelDevice device, int option, int value) {
 
 int sel_scene_release(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (scene->instanced_by > 0)
+        return fail(SEL_ERR_INVALID_OPERATION, "scene is instanced by a committed scene: release that one first");
     set_device(scene->dev);
     cudaStreamSynchronize(scene->dev->stream);
+    for (auto& r : scene->referenced) --r.first->instanced_by;
     for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
                     scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
-                    scene->vcm_block})
+                    scene->vcm_block, scene->d_insts})
         if (p) cudaFree(p);
     delete scene;
     return SEL_OK;
@@ -297,6 +469,8 @@ int sel_scene_release(SelScene scene) {
 static int check_query(SelScene scene) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    if (!instances_fresh(scene))
+        return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene changed since this scene was committed");
     return SEL_OK;
 }
 

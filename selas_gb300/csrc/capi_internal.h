@@ -27,6 +27,19 @@ struct SelSceneTy {
     uint32_t tuned_paths_in_flight = 0; // sel_scene_autotune's choices (0: built-in defaults)
     uint32_t tuned_trace_block = 0;
     std::vector<sel::MeshInput> meshes;
+    // instances of other committed scenes (sel_scene_attach_instance): id, instanced scene, transforms
+    struct InstanceInput {
+        uint32_t instID;
+        SelSceneTy* scene;
+        float l2w[12], w2l[12];  // rows
+    };
+    std::vector<InstanceInput> instances;
+    void* d_insts = nullptr;                  // InstanceRecord[instances] of the last commit
+    uint32_t inst_levels = 0;                 // instance levels below this scene at the last commit (0..2)
+    uint32_t stack_need = 0;                  // worst-case instanced-traversal stack entries from here down
+    uint64_t generation = 0;                  // incremented by every commit
+    std::vector<std::pair<SelSceneTy*, uint64_t>> referenced;  // instanced scenes and their generations
+    int instanced_by = 0;                     // committed scenes whose instances reference this one
     bool committed = false;
     void* d_nodes = nullptr;
     void* d_tris = nullptr;

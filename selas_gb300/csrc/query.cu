@@ -2,6 +2,7 @@
 // launchers.  One thread per ray; each thread keeps its traversal stack in shared memory.
 #include "query.h"
 
+#include "instance.cuh"
 #include "traverse.cuh"
 
 namespace sel {
@@ -29,6 +30,39 @@ __device__ __forceinline__ void store_hit(SelRayHit* rh, const float4* __restric
     hp[0] = make_float4(ng.x, ng.y, ng.z, h.u);
     hp[1] = make_float4(h.v, p0.w, p1.w, __uint_as_float(SEL_INVALID_GEOMETRY_ID));
     reinterpret_cast<uint32_t*>(base)[20] = SEL_INVALID_GEOMETRY_ID;
+}
+
+__device__ __forceinline__ void store_hit_instanced(SelRayHit* rh, const InstHit& h) {
+    const float4* tp = h.tris + size_t(h.tri) * 3;
+    const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+    const float3 ng = triangle_ng(p0, p1, p2);  // object space of the hit mesh
+    float* base = reinterpret_cast<float*>(rh);
+    base[8] = h.t;
+    float4* hp = reinterpret_cast<float4*>(base + 12);
+    hp[0] = make_float4(ng.x, ng.y, ng.z, h.u);
+    hp[1] = make_float4(h.v, p0.w, p1.w, __uint_as_float(h.inst[0]));
+    reinterpret_cast<uint32_t*>(base)[20] = h.inst[1];
+}
+
+// Scenes with instances: one thread per ray, the instanced traversal with its deeper shared-memory stack.
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kQueryBlock)
+    k_query_instanced(const uint4* __restrict__ nodes, const float4* __restrict__ tris, const InstanceRecord* insts,
+                      float4* rays, uint32_t record_float4s, uint32_t n, uint32_t* err) {
+    __shared__ uint2 stack_mem[kInstStack * kQueryBlock];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    InstHit h;
+    uint32_t status = 0;
+    const bool found = trace_instanced<kAnyHit>(nodes, tris, insts, load_ray(rays + size_t(i) * record_float4s), h,
+                                                stack_mem + threadIdx.x, kQueryBlock, status);
+    if (status) atomicOr(err, status);
+    if (found) {
+        if (kAnyHit)
+            reinterpret_cast<float*>(rays + size_t(i) * record_float4s)[8] = -__int_as_float(0x7f800000);
+        else
+            store_hit_instanced(reinterpret_cast<SelRayHit*>(rays + size_t(i) * record_float4s), h);
+    }
 }
 
 // 8-wide traversal: one thread per ray over the whole batch, 8 resident 128-thread blocks per SM
@@ -83,7 +117,10 @@ cudaError_t launch_query(const DeviceBvh& bvh, float4* d_rays, uint32_t record_f
                          cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const dim3 grid((n + kQueryBlock - 1) / kQueryBlock);
-    if (bvh.kind == SEL_BVH_WIDE8_Q8) {
+    if (bvh.insts) {
+        k_query_instanced<kAnyHit><<<grid, kQueryBlock, 0, s>>>(static_cast<const uint4*>(bvh.nodes), bvh.tris,
+                                                                bvh.insts, d_rays, record_float4s, n, d_err);
+    } else if (bvh.kind == SEL_BVH_WIDE8_Q8) {
         k_query_wide<kAnyHit><<<grid, kQueryBlock, 0, s>>>(static_cast<const uint4*>(bvh.nodes), bvh.tris, d_rays,
                                                            record_float4s, n, d_err);
     } else {

@@ -13,6 +13,7 @@ struct DeviceBvh {
     const void* nodes = nullptr;   // WideNode[] or BinaryNode[]
     const float4* tris = nullptr;  // TriRecord[] as 3 x float4
     uint32_t tri_count = 0;
+    const InstanceRecord* insts = nullptr;  // instance table of a scene with instances (8-wide layout only)
 };
 
 cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);

@@ -91,4 +91,35 @@ std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max
 constexpr int kWideStack = 24;
 constexpr int kBinaryStack = 64;
 
+// ---------------------------------------------------------------------------------------------------
+// Instances (two levels, as Embree's RTC_MAX_INSTANCE_LEVEL_COUNT = 2)
+// ---------------------------------------------------------------------------------------------------
+// An instance enters its parent's BVH as a leaf record whose geomID word is kInstanceGeom and whose primID
+// word is the instance's index in the parent's instance table; its vertices (lo, hi, lo) span the world box.
+constexpr uint32_t kInstanceGeom = 0xFFFFFFFEu;
+// Stack entries per thread of the instanced traversal: the sum over the levels a ray can enter of the tree
+// depth, plus 2 per instance level (a pending-leaf entry and a level marker); commit rejects deeper nestings.
+constexpr int kInstStack = 40;
+
+// Device record of one instance (144 bytes = 9 x float4), in the parent scene's instance table.
+//   w2l: world-to-local affine rows (object point = w2l . (x, y, z, 1)); l2w: local-to-world rows;
+//   nodes / tris / insts: the instanced scene's 8-wide BVH, leaf records and own instance table (null: none);
+//   shading: the instanced scene's shading view for the integrators (null until its shading data is synced).
+struct InstanceRecord {
+    float w2l[12];
+    float l2w[12];
+    const void* nodes;
+    const void* tris;
+    const InstanceRecord* insts;
+    const void* shading;
+    uint32_t instID;
+    uint32_t pad[3];
+};
+static_assert(sizeof(InstanceRecord) == 144, "InstanceRecord must be 144 bytes");
+
+// World-to-local rows of an affine local-to-world (rows, 12 floats): the 3 x 3 inverse by cofactors and the
+// translation -inv . t, in double, rounded to float.  Returns false when the 3 x 3 part is singular or the
+// result is not finite.
+bool affine_inverse(const float l2w[12], float w2l[12]);
+
 }  // namespace sel

@@ -160,59 +160,69 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t byte) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | byte)) - 8388608.0f;
 }
 
+// Visits the nearest pending node of s.group (which must have one): pushes the rest of the group, tests the
+// node's eight child boxes, makes its hit internal children the new group and returns the triangles of its
+// hit leaf children as a bit mask over records tbase..tbase+23.  Returns false on stack overflow.
+template <int kDepth>
+__device__ __forceinline__ bool wide_visit(WideState& s, const uint4* __restrict__ nodes, uint2* stack, int stride,
+                                           uint32_t& status, uint32_t& tmask, uint32_t& tbase) {
+    const int b = __ffs(s.group.y >> 24) - 1;
+    s.group.y &= ~(1u << (24 + b));
+    const uint32_t slot = uint32_t(b) ^ s.oct;
+    const uint32_t idx = s.group.x + __popc(s.group.y & ((1u << slot) - 1u));
+    if (s.group.y & 0xff000000u) {
+        if (s.sp >= kDepth) { status |= kErrStackOverflow; return false; }
+        stack[s.sp * stride] = s.group;
+        ++s.sp;
+    }
+    const uint4* np = nodes + size_t(idx) * 5;
+    const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+    const float sxs = __fmul_rn(__uint_as_float((n0.w & 0xffu) << 23), s.ix);
+    const float sys = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xffu) << 23), s.iy);
+    const float szs = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xffu) << 23), s.iz);
+    const float oxa = __fmul_rn(__fsub_rn(__uint_as_float(n0.x), s.ox), s.ix);
+    const float oya = __fmul_rn(__fsub_rn(__uint_as_float(n0.y), s.oy), s.iy);
+    const float oza = __fmul_rn(__fsub_rn(__uint_as_float(n0.z), s.oz), s.iz);
+    const uint32_t imask = n0.w >> 24;
+    const float tnear_box = s.tnear - fabsf(s.tnear) * kBoxMargin;
+    const float tfar_box = s.tfar + fabsf(s.tfar) * kBoxMargin;
+    const bool px = s.ix >= 0.0f, py = s.iy >= 0.0f, pz = s.iz >= 0.0f;
+    const uint32_t nx0 = px ? n2.x : n3.z, nx1 = px ? n2.y : n3.w, fx0 = px ? n3.z : n2.x, fx1 = px ? n3.w : n2.y;
+    const uint32_t ny0 = py ? n2.z : n4.x, ny1 = py ? n2.w : n4.y, fy0 = py ? n4.x : n2.z, fy1 = py ? n4.y : n2.w;
+    const uint32_t nz0 = pz ? n3.x : n4.z, nz1 = pz ? n3.y : n4.w, fz0 = pz ? n4.z : n3.x, fz1 = pz ? n4.w : n3.y;
+    uint32_t new_hits = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const uint32_t byte = uint32_t(c & 3);
+        const float tnx = fmaf(qbyte(c < 4 ? nx0 : nx1, byte), sxs, oxa);
+        const float tfx = fmaf(qbyte(c < 4 ? fx0 : fx1, byte), sxs, oxa);
+        const float tny = fmaf(qbyte(c < 4 ? ny0 : ny1, byte), sys, oya);
+        const float tfy = fmaf(qbyte(c < 4 ? fy0 : fy1, byte), sys, oya);
+        const float tnz = fmaf(qbyte(c < 4 ? nz0 : nz1, byte), szs, oza);
+        const float tfz = fmaf(qbyte(c < 4 ? fz0 : fz1, byte), szs, oza);
+        const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tnear_box));
+        const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_box));
+        if (tmin <= tmax) {
+            if ((imask >> c) & 1u) {
+                new_hits |= 1u << (uint32_t(c) ^ s.oct);
+            } else {
+                const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
+                tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+            }
+        }
+    }
+    s.group = make_uint2(n1.x, (new_hits << 24) | imask);
+    tbase = n1.y;
+    return true;
+}
+
 // One traversal step.  Returns true when the ray is finished (any-hit: on the first hit).
 template <bool kAnyHit>
 __device__ __forceinline__ bool wide_step(WideState& s, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                           uint2* stack, int stride, uint32_t& status) {
     uint32_t tmask = 0, tbase = 0;
     if (s.group.y & 0xff000000u) {
-        const int b = __ffs(s.group.y >> 24) - 1;
-        s.group.y &= ~(1u << (24 + b));
-        const uint32_t slot = uint32_t(b) ^ s.oct;
-        const uint32_t idx = s.group.x + __popc(s.group.y & ((1u << slot) - 1u));
-        if (s.group.y & 0xff000000u) {
-            if (s.sp >= kWideStack) { status |= kErrStackOverflow; return true; }
-            stack[s.sp * stride] = s.group;
-            ++s.sp;
-        }
-        const uint4* np = nodes + size_t(idx) * 5;
-        const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
-        const float sxs = __fmul_rn(__uint_as_float((n0.w & 0xffu) << 23), s.ix);
-        const float sys = __fmul_rn(__uint_as_float(((n0.w >> 8) & 0xffu) << 23), s.iy);
-        const float szs = __fmul_rn(__uint_as_float(((n0.w >> 16) & 0xffu) << 23), s.iz);
-        const float oxa = __fmul_rn(__fsub_rn(__uint_as_float(n0.x), s.ox), s.ix);
-        const float oya = __fmul_rn(__fsub_rn(__uint_as_float(n0.y), s.oy), s.iy);
-        const float oza = __fmul_rn(__fsub_rn(__uint_as_float(n0.z), s.oz), s.iz);
-        const uint32_t imask = n0.w >> 24;
-        const float tnear_box = s.tnear - fabsf(s.tnear) * kBoxMargin;
-        const float tfar_box = s.tfar + fabsf(s.tfar) * kBoxMargin;
-        const bool px = s.ix >= 0.0f, py = s.iy >= 0.0f, pz = s.iz >= 0.0f;
-        const uint32_t nx0 = px ? n2.x : n3.z, nx1 = px ? n2.y : n3.w, fx0 = px ? n3.z : n2.x, fx1 = px ? n3.w : n2.y;
-        const uint32_t ny0 = py ? n2.z : n4.x, ny1 = py ? n2.w : n4.y, fy0 = py ? n4.x : n2.z, fy1 = py ? n4.y : n2.w;
-        const uint32_t nz0 = pz ? n3.x : n4.z, nz1 = pz ? n3.y : n4.w, fz0 = pz ? n4.z : n3.x, fz1 = pz ? n4.w : n3.y;
-        uint32_t new_hits = 0;
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const uint32_t byte = uint32_t(c & 3);
-            const float tnx = fmaf(qbyte(c < 4 ? nx0 : nx1, byte), sxs, oxa);
-            const float tfx = fmaf(qbyte(c < 4 ? fx0 : fx1, byte), sxs, oxa);
-            const float tny = fmaf(qbyte(c < 4 ? ny0 : ny1, byte), sys, oya);
-            const float tfy = fmaf(qbyte(c < 4 ? fy0 : fy1, byte), sys, oya);
-            const float tnz = fmaf(qbyte(c < 4 ? nz0 : nz1, byte), szs, oza);
-            const float tfz = fmaf(qbyte(c < 4 ? fz0 : fz1, byte), szs, oza);
-            const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tnear_box));
-            const float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tfar_box));
-            if (tmin <= tmax) {
-                if ((imask >> c) & 1u) {
-                    new_hits |= 1u << (uint32_t(c) ^ s.oct);
-                } else {
-                    const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
-                    tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
-                }
-            }
-        }
-        s.group = make_uint2(n1.x, (new_hits << 24) | imask);
-        tbase = n1.y;
+        if (!wide_visit<kWideStack>(s, nodes, stack, stride, status, tmask, tbase)) return true;
     }
     while (tmask) {
         const int b = __ffs(tmask) - 1;
