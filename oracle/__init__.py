@@ -43,6 +43,11 @@ def lib() -> ctypes.CDLL:
             "oracle_instanced_query": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i, _i],
                                        None),
             "oracle_affine_inverse": ([_vp, _vp], _i),
+            "oracle_graph_render": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _i, _i, _i, ctypes.c_uint32, _vp],
+                                    None),
+            "oracle_graph_intersect": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i], None),
             "oracle_vcm_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_uint64, _i, _vp, _i, _vp, _i, _i, _vp], None),
@@ -186,6 +191,73 @@ def affine_inverse(l2w_rows):
     out = np.zeros((3, 4), np.float32)
     if not lib().oracle_affine_inverse(_p(a), _p(out)):
         raise ValueError("singular transform")
+    return out
+
+
+def _graph_arrays(scenes):
+    """Flat arrays of an instanced scene graph: triangles (verts, prim, geom, owning scene) and instances
+    (local-to-world rows, id, owning scene, instanced scene)."""
+    verts, prim, geom, owner = [], [], [], []
+    l2w, ids, holder, proto = [], [], [], []
+    for si, sc in enumerate(scenes):
+        for gid, v, idx in sc.get("meshes", []):
+            v = np.asarray(v, np.float32).reshape(-1, 3)
+            idx = np.asarray(idx, np.int64).reshape(-1, 3)
+            verts.append(v[idx].reshape(-1, 9))
+            prim.append(np.arange(idx.shape[0], dtype=np.uint32))
+            geom.append(np.full(idx.shape[0], gid, np.uint32))
+            owner.append(np.full(idx.shape[0], si, np.uint32))
+        for iid, pi, m in sc.get("instances", []):
+            l2w.append(np.asarray(m, np.float32)[:3, :4].reshape(12))
+            ids.append(iid)
+            holder.append(si)
+            proto.append(pi)
+    cat = lambda xs, dt, shape: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(shape, dt)
+    return (cat(verts, np.float32, (0, 9)), cat(prim, np.uint32, 0), cat(geom, np.uint32, 0), cat(owner, np.uint32, 0),
+            np.ascontiguousarray(np.array(l2w, np.float32).reshape(-1, 12)), np.array(ids, np.uint32),
+            np.array(holder, np.uint32), np.array(proto, np.uint32))
+
+
+def graph_intersect(scenes, top, rayhits, nthreads=None):
+    """The render oracle's per-scene-BVH instanced traversal (closest hit; instIDs are not written)."""
+    V, P, G, O, L, I, H, Q = _graph_arrays(scenes)
+    lib().oracle_graph_intersect(len(scenes), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(L), _p(I), _p(H), _p(Q),
+                                 L.shape[0], top, _p(rayhits), rayhits.shape[0], nthreads or threads())
+
+
+def graph_render(iscene, width, height, begin, end, max_bounces=8, seed=0x5E1A5000, deferred=False,
+                 samples_per_axis=4, nthreads=None, physical_nee=False):
+    """CPU oracle path tracer (deferred=False: shape (2, height, width, 3), passes [begin, end)) or deferred
+    path tracer (shape (height, width, 3), samples [begin, end)) over an InstancedRenderScene, PCG32 sampling;
+    FP64 sums."""
+    from selas_gb300.scenes import light_records, material_records
+    V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
+    mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
+    for part in iscene.parts:
+        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) + [0])
+        m = material_records(part.materials, count)
+        r, t = part.ptex_tables(m)
+        mats.append(m)
+        mat_off.append(mat_off[-1] + m.shape[0])
+        rows.append(r)
+        row_off.append(row_off[-1] + r.shape[0])
+        tex = t if r.shape[0] else np.zeros(0, np.uint16)
+        texels.append(tex)
+        tex_off.append(tex_off[-1] + tex.size // 3)
+    M = np.ascontiguousarray(np.concatenate(mats))
+    R = np.ascontiguousarray(np.concatenate(rows).astype(np.int32)).reshape(-1, 8)
+    T = np.ascontiguousarray(np.concatenate(texels + [np.zeros(3, np.uint16)]))
+    MO, RO, TO = np.array(mat_off, np.int32), np.array(row_off, np.int32), np.array(tex_off, np.int64)
+    top = iscene.parts[0]
+    lights, sets = light_records(top.lights)
+    bg = np.array(top.background, np.float32)
+    c = top.camera
+    cam = np.array(list(c["position"]) + list(c["look_at"]) + list(c["up"]) + [c["fov_degrees"]], np.float32)
+    out = np.zeros((height, width, 3) if deferred else (2, height, width, 3), np.float64)
+    lib().oracle_graph_render(len(iscene.parts), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(L), _p(I), _p(H), _p(Q),
+                              L.shape[0], 0, _p(M), _p(MO), _p(R), _p(RO), _p(T), _p(TO), _p(lights), lights.shape[0],
+                              _p(sets), sets.shape[0], _p(bg), _p(cam), width, height, begin, end, max_bounces, seed,
+                              nthreads or threads(), int(physical_nee), int(deferred), samples_per_axis, _p(out))
     return out
 
 

@@ -173,7 +173,10 @@ void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad
 }
 
 struct Scene {
-    const void* bvh;
+    const void* bvh = nullptr;
+    const void* graph = nullptr;                    // instanced scene graph (replaces bvh when set)
+    std::vector<std::vector<Material>> gmats;       // graph: materials of each scene, by geomID
+    std::vector<const orp::Texture*> gptex;         // graph: Ptex of each scene (null: none)
     const orp::Texture* ptex = nullptr;
     bool physical_nee = false;
     std::vector<Material> materials;
@@ -181,6 +184,20 @@ struct Scene {
     std::vector<uint32_t> set_first, set_count;
     V3 background;
 };
+
+bool sc_closest(const Scene& sc, const float* o, const float* d, float tnear, float tfar, orq::Hit& h) {
+    return sc.graph ? orq::closest_graph(sc.graph, o, d, tnear, tfar, h) : orq::closest(sc.bvh, o, d, tnear, tfar, h);
+}
+
+bool sc_occluded(const Scene& sc, const float* o, const float* d, float tnear, float tfar) {
+    return sc.graph ? orq::occluded_graph(sc.graph, o, d, tnear, tfar) : orq::occluded(sc.bvh, o, d, tnear, tfar);
+}
+
+// A vector through local-to-world rows (the device's fma chain).
+V3 xvector(const float* m, V3 v) {
+    return V3(std::fma(m[0], v.x, std::fma(m[1], v.y, m[2] * v.z)), std::fma(m[4], v.x, std::fma(m[5], v.y, m[6] * v.z)),
+              std::fma(m[8], v.x, std::fma(m[9], v.y, m[10] * v.z)));
+}
 
 V3 offset(V3 p, V3 n, float err, V3 dir, float scale) {
     const float side = orc::Dot(dir, n) < 0.0f ? -1.0f : 1.0f;
@@ -195,19 +212,26 @@ struct SurfHit {
     V3 n, view;
 };
 
+// Instanced hits (ModelDataFromRayIds, SceneResource.cpp:362-378): material and Ptex of the hit mesh's scene;
+// the object-space normal through the instances' localToWorld, innermost first (SurfaceParameters.cpp:161-168).
 void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) {
-    const Material& m = sc.materials[h.geom < sc.materials.size() ? h.geom : 0];
+    const std::vector<Material>& mats = sc.graph ? sc.gmats[h.scene] : sc.materials;
+    const orp::Texture* ptex = sc.graph ? sc.gptex[h.scene] : sc.ptex;
+    const Material& m = mats[h.geom < mats.size() ? h.geom : 0];
     o.m = &m;
     o.err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(pos.x), std::fabs(pos.y)), std::max(std::fabs(pos.z), h.t));
     orc::Surf& s = o.s;
-    const V3 n = orc::Norm(V3(h.ng[0], h.ng[1], h.ng[2]));
+    V3 ngv(h.ng[0], h.ng[1], h.ng[2]);
+    if (h.l2w[1]) ngv = xvector(h.l2w[1], ngv);
+    if (h.l2w[0]) ngv = xvector(h.l2w[0], ngv);
+    const V3 n = orc::Norm(ngv);
     V3 t, b;
     if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
     else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
     b = orc::Cross(n, t);
     s.t = t; s.n = n; s.b = b;
     float base[3] = {m.base[0], m.base[1], m.base[2]};
-    if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
     s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
     s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
@@ -241,7 +265,7 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
         }
         orq::Hit h;
         const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
-        const bool hit = orq::closest(sc.bvh, o, d, 0.0f, tfar, h);
+        const bool hit = sc_closest(sc, o, d, 0.0f, tfar, h);
         float ray_distance = tfar;
         V3 pos;
         if (hit) {
@@ -277,7 +301,7 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
                 if (orc::Dot(refl, V3(1.0f)) > 0) {
                     const V3 so = offset(pos, n, err, ldir, 0.1f);
                     const float soa[3] = {so.x, so.y, so.z}, lda[3] = {ldir.x, ldir.y, ldir.z};
-                    if (!orq::occluded(sc.bvh, soa, lda, err, ldist)) ld1 = ld1 + refl * lrad * (1.0f / lpdf) * thr;
+                    if (!sc_occluded(sc, soa, lda, err, ldist)) ld1 = ld1 + refl * lrad * (1.0f / lpdf) * thr;
                 }
             }
             // BSDF sample: uniforms drawn lazily, in order
@@ -388,7 +412,7 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
     for (uint32_t bounce = 0; bounce < max_bounces; ++bounce) {
         orq::Hit h;
         const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
-        if (!orq::closest(sc.bvh, o, d, 0.0f, 3.402823466e+38f, h)) {
+        if (!sc_closest(sc, o, d, 0.0f, 3.402823466e+38f, h)) {
             add(acc, sc.background * thr);
             break;
         }
@@ -415,7 +439,7 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
             if (orc::Dot(sample, V3(1.0f)) > 0) {
                 const V3 so = offset(pos, sh.n, sh.err, ldir, 0.1f);
                 const float soa[3] = {so.x, so.y, so.z}, lda[3] = {ldir.x, ldir.y, ldir.z};
-                if (!orq::occluded(sc.bvh, soa, lda, 0.0f, ldist)) add(acc, sample * thr);
+                if (!sc_occluded(sc, soa, lda, 0.0f, ldist)) add(acc, sample * thr);
             }
         }
         // background (SampleBackground -> BackgroundLightSample, AreaLighting.cpp:334-350: uniform sphere
@@ -433,7 +457,7 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
             if (orc::Dot(sample, V3(1.0f)) > 0) {
                 const V3 so = offset(pos, sh.n, sh.err, sdir, 0.1f);
                 const float soa[3] = {so.x, so.y, so.z}, sda[3] = {sdir.x, sdir.y, sdir.z};
-                if (!orq::occluded(sc.bvh, soa, sda, 0.0f, 1e36f)) add(acc, sample * thr);
+                if (!sc_occluded(sc, soa, sda, 0.0f, 1e36f)) add(acc, sample * thr);
             }
         }
         // BSDF sample, weighted against the background density 1 / (4 pi)
@@ -460,6 +484,88 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
 }
 
 }  // namespace
+
+// Per-pixel render loops shared by the flat and instanced entry points.
+static void run_pt(const Scene& sc, const float* camera, uint32_t width, uint32_t height, uint32_t pass_begin,
+            uint32_t pass_end, uint32_t max_bounces, uint64_t seed, int rng_mode, int threads, double* out) {
+    const Camera cam = make_camera(camera, width, height);
+    const uint32_t npix = width * height;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const uint32_t pix0 = next.fetch_add(16);
+            if (pix0 >= npix) break;
+            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
+                const uint32_t y = pixel / width, x = pixel - y * width;
+                Rng rng;
+                if (rng_mode == 1) {
+                    rng.pcg = false;
+                    rng.mt.seed(uint32_t(seed) + pixel);
+                }
+                double acc[6] = {0, 0, 0, 0, 0, 0};
+                for (uint32_t pass = pass_begin; pass < pass_end; ++pass) {
+                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(pass) * npix + pixel);
+                    const float vx = float(x) + rng.uniform();
+                    const float vy = float(y) + rng.uniform();
+                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
+                    const float cy = 1.0f - 2.0f * vy / cam.h;
+                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
+                    V3 l0, l1;
+                    evaluate_path(sc, rng, cam.pos, d, max_bounces, l0, l1);
+                    acc[0] += l0.x; acc[1] += l0.y; acc[2] += l0.z;
+                    acc[3] += l1.x; acc[4] += l1.y; acc[5] += l1.z;
+                }
+                for (int c = 0; c < 3; ++c) {
+                    out[size_t(pixel) * 3 + c] += acc[c];
+                    out[(size_t(npix) + pixel) * 3 + c] += acc[3 + c];
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    const int nt = std::max(1, threads);
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+}
+
+static void run_deferred(const Scene& sc, const float* camera, uint32_t width, uint32_t height, uint32_t samples_per_axis,
+                  uint32_t sample_begin, uint32_t sample_end, uint32_t max_bounces, uint64_t seed, int rng_mode,
+                  int threads, double* out) {
+    const Camera cam = make_camera(camera, width, height);
+    const uint32_t npix = width * height;
+    const int32_t m = int32_t(samples_per_axis);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const uint32_t pix0 = next.fetch_add(16);
+            if (pix0 >= npix) break;
+            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
+                const uint32_t y = pixel / width, x = pixel - y * width;
+                double acc[3] = {0, 0, 0};
+                Rng rng;
+                if (rng_mode == 1) {
+                    rng.pcg = false;
+                    rng.mt.seed(uint32_t(seed) + pixel);
+                }
+                for (uint32_t smp = sample_begin; smp < sample_end; ++smp) {
+                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(smp) * npix + pixel);
+                    float jx, jy;
+                    cmj(int32_t(smp), m, m, int32_t(pixel), jx, jy);
+                    const float vx = float(x) + jx, vy = float(y) + jy;
+                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
+                    const float cy = 1.0f - 2.0f * vy / cam.h;
+                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
+                    deferred_path(sc, rng, cam.pos, d, max_bounces, acc);
+                }
+                for (int c = 0; c < 3; ++c) out[size_t(pixel) * 3 + c] += acc[c];
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    const int nt = std::max(1, threads);
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& th : pool) th.join();
+}
 
 // Scene tables of the oracle renderers' common arguments; returns the Ptex texture to delete.
 static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
@@ -508,44 +614,7 @@ void oracle_pt_render(const float* verts, const uint32_t* prim, const uint32_t* 
     Scene sc;
     orp::Texture* tex = load_scene(sc, verts, prim, geom, ntri, materials, n_materials, lights, n_lights, sets, n_sets,
                                    background, ptex_rows, ptex_faces, ptex_texels, physical_nee);
-    const Camera cam = make_camera(camera, width, height);
-    const uint32_t npix = width * height;
-    std::atomic<uint32_t> next{0};
-    auto worker = [&]() {
-        for (;;) {
-            const uint32_t pix0 = next.fetch_add(16);
-            if (pix0 >= npix) break;
-            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
-                const uint32_t y = pixel / width, x = pixel - y * width;
-                Rng rng;
-                if (rng_mode == 1) {
-                    rng.pcg = false;
-                    rng.mt.seed(uint32_t(seed) + pixel);
-                }
-                double acc[6] = {0, 0, 0, 0, 0, 0};
-                for (uint32_t pass = pass_begin; pass < pass_end; ++pass) {
-                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(pass) * npix + pixel);
-                    const float vx = float(x) + rng.uniform();
-                    const float vy = float(y) + rng.uniform();
-                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
-                    const float cy = 1.0f - 2.0f * vy / cam.h;
-                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
-                    V3 l0, l1;
-                    evaluate_path(sc, rng, cam.pos, d, max_bounces, l0, l1);
-                    acc[0] += l0.x; acc[1] += l0.y; acc[2] += l0.z;
-                    acc[3] += l1.x; acc[4] += l1.y; acc[5] += l1.z;
-                }
-                for (int c = 0; c < 3; ++c) {
-                    out[size_t(pixel) * 3 + c] += acc[c];
-                    out[(size_t(npix) + pixel) * 3 + c] += acc[3 + c];
-                }
-            }
-        }
-    };
-    std::vector<std::thread> pool;
-    const int nt = std::max(1, threads);
-    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
-    for (auto& th : pool) th.join();
+    run_pt(sc, camera, width, height, pass_begin, pass_end, max_bounces, seed, rng_mode, threads, out);
     orq::release(const_cast<void*>(sc.bvh));
     delete tex;
 }
@@ -571,40 +640,8 @@ void oracle_deferred_render(const float* verts, const uint32_t* prim, const uint
     Scene sc;
     orp::Texture* tex = load_scene(sc, verts, prim, geom, ntri, materials, n_materials, lights, n_lights, sets, n_sets,
                                    background, ptex_rows, ptex_faces, ptex_texels, physical_nee);
-    const Camera cam = make_camera(camera, width, height);
-    const uint32_t npix = width * height;
-    const int32_t m = int32_t(samples_per_axis);
-    std::atomic<uint32_t> next{0};
-    auto worker = [&]() {
-        for (;;) {
-            const uint32_t pix0 = next.fetch_add(16);
-            if (pix0 >= npix) break;
-            for (uint32_t pixel = pix0; pixel < std::min(npix, pix0 + 16); ++pixel) {
-                const uint32_t y = pixel / width, x = pixel - y * width;
-                double acc[3] = {0, 0, 0};
-                Rng rng;
-                if (rng_mode == 1) {
-                    rng.pcg = false;
-                    rng.mt.seed(uint32_t(seed) + pixel);
-                }
-                for (uint32_t smp = sample_begin; smp < sample_end; ++smp) {
-                    if (rng_mode == 0) rng.seed_pcg(seed, uint64_t(smp) * npix + pixel);
-                    float jx, jy;
-                    cmj(int32_t(smp), m, m, int32_t(pixel), jx, jy);
-                    const float vx = float(x) + jx, vy = float(y) + jy;
-                    const float cx = (vx / cam.w) * 2.0f - 1.0f;
-                    const float cy = 1.0f - 2.0f * vy / cam.h;
-                    const V3 d = orc::Norm(cam.z - cx * cam.x + cy * cam.y);
-                    deferred_path(sc, rng, cam.pos, d, max_bounces, acc);
-                }
-                for (int c = 0; c < 3; ++c) out[size_t(pixel) * 3 + c] += acc[c];
-            }
-        }
-    };
-    std::vector<std::thread> pool;
-    const int nt = std::max(1, threads);
-    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
-    for (auto& th : pool) th.join();
+    run_deferred(sc, camera, width, height, samples_per_axis, sample_begin, sample_end, max_bounces, seed, rng_mode,
+                 threads, out);
     orq::release(const_cast<void*>(sc.bvh));
     delete tex;
 }
@@ -612,6 +649,54 @@ void oracle_deferred_render(const float* verts, const uint32_t* prim, const uint
 // Correlated multi-jittered sample points (for tests): n samples s = 0..n-1 of an m x m pattern with p.
 void oracle_cmj(int32_t m, int32_t p, int32_t n, float* xy) {
     for (int32_t s = 0; s < n; ++s) cmj(s, m, m, p, xy[2 * s], xy[2 * s + 1]);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// The path tracer (deferred = 0; out [2][height][width][3]) or the deferred path tracer (deferred = 1; out
+// [height][width][3]) over an instanced scene graph.  Triangles and instances as oracle_instanced_query (with
+// local-to-world rows); scene s has materials[mat_offsets[s] .. mat_offsets[s+1]) (32-word records by geomID)
+// and Ptex faces ptex_rows[row_offsets[s] ..) whose texel offsets are relative to texels + texel_offsets[s];
+// lights, light sets, background and camera are the top scene's.  PCG32 sampling.
+void oracle_graph_render(int n_scenes, const float* verts, const uint32_t* prim, const uint32_t* geom,
+                         const uint32_t* tri_scene, int64_t ntri, const float* l2w, const uint32_t* inst_id,
+                         const uint32_t* inst_scene, const uint32_t* inst_proto, int64_t ninst, int top,
+                         const float* materials, const int32_t* mat_offsets, const int32_t* ptex_rows,
+                         const int32_t* row_offsets, const uint16_t* texels, const int64_t* texel_offsets,
+                         const float* lights, int n_lights, const uint32_t* sets, int n_sets, const float* background,
+                         const float* camera, uint32_t width, uint32_t height, uint32_t begin, uint32_t end,
+                         uint32_t max_bounces, uint64_t seed, int threads, int physical_nee, int deferred,
+                         uint32_t samples_per_axis, double* out) {
+    Scene sc;
+    // lights, background and the top scene's tables through the flat loader (no triangles: the graph traces)
+    orp::Texture* unused = load_scene(sc, nullptr, nullptr, nullptr, 0, materials + 32 * mat_offsets[top],
+                                      mat_offsets[top + 1] - mat_offsets[top], lights, n_lights, sets, n_sets, background,
+                                      nullptr, 0, nullptr, physical_nee);
+    delete unused;
+    if (sc.bvh) orq::release(const_cast<void*>(sc.bvh));
+    sc.bvh = nullptr;
+    sc.graph = orq::build_graph(n_scenes, verts, prim, geom, tri_scene, ntri, l2w, inst_id, inst_scene, inst_proto,
+                                ninst, top);
+    std::vector<orp::Texture*> owned;
+    for (int s = 0; s < n_scenes; ++s) {
+        std::vector<Material> mats;
+        for (int i = mat_offsets[s]; i < mat_offsets[s + 1]; ++i) mats.push_back(read_material(materials + 32 * i));
+        if (mats.empty()) mats.push_back(read_material(materials + 32 * mat_offsets[top]));
+        sc.gmats.push_back(mats);
+        const int nf = row_offsets[s + 1] - row_offsets[s];
+        orp::Texture* t = nf > 0 ? new orp::Texture(ptex_rows + 8 * row_offsets[s], nf, texels + 3 * texel_offsets[s])
+                                 : nullptr;
+        owned.push_back(t);
+        sc.gptex.push_back(t);
+    }
+    if (deferred)
+        run_deferred(sc, camera, width, height, samples_per_axis, begin, end, max_bounces, seed, 0, threads, out);
+    else
+        run_pt(sc, camera, width, height, begin, end, max_bounces, seed, 0, threads, out);
+    orq::release_graph(const_cast<void*>(sc.graph));
+    for (orp::Texture* t : owned) delete t;
 }
 
 }  // extern "C"

@@ -576,4 +576,215 @@ bool occluded(const void* h, const float* org, const float* dir, float tnear, fl
     return trace<true>(bvh, r, best);
 }
 
+// ---------------------------------------------------------------------------------------------------
+// Instanced graphs with per-scene BVHs (the render oracle's form of oracle_instanced_query)
+// ---------------------------------------------------------------------------------------------------
+namespace {
+
+struct GInst {
+    float w2l[12], l2w[12];
+    uint32_t id, proto;
+    Box box;  // world box in the owning scene's frame, padded generously (culling only)
+};
+struct GScene {
+    Bvh* bvh = nullptr;
+    std::vector<GInst> insts;
+    Box bounds;
+};
+struct Graph {
+    std::vector<GScene> scenes;
+    uint32_t top = 0;
+    ~Graph() {
+        for (GScene& s : scenes) delete s.bvh;
+    }
+};
+struct GBest {
+    float t = 0, u = 0, v = 0;
+    const Tri* tri = nullptr;
+    uint64_t inst = ~0ull, key = ~0ull;
+    uint32_t scene = 0;
+    const float* l2w[2] = {nullptr, nullptr};
+    uint64_t updates = 0;
+};
+
+void scene_bounds(Graph& G, uint32_t s, std::vector<int>& done) {
+    if (done[s]) return;
+    GScene& S = G.scenes[s];
+    S.bounds.reset();
+    if (S.bvh && !S.bvh->nodes.empty()) S.bounds.grow(S.bvh->nodes[0].box);
+    for (GInst& in : S.insts) {
+        scene_bounds(G, in.proto, done);
+        const Box& pb = G.scenes[in.proto].bounds;
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = 0; k < 8; ++k) {
+            const double p[3] = {(k & 1) ? pb.hi[0] : pb.lo[0], (k & 2) ? pb.hi[1] : pb.lo[1], (k & 4) ? pb.hi[2] : pb.lo[2]};
+            for (int r = 0; r < 3; ++r) {
+                const double w = double(in.l2w[4 * r]) * p[0] + double(in.l2w[4 * r + 1]) * p[1] +
+                                 double(in.l2w[4 * r + 2]) * p[2] + double(in.l2w[4 * r + 3]);
+                lo[r] = std::min(lo[r], w);
+                hi[r] = std::max(hi[r], w);
+            }
+        }
+        for (int r = 0; r < 3; ++r) {
+            const double pad = (std::max(std::fabs(lo[r]), std::fabs(hi[r])) + (hi[r] - lo[r])) * 1e-3 + 1e-20;
+            in.box.lo[r] = float(lo[r] - pad);
+            in.box.hi[r] = float(hi[r] + pad);
+        }
+        S.bounds.grow(in.box);
+    }
+    done[s] = 1;
+}
+
+// Closest hit in scene s at instance level `level`, merged into `best` by (t, instance ids, geomID, primID).
+void gclosest(const Graph& G, uint32_t s, const float* o, const float* d, float tnear, float& tfar, uint64_t cur,
+              int level, const float* chain0, GBest& best) {
+    const GScene& S = G.scenes[s];
+    if (S.bvh && !S.bvh->nodes.empty()) {
+        Ray r;
+        std::memcpy(r.org, o, 12);
+        std::memcpy(r.dir, d, 12);
+        r.tnear = tnear;
+        r.tfar = tfar;
+        Best b;
+        if (trace<false>(*S.bvh, r, b)) {
+            const uint64_t k = b.key;
+            if (b.t < tfar || cur < best.inst || (cur == best.inst && k < best.key)) {
+                tfar = b.t;
+                best.t = b.t; best.u = b.u; best.v = b.v;
+                best.tri = &S.bvh->tris[size_t(b.tri)];
+                best.inst = cur;
+                best.key = k;
+                best.scene = s;
+                best.l2w[0] = chain0;
+                best.l2w[1] = nullptr;
+                ++best.updates;
+            }
+        }
+    }
+    if (level >= 2) return;
+    for (const GInst& in : S.insts) {
+        float tmin;
+        if (!box_hit(in.box, o, d, tnear, tfar, tmin)) continue;
+        float o2[3], d2[3];
+        xpoint(in.w2l, o, o2);
+        xvector(in.w2l, d, d2);
+        if (untraceable(o2, d2)) continue;
+        const uint64_t ci = level == 0 ? ((uint64_t(in.id) << 32) | 0xffffffffull) : ((cur & 0xffffffff00000000ull) | in.id);
+        const uint64_t before = best.updates;
+        gclosest(G, in.proto, o2, d2, tnear, tfar, ci, level + 1, level == 0 ? in.l2w : chain0, best);
+        if (level == 1 && best.updates != before) best.l2w[1] = in.l2w;  // the best hit lies in this inner instance
+    }
+}
+
+bool goccluded(const Graph& G, uint32_t s, const float* o, const float* d, float tnear, float tfar, int level) {
+    const GScene& S = G.scenes[s];
+    if (S.bvh && !S.bvh->nodes.empty()) {
+        Ray r;
+        std::memcpy(r.org, o, 12);
+        std::memcpy(r.dir, d, 12);
+        r.tnear = tnear;
+        r.tfar = tfar;
+        Best b;
+        if (trace<true>(*S.bvh, r, b)) return true;
+    }
+    if (level >= 2) return false;
+    for (const GInst& in : S.insts) {
+        float tmin;
+        if (!box_hit(in.box, o, d, tnear, tfar, tmin)) continue;
+        float o2[3], d2[3];
+        xpoint(in.w2l, o, o2);
+        xvector(in.w2l, d, d2);
+        if (untraceable(o2, d2)) continue;
+        if (goccluded(G, in.proto, o2, d2, tnear, tfar, level + 1)) return true;
+    }
+    return false;
+}
+
+}  // namespace
+
+void* build_graph(int n_scenes, const float* verts, const uint32_t* prim, const uint32_t* geom,
+                  const uint32_t* tri_scene, int64_t ntri, const float* l2w, const uint32_t* inst_id,
+                  const uint32_t* inst_scene, const uint32_t* inst_proto, int64_t ninst, int top) {
+    Graph* G = new Graph();
+    G->scenes.resize(size_t(std::max(n_scenes, 1)));
+    G->top = uint32_t(top);
+    std::vector<std::vector<int64_t>> members(G->scenes.size());
+    for (int64_t i = 0; i < ntri; ++i) members[tri_scene[i]].push_back(i);
+    for (size_t s = 0; s < G->scenes.size(); ++s) {
+        if (members[s].empty()) continue;
+        std::vector<float> v;
+        std::vector<uint32_t> p, g;
+        for (int64_t i : members[s]) {
+            v.insert(v.end(), verts + 9 * i, verts + 9 * i + 9);
+            p.push_back(prim[i]);
+            g.push_back(geom[i]);
+        }
+        G->scenes[s].bvh = static_cast<Bvh*>(oracle_bvh_build(v.data(), p.data(), g.data(), int64_t(p.size())));
+    }
+    for (int64_t i = 0; i < ninst; ++i) {
+        GInst in;
+        std::memcpy(in.l2w, l2w + 12 * i, 48);
+        oracle_affine_inverse(in.l2w, in.w2l);
+        in.id = inst_id[i];
+        in.proto = inst_proto[i];
+        G->scenes[inst_scene[i]].insts.push_back(in);
+    }
+    std::vector<int> done(G->scenes.size(), 0);
+    for (uint32_t s = 0; s < G->scenes.size(); ++s) scene_bounds(*G, s, done);
+    return G;
+}
+
+bool closest_graph(const void* g, const float* org, const float* dir, float tnear, float tfar, Hit& out) {
+    const Graph& G = *static_cast<const Graph*>(g);
+    if (untraceable(org, dir)) return false;
+    GBest best;
+    gclosest(G, G.top, org, dir, tnear, tfar, ~0ull, 0, nullptr, best);
+    if (!best.tri) return false;
+    out.t = best.t;
+    out.u = best.u;
+    out.v = best.v;
+    normal(*best.tri, out.ng);
+    out.prim = best.tri->prim;
+    out.geom = best.tri->geom;
+    out.scene = best.scene;
+    out.l2w[0] = best.l2w[0];
+    out.l2w[1] = best.l2w[1];
+    return true;
+}
+
+bool occluded_graph(const void* g, const float* org, const float* dir, float tnear, float tfar) {
+    const Graph& G = *static_cast<const Graph*>(g);
+    if (untraceable(org, dir)) return false;
+    return goccluded(G, G.top, org, dir, tnear, tfar, 0);
+}
+
+void release_graph(void* g) { delete static_cast<Graph*>(g); }
+
 }  // namespace orq
+
+extern "C" {
+
+// The render oracle's instanced traversal (per-scene BVHs) on SelRayHit records, to check it against the
+// brute-force instanced query.  Arguments as oracle_instanced_query, with local-to-world rows.
+void oracle_graph_intersect(int n_scenes, const float* verts, const uint32_t* prim, const uint32_t* geom,
+                            const uint32_t* tri_scene, int64_t ntri, const float* l2w, const uint32_t* inst_id,
+                            const uint32_t* inst_scene, const uint32_t* inst_proto, int64_t ninst, int top, void* rayhits,
+                            int64_t m, int threads) {
+    void* g = orq::build_graph(n_scenes, verts, prim, geom, tri_scene, ntri, l2w, inst_id, inst_scene, inst_proto,
+                               ninst, top);
+    RayHit* rh = static_cast<RayHit*>(rayhits);
+    parallel_for(m, threads, [&](int64_t i) {
+        orq::Hit h;
+        if (!orq::closest_graph(g, rh[i].ray.org, rh[i].ray.dir, rh[i].ray.tnear, rh[i].ray.tfar, h)) return;
+        rh[i].ray.tfar = h.t;
+        std::memcpy(rh[i].ng, h.ng, 12);
+        rh[i].u = h.u;
+        rh[i].v = h.v;
+        rh[i].prim = h.prim;
+        rh[i].geom = h.geom;
+        rh[i].inst[0] = rh[i].inst[1] = 0xffffffffu;
+    });
+    orq::release_graph(g);
+}
+
+}  // extern "C"

@@ -302,7 +302,7 @@ int finish_instances(SelSceneTy* scene, uint32_t levels, uint32_t below) {
         r.nodes = ii.scene->d_nodes;
         r.tris = ii.scene->d_tris;
         r.insts = static_cast<const InstanceRecord*>(ii.scene->d_insts);
-        r.shading = nullptr;
+        r.shading = ii.scene->d_view;
         r.instID = ii.instID;
     }
     if (n) {
@@ -351,6 +351,15 @@ extern "C" int sel_scene_commit(SelScene scene) {
     if (rc != SEL_OK) {
         scene->committed = false;
         return rc;
+    }
+    if (!scene->d_view) {
+        cudaError_t e = cudaMalloc(&scene->d_view, sizeof(ShadeView));
+        if (e == cudaSuccess) e = cudaMemset(scene->d_view, 0, sizeof(ShadeView));
+        if (e != cudaSuccess) {
+            scene->d_view = nullptr;
+            return cuda_fail(e, "cudaMalloc(shading view)");
+        }
+        scene->shading_dirty = true;  // the view is written by the next shading upload
     }
     ++scene->generation;
     scene->committed = true;
@@ -455,7 +464,7 @@ int sel_scene_release(SelScene scene) {
     for (auto& r : scene->referenced) --r.first->instanced_by;
     for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
                     scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
-                    scene->vcm_block, scene->d_insts})
+                    scene->vcm_block, scene->d_insts, scene->d_view})
         if (p) cudaFree(p);
     delete scene;
     return SEL_OK;

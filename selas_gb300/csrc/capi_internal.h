@@ -35,6 +35,9 @@ struct SelSceneTy {
     };
     std::vector<InstanceInput> instances;
     void* d_insts = nullptr;                  // InstanceRecord[instances] of the last commit
+    void* d_view = nullptr;                   // ShadeView of this scene (allocated by the first commit)
+    uint32_t class_mask = 0;                  // material classes of the meshes (bit shader * 4 + Ptex * 2 + transp.)
+    bool sort_hint_ptex = false;              // a material of this scene uses Ptex
     uint32_t inst_levels = 0;                 // instance levels below this scene at the last commit (0..2)
     uint32_t stack_need = 0;                  // worst-case instanced-traversal stack entries from here down
     uint64_t generation = 0;                  // incremented by every commit
@@ -91,6 +94,8 @@ float vcm_default_radius(const SelSceneTy* sc);
 void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c);
 void vcm_lights(const SelSceneTy* sc, VcmSettings& set);
 int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
+// capi.cpp: every scene instanced (directly or below) is still the one committed when `sc` was committed
+bool instances_fresh(const SelSceneTy* sc);
 // Deferred path tracer: check_render_args plus samplesPerPixel = m * m (m <= 256) and maxBounces 1..1024.
 int check_deferred_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
 uint32_t deferred_axis(const SelPtSettings& settings);

@@ -208,6 +208,13 @@ __device__ __forceinline__ bool inst_step(InstState& s, uint2* stack, int stride
     return false;
 }
 
+// Render-kernel policy of the instanced traversal (the flat layouts are Tracer<0> and Tracer<1>).
+template <>
+struct Tracer<2> {
+    using Entry = uint2;
+    static constexpr int kDepth = kInstStack;
+};
+
 // Whole-ray form (one thread, one ray) over a scene with instances.
 template <bool kAnyHit>
 __device__ __forceinline__ bool trace_instanced(const uint4* __restrict__ nodes, const float4* __restrict__ tris,

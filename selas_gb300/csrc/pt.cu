@@ -29,6 +29,7 @@
 #include "capi_internal.h"
 #include "cmj.cuh"
 #include "graph.h"
+#include "instance.cuh"
 #include "ptex.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
@@ -162,10 +163,79 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
     }
 }
 
+// Instances entered to a hit, as 1 + index in the parent's instance table (0: none).
+__device__ __forceinline__ uint2 inst_indices(const PtScene& sc, const InstHit& h) {
+    const uint32_t a = h.rec[0] ? uint32_t(h.rec[0] - sc.insts) + 1u : 0u;
+    const uint32_t b = h.rec[1] ? uint32_t(h.rec[1] - h.rec[0]->insts) + 1u : 0u;
+    return make_uint2(a, b);
+}
+
+// A hit's leaf record and the shading data of the scene whose mesh was hit: the job's scene, or the scene of
+// the innermost instance entered (ModelDataFromRayIds, SceneResource.cpp:362-378).
+struct HitRef {
+    const float4* tp;
+    const MaterialDev* mats;
+    uint32_t mat_count;
+    uint32_t ptex_count;
+    const void* ptex_faces;
+    const void* ptex_texels;
+    const InstanceRecord* rec0;
+    const InstanceRecord* rec1;
+};
+
+template <bool kInst>
+__device__ __forceinline__ HitRef hit_ref(const PtState& st, const PtScene& S, uint32_t s, uint32_t tri) {
+    HitRef r;
+    r.rec0 = r.rec1 = nullptr;
+    const float4* tris = S.tris;
+    r.mats = S.materials;
+    r.mat_count = S.material_count;
+    r.ptex_faces = S.ptex_faces;
+    r.ptex_texels = S.ptex_texels;
+    r.ptex_count = S.ptex_face_count;
+    if (kInst) {
+        const uint2 hi = st.hinst[s];
+        if (hi.x) {
+            r.rec0 = S.insts + (hi.x - 1u);
+            const InstanceRecord* in = r.rec0;
+            if (hi.y) {
+                r.rec1 = r.rec0->insts + (hi.y - 1u);
+                in = r.rec1;
+            }
+            tris = static_cast<const float4*>(in->tris);
+            const ShadeView* v = static_cast<const ShadeView*>(in->shading);
+            r.mats = v->materials;
+            r.mat_count = v->material_count;
+            r.ptex_faces = v->ptex_faces;
+            r.ptex_texels = v->ptex_texels;
+            r.ptex_count = v->ptex_face_count;
+        }
+    }
+    r.tp = tris + size_t(tri) * 3;
+    return r;
+}
+
+// World normal of a hit: the object-space normal through the entered instances' local-to-world rows,
+// innermost first (CalculateSurfaceParams transforms Ng by the composed localToWorld,
+// SurfaceParameters.cpp:161-168; not the inverse transpose).
+__device__ __forceinline__ float3 world_normal(const HitRef& r, float3 ng) {
+    const InstanceRecord* recs[2] = {r.rec1, r.rec0};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (!recs[k]) continue;
+        const float4* m = reinterpret_cast<const float4*>(recs[k]->l2w);
+        const float4 r0 = __ldg(m), r1 = __ldg(m + 1), r2 = __ldg(m + 2);
+        float x, y, z;
+        xform_vector(r0, r1, r2, ng.x, ng.y, ng.z, x, y, z);
+        ng = make_float3(x, y, z);
+    }
+    return ng;
+}
+
 // Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
-// so expensive and cheap rays balance across the GPU.
+// so expensive and cheap rays balance across the GPU.  K = 2: the instanced traversal of the 8-wide layout.
 template <int K, int B>
-__global__ void __launch_bounds__(B, 1024 / B) k_extend(PtParams P, int cur) {
+__global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_extend(PtParams P, int cur) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
@@ -199,12 +269,21 @@ __global__ void __launch_bounds__(B, 1024 / B) k_extend(PtParams P, int cur) {
             QueryRay q;
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = tfar;
-            QueryHit h;
             const PtScene& sc = P.st.jobs[P.st.job[s]].scene;
-            const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x, B,
-                                                                status);
-            P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
-                                : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+            if constexpr (K == 2) {
+                InstHit h;
+                const bool found = trace_instanced<false>(static_cast<const uint4*>(sc.nodes), sc.tris, sc.insts, q,
+                                                          h, stack_mem + threadIdx.x, B, status);
+                P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                    : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+                P.st.hinst[s] = found ? inst_indices(sc, h) : make_uint2(0u, 0u);
+            } else {
+                QueryHit h;
+                const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x,
+                                                                    B, status);
+                P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                    : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+            }
         }
     }
     if (status) atomicOr(P.err, status);
@@ -212,12 +291,14 @@ __global__ void __launch_bounds__(B, 1024 / B) k_extend(PtParams P, int cur) {
 
 // Material class of a queued path's hit: 0 miss; else 1 + shader * 4 + 2 (Ptex) + 1 (transparent).  Paths
 // are counting-sorted by class before shading, so a warp shades one kind of surface.
+template <bool kInst>
 __device__ __forceinline__ uint32_t material_class(const PtParams& P, uint32_t s) {
     const uint32_t tri = __float_as_uint(P.st.hit[s].w);
     if (tri == 0xffffffffu) return 0u;
     const PtScene& S = P.st.jobs[P.st.job[s]].scene;
-    const uint32_t geom = __float_as_uint(__ldg(S.tris + size_t(tri) * 3 + 1).w);
-    const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
+    const HitRef r = hit_ref<kInst>(P.st, S, s, tri);
+    const uint32_t geom = __float_as_uint(__ldg(r.tp + 1).w);
+    const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
     const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
     return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
 }
@@ -226,12 +307,13 @@ __global__ void k_class_reset(uint32_t* counters) {
     if (threadIdx.x < 2 * kPtClasses) counters[32 + threadIdx.x] = 0u;
 }
 
+template <bool kInst>
 __global__ void __launch_bounds__(kBlock) k_classify(PtParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
         const bool valid = e < n;
-        const uint32_t c = valid ? material_class(P, P.st.queue[cur][e]) : 0xffu;
+        const uint32_t c = valid ? material_class<kInst>(P, P.st.queue[cur][e]) : 0xffu;
         if (valid) P.st.cls[e] = c;
         const uint32_t peers = __match_any_sync(0xffffffffu, c);
         const uint32_t lane = threadIdx.x & 31u;
@@ -267,6 +349,7 @@ __global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
 
 // Ptex base colour of the sorted paths whose hit material is textured (SurfaceParameters.cpp:196-206): a
 // kernel of its own keeps the filter's code out of the shading kernel.
+template <bool kInst>
 __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
@@ -276,15 +359,15 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
         const uint32_t tri = __float_as_uint(hit.w);
         if (tri == 0xffffffffu) continue;
         const PtScene& S = P.st.jobs[P.st.job[s]].scene;
-        const float4* tp = S.tris + size_t(tri) * 3;
-        const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1);
+        const HitRef r = hit_ref<kInst>(P.st, S, s, tri);
+        const float4 p0 = __ldg(r.tp), p1 = __ldg(r.tp + 1);
         const uint32_t geom = __float_as_uint(p1.w);
-        const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
+        const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
         if (!(m.flags & kMaterialUsesPtex)) continue;
         float3 base = ld3(m.base_color);
         uint32_t pstatus = 0;
-        ptex_eval(static_cast<const PtexFace*>(S.ptex_faces), int(S.ptex_face_count),
-                  static_cast<const __half*>(S.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z,
+        ptex_eval(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count),
+                  static_cast<const __half*>(r.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z,
                   base, pstatus);
         status |= pstatus;
         P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
@@ -294,7 +377,7 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
 
 // kModes: bit 0 path-tracer jobs, bit 1 deferred jobs in the batch (a single-mode batch compiles the other
 // integrator out of the kernel).
-template <uint32_t kModes>
+template <uint32_t kModes, bool kInst>
 __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     const int next = cur ^ 1;
@@ -332,11 +415,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
             }
             bool alive = true;
             if (tri != 0xffffffffu) {
-                const float4* tp = S.tris + size_t(tri) * 3;
-                const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-                const float3 ng = triangle_ng(p0, p1, p2);
+                const HitRef hr = hit_ref<kInst>(P.st, S, s, tri);
+                const float4 p0 = __ldg(hr.tp), p1 = __ldg(hr.tp + 1), p2 = __ldg(hr.tp + 2);
+                const float3 ng = kInst ? world_normal(hr, triangle_ng(p0, p1, p2)) : triangle_ng(p0, p1, p2);
                 const uint32_t geom = __float_as_uint(p1.w);
-                const MaterialDev& m = S.materials[geom < S.material_count ? geom : 0];
+                const MaterialDev& m = hr.mats[geom < hr.mat_count ? geom : 0];
                 // RayPick error bound (PathTracer.cpp:134-136)
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
@@ -499,7 +582,8 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
 }
 
 template <int K, int B>
-__global__ void __launch_bounds__(B, 1024 / B) k_shadow(PtParams P) {
+__global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_shadow(PtParams P) {
+    static_assert(K != 2 || B == 128, "the instanced stack fills the static shared memory at 128 threads");
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
@@ -518,9 +602,17 @@ __global__ void __launch_bounds__(B, 1024 / B) k_shadow(PtParams P) {
             QueryRay q;
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
-            QueryHit h;
-            if (!Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, B,
-                                                 status))
+            bool blocked;
+            if constexpr (K == 2) {
+                InstHit h;
+                blocked = trace_instanced<true>(static_cast<const uint4*>(J.scene.nodes), J.scene.tris, J.scene.insts,
+                                                q, h, stack_mem + threadIdx.x, B, status);
+            } else {
+                QueryHit h;
+                blocked = Tracer<K>::template trace<true>(J.scene.nodes, J.scene.tris, q, h, stack_mem + threadIdx.x, B,
+                                                          status);
+            }
+            if (!blocked)
                 accumulate(J.accum, J.cam.width * J.cam.height, J.mode == kPtModeDeferred ? 0 : 1, tag & 0x0fffffffu,
                            f3(c.x, c.y, c.z));
         }
@@ -546,6 +638,7 @@ void pt_layout(PtState& st, Take take, uint32_t paths) {
     st.thr = reinterpret_cast<float4*>(take(16ull * paths));
     st.medium = reinterpret_cast<float4*>(take(16ull * paths));
     st.hit = reinterpret_cast<float4*>(take(16ull * paths));
+    st.hinst = reinterpret_cast<uint2*>(take(8ull * paths));
     st.pixel = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.job = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.path_id = reinterpret_cast<uint64_t*>(take(8ull * paths));
@@ -588,10 +681,11 @@ size_t pt_state_block_bytes(uint32_t paths) {
 }
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
-                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes) {
-    // 256-thread traversal blocks only for the 8-wide layout (its 24-entry stack then fills the 48 KB of
-    // static shared memory; the binary layout's 64-entry stack would not fit)
-    const int tb = (trace_block == 256 && bvh_kind == 0) ? 256 : 128;
+                           uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
+                           bool instanced) {
+    // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
+    // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
+    const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -608,21 +702,31 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         for (uint32_t b = 0; b < bounces; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, s>>>(st.counters, cur ^ 1);
-            if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
+            if (instanced) k_extend<2, 128><<<trace_grid, tb, 0, s>>>(P, cur);
+            else if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
             else if (bvh_kind == 0) k_extend<0, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             else k_extend<1, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             if (sort) {
                 k_class_reset<<<1, 32, 0, s>>>(st.counters);
-                k_classify<<<shade_grid, kBlock, 0, s>>>(P, cur);
+                if (instanced) k_classify<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                else k_classify<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 k_class_offsets<<<1, 32, 0, s>>>(st.counters);
                 k_class_scatter<<<shade_grid, kBlock, 0, s>>>(P, cur);
-                k_texture<<<shade_grid, kBlock, 0, s>>>(P, cur);
+                if (instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                else k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
             }
             const uint32_t* q = sort ? st.queue_sorted : st.queue[cur];
-            if (modes == 2u) k_shade<2><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-            else if (modes == 3u) k_shade<3><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-            else k_shade<1><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-            if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
+            if (instanced) {
+                if (modes == 2u) k_shade<2, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else if (modes == 3u) k_shade<3, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else k_shade<1, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+            } else {
+                if (modes == 2u) k_shade<2, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else if (modes == 3u) k_shade<3, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else k_shade<1, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+            }
+            if (instanced) k_shadow<2, 128><<<trace_grid, tb, 0, s>>>(P);
+            else if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0) k_shadow<0, 128><<<trace_grid, tb, 0, s>>>(P);
             else k_shadow<1, 128><<<trace_grid, tb, 0, s>>>(P);
         }
@@ -633,7 +737,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes;
+        uint32_t modes, instanced;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -643,6 +747,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.sort = sort ? 1u : 0u;
     key.tb = tb;
     key.modes = modes;
+    key.instanced = instanced ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -667,7 +772,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     if (e != cudaSuccess) return e;
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
-                          trace_block, set.mode == kPtModeDeferred ? 2u : 1u);
+                          trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

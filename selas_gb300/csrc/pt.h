@@ -12,6 +12,7 @@ namespace sel {
 
 struct MaterialDev;
 struct QuadLight;
+struct InstanceRecord;
 
 constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
                                 // [8] holds the current batch size, [32..47] material-class counts,
@@ -34,6 +35,7 @@ struct PtScene {
     uint32_t ptex_face_count;
     float background[3];
     uint32_t sort_hint;  // 1: the scene has Ptex materials or several material classes (sort before shading)
+    const InstanceRecord* insts;  // instance table (null: no instances); lights and background stay this scene's
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.
@@ -84,6 +86,7 @@ struct PtState {
     float4* thr;      // throughput, isDeltaOnly
     float4* medium;   // phase (0 vacuum / 1 isotropic), extinction
     float4* hit;      // t, u, v, triangle (bits; all ones = miss)
+    uint2* hinst;     // instances entered to the hit, as 1 + index in the parent's table (0: none)
     uint32_t* pixel;
     uint32_t* job;    // job slot of the path
     uint64_t* path_id;  // index of the path within its job (its PCG32 stream)
@@ -112,9 +115,10 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // (required when a job's scene uses Ptex).
 // `trace_block`: threads per block of the traversal kernels (128, or 256 with the 8-wide layout).
 // `modes`: integrators of the jobs, bit 0 kPtModePath, bit 1 kPtModeDeferred.
+// `instanced`: a job's scene has instances (the instanced traversal, which also walks flat scenes).
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128,
-                           uint32_t modes = 1u);
+                           uint32_t modes = 1u, bool instanced = false);
 
 // Single render (PathTracer::GenerateImage, or DeferredPathTracer::GenerateImage with set.mode =
 // kPtModeDeferred): one job, batches until all its paths are done.

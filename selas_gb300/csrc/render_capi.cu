@@ -67,8 +67,24 @@ int upload(void*& dst, const T* src, size_t count) {
 
 namespace sel {
 
+// Material classes (bit shader * 4 + Ptex * 2 + transparent) and Ptex use of a scene and the scenes its
+// instances reference.
+void tree_classes(const SelSceneTy* sc, uint32_t& mask, bool& ptex) {
+    mask |= sc->class_mask;
+    ptex |= sc->sort_hint_ptex;
+    for (const auto& r : sc->referenced) tree_classes(r.first, mask, ptex);
+}
+
 int sync_shading(SelSceneTy* sc) {
-    if (!sc->shading_dirty) return SEL_OK;
+    for (const auto& r : sc->referenced)  // instanced scenes first: their views must be current
+        if (int rc = sync_shading(r.first)) return rc;
+    if (!sc->shading_dirty) {
+        uint32_t mask = 0;
+        bool ptex = false;
+        tree_classes(sc, mask, ptex);
+        sc->sort_hint = (ptex || __builtin_popcount(mask) > 1) ? 1u : 0u;
+        return SEL_OK;
+    }
     uint32_t max_geom = 0;
     for (const MeshInput& m : sc->meshes) max_geom = m.geomID + 1 > max_geom ? m.geomID + 1 : max_geom;
     if (max_geom > kMaxGeom) return fail(SEL_ERR_INVALID_OPERATION, "rendering needs geomIDs below 65536");
@@ -111,7 +127,11 @@ int sync_shading(SelSceneTy* sc) {
         }
         bool ptex = false;
         for (const auto& m : mats) ptex |= (m.flags & kMaterialUsesPtex) != 0;
-        sc->sort_hint = (ptex || __builtin_popcount(seen) > 1) ? 1u : 0u;
+        sc->class_mask = seen;
+        sc->sort_hint_ptex = ptex;
+        uint32_t mask = 0;
+        tree_classes(sc, mask, ptex);
+        sc->sort_hint = (ptex || __builtin_popcount(mask) > 1) ? 1u : 0u;
     }
     if (int rc = upload(sc->d_ptex_faces, faces.data(), faces.size())) return rc;
     if (int rc = upload(sc->d_ptex_texels, texels.data(), texels.size())) return rc;
@@ -119,6 +139,16 @@ int sync_shading(SelSceneTy* sc) {
     if (int rc = upload(sc->d_materials, mats.data(), mats.size())) return rc;
     if (int rc = upload(sc->d_lights, lights.data(), lights.size())) return rc;
     if (int rc = upload(sc->d_light_sets, sets.data(), sets.size())) return rc;
+    if (sc->d_view) {
+        ShadeView v;
+        v.materials = static_cast<const MaterialDev*>(sc->d_materials);
+        v.ptex_faces = sc->d_ptex_faces;
+        v.ptex_texels = sc->d_ptex_texels;
+        v.material_count = uint32_t(mats.size());
+        v.ptex_face_count = sc->ptex_face_count;
+        cudaError_t e = cudaMemcpy(sc->d_view, &v, sizeof(v), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "shading view");
+    }
     sc->shading_dirty = false;
     return SEL_OK;
 }
@@ -145,6 +175,8 @@ namespace sel {
 int check_render_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    if (!instances_fresh(scene))
+        return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene changed since this scene was committed");
     if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
         return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
@@ -198,6 +230,7 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
     ps.sort_hint = sc->sort_hint;
+    ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     return ps;
 }
 
@@ -283,6 +316,7 @@ namespace sel {
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    if (scene->d_insts) return fail(SEL_ERR_INVALID_OPERATION, "VCM renders scenes without instances");
     if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
         return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))

@@ -28,6 +28,17 @@ struct MaterialDev {
 };
 static_assert(sizeof(MaterialDev) == 128, "MaterialDev must be 128 bytes");
 
+// Shading data of one scene as the integrators read it for hits inside instances of that scene (the model data
+// ModelDataFromRayIds finds, SceneResource.cpp:362-378): one fixed device record per scene, rewritten whenever
+// the scene's shading data is uploaded, so instance records can point at it.
+struct ShadeView {
+    const MaterialDev* materials;
+    const void* ptex_faces;   // PtexFace[]
+    const void* ptex_texels;  // half RGB
+    uint32_t material_count;
+    uint32_t ptex_face_count;
+};
+
 constexpr uint32_t kMaterialTransparent = 1u;  // DisneySolid with diffTrans or specTrans (BuildModel.cpp:60-65)
 constexpr uint32_t kMaterialUsesPtex = 2u;
 

@@ -481,3 +481,198 @@ def orbit_camera(camera: dict, yaw: float) -> dict:
     cs, sn = np.cos(yaw), np.sin(yaw)
     q = c + np.array([cs * d[0] + sn * d[2], d[1], -sn * d[0] + cs * d[2]])
     return {**camera, "position": tuple(float(x) for x in q)}
+
+
+# ---------------------------------------------------------------------------------------------------
+# Instanced scenes (two levels: scene -> instances of scenes -> their instances)
+# ---------------------------------------------------------------------------------------------------
+@dataclass
+class InstancedRenderScene:
+    """Render scenes linked by instances.  parts[0] is the world: its lights, background and camera are the
+    render's; instances[i] lists (instID, index of the instanced part, local-to-world 3 x 4 or 4 x 4) attached
+    to part i.  A part's materials and Ptex belong to its own meshes (ModelDataFromRayIds picks them by the
+    hit's instance ids and geomID)."""
+    parts: list
+    instances: list
+
+    @property
+    def camera(self):
+        return self.parts[0].camera
+
+    def graph(self):
+        """Meshes and instances of every part, as the instanced oracles take them."""
+        return [{"meshes": p.geometry.meshes, "instances": list(self.instances[i])} for i, p in enumerate(self.parts)]
+
+    def release(self, built) -> None:
+        """Releases the scenes `build` returned, every scene before the scenes it instances."""
+        left = set(range(len(built)))
+        while left:
+            for i in sorted(left):
+                if not any(i in {pi for _, pi, _ in self.instances[j]} for j in left):
+                    built[i].release()
+                    left.discard(i)
+                    break
+
+    def build(self, sel_module, device, build_mode=None):
+        """Creates and commits one selas_gb300 Scene per part, instanced parts first; returns them in part order
+        (free them with `release`)."""
+        built = [None] * len(self.parts)
+
+        def make(i):
+            if built[i] is not None:
+                return
+            for _, pi, _ in self.instances[i]:
+                make(pi)
+            p = self.parts[i]
+            sc = sel_module.Scene(device, 0, build_mode)
+            if p.geometry.meshes:
+                p.geometry.attach_to(sc)
+            for gid, m in p.materials.items():
+                sc.set_material(gid, sel_module.material(**m))
+            for ls, l in p.lights:
+                sc.add_quad_light(ls, l["position"], l["direction"], l["x"], l["z"], l["radiance"])
+            sc.set_background(p.background)
+            for gid in sorted(p.ptex):
+                rows, tex = p.ptex[gid]
+                sc.set_ptex(gid, rows, tex)
+            for iid, pi, m in self.instances[i]:
+                sc.attach_instance(iid, built[pi], m)
+            sc.commit()
+            built[i] = sc
+
+        for i in range(len(self.parts)):
+            make(i)
+        return built
+
+    def sel_camera(self, sel_module, width, height):
+        return self.parts[0].sel_camera(sel_module, width, height)
+
+
+def _rotation_matrix(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def fbm_heightfield(n: int, octaves: int, seed: int, chunk_rows: int = 256) -> np.ndarray:
+    """(n, n) float32 fractal value noise: `octaves` octaves of bilinear value noise on lattices doubling from
+    4 x 4, amplitudes halving, normalised to [-1, 1]."""
+    rng = np.random.default_rng(seed)
+    lattices = [rng.uniform(-1, 1, size=((4 << o) + 1, (4 << o) + 1)).astype(np.float32) for o in range(octaves)]
+    out = np.empty((n, n), np.float32)
+    t = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    for r0 in range(0, n, chunk_rows):
+        r1 = min(n, r0 + chunk_rows)
+        acc = np.zeros((r1 - r0, n), np.float32)
+        amp = 1.0
+        for lat in lattices:
+            m = lat.shape[0] - 1
+            y = t[r0:r1] * m
+            x = t * m
+            iy = np.minimum(y.astype(np.int64), m - 1)
+            ix = np.minimum(x.astype(np.int64), m - 1)
+            fy = (y - iy)[:, None]
+            fx = (x - ix)[None, :]
+            a = lat[iy][:, ix]
+            b = lat[iy][:, ix + 1]
+            c = lat[iy + 1][:, ix]
+            d = lat[iy + 1][:, ix + 1]
+            acc += amp * ((a * (1 - fx) + b * fx) * (1 - fy) + (c * (1 - fx) + d * fx) * fy)
+            amp *= 0.5
+        out[r0:r1] = acc
+    out /= np.float32(2.0 - 2.0 ** (1 - octaves))
+    return out
+
+
+def heightfield_mesh(h: np.ndarray, extent: float, height: float):
+    """Grid mesh of a heightfield over [-extent, extent]^2 in x, z: 2 (n-1)^2 triangles, uint32 indices."""
+    n = h.shape[0]
+    xs = np.linspace(-extent, extent, n, dtype=np.float32)
+    v = np.empty((n * n, 3), np.float32)
+    v[:, 0] = np.tile(xs, n)
+    v[:, 2] = np.repeat(xs, n)
+    v[:, 1] = h.reshape(-1) * np.float32(height)
+    i = np.arange(n - 1, dtype=np.uint32)
+    a = (i[:, None] * n + i[None, :]).reshape(-1)  # row z, column x
+    idx = np.empty((a.size * 2, 3), np.uint32)
+    idx[0::2, 0], idx[0::2, 1], idx[0::2, 2] = a, a + n, a + n + 1
+    idx[1::2, 0], idx[1::2, 1], idx[1::2, 2] = a, a + n + 1, a + 1
+    return v, idx
+
+
+def instanced_terrain(grid: int = 4096, instances: int = 5000, mesh_level: int = 5, log2: int = 2, groups: int = 0,
+                      seed: int = 0x5E1A5004) -> InstancedRenderScene:
+    """The instanced-terrain configuration: a grid x grid fBm heightfield (8 octaves; 2 (grid-1)^2 triangles)
+    over [-1000, 1000]^2 and `instances` instances of one displaced icosphere of 20 * 4^mesh_level triangles
+    (level 5: 20,480) with per-face Ptex FP16 value noise (2^log2 texels a side), each with a random rotation
+    and a uniform scale in [0.5, 2] x 8, resting on the terrain.  groups > 0 adds a second instancing level:
+    that many instances of a cluster scene holding three instances of the mesh.  One quad light (sun) and a
+    sky background; the camera looks over the terrain."""
+    rng = np.random.default_rng(seed)
+    extent, height = 1000.0, 120.0
+    h = fbm_heightfield(grid, 8, seed + 1)
+    tv, tf = heightfield_mesh(h, extent, height)
+    world = TriangleScene()
+    world.add(0, tv, tf)
+    unit_v, f = icosphere(mesh_level)
+    disp = 1.0 + 0.25 * value_noise_dirs(unit_v, rng)
+    mesh = TriangleScene()
+    mesh.add(0, (unit_v * disp[:, None]).astype(np.float32), f.astype(np.uint32))
+    mesh_mats = {0: dict(shader=1, lightSetIndex=0, roughness=0.45, metallic=0.0, ior=1.5, usesPtex=1)}
+    mesh_ptex = {0: (ptex_faces(f, log2), _noise_texels_f32(f.shape[0], log2, rng))}
+    parts = [RenderScene(world, {0: dict(shader=1, lightSetIndex=0, baseColor=(0.35, 0.32, 0.25), roughness=0.8,
+                                         ior=1.5)},
+                         [(0, dict(position=(0.0, 900.0, 0.0), direction=(0.0, -1.0, 0.0), x=(300.0, 0.0, 0.0),
+                                   z=(0.0, 0.0, 300.0), radiance=(40.0, 38.0, 34.0)))],
+                         (0.35, 0.45, 0.6),
+                         dict(position=(-700.0, 260.0, -700.0), look_at=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
+                              fov_degrees=60.0)),
+             RenderScene(mesh, mesh_mats, [], (0.0, 0.0, 0.0), {}, mesh_ptex)]
+    inst_lists = [[], []]
+
+    def ground(x, z):
+        gx = np.clip(((x + extent) / (2 * extent) * (grid - 1)).astype(np.int64), 0, grid - 1)
+        gz = np.clip(((z + extent) / (2 * extent) * (grid - 1)).astype(np.int64), 0, grid - 1)
+        return h[gz, gx] * height
+
+    xz = rng.uniform(-0.9 * extent, 0.9 * extent, size=(instances, 2))
+    scales = rng.uniform(0.5, 2.0, instances) * 8.0
+    ys = ground(xz[:, 0], xz[:, 1]) + scales * 0.6
+    for k in range(instances):
+        m = np.zeros((3, 4), np.float32)
+        m[:, :3] = _rotation_matrix(rng) * scales[k]
+        m[:, 3] = (xz[k, 0], ys[k], xz[k, 1])
+        inst_lists[0].append((k + 1, 1, m))  # instIDs share the world's ID space with its terrain (0)
+    if groups:
+        cluster = TriangleScene()
+        parts.append(RenderScene(cluster, {}, [], (0.0, 0.0, 0.0), {}, {}))
+        inst_lists.append([])
+        for j in range(3):
+            m = np.zeros((3, 4), np.float32)
+            m[:, :3] = _rotation_matrix(rng) * 0.6
+            m[:, 3] = rng.uniform(-1.5, 1.5, 3)
+            inst_lists[2].append((100 + j, 1, m))
+        gxz = rng.uniform(-0.9 * extent, 0.9 * extent, size=(groups, 2))
+        gs = rng.uniform(4.0, 12.0, groups)
+        gy = ground(gxz[:, 0], gxz[:, 1]) + gs * 2.0
+        for k in range(groups):
+            m = np.zeros((3, 4), np.float32)
+            m[:, :3] = _rotation_matrix(rng) * gs[k]
+            m[:, 3] = (gxz[k, 0], gy[k], gxz[k, 1])
+            inst_lists[0].append((instances + 1 + k, 2, m))
+    return InstancedRenderScene(parts, inst_lists)
+
+
+def terrain_views(scene: InstancedRenderScene, count: int = 16):
+    """`count` cameras circling the terrain at two heights, looking at its centre."""
+    cams = []
+    for k in range(count):
+        a = 2 * np.pi * k / count
+        r = 700.0 if k % 2 == 0 else 450.0
+        y = 260.0 if k % 2 == 0 else 160.0
+        cams.append(dict(position=(r * np.cos(a), y, r * np.sin(a)), look_at=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
+                         fov_degrees=60.0))
+    return cams
