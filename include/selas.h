@@ -328,6 +328,18 @@ int sel_deferred_generate_image(SelScene scene, const SelCamera* camera, const S
 int sel_deferred_render_device(SelScene scene, const SelCamera* camera, const SelPtSettings* settings, double* d_accum,
                                void* stream);
 
+/* Several views of one scene in one shared wavefront (no reference counterpart: main.cpp renders one camera per
+ * run).  1..16 cameras; integrator SEL_INTEGRATOR_PT or SEL_INTEGRATOR_DEFERRED with the settings those entry
+ * points take.  View k uses seed settings->seed + k, so its image equals the single-view entry point's with that
+ * seed; every wavefront batch takes an equal share of paths from each view, and one batch is captured as a CUDA
+ * graph and replayed until all views are done.  out: the views' images one after another, each laid out as the
+ * single-view entry point writes it (already scaled by 1/spp); the device form adds FP64 sums into d_accum laid
+ * out the same way. */
+int sel_render_views(SelScene scene, const SelCamera* cameras, unsigned int count, unsigned int integrator,
+                     const SelPtSettings* settings, float* out);
+int sel_render_views_device(SelScene scene, const SelCamera* cameras, unsigned int count, unsigned int integrator,
+                            const SelPtSettings* settings, double* d_accum, void* stream);
+
 /* Autotuner (no reference counterpart).  Renders the given path-tracer workload (timed with CUDA events,
  * after one untimed render per configuration) over BVH layout and leaf size {8-wide quantised with 2, 3, 4
  * triangles per leaf; binary FP32}, wavefront capacity {1,048,576; 4,194,304; 8,388,608 paths} and traversal

@@ -279,6 +279,8 @@ register_signatures({
     "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
     "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
     "sel_deferred_settings_defaults": [ctypes.POINTER(SelPtSettings)],
+    "sel_render_views": [_vp, _vp, _u, _u, ctypes.POINTER(SelPtSettings), _vp],
+    "sel_render_views_device": [_vp, _vp, _u, _u, ctypes.POINTER(SelPtSettings), _vp, _vp],
     "sel_deferred_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
     "sel_deferred_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
 })
@@ -362,6 +364,24 @@ def _scene_deferred_generate_image(self, cam: SelCamera, settings: SelPtSettings
     return out
 
 
+def _scene_render_views(self, cams, settings: SelPtSettings, deferred: bool = False) -> list:
+    """Several views in one shared wavefront (sel_render_views): one image per camera, as pt_generate_image
+    (deferred=False) or deferred_generate_image (deferred=True) gives it with seed settings.seed + k."""
+    arr = (SelCamera * len(cams))(*cams)
+    layers = 1 if deferred else 2
+    sizes = [layers * c.height * c.width * 3 for c in cams]
+    out = np.zeros(sum(sizes), np.float32)
+    integ = 2 if deferred else 0
+    check(lib().sel_render_views(self.handle, ctypes.cast(arr, _vp), len(cams), integ, ctypes.byref(settings),
+                                 out.ctypes.data))
+    imgs, at = [], 0
+    for c, n in zip(cams, sizes):
+        shape = (c.height, c.width, 3) if deferred else (2, c.height, c.width, 3)
+        imgs.append(out[at:at + n].reshape(shape))
+        at += n
+    return imgs
+
+
 def _scene_vcm_generate_image(self, cam: SelCamera, settings: SelVcmSettings) -> np.ndarray:
     """VCM::GenerateImage: (height, width, 3) float32, the mean over the passes."""
     out = np.zeros((cam.height, cam.width, 3), np.float32)
@@ -383,6 +403,7 @@ Scene.set_background = _scene_set_background
 Scene.pt_generate_image = _scene_pt_generate_image
 Scene.vcm_generate_image = _scene_vcm_generate_image
 Scene.deferred_generate_image = _scene_deferred_generate_image
+Scene.render_views = _scene_render_views
 
 
 # ---------------------------------------------------------------------------------------------------

@@ -296,6 +296,68 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
 }
 
+// Several views of one scene in one shared wavefront: view k is job k of the job table (seed + k), each batch
+// takes an equal share of the wavefront's paths from every view, and the batch is captured once and replayed.
+// d_accum: the views' accumulators one after another (PT: 2 layers, deferred: 1 layer of W x H x 3 doubles).
+int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, const SelPtSettings& settings,
+                        double* d_accum, cudaStream_t stream, uint32_t mode) {
+    if (int rc = sync_shading(sc)) return rc;
+    uint64_t all = 0;
+    for (uint32_t k = 0; k < count; ++k) all += uint64_t(cams[k].width) * cams[k].height * settings.samplesPerPixel;
+    uint32_t cap = settings.pathsInFlight ? settings.pathsInFlight
+                   : (sc->tuned_paths_in_flight ? sc->tuned_paths_in_flight : kDefaultPathsInFlight);
+    if (uint64_t(cap) > all) cap = uint32_t(all);
+    if (cap < count) cap = count;
+    if (int rc = ensure_pt_state(sc, cap)) return rc;
+    const PtScene ps = scene_view(sc);
+    const PtState st = pt_state_carve(sc->pt_block, cap);
+    PtJob jobs[kMaxPtJobs];
+    PtControl ctl;
+    std::memset(jobs, 0, sizeof(jobs));
+    std::memset(&ctl, 0, sizeof(ctl));
+    const uint32_t layers = mode == kPtModeDeferred ? 1u : 2u;
+    uint64_t batches = 0;
+    size_t offset = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        PtJob& j = jobs[k];
+        j.scene = ps;
+        init_camera(cams[k], j.cam);
+        j.max_bounces = settings.maxBounces;
+        j.mode = mode;
+        j.samples_per_axis = mode == kPtModeDeferred ? deferred_axis(settings) : 0u;
+        j.seed = settings.seed + k;
+        j.total = uint64_t(cams[k].width) * cams[k].height * settings.samplesPerPixel;
+        j.accum = d_accum + offset;
+        offset += size_t(layers) * cams[k].width * cams[k].height * 3;
+        ctl.quota[k] = cap / count;
+        batches = std::max(batches, (j.total + ctl.quota[k] - 1) / ctl.quota[k]);
+    }
+    ctl.njobs = count;
+    cudaError_t e = cudaMemcpyAsync(st.jobs, jobs, sizeof(PtJob) * kMaxPtJobs, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(st.control, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "view table upload");
+    const int block = int(settings.traceBlockSize ? settings.traceBlockSize
+                                                  : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
+    e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
+                       sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
+                       ps.insts != nullptr);
+    return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
+}
+
+int check_views(SelScene scene, const SelCamera* cams, unsigned int count, unsigned int integrator,
+                const SelPtSettings* settings) {
+    if (!cams || count == 0 || count > uint32_t(kMaxPtJobs))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "1..16 cameras are needed");
+    if (integrator != SEL_INTEGRATOR_PT && integrator != SEL_INTEGRATOR_DEFERRED)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "integrator must be SEL_INTEGRATOR_PT or SEL_INTEGRATOR_DEFERRED");
+    for (unsigned int k = 0; k < count; ++k) {
+        const int rc = integrator == SEL_INTEGRATOR_PT ? check_render_args(scene, &cams[k], settings)
+                                                       : check_deferred_args(scene, &cams[k], settings);
+        if (rc) return rc;
+    }
+    return SEL_OK;
+}
+
 constexpr uint32_t kVcmChunk = 1024;  // passes per constants table
 
 SelVcmSettings default_vcm_settings() {
@@ -520,6 +582,53 @@ int sel_pt_generate_image(SelScene scene, const SelCamera* camera, const SelPtSe
     return read_error_word(dev, s);
 }
 
+int sel_render_views_device(SelScene scene, const SelCamera* cameras, unsigned int count, unsigned int integrator,
+                            const SelPtSettings* settings, double* d_accum, void* stream) {
+    if (int rc = check_views(scene, cameras, count, integrator, settings)) return rc;
+    if (!d_accum || (reinterpret_cast<uintptr_t>(d_accum) & 7u))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "d_accum must be an 8-byte aligned device pointer");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    return render_views_device(scene, cameras, count, *settings, d_accum, static_cast<cudaStream_t>(stream),
+                               integrator == SEL_INTEGRATOR_DEFERRED ? kPtModeDeferred : kPtModePath);
+}
+
+int sel_render_views(SelScene scene, const SelCamera* cameras, unsigned int count, unsigned int integrator,
+                     const SelPtSettings* settings, float* out) {
+    if (int rc = check_views(scene, cameras, count, integrator, settings)) return rc;
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (int rc = set_device(scene->dev)) return rc;
+    SelDeviceTy* dev = scene->dev;
+    std::lock_guard<std::mutex> dlock(dev->mu);
+    cudaStream_t s = dev->stream;
+    const uint32_t layers = integrator == SEL_INTEGRATOR_DEFERRED ? 1u : 2u;
+    size_t values = 0;
+    for (unsigned int k = 0; k < count; ++k) values += size_t(layers) * cameras[k].width * cameras[k].height * 3;
+    const size_t accum_bytes = values * sizeof(double);
+    const size_t need = accum_bytes + values * sizeof(float);
+    if (scene->accum_bytes < need) {
+        if (scene->d_accum) cudaFree(scene->d_accum);
+        scene->d_accum = nullptr;
+        scene->accum_bytes = 0;
+        cudaError_t e = cudaMalloc(&scene->d_accum, need);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(accumulator)");
+        scene->accum_bytes = need;
+    }
+    double* acc = static_cast<double*>(scene->d_accum);
+    float* res = reinterpret_cast<float*>(static_cast<char*>(scene->d_accum) + accum_bytes);
+    cudaError_t e = cudaMemsetAsync(acc, 0, accum_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(accumulator)");
+    if (int rc = render_views_device(scene, cameras, count, *settings, acc, s,
+                                     integrator == SEL_INTEGRATOR_DEFERRED ? kPtModeDeferred : kPtModePath))
+        return rc;
+    e = pt_resolve(acc, uint32_t(values), 1.0 / double(settings->samplesPerPixel), res, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, res, values * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "multi-view render");
+    return read_error_word(dev, s);
+}
+
 int sel_deferred_settings_defaults(SelPtSettings* out) {
     if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
     std::memset(out, 0, sizeof(*out));
@@ -655,7 +764,8 @@ int sel_scene_autotune(SelScene scene, const SelCamera* camera, const SelPtSetti
         if (sel_scene_commit(scene) != SEL_OK) continue;  // e.g. a tree deeper than a traversal stack
         for (uint32_t cap : capacities)
             for (int block : blocks) {
-                if (block == 256 && L.kind != SEL_BVH_WIDE8_Q8) continue;
+                // 256-thread traversal blocks exist for the flat 8-wide layout only
+                if (block == 256 && (L.kind != SEL_BVH_WIDE8_Q8 || !scene->instances.empty())) continue;
                 SelPtSettings st = *settings;
                 st.pathsInFlight = cap;
                 st.traceBlockSize = uint32_t(block);

@@ -151,3 +151,25 @@ def test_gpu_served_instanced_job_equals_direct_render(device):
     assert st.status == 0
     np.testing.assert_allclose(img, direct, rtol=1e-5, atol=1e-8)
     s.release(built)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("deferred", [False, True])
+def test_gpu_views_in_one_wavefront_equal_single_renders(device, deferred):
+    """sel_render_views: view k equals the single-view render with seed + k; views of different sizes."""
+    import selas_gb300 as sel
+    s = _terrain()
+    built = s.build(sel, device)
+    base = s.camera
+    cams = []
+    for k, (w, h) in enumerate([(48, 40), (32, 32), (64, 24)]):
+        pos = np.array(base["position"]) + np.array([8.0 * k, 0.0, -5.0 * k])
+        cams.append(sel.camera(tuple(pos), base["look_at"], base["up"], base["fov_degrees"], w, h))
+    st = sel.deferred_settings(3, 12, seed=40) if deferred else sel.pt_settings(6, 6, seed=40)
+    st.pathsInFlight = 3000  # several batches, each with paths of every view
+    views = built[0].render_views(cams, st, deferred=deferred)
+    for k, cam in enumerate(cams):
+        one = sel.deferred_settings(3, 12, seed=40 + k) if deferred else sel.pt_settings(6, 6, seed=40 + k)
+        single = built[0].deferred_generate_image(cam, one) if deferred else built[0].pt_generate_image(cam, one)
+        np.testing.assert_allclose(views[k], single, rtol=1e-5, atol=1e-8)
+    s.release(built)
