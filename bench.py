@@ -457,7 +457,7 @@ def instanced_metrics(sel, scenes, dev, stream, args):
     rad = acc[:, 1]
     finite = torch.isfinite(rad).all(dim=-1)
     img_mean = float(rad[finite].mean().item()) / spp
-    nonfinite = int((~finite).sum().item())  # the reference BSDF's zero-uniform quirk, about one path in 10^8
+    nonfinite = int((~finite).sum().item())  # the reference BSDF's zero-uniform quirk
     # autotuner on one view at reduced size
     cam1 = sel.camera(views[0]["position"], views[0]["look_at"], views[0]["up"], views[0]["fov_degrees"], 960, 540)
     tst = sel.pt_settings(4, 8)
