@@ -55,7 +55,7 @@ def parse_args():
     p.add_argument("--terrain-grid", type=int, default=4096, help="instanced terrain heightfield size (0: skip)")
     p.add_argument("--terrain-instances", type=int, default=5000)
     p.add_argument("--terrain-spp", type=int, default=64)
-    p.add_argument("--profile-case", choices=["query", "build", "pt", "vcm", "all"],
+    p.add_argument("--profile-case", choices=["query", "build", "pt", "vcm", "deferred", "instanced", "all"],
                    help="run one bounded case for an ncu capture (no timing, no JSON line) and exit")
     return p.parse_args()
 
@@ -293,8 +293,10 @@ def serve_metrics(sel, scenes, dev, room, args):
 def profile_case(case):
     """Bounded workloads sized for ncu captures (a few GB on the device at most): ray queries on the 5.24 M-
     triangle scene (1,048,576 coherent and incoherent rays, closest + any hit), two device BVH builds of
-    that scene, and the path tracer (4 spp) and VCM (2 passes) on the room with 8 textured icospheres at
-    640 x 360."""
+    that scene, and the path tracer (4 spp), VCM (2 passes) and the deferred path tracer (4 and 9 samples, at
+    most 16 segments) on the room with 8 textured icospheres at 640 x 360; the instanced terrain at 1024 x 1024
+    (2.1 M terrain triangles, 5,000 instances of 20,480 triangles): 1,048,576 camera rays (closest + any hit)
+    and the path tracer at 640 x 360, 4 spp."""
     from selas_gb300._build import build_library
     build_library()
     import selas_gb300 as sel
@@ -327,6 +329,33 @@ def profile_case(case):
             lo, hi = room.geometry.bounds()
             sc.vcm_generate_image(cam, sel.vcm_settings(2, 10, radius=0.003 * float(np.linalg.norm(hi - lo))))
         sc.release()
+    if case in ("deferred", "all"):
+        room = scenes.vcm_room(icospheres=8)
+        sc = room.build(sel, dev)
+        cam = room.sel_camera(sel, 640, 360)
+        sc.deferred_generate_image(cam, sel.deferred_settings(2, 16))
+        sc.deferred_generate_image(cam, sel.deferred_settings(3, 16))
+        sc.release()
+    if case in ("instanced", "all"):
+        terrain = scenes.instanced_terrain(grid=1024, instances=5000)
+        built = terrain.build(sel, dev)
+        v = scenes.terrain_views(terrain, 16)[0]
+        n = 1024
+        pos = np.array(v["position"], np.float32)
+        fwd = np.array(v["look_at"], np.float32) - pos
+        fwd /= np.linalg.norm(fwd)
+        right = np.cross(np.float32([0, 1, 0]), fwd)
+        right /= np.linalg.norm(right)
+        up = np.cross(fwd, right)
+        u = (np.arange(n, dtype=np.float32) + 0.5) / n * 2 - 1
+        gx, gy = np.meshgrid(u, u)
+        d = (fwd[None] + 0.577 * (gx.reshape(-1, 1) * right[None] - gy.reshape(-1, 1) * up[None])).astype(np.float32)
+        org = np.tile(pos, (d.shape[0], 1))
+        built[0].intersect1M(sel.make_rayhits(org, d))
+        built[0].occluded1M(sel.make_rays(org, d))
+        cam = sel.camera(v["position"], v["look_at"], v["up"], v["fov_degrees"], 640, 360)
+        built[0].pt_generate_image(cam, sel.pt_settings(4, 8))
+        terrain.release(built)
     dev.release()
 
 
