@@ -440,6 +440,51 @@ def render_metrics(sel, scenes, dev, stream, args, room=None):
                        "default_ms": round(default_ms, 3), "tuned_ms": round(tuned_ms, 3),
                        "speedup": round(default_ms / tuned_ms, 3)}
     sc.release()
+    # production form against the plain GPU path on the textured room: plain = binary FP32 BVH, shading in queue
+    # order (no material sort), kernel-by-kernel launches, default wavefront capacity; production = 8-wide
+    # quantised BVH, material-sorted shading, graph replay, autotuned capacity and block (path tracer).
+    prod = {}
+    w2, h2 = 1280, 720
+    for name, kind, sort, graphs in (("plain", sel.SEL_BVH_BINARY_FP32, 0, 0), ("production", sel.SEL_BVH_WIDE8_Q8, 1, 1)):
+        dev.set_option(sel.SEL_OPTION_MATERIAL_SORT, sort)
+        dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, graphs)
+        sc = room.build(sel, dev, bvh_kind=kind)
+        camp = room.sel_camera(sel, w2, h2)
+        accp = torch.zeros((2, h2, w2, 3), dtype=torch.float64, device="cuda")
+        stp = sel.pt_settings(16, 8)
+        tuned = None
+        if name == "production":
+            tb = sc.autotune(room.sel_camera(sel, 512, 512), sel.pt_settings(16, 8)).best
+            tuned = {"bvh": "8-wide quantised" if tb.bvh_kind == 0 else "binary FP32", "leaf": int(tb.leaf_size),
+                     "paths_in_flight": int(tb.paths_in_flight), "trace_block": int(tb.trace_block)}
+        pt_ms = timed(lambda: sel.check(lib.sel_pt_render_device(sc.handle, ctypes.byref(camp), ctypes.byref(stp),
+                                                                   accp.data_ptr(), sp)), 2)
+        del accp
+        accv = torch.zeros((h2, w2, 3), dtype=torch.float64, device="cuda")
+        passes = max(1, args.vcm_passes // (8 if name == "plain" else 2))
+        sv = sel.vcm_settings(passes, 10, radius=r0)
+        sel.check(lib.sel_vcm_render_device(sc.handle, ctypes.byref(camp), ctypes.byref(sel.vcm_settings(1, 10, radius=r0)),
+                                            accv.data_ptr(), sp))
+        vcm_ms = timed(lambda: sel.check(lib.sel_vcm_render_device(sc.handle, ctypes.byref(camp), ctypes.byref(sv),
+                                                                    accv.data_ptr(), sp)), 1)
+        dev.sync(sp)
+        del accv
+        prod[name] = {"pt_paths_per_s": round(w2 * h2 * 16 / (pt_ms * 1e-3), 1), "pt_ms": round(pt_ms, 2),
+                      "vcm_passes": passes, "vcm_ms_per_pass": round(vcm_ms / passes, 3),
+                      "vcm_paths_per_s": round(2 * w2 * h2 * passes / (vcm_ms * 1e-3), 1)}
+        if tuned:
+            prod[name]["autotuned"] = tuned
+        sc.release()
+    dev.set_option(sel.SEL_OPTION_MATERIAL_SORT, 1)
+    dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
+    out["production_vs_plain"] = {
+        "workload": f"room, {w2}x{h2}: path tracer 16 spp depth 8; VCM length 10, r0 {r0:.4f}",
+        "plain": "binary FP32 BVH, queue-order shading, kernel-by-kernel launches, default capacity",
+        "production": "8-wide quantised BVH, material-sorted shading, CUDA-graph replay, autotuned capacity/block",
+        **prod,
+        "pt_speedup": round(prod["production"]["pt_paths_per_s"] / prod["plain"]["pt_paths_per_s"], 3),
+        "vcm_speedup": round(prod["production"]["vcm_paths_per_s"] / prod["plain"]["vcm_paths_per_s"], 3),
+        "equal_rmse": "same paths in both forms (tests: same image with and without sorting, graphs, either layout)"}
     out["vcm"] = {"workload": f"room 20x20x10 with {room.geometry.triangle_count} triangles (24 displaced icospheres "
                               f"with 16x16 FP16 Ptex per face, 40 glass spheres), 1280x720, max path length 10, "
                               f"r0 {r0:.4f} (0.003 x diagonal), alpha 0.75",

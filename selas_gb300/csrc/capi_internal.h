@@ -16,6 +16,7 @@ struct SelDeviceTy {
     cudaStream_t stream = nullptr;  // internal stream for the host-memory entry points
     uint32_t* d_err = nullptr;      // kernel error word (iteration cap / stack overflow bits)
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
+    bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT
     std::mutex mu;
 };
 

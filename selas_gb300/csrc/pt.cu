@@ -163,6 +163,13 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
     }
 }
 
+}  // namespace
+
+// A scene whose hits may need Ptex (its own faces, or instances whose scenes may have some).
+bool pt_scene_textured(const PtScene& sc) { return sc.ptex_face_count > 0 || sc.insts != nullptr; }
+
+namespace {
+
 // Instances entered to a hit, as 1 + index in the parent's instance table (0: none).
 __device__ __forceinline__ uint2 inst_indices(const PtScene& sc, const InstHit& h) {
     const uint32_t a = h.rec[0] ? uint32_t(h.rec[0] - sc.insts) + 1u : 0u;
@@ -350,11 +357,11 @@ __global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
 // Ptex base colour of the sorted paths whose hit material is textured (SurfaceParameters.cpp:196-206): a
 // kernel of its own keeps the filter's code out of the shading kernel.
 template <bool kInst>
-__global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur) {
+__global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const uint32_t s = P.st.queue_sorted[e];
+        const uint32_t s = in_queue[e];
         const float4 hit = P.st.hit[s];
         const uint32_t tri = __float_as_uint(hit.w);
         if (tri == 0xffffffffu) continue;
@@ -682,7 +689,7 @@ size_t pt_state_block_bytes(uint32_t paths) {
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
-                           bool instanced) {
+                           bool instanced, bool texture) {
     // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
     // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
     const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;
@@ -712,10 +719,11 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
                 else k_classify<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 k_class_offsets<<<1, 32, 0, s>>>(st.counters);
                 k_class_scatter<<<shade_grid, kBlock, 0, s>>>(P, cur);
-                if (instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
-                else k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
             }
+            // Ptex base colours of the hits (the shading kernel reads them), in shading order
             const uint32_t* q = sort ? st.queue_sorted : st.queue[cur];
+            if (texture && instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
+            else if (texture) k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
             if (instanced) {
                 if (modes == 2u) k_shade<2, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
                 else if (modes == 3u) k_shade<3, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
@@ -737,7 +745,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes, instanced;
+        uint32_t modes, instanced, texture;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -748,6 +756,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.tb = tb;
     key.modes = modes;
     key.instanced = instanced ? 1u : 0u;
+    key.texture = texture ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -772,7 +781,8 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     if (e != cudaSuccess) return e;
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
-                          trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr);
+                          trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr,
+                          pt_scene_textured(sc));
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -111,14 +111,16 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // Launches `batches` batches of the shared wavefront over the jobs in st.jobs / st.control (uploaded by the
 // caller).  `bounces` is the number of extend/shade/shadow rounds per batch (the largest max_bounces of the
 // jobs).  With `graphs`, one batch is captured as a CUDA graph and replayed.
-// `sort`: order each bounce's queue by material class and filter Ptex in a kernel of its own before shading
-// (required when a job's scene uses Ptex).
+// `sort`: order each bounce's queue by material class before shading (Ptex is filtered by a kernel of its own
+// either way, in shading order).
 // `trace_block`: threads per block of the traversal kernels (128, or 256 with the 8-wide layout).
 // `modes`: integrators of the jobs, bit 0 kPtModePath, bit 1 kPtModeDeferred.
 // `instanced`: a job's scene has instances (the instanced traversal, which also walks flat scenes).
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128,
-                           uint32_t modes = 1u, bool instanced = false);
+                           uint32_t modes = 1u, bool instanced = false, bool texture = true);
+// `texture`: a job's hits may need Ptex (see pt_scene_textured); the Ptex kernel runs only then.
+bool pt_scene_textured(const PtScene& sc);
 
 // Single render (PathTracer::GenerateImage, or DeferredPathTracer::GenerateImage with set.mode =
 // kPtModeDeferred): one job, batches until all its paths are done.

@@ -229,7 +229,7 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.ptex_texels = sc->d_ptex_texels;
     ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
-    ps.sort_hint = sc->sort_hint;
+    ps.sort_hint = (sc->sort_hint && sc->dev->material_sort) ? 1u : 0u;
     ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     return ps;
 }
@@ -340,7 +340,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
                        sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
-                       ps.insts != nullptr);
+                       ps.insts != nullptr, pt_scene_textured(ps));
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
 }
 

@@ -226,7 +226,10 @@ __device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const
 }
 
 // Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
-__device__ void make_vhit(const VcmParams& P, float3 org, float3 dir, float4 hit, VHit& h, uint32_t& status) {
+// kPretex: the Ptex base colour was filtered by k_vtexture into P.st.base[s] (material-sorted bounces).
+template <bool kPretex>
+__device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir, float4 hit, VHit& h,
+                          uint32_t& status) {
     const uint32_t tri = __float_as_uint(hit.w);
     const float4* tp = P.tris + size_t(tri) * 3;
     const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
@@ -237,10 +240,15 @@ __device__ void make_vhit(const VcmParams& P, float3 org, float3 dir, float4 hit
     h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), hit.x));
     float3 base = ld3(m.base_color);
     if (m.flags & kMaterialUsesPtex) {
-        uint32_t pstatus = 0;
-        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
-                  hit.y, hit.z, base, pstatus);
-        status |= pstatus;
+        if constexpr (kPretex) {
+            const float4 b = P.st.base[s];
+            base = f3(b.x, b.y, b.z);
+        } else {
+            uint32_t pstatus = 0;
+            ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
+                      hit.y, hit.z, base, pstatus);
+            status |= pstatus;
+        }
     }
     h.view = -dir;
     h.s = make_surface(m, triangle_ng(p0, p1, p2), h.view, base);
@@ -414,7 +422,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_shadow(VcmParams P) {
 
 // Light sub-path vertices (EvaluateLightPaths, VCM.cpp:502-561): MIS update, stored vertex, connection to
 // the camera (ConnectLightPathToCamera, VCM.cpp:190-233; tech report sec. 5.3) and scattering.
-__global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur) {
+template <bool kSorted>
+__global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const uint32_t* in_queue) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[cur];
     const uint32_t N = P.npaths;
@@ -428,11 +437,11 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur) {
         float3 to_cam = f3(0.0f), contrib = f3(0.0f);
         float sh_tfar = 0.0f;
         if (e < n) {
-            s = P.st.queue[cur][e];
+            s = in_queue[e];
             const float4 hit = P.st.phit[s];
             if (__float_as_uint(hit.w) != 0xffffffffu) {
                 PathState st = load_path(P, s);
-                make_vhit(P, st.org, st.dir, hit, h, status);
+                make_vhit<kSorted>(P, s, st.org, st.dir, hit, h, status);
                 const float3 seg = h.pos - st.org;
                 const float d2 = dot(seg, seg);
                 const float cos_in = fabsf(dot(h.n, h.view));
@@ -483,6 +492,86 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur) {
         if (cont) P.st.queue[next][q] = s;
         const uint32_t sq = warp_append(&P.st.counters[2], shadow);
         if (shadow) push_shadow(P, sq, h, to_cam, sh_tfar, contrib, pixel);
+    }
+    if (status) atomicOr(P.err, status);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Material-class sort of a bounce's hits (as the path tracer's): counting sort by class (0 miss; else
+// 1 + shader * 4 + 2 (Ptex) + 1 (transparent)), then the Ptex filter of the sorted hits in a kernel of its own,
+// so the shading kernels run one kind of surface per warp and carry no filter code.
+// ---------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t vmaterial_class(const VcmParams& P, uint32_t s) {
+    const uint32_t tri = __float_as_uint(P.st.phit[s].w);
+    if (tri == 0xffffffffu) return 0u;
+    const uint32_t geom = __float_as_uint(__ldg(P.tris + size_t(tri) * 3 + 1).w);
+    const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+    const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
+    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+}
+
+__global__ void k_vclass_reset(uint32_t* counters) {
+    if (threadIdx.x < 32) counters[32 + threadIdx.x] = 0u;
+}
+
+__global__ void __launch_bounds__(kBlock) k_vclassify(VcmParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t c = valid ? vmaterial_class(P, P.st.queue[cur][e]) : 0xffu;
+        if (valid) P.st.cls[e] = c;
+        const uint32_t peers = __match_any_sync(0xffffffffu, c);
+        const uint32_t lane = threadIdx.x & 31u;
+        if (valid && (__ffs(peers) - 1) == int(lane)) atomicAdd(&P.st.counters[32 + c], __popc(peers));
+    }
+}
+
+__global__ void k_vclass_offsets(uint32_t* counters) {
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int c = 0; c < 16; ++c) {
+            counters[48 + c] = run;
+            run += counters[32 + c];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_vclass_scatter(VcmParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t c = valid ? P.st.cls[e] : 0xffu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, c);
+        const uint32_t lane = threadIdx.x & 31u;
+        const int leader = __ffs(peers) - 1;
+        uint32_t at = 0;
+        if (valid && leader == int(lane)) at = atomicAdd(&P.st.counters[48 + c], __popc(peers));
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (valid) P.st.queue_sorted[at + __popc(peers & ((1u << lane) - 1u))] = P.st.queue[cur][e];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    uint32_t status = 0;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint32_t s = P.st.queue_sorted[e];
+        const float4 hit = P.st.phit[s];
+        const uint32_t tri = __float_as_uint(hit.w);
+        if (tri == 0xffffffffu) continue;
+        const float4* tp = P.tris + size_t(tri) * 3;
+        const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1);
+        const uint32_t geom = __float_as_uint(p1.w);
+        const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+        if (!(m.flags & kMaterialUsesPtex)) continue;
+        float3 base = ld3(m.base_color);
+        uint32_t pstatus = 0;
+        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                  hit.z, base, pstatus);
+        status |= pstatus;
+        P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
     }
     if (status) atomicOr(P.err, status);
 }
@@ -675,7 +764,8 @@ __device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
     return cv;
 }
 
-__global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur) {
+template <bool kSorted>
+__global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const uint32_t* in_queue) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[cur];
     const uint32_t N = P.npaths;
@@ -693,12 +783,12 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur) {
         float3 to_l = f3(0.0f), contrib = f3(0.0f);
         float tfar = 0.0f;
         if (e < n) {
-            s = P.st.queue[cur][e];
+            s = in_queue[e];
             const float4 hit = P.st.phit[s];
             if (__float_as_uint(hit.w) != 0xffffffffu) {
                 hit_ok = true;
                 st = load_path(P, s);
-                make_vhit(P, st.org, st.dir, hit, h, status);
+                make_vhit<kSorted>(P, s, st.org, st.dir, hit, h, status);
                 const float3 seg = h.pos - st.org;
                 const float d2 = dot(seg, seg);
                 const float cos_in = fabsf(dot(h.n, h.view));
@@ -984,11 +1074,14 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.phit = reinterpret_cast<float4*>(take(16ull * paths));
     st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.queue_sorted = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.cls = reinterpret_cast<uint32_t*>(take(4ull * paths));
+    st.base = reinterpret_cast<float4*>(take(16ull * paths));
     st.so = reinterpret_cast<float4*>(take(16 * shadow));
     st.sd = reinterpret_cast<float4*>(take(16 * shadow));
     st.sc = reinterpret_cast<float4*>(take(16 * shadow));
     st.shadow_capacity = uint32_t(shadow);
-    st.counters = reinterpret_cast<uint32_t*>(take(4 * 16));
+    st.counters = reinterpret_cast<uint32_t*>(take(4 * 64));
     st.rays = reinterpret_cast<unsigned long long*>(take(8));
     st.cverts = reinterpret_cast<float4*>(take(96ull * paths));
     st.pairs = reinterpret_cast<uint2*>(take(8 * nv));
@@ -1091,6 +1184,17 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     P.sorted_index = st.vals[cur];
     const int trace_grid = sms * 8;
     const int shade_grid = sms * 8;
+    const bool sort = sc.sort_hint != 0;
+    // material-class sort and Ptex of a bounce's hits; returns the queue the shading kernel reads
+    auto sort_hits = [&](cudaStream_t stream, int cur) -> const uint32_t* {
+        if (!sort) return st.queue[cur];
+        k_vclass_reset<<<1, 32, 0, stream>>>(st.counters);
+        k_vclassify<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        k_vclass_offsets<<<1, 32, 0, stream>>>(st.counters);
+        k_vclass_scatter<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        k_vtexture<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        return st.queue_sorted;
+    };
     // one pass; identical launches every pass (the pass reads its constants through st.iter)
     auto enqueue = [&](cudaStream_t stream) {
         // light sub-paths: vertices and light tracing
@@ -1101,7 +1205,9 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
             if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
             else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            k_l_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            const uint32_t* q = sort_hits(stream, cur);
+            if (sort) k_l_shade<true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+            else k_l_shade<false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
             if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
             else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
         }
@@ -1129,7 +1235,9 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
             if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
             else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            k_c_shade<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            const uint32_t* q = sort_hits(stream, cur);
+            if (sort) k_c_shade<true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+            else k_c_shade<false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
             k_c_connect<<<shade_grid, kBlock, 0, stream>>>(P);
             k_c_merge<<<shade_grid, kBlock, 0, stream>>>(P);
             if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
@@ -1139,13 +1247,14 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     };
     struct Key {
         VcmParams P;
-        int kind, sms, radix_passes;
+        int kind, sms, radix_passes, sort;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
     key.kind = sc.bvh_kind;
     key.sms = sms;
     key.radix_passes = radix_passes;
+    key.sort = sort ? 1 : 0;
     return replay(graphs, &key, sizeof(key), stream, passes, enqueue);
 }
 

@@ -44,13 +44,17 @@ struct VcmState {
     uint64_t* prng;       // PCG32 state (the stream is a function of the pass and the slot)
     float4* phit;         // t, u, v, triangle bits (all ones: miss)
     uint32_t* queue[2];   // live path slots, ping-pong between bounces
+    uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort)
+    uint32_t* cls;        // material class of each current queue entry
+    float4* base;         // Ptex base colour (authored) of the path's current hit, filtered before shading
     // shadow queue: light tracing, next-event and connection segments with their contributions
     float4* so;           // origin, tnear
     float4* sd;           // direction, tfar
     float4* sc;           // contribution, pixel bits (zero contribution: null entry)
     uint32_t shadow_capacity;
     uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor,
-                          // [5] camera-vertex records, [6] connection pairs
+                          // [5] camera-vertex records, [6] connection pairs; [32..47] material-class counts,
+                          // [48..63] their scatter cursors
     unsigned long long* rays;  // rays traced (closest + any hit), a running total
     float4* cverts;       // camera-vertex records of the current bounce, 6 x float4 each
     uint2* pairs;         // (camera-vertex record, light-vertex index) connection pairs of the current bounce

@@ -169,3 +169,22 @@ def test_gpu_vcm_graph_replay_matches_direct_launches(device, cornell):
         imgs.append(_gpu_vcm(device, cornell, 40, 5))
     device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
     np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_material_sort_does_not_change_the_image(device):
+    """SEL_OPTION_MATERIAL_SORT: hits shaded in material-class order with Ptex filtered in a kernel of its own
+    give the image of queue-order shading (same paths; only the order of FP64 additions differs)."""
+    import selas_gb300 as sel
+    rs = scenes.textured_spheres(count=4, level=3)
+    sc = rs.build(sel, device)
+    cam = rs.sel_camera(sel, 48, 40)
+    imgs = []
+    for sort in (1, 0):
+        device.set_option(sel.SEL_OPTION_MATERIAL_SORT, sort)
+        imgs.append((sc.vcm_generate_image(cam, sel.vcm_settings(3, 8, seed=5)),
+                     sc.pt_generate_image(cam, sel.pt_settings(4, 6, seed=5))))
+    device.set_option(sel.SEL_OPTION_MATERIAL_SORT, 1)
+    sc.release()
+    np.testing.assert_allclose(imgs[0][0], imgs[1][0], rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(imgs[0][1], imgs[1][1], rtol=1e-5, atol=1e-8)
