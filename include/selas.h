@@ -256,6 +256,16 @@ typedef struct SelQuadLight {
 int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const SelQuadLight* light);
 /* backgroundIntensity (default 1, BuildCommon/CSceneBuildProcessor.cpp:59). */
 int sel_scene_set_background(SelScene scene, float r, float g, float b);
+/* Image-based light (SceneResource::iblResource; ImageBasedLightResource.h:24-35): a latitude-longitude RGB
+ * image of width x height (row y at polar angle (y + 0.5) pi / height from +y, column x at azimuth
+ * (x + 0.5) 2 pi / width + rotationRadians - pi from +x towards +z), scaled by exposureScale, which lights
+ * the scene and is importance-sampled through marginal / conditional densities of sin(theta) x luma
+ * (BuildCommon/BuildImageBasedLight.cpp:18-107, built here); `miss` (may be null: the light image times the
+ * exposure) is what camera rays and pure-specular chains see (EvaluateBackgroundMiss).  Replaces the uniform
+ * background in the path tracer (misses) and the deferred path tracer (misses, background next-event
+ * estimation and its MIS); VCM ignores it.  width == 0 removes the image. */
+int sel_scene_set_ibl(SelScene scene, const float* rgb, unsigned int width, unsigned int height, const float* miss_rgb,
+                      unsigned int miss_width, unsigned int miss_height, float rotationRadians, float exposureScale);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Ptex per-face textures.                                                                           */

@@ -40,6 +40,10 @@ def lib() -> ctypes.CDLL:
                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                         ctypes.c_uint32, ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
             "oracle_cmj": ([_i, _i, _i, _vp], None),
+            "oracle_set_ibl": ([_vp, ctypes.c_uint32, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.c_float, ctypes.c_float], None),
+            "oracle_ibl_sample": ([_vp, _i, _vp, _vp], None),
+            "oracle_ibl_pdf": ([_vp, _i, _vp], None),
             "oracle_instanced_query": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i, _i],
                                        None),
             "oracle_affine_inverse": ([_vp, _vp], _i),
@@ -134,11 +138,43 @@ class consistent_lambert:
         return False
 
 
+def set_ibl(ibl):
+    """Image-based light of the following oracle renders (a RenderScene.ibl dict, or None)."""
+    if not ibl:
+        lib().oracle_set_ibl(None, 0, 0, None, 0, 0, 0.0, 1.0)
+        return
+    a = np.ascontiguousarray(ibl["light"], np.float32)
+    m = ibl.get("miss")
+    m = None if m is None else np.ascontiguousarray(m, np.float32)
+    lib().oracle_set_ibl(_p(a), a.shape[1], a.shape[0], None if m is None else _p(m), 0 if m is None else m.shape[1],
+                         0 if m is None else m.shape[0], float(ibl.get("rotation", 0.0)), float(ibl.get("exposure", 1.0)))
+
+
+def ibl_sample(ibl, r):
+    """Oracle IBL sampling of (n, 2) uniforms: (n, 7) [dir, radiance, pdf] and (n, 7) [pdf, light rgb, miss rgb]
+    looked up again for the sampled directions."""
+    set_ibl(ibl)
+    r = np.ascontiguousarray(r, np.float32)
+    out = np.zeros((r.shape[0], 7), np.float32)
+    ev = np.zeros((r.shape[0], 7), np.float32)
+    lib().oracle_ibl_sample(_p(r), r.shape[0], _p(out), _p(ev))
+    return out, ev
+
+
+def ibl_pdf(ibl, dirs):
+    set_ibl(ibl)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(d.shape[0], np.float32)
+    lib().oracle_ibl_pdf(_p(d), d.shape[0], _p(out))
+    return out
+
+
 def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, seed=0x5E1A5000, rng="pcg",
               nthreads=None, physical_nee=False):
     """CPU oracle path tracer (oracle_pt.cpp): FP64 per-pixel sums over passes [pass_begin, pass_end),
     shape (2, height, width, 3)."""
     from selas_gb300.scenes import light_records, material_records
+    set_ibl(getattr(render_scene, "ibl", None))
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)
@@ -161,6 +197,7 @@ def deferred_render(render_scene, width, height, sample_begin, sample_end, sampl
     samples [sample_begin, sample_end) of samples_per_axis^2 per pixel, shape (height, width, 3).  rng "pcg":
     the GPU's streams; "mt": MT19937 per pixel as the reference's sampler."""
     from selas_gb300.scenes import light_records, material_records
+    set_ibl(getattr(render_scene, "ibl", None))
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)
@@ -231,6 +268,7 @@ def graph_render(iscene, width, height, begin, end, max_bounces=8, seed=0x5E1A50
     path tracer (shape (height, width, 3), samples [begin, end)) over an InstancedRenderScene, PCG32 sampling;
     FP64 sums."""
     from selas_gb300.scenes import light_records, material_records
+    set_ibl(iscene.parts[0].ibl)
     V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
     mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
     for part in iscene.parts:

@@ -172,8 +172,131 @@ void sample_light(const Light& L, V3 p, V3 n, float u, float v, V3& dir, V3& rad
     }
 }
 
+// Image-based light (ImageBasedLightResource.cpp:81-268; densities as BuildImageBasedLight.cpp:18-107).
+struct Ibl {
+    uint32_t w = 0, h = 0, mw = 0, mh = 0;
+    float rot = 0, exposure = 1;
+    std::vector<float> mdf, cdf, light, miss;  // light / miss: RGB
+
+    void build(const float* rgb, uint32_t width, uint32_t height, const float* miss_rgb, uint32_t miss_w,
+               uint32_t miss_h, float rotation, float scale) {
+        w = width; h = height; rot = rotation; exposure = scale;
+        light.assign(rgb, rgb + size_t(w) * h * 3);
+        if (miss_rgb) {
+            mw = miss_w; mh = miss_h;
+            miss.assign(miss_rgb, miss_rgb + size_t(mw) * mh * 3);
+        } else {
+            mw = w; mh = h;
+            miss.resize(light.size());
+            for (size_t i = 0; i < light.size(); ++i) miss[i] = scale * light[i];
+        }
+        std::vector<float> inten(size_t(w) * h);
+        for (uint32_t y = 0; y < h; ++y) {
+            const float sin_theta = std::sin((float(y) + 0.5f) * kPi / float(h));
+            for (uint32_t x = 0; x < w; ++x) {
+                const float* c = &light[(size_t(y) * w + x) * 3];
+                inten[size_t(y) * w + x] = sin_theta * (c[0] * 0.299f + c[1] * 0.587f + c[2] * 0.114f);
+            }
+        }
+        mdf.assign(h, 0.0f);
+        cdf.assign(size_t(w) * h, 0.0f);
+        float msum = 0.0f;
+        for (uint32_t y = 0; y < h; ++y) {
+            float rsum = 0.0f;
+            for (uint32_t x = 0; x < w; ++x) rsum += inten[size_t(y) * w + x];
+            mdf[y] = rsum;
+            msum += rsum;
+            if (rsum > 0.0f) {
+                const float oo = 1.0f / rsum;
+                float acc = 0.0f;
+                for (uint32_t x = 0; x < w; ++x) {
+                    acc += oo * inten[size_t(y) * w + x];
+                    cdf[size_t(y) * w + x] = acc;
+                }
+            }
+            cdf[size_t(y) * w + w - 1] = 1.0f;
+        }
+        if (msum > 0.0f) {
+            const float oo = 1.0f / msum;
+            float acc = 0.0f;
+            for (uint32_t y = 0; y < h; ++y) {
+                acc += mdf[y] * oo;
+                mdf[y] = acc;
+            }
+        }
+        mdf[h - 1] = 1.0f;
+    }
+    static void search(const float* f, uint32_t count, float r, uint32_t& index, float& pdf) {
+        int lo = 0, hi = int(count) - 1;
+        index = count - 1;
+        pdf = 0.0f;
+        while (lo <= hi) {
+            const int mid = (lo + hi) / 2;
+            if (f[mid] >= r) {
+                index = uint32_t(mid);
+                pdf = mid > 0 ? f[mid] - f[mid - 1] : f[mid];
+                hi = mid - 1;
+            } else {
+                lo = mid + 1;
+            }
+        }
+    }
+    void texel(V3 wi, uint32_t width, uint32_t height, int& x, int& y, float& theta) const {
+        theta = std::acos(std::min(std::max(wi.y, -1.0f), 1.0f));
+        float phi = std::atan2(wi.z, wi.x);
+        phi = std::fmod(phi + kPi + rot, 2.0f * kPi);
+        x = int(phi * float(width) / (2.0f * kPi) - 0.5f);
+        y = int(theta * float(height) / kPi - 0.5f);
+        x = std::min(std::max(x, 0), int(width) - 1);
+        y = std::min(std::max(y, 0), int(height) - 1);
+    }
+    float pdf_at(int x, int y, float theta) const {
+        const float m = y > 0 ? mdf[y] - mdf[y - 1] : mdf[y];
+        const float* row = &cdf[size_t(y) * w];
+        const float c = x > 0 ? row[x] - row[x - 1] : row[x];
+        const float inv_j = (float(w) * float(h)) / (2.0f * kPi);
+        const float st = std::sin(theta);
+        return st > 0.0f ? m * c * inv_j / st : 0.0f;
+    }
+    float pdf(V3 wi) const {
+        int x, y;
+        float theta;
+        texel(wi, w, h, x, y, theta);
+        return pdf_at(x, y, theta);
+    }
+    V3 radiance(V3 wi) const {
+        int x, y;
+        float theta;
+        texel(wi, w, h, x, y, theta);
+        const float* c = &light[(size_t(y) * w + x) * 3];
+        return exposure * V3(c[0], c[1], c[2]);
+    }
+    V3 miss_radiance(V3 wi) const {
+        int x, y;
+        float theta;
+        texel(wi, mw, mh, x, y, theta);
+        const float* c = &miss[(size_t(y) * mw + x) * 3];
+        return V3(c[0], c[1], c[2]);
+    }
+    void sample(float r0, float r1, V3& dir, V3& rad, float& p) const {
+        uint32_t x, y;
+        float m, c;
+        search(mdf.data(), h, r0, y, m);
+        search(&cdf[size_t(y) * w], w, r1, x, c);
+        const float theta = (float(y) + 0.5f) * kPi / float(h);
+        const float phi = std::fmod(((float(x) + 0.5f) * (2.0f * kPi) / float(w)) + rot, 2.0f * kPi) - kPi;
+        const float inv_j = (float(w) * float(h)) / (2.0f * kPi);
+        const float st = std::sin(theta);
+        p = st > 0.0f ? m * c * inv_j / st : 0.0f;
+        dir = V3(st * std::cos(phi), std::cos(theta), st * std::sin(phi));
+        const float* l = &light[(size_t(y) * w + x) * 3];
+        rad = exposure * V3(l[0], l[1], l[2]);
+    }
+};
+
 struct Scene {
     const void* bvh = nullptr;
+    const Ibl* ibl = nullptr;                       // image-based light (null: the uniform background)
     const void* graph = nullptr;                    // instanced scene graph (replaces bvh when set)
     std::vector<std::vector<Material>> gmats;       // graph: materials of each scene, by geomID
     std::vector<const orp::Texture*> gptex;         // graph: Ptex of each scene (null: none)
@@ -248,6 +371,7 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
     ld0 = V3(0.0f);
     ld1 = V3(0.0f);
     V3 thr(1.0f);
+    bool delta_only = true;
     int phase = 0;
     V3 ext(0.0f);
     uint32_t bounce = 0;
@@ -313,6 +437,7 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
             const bool ok = orc::bsdf_sample(s, view, u4, used, bs);
             for (int k = 0; k < used; ++k) rng.uniform();
             if (!ok) break;
+            delta_only = delta_only && (bs.flags & 4u);
             if (bs.flags == 2u) {
                 if (phase == 0) { phase = bs.phase; ext = bs.ext; }
                 else { phase = 0; ext = V3(0.0f); }
@@ -329,7 +454,8 @@ void evaluate_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
             const float th = 2.0f * kPi * r0;
             dir = V3(nn * std::cos(th), uu, nn * std::sin(th));
         } else {
-            ld1 = ld1 + sc.background * thr;
+            const V3 bg = sc.ibl ? (delta_only ? sc.ibl->miss_radiance(dir) : sc.ibl->radiance(dir)) : sc.background;
+            ld1 = ld1 + bg * thr;
             break;
         }
         ++bounce;
@@ -409,11 +535,13 @@ void add(double* acc, V3 c) {
 void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounces, double* acc) {
     const float kInv4Pi = 1.0f / (4.0f * kPi);
     V3 thr(1.0f);
+    bool dirac_only = true;
     for (uint32_t bounce = 0; bounce < max_bounces; ++bounce) {
         orq::Hit h;
         const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
         if (!sc_closest(sc, o, d, 0.0f, 3.402823466e+38f, h)) {
-            add(acc, sc.background * thr);
+            const V3 bg = sc.ibl ? (dirac_only ? sc.ibl->miss_radiance(dir) : sc.ibl->radiance(dir)) : sc.background;
+            add(acc, bg * thr);
             break;
         }
         const V3 pos(org.x + h.t * dir.x, org.y + h.t * dir.y, org.z + h.t * dir.z);
@@ -442,18 +570,27 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
                 if (!sc_occluded(sc, soa, lda, 0.0f, ldist)) add(acc, sample * thr);
             }
         }
-        // background (SampleBackground -> BackgroundLightSample, AreaLighting.cpp:334-350: uniform sphere
-        // direction, density recorded as 1), balance heuristic against the BSDF's density
+        // background (SampleBackground, AreaLighting.cpp:393-401: DirectIblLightSample with an image, else
+        // BackgroundLightSample, :334-350, a uniform sphere direction with density recorded as 1), balance
+        // heuristic against the BSDF's density
         const float r0 = rng.uniform(), r1 = rng.uniform();
-        const float uu = 2.0f * r1 - 1.0f;
-        const float nn = std::sqrt(std::max(0.0f, 1.0f - uu * uu));
-        const float th = 2.0f * kPi * r0;
-        const V3 sdir(nn * std::cos(th), uu, nn * std::sin(th));
-        if (orc::Dot(sc.background, V3(1.0f)) > 0) {
+        V3 sdir, srad;
+        float spdf;
+        if (sc.ibl) {
+            sc.ibl->sample(r0, r1, sdir, srad, spdf);
+        } else {
+            const float uu = 2.0f * r1 - 1.0f;
+            const float nn = std::sqrt(std::max(0.0f, 1.0f - uu * uu));
+            const float th = 2.0f * kPi * r0;
+            sdir = V3(nn * std::cos(th), uu, nn * std::sin(th));
+            srad = sc.background;
+            spdf = 1.0f;
+        }
+        if (orc::Dot(srad, V3(1.0f)) > 0) {
             float fp, rp;
             const V3 refl = orc::bsdf_evaluate(sh.s, sh.view, sdir, fp, rp);
-            const float mis = 1.0f / (1.0f + fp);
-            const V3 sample = mis * refl * sc.background * (1.0f / 1.0f);
+            const float mis = (1.0f * spdf) / (1.0f * spdf + 1.0f * fp);
+            const V3 sample = mis * refl * srad * (1.0f / spdf);
             if (orc::Dot(sample, V3(1.0f)) > 0) {
                 const V3 so = offset(pos, sh.n, sh.err, sdir, 0.1f);
                 const float soa[3] = {so.x, so.y, so.z}, sda[3] = {sdir.x, sdir.y, sdir.z};
@@ -469,7 +606,9 @@ void deferred_path(const Scene& sc, Rng& rng, V3 org, V3 dir, uint32_t max_bounc
         const bool ok = orc::bsdf_sample(sh.s, sh.view, u4, used, bs);
         for (int k = 0; k < used; ++k) rng.uniform();
         if (!ok) break;
-        const float mis = bs.fwd / (bs.fwd + kInv4Pi);
+        const float sky_pdf = sc.ibl ? sc.ibl->pdf(bs.wi) : kInv4Pi;
+        const float mis = (1.0f * bs.fwd) / (1.0f * bs.fwd + 1.0f * sky_pdf);
+        dirac_only = dirac_only && (bs.flags & 4u);
         V3 t = mis * thr * bs.refl;
         if (orc::Dot(t, t) == 0.0f) break;
         if (bounce >= 7) {  // Russian roulette once MaxTrackedBounces_ = 7 bounces are tracked
@@ -567,6 +706,9 @@ static void run_deferred(const Scene& sc, const float* camera, uint32_t width, u
     for (auto& th : pool) th.join();
 }
 
+// The image-based light the renderers use (oracle_set_ibl; none when its width is 0).
+static Ibl g_ibl;
+
 // Scene tables of the oracle renderers' common arguments; returns the Ptex texture to delete.
 static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
                          const float* materials, int n_materials, const float* lights, int n_lights,
@@ -592,6 +734,7 @@ static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* p
         sc.set_count.push_back(sets[2 * i + 1]);
     }
     sc.background = V3(background[0], background[1], background[2]);
+    sc.ibl = g_ibl.w ? &g_ibl : nullptr;
     return tex;
 }
 
@@ -697,6 +840,41 @@ void oracle_graph_render(int n_scenes, const float* verts, const uint32_t* prim,
         run_pt(sc, camera, width, height, begin, end, max_bounces, seed, 0, threads, out);
     orq::release_graph(const_cast<void*>(sc.graph));
     for (orp::Texture* t : owned) delete t;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Sets (width > 0) or clears the image-based light of the following oracle renders: RGB light image, optional
+// miss image (null: the light image times the exposure), rotation in radians, exposure scale.
+void oracle_set_ibl(const float* rgb, uint32_t width, uint32_t height, const float* miss_rgb, uint32_t miss_width,
+                    uint32_t miss_height, float rotation, float exposure) {
+    if (!width) {
+        g_ibl = Ibl();
+        return;
+    }
+    g_ibl.build(rgb, width, height, miss_rgb, miss_width, miss_height, rotation, exposure);
+}
+
+// IBL sampling for tests: n directions from (r0, r1) pairs (out: dir xyz, radiance rgb, pdf; 7 floats each) and
+// the density and radiance the lookups give back for those directions (eval: pdf, rgb, miss rgb; 7 floats).
+void oracle_ibl_sample(const float* r, int n, float* out, float* eval) {
+    for (int i = 0; i < n; ++i) {
+        V3 d, rad;
+        float p;
+        g_ibl.sample(r[2 * i], r[2 * i + 1], d, rad, p);
+        float* o = out + 7 * i;
+        o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = rad.x; o[4] = rad.y; o[5] = rad.z; o[6] = p;
+        const V3 lr = g_ibl.radiance(d), mr = g_ibl.miss_radiance(d);
+        float* e = eval + 7 * i;
+        e[0] = g_ibl.pdf(d); e[1] = lr.x; e[2] = lr.y; e[3] = lr.z; e[4] = mr.x; e[5] = mr.y; e[6] = mr.z;
+    }
+}
+
+// Solid-angle density of directions (n x 3 floats) under the image's sampling.
+void oracle_ibl_pdf(const float* dirs, int n, float* out) {
+    for (int i = 0; i < n; ++i) out[i] = g_ibl.pdf(V3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
 }
 
 }  // extern "C"

@@ -280,6 +280,7 @@ register_signatures({
     "sel_vcm_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp],
     "sel_vcm_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelVcmSettings), _vp, _vp],
     "sel_deferred_settings_defaults": [ctypes.POINTER(SelPtSettings)],
+    "sel_scene_set_ibl": [_vp, _vp, _u, _u, _vp, _u, _u, ctypes.c_float, ctypes.c_float],
     "sel_render_views": [_vp, _vp, _u, _u, ctypes.POINTER(SelPtSettings), _vp],
     "sel_render_views_device": [_vp, _vp, _u, _u, ctypes.POINTER(SelPtSettings), _vp, _vp],
     "sel_deferred_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
@@ -351,6 +352,19 @@ def _scene_set_background(self, rgb) -> None:
     check(lib().sel_scene_set_background(self.handle, *map(float, rgb)))
 
 
+def _scene_set_ibl(self, light, miss=None, rotation=0.0, exposure=1.0) -> None:
+    """Image-based light: light (height, width, 3) float32 latitude-longitude RGB; miss likewise (None: light x
+    exposure); rotation in radians; exposure scale.  light=None removes it."""
+    if light is None:
+        check(lib().sel_scene_set_ibl(self.handle, None, 0, 0, None, 0, 0, 0.0, 1.0))
+        return
+    a = np.ascontiguousarray(light, np.float32)
+    m = None if miss is None else np.ascontiguousarray(miss, np.float32)
+    check(lib().sel_scene_set_ibl(self.handle, a.ctypes.data, a.shape[1], a.shape[0],
+                                  None if m is None else m.ctypes.data, 0 if m is None else m.shape[1],
+                                  0 if m is None else m.shape[0], float(rotation), float(exposure)))
+
+
 def _scene_pt_generate_image(self, cam: SelCamera, settings: SelPtSettings) -> np.ndarray:
     """PathTracer::GenerateImage: (2, height, width, 3) float32 layers, scaled by 1/spp."""
     out = np.zeros((2, cam.height, cam.width, 3), np.float32)
@@ -401,6 +415,7 @@ Scene.set_ptex = _scene_set_ptex
 Scene.set_material = _scene_set_material
 Scene.add_quad_light = _scene_add_quad_light
 Scene.set_background = _scene_set_background
+Scene.set_ibl = _scene_set_ibl
 Scene.pt_generate_image = _scene_pt_generate_image
 Scene.vcm_generate_image = _scene_vcm_generate_image
 Scene.deferred_generate_image = _scene_deferred_generate_image

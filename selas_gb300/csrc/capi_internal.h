@@ -55,6 +55,11 @@ struct SelSceneTy {
     std::vector<sel::MaterialDev> materials;
     std::vector<std::vector<sel::QuadLight>> light_sets;
     float background[3] = {1.0f, 1.0f, 1.0f};  // backgroundIntensity default (CSceneBuildProcessor.cpp:59)
+    // image-based light (sel_scene_set_ibl): RGB images, densities built on upload
+    std::vector<float> ibl_light, ibl_miss;
+    uint32_t ibl_w = 0, ibl_h = 0, ibl_mw = 0, ibl_mh = 0;
+    float ibl_rotation = 0.0f, ibl_exposure = 1.0f;
+    void* d_ibl = nullptr;  // IblDev followed by its arrays (null: no image)
     bool shading_dirty = true;
     struct PtexBinding {
         uint32_t geomID;
@@ -89,7 +94,10 @@ struct PtScene;
 struct VcmConsts;
 struct VcmSettings;
 // render_capi.cu
-int sync_shading(SelSceneTy* sc);              // uploads materials, lights and Ptex when they changed
+int sync_shading(SelSceneTy* sc);              // uploads materials, lights, Ptex and the IBL when they changed
+// CalculateIntensityMap + CalculateStrataDistributionFunctions (BuildImageBasedLight.cpp:18-107): marginal CDF
+// (height) and conditional CDFs (width x height) of sin(theta) x luma of an RGB latitude-longitude image.
+void ibl_densities(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& mdf, std::vector<float>& cdf);
 PtScene scene_view(const SelSceneTy* sc);       // device pointers of a committed, synced scene
 float vcm_default_radius(const SelSceneTy* sc);
 void vcm_constants(float radius0, float alpha, uint32_t paths, bool merging, uint32_t pass, VcmConsts& c);

@@ -29,6 +29,7 @@
 #include "capi_internal.h"
 #include "cmj.cuh"
 #include "graph.h"
+#include "ibl.cuh"
 #include "instance.cuh"
 #include "ptex.cuh"
 #include "shading.cuh"
@@ -476,20 +477,28 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                     }
                 }
                 if (deferred) {
-                    // SampleBackground -> BackgroundLightSample (AreaLighting.cpp:334-350): a uniform sphere
-                    // direction whose density is recorded as 1, at distance 1e36; balance heuristic against the
-                    // BSDF's density (DeferredPathTracer.cpp:90-111)
+                    // SampleBackground (AreaLighting.cpp:393-401): with an image DirectIblLightSample (:293-314),
+                    // else BackgroundLightSample (:334-350), a uniform sphere direction whose density is recorded
+                    // as 1; at distance 1e36; balance heuristic against the BSDF's density
+                    // (DeferredPathTracer.cpp:90-111)
                     const float r0 = pcg_float(rng), r1 = pcg_float(rng);
-                    const float uu = 2.0f * r1 - 1.0f;
-                    const float nn = sqrtf(fmaxf(0.0f, 1.0f - uu * uu));
-                    const float th = kTwoPi * r0;
-                    const float3 sdir = f3(nn * cosf(th), uu, nn * sinf(th));
-                    const float3 bg = f3(S.background[0], S.background[1], S.background[2]);
+                    float3 sdir, bg;
+                    float spdf;
+                    if (S.ibl) {
+                        ibl_sample(*S.ibl, r0, r1, sdir, bg, spdf);
+                    } else {
+                        const float uu = 2.0f * r1 - 1.0f;
+                        const float nn = sqrtf(fmaxf(0.0f, 1.0f - uu * uu));
+                        const float th = kTwoPi * r0;
+                        sdir = f3(nn * cosf(th), uu, nn * sinf(th));
+                        bg = f3(S.background[0], S.background[1], S.background[2]);
+                        spdf = 1.0f;
+                    }
                     if (dot(bg, f3(1.0f)) > 0.0f) {
                         float fpdf, rpdf;
                         const float3 refl = bsdf_evaluate(sf, -d, sdir, fpdf, rpdf);
-                        const float mis = (1.0f * 1.0f) / (1.0f * 1.0f + 1.0f * fpdf);
-                        const float3 smp = mis * refl * bg * (1.0f / 1.0f);
+                        const float mis = (1.0f * spdf) / (1.0f * spdf + 1.0f * fpdf);
+                        const float3 smp = mis * refl * bg * (1.0f / spdf);
                         if (dot(smp, f3(1.0f)) > 0.0f) {
                             const float3 so = offset_origin(pos, sf.n, err, sdir, 0.1f);
                             const float3 c = smp * thr;
@@ -511,8 +520,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 if (!ok) {
                     alive = false;
                 } else if (deferred) {
-                    // balance heuristic against the background density (BackgroundLightingPdf = 1 / (4 pi))
-                    const float mis = (1.0f * bs.forward_pdf) / (1.0f * bs.forward_pdf + 1.0f * kInv4Pi);
+                    // balance heuristic against the background density (BackgroundLightingPdf, AreaLighting.cpp:
+                    // 404-413: the image's density, else 1 / (4 pi))
+                    const float sky_pdf = S.ibl ? ibl_pdf(*S.ibl, bs.wi) : kInv4Pi;
+                    const float mis = (1.0f * bs.forward_pdf) / (1.0f * bs.forward_pdf + 1.0f * sky_pdf);
+                    if (!(bs.flags & kDiracEvent)) thr4.w = 0.0f;  // diracScatterOnly
                     const float3 t = mis * thr * bs.reflectance;
                     if (dot(t, t) == 0.0f) {
                         alive = false;
@@ -545,9 +557,11 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                 P.st.ray_o[s] = make_float4(no.x, no.y, no.z, 0.0f);
                 P.st.ray_d[s] = make_float4(nd.x, nd.y, nd.z, kFloatMax);
             } else {
-                // miss: background (EvaluateBackground / EvaluateBackgroundMiss without an IBL)
-                accumulate(J.accum, npix, deferred ? 0 : 1, pixel,
-                           f3(S.background[0], S.background[1], S.background[2]) * thr);
+                // miss: EvaluateBackgroundMiss for a camera ray or a pure specular chain, else EvaluateBackground
+                // (AreaLighting.cpp:415-436): the image's miss / light texel, or the uniform background
+                float3 bg = f3(S.background[0], S.background[1], S.background[2]);
+                if (S.ibl) bg = thr4.w != 0.0f ? ibl_miss(*S.ibl, d) : ibl_radiance(*S.ibl, d);
+                accumulate(J.accum, npix, deferred ? 0 : 1, pixel, bg * thr);
                 alive = false;
             }
             if (alive) {

@@ -13,6 +13,7 @@ namespace sel {
 struct MaterialDev;
 struct QuadLight;
 struct InstanceRecord;
+struct IblDev;
 
 constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
                                 // [8] holds the current batch size, [32..47] material-class counts,
@@ -36,6 +37,7 @@ struct PtScene {
     float background[3];
     uint32_t sort_hint;  // 1: the scene has Ptex materials or several material classes (sort before shading)
     const InstanceRecord* insts;  // instance table (null: no instances); lights and background stay this scene's
+    const IblDev* ibl;            // image-based light (null: the uniform background)
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.

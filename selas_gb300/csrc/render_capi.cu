@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "capi_internal.h"
+#include "ibl.cuh"
 #include "pt.h"
 #include "vcm.h"
 
@@ -66,6 +67,91 @@ int upload(void*& dst, const T* src, size_t count) {
 }  // namespace
 
 namespace sel {
+
+void ibl_densities(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& mdf, std::vector<float>& cdf) {
+    mdf.assign(height, 0.0f);
+    cdf.assign(size_t(width) * height, 0.0f);
+    const float heightf = float(height);
+    std::vector<float> intensity(size_t(width) * height);
+    for (uint32_t y = 0; y < height; ++y) {
+        const float theta = (float(y) + 0.5f) * kPi / heightf;
+        const float sin_theta = std::sin(theta);
+        for (uint32_t x = 0; x < width; ++x) {
+            const float* c = rgb + (size_t(y) * width + x) * 3;
+            intensity[size_t(y) * width + x] = sin_theta * (c[0] * 0.299f + c[1] * 0.587f + c[2] * 0.114f);
+        }
+    }
+    float marginal_sum = 0.0f;
+    for (uint32_t y = 0; y < height; ++y) {
+        float row_sum = 0.0f;
+        for (uint32_t x = 0; x < width; ++x) row_sum += intensity[size_t(y) * width + x];
+        mdf[y] = row_sum;
+        marginal_sum += row_sum;
+        if (row_sum > 0.0f) {
+            const float oo = 1.0f / row_sum;
+            float integral = 0.0f;
+            for (uint32_t x = 0; x < width; ++x) {
+                integral += oo * intensity[size_t(y) * width + x];
+                cdf[size_t(y) * width + x] = integral;
+            }
+        }
+        cdf[size_t(y) * width + width - 1] = 1.0f;  // floating-point imprecision, as the reference
+    }
+    if (marginal_sum > 0.0f) {
+        const float oo = 1.0f / marginal_sum;
+        float integral = 0.0f;
+        for (uint32_t y = 0; y < height; ++y) {
+            integral += mdf[y] * oo;
+            mdf[y] = integral;
+        }
+    }
+    mdf[height - 1] = 1.0f;
+}
+
+// One device block: the IblDev record, then its marginal and conditional CDFs and the two images (float4 texels).
+static int upload_ibl(SelSceneTy* sc) {
+    if (sc->d_ibl) cudaFree(sc->d_ibl);
+    sc->d_ibl = nullptr;
+    if (!sc->ibl_w) return SEL_OK;
+    std::vector<float> mdf, cdf;
+    ibl_densities(sc->ibl_light.data(), sc->ibl_w, sc->ibl_h, mdf, cdf);
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t n_light = size_t(sc->ibl_w) * sc->ibl_h, n_miss = size_t(sc->ibl_mw) * sc->ibl_mh;
+    const size_t o_mdf = up(sizeof(IblDev)), o_cdf = o_mdf + up(mdf.size() * 4), o_light = o_cdf + up(cdf.size() * 4);
+    const size_t o_miss = o_light + up(n_light * 16), total = o_miss + up(n_miss * 16);
+    std::vector<unsigned char> host(total, 0);
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, total);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(image-based light)");
+    char* base = static_cast<char*>(d);
+    IblDev v;
+    v.mdf = reinterpret_cast<const float*>(base + o_mdf);
+    v.cdf = reinterpret_cast<const float*>(base + o_cdf);
+    v.light = reinterpret_cast<const float4*>(base + o_light);
+    v.miss = reinterpret_cast<const float4*>(base + o_miss);
+    v.width = sc->ibl_w;
+    v.height = sc->ibl_h;
+    v.miss_width = sc->ibl_mw;
+    v.miss_height = sc->ibl_mh;
+    v.rotation = sc->ibl_rotation;
+    v.exposure = sc->ibl_exposure;
+    std::memcpy(host.data(), &v, sizeof(v));
+    std::memcpy(host.data() + o_mdf, mdf.data(), mdf.size() * 4);
+    std::memcpy(host.data() + o_cdf, cdf.data(), cdf.size() * 4);
+    float* lt = reinterpret_cast<float*>(host.data() + o_light);
+    for (size_t i = 0; i < n_light; ++i)
+        for (int c = 0; c < 3; ++c) lt[4 * i + c] = sc->ibl_light[3 * i + c];
+    float* ms = reinterpret_cast<float*>(host.data() + o_miss);
+    for (size_t i = 0; i < n_miss; ++i)
+        for (int c = 0; c < 3; ++c) ms[4 * i + c] = sc->ibl_miss[3 * i + c];
+    e = cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "uploading the image-based light");
+    }
+    sc->d_ibl = d;
+    return SEL_OK;
+}
 
 // Material classes (bit shader * 4 + Ptex * 2 + transparent) and Ptex use of a scene and the scenes its
 // instances reference.
@@ -139,6 +225,7 @@ int sync_shading(SelSceneTy* sc) {
     if (int rc = upload(sc->d_materials, mats.data(), mats.size())) return rc;
     if (int rc = upload(sc->d_lights, lights.data(), lights.size())) return rc;
     if (int rc = upload(sc->d_light_sets, sets.data(), sets.size())) return rc;
+    if (int rc = upload_ibl(sc)) return rc;
     if (sc->d_view) {
         ShadeView v;
         v.materials = static_cast<const MaterialDev*>(sc->d_materials);
@@ -231,6 +318,7 @@ PtScene scene_view(const SelSceneTy* sc) {
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
     ps.sort_hint = (sc->sort_hint && sc->dev->material_sort) ? 1u : 0u;
     ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
+    ps.ibl = static_cast<const IblDev*>(sc->d_ibl);
     return ps;
 }
 
@@ -528,6 +616,41 @@ int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* f
             return SEL_OK;
         }
     scene->ptex.push_back(std::move(pb));
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_set_ibl(SelScene scene, const float* rgb, unsigned int width, unsigned int height, const float* miss_rgb,
+                      unsigned int miss_width, unsigned int miss_height, float rotationRadians, float exposureScale) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (width && (!rgb || height == 0)) return fail(SEL_ERR_INVALID_ARGUMENT, "image is null or empty");
+    if (width > 32768 || height > 32768) return fail(SEL_ERR_INVALID_ARGUMENT, "image sides must be at most 32768");
+    if (miss_rgb && (miss_width == 0 || miss_height == 0 || miss_width > 32768 || miss_height > 32768))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "miss image sides must lie in 1..32768");
+    if (!std::isfinite(rotationRadians) || !std::isfinite(exposureScale))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "rotation and exposure must be finite");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    try {
+        scene->ibl_light.assign(rgb, rgb + size_t(width) * height * 3 * (width ? 1 : 0));
+        if (miss_rgb && width) {
+            scene->ibl_miss.assign(miss_rgb, miss_rgb + size_t(miss_width) * miss_height * 3);
+            scene->ibl_mw = miss_width;
+            scene->ibl_mh = miss_height;
+        } else {  // the miss image defaults to the light image times the exposure
+            scene->ibl_miss.resize(scene->ibl_light.size());
+            for (size_t i = 0; i < scene->ibl_light.size(); ++i) scene->ibl_miss[i] = exposureScale * scene->ibl_light[i];
+            scene->ibl_mw = width;
+            scene->ibl_mh = height;
+        }
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    for (float v : scene->ibl_light)
+        if (!std::isfinite(v) || v < 0.0f) return fail(SEL_ERR_INVALID_ARGUMENT, "image values must be finite and >= 0");
+    scene->ibl_w = width;
+    scene->ibl_h = width ? height : 0;
+    scene->ibl_rotation = rotationRadians;
+    scene->ibl_exposure = exposureScale;
     scene->shading_dirty = true;
     return SEL_OK;
 }

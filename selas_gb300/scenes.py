@@ -192,6 +192,7 @@ class RenderScene:
     background: tuple = (0.0, 0.0, 0.0)
     camera: dict = field(default_factory=dict)      # position, look_at, up, fov_degrees
     ptex: dict = field(default_factory=dict)        # geomID -> (face rows (n, 8) int32, texels float16)
+    ibl: dict = None                                # light (H, W, 3), miss (h, w, 3) or None, rotation, exposure
 
     def ptex_tables(self, material_recs=None):
         """Combined face table (rows rebased) and texels of all textured geometries, in geomID order; writes
@@ -222,6 +223,9 @@ class RenderScene:
         for ls, l in self.lights:
             sc.add_quad_light(ls, l["position"], l["direction"], l["x"], l["z"], l["radiance"])
         sc.set_background(self.background)
+        if self.ibl:
+            sc.set_ibl(self.ibl["light"], self.ibl.get("miss"), self.ibl.get("rotation", 0.0),
+                       self.ibl.get("exposure", 1.0))
         for gid in sorted(self.ptex):
             rows, tex = self.ptex[gid]
             sc.set_ptex(gid, rows, tex)
@@ -532,6 +536,8 @@ class InstancedRenderScene:
             for ls, l in p.lights:
                 sc.add_quad_light(ls, l["position"], l["direction"], l["x"], l["z"], l["radiance"])
             sc.set_background(p.background)
+            if p.ibl:
+                sc.set_ibl(p.ibl["light"], p.ibl.get("miss"), p.ibl.get("rotation", 0.0), p.ibl.get("exposure", 1.0))
             for gid in sorted(p.ptex):
                 rows, tex = p.ptex[gid]
                 sc.set_ptex(gid, rows, tex)
@@ -676,3 +682,34 @@ def terrain_views(scene: InstancedRenderScene, count: int = 16):
         cams.append(dict(position=(r * np.cos(a), y, r * np.sin(a)), look_at=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
                          fov_degrees=60.0))
     return cams
+
+
+def sky_ibl(width: int = 256, height: int = 128, sun=(0.4, 0.75, 0.3), sun_radius: float = 0.06,
+            sun_radiance=(60.0, 52.0, 40.0), miss_size=(64, 32), rotation: float = 0.3, exposure: float = 1.5,
+            seed: int = 0x5E1A5105) -> dict:
+    """A synthetic latitude-longitude sky for the image-based light: a zenith-to-horizon gradient with seeded
+    value-noise clouds, a dark ground hemisphere and a bright sun disc; the miss image is a coarser copy
+    without the sun.  Returns the dict RenderScene.ibl takes."""
+    rng = np.random.default_rng(seed)
+
+    def image(w, h, with_sun):
+        theta = (np.arange(h, dtype=np.float64) + 0.5) * np.pi / h
+        phi = (np.arange(w, dtype=np.float64) + 0.5) * 2 * np.pi / w - np.pi
+        th, ph = np.meshgrid(theta, phi, indexing="ij")
+        d = np.stack([np.sin(th) * np.cos(ph), np.cos(th), np.sin(th) * np.sin(ph)], -1)
+        up = np.clip(d[..., 1], 0.0, 1.0)[..., None]
+        sky = (1.0 - up) * np.array([0.9, 0.95, 1.0]) + up * np.array([0.25, 0.4, 0.85])
+        ground = np.array([0.12, 0.1, 0.08])
+        img = np.where(d[..., 1:2] > 0, sky, ground)
+        lat = rng.uniform(0.7, 1.3, size=(8, 16))
+        iy = np.minimum((th / np.pi * 8).astype(int), 7)
+        ix = np.minimum(((ph + np.pi) / (2 * np.pi) * 16).astype(int), 15)
+        img = img * lat[iy, ix][..., None]
+        if with_sun:
+            s = np.array(sun, np.float64)
+            s /= np.linalg.norm(s)
+            img = np.where((np.arccos(np.clip(d @ s, -1, 1)) < sun_radius)[..., None], np.array(sun_radiance), img)
+        return img.astype(np.float32)
+
+    return dict(light=image(width, height, True), miss=image(miss_size[0], miss_size[1], False), rotation=rotation,
+                exposure=exposure)
