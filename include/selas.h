@@ -144,6 +144,18 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
  * requires committing `scene` again.  Scenes with instances use the SEL_BVH_WIDE8_Q8 layout. */
 int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld);
 int sel_scene_commit(SelScene scene);
+/* Per-vertex attributes: rtcSetGeometryVertexAttributeCount + rtcSetSharedGeometryBuffer(
+ * RTC_BUFFER_TYPE_VERTEX_ATTRIBUTE, slot, RTC_FORMAT_FLOAT<components>) (ModelResource.cpp:183-197).  Slot 0..3
+ * of mesh geomID gets vertex_count records of `components` (1..4) floats (copied; vertex_count must equal the
+ * mesh's).  As CalculateSurfaceParams reads them (SurfaceParameters.cpp:157-184), the integrators take slot 0
+ * (3 floats) as shading normals and slot 1 (4 floats: xyz and the bitangent sign) as tangents; slot 2 holds uvs. */
+int sel_scene_set_vertex_attribute(SelScene scene, unsigned int geomID, unsigned int slot, const float* data,
+                                   size_t vertex_count, unsigned int components);
+/* rtcInterpolate0 (rtcore_geometry.h; called at SurfaceParameters.cpp:162,176,188): attribute `slot` of mesh
+ * geomID at barycentrics (u, v) of triangle primID, (1 - u - v) a0 + u a1 + v a2 per component, `count` floats
+ * (at most the attribute's components) to out.  Host-side, from the scene's copies. */
+int sel_interpolate0(SelScene scene, unsigned int geomID, unsigned int primID, float u, float v, unsigned int slot,
+                     float* out, unsigned int count);
 int sel_scene_get_info(SelScene scene, SelSceneInfo* out_info);
 int sel_scene_release(SelScene scene);
 

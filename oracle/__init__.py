@@ -44,6 +44,7 @@ def lib() -> ctypes.CDLL:
                                 ctypes.c_float, ctypes.c_float], None),
             "oracle_ibl_sample": ([_vp, _i, _vp, _vp], None),
             "oracle_ibl_pdf": ([_vp, _i, _vp], None),
+            "oracle_set_attributes": ([_i64, _vp, _vp, _vp], None),
             "oracle_instanced_query": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i, _i],
                                        None),
             "oracle_affine_inverse": ([_vp, _vp], _i),
@@ -150,6 +151,18 @@ def set_ibl(ibl):
                          0 if m is None else m.shape[0], float(ibl.get("rotation", 0.0)), float(ibl.get("exposure", 1.0)))
 
 
+def set_attributes(parts):
+    """Vertex attributes of the next oracle renders' soup: the RenderScenes whose meshes make it, in order."""
+    soups = [p.attribute_soup() for p in parts]
+    n = np.ascontiguousarray(np.concatenate([s[0] for s in soups]))
+    t = np.ascontiguousarray(np.concatenate([s[1] for s in soups]))
+    f = np.ascontiguousarray(np.concatenate([s[2] for s in soups]))
+    if not f.any():
+        lib().oracle_set_attributes(0, None, None, None)
+        return
+    lib().oracle_set_attributes(f.shape[0], _p(n), _p(t), _p(f))
+
+
 def ibl_sample(ibl, r):
     """Oracle IBL sampling of (n, 2) uniforms: (n, 7) [dir, radiance, pdf] and (n, 7) [pdf, light rgb, miss rgb]
     looked up again for the sampled directions."""
@@ -175,6 +188,7 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
     shape (2, height, width, 3)."""
     from selas_gb300.scenes import light_records, material_records
     set_ibl(getattr(render_scene, "ibl", None))
+    set_attributes([render_scene])
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)
@@ -198,6 +212,7 @@ def deferred_render(render_scene, width, height, sample_begin, sample_end, sampl
     the GPU's streams; "mt": MT19937 per pixel as the reference's sampler."""
     from selas_gb300.scenes import light_records, material_records
     set_ibl(getattr(render_scene, "ibl", None))
+    set_attributes([render_scene])
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)
@@ -269,6 +284,7 @@ def graph_render(iscene, width, height, begin, end, max_bounces=8, seed=0x5E1A50
     FP64 sums."""
     from selas_gb300.scenes import light_records, material_records
     set_ibl(iscene.parts[0].ibl)
+    set_attributes(iscene.parts)
     V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
     mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
     for part in iscene.parts:
@@ -344,6 +360,7 @@ def vcm_render(render_scene, width, height, iter_begin, iter_end, max_len=10, ra
     (height, width, 3).  radius0 defaults to 0.0025 x the scene's bounding-sphere radius (VCM.cpp:778 with
     VcmRadiusFactor_ = 0.0025), the sphere taken about the bounding box (radius = half its diagonal)."""
     from selas_gb300.scenes import light_records, material_records
+    set_attributes([render_scene])
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)

@@ -24,10 +24,12 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <random>
 #include <thread>
 #include <vector>
 
+#include "oracle_attrs.h"
 #include "oracle_bsdf.h"
 #include "oracle_ptex.h"
 #include "oracle_query.h"
@@ -294,9 +296,18 @@ struct Ibl {
     }
 };
 
+// Vertex attributes of the soup (oracle_set_attributes): per triangle, the three corners' shading normals and
+// tangents and flags (1 normals, 2 tangents); `first` maps (scene << 32 | geomID) to the mesh's first triangle.
+struct Attrs {
+    std::vector<float> normals, tangents;
+    std::vector<uint8_t> flags;
+    std::map<uint64_t, int64_t> first;
+};
+
 struct Scene {
     const void* bvh = nullptr;
     const Ibl* ibl = nullptr;                       // image-based light (null: the uniform background)
+    const Attrs* attrs = nullptr;                   // vertex attributes (null: none)
     const void* graph = nullptr;                    // instanced scene graph (replaces bvh when set)
     std::vector<std::vector<Material>> gmats;       // graph: materials of each scene, by geomID
     std::vector<const orp::Texture*> gptex;         // graph: Ptex of each scene (null: none)
@@ -335,6 +346,43 @@ struct SurfHit {
     V3 n, view;
 };
 
+// Shading frame of a hit (CalculateSurfaceParams, SurfaceParameters.cpp:157-184): interpolated vertex normal and
+// tangent where the mesh has them, through the entered instances' localToWorld.
+void shading_frame(const Scene& sc, const orq::Hit& h, V3& n, V3& t, V3& b) {
+    // shading normal and tangent from vertex attributes (SurfaceParameters.cpp:157-184)
+    int64_t ai = -1;
+    if (sc.attrs) {
+        const auto it = sc.attrs->first.find((uint64_t(h.scene) << 32) | h.geom);
+        if (it != sc.attrs->first.end()) ai = it->second + h.prim;
+    }
+    const uint8_t aflags = ai >= 0 ? sc.attrs->flags[size_t(ai)] : 0;
+    auto lerp = [&](float a0, float a1, float a2) {
+        const float w = 1.0f - h.u - h.v;
+        return w * a0 + h.u * a1 + h.v * a2;
+    };
+    V3 ngv(h.ng[0], h.ng[1], h.ng[2]);
+    if (aflags & 1u) {
+        const float* c = &sc.attrs->normals[size_t(ai) * 9];
+        ngv = V3(lerp(c[0], c[3], c[6]), lerp(c[1], c[4], c[7]), lerp(c[2], c[5], c[8]));
+    }
+    if (h.l2w[1]) ngv = xvector(h.l2w[1], ngv);
+    if (h.l2w[0]) ngv = xvector(h.l2w[0], ngv);
+    n = orc::Norm(ngv);
+    if (aflags & 2u) {
+        const float* c = &sc.attrs->tangents[size_t(ai) * 12];
+        V3 tl(lerp(c[0], c[4], c[8]), lerp(c[1], c[5], c[9]), lerp(c[2], c[6], c[10]));
+        const float sign = lerp(c[3], c[7], c[11]);
+        if (h.l2w[1]) tl = xvector(h.l2w[1], tl);
+        if (h.l2w[0]) tl = xvector(h.l2w[0], tl);
+        t = tl;
+        b = orc::Cross(n, t) * sign;
+    } else {
+        if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
+        else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
+        b = orc::Cross(n, t);
+    }
+}
+
 // Instanced hits (ModelDataFromRayIds, SceneResource.cpp:362-378): material and Ptex of the hit mesh's scene;
 // the object-space normal through the instances' localToWorld, innermost first (SurfaceParameters.cpp:161-168).
 void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) {
@@ -344,14 +392,8 @@ void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) 
     o.m = &m;
     o.err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(pos.x), std::fabs(pos.y)), std::max(std::fabs(pos.z), h.t));
     orc::Surf& s = o.s;
-    V3 ngv(h.ng[0], h.ng[1], h.ng[2]);
-    if (h.l2w[1]) ngv = xvector(h.l2w[1], ngv);
-    if (h.l2w[0]) ngv = xvector(h.l2w[0], ngv);
-    const V3 n = orc::Norm(ngv);
-    V3 t, b;
-    if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
-    else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
-    b = orc::Cross(n, t);
+    V3 n, t, b;
+    shading_frame(sc, h, n, t, b);
     s.t = t; s.n = n; s.b = b;
     float base[3] = {m.base[0], m.base[1], m.base[2]};
     if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
@@ -708,6 +750,16 @@ static void run_deferred(const Scene& sc, const float* camera, uint32_t width, u
 
 // The image-based light the renderers use (oracle_set_ibl; none when its width is 0).
 static Ibl g_ibl;
+// The vertex attributes of the next render's soup (oracle_set_attributes; none when empty).
+static Attrs g_attrs;
+
+// Maps each mesh of a soup (triangles of one (scene, geomID) are contiguous, primID counting from 0) to its first
+// triangle.
+static void index_attrs(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene, int64_t ntri) {
+    g_attrs.first.clear();
+    for (int64_t i = 0; i < ntri; ++i)
+        if (prim[i] == 0) g_attrs.first[(uint64_t(tri_scene ? tri_scene[i] : 0) << 32) | geom[i]] = i;
+}
 
 // Scene tables of the oracle renderers' common arguments; returns the Ptex texture to delete.
 static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
@@ -735,6 +787,10 @@ static orp::Texture* load_scene(Scene& sc, const float* verts, const uint32_t* p
     }
     sc.background = V3(background[0], background[1], background[2]);
     sc.ibl = g_ibl.w ? &g_ibl : nullptr;
+    if (!g_attrs.flags.empty() && ntri > 0) {
+        index_attrs(prim, geom, nullptr, ntri);
+        sc.attrs = &g_attrs;
+    }
     return tex;
 }
 
@@ -822,6 +878,10 @@ void oracle_graph_render(int n_scenes, const float* verts, const uint32_t* prim,
     sc.bvh = nullptr;
     sc.graph = orq::build_graph(n_scenes, verts, prim, geom, tri_scene, ntri, l2w, inst_id, inst_scene, inst_proto,
                                 ninst, top);
+    if (!g_attrs.flags.empty()) {
+        index_attrs(prim, geom, tri_scene, ntri);
+        sc.attrs = &g_attrs;
+    }
     std::vector<orp::Texture*> owned;
     for (int s = 0; s < n_scenes; ++s) {
         std::vector<Material> mats;
@@ -878,3 +938,45 @@ void oracle_ibl_pdf(const float* dirs, int n, float* out) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Vertex attributes of the soup of the next renders (n triangles in the soup's order): corner normals (n x 9),
+// corner tangents (n x 12) and flags (1 normals, 2 tangents); n = 0 clears them.
+void oracle_set_attributes(int64_t n, const float* normals, const float* tangents, const uint8_t* flags) {
+    g_attrs = Attrs();
+    if (n <= 0) return;
+    g_attrs.normals.assign(normals, normals + 9 * n);
+    g_attrs.tangents.assign(tangents, tangents + 12 * n);
+    g_attrs.flags.assign(flags, flags + n);
+}
+
+}  // extern "C"
+
+namespace ora {
+
+bool index(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene, int64_t ntri) {
+    if (g_attrs.flags.empty() || ntri <= 0) return false;
+    index_attrs(prim, geom, tri_scene, ntri);
+    return true;
+}
+
+void frame(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, const float ng[3], float n[3], float t[3],
+           float b[3]) {
+    orq::Hit h;
+    h.u = u;
+    h.v = v;
+    h.prim = prim;
+    h.geom = geom;
+    h.scene = scene;
+    for (int k = 0; k < 3; ++k) h.ng[k] = ng[k];
+    Scene sc;
+    sc.attrs = g_attrs.flags.empty() ? nullptr : &g_attrs;
+    V3 nn, tt, bb;
+    shading_frame(sc, h, nn, tt, bb);
+    n[0] = nn.x; n[1] = nn.y; n[2] = nn.z;
+    t[0] = tt.x; t[1] = tt.y; t[2] = tt.z;
+    b[0] = bb.x; b[1] = bb.y; b[2] = bb.z;
+}
+
+}  // namespace ora

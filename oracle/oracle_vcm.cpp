@@ -26,6 +26,7 @@
 #include <thread>
 #include <vector>
 
+#include "oracle_attrs.h"
 #include "oracle_bsdf.h"
 #include "oracle_ptex.h"
 #include "oracle_query.h"
@@ -120,12 +121,12 @@ bool make_hit(const Scene& sc, V3 org, V3 dir, Hit& out) {
     out.pos = V3(org.x + h.t * dir.x, org.y + h.t * dir.y, org.z + h.t * dir.z);
     out.err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(out.pos.x), std::fabs(out.pos.y)),
                                               std::max(std::fabs(out.pos.z), h.t));
-    const V3 n = orc::Norm(V3(h.ng[0], h.ng[1], h.ng[2]));
-    V3 t;
-    if (std::fabs(n.x) > std::fabs(n.y)) t = V3(-n.z, 0, n.x) * (1.0f / std::sqrt(n.x * n.x + n.z * n.z));
-    else t = V3(0, n.z, -n.y) * (1.0f / std::sqrt(n.y * n.y + n.z * n.z));
+    // shading frame, with vertex normals and tangents where the mesh has them (SurfaceParameters.cpp:157-184)
+    float fn[3], ft[3], fb[3];
+    ora::frame(0, h.geom, h.prim, h.u, h.v, h.ng, fn, ft, fb);
+    const V3 n(fn[0], fn[1], fn[2]);
     orc::Surf& s = out.s;
-    s.t = t; s.n = n; s.b = orc::Cross(n, t);
+    s.t = V3(ft[0], ft[1], ft[2]); s.n = n; s.b = V3(fb[0], fb[1], fb[2]);
     float base[3] = {m.base[0], m.base[1], m.base[2]};
     if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
@@ -297,6 +298,7 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
     const bool use_nee = strategies & 1, use_vc = strategies & 2, use_vm = strategies & 4, use_lt = strategies & 8;
     Scene sc;
     sc.bvh = orq::build(verts, prim, geom, ntri);
+    ora::index(prim, geom, nullptr, ntri);
     orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
     sc.ptex = tex;
     sc.max_len = max_len;

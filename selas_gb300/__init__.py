@@ -74,6 +74,8 @@ _SIGNATURES = {
     "sel_scene_attach_triangle_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
     "sel_scene_commit": [_vp],
     "sel_scene_attach_instance": [_vp, _u, _vp, _vp],
+    "sel_scene_set_vertex_attribute": [_vp, _u, _u, _vp, _sz, _u],
+    "sel_interpolate0": [_vp, _u, _u, ctypes.c_float, ctypes.c_float, _u, _vp, _u],
     "sel_scene_get_info": [_vp, ctypes.POINTER(SceneInfo)],
     "sel_scene_release": [_vp],
     "sel_intersect1": [_vp, _vp],
@@ -173,6 +175,17 @@ class Scene:
         m[:a.shape[0], :] = a
         cm = np.ascontiguousarray(m.T.astype(np.float32)).reshape(16)
         check(lib().sel_scene_attach_instance(self.handle, inst_id, instanced.handle, _ptr(cm)))
+
+    def set_vertex_attribute(self, geom_id: int, slot: int, data) -> None:
+        """Per-vertex attribute of a mesh (slot 0: normals (n, 3); slot 1: tangents (n, 4); 2..3: anything)."""
+        a = np.ascontiguousarray(data, np.float32)
+        a = a.reshape(a.shape[0], -1)
+        check(lib().sel_scene_set_vertex_attribute(self.handle, geom_id, slot, _ptr(a), a.shape[0], a.shape[1]))
+
+    def interpolate0(self, geom_id: int, prim_id: int, u: float, v: float, slot: int, count: int) -> np.ndarray:
+        out = np.zeros(count, np.float32)
+        check(lib().sel_interpolate0(self.handle, geom_id, prim_id, u, v, slot, _ptr(out), count))
+        return out
 
     def commit(self) -> None:
         check(lib().sel_scene_commit(self.handle))

@@ -210,6 +210,53 @@ int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene inst
     return SEL_OK;
 }
 
+int sel_scene_set_vertex_attribute(SelScene scene, unsigned int geomID, unsigned int slot, const float* data,
+                                   size_t vertex_count, unsigned int components) {
+    if (!scene || (!data && vertex_count)) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (slot > 3 || components < 1 || components > 4)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "slot must lie in 0..3 and components in 1..4");
+    if ((slot == 0 && components != 3) || (slot == 1 && components != 4))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "slot 0 (normals) takes 3 floats and slot 1 (tangents) 4");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    for (MeshInput& m : scene->meshes) {
+        if (m.geomID != geomID) continue;
+        if (vertex_count != m.vertices.size() / 3)
+            return fail(SEL_ERR_INVALID_ARGUMENT, "vertex_count differs from the mesh's vertex count");
+        for (size_t i = 0; i < vertex_count * components; ++i)
+            if (!std::isfinite(data[i])) return fail(SEL_ERR_INVALID_ARGUMENT, "non-finite attribute");
+        try {
+            m.attr[slot].assign(data, data + vertex_count * components);
+        } catch (const std::bad_alloc&) {
+            return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+        }
+        m.attr_n[slot] = components;
+        scene->shading_dirty = true;
+        return SEL_OK;
+    }
+    return fail(SEL_ERR_INVALID_ARGUMENT, "no mesh with this geomID");
+}
+
+int sel_interpolate0(SelScene scene, unsigned int geomID, unsigned int primID, float u, float v, unsigned int slot,
+                     float* out, unsigned int count) {
+    if (!scene || !out) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (slot > 3) return fail(SEL_ERR_INVALID_ARGUMENT, "slot must lie in 0..3");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    for (const MeshInput& m : scene->meshes) {
+        if (m.geomID != geomID) continue;
+        const uint32_t n = m.attr_n[slot];
+        if (!n) return fail(SEL_ERR_INVALID_OPERATION, "the mesh has no attribute in this slot");
+        if (count > n) return fail(SEL_ERR_INVALID_ARGUMENT, "count exceeds the attribute's components");
+        if (size_t(primID) * 3 + 2 >= m.indices.size()) return fail(SEL_ERR_INVALID_ARGUMENT, "primID out of range");
+        const float* a0 = &m.attr[slot][size_t(m.indices[3 * size_t(primID)]) * n];
+        const float* a1 = &m.attr[slot][size_t(m.indices[3 * size_t(primID) + 1]) * n];
+        const float* a2 = &m.attr[slot][size_t(m.indices[3 * size_t(primID) + 2]) * n];
+        const float w = 1.0f - u - v;
+        for (unsigned int k = 0; k < count; ++k) out[k] = w * a0[k] + u * a1[k] + v * a2[k];
+        return SEL_OK;
+    }
+    return fail(SEL_ERR_INVALID_ARGUMENT, "no mesh with this geomID");
+}
+
 int sel_scene_set_build_mode(SelScene scene, int build_mode) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     if (build_mode != SEL_BUILD_HOST && build_mode != SEL_BUILD_DEVICE)
@@ -467,7 +514,7 @@ int sel_scene_release(SelScene scene) {
     for (auto& r : scene->referenced) --r.first->instanced_by;
     for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
                     scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
-                    scene->vcm_block, scene->d_insts, scene->d_view, scene->d_ibl})
+                    scene->vcm_block, scene->d_insts, scene->d_view, scene->d_ibl, scene->d_attrs})
         if (p) cudaFree(p);
     delete scene;
     return SEL_OK;

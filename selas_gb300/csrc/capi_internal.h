@@ -60,6 +60,8 @@ struct SelSceneTy {
     uint32_t ibl_w = 0, ibl_h = 0, ibl_mw = 0, ibl_mh = 0;
     float ibl_rotation = 0.0f, ibl_exposure = 1.0f;
     void* d_ibl = nullptr;  // IblDev followed by its arrays (null: no image)
+    void* d_attrs = nullptr;  // MeshAttrDev table by geomID, then the index, normal and tangent arrays
+    uint32_t attr_count = 0;
     bool shading_dirty = true;
     struct PtexBinding {
         uint32_t geomID;

@@ -187,6 +187,8 @@ struct HitRef {
     uint32_t ptex_count;
     const void* ptex_faces;
     const void* ptex_texels;
+    const MeshAttrDev* attrs;
+    uint32_t attr_count;
     const InstanceRecord* rec0;
     const InstanceRecord* rec1;
 };
@@ -201,6 +203,8 @@ __device__ __forceinline__ HitRef hit_ref(const PtState& st, const PtScene& S, u
     r.ptex_faces = S.ptex_faces;
     r.ptex_texels = S.ptex_texels;
     r.ptex_count = S.ptex_face_count;
+    r.attrs = S.attrs;
+    r.attr_count = S.attr_count;
     if (kInst) {
         const uint2 hi = st.hinst[s];
         if (hi.x) {
@@ -217,6 +221,8 @@ __device__ __forceinline__ HitRef hit_ref(const PtState& st, const PtScene& S, u
             r.ptex_faces = v->ptex_faces;
             r.ptex_texels = v->ptex_texels;
             r.ptex_count = v->ptex_face_count;
+            r.attrs = v->attrs;
+            r.attr_count = v->attr_count;
         }
     }
     r.tp = tris + size_t(tri) * 3;
@@ -425,9 +431,13 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
             if (tri != 0xffffffffu) {
                 const HitRef hr = hit_ref<kInst>(P.st, S, s, tri);
                 const float4 p0 = __ldg(hr.tp), p1 = __ldg(hr.tp + 1), p2 = __ldg(hr.tp + 2);
-                const float3 ng = kInst ? world_normal(hr, triangle_ng(p0, p1, p2)) : triangle_ng(p0, p1, p2);
                 const uint32_t geom = __float_as_uint(p1.w);
                 const MaterialDev& m = hr.mats[geom < hr.mat_count ? geom : 0];
+                const MeshAttrDev* attr = geom < hr.attr_count ? hr.attrs + geom : nullptr;
+                float3 fn, ft, fb;
+                float fsign;
+                shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2),
+                              [&](float3 x) { return kInst ? world_normal(hr, x) : x; }, fn, ft, fb, fsign);
                 // RayPick error bound (PathTracer.cpp:134-136)
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
@@ -436,7 +446,7 @@ __global__ void __launch_bounds__(kBlock) k_shade(PtParams P, int cur, uint32_t 
                     const float4 b = P.st.base[s];
                     base = f3(b.x, b.y, b.z);
                 }
-                const Surface sf = make_surface(m, ng, -d, base);
+                const Surface sf = make_surface_frame(m, ft, fn, fb, -d, pow3(base, 2.2f));
                 // Next-event estimation to the surface's light set (AreaLighting.cpp:353-373)
                 LightSample ls;
                 ls.radiance = f3(0.0f);

@@ -14,6 +14,7 @@ struct MaterialDev;
 struct QuadLight;
 struct InstanceRecord;
 struct IblDev;
+struct MeshAttrDev;
 
 constexpr int kPtCounters = 8;  // [0],[1] queue lengths, [2] shadow queue length, [3],[4] fetch cursors;
                                 // [8] holds the current batch size, [32..47] material-class counts,
@@ -38,6 +39,8 @@ struct PtScene {
     uint32_t sort_hint;  // 1: the scene has Ptex materials or several material classes (sort before shading)
     const InstanceRecord* insts;  // instance table (null: no instances); lights and background stay this scene's
     const IblDev* ibl;            // image-based light (null: the uniform background)
+    const MeshAttrDev* attrs;     // vertex attributes by geomID (null: none)
+    uint32_t attr_count;
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.

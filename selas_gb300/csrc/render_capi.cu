@@ -153,6 +153,59 @@ static int upload_ibl(SelSceneTy* sc) {
     return SEL_OK;
 }
 
+// One device block: the MeshAttrDev table (by geomID), then the vertex indices, normals (float3) and tangents
+// (float4) of the meshes that have shading normals or tangents.
+static int upload_attrs(SelSceneTy* sc) {
+    if (sc->d_attrs) cudaFree(sc->d_attrs);
+    sc->d_attrs = nullptr;
+    sc->attr_count = 0;
+    uint32_t max_geom = 0;
+    size_t n_idx = 0, n_nrm = 0, n_tan = 0;
+    for (const MeshInput& m : sc->meshes) {
+        if (!m.attr_n[0] && !m.attr_n[1]) continue;
+        max_geom = std::max(max_geom, m.geomID + 1);
+        n_idx += m.indices.size();
+        if (m.attr_n[0]) n_nrm += m.attr[0].size();
+        if (m.attr_n[1]) n_tan += m.attr[1].size();
+    }
+    if (!max_geom) return SEL_OK;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t o_idx = up(sizeof(MeshAttrDev) * max_geom), o_nrm = o_idx + up(n_idx * 4), o_tan = o_nrm + up(n_nrm * 4);
+    const size_t total = o_tan + up(n_tan * 4);
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, total);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(vertex attributes)");
+    char* base = static_cast<char*>(d);
+    std::vector<unsigned char> host(total, 0);
+    MeshAttrDev* table = reinterpret_cast<MeshAttrDev*>(host.data());
+    size_t ai = 0, an = 0, at = 0;
+    for (const MeshInput& m : sc->meshes) {
+        if (!m.attr_n[0] && !m.attr_n[1]) continue;
+        MeshAttrDev& t = table[m.geomID];
+        t.indices = reinterpret_cast<const uint32_t*>(base + o_idx + ai * 4);
+        std::memcpy(host.data() + o_idx + ai * 4, m.indices.data(), m.indices.size() * 4);
+        ai += m.indices.size();
+        if (m.attr_n[0]) {
+            t.normals = reinterpret_cast<const float*>(base + o_nrm + an * 4);
+            std::memcpy(host.data() + o_nrm + an * 4, m.attr[0].data(), m.attr[0].size() * 4);
+            an += m.attr[0].size();
+        }
+        if (m.attr_n[1]) {
+            t.tangents = reinterpret_cast<const float4*>(base + o_tan + at * 4);
+            std::memcpy(host.data() + o_tan + at * 4, m.attr[1].data(), m.attr[1].size() * 4);
+            at += m.attr[1].size();
+        }
+    }
+    e = cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "uploading vertex attributes");
+    }
+    sc->d_attrs = d;
+    sc->attr_count = max_geom;
+    return SEL_OK;
+}
+
 // Material classes (bit shader * 4 + Ptex * 2 + transparent) and Ptex use of a scene and the scenes its
 // instances reference.
 void tree_classes(const SelSceneTy* sc, uint32_t& mask, bool& ptex) {
@@ -226,6 +279,7 @@ int sync_shading(SelSceneTy* sc) {
     if (int rc = upload(sc->d_lights, lights.data(), lights.size())) return rc;
     if (int rc = upload(sc->d_light_sets, sets.data(), sets.size())) return rc;
     if (int rc = upload_ibl(sc)) return rc;
+    if (int rc = upload_attrs(sc)) return rc;
     if (sc->d_view) {
         ShadeView v;
         v.materials = static_cast<const MaterialDev*>(sc->d_materials);
@@ -233,6 +287,9 @@ int sync_shading(SelSceneTy* sc) {
         v.ptex_texels = sc->d_ptex_texels;
         v.material_count = uint32_t(mats.size());
         v.ptex_face_count = sc->ptex_face_count;
+        v.attrs = static_cast<const MeshAttrDev*>(sc->d_attrs);
+        v.attr_count = sc->attr_count;
+        v.pad = 0;
         cudaError_t e = cudaMemcpy(sc->d_view, &v, sizeof(v), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_fail(e, "shading view");
     }
@@ -319,6 +376,8 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.sort_hint = (sc->sort_hint && sc->dev->material_sort) ? 1u : 0u;
     ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     ps.ibl = static_cast<const IblDev*>(sc->d_ibl);
+    ps.attrs = static_cast<const MeshAttrDev*>(sc->d_attrs);
+    ps.attr_count = sc->attr_count;
     return ps;
 }
 

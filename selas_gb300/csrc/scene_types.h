@@ -31,12 +31,24 @@ static_assert(sizeof(MaterialDev) == 128, "MaterialDev must be 128 bytes");
 // Shading data of one scene as the integrators read it for hits inside instances of that scene (the model data
 // ModelDataFromRayIds finds, SceneResource.cpp:362-378): one fixed device record per scene, rewritten whenever
 // the scene's shading data is uploaded, so instance records can point at it.
+// Vertex attributes of one mesh the shading reads (by geomID): its triangles' vertex indices, shading normals
+// (slot 0, 3 floats per vertex) and tangents (slot 1, xyz + bitangent sign); null where absent.
+struct MeshAttrDev {
+    const uint32_t* indices;
+    const float* normals;
+    const float4* tangents;
+    const void* pad;
+};
+
 struct ShadeView {
     const MaterialDev* materials;
     const void* ptex_faces;   // PtexFace[]
     const void* ptex_texels;  // half RGB
     uint32_t material_count;
     uint32_t ptex_face_count;
+    const MeshAttrDev* attrs;  // by geomID (null: no mesh has attributes)
+    uint32_t attr_count;
+    uint32_t pad;
 };
 
 constexpr uint32_t kMaterialTransparent = 1u;  // DisneySolid with diffTrans or specTrans (BuildModel.cpp:60-65)

@@ -62,6 +62,8 @@ struct MeshInput {
     uint32_t geomID;
     std::vector<float> vertices;   // xyz packed
     std::vector<uint32_t> indices; // 3 per triangle
+    std::vector<float> attr[4];    // per-vertex attributes (sel_scene_set_vertex_attribute), attr_n[slot] floats each
+    uint32_t attr_n[4] = {0, 0, 0, 0};
 };
 
 struct BuiltBvh {

@@ -150,12 +150,46 @@ SEL_HD void orthonormal_basis(float3 v1, float3& v2, float3& v3) {
 }
 
 
-// CalculateSurfaceParams (Shading/SurfaceParameters.cpp:144-247) for meshes without shading normals,
-// tangents or uvs, from the unit geometric normal n and the linear base colour.
-SEL_HD Surface make_surface_linear(const MaterialDev& m, float3 n, float3 view, float3 base_color_linear) {
+// rtcInterpolate0 of a per-vertex attribute: (1 - u - v) a0 + u a1 + v a2 per component.
+SEL_HD float attr_lerp(float a0, float a1, float a2, float u, float v) {
+    const float w = 1.0f - u - v;
+    return w * a0 + u * a1 + v * a2;
+}
+
+// Shading frame of a hit (CalculateSurfaceParams, SurfaceParameters.cpp:157-184): the normal interpolated from
+// the mesh's vertex normals where it has them (else the geometric normal), the tangent from its vertex tangents
+// with b = cross(n, t) x the interpolated sign (returned in `sign`), else an orthonormal basis around n (sign 1).
+// `xf` carries a vector to world space (the instances' localToWorld; identity for a mesh of the rendered scene).
+template <typename Xf>
+SEL_HD void shading_frame(const MeshAttrDev* A, uint32_t prim, float u, float v, float3 ng, Xf xf, float3& n,
+                          float3& t, float3& b, float& sign) {
+    float3 nrm = ng;
+    if (A && A->normals) {
+        const uint32_t i0 = A->indices[3 * prim], i1 = A->indices[3 * prim + 1], i2 = A->indices[3 * prim + 2];
+        const float* a = A->normals;
+        nrm = f3(attr_lerp(a[3 * i0], a[3 * i1], a[3 * i2], u, v), attr_lerp(a[3 * i0 + 1], a[3 * i1 + 1], a[3 * i2 + 1], u, v),
+                 attr_lerp(a[3 * i0 + 2], a[3 * i1 + 2], a[3 * i2 + 2], u, v));
+    }
+    n = normalize(xf(nrm));
+    if (A && A->tangents) {
+        const uint32_t i0 = A->indices[3 * prim], i1 = A->indices[3 * prim + 1], i2 = A->indices[3 * prim + 2];
+        const float4 a0 = A->tangents[i0], a1 = A->tangents[i1], a2 = A->tangents[i2];
+        const float3 tl = f3(attr_lerp(a0.x, a1.x, a2.x, u, v), attr_lerp(a0.y, a1.y, a2.y, u, v),
+                             attr_lerp(a0.z, a1.z, a2.z, u, v));
+        sign = attr_lerp(a0.w, a1.w, a2.w, u, v);
+        t = xf(tl);
+        b = cross(n, t) * sign;
+    } else {
+        orthonormal_basis(n, t, b);
+        sign = 1.0f;
+    }
+}
+
+// CalculateSurfaceParams (Shading/SurfaceParameters.cpp:144-247) from a shading frame (t, n, b) and the linear
+// base colour.
+SEL_HD Surface make_surface_frame(const MaterialDev& m, float3 t, float3 n, float3 b, float3 view,
+                                  float3 base_color_linear) {
     Surface s;
-    float3 t, b;
-    orthonormal_basis(n, t, b);
     s.t = t;
     s.n = n;
     s.b = b;
@@ -177,6 +211,13 @@ SEL_HD Surface make_surface_linear(const MaterialDev& m, float3 n, float3 view, 
     s.shader = m.shader;
     s.relative_ior = ((m.flags & kMaterialTransparent) && dot(view, n) < 0.0f) ? s.ior : 1.0f / s.ior;
     return s;
+}
+
+// The same for meshes without shading normals or tangents: the frame around the unit geometric normal n.
+SEL_HD Surface make_surface_linear(const MaterialDev& m, float3 n, float3 view, float3 base_color_linear) {
+    float3 t, b;
+    orthonormal_basis(n, t, b);
+    return make_surface_frame(m, t, n, b, view, base_color_linear);
 }
 
 // The same from a hit: frame from the normalised geometric normal, authored base colour raised to the

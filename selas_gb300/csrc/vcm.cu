@@ -52,6 +52,8 @@ struct VcmParams {
     const PtexFace* ptex_faces;
     const __half* ptex_texels;
     uint32_t ptex_face_count;
+    const MeshAttrDev* attrs;
+    uint32_t attr_count;
     CameraDev cam;
     float image_plane;
     uint32_t width, height, npaths, max_len, slots;
@@ -66,7 +68,7 @@ struct VcmParams {
 // A shading point of a sub-path.
 struct VHit {
     float3 pos, n, view;
-    float err, cont;
+    float err, cont, bsign;  // bsign: the shading frame's bitangent sign (b = cross(n, t) x bsign)
     Surface s;
     uint32_t mat;
     bool delta, transparent;
@@ -78,12 +80,15 @@ struct PathState {
     uint32_t len;
 };
 
-// Stored light vertex: 80 bytes.
+// Stored light vertex: 96 bytes (kVertF4 float4s); the tangent and bitangent sign rebuild the shading frame.
+constexpr int kVertF4 = 6;
 struct LightVertex {
-    float3 pos, n, view, thr, base;
-    float dvcm, dvc, dvm;
+    float3 pos, n, view, thr, base, t;
+    float dvcm, dvc, dvm, bsign;
     uint32_t len, mat;
 };
+
+
 
 __device__ __forceinline__ void store_vertex(float4* v, const VHit& h, const PathState& st) {
     v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, __uint_as_float(st.len));
@@ -91,10 +96,11 @@ __device__ __forceinline__ void store_vertex(float4* v, const VHit& h, const Pat
     v[2] = make_float4(h.view.x, h.view.y, h.view.z, st.dvcm);
     v[3] = make_float4(st.thr.x, st.thr.y, st.thr.z, st.dvc);
     v[4] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, st.dvm);
+    v[5] = make_float4(h.s.t.x, h.s.t.y, h.s.t.z, h.bsign);
 }
 
 __device__ __forceinline__ LightVertex load_vertex(const float4* v) {
-    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4];
+    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], g = v[5];
     LightVertex lv;
     lv.pos = f3(a.x, a.y, a.z);
     lv.len = __float_as_uint(a.w);
@@ -106,6 +112,8 @@ __device__ __forceinline__ LightVertex load_vertex(const float4* v) {
     lv.dvc = d.w;
     lv.base = f3(e.x, e.y, e.z);
     lv.dvm = e.w;
+    lv.t = f3(g.x, g.y, g.z);
+    lv.bsign = g.w;
     return lv;
 }
 
@@ -251,7 +259,11 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
         }
     }
     h.view = -dir;
-    h.s = make_surface(m, triangle_ng(p0, p1, p2), h.view, base);
+    const MeshAttrDev* attr = geom < P.attr_count ? P.attrs + geom : nullptr;
+    float3 fn, ft, fb;
+    shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2), [](float3 x) { return x; }, fn, ft,
+                  fb, h.bsign);
+    h.s = make_surface_frame(m, ft, fn, fb, h.view, pow3(base, 2.2f));
     h.n = h.s.n;
     h.cont = continuation_probability(h.s);
     h.mat = mi;
@@ -451,7 +463,7 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const 
                 st.dvm *= 1.0f / cos_in;
                 if (!h.delta) {
                     const uint32_t k = P.st.vcount[s];
-                    store_vertex(P.st.verts + (size_t(s) * P.slots + k) * 5, h, st);
+                    store_vertex(P.st.verts + (size_t(s) * P.slots + k) * kVertF4, h, st);
                     P.st.vcount[s] = k + 1;
                     int px, py;
                     if (st.len + 1 <= P.max_len && to_pixel(P.cam, h.pos, px, py)) {
@@ -593,9 +605,9 @@ __global__ void __launch_bounds__(256) k_bounds(VcmParams P) {
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < P.npaths; p += gridDim.x * blockDim.x) {
         const uint32_t n = P.st.vcount[p];
-        const float4* v = P.st.verts + size_t(p) * P.slots * 5;
+        const float4* v = P.st.verts + size_t(p) * P.slots * kVertF4;
         for (uint32_t k = 0; k < n; ++k) {
-            const float4 a = v[size_t(k) * 5];
+            const float4 a = v[size_t(k) * kVertF4];
             mn[0] = fminf(mn[0], a.x); mn[1] = fminf(mn[1], a.y); mn[2] = fminf(mn[2], a.z);
             mx[0] = fmaxf(mx[0], a.x); mx[1] = fmaxf(mx[1], a.y); mx[2] = fmaxf(mx[2], a.z);
         }
@@ -648,7 +660,7 @@ __global__ void __launch_bounds__(256) k_keys(VcmParams P) {
         const uint32_t n = P.st.vcount[p], at = P.st.vpos[p];
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t slot = p * P.slots + k;
-            const float4 a = P.st.verts[size_t(slot) * 5];
+            const float4 a = P.st.verts[size_t(slot) * kVertF4];
             const uint32_t cell = cell_of(P.st.grid, f3(a.x, a.y, a.z), cells);
             P.st.keys[0][at + k] = cell;
             P.st.vals[0][at + k] = slot;
@@ -728,10 +740,11 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t* keys_in, 
 // goes straight to the pixel.
 // ---------------------------------------------------------------------------------------------------
 
-// Camera vertex record: 96 bytes.
+// Camera vertex record: 112 bytes (kCamF4 float4s).
+constexpr int kCamF4 = 7;
 struct CameraVertex {
-    float3 pos, n, view, base, thr;
-    float err, cont, dvcm, dvc, dvm;
+    float3 pos, n, view, base, thr, t;
+    float err, cont, dvcm, dvc, dvm, bsign;
     uint32_t mat, pixel, len, transparent;
 };
 
@@ -742,10 +755,11 @@ __device__ __forceinline__ void store_camera_vertex(float4* v, const VHit& h, co
     v[3] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, __uint_as_float(pixel));
     v[4] = make_float4(st.thr.x, st.thr.y, st.thr.z, __uint_as_float(st.len));
     v[5] = make_float4(st.dvcm, st.dvc, st.dvm, __uint_as_float(h.transparent ? 1u : 0u));
+    v[6] = make_float4(h.s.t.x, h.s.t.y, h.s.t.z, h.bsign);
 }
 
 __device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
-    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], f = v[5];
+    const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], f = v[5], g = v[6];
     CameraVertex cv;
     cv.pos = f3(a.x, a.y, a.z);
     cv.err = a.w;
@@ -761,6 +775,8 @@ __device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
     cv.dvc = f.y;
     cv.dvm = f.z;
     cv.transparent = __float_as_uint(f.w);
+    cv.t = f3(g.x, g.y, g.z);
+    cv.bsign = g.w;
     return cv;
 }
 
@@ -832,14 +848,14 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const 
                     }
                     // light vertices of path s that a connection may join (path length bound)
                     const uint32_t lcount = P.st.vcount[s];
-                    const float4* lslots = P.st.verts + size_t(s) * P.slots * 5;
-                    while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * 5].w) + 1 + st.len <= P.max_len) ++nvc;
+                    const float4* lslots = P.st.verts + size_t(s) * P.slots * kVertF4;
+                    while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * kVertF4].w) + 1 + st.len <= P.max_len) ++nvc;
                 }
             }
         }
         // camera-vertex record with the state at the vertex, its connection pairs, the next-event segment
         const uint32_t vi = warp_append(&P.st.counters[5], record);
-        if (record) store_camera_vertex(P.st.cverts + size_t(vi) * 6, h, st, s);
+        if (record) store_camera_vertex(P.st.cverts + size_t(vi) * kCamF4, h, st, s);
         const uint32_t pair0 = warp_reserve(&P.st.counters[6], nvc);
         for (uint32_t k = 0; k < nvc; ++k) P.st.pairs[pair0 + k] = make_uint2(vi, k);
         const uint32_t sq = warp_append(&P.st.counters[2], nee_ray);
@@ -872,16 +888,18 @@ __global__ void __launch_bounds__(kBlock) k_c_connect(VcmParams P) {
         cv.pixel = 0;
         if (e < n) {
             const uint2 pr = P.st.pairs[e];
-            cv = load_camera_vertex(P.st.cverts + size_t(pr.x) * 6);
-            const LightVertex lv = load_vertex(P.st.verts + (size_t(cv.pixel) * P.slots + pr.y) * 5);
+            cv = load_camera_vertex(P.st.cverts + size_t(pr.x) * kCamF4);
+            const LightVertex lv = load_vertex(P.st.verts + (size_t(cv.pixel) * P.slots + pr.y) * kVertF4);
             dir = lv.pos - cv.pos;
             const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
             dir = dir * (1.0f / dist);
-            const Surface cs = make_surface_linear(P.materials[cv.mat], cv.n, cv.view, cv.base);
+            const Surface cs = make_surface_frame(P.materials[cv.mat], cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
+                                                  cv.base);
             float cfwd, crev, lfwd, lrev;
             const float3 cf = bsdf_evaluate(cs, cv.view, dir, cfwd, crev);
             if (nonzero(cf)) {
-                const Surface ls = make_surface_linear(P.materials[lv.mat], lv.n, lv.view, lv.base);
+                const Surface ls = make_surface_frame(P.materials[lv.mat], lv.t, lv.n, cross(lv.n, lv.t) * lv.bsign,
+                                                      lv.view, lv.base);
                 const float lcont = continuation_probability(ls);
                 const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
                 const float lcos_view = fabsf(dot(lv.n, lv.view));
@@ -919,7 +937,7 @@ __global__ void __launch_bounds__(256) k_gather_positions(VcmParams P) {
     const uint32_t total = P.st.vpos[P.npaths];
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
         const uint32_t slot = P.sorted_index[k];
-        const float4 a = P.st.verts[size_t(slot) * 5];
+        const float4 a = P.st.verts[size_t(slot) * kVertF4];
         P.st.spos[k] = make_float4(a.x, a.y, a.z, __uint_as_float(slot));
     }
 }
@@ -941,7 +959,7 @@ __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-        const float4* rec = P.st.cverts + size_t(i) * 6;
+        const float4* rec = P.st.cverts + size_t(i) * kCamF4;
         const float4 r0 = rec[0];
         const float3 pos = f3(r0.x, r0.y, r0.z);
         const float3 dmin = pos - glo, dmax = ghi - pos;
@@ -975,7 +993,8 @@ __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
             ends[j] = __shfl_sync(0xffffffffu, incl, j);
         }
         const CameraVertex cv = load_camera_vertex(rec);
-        const Surface cs = make_surface_linear(P.materials[cv.mat], cv.n, cv.view, cv.base);
+        const Surface cs = make_surface_frame(P.materials[cv.mat], cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
+                                              cv.base);
         float3 merged = f3(0.0f);
         // two phases so that the BSDF work runs on full warps: lanes test 32 candidates at a time against
         // the radius and append the ones inside to the warp's buffer; every 32 buffered candidates are
@@ -984,7 +1003,7 @@ __global__ void __launch_bounds__(kBlock) k_c_merge(VcmParams P) {
         uint32_t pending = 0;
         const uint32_t below = (1u << lane) - 1u;
         auto evaluate = [&](uint32_t vslot) {
-            const LightVertex lv = load_vertex(P.st.verts + size_t(vslot) * 5);
+            const LightVertex lv = load_vertex(P.st.verts + size_t(vslot) * kVertF4);
             if (cv.len + lv.len > P.max_len) return;
             // the reference merges only between surfaces of the same transparency (VCM.cpp:372-375)
             const uint32_t lt = (P.materials[lv.mat].flags & kMaterialTransparent) ? 1u : 0u;
@@ -1063,7 +1082,7 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     const size_t ntiles = (nv + kSortTile - 1) / kSortTile;
     const size_t scan_n = std::max<size_t>(std::max<size_t>(size_t(paths) + 1, 256 * ntiles), 1);
     const size_t shadow = size_t(paths) * max_len;  // per bounce: one next-event + up to max_len - 1 connections
-    st.verts = reinterpret_cast<float4*>(take(80 * nv));
+    st.verts = reinterpret_cast<float4*>(take(16 * kVertF4 * nv));
     st.vcount = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.vpos = reinterpret_cast<uint32_t*>(take(4ull * (paths + 1)));
     st.po = reinterpret_cast<float4*>(take(16ull * paths));
@@ -1083,7 +1102,7 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.shadow_capacity = uint32_t(shadow);
     st.counters = reinterpret_cast<uint32_t*>(take(4 * 64));
     st.rays = reinterpret_cast<unsigned long long*>(take(8));
-    st.cverts = reinterpret_cast<float4*>(take(96ull * paths));
+    st.cverts = reinterpret_cast<float4*>(take(16ull * kCamF4 * paths));
     st.pairs = reinterpret_cast<uint2*>(take(8 * nv));
     st.spos = reinterpret_cast<float4*>(take(16 * nv));
     for (int k = 0; k < 2; ++k) {
@@ -1152,6 +1171,8 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     P.ptex_faces = static_cast<const PtexFace*>(sc.ptex_faces);
     P.ptex_texels = static_cast<const __half*>(sc.ptex_texels);
     P.ptex_face_count = sc.ptex_face_count;
+    P.attrs = sc.attrs;
+    P.attr_count = sc.attr_count;
     P.cam.x = make_float3(cam.cam.x[0], cam.cam.x[1], cam.cam.x[2]);
     P.cam.y = make_float3(cam.cam.y[0], cam.cam.y[1], cam.cam.y[2]);
     P.cam.z = make_float3(cam.cam.z[0], cam.cam.z[1], cam.cam.z[2]);

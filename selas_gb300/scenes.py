@@ -193,6 +193,29 @@ class RenderScene:
     camera: dict = field(default_factory=dict)      # position, look_at, up, fov_degrees
     ptex: dict = field(default_factory=dict)        # geomID -> (face rows (n, 8) int32, texels float16)
     ibl: dict = None                                # light (H, W, 3), miss (h, w, 3) or None, rotation, exposure
+    attrs: dict = None                              # geomID -> {"normals": (n, 3), "tangents": (n, 4)}
+
+    def attach_attributes(self, sc) -> None:
+        for gid, a in (self.attrs or {}).items():
+            if a.get("normals") is not None:
+                sc.set_vertex_attribute(gid, 0, a["normals"])
+            if a.get("tangents") is not None:
+                sc.set_vertex_attribute(gid, 1, a["tangents"])
+
+    def attribute_soup(self):
+        """Per-triangle corner normals (n, 9), tangents (n, 12) and flags (1 normals, 2 tangents), in soup()
+        order, for the oracle."""
+        ns, ts, fs = [], [], []
+        for gid, v, idx in self.geometry.meshes:
+            a = (self.attrs or {}).get(gid, {})
+            n, t = a.get("normals"), a.get("tangents")
+            m = idx.shape[0]
+            ns.append(np.asarray(n, np.float32)[idx].reshape(m, 9) if n is not None else np.zeros((m, 9), np.float32))
+            ts.append(np.asarray(t, np.float32)[idx].reshape(m, 12) if t is not None else np.zeros((m, 12), np.float32))
+            fs.append(np.full(m, (1 if n is not None else 0) | (2 if t is not None else 0), np.uint8))
+        if not ns:
+            return np.zeros((0, 9), np.float32), np.zeros((0, 12), np.float32), np.zeros(0, np.uint8)
+        return np.concatenate(ns), np.concatenate(ts), np.concatenate(fs)
 
     def ptex_tables(self, material_recs=None):
         """Combined face table (rows rebased) and texels of all textured geometries, in geomID order; writes
@@ -218,6 +241,7 @@ class RenderScene:
         """Creates and commits a selas_gb300 Scene with this content."""
         sc = sel_module.Scene(device, bvh_kind, build_mode)
         self.geometry.attach_to(sc)
+        self.attach_attributes(sc)
         for gid, m in self.materials.items():
             sc.set_material(gid, sel_module.material(**m))
         for ls, l in self.lights:
@@ -531,6 +555,7 @@ class InstancedRenderScene:
             sc = sel_module.Scene(device, 0, build_mode)
             if p.geometry.meshes:
                 p.geometry.attach_to(sc)
+                p.attach_attributes(sc)
             for gid, m in p.materials.items():
                 sc.set_material(gid, sel_module.material(**m))
             for ls, l in p.lights:
@@ -713,3 +738,35 @@ def sky_ibl(width: int = 256, height: int = 128, sun=(0.4, 0.75, 0.3), sun_radiu
 
     return dict(light=image(width, height, True), miss=image(miss_size[0], miss_size[1], False), rotation=rotation,
                 exposure=exposure)
+
+
+def smooth_spheres(count: int = 4, level: int = 3, seed: int = 0x5E1A5106) -> RenderScene:
+    """Displaced icospheres shaded with vertex normals (the normalised radial direction) on a grey floor; the
+    even ones also carry vertex tangents (around +y, alternating handedness).  One quad light, a dim
+    background."""
+    rng = np.random.default_rng(seed)
+    unit_v, f = icosphere(level)
+    g = TriangleScene()
+    mats, attrs = {}, {}
+    for i in range(count):
+        centre = np.array([rng.uniform(-3, 3), rng.uniform(1.0, 2.0), rng.uniform(-2, 2)])
+        radius = rng.uniform(0.6, 1.1)
+        disp = 1.0 + 0.08 * value_noise_dirs(unit_v, rng)
+        g.add(i, (centre + unit_v * (radius * disp)[:, None]).astype(np.float32), f.astype(np.uint32))
+        mats[i] = dict(shader=1, lightSetIndex=0, baseColor=tuple(rng.uniform(0.2, 0.9, 3)),
+                       roughness=float(rng.uniform(0.1, 0.8)), metallic=float(i % 3 == 0), ior=1.5)
+        n = unit_v.astype(np.float32)
+        a = {"normals": n}
+        if i % 2 == 0:
+            t = np.cross(np.array([0.0, 1.0, 0.0]), unit_v)
+            t /= np.maximum(np.linalg.norm(t, axis=1, keepdims=True), 1e-6)
+            sign = np.where(np.arange(unit_v.shape[0]) % 2 == 0, 1.0, -1.0)[:, None]
+            a["tangents"] = np.concatenate([t, sign], 1).astype(np.float32)
+        attrs[i] = a
+    floor = np.array([[-20, 0, -20], [-20, 0, 20], [20, 0, 20], [20, 0, -20]], np.float32)
+    g.add(count, floor, np.array([[0, 1, 2], [0, 2, 3]], np.uint32))
+    mats[count] = dict(shader=1, lightSetIndex=0, baseColor=(0.6, 0.6, 0.6), roughness=0.7, ior=1.5)
+    light = dict(position=(0.0, 6.0, 0.0), direction=(0.0, -1.0, 0.0), x=(2.0, 0.0, 0.0), z=(0.0, 0.0, 2.0),
+                 radiance=(30.0, 28.0, 25.0))
+    cam = dict(position=(0.0, 3.0, -10.0), look_at=(0.0, 1.2, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=55.0)
+    return RenderScene(g, mats, [(0, light)], (0.05, 0.05, 0.08), cam, {}, attrs=attrs)
