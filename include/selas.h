@@ -103,9 +103,12 @@ int sel_device_sync(SelDevice device, void* stream);
 enum {
     SEL_OPTION_GRAPH_REPLAY = 1,  /* 1 (default): the integrators capture one path batch / VCM pass as a CUDA
                                      graph per argument set and replay it; 0: launch kernel by kernel */
-    SEL_OPTION_MATERIAL_SORT = 2  /* 1 (default): before shading, the integrators order each bounce's hits by
+    SEL_OPTION_MATERIAL_SORT = 2, /* 1 (default): before shading, the integrators order each bounce's hits by
                                      material class and filter Ptex in a kernel of their own when the scene has
                                      Ptex or several material classes; 0: shade in queue order */
+    SEL_OPTION_RAY_SORT = 3       /* 1: the path tracers order each bounce's continuing rays by direction bin
+                                     (dominant axis and sign) and a Morton code of the origin before tracing
+                                     them (PathTracingBatcher.cpp:162-258); 0 (default): queue order */
 };
 int sel_device_set_option(SelDevice device, int option, int value);
 

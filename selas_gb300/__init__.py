@@ -23,6 +23,7 @@ SEL_ERR_DEVICE_LIMIT = 5
 
 SEL_OPTION_GRAPH_REPLAY = 1
 SEL_OPTION_MATERIAL_SORT = 2
+SEL_OPTION_RAY_SORT = 3
 SEL_BUILD_HOST, SEL_BUILD_DEVICE = 0, 1
 SEL_BVH_WIDE8_Q8 = 0
 SEL_BVH_BINARY_FP32 = 1

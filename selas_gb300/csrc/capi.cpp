@@ -500,6 +500,9 @@ int sel_device_set_option(SelDevice device, int option, int value) {
         case SEL_OPTION_MATERIAL_SORT:
             device->material_sort = value != 0;
             return SEL_OK;
+        case SEL_OPTION_RAY_SORT:
+            device->ray_sort = value != 0;
+            return SEL_OK;
         default:
             return fail(SEL_ERR_INVALID_ARGUMENT, "unknown option");
     }

@@ -17,6 +17,7 @@ struct SelDeviceTy {
     uint32_t* d_err = nullptr;      // kernel error word (iteration cap / stack overflow bits)
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT
+    bool ray_sort = false;          // SEL_OPTION_RAY_SORT
     std::mutex mu;
 };
 

@@ -32,6 +32,8 @@
 #include "ibl.cuh"
 #include "instance.cuh"
 #include "ptex.cuh"
+#include "radix.cuh"
+#include "scan.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
 
@@ -651,6 +653,37 @@ __global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_shadow(PtParams P)
     if (status) atomicOr(P.err, status);
 }
 
+// Sort key of a continuing ray (the batcher's order, PathTracingBatcher.cpp:162-258): direction bin (dominant axis
+// x 2 + sign, 3 bits) above a 12-bit Morton code of the origin in the job scene's bounds (4 bits per axis).
+__device__ __forceinline__ uint32_t spread4(uint32_t x) {
+    x &= 15u;
+    x = (x | (x << 4)) & 0x0C3u;
+    x = (x | (x << 2)) & 0x249u;
+    return x;
+}
+
+__global__ void __launch_bounds__(kBlock) k_ray_keys(PtParams P, int next) {
+    const uint32_t n = P.st.counters[next];
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint32_t s = P.st.queue[next][e];
+        const float4 o = P.st.ray_o[s], d = P.st.ray_d[s];
+        const PtScene& S = P.st.jobs[P.st.job[s]].scene;
+        const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+        const uint32_t axis = (ax >= ay && ax >= az) ? 0u : (ay >= az ? 1u : 2u);
+        const float dc = axis == 0 ? d.x : (axis == 1 ? d.y : d.z);
+        const uint32_t bin = axis * 2u + (dc < 0.0f ? 1u : 0u);
+        uint32_t q[3];
+        const float oc[3] = {o.x, o.y, o.z};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float ext = S.hi[a] - S.lo[a];
+            const float t = ext > 0.0f ? (oc[a] - S.lo[a]) / ext : 0.0f;
+            q[a] = uint32_t(fminf(fmaxf(t * 16.0f, 0.0f), 15.0f));
+        }
+        P.st.rkeys[0][e] = (bin << 12) | spread4(q[0]) | (spread4(q[1]) << 1) | (spread4(q[2]) << 2);
+    }
+}
+
 __global__ void k_resolve(const double* accum, uint32_t count, double scale, float* out) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
         out[i] = float(accum[i] * scale);
@@ -683,6 +716,15 @@ void pt_layout(PtState& st, Take take, uint32_t paths) {
     st.sh_d = reinterpret_cast<float4*>(take(32ull * paths));
     st.sh_c = reinterpret_cast<float4*>(take(32ull * paths));
     st.counters = reinterpret_cast<uint32_t*>(take(64 * sizeof(uint32_t)));
+    {
+        const size_t ntiles = (size_t(paths) + kSortTile - 1) / kSortTile;
+        st.rkeys[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+        st.rkeys[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
+        st.rvals = reinterpret_cast<uint32_t*>(take(4ull * paths));
+        st.rhist = reinterpret_cast<uint32_t*>(take(4 * 256 * ntiles));
+        st.rhist_off = reinterpret_cast<uint32_t*>(take(4 * (256 * ntiles + 1)));
+        st.rscan_tmp = reinterpret_cast<uint32_t*>(take(4 * ((256 * ntiles + 1 + kScanTile - 1) / kScanTile + 1)));
+    }
     st.rays = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
     st.control = reinterpret_cast<PtControl*>(take(sizeof(PtControl)));
     st.jobs = reinterpret_cast<PtJob*>(take(sizeof(PtJob) * kMaxPtJobs));
@@ -713,7 +755,7 @@ size_t pt_state_block_bytes(uint32_t paths) {
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
-                           bool instanced, bool texture) {
+                           bool instanced, bool texture, bool ray_sort) {
     // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
     // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
     const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;
@@ -761,6 +803,25 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             else if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0) k_shadow<0, 128><<<trace_grid, tb, 0, s>>>(P);
             else k_shadow<1, 128><<<trace_grid, tb, 0, s>>>(P);
+            if (ray_sort && b + 1 < bounces) {
+                // order the next bounce's queue by (direction bin, origin cell): two 8-bit radix passes, the
+                // queue ping-ponging through rvals
+                const int next = cur ^ 1;
+                k_ray_keys<<<shade_grid, kBlock, 0, s>>>(P, next);
+                const uint32_t ntiles = (st.capacity + kSortTile - 1) / kSortTile;
+                uint32_t* kin = st.rkeys[0];
+                uint32_t* kout = st.rkeys[1];
+                uint32_t* vin = st.queue[next];
+                uint32_t* vout = st.rvals;
+                for (int r = 0; r < 2; ++r) {
+                    k_radix_hist<<<ntiles, 256, 0, s>>>(kin, st.counters + next, 8 * r, st.rhist, ntiles);
+                    scan_exclusive(st.rhist, 256 * ntiles, st.rhist_off, st.rscan_tmp, s);
+                    k_radix_scatter<<<ntiles, 256, 0, s>>>(kin, vin, kout, vout, st.counters + next, 8 * r,
+                                                           st.rhist_off, ntiles);
+                    std::swap(kin, kout);
+                    std::swap(vin, vout);
+                }
+            }
         }
         k_batch_end<<<1, 32, 0, s>>>(P);
     };
@@ -769,7 +830,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes, instanced, texture;
+        uint32_t modes, instanced, texture, ray_sort;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -781,6 +842,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.modes = modes;
     key.instanced = instanced ? 1u : 0u;
     key.texture = texture ? 1u : 0u;
+    key.ray_sort = ray_sort ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -806,7 +868,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
                           trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr,
-                          pt_scene_textured(sc));
+                          pt_scene_textured(sc), sc.ray_sort != 0);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -41,6 +41,8 @@ struct PtScene {
     const IblDev* ibl;            // image-based light (null: the uniform background)
     const MeshAttrDev* attrs;     // vertex attributes by geomID (null: none)
     uint32_t attr_count;
+    float lo[3], hi[3];           // bounds (the origin cells of the ray sort)
+    uint32_t ray_sort;            // 1: sort each bounce's continuing rays (SEL_OPTION_RAY_SORT)
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.
@@ -105,6 +107,11 @@ struct PtState {
     float4* sh_c;     // contribution, (job << 28 | pixel) bits
     uint32_t* counters;
     unsigned long long* rays;  // rays traced (closest + any hit), a running total
+    uint32_t* rkeys[2];       // ray sort: keys and the ping-pong partner of the queue
+    uint32_t* rvals;
+    uint32_t* rhist;          // digit counts per tile and their scan
+    uint32_t* rhist_off;
+    uint32_t* rscan_tmp;
     PtControl* control;
     PtJob* jobs;      // job table (kMaxPtJobs entries)
     uint32_t capacity;
@@ -123,7 +130,8 @@ PtState pt_state_carve(void* block, uint32_t paths);
 // `instanced`: a job's scene has instances (the instanced traversal, which also walks flat scenes).
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128,
-                           uint32_t modes = 1u, bool instanced = false, bool texture = true);
+                           uint32_t modes = 1u, bool instanced = false, bool texture = true, bool ray_sort = false);
+// `ray_sort`: order each bounce's continuing rays by (direction bin, origin cell) before tracing them.
 // `texture`: a job's hits may need Ptex (see pt_scene_textured); the Ptex kernel runs only then.
 bool pt_scene_textured(const PtScene& sc);
 

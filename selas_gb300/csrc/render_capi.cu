@@ -378,6 +378,11 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.ibl = static_cast<const IblDev*>(sc->d_ibl);
     ps.attrs = static_cast<const MeshAttrDev*>(sc->d_attrs);
     ps.attr_count = sc->attr_count;
+    for (int a = 0; a < 3; ++a) {
+        ps.lo[a] = sc->info.bounds_lo[a];
+        ps.hi[a] = sc->info.bounds_hi[a];
+    }
+    ps.ray_sort = sc->dev->ray_sort ? 1u : 0u;
     return ps;
 }
 
@@ -487,7 +492,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
                        sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
-                       ps.insts != nullptr, pt_scene_textured(ps));
+                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
 }
 

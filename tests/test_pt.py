@@ -124,3 +124,23 @@ def test_gpu_graph_replay_matches_direct_launches(device, cornell):
         imgs.append(_gpu_image(device, cornell, 40, 15, paths_in_flight=2000))
     device.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
     np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_ray_sort_does_not_change_the_image(device):
+    """SEL_OPTION_RAY_SORT: continuing rays traced in (direction bin, origin cell) order give the image of queue
+    order (same paths; only the order of FP64 additions differs), for both integrators."""
+    import selas_gb300 as sel
+    rs = scenes.textured_spheres(count=4, level=3)
+    sc = rs.build(sel, device)
+    cam = rs.sel_camera(sel, 48, 40)
+    imgs = []
+    for sort in (1, 0):
+        device.set_option(sel.SEL_OPTION_RAY_SORT, sort)
+        st = sel.pt_settings(6, 6, seed=9)
+        st.pathsInFlight = 3000
+        imgs.append((sc.pt_generate_image(cam, st), sc.deferred_generate_image(cam, sel.deferred_settings(3, 12, seed=9))))
+    device.set_option(sel.SEL_OPTION_RAY_SORT, 0)
+    sc.release()
+    np.testing.assert_allclose(imgs[0][0], imgs[1][0], rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(imgs[0][1], imgs[1][1], rtol=1e-5, atol=1e-8)
