@@ -104,10 +104,13 @@ int sel_device_new(int cuda_device, SelDevice* out_device) {
     dev->cuda_device = cuda_device;
     if (int rc = set_device(dev)) { delete dev; return rc; }
     e = cudaStreamCreateWithFlags(&dev->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&dev->qstream[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&dev->d_err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(dev->d_err, 0, sizeof(uint32_t));
     if (e != cudaSuccess) {
         if (dev->stream) cudaStreamDestroy(dev->stream);
+        for (cudaStream_t q : dev->qstream)
+            if (q) cudaStreamDestroy(q);
         if (dev->d_err) cudaFree(dev->d_err);
         delete dev;
         return cuda_fail(e, "device setup");
@@ -121,6 +124,10 @@ int sel_device_release(SelDevice device) {
     set_device(device);
     cudaStreamSynchronize(device->stream);
     cudaStreamDestroy(device->stream);
+    for (cudaStream_t q : device->qstream) {
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+    }
     cudaFree(device->d_err);
     delete device;
     return SEL_OK;
@@ -547,11 +554,36 @@ static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_str
     SelDeviceTy* dev = scene->dev;
     std::lock_guard<std::mutex> dlock(dev->mu);
     const size_t bytes = size_t(M) * sizeof(Rec);
+    const bool dense = byte_stride == sizeof(Rec);
+    cudaError_t e = cudaSuccess;
+    // Large dense batches: chunks pipelined over three streams, so that one chunk's upload, another's
+    // traversal and a third's download overlap (the copy engines and the SMs work at once).
+    constexpr unsigned kChunk = 1u << 18;
+    if (dense && M > 2 * kChunk) {
+        if (int rc = ensure_scratch(scene, 3 * size_t(kChunk) * sizeof(Rec))) return rc;
+        Rec* slots = static_cast<Rec*>(scene->scratch);
+        const DeviceBvh bvh = device_bvh(scene);
+        for (unsigned c0 = 0, c = 0; c0 < M && e == cudaSuccess; c0 += kChunk, ++c) {
+            const unsigned n = std::min(kChunk, M - c0);
+            cudaStream_t q = dev->qstream[c % 3];
+            Rec* d = slots + size_t(c % 3) * kChunk;
+            e = cudaMemcpyAsync(d, recs + c0, size_t(n) * sizeof(Rec), cudaMemcpyHostToDevice, q);
+            if (e != cudaSuccess) break;
+            e = kHit ? launch_intersect(bvh, reinterpret_cast<SelRayHit*>(d), n, dev->d_err, q)
+                     : launch_occluded(bvh, reinterpret_cast<SelRay*>(d), n, dev->d_err, q);
+            if (e != cudaSuccess) break;
+            e = cudaMemcpyAsync(recs + c0, d, size_t(n) * sizeof(Rec), cudaMemcpyDeviceToHost, q);
+        }
+        for (cudaStream_t q : dev->qstream) {
+            const cudaError_t es = cudaStreamSynchronize(q);
+            if (e == cudaSuccess) e = es;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "pipelined query");
+        return read_error_word(dev, dev->stream);
+    }
     if (int rc = ensure_scratch(scene, bytes)) return rc;
     cudaStream_t s = dev->stream;
-    cudaError_t e;
     std::vector<Rec> packed;
-    const bool dense = byte_stride == sizeof(Rec);
     if (dense) {
         e = cudaMemcpyAsync(scene->scratch, recs, bytes, cudaMemcpyHostToDevice, s);
     } else {

@@ -143,6 +143,13 @@ def test_full_size_workload(device, full_workload):
         a = _trace_device(wide, org, d)
         b = _trace_device(binary, org, d)
         assert_hits_equal(a, b)
+        # the host-memory form pipelines chunks of a large batch over several streams: same records
+        h = sel.make_rayhits(org, d)
+        wide.intersect1M(h)
+        assert_hits_equal(h, a)
+        ho = sel.make_rays(org, d)
+        wide.occluded1M(ho)
+        assert np.array_equal(np.isneginf(ho["tfar"]), a["geomID"] != sel.INVALID_ID)
         hit = a["geomID"] != sel.INVALID_ID
         assert hit.mean() > 0.05
         occ = _trace_device(wide, org, d, any_hit=True)
