@@ -393,9 +393,10 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const u
 
 // kModes: bit 0 path-tracer jobs, bit 1 deferred jobs in the batch (a single-mode batch compiles the other
 // integrator out of the kernel).
-// At most 96 registers (5 blocks per SM; a few bytes spill): 2 % faster renders of the room than 102 registers.
+// The path tracer's shading at most 96 registers (5 blocks per SM; a few bytes spill): 2 % faster renders of the
+// room than 102 registers.  The deferred and mixed forms keep 4 blocks per SM (their bigger code would spill).
 template <uint32_t kModes, bool kInst>
-__global__ void __launch_bounds__(kBlock, 5) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
+__global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     const int next = cur ^ 1;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
