@@ -306,7 +306,12 @@ __global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_extend(PtParams P,
 }
 
 // Material class of a queued path's hit: 0 miss; else 1 + shader * 4 + 2 (Ptex) + 1 (transparent).  Paths
-// are counting-sorted by class before shading, so a warp shades one kind of surface.
+// are sorted by class before shading, so a warp shades one kind of surface.
+__device__ __forceinline__ uint32_t class_of(const MaterialDev& m) {
+    const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
+    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+}
+
 template <bool kInst>
 __device__ __forceinline__ uint32_t material_class(const PtParams& P, uint32_t s) {
     const uint32_t tri = __float_as_uint(P.st.hit[s].w);
@@ -314,9 +319,7 @@ __device__ __forceinline__ uint32_t material_class(const PtParams& P, uint32_t s
     const PtScene& S = P.st.jobs[P.st.job[s]].scene;
     const HitRef r = hit_ref<kInst>(P.st, S, s, tri);
     const uint32_t geom = __float_as_uint(__ldg(r.tp + 1).w);
-    const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
-    const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
-    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+    return class_of(r.mats[geom < r.mat_count ? geom : 0]);
 }
 
 __global__ void k_class_reset(uint32_t* counters) {
@@ -360,6 +363,36 @@ __global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
         if (valid && leader == int(lane)) at = atomicAdd(&P.st.counters[48 + c], __popc(peers));
         at = __shfl_sync(0xffffffffu, at, leader);
         if (valid) P.st.queue_sorted[at + __popc(peers & ((1u << lane) - 1u))] = P.st.queue[cur][e];
+    }
+}
+
+// Sort key of a queued hit in a textured scene: the material class (bits 20-23) above, for a Ptex-textured hit,
+// its face modulo 2^17 (bits 3-19) and the edges its filter footprint crosses (bits 0-2).  Hits on one face sit together, as
+// the reference's batcher orders hits by (instance, geometry, primitive) before shading
+// (PathTracingBatcher.cpp:221-238,799-825), and hits whose footprints cross the same edges walk the same faces,
+// so a warp's Ptex filter walks stay in step.  Three 8-bit radix passes order the queue by it.
+template <bool kInst>
+__global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
+    const uint32_t n = P.st.counters[cur];
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const uint32_t s = P.st.queue[cur][e];
+        const float4 hit = P.st.hit[s];
+        const uint32_t tri = __float_as_uint(hit.w);
+        uint32_t key = 0u;
+        if (tri != 0xffffffffu) {
+            const PtScene& S = P.st.jobs[P.st.job[s]].scene;
+            const HitRef r = hit_ref<kInst>(P.st, S, s, tri);
+            const float4 p0 = __ldg(r.tp), p1 = __ldg(r.tp + 1);
+            const uint32_t geom = __float_as_uint(p1.w);
+            const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
+            key = class_of(m) << 20;
+            if (m.flags & kMaterialUsesPtex) {
+                const int face = int(m.ptex_base + __float_as_uint(p0.w));
+                key |= ((uint32_t(face) & 0x1ffffu) << 3) |
+                       ptex_region(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count), face, hit.y, hit.z);
+            }
+        }
+        P.st.rkeys[0][e] = key;
     }
 }
 
@@ -781,7 +814,25 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             else if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
             else if (bvh_kind == 0) k_extend<0, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             else k_extend<1, 128><<<trace_grid, tb, 0, s>>>(P, cur);
-            if (sort) {
+            if (sort && texture) {
+                // textured scenes: order by (class, Ptex face, footprint region), three 8-bit radix passes from
+                // the queue to queue_sorted (through rvals)
+                if (instanced) k_sort_keys<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                else k_sort_keys<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                const uint32_t ntiles = (st.capacity + kSortTile - 1) / kSortTile;
+                uint32_t* kin = st.rkeys[0];
+                uint32_t* kout = st.rkeys[1];
+                const uint32_t* vin = st.queue[cur];
+                for (int r = 0; r < 3; ++r) {
+                    uint32_t* vout = (r & 1) ? st.rvals : st.queue_sorted;
+                    k_radix_hist<<<ntiles, 256, 0, s>>>(kin, st.counters + cur, 8 * r, st.rhist, ntiles);
+                    scan_exclusive(st.rhist, 256 * ntiles, st.rhist_off, st.rscan_tmp, s);
+                    k_radix_scatter<<<ntiles, 256, 0, s>>>(kin, vin, kout, vout, st.counters + cur, 8 * r,
+                                                           st.rhist_off, ntiles);
+                    std::swap(kin, kout);
+                    vin = vout;
+                }
+            } else if (sort) {
                 k_class_reset<<<1, 32, 0, s>>>(st.counters);
                 if (instanced) k_classify<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 else k_classify<false><<<shade_grid, kBlock, 0, s>>>(P, cur);

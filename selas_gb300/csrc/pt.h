@@ -99,7 +99,8 @@ struct PtState {
     uint64_t* path_id;  // index of the path within its job (its PCG32 stream)
     uint64_t* rng;
     uint32_t* queue[2];
-    uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort)
+    uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort; textured scenes:
+                             // class, then Ptex face, by radix sort)
     uint32_t* cls;    // material class of each current queue entry
     float4* base;     // Ptex base colour (authored, before the 2.2 power) of the path's current hit
     float4* sh_o;     // shadow rays (2 per path slot): origin, tnear

@@ -93,10 +93,10 @@ __device__ __forceinline__ void ptex_walk(int rowlen, float ku, float kv, int u1
     }
 }
 
-// PtexTriangleFilter::apply: clamp, build the even and odd iterators, walk both.
-__device__ __forceinline__ void ptex_apply(PtexKernel k, const PtexFace& f, const __half* __restrict__ texels,
-                                           float3& acc, float& weight) {
-    const int flog2 = f.log2;
+// PtexTriangleFilter::apply: clamp, build the even and odd iterators, walk both over the face whose
+// resolution is 2^flog2 and whose texels start at `data`.
+__device__ __forceinline__ void ptex_apply(PtexKernel k, int flog2, const __half* __restrict__ data, float3& acc,
+                                           float& weight) {
     k.reslog2 = min(k.reslog2, flog2);
     k.u1 = fmaxf(k.u1, 0.0f);
     k.v1 = fmaxf(k.v1, 0.0f);
@@ -110,7 +110,6 @@ __device__ __forceinline__ void ptex_apply(PtexKernel k, const PtexFace& f, cons
     const float third = float(1 / 3.0);
     const float scale = (float)resu;
     const float wscale = 1.0f / ((float)resu * (float)resu);
-    const __half* data = texels + size_t(f.offset) * 3;
     // even iterator
     const int eu1 = int(ceilf(k.u1 * scale - third)), ev1 = int(ceilf(k.v1 * scale - third));
     const int ew1 = int(ceilf(k.w1 * scale - third)), eu2 = int(ceilf(k.u2 * scale - third));
@@ -136,16 +135,32 @@ __device__ __forceinline__ void ptex_apply(PtexKernel k, const PtexFace& f, cons
     }
 }
 
-// Filtered RGB at (face, u, v).  Returns false (and leaves `out`) for a face outside [0, nfaces).
-__device__ __forceinline__ bool ptex_eval(const PtexFace* __restrict__ faces, int nfaces,
-                                          const __half* __restrict__ texels, int face, float u, float v,
-                                          float3& out, uint32_t& status) {
-    if (face < 0 || face >= nfaces) return false;
-    const PtexFace f0 = faces[face];
+// One application of the filter: the kernel in one face's coordinates (before apply's clamping), the face's
+// resolution and its first texel.
+struct PtexApp {
+    PtexKernel k;
+    int log2;
+    const __half* data;
+};
+
+// splitAndApply (PtexTriangleFilter.cpp:96-167) as a resumable depth-first walk over an explicit frame stack:
+// each call of ptex_split_next runs to the next application, in the order of the reference's recursion.
+struct PtexSplit {
+    struct Frame {
+        PtexKernel k;
+        int face;
+        int phase;  // 0/1/2: split across edges 2 (u), 0 (v), 1 (w) next; 3: apply
+    };
+    Frame st[kPtexStack];
+    int sp;
+};
+
+// buildKernel for a zero-size footprint (PtexTriangleFilter.cpp:50-94) on a face of resolution 2^log2: only the
+// texel-size term of the blur survives.  u and v are clamped to [0, 1].
+__device__ __forceinline__ void ptex_root_kernel(int log2, float u, float v, PtexKernel& k) {
     u = clampf(u, 0.0f, 1.0f);
     v = clampf(v, 0.0f, 1.0f);
-    // buildKernel for a zero-size footprint: only the texel-size term of the blur survives
-    const float res = (float)(1 << f0.log2);
+    const float res = (float)(1 << log2);
     const float b = (0.5f / res) * (0.5f / res);
     const float Ac = 0.0f + b, Cc = 0.0f + b, Bc = 0.0f, X = 0.0f;
     const float m = sqrtf(2.0f * (Ac * Cc - 0.25f * Bc * Bc) / (Ac + Cc + X));
@@ -159,26 +174,40 @@ __device__ __forceinline__ bool ptex_eval(const PtexFace* __restrict__ faces, in
     C *= sc;
     const float uw = fminf(sqrtf(C), 1.0f), vw = fminf(sqrtf(A), 1.0f), ww = fminf(sqrtf(A - B + C), 1.0f);
     const float w = 1.0f - u - v;
+    k.u = u; k.v = v;
+    k.u1 = u - uw; k.v1 = v - vw; k.w1 = w - ww;
+    k.u2 = u + uw; k.v2 = v + vw; k.w2 = w + ww;
+    k.A = A; k.B = B; k.C = C;
+    k.reslog2 = reslog2;
+}
 
-    struct Frame {
-        PtexKernel k;
-        int face;
-        int phase;
-    };
-    Frame st[kPtexStack];
-    int sp = 0;
-    st[0].k.u = u; st[0].k.v = v;
-    st[0].k.u1 = u - uw; st[0].k.v1 = v - vw; st[0].k.w1 = w - ww;
-    st[0].k.u2 = u + uw; st[0].k.v2 = v + vw; st[0].k.w2 = w + ww;
-    st[0].k.A = A; st[0].k.B = B; st[0].k.C = C;
-    st[0].k.reslog2 = reslog2;
-    st[0].face = face;
-    st[0].phase = 0;
-    float3 acc = f3(0.0f);
-    float weight = 0.0f;
-    // splitAndApply as a loop: phases 0/1/2 split across edges 2 (u), 0 (v), 1 (w); phase 3 applies
-    while (sp >= 0) {
-        Frame& fr = st[sp];
+// `face` must be a valid face index.
+__device__ __forceinline__ void ptex_split_init(PtexSplit& w, const PtexFace* __restrict__ faces, int face, float u,
+                                                float v) {
+    PtexSplit::Frame& fr = w.st[0];
+    ptex_root_kernel(faces[face].log2, u, v, fr.k);
+    fr.face = face;
+    fr.phase = 0;
+    w.sp = 0;
+}
+
+// The edges that the footprint of a query at (face, u, v) crosses (bit 0: u, bit 1: v, bit 2: w below 0): the
+// first branches of the split walk.  Queries with the same face and region mostly walk the same faces, so a
+// queue ordered by (face, region) keeps a warp's filter walks in step.  0 for a face outside [0, nfaces).
+__device__ __forceinline__ uint32_t ptex_region(const PtexFace* __restrict__ faces, int nfaces, int face, float u,
+                                                float v) {
+    if (face < 0 || face >= nfaces) return 0u;
+    PtexKernel k;
+    ptex_root_kernel(faces[face].log2, u, v, k);
+    return (k.u1 < 0.0f ? 1u : 0u) | (k.v1 < 0.0f ? 2u : 0u) | (k.w1 < 0.0f ? 4u : 0u);
+}
+
+// The next application of the walk into `app`; false when the walk is over (or its stack overflowed, which
+// sets kErrPtexStack and ends it as the reference's filter would have run out of stack).
+__device__ __forceinline__ bool ptex_split_next(PtexSplit& w, const PtexFace* __restrict__ faces,
+                                                const __half* __restrict__ texels, PtexApp& app, uint32_t& status) {
+    while (w.sp >= 0) {
+        PtexSplit::Frame& fr = w.st[w.sp];
         const PtexFace f = faces[fr.face];
         int eid = -1;
         while (fr.phase < 3 && eid < 0) {
@@ -188,9 +217,10 @@ __device__ __forceinline__ bool ptex_eval(const PtexFace* __restrict__ faces, in
             else if (ph == 2 && fr.k.w1 < 0.0f && f.adj[1] >= 0) eid = 1;
         }
         if (eid >= 0) {
-            if (sp + 1 >= kPtexStack) {
+            if (w.sp + 1 >= kPtexStack) {
                 status |= kErrPtexStack;
-                break;
+                w.sp = -1;
+                return false;
             }
             PtexKernel ka = fr.k;
             if (eid == 2) { fr.k.u1 = 0.0f; ka.u2 = 0.0f; }
@@ -198,16 +228,34 @@ __device__ __forceinline__ bool ptex_eval(const PtexFace* __restrict__ faces, in
             else { fr.k.w1 = 0.0f; ka.w2 = 0.0f; }
             const int aeid = f.adjedge[eid];
             pk_reorient(ka, eid, aeid);
-            Frame& nx = st[sp + 1];
+            PtexSplit::Frame& nx = w.st[w.sp + 1];
             nx.k = ka;
             nx.face = f.adj[eid];
             nx.phase = 0;
-            ++sp;
+            ++w.sp;
             continue;
         }
-        ptex_apply(fr.k, f, texels, acc, weight);
-        --sp;
+        app.k = fr.k;
+        app.log2 = f.log2;
+        app.data = texels + size_t(f.offset) * 3;
+        --w.sp;
+        return true;
     }
+    return false;
+}
+
+// Filtered RGB at (face, u, v), one query per thread.  Returns false (and leaves `out`) for a face outside
+// [0, nfaces).
+__device__ __forceinline__ bool ptex_eval(const PtexFace* __restrict__ faces, int nfaces,
+                                          const __half* __restrict__ texels, int face, float u, float v,
+                                          float3& out, uint32_t& status) {
+    if (face < 0 || face >= nfaces) return false;
+    PtexSplit w;
+    ptex_split_init(w, faces, face, u, v);
+    float3 acc = f3(0.0f);
+    float weight = 0.0f;
+    PtexApp a;
+    while (ptex_split_next(w, faces, texels, a, status)) ptex_apply(a.k, a.log2, a.data, acc, weight);
     const float s = 1.0f / (weight * 1.0f);
     out = f3(acc.x * s, acc.y * s, acc.z * s);
     return true;

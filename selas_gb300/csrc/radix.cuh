@@ -35,11 +35,13 @@ __global__ void __launch_bounds__(256) k_radix_scatter(const uint32_t* keys_in, 
     __shared__ uint32_t chunk_count[256];
     __shared__ uint32_t warp_hist[8][256];
     const uint32_t total = *total_ptr;
+    const size_t base = size_t(blockIdx.x) * kSortTile;
+    if (base >= total) return;  // tiles past the live count (block-uniform)
     tile_base[threadIdx.x] = offsets[size_t(threadIdx.x) * ntiles + blockIdx.x];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    const size_t base = size_t(blockIdx.x) * kSortTile;
     for (int chunk = 0; chunk < kSortTile / 256; ++chunk) {
+        if (base + size_t(chunk) * 256 >= total) break;  // block-uniform
         for (int k = 0; k < 8; ++k) warp_hist[k][threadIdx.x] = 0;
         __syncthreads();
         const size_t i = base + size_t(chunk) * 256 + threadIdx.x;
