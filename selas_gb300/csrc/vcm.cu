@@ -926,12 +926,6 @@ __global__ void __launch_bounds__(kBlock, 4) k_c_merge(VcmParams P) {
         }
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 7);
         if (total == 0) continue;
-        uint32_t bases[8], ends[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            bases[j] = __shfl_sync(0xffffffffu, cb, j);
-            ends[j] = __shfl_sync(0xffffffffu, incl, j);
-        }
         const CameraVertex cv = load_camera_vertex(rec);
         const Surface cs = make_surface_frame(P.materials[cv.mat], cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
                                               cv.base);
@@ -964,14 +958,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_c_merge(VcmParams P) {
             const uint32_t t = t0 + lane;
             bool in = false;
             uint32_t vslot = 0;
+            // the cell whose range of the concatenation holds t: lanes 0..7 hold each cell's start (cb) and
+            // inclusive end (incl); shuffled per round rather than held in registers across the loop
+            uint32_t start = 0, b = 0, prev = 0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const uint32_t eq = __shfl_sync(0xffffffffu, incl, q);
+                const uint32_t bq = __shfl_sync(0xffffffffu, cb, q);
+                if (t >= prev && t < eq) { b = bq; start = prev; }
+                prev = eq;
+            }
             if (t < total) {
-                int j = 0;
-#pragma unroll
-                for (int q = 0; q < 7; ++q) j += t >= ends[q] ? 1 : 0;
-                uint32_t start = 0, b = 0;
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q == j) { b = bases[q]; start = q > 0 ? ends[q - 1] : 0u; }
                 const float4 sp = P.st.spos[b + (t - start)];
                 const float3 dd = pos - f3(sp.x, sp.y, sp.z);
                 in = dot(dd, dd) <= gr2;
@@ -1000,8 +997,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_c_merge(VcmParams P) {
             merged.z += __shfl_xor_sync(0xffffffffu, merged.z, o);
         }
         if (lane == 0) {
-            const float3 mc = c.vm_norm * (cv.thr * merged);
-            if (nonzero(mc)) splat(P.accum, cv.pixel, mc);
+            const float4 e = rec[4];  // throughput, reloaded rather than held across the loop
+            const float3 mc = c.vm_norm * (f3(e.x, e.y, e.z) * merged);
+            if (nonzero(mc)) splat(P.accum, __float_as_uint(rec[3].w), mc);
         }
     }
 }
