@@ -358,9 +358,13 @@ def vcm_render(render_scene, width, height, iter_begin, iter_end, max_len=10, ra
                seed=0x5E1A5000, nthreads=None, merging=True, strategies=15):
     """CPU oracle VCM (oracle_vcm.cpp): FP64 per-pixel sums over iterations [iter_begin, iter_end), shape
     (height, width, 3).  radius0 defaults to 0.0025 x the scene's bounding-sphere radius (VCM.cpp:778 with
-    VcmRadiusFactor_ = 0.0025), the sphere taken about the bounding box (radius = half its diagonal)."""
+    VcmRadiusFactor_ = 0.0025), the sphere taken about the bounding box (radius = half its diagonal).  The
+    scene's image-based light, if any, is an environment emitter.  strategies: bit 0 next-event estimation,
+    1 vertex connection, 2 vertex merging, 3 light tracing (15: all, MIS-weighted); a subset is unweighted,
+    and bit 4 adds camera paths that hit the environment to it."""
     from selas_gb300.scenes import light_records, material_records
     set_attributes([render_scene])
+    set_ibl(getattr(render_scene, "ibl", None))
     verts, prim, geom = render_scene.geometry.soup()
     mats = material_records(render_scene.materials, int(geom.max()) + 1)
     rows, texels = render_scene.ptex_tables(mats)

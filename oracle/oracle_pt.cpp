@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "oracle_attrs.h"
+#include "oracle_env.h"
 #include "oracle_bsdf.h"
 #include "oracle_ptex.h"
 #include "oracle_query.h"
@@ -279,6 +280,51 @@ struct Ibl {
         texel(wi, mw, mh, x, y, theta);
         const float* c = &miss[(size_t(y) * mw + x) * 3];
         return V3(c[0], c[1], c[2]);
+    }
+    // Environment emitter of the VCM oracle (the device's ibl_env_*): a texel from (r0, r1) by the CDFs, the
+    // direction jittered by (r2, r3) uniformly in (theta, phi) over the directions that look the texel up, so
+    // the solid-angle density m c / (area sin theta) belongs to the texel a direction's lookup returns.  The
+    // azimuth is wrapped into [0, 2 pi) (the lookup's fmod leaves negative rotations negative).
+    static void env_span(uint32_t i, uint32_t n, float& a, float& b) {
+        a = i == 0 ? 0.0f : float(i) + 0.5f;
+        b = i + 1 >= n ? float(n) : float(i) + 1.5f;
+    }
+    void env_texel(V3 wi, int& x, int& y, float& theta) const {
+        theta = std::acos(std::min(std::max(wi.y, -1.0f), 1.0f));
+        float phi = std::atan2(wi.z, wi.x);
+        phi = std::fmod(phi + kPi + rot, 2.0f * kPi);
+        if (phi < 0.0f) phi += 2.0f * kPi;
+        x = int(phi * float(w) / (2.0f * kPi) - 0.5f);
+        y = int(theta * float(h) / kPi - 0.5f);
+        x = std::min(std::max(x, 0), int(w) - 1);
+        y = std::min(std::max(y, 0), int(h) - 1);
+    }
+    float env_pdf(V3 wi) const {
+        int x, y;
+        float theta;
+        env_texel(wi, x, y, theta);
+        const float m = y > 0 ? mdf[y] - mdf[y - 1] : mdf[y];
+        const float* row = &cdf[size_t(y) * w];
+        const float c = x > 0 ? row[x] - row[x - 1] : row[x];
+        float ax, bx, ay, by;
+        env_span(uint32_t(x), w, ax, bx);
+        env_span(uint32_t(y), h, ay, by);
+        const float area = ((bx - ax) * ((2.0f * kPi) / float(w))) * ((by - ay) * (kPi / float(h)));
+        const float st = std::sin(theta);
+        return st > 0.0f ? m * c / (area * st) : 0.0f;
+    }
+    V3 env_direction(float r0, float r1, float r2, float r3) const {
+        uint32_t x, y;
+        float m, c;
+        search(mdf.data(), h, r0, y, m);
+        search(&cdf[size_t(y) * w], w, r1, x, c);
+        float ax, bx, ay, by;
+        env_span(x, w, ax, bx);
+        env_span(y, h, ay, by);
+        const float theta = (ay + r2 * (by - ay)) * (kPi / float(h));
+        const float phi = (ax + r3 * (bx - ax)) * ((2.0f * kPi) / float(w)) - kPi - rot;
+        const float st = std::sin(theta);
+        return V3(st * std::cos(phi), std::cos(theta), st * std::sin(phi));
     }
     void sample(float r0, float r1, V3& dir, V3& rad, float& p) const {
         uint32_t x, y;
@@ -954,6 +1000,25 @@ void oracle_set_attributes(int64_t n, const float* normals, const float* tangent
 }  // extern "C"
 
 namespace ora {
+
+bool env_present() { return g_ibl.w != 0; }
+
+void env_direction(float r0, float r1, float r2, float r3, float dir[3]) {
+    const V3 d = g_ibl.env_direction(r0, r1, r2, r3);
+    dir[0] = d.x; dir[1] = d.y; dir[2] = d.z;
+}
+
+float env_pdf(const float dir[3]) { return g_ibl.env_pdf(V3(dir[0], dir[1], dir[2])); }
+
+void env_radiance(const float dir[3], float rad[3]) {
+    const V3 r = g_ibl.radiance(V3(dir[0], dir[1], dir[2]));
+    rad[0] = r.x; rad[1] = r.y; rad[2] = r.z;
+}
+
+void env_miss(const float dir[3], float rad[3]) {
+    const V3 r = g_ibl.miss_radiance(V3(dir[0], dir[1], dir[2]));
+    rad[0] = r.x; rad[1] = r.y; rad[2] = r.z;
+}
 
 bool index(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene, int64_t ntri) {
     if (g_attrs.flags.empty() || ntri <= 0) return false;

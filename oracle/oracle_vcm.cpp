@@ -12,11 +12,18 @@
 //   hash grid                 VCMHashGrid.cpp:15-155 (cells of 2r over the vertex bounds widened by r,
 //                             3-prime hash, counting sort, 2x2x2 cell search)
 // with the reference's lights: quad lights that NEE and light tracing use but that camera and BSDF rays
-// never hit, so the strategy "camera path hits the emitter" does not exist and its MIS terms are zero
-// (dVC = dVM = 0 at the emitter, wLight = 0 in next-event estimation), as for delta lights.  The BSDF is
-// the reference Disney model (oracle_bsdf.cpp), whose evaluation returns f * |cos(l)|.  Lights come from
-// light set 0; the background is not an emitter here.  Random numbers: PCG32, stream
-// (2 * iteration + 0) * N + p for light path p and (2 * iteration + 1) * N + p for camera path p.
+// never hit, so the strategy "camera path hits the emitter" does not exist for them and its MIS terms are
+// zero (dVC = dVM = 0 at the emitter, wLight = 0 in next-event estimation), as for delta lights.  The
+// image-based light, the reference VCM's only emitter (GenerateLightSample, VCMCommon.cpp:37-62), is an
+// environment emitter (tech report sec. 5.1, the infinite light): light sub-paths start on a disc of the
+// scene's bounding-sphere radius facing a sampled direction (EmitIblLightSample, AreaLighting.cpp:246-290),
+// next-event estimation samples it, and camera paths that leave the scene take its radiance with the
+// camera-hit weight (ConnectToSkyLight, VCM.cpp:171-187).  It is one more light in the uniform light pick.
+// Its directions are drawn from the image's CDFs and jittered within the texel (ora::env_direction), so the
+// density a strategy weighs with is the one it sampled with.  The BSDF is the reference Disney model
+// (oracle_bsdf.cpp), whose evaluation returns f * |cos(l)|.  Quad lights come from light set 0; a uniform
+// background is not an emitter here.  Random numbers: PCG32, stream (2 * iteration + 0) * N + p for light
+// path p and (2 * iteration + 1) * N + p for camera path p.
 
 #include <algorithm>
 #include <atomic>
@@ -28,6 +35,7 @@
 
 #include "oracle_attrs.h"
 #include "oracle_bsdf.h"
+#include "oracle_env.h"
 #include "oracle_ptex.h"
 #include "oracle_query.h"
 
@@ -101,7 +109,41 @@ struct Scene {
     std::vector<Light> lights;  // light set 0
     Camera cam;
     uint32_t max_len;
+    bool env = false;          // the image-based light emits (one light after the quads)
+    V3 center;                 // bounding sphere of the scene's bounding box
+    float radius = 0.0f;
+    float disc_pdf = 0.0f;     // ConcentricDiscPdf / radius^2: area density of the emission disc
 };
+
+// MakeOrthogonalCoordinateSystem (GeometryLib/CoordinateSystem.h:14-21)
+void basis(V3 v1, V3& v2, V3& v3) {
+    if (std::fabs(v1.x) > std::fabs(v1.y))
+        v2 = V3(-v1.z, 0.0f, v1.x) * (1.0f / std::sqrt(v1.x * v1.x + v1.z * v1.z));
+    else
+        v2 = V3(0.0f, v1.z, -v1.y) * (1.0f / std::sqrt(v1.y * v1.y + v1.z * v1.z));
+    v3 = orc::Cross(v1, v2);
+}
+
+// Concentric map of the unit square onto the unit disc (Shirley and Chiu, "A Low Distortion Map Between Disk
+// and Square", 1997), the disc sample of EmitIblLightSample.
+void concentric_disc(float r0, float r1, float& u, float& v) {
+    const float a = 2.0f * r0 - 1.0f, b = 2.0f * r1 - 1.0f;
+    if (a == 0.0f && b == 0.0f) {
+        u = 0.0f;
+        v = 0.0f;
+        return;
+    }
+    float r, phi;
+    if (std::fabs(a) > std::fabs(b)) {
+        r = a;
+        phi = (kPi / 4.0f) * (b / a);
+    } else {
+        r = b;
+        phi = kPi / 2.0f - (kPi / 4.0f) * (a / b);
+    }
+    u = r * std::cos(phi);
+    v = r * std::sin(phi);
+}
 
 // Surface at a hit (CalculateSurfaceParams without normals/tangents/uvs, as the path tracers use).
 struct Hit {
@@ -148,6 +190,7 @@ struct PathState {
     V3 org, dir, thr;
     float dVCM, dVC, dVM;
     uint32_t len;
+    bool delta_only = true;  // camera path: every vertex so far is a Dirac surface
 };
 
 struct LightVertex {
@@ -292,10 +335,12 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
                        uint32_t max_len, float radius0, float alpha, uint64_t seed, int threads,
                        const int32_t* ptex_rows, int ptex_faces, const uint16_t* ptex_texels, int merging,
                        int strategies, double* out) {
-    // strategies: bit 0 next-event estimation, 1 vertex connection, 2 vertex merging, 3 light tracing;
-    // a single enabled strategy is weighted 1 (an unweighted estimator of its own paths)
-    const bool single = strategies != 15;
+    // strategies: bit 0 next-event estimation, 1 vertex connection, 2 vertex merging, 3 light tracing (15: all,
+    // MIS-weighted, with camera paths hitting the environment); otherwise the enabled strategies are weighted 1
+    // (unweighted estimators of their own paths), and bit 4 adds camera paths hitting the environment
+    const bool single = (strategies & 15) != 15;
     const bool use_nee = strategies & 1, use_vc = strategies & 2, use_vm = strategies & 4, use_lt = strategies & 8;
+    const bool use_hit = !single || (strategies & 16);
     Scene sc;
     sc.bvh = orq::build(verts, prim, geom, ntri);
     ora::index(prim, geom, nullptr, ntri);
@@ -308,6 +353,27 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
         sc.lights.push_back({V3(l[0], l[1], l[2]), V3(l[3], l[4], l[5]), V3(l[6], l[7], l[8]), V3(l[9], l[10], l[11]),
                              V3(l[12], l[13], l[14])});
     }
+    if (ora::env_present() && ntri > 0) {
+        // the scene's bounding sphere (SceneResource.h:77-78 keeps aaBox and boundingSphere), taken about the
+        // bounding box as for the default merge radius
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int64_t k = 0; k < ntri * 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], verts[k * 3 + a]);
+                hi[a] = std::max(hi[a], verts[k * 3 + a]);
+            }
+        float d2 = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            const float e = hi[a] - lo[a];
+            d2 += e * e;
+        }
+        sc.env = true;
+        sc.center = V3(0.5f * (lo[0] + hi[0]), 0.5f * (lo[1] + hi[1]), 0.5f * (lo[2] + hi[2]));
+        sc.radius = 0.5f * std::sqrt(d2);
+        sc.disc_pdf = (1.0f / kPi) * (1.0f / (sc.radius * sc.radius));
+    }
+    const uint32_t nq = uint32_t(sc.lights.size());
+    const uint32_t n_emitters = nq + (sc.env ? 1u : 0u);
     {  // InitializeRayCastCamera (GeometryLib/Camera.cpp:89-115); the pixel-area image plane uses tan(fov/2)
         const float aspect = float(width) / float(height);
         const float hfov = camera[9] * (kPi / 180.0f);
@@ -327,7 +393,7 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
     const uint32_t N = width * height;
     const int nt = std::max(1, threads);
     std::vector<std::vector<double>> lt_images(size_t(nt), std::vector<double>(size_t(N) * 3, 0.0));
-    const float light_pick = sc.lights.empty() ? 0.0f : 1.0f / float(sc.lights.size());
+    const float light_pick = n_emitters == 0 ? 0.0f : 1.0f / float(n_emitters);
 
     for (uint32_t it = iter_begin; it < iter_end; ++it) {
         Consts c;
@@ -347,37 +413,61 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
             for (;;) {
                 const uint32_t p = next.fetch_add(1);
                 if (p >= N) break;
-                if (sc.lights.empty()) continue;
+                if (n_emitters == 0) continue;
                 Rng rng;
                 rng.seed(seed, (uint64_t(it) * 2 + 0) * N + p);
-                // GenerateLightSample for a quad light: uniform point, cosine-weighted direction
                 const float pick = rng.uniform();
-                uint32_t li = std::min(uint32_t(pick * float(sc.lights.size())), uint32_t(sc.lights.size() - 1));
-                const Light& L = sc.lights[li];
-                const float u = rng.uniform(), v = rng.uniform();
-                const V3 lp = L.pos - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                const float pdfA = 1.0f / (orc::Len(L.x) * orc::Len(L.z));
-                const V3 ln = orc::Norm(L.dir);
-                V3 lt, lb;
-                if (std::fabs(ln.x) > std::fabs(ln.y)) lt = V3(-ln.z, 0, ln.x) * (1.0f / std::sqrt(ln.x * ln.x + ln.z * ln.z));
-                else lt = V3(0, ln.z, -ln.y) * (1.0f / std::sqrt(ln.y * ln.y + ln.z * ln.z));
-                lb = orc::Cross(ln, lt);
-                const float r0 = rng.uniform(), r1 = rng.uniform();
-                const float rr = std::sqrt(r0), ph = 2.0f * kPi * r1;
-                const float cosl = std::sqrt(std::max(0.0f, 1.0f - r0));
-                const V3 dir = orc::Norm(rr * std::cos(ph) * lt + cosl * ln + rr * std::sin(ph) * lb);
-                if (!(cosl > 0.0f)) continue;
-                const float emission_pdf = pdfA * cosl / kPi * light_pick;
-                const float direct_pdfA = pdfA * light_pick;
+                const uint32_t li = std::min(uint32_t(pick * float(n_emitters)), n_emitters - 1);
                 PathState st;
-                st.org = lp;
-                st.dir = dir;
-                st.thr = L.radiance * (cosl / emission_pdf);
-                st.dVCM = direct_pdfA / emission_pdf;
-                st.dVC = 0.0f;  // the emitter cannot be hit by camera or BSDF rays
-                st.dVM = 0.0f;
-                st.len = 1;
                 bool area_start = true;
+                if (li == nq) {
+                    // EmitIblLightSample (AreaLighting.cpp:246-290): a direction toward the environment, the ray
+                    // entering the scene from a disc of the bounding-sphere radius facing it
+                    const float r0 = rng.uniform(), r1 = rng.uniform(), r2 = rng.uniform(), r3 = rng.uniform();
+                    const float r4 = rng.uniform(), r5 = rng.uniform();
+                    float d[3], rad[3];
+                    ora::env_direction(r0, r1, r2, r3, d);
+                    const float pdf_w = ora::env_pdf(d);
+                    if (!(pdf_w > 0.0f)) continue;
+                    ora::env_radiance(d, rad);
+                    const V3 to_env(d[0], d[1], d[2]);
+                    float du, dv;
+                    concentric_disc(r4, r5, du, dv);
+                    V3 dx, dz;
+                    basis(to_env, dx, dz);
+                    const float emission_pdf = pdf_w * sc.disc_pdf * light_pick;
+                    const float direct_pdfA = pdf_w * light_pick;
+                    st.org = sc.center + sc.radius * (to_env + du * dx + dv * dz);
+                    st.dir = -1.0f * to_env;
+                    st.thr = V3(rad[0], rad[1], rad[2]) * (1.0f / emission_pdf);
+                    st.dVCM = direct_pdfA / emission_pdf;
+                    st.dVC = 1.0f / emission_pdf;  // cos at an infinite light: 1
+                    st.dVM = st.dVC * c.vc_weight;
+                    area_start = false;            // no distance term on the first segment
+                } else {
+                    // GenerateLightSample for a quad light: uniform point, cosine-weighted direction
+                    const Light& L = sc.lights[li];
+                    const float u = rng.uniform(), v = rng.uniform();
+                    const V3 lp = L.pos - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                    const float pdfA = 1.0f / (orc::Len(L.x) * orc::Len(L.z));
+                    const V3 ln = orc::Norm(L.dir);
+                    V3 lt, lb;
+                    basis(ln, lt, lb);
+                    const float r0 = rng.uniform(), r1 = rng.uniform();
+                    const float rr = std::sqrt(r0), ph = 2.0f * kPi * r1;
+                    const float cosl = std::sqrt(std::max(0.0f, 1.0f - r0));
+                    const V3 dir = orc::Norm(rr * std::cos(ph) * lt + cosl * ln + rr * std::sin(ph) * lb);
+                    if (!(cosl > 0.0f)) continue;
+                    const float emission_pdf = pdfA * cosl / kPi * light_pick;
+                    const float direct_pdfA = pdfA * light_pick;
+                    st.org = lp;
+                    st.dir = dir;
+                    st.thr = L.radiance * (cosl / emission_pdf);
+                    st.dVCM = direct_pdfA / emission_pdf;
+                    st.dVC = 0.0f;  // the emitter cannot be hit by camera or BSDF rays
+                    st.dVM = 0.0f;
+                }
+                st.len = 1;
                 while (st.len + 2 <= sc.max_len + 1) {
                     Hit h;
                     if (!make_hit(sc, st.org, st.dir, h)) break;
@@ -472,39 +562,86 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
                 V3 color(0.0f);
                 for (;;) {
                     Hit h;
-                    if (!make_hit(sc, st.org, st.dir, h)) break;
+                    if (!make_hit(sc, st.org, st.dir, h)) {
+                        // the path leaves the scene: the environment's radiance with the camera-hit weight
+                        // (ConnectToSkyLight, VCM.cpp:171-187; tech report sec. 5.2); camera rays and chains of
+                        // Dirac vertices see the miss image, with weight 1 (no other strategy makes them)
+                        if (sc.env && use_hit) {
+                            const float d[3] = {st.dir.x, st.dir.y, st.dir.z};
+                            float rad[3];
+                            if (st.delta_only) ora::env_miss(d, rad);
+                            else ora::env_radiance(d, rad);
+                            float mis = 1.0f;
+                            if (st.len > 1 && !single) {
+                                const float pdf_w = ora::env_pdf(d);
+                                const float direct_pdfA = pdf_w * light_pick;
+                                const float emission_pdf = pdf_w * sc.disc_pdf * light_pick;
+                                const float w_camera = direct_pdfA * st.dVCM + emission_pdf * st.dVC;
+                                mis = 1.0f / (1.0f + w_camera);
+                            }
+                            color = color + mis * (st.thr * V3(rad[0], rad[1], rad[2]));
+                        }
+                        break;
+                    }
                     const float d2 = orc::Dot(h.pos - st.org, h.pos - st.org);
                     const float cos_in = std::fabs(orc::Dot(h.n, h.view));
                     st.dVCM *= d2;
                     st.dVCM *= 1.0f / cos_in;
                     st.dVC *= 1.0f / cos_in;
                     st.dVM *= 1.0f / cos_in;
+                    st.delta_only = st.delta_only && h.delta;
                     if (!h.delta) {
-                        // next-event estimation to light set 0 (tech report sec. 5.4; wLight = 0)
-                        if (st.len + 1 <= sc.max_len && !sc.lights.empty()) {
+                        // next-event estimation to light set 0 and the environment (tech report sec. 5.4; wLight
+                        // = 0 for the quads, which BSDF rays cannot hit)
+                        if (st.len + 1 <= sc.max_len && n_emitters > 0) {
                             const float pick = rng.uniform();
-                            uint32_t li = std::min(uint32_t(pick * float(sc.lights.size())), uint32_t(sc.lights.size() - 1));
-                            const Light& L = sc.lights[li];
-                            const float u = rng.uniform(), v = rng.uniform();
-                            const V3 lp = L.pos - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                            const float pdfA = 1.0f / (orc::Len(L.x) * orc::Len(L.z));
-                            V3 to_l = lp - h.pos;
-                            const float dl2 = orc::Dot(to_l, to_l), dl = std::sqrt(dl2);
-                            to_l = to_l * (1.0f / dl);
-                            const float cos_light = orc::Dot(orc::Norm(L.dir), -1.0f * to_l);
-                            if (cos_light > 0.0f) {
-                                float fwd, rev;
-                                const V3 f = orc::bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
-                                if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
-                                    rev *= h.cont;
-                                    const float direct_pdfW = pdfA * dl2 / cos_light;
-                                    const float emission_pdfW = pdfA * cos_light / kPi;
-                                    const float cos_to_light = std::fabs(orc::Dot(h.n, to_l));
-                                    const float w_camera = (emission_pdfW * cos_to_light / (direct_pdfW * cos_light)) *
-                                                           (c.vm_weight + st.dVCM + st.dVC * rev);
-                                    const float mis = single ? 1.0f : 1.0f / (1.0f + w_camera);
-                                    const V3 contrib = (mis / (light_pick * direct_pdfW)) * (L.radiance * f);
-                                    if (use_nee && visible(sc, h, to_l, dl * (1.0f - 1e-4f))) color = color + st.thr * contrib;
+                            const uint32_t li = std::min(uint32_t(pick * float(n_emitters)), n_emitters - 1);
+                            if (li == nq) {
+                                const float r0 = rng.uniform(), r1 = rng.uniform(), r2 = rng.uniform(), r3 = rng.uniform();
+                                float d[3], rad[3];
+                                ora::env_direction(r0, r1, r2, r3, d);
+                                const float pdf_w = ora::env_pdf(d);
+                                const V3 to_l(d[0], d[1], d[2]);
+                                if (pdf_w > 0.0f) {
+                                    float fwd, rev;
+                                    const V3 f = orc::bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                                    if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
+                                        ora::env_radiance(d, rad);
+                                        fwd *= h.cont;
+                                        rev *= h.cont;
+                                        const float emission_pdfW = pdf_w * sc.disc_pdf;
+                                        const float cos_to_light = std::fabs(orc::Dot(h.n, to_l));
+                                        const float w_light = fwd / (light_pick * pdf_w);
+                                        const float w_camera = (emission_pdfW * cos_to_light / pdf_w) *
+                                                               (c.vm_weight + st.dVCM + st.dVC * rev);
+                                        const float mis = single ? 1.0f : 1.0f / (w_light + 1.0f + w_camera);
+                                        const V3 contrib = (mis / (light_pick * pdf_w)) * (V3(rad[0], rad[1], rad[2]) * f);
+                                        if (use_nee && visible(sc, h, to_l, 3.402823466e+38f)) color = color + st.thr * contrib;
+                                    }
+                                }
+                            } else {
+                                const Light& L = sc.lights[li];
+                                const float u = rng.uniform(), v = rng.uniform();
+                                const V3 lp = L.pos - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                                const float pdfA = 1.0f / (orc::Len(L.x) * orc::Len(L.z));
+                                V3 to_l = lp - h.pos;
+                                const float dl2 = orc::Dot(to_l, to_l), dl = std::sqrt(dl2);
+                                to_l = to_l * (1.0f / dl);
+                                const float cos_light = orc::Dot(orc::Norm(L.dir), -1.0f * to_l);
+                                if (cos_light > 0.0f) {
+                                    float fwd, rev;
+                                    const V3 f = orc::bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                                    if (f.x != 0.0f || f.y != 0.0f || f.z != 0.0f) {
+                                        rev *= h.cont;
+                                        const float direct_pdfW = pdfA * dl2 / cos_light;
+                                        const float emission_pdfW = pdfA * cos_light / kPi;
+                                        const float cos_to_light = std::fabs(orc::Dot(h.n, to_l));
+                                        const float w_camera = (emission_pdfW * cos_to_light / (direct_pdfW * cos_light)) *
+                                                               (c.vm_weight + st.dVCM + st.dVC * rev);
+                                        const float mis = single ? 1.0f : 1.0f / (1.0f + w_camera);
+                                        const V3 contrib = (mis / (light_pick * direct_pdfW)) * (L.radiance * f);
+                                        if (use_nee && visible(sc, h, to_l, dl * (1.0f - 1e-4f))) color = color + st.thr * contrib;
+                                    }
                                 }
                             }
                         }

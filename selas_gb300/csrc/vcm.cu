@@ -28,6 +28,7 @@
 
 #include "capi_internal.h"
 #include "graph.h"
+#include "ibl.cuh"
 #include "ptex.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
@@ -49,6 +50,9 @@ struct VcmParams {
     uint32_t material_count;
     const QuadLight* lights;  // light set 0
     uint32_t light_count;
+    const IblDev* ibl;        // the image-based light as an environment emitter (null: none), picked after the quads
+    float3 env_center;        // bounding sphere of the scene's bounding box: the environment's emission disc
+    float env_radius, env_disc_pdf;
     const PtexFace* ptex_faces;
     const __half* ptex_texels;
     uint32_t ptex_face_count;
@@ -78,7 +82,10 @@ struct PathState {
     float3 org, dir, thr;
     float dvcm, dvc, dvm;
     uint32_t len;
+    uint32_t flags;  // kPathEnvStart, kPathNonDelta (stored in the top bits of the length word)
 };
+constexpr uint32_t kPathEnvStart = 1u;  // light path from the environment: no distance term on its first segment
+constexpr uint32_t kPathNonDelta = 2u;  // camera path: a non-Dirac vertex seen (else a miss sees the miss image)
 
 // Stored light vertex: 96 bytes (kVertF4 float4s); the tangent and bitangent sign rebuild the shading frame.
 constexpr int kVertF4 = 6;
@@ -222,7 +229,9 @@ __device__ __forceinline__ PathState load_path(const VcmParams& P, uint32_t s) {
     st.dvc = d.w;
     st.thr = f3(t.x, t.y, t.z);
     st.dvm = t.w;
-    st.len = P.st.plen[s];
+    const uint32_t pl = P.st.plen[s];
+    st.len = pl & 0x3fffffffu;
+    st.flags = pl >> 30;
     return st;
 }
 
@@ -230,7 +239,7 @@ __device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const
     P.st.po[s] = make_float4(st.org.x, st.org.y, st.org.z, st.dvcm);
     P.st.pd[s] = make_float4(st.dir.x, st.dir.y, st.dir.z, st.dvc);
     P.st.pt[s] = make_float4(st.thr.x, st.thr.y, st.thr.z, st.dvm);
-    P.st.plen[s] = st.len;
+    P.st.plen[s] = st.len | (st.flags << 30);
 }
 
 // Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
@@ -296,48 +305,100 @@ __global__ void k_bounce_reset(uint32_t* counters, int next) {
     }
 }
 
-// GenerateLightSample for a quad light of light set 0 (VCMCommon.cpp:37-62 restated for an area emitter:
-// uniform point on the quad, cosine-weighted direction about its facing direction).
+// Concentric map of the unit square onto the unit disc (Shirley and Chiu, "A Low Distortion Map Between Disk and
+// Square", 1997): the disc sample of EmitIblLightSample (AreaLighting.cpp:268-272).
+__device__ __forceinline__ void concentric_disc(float r0, float r1, float& u, float& v) {
+    const float a = 2.0f * r0 - 1.0f, b = 2.0f * r1 - 1.0f;
+    if (a == 0.0f && b == 0.0f) {
+        u = 0.0f;
+        v = 0.0f;
+        return;
+    }
+    float r, phi;
+    if (fabsf(a) > fabsf(b)) {
+        r = a;
+        phi = (kPi / 4.0f) * (b / a);
+    } else {
+        r = b;
+        phi = kPi / 2.0f - (kPi / 4.0f) * (a / b);
+    }
+    u = r * cosf(phi);
+    v = r * sinf(phi);
+}
+
+// GenerateLightSample (VCMCommon.cpp:37-62): a light picked uniformly among the quads of light set 0 and the
+// environment.  A quad emits from a uniform point, cosine-weighted about its facing direction; the environment
+// (EmitIblLightSample, AreaLighting.cpp:246-290; tech report sec. 5.1) along a sampled direction from a disc of
+// the bounding-sphere radius facing it, as an infinite light (cos 1, hit by camera and BSDF rays).
 __global__ void __launch_bounds__(kBlock) k_l_generate(VcmParams P) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t N = P.npaths;
+    const uint32_t n_emitters = P.light_count + (P.ibl ? 1u : 0u);
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
         const uint32_t p = base + threadIdx.x;
         bool alive = false;
         if (p < N) {
             P.st.vcount[p] = 0;
-            if (P.light_count > 0) {
+            if (n_emitters > 0) {
                 const uint64_t stream = (uint64_t(c.pass) * 2 + 0) * N + p;
                 Pcg32 rng = pcg_seed(P.seed, stream);
                 const float pick = pcg_float(rng);
-                uint32_t li = uint32_t(pick * float(P.light_count));
-                li = li < P.light_count - 1 ? li : P.light_count - 1;
-                const QuadLight L = P.lights[li];
-                const float u = pcg_float(rng), v = pcg_float(rng);
-                const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                const float pdf_a = 1.0f / (length(L.x) * length(L.z));
-                const float3 ln = normalize(L.direction);
-                float3 lt, lb;
-                orthonormal_basis(ln, lt, lb);
-                const float r0 = pcg_float(rng), r1 = pcg_float(rng);
-                const float rr = sqrtf(r0), ph = 2.0f * kPi * r1;
-                const float cosl = sqrtf(fmaxf(0.0f, 1.0f - r0));
-                const float3 dir = normalize(rr * cosf(ph) * lt + cosl * ln + rr * sinf(ph) * lb);
-                if (cosl > 0.0f) {
-                    const float light_pick = 1.0f / float(P.light_count);
-                    const float emission_pdf = pdf_a * cosl / kPi * light_pick;
-                    const float direct_pdf_a = pdf_a * light_pick;
-                    PathState st;
-                    st.org = lp;
-                    st.dir = dir;
-                    st.thr = L.radiance * (cosl / emission_pdf);
-                    st.dvcm = direct_pdf_a / emission_pdf;
-                    st.dvc = 0.0f;  // the emitter cannot be hit by camera or BSDF rays
-                    st.dvm = 0.0f;
-                    st.len = 1;
+                uint32_t li = uint32_t(pick * float(n_emitters));
+                li = li < n_emitters - 1 ? li : n_emitters - 1;
+                const float light_pick = 1.0f / float(n_emitters);
+                PathState st;
+                st.len = 1;
+                st.flags = 0;
+                if (li == P.light_count) {
+                    const float r0 = pcg_float(rng), r1 = pcg_float(rng), r2 = pcg_float(rng), r3 = pcg_float(rng);
+                    const float r4 = pcg_float(rng), r5 = pcg_float(rng);
+                    const IblDev& ibl = *P.ibl;
+                    const float3 to_env = ibl_env_direction(ibl, r0, r1, r2, r3);
+                    const float pdf_w = ibl_env_pdf(ibl, to_env);
+                    if (pdf_w > 0.0f) {
+                        const float3 rad = ibl_radiance(ibl, to_env);
+                        float du, dv;
+                        concentric_disc(r4, r5, du, dv);
+                        float3 dx, dz;
+                        orthonormal_basis(to_env, dx, dz);
+                        const float emission_pdf = pdf_w * P.env_disc_pdf * light_pick;
+                        const float direct_pdf_a = pdf_w * light_pick;
+                        st.org = P.env_center + P.env_radius * (to_env + du * dx + dv * dz);
+                        st.dir = -to_env;
+                        st.thr = rad * (1.0f / emission_pdf);
+                        st.dvcm = direct_pdf_a / emission_pdf;
+                        st.dvc = 1.0f / emission_pdf;  // cos at an infinite light: 1
+                        st.dvm = st.dvc * c.vc_weight;
+                        st.flags = kPathEnvStart;
+                        alive = true;
+                    }
+                } else {
+                    const QuadLight L = P.lights[li];
+                    const float u = pcg_float(rng), v = pcg_float(rng);
+                    const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                    const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                    const float3 ln = normalize(L.direction);
+                    float3 lt, lb;
+                    orthonormal_basis(ln, lt, lb);
+                    const float r0 = pcg_float(rng), r1 = pcg_float(rng);
+                    const float rr = sqrtf(r0), ph = 2.0f * kPi * r1;
+                    const float cosl = sqrtf(fmaxf(0.0f, 1.0f - r0));
+                    const float3 dir = normalize(rr * cosf(ph) * lt + cosl * ln + rr * sinf(ph) * lb);
+                    if (cosl > 0.0f) {
+                        const float emission_pdf = pdf_a * cosl / kPi * light_pick;
+                        const float direct_pdf_a = pdf_a * light_pick;
+                        st.org = lp;
+                        st.dir = dir;
+                        st.thr = L.radiance * (cosl / emission_pdf);
+                        st.dvcm = direct_pdf_a / emission_pdf;
+                        st.dvc = 0.0f;  // the emitter cannot be hit by camera or BSDF rays
+                        st.dvm = 0.0f;
+                        alive = true;
+                    }
+                }
+                if (alive) {
                     store_path(P, p, st);
                     P.st.prng[p] = rng.state;
-                    alive = true;
                 }
             }
         }
@@ -366,6 +427,7 @@ __global__ void __launch_bounds__(kBlock) k_c_generate(VcmParams P) {
         st.dvc = 0.0f;
         st.dvm = 0.0f;
         st.len = 1;
+        st.flags = 0;
         store_path(P, p, st);
         P.st.prng[p] = rng.state;
         P.st.queue[0][p] = p;
@@ -457,7 +519,7 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const 
                 const float3 seg = h.pos - st.org;
                 const float d2 = dot(seg, seg);
                 const float cos_in = fabsf(dot(h.n, h.view));
-                st.dvcm *= d2;
+                if (st.len > 1 || !(st.flags & kPathEnvStart)) st.dvcm *= d2;
                 st.dvcm *= 1.0f / cos_in;
                 st.dvc *= 1.0f / cos_in;
                 st.dvm *= 1.0f / cos_in;
@@ -752,36 +814,65 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const 
                 st.dvc *= 1.0f / cos_in;
                 st.dvm *= 1.0f / cos_in;
                 rng = load_rng(P, s, (uint64_t(c.pass) * 2 + 1) * N + s);
+                if (!h.delta) st.flags |= kPathNonDelta;
+                const uint32_t n_emitters = P.light_count + (P.ibl ? 1u : 0u);
+                const float light_pick = n_emitters ? 1.0f / float(n_emitters) : 0.0f;
                 if (!h.delta) {
                     record = true;
-                    // next-event estimation to light set 0 (tech report sec. 5.4; wLight = 0)
-                    if (st.len + 1 <= P.max_len && P.light_count > 0) {
+                    // next-event estimation to light set 0 and the environment (tech report sec. 5.4; wLight = 0
+                    // for the quads, which BSDF rays cannot hit)
+                    if (st.len + 1 <= P.max_len && n_emitters > 0) {
                         const float pick = pcg_float(rng);
-                        uint32_t li = uint32_t(pick * float(P.light_count));
-                        li = li < P.light_count - 1 ? li : P.light_count - 1;
-                        const QuadLight L = P.lights[li];
-                        const float u = pcg_float(rng), v = pcg_float(rng);
-                        const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
-                        const float pdf_a = 1.0f / (length(L.x) * length(L.z));
-                        to_l = lp - h.pos;
-                        const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
-                        to_l = to_l * (1.0f / dl);
-                        const float cos_light = dot(normalize(L.direction), -to_l);
-                        if (cos_light > 0.0f) {
-                            float fwd, rev;
-                            const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
-                            if (nonzero(f)) {
-                                rev *= h.cont;
-                                const float light_pick = 1.0f / float(P.light_count);
-                                const float direct_pdf_w = pdf_a * dl2 / cos_light;
-                                const float emission_pdf_w = pdf_a * cos_light / kPi;
-                                const float cos_to_light = fabsf(dot(h.n, to_l));
-                                const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
-                                                       (c.vm_weight + st.dvcm + st.dvc * rev);
-                                const float mis = 1.0f / (1.0f + w_camera);
-                                contrib = st.thr * ((mis / (light_pick * direct_pdf_w)) * (L.radiance * f));
-                                tfar = dl * (1.0f - 1e-4f);
-                                nee_ray = nonzero(contrib);
+                        uint32_t li = uint32_t(pick * float(n_emitters));
+                        li = li < n_emitters - 1 ? li : n_emitters - 1;
+                        if (li == P.light_count) {
+                            const float r0 = pcg_float(rng), r1 = pcg_float(rng), r2 = pcg_float(rng);
+                            const float r3 = pcg_float(rng);
+                            const IblDev& ibl = *P.ibl;
+                            to_l = ibl_env_direction(ibl, r0, r1, r2, r3);
+                            const float pdf_w = ibl_env_pdf(ibl, to_l);
+                            if (pdf_w > 0.0f) {
+                                float fwd, rev;
+                                const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                                if (nonzero(f)) {
+                                    const float3 rad = ibl_radiance(ibl, to_l);
+                                    fwd *= h.cont;
+                                    rev *= h.cont;
+                                    const float emission_pdf_w = pdf_w * P.env_disc_pdf;
+                                    const float cos_to_light = fabsf(dot(h.n, to_l));
+                                    const float w_light = fwd / (light_pick * pdf_w);
+                                    const float w_camera = (emission_pdf_w * cos_to_light / pdf_w) *
+                                                           (c.vm_weight + st.dvcm + st.dvc * rev);
+                                    const float mis = 1.0f / (w_light + 1.0f + w_camera);
+                                    contrib = st.thr * ((mis / (light_pick * pdf_w)) * (rad * f));
+                                    tfar = kFloatMax;
+                                    nee_ray = nonzero(contrib);
+                                }
+                            }
+                        } else {
+                            const QuadLight L = P.lights[li];
+                            const float u = pcg_float(rng), v = pcg_float(rng);
+                            const float3 lp = L.position - 0.5f * L.x - 0.5f * L.z + u * L.x + v * L.z;
+                            const float pdf_a = 1.0f / (length(L.x) * length(L.z));
+                            to_l = lp - h.pos;
+                            const float dl2 = dot(to_l, to_l), dl = sqrtf(dl2);
+                            to_l = to_l * (1.0f / dl);
+                            const float cos_light = dot(normalize(L.direction), -to_l);
+                            if (cos_light > 0.0f) {
+                                float fwd, rev;
+                                const float3 f = bsdf_evaluate(h.s, h.view, to_l, fwd, rev);
+                                if (nonzero(f)) {
+                                    rev *= h.cont;
+                                    const float direct_pdf_w = pdf_a * dl2 / cos_light;
+                                    const float emission_pdf_w = pdf_a * cos_light / kPi;
+                                    const float cos_to_light = fabsf(dot(h.n, to_l));
+                                    const float w_camera = (emission_pdf_w * cos_to_light / (direct_pdf_w * cos_light)) *
+                                                           (c.vm_weight + st.dvcm + st.dvc * rev);
+                                    const float mis = 1.0f / (1.0f + w_camera);
+                                    contrib = st.thr * ((mis / (light_pick * direct_pdf_w)) * (L.radiance * f));
+                                    tfar = dl * (1.0f - 1e-4f);
+                                    nee_ray = nonzero(contrib);
+                                }
                             }
                         }
                     }
@@ -790,6 +881,24 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const 
                     const float4* lslots = P.st.verts + size_t(s) * P.slots * kVertF4;
                     while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * kVertF4].w) + 1 + st.len <= P.max_len) ++nvc;
                 }
+            } else if (P.ibl) {
+                // the path leaves the scene: the environment's radiance with the camera-hit weight (ConnectToSkyLight,
+                // VCM.cpp:171-187; tech report sec. 5.2); camera rays and chains of Dirac vertices see the miss
+                // image, with weight 1 (no other strategy makes them)
+                const PathState ms = load_path(P, s);
+                const IblDev& ibl = *P.ibl;
+                const float3 rad = (ms.flags & kPathNonDelta) ? ibl_radiance(ibl, ms.dir) : ibl_miss(ibl, ms.dir);
+                float mis = 1.0f;
+                if (ms.len > 1) {
+                    const float pdf_w = ibl_env_pdf(ibl, ms.dir);
+                    const float light_pick = 1.0f / float(P.light_count + 1u);
+                    const float direct_pdf_a = pdf_w * light_pick;
+                    const float emission_pdf = pdf_w * P.env_disc_pdf * light_pick;
+                    const float w_camera = direct_pdf_a * ms.dvcm + emission_pdf * ms.dvc;
+                    mis = 1.0f / (1.0f + w_camera);
+                }
+                const float3 env = mis * (ms.thr * rad);
+                if (nonzero(env)) splat(P.accum, s, env);
             }
         }
         // camera-vertex record with the state at the vertex, its connection pairs, the next-event segment
@@ -1130,6 +1239,18 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     P.err = d_err;
     P.lights = sc.lights + set.light_first;
     P.light_count = set.light_count;
+    if (sc.ibl) {
+        // the environment's emission disc: the bounding sphere of the scene's bounding box, radius half its diagonal
+        float d2 = 0.0f;
+        for (int a = 0; a < 3; ++a) {
+            const float e = sc.hi[a] - sc.lo[a];
+            d2 += e * e;
+        }
+        P.ibl = sc.ibl;
+        P.env_center = make_float3(0.5f * (sc.lo[0] + sc.hi[0]), 0.5f * (sc.lo[1] + sc.hi[1]), 0.5f * (sc.lo[2] + sc.hi[2]));
+        P.env_radius = 0.5f * std::sqrt(d2);
+        P.env_disc_pdf = (1.0f / kPi) * (1.0f / (P.env_radius * P.env_radius));
+    }
 
     const uint32_t N = st.paths;
     const size_t nv = size_t(N) * st.slots_per_path;

@@ -5,6 +5,7 @@ VCM, bidirectional path tracing and each strategy alone must converge to the ora
 The reference Disney BSDF is not of that kind (its diffuse sample weight and pdf differ from f * cos /
 density by a factor pi, Disney.cpp:466-519), so on it VCM converges to its own image, the FP64 oracle VCM.
 """
+import dataclasses
 from pathlib import Path
 
 import numpy as np
@@ -65,6 +66,40 @@ def test_oracle_merging_alone_converges(cornell, lambert_pt):
         img = oracle.vcm_render(cornell, SIZE, SIZE, 0, it, max_len=2, merging=True, strategies=4,
                                 radius0=3.0) / it
     np.testing.assert_allclose(_mean(img), lambert_pt[2], rtol=0.02)
+
+
+def _env_scene(cornell, quads=False, rotation=0.0):
+    """The Cornell box (open at the front) lit by the image-based light, with or without its quad light."""
+    return dataclasses.replace(cornell, ibl=scenes.sky_ibl(rotation=rotation), lights=cornell.lights if quads else [])
+
+
+@pytest.mark.parametrize("length", [2, 3])
+def test_oracle_vcm_with_environment_converges_to_path_tracing(cornell, length):
+    """The image-based light as VCM's environment emitter (light paths from a disc of the bounding-sphere radius,
+    next-event estimation, camera paths that leave the scene): with it the only light, VCM with paths of at most L
+    segments converges to the oracle path tracer with L bounces, which sees the environment only where BSDF
+    sampling leaves the scene.  Both merging and bidirectional path tracing."""
+    rs = _env_scene(cornell)
+    with oracle.consistent_lambert():
+        spp = 4096
+        pt = _mean(oracle.pt_render(rs, 24, 24, 0, spp, max_bounces=length, physical_nee=True)[1] / spp)
+        it = 256
+        for merging in (True, False):
+            img = oracle.vcm_render(rs, 24, 24, 0, it, max_len=length, merging=merging) / it
+            np.testing.assert_allclose(_mean(img), pt, rtol=0.015)
+        # the camera-hit strategy alone is the path tracer's estimator of the environment
+        hit = oracle.vcm_render(rs, 24, 24, 0, it, max_len=length, strategies=16) / it
+        np.testing.assert_allclose(_mean(hit), pt, rtol=0.015)
+
+
+def test_oracle_vcm_light_pick_is_linear(cornell):
+    """Quads and the environment share one uniform light pick: the image of both is the sum of each alone."""
+    with oracle.consistent_lambert():
+        it = 256
+        both = _mean(oracle.vcm_render(_env_scene(cornell, quads=True), 24, 24, 0, it, max_len=3) / it)
+        env = _mean(oracle.vcm_render(_env_scene(cornell), 24, 24, 0, it, max_len=3) / it)
+        quads = _mean(oracle.vcm_render(cornell, 24, 24, 0, it, max_len=3) / it)
+    np.testing.assert_allclose(both, env + quads, rtol=0.015)
 
 
 def test_oracle_vcm_without_merging_is_bpt_at_zero_radius_weight(cornell):
@@ -188,3 +223,28 @@ def test_gpu_material_sort_does_not_change_the_image(device):
     sc.release()
     np.testing.assert_allclose(imgs[0][0], imgs[1][0], rtol=1e-5, atol=1e-8)
     np.testing.assert_allclose(imgs[0][1], imgs[1][1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("rotation", [0.0, 0.3])
+def test_gpu_vcm_with_environment_traces_the_oracles_paths(device, cornell, rotation):
+    """Quads and the image-based light together: the GPU passes trace the oracle's light paths (from either
+    emitter), next-event rays and camera paths that leave the scene."""
+    rs = _env_scene(cornell, quads=True, rotation=rotation)
+    passes, size = 4, 48
+    gpu = _gpu_vcm(device, rs, size, passes)
+    cpu = oracle.vcm_render(rs, size, size, 0, passes, max_len=10, radius0=R0, seed=SEED) / passes
+    _same_paths(gpu, cpu)
+
+
+@pytest.mark.gpu
+def test_gpu_vcm_with_environment_on_a_textured_open_scene(device):
+    """The textured spheres under the sky alone (material-sorted bounces, Ptex, most camera paths leaving the
+    scene): same paths as the oracle."""
+    import selas_gb300 as sel
+    rs = dataclasses.replace(scenes.textured_spheres(count=4, level=3), ibl=scenes.sky_ibl(rotation=0.3), lights=[])
+    sc = rs.build(sel, device)
+    gpu = sc.vcm_generate_image(rs.sel_camera(sel, 48, 40), sel.vcm_settings(3, 8, SEED, 0, True, R0))
+    sc.release()
+    cpu = oracle.vcm_render(rs, 48, 40, 0, 3, max_len=8, radius0=R0, seed=SEED) / 3
+    _same_paths(gpu.astype(np.float64), cpu)
