@@ -278,7 +278,10 @@ int sel_scene_set_background(SelScene scene, float r, float g, float b);
  * (BuildCommon/BuildImageBasedLight.cpp:18-107, built here); `miss` (may be null: the light image times the
  * exposure) is what camera rays and pure-specular chains see (EvaluateBackgroundMiss).  Replaces the uniform
  * background in the path tracer (misses) and the deferred path tracer (misses, background next-event
- * estimation and its MIS); VCM ignores it.  width == 0 removes the image. */
+ * estimation and its MIS).  In VCM it is an environment emitter beside the quad lights of light set 0 (light
+ * sub-paths from a disc of the scene's bounding-sphere radius, next-event estimation, camera paths that leave
+ * the scene; GenerateLightSample, VCMCommon.cpp:37-62), sampled with the density of the directions whose lookup
+ * returns each texel; without it VCM's misses carry no radiance.  width == 0 removes the image. */
 int sel_scene_set_ibl(SelScene scene, const float* rgb, unsigned int width, unsigned int height, const float* miss_rgb,
                       unsigned int miss_width, unsigned int miss_height, float rotationRadians, float exposureScale);
 
