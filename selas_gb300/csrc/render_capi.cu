@@ -582,6 +582,7 @@ int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSetti
     set.max_len = settings.maxPathLength;
     set.seed = settings.seed;
     set.merging = settings.disableMerging ? 0 : 1;
+    set.trace_block = sc->tuned_trace_block;
     vcm_lights(sc, set);
     const PtScene ps = scene_view(sc);
     const VcmState st = vcm_state_carve(sc->vcm_block, paths, settings.maxPathLength, kVcmChunk);

@@ -190,6 +190,7 @@ bool admit_one(SelServerTy* S, Job* j) {
         j->vset.max_len = d.vcm.maxPathLength;
         j->vset.seed = d.vcm.seed;
         j->vset.merging = d.vcm.disableMerging ? 0 : 1;
+        j->vset.trace_block = sc->tuned_trace_block;
         vcm_lights(sc, j->vset);
         const float r0 = d.vcm.radius != 0.0f ? d.vcm.radius : vcm_default_radius(sc);
         std::vector<VcmConsts> consts(d.vcm.passes);

@@ -436,9 +436,9 @@ __global__ void __launch_bounds__(kBlock) k_c_generate(VcmParams P) {
 }
 
 // Closest hits of the queued paths: persistent blocks, warps take 32-entry packets through an atomic cursor.
-template <int K>
-__global__ void __launch_bounds__(kBlock, 8) k_extend(VcmParams P, int cur) {
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+template <int K, int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_extend(VcmParams P, int cur) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     const uint32_t* queue = P.st.queue[cur];
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(VcmParams P, int cur) {
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = kFloatMax;
             QueryHit h;
-            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock,
+            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B,
                                                                 status);
             P.st.phit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
                                  : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
@@ -466,9 +466,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_extend(VcmParams P, int cur) {
 }
 
 // Any-hit of the queued shadow rays; unoccluded ones add their contribution to their pixel.
-template <int K>
-__global__ void __launch_bounds__(kBlock, 8) k_shadow(VcmParams P) {
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * kBlock];
+template <int K, int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_shadow(VcmParams P) {
+    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     uint32_t status = 0;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_shadow(VcmParams P) {
                 q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
                 q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
                 QueryHit h;
-                if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, kBlock, status))
+                if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B, status))
                     splat(P.accum, __float_as_uint(c.w), f3(c.x, c.y, c.z));
             }
         }
@@ -1262,8 +1262,20 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     int cur = 0;
     for (int r = 0; r < radix_passes; ++r) cur ^= 1;
     P.sorted_index = st.vals[cur];
-    const int trace_grid = sms * 8;
+    // traversal blocks of 256 or 128 threads, 1024 threads per SM either way (the scene's tuned block size)
+    const int tb = (set.trace_block == 256 && sc.bvh_kind == 0) ? 256 : 128;
+    const int trace_grid = sms * (1024 / tb);
     const int shade_grid = sms * 8;
+    auto extend = [&](cudaStream_t stream, int cur) {
+        if (sc.bvh_kind != 0) k_extend<1, 128><<<trace_grid, 128, 0, stream>>>(P, cur);
+        else if (tb == 256) k_extend<0, 256><<<trace_grid, 256, 0, stream>>>(P, cur);
+        else k_extend<0, 128><<<trace_grid, 128, 0, stream>>>(P, cur);
+    };
+    auto shadow = [&](cudaStream_t stream) {
+        if (sc.bvh_kind != 0) k_shadow<1, 128><<<trace_grid, 128, 0, stream>>>(P);
+        else if (tb == 256) k_shadow<0, 256><<<trace_grid, 256, 0, stream>>>(P);
+        else k_shadow<0, 128><<<trace_grid, 128, 0, stream>>>(P);
+    };
     const bool sort = sc.sort_hint != 0;
     // material-class sort and Ptex of a bounce's hits; returns the queue the shading kernel reads
     auto sort_hits = [&](cudaStream_t stream, int cur) -> const uint32_t* {
@@ -1283,13 +1295,11 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         for (uint32_t b = 0; b + 1 < set.max_len; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
-            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
             if (sort) k_l_shade<true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
             else k_l_shade<false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
-            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
-            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
+            shadow(stream);
         }
         // hash grid over the stored vertices
         k_bounds<<<kBoundsBlocks, 256, 0, stream>>>(P);
@@ -1313,25 +1323,24 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         for (uint32_t b = 0; b < set.max_len; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
-            if (sc.bvh_kind == 0) k_extend<0><<<trace_grid, kBlock, 0, stream>>>(P, cur);
-            else k_extend<1><<<trace_grid, kBlock, 0, stream>>>(P, cur);
+            extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
             if (sort) k_c_shade<true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
             else k_c_shade<false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
             k_c_connect<<<shade_grid, kBlock, 0, stream>>>(P);
             k_c_merge<<<shade_grid, kBlock, 0, stream>>>(P);
-            if (sc.bvh_kind == 0) k_shadow<0><<<trace_grid, kBlock, 0, stream>>>(P);
-            else k_shadow<1><<<trace_grid, kBlock, 0, stream>>>(P);
+            shadow(stream);
         }
         k_pass_end<<<1, 32, 0, stream>>>(st.iter);
     };
     struct Key {
         VcmParams P;
-        int kind, sms, radix_passes, sort;
+        int kind, sms, radix_passes, sort, tb;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
     key.kind = sc.bvh_kind;
+    key.tb = tb;
     key.sms = sms;
     key.radix_passes = radix_passes;
     key.sort = sort ? 1 : 0;

@@ -28,6 +28,7 @@ struct VcmSettings {
     uint64_t seed;
     int merging;       // 0: bidirectional path tracing (no merge term, no merge weights)
     uint32_t light_first, light_count;  // light set 0 within the scene's light array
+    uint32_t trace_block;  // threads per traversal block: 256 or 128 (the 8-wide layout; the binary one: 128)
 };
 
 // Device scratch of one VCM pass for `paths` light and camera paths (paths = width * height): the light
