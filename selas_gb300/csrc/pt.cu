@@ -24,6 +24,7 @@
 // job accumulates one layer (radiance).
 #include "pt.h"
 
+#include <algorithm>
 #include <cstring>
 
 #include "capi_internal.h"
@@ -790,7 +791,8 @@ size_t pt_state_block_bytes(uint32_t paths) {
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
-                           bool instanced, bool texture, bool ray_sort) {
+                           bool instanced, bool texture, bool ray_sort, uint64_t batch_paths) {
+    const bool face_order = sort && texture && batch_paths >= kFaceOrderPaths;
     // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
     // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
     const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;
@@ -814,9 +816,9 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             else if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
             else if (bvh_kind == 0) k_extend<0, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             else k_extend<1, 128><<<trace_grid, tb, 0, s>>>(P, cur);
-            if (sort && texture) {
-                // textured scenes: order by (class, Ptex face, footprint region), three 8-bit radix passes from
-                // the queue to queue_sorted (through rvals)
+            if (face_order) {
+                // textured scenes, large batches: order by (class, Ptex face, footprint region), three 8-bit
+                // radix passes from the queue to queue_sorted (through rvals)
                 if (instanced) k_sort_keys<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 else k_sort_keys<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 const uint32_t ntiles = (st.capacity + kSortTile - 1) / kSortTile;
@@ -883,7 +885,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes, instanced, texture, ray_sort;
+        uint32_t modes, instanced, texture, ray_sort, face_order;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -896,6 +898,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.instanced = instanced ? 1u : 0u;
     key.texture = texture ? 1u : 0u;
     key.ray_sort = ray_sort ? 1u : 0u;
+    key.face_order = face_order ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -921,7 +924,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
                           trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr,
-                          pt_scene_textured(sc), sc.ray_sort != 0);
+                          pt_scene_textured(sc), sc.ray_sort != 0, std::min<uint64_t>(job.total, st.capacity));
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -468,7 +468,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
     std::memset(jobs, 0, sizeof(jobs));
     std::memset(&ctl, 0, sizeof(ctl));
     const uint32_t layers = mode == kPtModeDeferred ? 1u : 2u;
-    uint64_t batches = 0;
+    uint64_t batches = 0, batch_paths = 0;
     size_t offset = 0;
     for (uint32_t k = 0; k < count; ++k) {
         PtJob& j = jobs[k];
@@ -483,6 +483,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
         offset += size_t(layers) * cams[k].width * cams[k].height * 3;
         ctl.quota[k] = cap / count;
         batches = std::max(batches, (j.total + ctl.quota[k] - 1) / ctl.quota[k]);
+        batch_paths += std::min<uint64_t>(j.total, ctl.quota[k]);
     }
     ctl.njobs = count;
     cudaError_t e = cudaMemcpyAsync(st.jobs, jobs, sizeof(PtJob) * kMaxPtJobs, cudaMemcpyHostToDevice, stream);
@@ -492,7 +493,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
                        sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
-                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0);
+                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0, batch_paths);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
 }
 

@@ -297,8 +297,10 @@ bool pt_round(SelServerTy* S) {
             modes |= S->slots[k]->desc.integrator == SEL_INTEGRATOR_DEFERRED ? 2u : 1u;
         }
     // rounds per batch: the largest maxBounces of the jobs in the slots (at most config.max_bounces)
+    uint64_t batch_paths = 0;
+    for (int k = 0; k < kMaxPtJobs; ++k) batch_paths += c.quota[k];
     cudaError_t e = pt_run_batches(0, bounces, sort, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph, 128,
-                                   modes, instanced, texture, ray_sort);
+                                   modes, instanced, texture, ray_sort, batch_paths);
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
         if (!j || c.quota[k] == 0) continue;

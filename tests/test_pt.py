@@ -144,3 +144,21 @@ def test_gpu_ray_sort_does_not_change_the_image(device):
     sc.release()
     np.testing.assert_allclose(imgs[0][0], imgs[1][0], rtol=1e-5, atol=1e-8)
     np.testing.assert_allclose(imgs[0][1], imgs[1][1], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_face_order_does_not_change_the_image(device):
+    """Batches of 2M paths or more order a textured scene's hits by Ptex face and footprint region as well as by
+    material class (here 64 x 64 x 512 spp in one batch): the same paths as queue order, so the same image up to
+    the order of FP64 additions."""
+    import selas_gb300 as sel
+    rs = scenes.textured_spheres(count=4, level=3)
+    sc = rs.build(sel, device)
+    cam = rs.sel_camera(sel, 64, 64)
+    imgs = []
+    for sort in (1, 0):
+        device.set_option(sel.SEL_OPTION_MATERIAL_SORT, sort)
+        imgs.append(sc.pt_generate_image(cam, sel.pt_settings(512, 6, seed=9)))
+    device.set_option(sel.SEL_OPTION_MATERIAL_SORT, 1)
+    sc.release()
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-8)
