@@ -293,8 +293,9 @@ def serve_metrics(sel, scenes, dev, room, args):
 def profile_case(case):
     """Bounded workloads sized for ncu captures (a few GB on the device at most): ray queries on the 5.24 M-
     triangle scene (1,048,576 coherent and incoherent rays, closest + any hit), two device BVH builds of
-    that scene, and the path tracer (4 spp), VCM (2 passes) and the deferred path tracer (4 and 9 samples, at
-    most 16 segments) on the room with 8 textured icospheres at 640 x 360; the instanced terrain at 1024 x 1024
+    that scene, and the path tracer (2 and 4 spp, then 4 spp at 1280 x 720 in one batch of 3.7 M paths), VCM
+    (2 passes) and the deferred path tracer (4 and 9 samples, at most 16 segments) on the room with 8 textured
+    icospheres at 640 x 360; the instanced terrain at 1024 x 1024
     (2.1 M terrain triangles, 5,000 instances of 20,480 triangles): 1,048,576 camera rays (closest + any hit)
     and the path tracer at 640 x 360, 4 spp."""
     from selas_gb300._build import build_library
@@ -325,6 +326,8 @@ def profile_case(case):
         if case in ("pt", "all"):
             sc.pt_generate_image(cam, sel.pt_settings(2, 8))
             sc.pt_generate_image(cam, sel.pt_settings(4, 8))
+            # one batch of 3.7 M paths: textured hits ordered by Ptex face as well as material class
+            sc.pt_generate_image(room.sel_camera(sel, 1280, 720), sel.pt_settings(4, 8))
         if case in ("vcm", "all"):
             lo, hi = room.geometry.bounds()
             sc.vcm_generate_image(cam, sel.vcm_settings(2, 10, radius=0.003 * float(np.linalg.norm(hi - lo))))
