@@ -259,6 +259,33 @@ int sel_material_defaults(SelMaterial* out);
 /* Material of geometry geomID (geomID < 65536); geometries without one use the default material. */
 int sel_scene_set_material(SelScene scene, unsigned int geomID, const SelMaterial* material);
 
+/* A material from the text of one material JSON file (ImportMaterial, BuildCommon/ImportMaterial.cpp:56-88, then
+ * BuildMaterial, BuildCommon/BuildModel.cpp:22-64): "shaderName" (DisneyThin, DisneySolid or DeltaTransparent,
+ * any case; DisneySolid otherwise), "baseColor" ([r, g, b], default 0.6 grey; a string names a texture, written
+ * NUL-terminated to base_color_texture (truncated to texture_capacity - 1 bytes, may be null) with the colour left
+ * 0.6 grey), "transmittanceColor" (default 0), the scalar attributes with the importer's defaults (metallic 0.3,
+ * roughness 0.5, ior 1.5, the others 0; a string there names a texture, which is not sampled: the default is
+ * kept), "usesPtex" (default false).  alphaTesting, invertDisplacement and displacement have no use here.
+ * Malformed JSON or a document that is not an object: SEL_ERR_INVALID_ARGUMENT, with the offset in the message.
+ * Needs no device. */
+int sel_material_from_json(const char* json, SelMaterial* out, char* base_color_texture, unsigned int texture_capacity);
+
+/* One entry of a Disney-island materials file. */
+typedef struct SelNamedMaterial {
+    char name[64];        /* material or assignment name, NUL-terminated (truncated to 63 bytes) */
+    SelMaterial material;
+    char colorMap[256];   /* Ptex path with '/' separators ("" when the material has none) */
+} SelNamedMaterial;
+
+/* The materials of a Disney-island materials file (ImportDisneyMaterials, ImportMaterial.cpp:91-146, then
+ * BuildMaterial): an object of named materials, each with "baseColor" (default 1), the scalar attributes (the
+ * importer's defaults), "type" ("solid": DisneySolid, else DisneyThin), an optional "colorMap" (usesPtex when
+ * non-empty) and an optional "assignment" array of further names that take the same material; transmittance
+ * colour 1.  Entries are written in document order, each material followed by its assignment names; *count
+ * receives the number of entries, of which the first `capacity` are written (call with capacity 0 to size
+ * `out`).  Needs no device. */
+int sel_disney_materials_from_json(const char* json, SelNamedMaterial* out, unsigned int capacity, unsigned int* count);
+
 /* SceneLight (SceneLib/SceneResource.h) as the lighting code reads it: quad centre, facing direction,
  * full edge vectors x and z, emitted radiance (AreaLighting.cpp:113-153). */
 typedef struct SelQuadLight {

@@ -255,6 +255,10 @@ class SelMaterial(ctypes.Structure):
                 ("usesPtex", ctypes.c_uint32)]
 
 
+class SelNamedMaterial(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 64), ("material", SelMaterial), ("colorMap", ctypes.c_char * 256)]
+
+
 class SelQuadLight(ctypes.Structure):
     _fields_ = [("position", _f3), ("direction", _f3), ("x", _f3), ("z", _f3), ("radiance", _f3)]
 
@@ -281,6 +285,9 @@ register_signatures({
     "sel_bsdf_evaluate_device": [_vp, _vp, _vp, _u, _vp, _vp],
     "sel_bsdf_sample_device": [_vp, _vp, _vp, _u, _vp, _vp],
     "sel_material_defaults": [ctypes.POINTER(SelMaterial)],
+    "sel_material_from_json": [ctypes.c_char_p, ctypes.POINTER(SelMaterial), ctypes.c_char_p, _u],
+    "sel_disney_materials_from_json": [ctypes.c_char_p, ctypes.POINTER(SelNamedMaterial), _u,
+                                       ctypes.POINTER(ctypes.c_uint)],
     "sel_scene_set_material": [_vp, _u, ctypes.POINTER(SelMaterial)],
     "sel_scene_add_quad_light": [_vp, _u, ctypes.POINTER(SelQuadLight)],
     "sel_scene_set_background": [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float],
@@ -312,6 +319,25 @@ def material(**kw) -> SelMaterial:
         else:
             setattr(m, k, v)
     return m
+
+
+def material_from_json(text: str):
+    """sel_material_from_json: (SelMaterial, base-colour texture name or "") from a material JSON document."""
+    m = SelMaterial()
+    tex = ctypes.create_string_buffer(512)
+    check(lib().sel_material_from_json(text.encode("utf-8"), ctypes.byref(m), tex, len(tex)))
+    return m, tex.value.decode("utf-8")
+
+
+def disney_materials_from_json(text: str):
+    """sel_disney_materials_from_json: [(name, SelMaterial, colorMap)] of a Disney-island materials file, each
+    material followed by its assignment names."""
+    data = text.encode("utf-8")
+    n = ctypes.c_uint(0)
+    check(lib().sel_disney_materials_from_json(data, None, 0, ctypes.byref(n)))
+    out = (SelNamedMaterial * max(1, n.value))()
+    check(lib().sel_disney_materials_from_json(data, out, n.value, ctypes.byref(n)))
+    return [(e.name.decode("utf-8"), e.material, e.colorMap.decode("utf-8")) for e in out[:n.value]]
 
 
 def camera(position, look_at, up, fov_degrees, width, height) -> SelCamera:
