@@ -286,6 +286,30 @@ typedef struct SelNamedMaterial {
  * `out`).  Needs no device. */
 int sel_disney_materials_from_json(const char* json, SelNamedMaterial* out, unsigned int capacity, unsigned int* count);
 
+/* One model or subscene instance of a scene file. */
+typedef struct SelSceneInstance {
+    char asset[256];        /* the "model" or "scene" name, NUL-terminated ("" when absent) */
+    float localToWorld[16]; /* "transform": the file's 16 numbers as they stand, rows r0..r3 of the reference's
+                               row-vector matrix (translation in r3), which is the column-major localToWorld that
+                               sel_scene_attach_instance takes; the identity unless an array of 16 numbers */
+} SelSceneInstance;
+
+typedef struct SelSceneDescription {
+    float backgroundIntensity[3];   /* default 1 (sel_scene_set_background) */
+    char ibl[256];                  /* image-based light name, "" when none */
+    unsigned int modelCount;        /* entries of "instances" in the document */
+    unsigned int sceneCount;        /* entries of "scenes" */
+} SelSceneDescription;
+
+/* A scene file (ParseSceneFile, BuildCommon/CSceneBuildProcessor.cpp:32-63): model instances ("instances":
+ * {"model", "transform"}), subscene instances ("scenes": {"scene", "transform"}), "backgroundIntensity" and
+ * "ibl".  The first model_capacity / scene_capacity instances are written (capacities 0 to size the arrays);
+ * the caller builds a scene per model or subscene name and attaches them with sel_scene_attach_instance.
+ * Malformed JSON, or "instances" / "scenes" that are not arrays of objects: SEL_ERR_INVALID_ARGUMENT.  Needs
+ * no device. */
+int sel_scene_description_from_json(const char* json, SelSceneDescription* out, SelSceneInstance* models,
+                                    unsigned int model_capacity, SelSceneInstance* scenes, unsigned int scene_capacity);
+
 /* SceneLight (SceneLib/SceneResource.h) as the lighting code reads it: quad centre, facing direction,
  * full edge vectors x and z, emitted radiance (AreaLighting.cpp:113-153). */
 typedef struct SelQuadLight {

@@ -259,6 +259,15 @@ class SelNamedMaterial(ctypes.Structure):
     _fields_ = [("name", ctypes.c_char * 64), ("material", SelMaterial), ("colorMap", ctypes.c_char * 256)]
 
 
+class SelSceneInstance(ctypes.Structure):
+    _fields_ = [("asset", ctypes.c_char * 256), ("localToWorld", ctypes.c_float * 16)]
+
+
+class SelSceneDescription(ctypes.Structure):
+    _fields_ = [("backgroundIntensity", _f3), ("ibl", ctypes.c_char * 256), ("modelCount", ctypes.c_uint),
+                ("sceneCount", ctypes.c_uint)]
+
+
 class SelQuadLight(ctypes.Structure):
     _fields_ = [("position", _f3), ("direction", _f3), ("x", _f3), ("z", _f3), ("radiance", _f3)]
 
@@ -288,6 +297,8 @@ register_signatures({
     "sel_material_from_json": [ctypes.c_char_p, ctypes.POINTER(SelMaterial), ctypes.c_char_p, _u],
     "sel_disney_materials_from_json": [ctypes.c_char_p, ctypes.POINTER(SelNamedMaterial), _u,
                                        ctypes.POINTER(ctypes.c_uint)],
+    "sel_scene_description_from_json": [ctypes.c_char_p, ctypes.POINTER(SelSceneDescription),
+                                        ctypes.POINTER(SelSceneInstance), _u, ctypes.POINTER(SelSceneInstance), _u],
     "sel_scene_set_material": [_vp, _u, ctypes.POINTER(SelMaterial)],
     "sel_scene_add_quad_light": [_vp, _u, ctypes.POINTER(SelQuadLight)],
     "sel_scene_set_background": [_vp, ctypes.c_float, ctypes.c_float, ctypes.c_float],
@@ -338,6 +349,24 @@ def disney_materials_from_json(text: str):
     out = (SelNamedMaterial * max(1, n.value))()
     check(lib().sel_disney_materials_from_json(data, out, n.value, ctypes.byref(n)))
     return [(e.name.decode("utf-8"), e.material, e.colorMap.decode("utf-8")) for e in out[:n.value]]
+
+
+def scene_description_from_json(text: str) -> dict:
+    """sel_scene_description_from_json: {"models": [(name, 4x4 localToWorld)], "scenes": [...],
+    "background": (r, g, b), "ibl": name}; each matrix is the column-major localToWorld of
+    Scene.attach_instance, returned as a (4, 4) array M with M[:, 3] the translation."""
+    data = text.encode("utf-8")
+    d = SelSceneDescription()
+    check(lib().sel_scene_description_from_json(data, ctypes.byref(d), None, 0, None, 0))
+    models = (SelSceneInstance * max(1, d.modelCount))()
+    scenes = (SelSceneInstance * max(1, d.sceneCount))()
+    check(lib().sel_scene_description_from_json(data, ctypes.byref(d), models, d.modelCount, scenes, d.sceneCount))
+
+    def entries(arr, n):
+        return [(e.asset.decode("utf-8"), np.array(list(e.localToWorld), np.float32).reshape(4, 4).T) for e in arr[:n]]
+
+    return {"models": entries(models, d.modelCount), "scenes": entries(scenes, d.sceneCount),
+            "background": tuple(d.backgroundIntensity), "ibl": d.ibl.decode("utf-8")}
 
 
 def camera(position, look_at, up, fov_degrees, width, height) -> SelCamera:

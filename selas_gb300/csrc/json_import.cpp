@@ -1,10 +1,12 @@
-// Material import from the reference's JSON material files (host C++, no CUDA).
+// Import of the reference's JSON asset descriptions (host C++, no CUDA): materials and scenes.
 //
 // sel_material_from_json restates ImportMaterial (Source/Core/BuildCommon/ImportMaterial.cpp:56-88) followed by
 // BuildMaterial (Source/Core/BuildCommon/BuildModel.cpp:22-64); sel_disney_materials_from_json restates
 // ImportDisneyMaterials (ImportMaterial.cpp:91-146), the Disney-island materials file, with the same
-// BuildMaterial.  The reference reads the files with rapidjson; a small recursive-descent JSON reader of our own
-// takes its place here (objects, arrays, strings with escapes, numbers through strtod, true / false / null).
+// BuildMaterial; sel_scene_description_from_json restates ParseSceneFile
+// (Source/Core/BuildCommon/CSceneBuildProcessor.cpp:32-63).  The reference reads the files with rapidjson; a
+// small recursive-descent JSON reader of our own takes its place here (objects, arrays, strings with escapes,
+// numbers through strtod, true / false / null).
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -319,6 +321,44 @@ bool parse_document(const char* json, JValue& doc) {
     return true;
 }
 
+// Json::ReadMatrix4x4 (UtilityLib/JsonUtilities.cpp:207-252): 16 numbers, rows r0..r3 of the reference's
+// row-vector matrix (translation in r3), else the identity.
+void read_matrix(const JValue& doc, const char* name, float out[16]) {
+    for (int k = 0; k < 16; ++k) out[k] = (k % 5 == 0) ? 1.0f : 0.0f;
+    const JValue* v = doc.member(name);
+    if (!v || v->kind != JValue::kArray || v->items.size() != 16) return;
+    for (const JValue& x : v->items)
+        if (!float_number(x)) return;
+    for (int k = 0; k < 16; ++k) out[k] = float(v->items[size_t(k)].num);
+}
+
+// Json::ReadFixedString: the string when the member is one, else "".
+std::string read_string(const JValue& doc, const char* name) {
+    const JValue* v = doc.member(name);
+    return (v && v->kind == JValue::kString) ? v->str : std::string();
+}
+
+// The "instances" (key "model") or "scenes" (key "scene") array of a scene file.
+int read_instances(const JValue& doc, const char* array, const char* key, SelSceneInstance* out,
+                   unsigned int capacity, unsigned int& count) {
+    count = 0;
+    const JValue* list = doc.member(array);
+    if (!list) return SEL_OK;
+    if (list->kind != JValue::kArray) return fail(SEL_ERR_INVALID_ARGUMENT, std::string(array) + " is not an array");
+    for (const JValue& item : list->items) {
+        if (item.kind != JValue::kObject)
+            return fail(SEL_ERR_INVALID_ARGUMENT, std::string(array) + " holds a non-object");
+        if (count < capacity) {
+            SelSceneInstance& inst = out[count];
+            std::memset(&inst, 0, sizeof(inst));
+            copy_text(read_string(item, key), inst.asset, sizeof(inst.asset));
+            read_matrix(item, "transform", inst.localToWorld);
+        }
+        ++count;
+    }
+    return SEL_OK;
+}
+
 }  // namespace
 }  // namespace sel
 
@@ -396,6 +436,23 @@ int sel_disney_materials_from_json(const char* json, SelNamedMaterial* out, unsi
     }
     *count = unsigned(all.size());
     for (size_t k = 0; k < all.size() && k < capacity; ++k) out[k] = all[k];
+    return SEL_OK;
+}
+
+int sel_scene_description_from_json(const char* json, SelSceneDescription* out, SelSceneInstance* models,
+                                    unsigned int model_capacity, SelSceneInstance* scenes, unsigned int scene_capacity) {
+    if (!json || !out || (model_capacity > 0 && !models) || (scene_capacity > 0 && !scenes))
+        return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    JValue doc;
+    if (!parse_document(json, doc)) return SEL_ERR_INVALID_ARGUMENT;
+    SelSceneDescription d;
+    std::memset(&d, 0, sizeof(d));
+    if (int rc = read_instances(doc, "instances", "model", models, model_capacity, d.modelCount)) return rc;
+    if (int rc = read_instances(doc, "scenes", "scene", scenes, scene_capacity, d.sceneCount)) return rc;
+    const float one[3] = {1.0f, 1.0f, 1.0f};
+    read_float3(doc, "backgroundIntensity", one, d.backgroundIntensity);
+    copy_text(read_string(doc, "ibl"), d.ibl, sizeof(d.ibl));
+    *out = d;
     return SEL_OK;
 }
 

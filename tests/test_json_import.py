@@ -1,8 +1,9 @@
-"""Material import from the reference's JSON material files, host code only (no device): ImportMaterial
+"""Import of the reference's JSON asset descriptions, host code only (no device): ImportMaterial
 (BuildCommon/ImportMaterial.cpp:56-88) and ImportDisneyMaterials (ImportMaterial.cpp:91-146), each followed by
-BuildMaterial (BuildCommon/BuildModel.cpp:22-64).  The documents below are written for these tests in the files'
-format: one material per file with "shaderName", "baseColor" and the scalar attributes, and the Disney-island
-materials file of named materials with "type", "colorMap" and "assignment"."""
+BuildMaterial (BuildCommon/BuildModel.cpp:22-64), and ParseSceneFile (BuildCommon/CSceneBuildProcessor.cpp:32-63).
+The documents below are written for these tests in the files' format: one material per file with "shaderName",
+"baseColor" and the scalar attributes; the Disney-island materials file of named materials with "type",
+"colorMap" and "assignment"; a scene file with model and subscene instances, background and image-based light."""
 import json
 
 import numpy as np
@@ -111,3 +112,29 @@ def ctypes_count(text):
     n = ctypes.c_uint(0)
     sel.check(sel.lib().sel_disney_materials_from_json(text.encode(), None, 0, ctypes.byref(n)))
     return n.value
+
+
+def test_scene_description():
+    # the reference's row-vector matrices: a rotation of 90 degrees about y, then a translation in the last row
+    rot_t = [0, 0, -1, 0,  0, 1, 0, 0,  1, 0, 0, 0,  5, 6, 7, 1]
+    doc = {"instances": [{"model": "Meshes/rock.fbx", "transform": rot_t},
+                         {"model": "Meshes/tree.fbx"},
+                         {"model": "Meshes/rock.fbx", "transform": [1, 2, 3]}],
+           "scenes": [{"scene": "Scenes/island.json", "transform": [2, 0, 0, 0, 0, 2, 0, 0, 0, 0, 2, 0, 0, 0, 0, 1]}],
+           "backgroundIntensity": [0.5, 0.25, 0.125], "ibl": "HDR/sky.hdr"}
+    d = sel.scene_description_from_json(json.dumps(doc))
+    assert [m[0] for m in d["models"]] == ["Meshes/rock.fbx", "Meshes/tree.fbx", "Meshes/rock.fbx"]
+    a = d["models"][0][1]
+    # as a column-vector matrix: the translation in the last column, and p' = A p maps x to -z as p M does
+    np.testing.assert_array_equal(a[:3, 3], [5, 6, 7])
+    np.testing.assert_array_equal(a @ np.float32([1, 0, 0, 1]), np.float32([1, 0, 0, 1]) @ np.float32(rot_t).reshape(4, 4))
+    np.testing.assert_array_equal(d["models"][1][1], np.eye(4))  # no transform: identity
+    np.testing.assert_array_equal(d["models"][2][1], np.eye(4))  # not 16 numbers: identity
+    assert d["scenes"][0][0] == "Scenes/island.json" and d["scenes"][0][1][0, 0] == 2.0
+    assert d["background"] == (0.5, 0.25, 0.125) and d["ibl"] == "HDR/sky.hdr"
+    empty = sel.scene_description_from_json("{}")
+    assert empty["models"] == [] and empty["scenes"] == [] and empty["background"] == (1.0, 1.0, 1.0)
+    assert empty["ibl"] == ""
+    for bad in ('{"instances": {}}', '{"scenes": [1]}', '{"instances": [', '[]'):
+        with pytest.raises(sel.SelError):
+            sel.scene_description_from_json(bad)
