@@ -792,7 +792,7 @@ size_t pt_state_block_bytes(uint32_t paths) {
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
                            bool instanced, bool texture, bool ray_sort, uint64_t batch_paths) {
-    const bool face_order = sort && texture && batch_paths >= kFaceOrderPaths;
+    const bool face_order = sort && texture && !instanced && batch_paths >= kFaceOrderPaths;
     // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
     // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
     const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;

@@ -135,8 +135,9 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
                            uint64_t batch_paths = 0);
 // `ray_sort`: order each bounce's continuing rays by (direction bin, origin cell) before tracing them.
 // `texture`: a job's hits may need Ptex (see pt_scene_textured); the Ptex kernel runs only then.
-// `batch_paths`: paths a batch holds; with `sort` and `texture`, batches of kFaceOrderPaths or more order the
-// textured hits by Ptex face as well (the face order's radix passes cost more than it saves on smaller batches).
+// `batch_paths`: paths a batch holds; with `sort` and `texture`, batches of kFaceOrderPaths or more of flat scenes
+// order the textured hits by Ptex face as well (the face order's radix passes cost more than it saves on smaller
+// batches, and on the instanced terrain, whose 4 x 4-texel faces filter cheaply: 110.6 against 114.8 M paths/s).
 bool pt_scene_textured(const PtScene& sc);
 
 // Batch size from which textured hits are ordered by Ptex face (room at 1280 x 720, 16 spp: 1M paths per batch
