@@ -770,3 +770,150 @@ def smooth_spheres(count: int = 4, level: int = 3, seed: int = 0x5E1A5106) -> Re
                  radiance=(30.0, 28.0, 25.0))
     cam = dict(position=(0.0, 3.0, -10.0), look_at=(0.0, 1.2, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=55.0)
     return RenderScene(g, mats, [(0, light)], (0.05, 0.05, 0.08), cam, {}, attrs=attrs)
+
+
+# ---------------------------------------------------------------------------------------------------
+# Scene files: the reference's scene JSON (model and subscene instances with transforms, background) with models
+# as Wavefront OBJ text and materials as the reference's material JSON files.  The reference cooks FBX / OBJ
+# models through assimp (BuildCommon/ImportModel.cpp) into binary model resources; the OBJ reader here stands in
+# for that import for OBJ content.
+# ---------------------------------------------------------------------------------------------------
+def load_obj(text: str):
+    """Wavefront OBJ text -> list of (material name, vertices (n, 3) f32, indices (m, 3) u32, normals (n, 3) or
+    None), one entry per `usemtl` group in order of first use ("" before any).  Faces may be polygons (fanned
+    from their first corner) with v, v/vt, v//vn or v/vt/vn corners and negative (relative) indices; a group's
+    vertices are its distinct (position, normal) pairs."""
+    pos, nrm = [], []
+    groups = {}
+    order = []
+    cur = ""
+
+    def index(tok, count):
+        k = int(tok)
+        return k - 1 if k > 0 else count + k
+
+    for line in text.splitlines():
+        parts = line.split("#", 1)[0].split()
+        if not parts:
+            continue
+        tag = parts[0]
+        if tag == "v":
+            pos.append([float(x) for x in parts[1:4]])
+        elif tag == "vn":
+            nrm.append([float(x) for x in parts[1:4]])
+        elif tag == "usemtl":
+            cur = parts[1] if len(parts) > 1 else ""
+        elif tag == "f":
+            corners = []
+            for c in parts[1:]:
+                f = c.split("/")
+                vi = index(f[0], len(pos))
+                ni = index(f[2], len(nrm)) if len(f) > 2 and f[2] else -1
+                if not 0 <= vi < len(pos) or not -1 <= ni < len(nrm):
+                    raise ValueError(f"face corner {c!r} indexes past the vertices read so far")
+                corners.append((vi, ni))
+            if len(corners) < 3:
+                raise ValueError("a face needs at least three corners")
+            if cur not in groups:
+                groups[cur] = ({}, [])
+                order.append(cur)
+            remap, tris = groups[cur]
+            ids = [remap.setdefault(key, len(remap)) for key in corners]
+            for k in range(1, len(ids) - 1):
+                tris.append((ids[0], ids[k], ids[k + 1]))
+    pos_a = np.asarray(pos, np.float32).reshape(-1, 3)
+    nrm_a = np.asarray(nrm, np.float32).reshape(-1, 3)
+    out = []
+    for name in order:
+        remap, tris = groups[name]
+        keys = sorted(remap, key=remap.get)
+        v = pos_a[[k[0] for k in keys]]
+        has_n = all(k[1] >= 0 for k in keys)
+        n = nrm_a[[k[1] for k in keys]] if has_n and keys else None
+        out.append((name, np.ascontiguousarray(v), np.asarray(tris, np.uint32).reshape(-1, 3), n))
+    return out
+
+
+def _material_fields(m) -> dict:
+    out = {}
+    for name, _ in type(m)._fields_:
+        v = getattr(m, name)
+        out[name] = list(v) if hasattr(v, "__len__") else v
+    return out
+
+
+def load_scene_file(path, camera: dict = None, lights: list = (), materials_dir=None) -> "InstancedRenderScene":
+    """A scene JSON file (ParseSceneFile, BuildCommon/CSceneBuildProcessor.cpp:32-63) as an InstancedRenderScene:
+    part 0 is the world (the given lights and camera, the file's backgroundIntensity), each distinct model an
+    instanced part (its OBJ `usemtl` groups geomIDs 0, 1, ... with the material `<materials_dir>/<name>.json`
+    when that file exists, else the default material; `usesPtex` is cleared, since no Ptex texels come with an
+    OBJ), and each subscene file a part instancing its own models (one level of subscenes).  Asset paths are read
+    relative to the scene file's folder; the image-based light the file names is not loaded.  Without a camera,
+    one looks at the instanced bounds from outside them."""
+    import pathlib
+
+    import selas_gb300 as sel
+
+    path = pathlib.Path(path)
+    mat_dir = pathlib.Path(materials_dir) if materials_dir else path.parent
+    parts, instances, index_of = [None], [[]], {}
+
+    def model_part(asset):
+        key = ("model", asset)
+        if key in index_of:
+            return index_of[key]
+        geometry, mats, attrs = TriangleScene(), {}, {}
+        for gid, (name, v, idx, n) in enumerate(load_obj((path.parent / asset).read_text())):
+            geometry.add(gid, v, idx)
+            f = mat_dir / f"{name}.json"
+            if name and f.exists():
+                fields = _material_fields(sel.material_from_json(f.read_text())[0])
+                fields["usesPtex"] = 0
+                mats[gid] = fields
+            if n is not None:
+                attrs[gid] = {"normals": n}
+        parts.append(RenderScene(geometry, mats, [], (0.0, 0.0, 0.0), {}, {}, None, attrs or None))
+        instances.append([])
+        index_of[key] = len(parts) - 1
+        return index_of[key]
+
+    def scene_instances(desc, owner, allow_subscenes):
+        next_id = 1
+        for asset, m in desc["models"]:
+            instances[owner].append((next_id, model_part(asset), m))
+            next_id += 1
+        for asset, m in desc["scenes"]:
+            if not allow_subscenes:
+                raise ValueError(f"{asset}: subscenes of subscenes exceed the two instance levels")
+            key = ("scene", asset)
+            if key not in index_of:
+                sub = sel.scene_description_from_json((path.parent / asset).read_text())
+                parts.append(RenderScene(TriangleScene(), {}, [], (0.0, 0.0, 0.0), {}))
+                instances.append([])
+                index_of[key] = len(parts) - 1
+                scene_instances(sub, index_of[key], False)
+            instances[owner].append((next_id, index_of[key], m))
+            next_id += 1
+
+    desc = sel.scene_description_from_json(path.read_text())
+    scene_instances(desc, 0, True)
+    if camera is None:
+        corners = []
+
+        def collect(i, xform):
+            p = parts[i]
+            if p is not None and p.geometry.meshes:  # part 0, the world, holds no meshes
+                lo, hi = p.geometry.bounds()
+                box = np.array([[x, y, z, 1.0] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])])
+                corners.append((xform @ box.T).T[:, :3])
+            for _, j, m in instances[i]:
+                collect(j, xform @ np.asarray(m, np.float64))
+
+        collect(0, np.eye(4))
+        pts = np.concatenate(corners) if corners else np.zeros((1, 3))
+        lo, hi = pts.min(axis=0), pts.max(axis=0)
+        centre, radius = (lo + hi) / 2, max(float(np.linalg.norm(hi - lo)) / 2, 1e-3)
+        camera = dict(position=tuple(centre + np.array([0.0, 0.5, -2.5]) * radius), look_at=tuple(centre),
+                      up=(0.0, 1.0, 0.0), fov_degrees=45.0)
+    parts[0] = RenderScene(TriangleScene(), {}, list(lights), tuple(desc["background"]), camera)
+    return InstancedRenderScene(parts, instances)

@@ -138,3 +138,113 @@ def test_scene_description():
     for bad in ('{"instances": {}}', '{"scenes": [1]}', '{"instances": [', '[]'):
         with pytest.raises(sel.SelError):
             sel.scene_description_from_json(bad)
+
+
+CUBE_OBJ = """# a cube, quads with normals, two material groups, relative indices on the last faces
+v -1 -1 -1
+v 1 -1 -1
+v 1 1 -1
+v -1 1 -1
+v -1 -1 1
+v 1 -1 1
+v 1 1 1
+v -1 1 1
+vn 0 0 -1
+vn 0 0 1
+vn -1 0 0
+vn 1 0 0
+vn 0 -1 0
+vn 0 1 0
+usemtl Red
+f 1//1 4//1 3//1 2//1
+f 5//2 6//2 7//2 8//2
+f 1//3 5//3 8//3 4//3
+f 2//4 3//4 7//4 6//4
+usemtl Gold
+f 1//5 2//5 6//5 5//5
+f -5//6 -1//6 -2//6 -6//6
+"""
+
+FLOOR_OBJ = """v -20 0 -20
+v 20 0 -20
+v 20 0 20
+v -20 0 20
+vt 0 0
+usemtl Floor
+f 1/1 4/1 3/1
+f 1/1 3/1 2/1
+"""
+
+
+def test_load_obj_groups_fans_and_indices():
+    from selas_gb300 import scenes
+    groups = scenes.load_obj(CUBE_OBJ)
+    assert [g[0] for g in groups] == ["Red", "Gold"]
+    red, gold = groups[0], groups[1]
+    assert red[2].shape == (8, 3) and gold[2].shape == (4, 3)  # quads fanned into two triangles each
+    assert red[1].shape == (16, 3) and red[3].shape == (16, 3)  # distinct (position, normal) corners
+    # the relative indices of the last face name the top (y = 1) corners with the +y normal
+    top = gold[1][gold[2][2:].reshape(-1)]
+    assert np.all(top[:, 1] == 1.0) and np.all(gold[3][gold[2][2:].reshape(-1)] == [0, 1, 0])
+    floor = scenes.load_obj(FLOOR_OBJ)
+    assert floor[0][0] == "Floor" and floor[0][3] is None and floor[0][2].shape == (2, 3)
+    with pytest.raises(ValueError):
+        scenes.load_obj("v 0 0 0\nf 1 2 3\n")
+
+
+def _write_scene(tmp_path):
+    (tmp_path / "cube.obj").write_text(CUBE_OBJ)
+    (tmp_path / "floor.obj").write_text(FLOOR_OBJ)
+    (tmp_path / "Red.json").write_text(json.dumps({"shaderName": "DisneySolid", "baseColor": [0.8, 0.1, 0.1],
+                                                   "roughness": 0.6, "metallic": 0.0}))
+    (tmp_path / "Gold.json").write_text(json.dumps({"shaderName": "DisneySolid", "baseColor": [0.9, 0.7, 0.3],
+                                                    "roughness": 0.3, "metallic": 1.0, "usesPtex": True}))
+    c, s = np.cos(0.6), np.sin(0.6)
+    rot = [c, 0, -s, 0, 0, 1, 0, 0, s, 0, c, 0, 0, 0, 0, 1]  # row-vector matrices, translation in the last row
+    doc = {"instances": [{"model": "floor.obj"},
+                         {"model": "cube.obj", "transform": rot[:12] + [-3, 1, 0, 1]},
+                         {"model": "cube.obj", "transform": [0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 0.5, 0, 2, 0.5, 1, 1]}],
+           "backgroundIntensity": [0.2, 0.3, 0.4]}
+    (tmp_path / "scene.json").write_text(json.dumps(doc))
+    light = dict(position=(0.0, 8.0, 0.0), direction=(0.0, -1.0, 0.0), x=(4.0, 0.0, 0.0), z=(0.0, 0.0, 4.0),
+                 radiance=(20.0, 20.0, 18.0))
+    return tmp_path / "scene.json", [(0, light)]
+
+
+def test_load_scene_file(tmp_path):
+    from selas_gb300 import scenes
+    path, lights = _write_scene(tmp_path)
+    s = scenes.load_scene_file(path, lights=lights)
+    assert len(s.parts) == 3  # world, floor, cube (shared by both of its instances)
+    world = s.instances[0]
+    assert [(i, p) for i, p, _ in world] == [(1, 1), (2, 2), (3, 2)]
+    np.testing.assert_allclose(world[1][2][:3, 3], [-3, 1, 0])
+    np.testing.assert_allclose(world[2][2][:3, :3], 0.5 * np.eye(3))
+    cube = s.parts[2]
+    assert [m[0] for m in cube.geometry.meshes] == [0, 1] and set(cube.attrs) == {0, 1}
+    assert cube.materials[0]["metallic"] == 0.0 and cube.materials[1]["metallic"] == 1.0
+    assert cube.materials[1]["usesPtex"] == 0  # no texels come with an OBJ
+    assert s.parts[1].materials == {}  # Floor.json does not exist: the default material
+    assert s.parts[0].background == pytest.approx((0.2, 0.3, 0.4)) and s.parts[0].lights == lights
+    assert set(s.camera) == {"position", "look_at", "up", "fov_degrees"}
+
+
+@pytest.mark.gpu
+def test_gpu_scene_file_renders_the_oracles_image(device, tmp_path):
+    """A scene file with OBJ models and JSON materials, built through the instancing API: the GPU traces the
+    oracle's paths on the same streams."""
+    import selas_gb300 as sel
+    import oracle
+    from selas_gb300 import scenes
+    path, lights = _write_scene(tmp_path)
+    s = scenes.load_scene_file(path, lights=lights)
+    built = s.build(sel, device)
+    gpu = built[0].pt_generate_image(s.sel_camera(sel, 48, 36), sel.pt_settings(8, 6, 0x5E1A5000)).astype(np.float64)
+    s.release(built)
+    cpu = oracle.graph_render(s, 48, 36, 0, 8, seed=0x5E1A5000, max_bounces=6) / 8.0
+    for layer in (0, 1):
+        g, c = gpu[layer], cpu[layer]
+        rel = np.abs(g - c) / np.maximum(np.abs(c), 1e-3 * c.mean())
+        assert np.median(rel) < 1e-4, np.median(rel)
+        assert (rel < 1e-2).mean() > 0.97
+    assert gpu[1].mean() > 0
