@@ -848,8 +848,9 @@ def load_scene_file(path, camera: dict = None, lights: list = (), materials_dir=
     instanced part (its OBJ `usemtl` groups geomIDs 0, 1, ... with the material `<materials_dir>/<name>.json`
     when that file exists, else the default material; `usesPtex` is cleared, since no Ptex texels come with an
     OBJ), and each subscene file a part instancing its own models (one level of subscenes).  Asset paths are read
-    relative to the scene file's folder; the image-based light the file names is not loaded.  Without a camera,
-    one looks at the instanced bounds from outside them."""
+    relative to the scene file's folder; the image-based light the file names (a .hdr image or a dual-IBL JSON
+    file, `load_ibl`) lights the world when the file exists.  Without a camera, one looks at the instanced
+    bounds from outside them."""
     import pathlib
 
     import selas_gb300 as sel
@@ -915,5 +916,82 @@ def load_scene_file(path, camera: dict = None, lights: list = (), materials_dir=
         centre, radius = (lo + hi) / 2, max(float(np.linalg.norm(hi - lo)) / 2, 1e-3)
         camera = dict(position=tuple(centre + np.array([0.0, 0.5, -2.5]) * radius), look_at=tuple(centre),
                       up=(0.0, 1.0, 0.0), fov_degrees=45.0)
-    parts[0] = RenderScene(TriangleScene(), {}, list(lights), tuple(desc["background"]), camera)
+    ibl = None
+    if desc["ibl"] and (path.parent / desc["ibl"]).exists():
+        ibl = load_ibl(path.parent / desc["ibl"])
+    parts[0] = RenderScene(TriangleScene(), {}, list(lights), tuple(desc["background"]), camera, {}, ibl)
     return InstancedRenderScene(parts, instances)
+
+
+def read_hdr(data: bytes) -> np.ndarray:
+    """Radiance RGBE (.hdr) image bytes -> float32 (height, width, 3), rows top to bottom (the format of Greg Ward's
+    Radiance; the reference reads it through stb_image, BuildImageBasedLight.cpp:124-150).  Flat and new-style
+    run-length scanlines; `-Y h +X w` orientation only."""
+    pos = 0
+
+    def line():
+        nonlocal pos
+        end = data.index(b"\n", pos)
+        s = data[pos:end].decode("ascii", "replace")
+        pos = end + 1
+        return s
+
+    if not line().startswith("#?"):
+        raise ValueError("not a Radiance HDR file")
+    while True:
+        s = line()
+        if s == "":
+            break
+        if s.startswith("FORMAT=") and s != "FORMAT=32-bit_rle_rgbe":
+            raise ValueError(f"unsupported {s}")
+    res = line().split()
+    if len(res) != 4 or res[0] != "-Y" or res[2] != "+X":
+        raise ValueError("only -Y height +X width images are read")
+    h, w = int(res[1]), int(res[3])
+    rgbe = np.zeros((h, w, 4), np.uint8)
+    for y in range(h):
+        if 8 <= w < 32768 and data[pos] == 2 and data[pos + 1] == 2 and (data[pos + 2] << 8 | data[pos + 3]) == w:
+            pos += 4
+            for c in range(4):  # one run-length coded channel after the other
+                x = 0
+                while x < w:
+                    n = data[pos]
+                    pos += 1
+                    if n > 128:
+                        n -= 128
+                        if x + n > w:
+                            raise ValueError("run past the end of a scanline")
+                        rgbe[y, x:x + n, c] = data[pos]
+                        pos += 1
+                    else:
+                        if n == 0 or x + n > w:
+                            raise ValueError("bad count in a scanline")
+                        rgbe[y, x:x + n, c] = np.frombuffer(data, np.uint8, n, pos)
+                        pos += n
+                    x += n
+        else:
+            rgbe[y] = np.frombuffer(data, np.uint8, 4 * w, pos).reshape(w, 4)
+            pos += 4 * w
+    e = rgbe[..., 3].astype(np.int32)
+    scale = np.where(e > 0, np.ldexp(np.float32(1.0), e - (128 + 8)), 0.0).astype(np.float32)
+    return rgbe[..., :3].astype(np.float32) * scale[..., None]
+
+
+def load_ibl(path) -> dict:
+    """An image-based light asset as RenderScene.ibl takes it: a .hdr image (ImportImageBasedLight,
+    BuildImageBasedLight.cpp:155-178: no miss image, no rotation) or a dual-IBL JSON file {"light", "miss",
+    "rotationDegrees", "exposure"} (ImageBasedLightBuildProcessor.cpp:52-119: rotation in radians, exposure scale
+    2^exposure), its images read relative to the file."""
+    import json
+    import pathlib
+
+    path = pathlib.Path(path)
+    if path.suffix.lower() == ".json":
+        d = json.loads(path.read_text())
+        if "light" not in d or "miss" not in d:
+            raise ValueError(f"{path}: a dual IBL names a light and a miss image")
+        return dict(light=read_hdr((path.parent / d["light"]).read_bytes()),
+                    miss=read_hdr((path.parent / d["miss"]).read_bytes()),
+                    rotation=float(np.float32(d.get("rotationDegrees", 0.0)) * np.float32(np.pi / 180.0)),
+                    exposure=float(np.float32(2.0) ** np.float32(d.get("exposure", 0.0))))
+    return dict(light=read_hdr(path.read_bytes()), miss=None, rotation=0.0, exposure=1.0)

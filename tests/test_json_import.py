@@ -248,3 +248,77 @@ def test_gpu_scene_file_renders_the_oracles_image(device, tmp_path):
         assert np.median(rel) < 1e-4, np.median(rel)
         assert (rel < 1e-2).mean() > 0.97
     assert gpu[1].mean() > 0
+
+
+def _rgbe(img):
+    """float (h, w, 3) -> RGBE bytes (h, w, 4), the format's shared-exponent encoding."""
+    m = img.max(axis=-1)
+    e = np.where(m > 1e-32, np.floor(np.log2(np.maximum(m, 1e-32))) + 1, 0).astype(np.int32)
+    scale = np.where(m > 1e-32, np.ldexp(1.0, 8 - e), 0.0)
+    out = np.zeros(img.shape[:2] + (4,), np.uint8)
+    out[..., :3] = np.clip(np.floor(img * scale[..., None]), 0, 255).astype(np.uint8)
+    out[..., 3] = np.where(m > 1e-32, e + 128, 0).astype(np.uint8)
+    return out
+
+
+def _hdr_bytes(img, rle):
+    h, w = img.shape[:2]
+    rgbe = _rgbe(img)
+    out = bytearray(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        if not rle:
+            out += rgbe[y].tobytes()
+            continue
+        out += bytes([2, 2, w >> 8, w & 255])
+        for c in range(4):
+            row, x = rgbe[y, :, c], 0
+            while x < w:
+                run = 1
+                while x + run < w and run < 127 and row[x + run] == row[x]:
+                    run += 1
+                if run >= 3:
+                    out += bytes([128 + run, row[x]])
+                    x += run
+                else:
+                    n = min(w - x, 128)
+                    out += bytes([n]) + row[x:x + n].tobytes()
+                    x += n
+    return bytes(out)
+
+
+@pytest.mark.parametrize("rle", [False, True])
+def test_read_hdr(rle):
+    from selas_gb300 import scenes
+    rng = np.random.default_rng(3)
+    img = rng.uniform(0.0, 4.0, (5, 24, 3)).astype(np.float32)
+    img[1, 3:12] = [0.5, 0.25, 2.0]  # runs
+    img[2, 0] = 0.0
+    got = scenes.read_hdr(_hdr_bytes(img, rle))
+    want = _rgbe(img)
+    e = want[..., 3].astype(np.int32)
+    ref = want[..., :3] * np.where(e > 0, np.ldexp(1.0, e - 136), 0.0)[..., None]
+    np.testing.assert_array_equal(got, ref.astype(np.float32))
+    # the shared exponent keeps each component to 8 bits of the pixel's largest one
+    assert np.all(np.abs(got - img) <= img.max(axis=-1, keepdims=True) * 2 ** -7 + 1e-6)
+    with pytest.raises(ValueError):
+        scenes.read_hdr(b"P6\n")
+
+
+def test_scene_file_with_dual_ibl(tmp_path):
+    from selas_gb300 import scenes
+    path, lights = _write_scene(tmp_path)
+    sky = np.full((8, 16, 3), 0.5, np.float32)
+    sky[:4] = [1.0, 1.5, 2.0]
+    (tmp_path / "sky.hdr").write_bytes(_hdr_bytes(sky, True))
+    (tmp_path / "miss.hdr").write_bytes(_hdr_bytes(sky[::2, ::2].copy(), False))
+    (tmp_path / "sky.json").write_text(json.dumps({"light": "sky.hdr", "miss": "miss.hdr", "rotationDegrees": 90,
+                                                   "exposure": 1.5}))
+    doc = json.loads(path.read_text())
+    doc["ibl"] = "sky.json"
+    path.write_text(json.dumps(doc))
+    ibl = scenes.load_scene_file(path, lights=lights).parts[0].ibl
+    assert np.all(np.abs(ibl["light"] - sky) <= sky.max(axis=-1, keepdims=True) * 2 ** -7)
+    assert ibl["miss"].shape == (4, 8, 3)
+    assert ibl["rotation"] == pytest.approx(np.pi / 2) and ibl["exposure"] == pytest.approx(2 ** 1.5)
+    single = scenes.load_ibl(tmp_path / "sky.hdr")
+    assert single["miss"] is None and single["rotation"] == 0.0 and single["exposure"] == 1.0
