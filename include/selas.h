@@ -336,6 +336,16 @@ int sel_scene_set_background(SelScene scene, float r, float g, float b);
 int sel_scene_set_ibl(SelScene scene, const float* rgb, unsigned int width, unsigned int height, const float* miss_rgb,
                       unsigned int miss_width, unsigned int miss_height, float rotationRadians, float exposureScale);
 
+/* A 2D base-colour image for geometry geomID, the reference's non-Ptex texture path (CalculateSurfaceParams,
+ * SurfaceParameters.cpp:186-213): a material without Ptex takes its base colour from the image at the hit's uvs
+ * (vertex attribute slot 2 as (u, v) pairs, sel_scene_set_vertex_attribute; (0, 0) without them), filtered by
+ * TextureFiltering::Triangle at mip level 0 (bilinear, texel centres at (i + 0.5) / size, Repeat wrapping by the
+ * signed remainder, TextureFiltering.h:30-100), converted from sRGB to linear (SrgbToLinearPrecise) and then,
+ * as every base colour, raised to 2.2.  width x height texels of `channels` floats (1: grey, 3: RGB, 4: RGBA,
+ * alpha unused), row 0 at v = 0.  width or height 0 removes the image.  Applies from the next render. */
+int sel_scene_set_texture(SelScene scene, unsigned int geomID, const float* data, unsigned int width,
+                          unsigned int height, unsigned int channels);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Ptex per-face textures.                                                                           */
 /* ------------------------------------------------------------------------------------------------ */

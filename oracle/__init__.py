@@ -44,7 +44,8 @@ def lib() -> ctypes.CDLL:
                                 ctypes.c_float, ctypes.c_float], None),
             "oracle_ibl_sample": ([_vp, _i, _vp, _vp], None),
             "oracle_ibl_pdf": ([_vp, _i, _vp], None),
-            "oracle_set_attributes": ([_i64, _vp, _vp, _vp], None),
+            "oracle_set_attributes": ([_i64, _vp, _vp, _vp, _vp], None),
+            "oracle_set_textures": ([ctypes.c_int, _vp, _vp, _vp, _vp], None),
             "oracle_instanced_query": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _i64, _i, _i],
                                        None),
             "oracle_affine_inverse": ([_vp, _vp], _i),
@@ -157,10 +158,37 @@ def set_attributes(parts):
     n = np.ascontiguousarray(np.concatenate([s[0] for s in soups]))
     t = np.ascontiguousarray(np.concatenate([s[1] for s in soups]))
     f = np.ascontiguousarray(np.concatenate([s[2] for s in soups]))
+    uv = np.ascontiguousarray(np.concatenate([s[3] for s in soups]))
     if not f.any():
-        lib().oracle_set_attributes(0, None, None, None)
+        lib().oracle_set_attributes(0, None, None, None, None)
+    else:
+        lib().oracle_set_attributes(f.shape[0], _p(n), _p(t), _p(f), _p(uv))
+    set_textures(parts)
+
+
+def set_textures(parts):
+    """2D base-colour images of the next oracle renders: those of the RenderScenes `parts` (scene index = position),
+    as RGBA (one channel: grey, three: alpha 1)."""
+    keys, dims, offs, data, off = [], [], [], [], 0
+    for si, p in enumerate(parts):
+        for gid, img in sorted((getattr(p, "textures", None) or {}).items()):
+            a = np.asarray(img, np.float32)
+            a = a.reshape(a.shape[0], a.shape[1], -1)
+            rgba = np.ones(a.shape[:2] + (4,), np.float32)
+            rgba[..., :3] = a[..., :1] if a.shape[2] == 1 else a[..., :3]
+            if a.shape[2] == 4:
+                rgba[..., 3] = a[..., 3]
+            keys += [si, gid]
+            dims += [a.shape[1], a.shape[0]]
+            offs.append(off)
+            data.append(rgba.reshape(-1))
+            off += rgba.size
+    if not keys:
+        lib().oracle_set_textures(0, None, None, None, None)
         return
-    lib().oracle_set_attributes(f.shape[0], _p(n), _p(t), _p(f))
+    k, d = np.asarray(keys, np.uint32), np.asarray(dims, np.uint32)
+    o, r = np.asarray(offs, np.int64), np.ascontiguousarray(np.concatenate(data))
+    lib().oracle_set_textures(len(offs), _p(k), _p(d), _p(o), _p(r))
 
 
 def ibl_sample(ibl, r):

@@ -15,4 +15,9 @@ bool index(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene
 void frame(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, const float ng[3], float n[3], float t[3],
            float b[3]);
 
+// Base colour of the 2D image bound to mesh (scene, geom) at a hit (the reference's non-Ptex texture path,
+// SurfaceParameters.cpp:186-213 with TextureFiltering::Triangle at level 0, Repeat wrapping, sRGB to linear): uvs
+// from attribute slot 2 ((0, 0) without them).  False when no image is bound.
+bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]);
+
 }  // namespace ora

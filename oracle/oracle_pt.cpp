@@ -345,7 +345,7 @@ struct Ibl {
 // Vertex attributes of the soup (oracle_set_attributes): per triangle, the three corners' shading normals and
 // tangents and flags (1 normals, 2 tangents); `first` maps (scene << 32 | geomID) to the mesh's first triangle.
 struct Attrs {
-    std::vector<float> normals, tangents;
+    std::vector<float> normals, tangents, uvs;  // uvs: (u, v) of the three corners, flag 4
     std::vector<uint8_t> flags;
     std::map<uint64_t, int64_t> first;
 };
@@ -443,6 +443,7 @@ void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) 
     s.t = t; s.n = n; s.b = b;
     float base[3] = {m.base[0], m.base[1], m.base[2]};
     if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    else ora::tex2d(sc.graph ? h.scene : 0u, h.geom, h.prim, h.u, h.v, base);
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
     s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
     s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
@@ -801,6 +802,12 @@ static Attrs g_attrs;
 
 // Maps each mesh of a soup (triangles of one (scene, geomID) are contiguous, primID counting from 0) to its first
 // triangle.
+struct Tex2D {
+    int w = 0, h = 0;
+    std::vector<float> rgba;
+};
+static std::map<uint64_t, Tex2D> g_tex2d;
+
 static void index_attrs(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene, int64_t ntri) {
     g_attrs.first.clear();
     for (int64_t i = 0; i < ntri; ++i)
@@ -989,17 +996,64 @@ extern "C" {
 
 // Vertex attributes of the soup of the next renders (n triangles in the soup's order): corner normals (n x 9),
 // corner tangents (n x 12) and flags (1 normals, 2 tangents); n = 0 clears them.
-void oracle_set_attributes(int64_t n, const float* normals, const float* tangents, const uint8_t* flags) {
+void oracle_set_attributes(int64_t n, const float* normals, const float* tangents, const uint8_t* flags,
+                           const float* uvs) {
     g_attrs = Attrs();
     if (n <= 0) return;
     g_attrs.normals.assign(normals, normals + 9 * n);
     g_attrs.tangents.assign(tangents, tangents + 12 * n);
     g_attrs.flags.assign(flags, flags + n);
+    if (uvs) g_attrs.uvs.assign(uvs, uvs + 6 * n);
+}
+
+// 2D base-colour images of the following renders: n images, image k bound to (scene, geom) = keys[2k], keys[2k+1],
+// dims[2k] x dims[2k+1] RGBA texels from rgba + offsets[k].
+void oracle_set_textures(int n, const uint32_t* keys, const uint32_t* dims, const int64_t* offsets, const float* rgba) {
+    g_tex2d.clear();
+    for (int k = 0; k < n; ++k) {
+        Tex2D& t = g_tex2d[(uint64_t(keys[2 * k]) << 32) | keys[2 * k + 1]];
+        t.w = int(dims[2 * k]);
+        t.h = int(dims[2 * k + 1]);
+        t.rgba.assign(rgba + offsets[k], rgba + offsets[k] + size_t(t.w) * t.h * 4);
+    }
 }
 
 }  // extern "C"
 
 namespace ora {
+
+bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]) {
+    const auto it = g_tex2d.find((uint64_t(scene) << 32) | geom);
+    if (it == g_tex2d.end() || it->second.w <= 0 || it->second.h <= 0) return false;
+    const Tex2D& t = it->second;
+    float su = 0.0f, sv = 0.0f;
+    const auto f = g_attrs.first.find((uint64_t(scene) << 32) | geom);
+    if (f != g_attrs.first.end() && !g_attrs.uvs.empty()) {
+        const int64_t tri = f->second + prim;
+        if ((g_attrs.flags[size_t(tri)] & 4u) != 0) {
+            const float* c = &g_attrs.uvs[size_t(tri) * 6];
+            const float w = 1.0f - u - v;
+            su = w * c[0] + u * c[2] + v * c[4];
+            sv = w * c[1] + u * c[3] + v * c[5];
+        }
+    }
+    auto texel = [&](int s, int tt, int ch) {
+        s = s % t.w;
+        tt = tt % t.h;
+        int i = tt * t.w + s;
+        i = i < 0 ? 0 : (i > t.w * t.h - 1 ? t.w * t.h - 1 : i);
+        return t.rgba[size_t(i) * 4 + ch];
+    };
+    const float s = su * float(t.w) - 0.5f, tt = sv * float(t.h) - 0.5f;
+    const int s0 = int(std::floor(s)), t0 = int(std::floor(tt));
+    const float ds = s - float(s0), dt = tt - float(t0);
+    for (int c = 0; c < 3; ++c) {
+        const float x = (1.0f - ds) * (1.0f - dt) * texel(s0, t0, c) + (1.0f - ds) * dt * texel(s0, t0 + 1, c) +
+                        ds * (1.0f - dt) * texel(s0 + 1, t0, c) + ds * dt * texel(s0 + 1, t0 + 1, c);
+        rgb[c] = x <= 0.04045f ? x / 12.92f : std::pow((x + 0.055f) / (1.0f + 0.055f), 2.4f);
+    }
+    return true;
+}
 
 bool env_present() { return g_ibl.w != 0; }
 

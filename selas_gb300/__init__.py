@@ -183,6 +183,15 @@ class Scene:
         a = a.reshape(a.shape[0], -1)
         check(lib().sel_scene_set_vertex_attribute(self.handle, geom_id, slot, _ptr(a), a.shape[0], a.shape[1]))
 
+    def set_texture(self, geom_id: int, image) -> None:
+        """2D base-colour image of a mesh, (h, w), (h, w, 1), (h, w, 3) or (h, w, 4) floats (None: remove)."""
+        if image is None:
+            check(lib().sel_scene_set_texture(self.handle, geom_id, None, 0, 0, 3))
+            return
+        a = np.asarray(image, np.float32)
+        a = np.ascontiguousarray(a.reshape(a.shape[0], a.shape[1], -1))
+        check(lib().sel_scene_set_texture(self.handle, geom_id, _ptr(a), a.shape[1], a.shape[0], a.shape[2]))
+
     def interpolate0(self, geom_id: int, prim_id: int, u: float, v: float, slot: int, count: int) -> np.ndarray:
         out = np.zeros(count, np.float32)
         check(lib().sel_interpolate0(self.handle, geom_id, prim_id, u, v, slot, _ptr(out), count))
@@ -295,6 +304,7 @@ register_signatures({
     "sel_bsdf_sample_device": [_vp, _vp, _vp, _u, _vp, _vp],
     "sel_material_defaults": [ctypes.POINTER(SelMaterial)],
     "sel_material_from_json": [ctypes.c_char_p, ctypes.POINTER(SelMaterial), ctypes.c_char_p, _u],
+    "sel_scene_set_texture": [_vp, _u, _vp, _u, _u, _u],
     "sel_disney_materials_from_json": [ctypes.c_char_p, ctypes.POINTER(SelNamedMaterial), _u,
                                        ctypes.POINTER(ctypes.c_uint)],
     "sel_scene_description_from_json": [ctypes.c_char_p, ctypes.POINTER(SelSceneDescription),

@@ -524,7 +524,7 @@ int sel_scene_release(SelScene scene) {
     for (auto& r : scene->referenced) --r.first->instanced_by;
     for (void* p : {scene->d_nodes, scene->d_tris, scene->scratch, scene->d_materials, scene->d_lights,
                     scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
-                    scene->vcm_block, scene->d_insts, scene->d_view, scene->d_ibl, scene->d_attrs})
+                    scene->vcm_block, scene->d_insts, scene->d_view, scene->d_ibl, scene->d_attrs, scene->d_textures})
         if (p) cudaFree(p);
     delete scene;
     return SEL_OK;

@@ -71,6 +71,13 @@ struct SelSceneTy {
         std::vector<uint16_t> texels;
     };
     std::vector<PtexBinding> ptex;
+    struct TextureBinding {  // sel_scene_set_texture: a 2D base-colour image, RGBA floats
+        uint32_t geomID, width, height;
+        std::vector<float> rgba;
+    };
+    std::vector<TextureBinding> textures;
+    void* d_textures = nullptr;  // their texels, one block
+    bool tex2d = false;          // a material samples one (set by the shading upload)
     void* d_ptex_faces = nullptr;
     void* d_ptex_texels = nullptr;
     uint32_t ptex_face_count = 0;

@@ -35,6 +35,7 @@
 #include "ptex.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
+#include "tex2d.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
 
@@ -170,7 +171,7 @@ __global__ void __launch_bounds__(kBlock) k_generate(PtParams P) {
 }  // namespace
 
 // A scene whose hits may need Ptex (its own faces, or instances whose scenes may have some).
-bool pt_scene_textured(const PtScene& sc) { return sc.ptex_face_count > 0 || sc.insts != nullptr; }
+bool pt_scene_textured(const PtScene& sc) { return sc.ptex_face_count > 0 || sc.tex2d != 0 || sc.insts != nullptr; }
 
 namespace {
 
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_extend(PtParams P,
 // are sorted by class before shading, so a warp shades one kind of surface.
 __device__ __forceinline__ uint32_t class_of(const MaterialDev& m) {
     const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
-    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+    return 1u + shader * 4u + ((m.flags & kMaterialTextured) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
 }
 
 template <bool kInst>
@@ -413,13 +414,18 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const u
         const float4 p0 = __ldg(r.tp), p1 = __ldg(r.tp + 1);
         const uint32_t geom = __float_as_uint(p1.w);
         const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
-        if (!(m.flags & kMaterialUsesPtex)) continue;
+        if (!(m.flags & kMaterialTextured)) continue;
         float3 base = ld3(m.base_color);
-        uint32_t pstatus = 0;
-        ptex_eval(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count),
-                  static_cast<const __half*>(r.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y, hit.z,
-                  base, pstatus);
-        status |= pstatus;
+        if (m.flags & kMaterialUsesPtex) {
+            uint32_t pstatus = 0;
+            ptex_eval(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count),
+                      static_cast<const __half*>(r.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                      hit.z, base, pstatus);
+            status |= pstatus;
+        } else {
+            base = tex2d_base_colour(m, geom < r.attr_count ? r.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
+                                     hit.z);
+        }
         P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
     }
     if (status) atomicOr(P.err, status);
@@ -480,7 +486,7 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
                 const float err = 32.0f * 1.19209e-07f *
                                   fmaxf(fmaxf(fabsf(pos.x), fabsf(pos.y)), fmaxf(fabsf(pos.z), hit.x));
                 float3 base = ld3(m.base_color);
-                if (m.flags & kMaterialUsesPtex) {  // filtered by k_texture for this hit
+                if (m.flags & kMaterialTextured) {  // filtered or sampled by k_texture for this hit
                     const float4 b = P.st.base[s];
                     base = f3(b.x, b.y, b.z);
                 }

@@ -43,6 +43,7 @@ struct PtScene {
     uint32_t attr_count;
     float lo[3], hi[3];           // bounds (the origin cells of the ray sort)
     uint32_t ray_sort;            // 1: sort each bounce's continuing rays (SEL_OPTION_RAY_SORT)
+    uint32_t tex2d;               // 1: a material takes its base colour from a 2D image (kMaterialUsesTexture)
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.

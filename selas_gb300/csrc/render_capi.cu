@@ -160,27 +160,30 @@ static int upload_attrs(SelSceneTy* sc) {
     sc->d_attrs = nullptr;
     sc->attr_count = 0;
     uint32_t max_geom = 0;
-    size_t n_idx = 0, n_nrm = 0, n_tan = 0;
+    size_t n_idx = 0, n_nrm = 0, n_tan = 0, n_uv = 0;
+    auto has_uvs = [](const MeshInput& m) { return m.attr_n[2] == 2; };  // slot 2 as (u, v) pairs
     for (const MeshInput& m : sc->meshes) {
-        if (!m.attr_n[0] && !m.attr_n[1]) continue;
+        if (!m.attr_n[0] && !m.attr_n[1] && !has_uvs(m)) continue;
         max_geom = std::max(max_geom, m.geomID + 1);
         n_idx += m.indices.size();
         if (m.attr_n[0]) n_nrm += m.attr[0].size();
         if (m.attr_n[1]) n_tan += m.attr[1].size();
+        if (has_uvs(m)) n_uv += m.attr[2].size();
     }
     if (!max_geom) return SEL_OK;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
     const size_t o_idx = up(sizeof(MeshAttrDev) * max_geom), o_nrm = o_idx + up(n_idx * 4), o_tan = o_nrm + up(n_nrm * 4);
-    const size_t total = o_tan + up(n_tan * 4);
+    const size_t o_uv = o_tan + up(n_tan * 4);
+    const size_t total = o_uv + up(n_uv * 4);
     void* d = nullptr;
     cudaError_t e = cudaMalloc(&d, total);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(vertex attributes)");
     char* base = static_cast<char*>(d);
     std::vector<unsigned char> host(total, 0);
     MeshAttrDev* table = reinterpret_cast<MeshAttrDev*>(host.data());
-    size_t ai = 0, an = 0, at = 0;
+    size_t ai = 0, an = 0, at = 0, au = 0;
     for (const MeshInput& m : sc->meshes) {
-        if (!m.attr_n[0] && !m.attr_n[1]) continue;
+        if (!m.attr_n[0] && !m.attr_n[1] && !has_uvs(m)) continue;
         MeshAttrDev& t = table[m.geomID];
         t.indices = reinterpret_cast<const uint32_t*>(base + o_idx + ai * 4);
         std::memcpy(host.data() + o_idx + ai * 4, m.indices.data(), m.indices.size() * 4);
@@ -194,6 +197,11 @@ static int upload_attrs(SelSceneTy* sc) {
             t.tangents = reinterpret_cast<const float4*>(base + o_tan + at * 4);
             std::memcpy(host.data() + o_tan + at * 4, m.attr[1].data(), m.attr[1].size() * 4);
             at += m.attr[1].size();
+        }
+        if (has_uvs(m)) {
+            t.uvs = reinterpret_cast<const float2*>(base + o_uv + au * 4);
+            std::memcpy(host.data() + o_uv + au * 4, m.attr[2].data(), m.attr[2].size() * 4);
+            au += m.attr[2].size();
         }
     }
     e = cudaMemcpy(d, host.data(), total, cudaMemcpyHostToDevice);
@@ -256,18 +264,47 @@ int sync_shading(SelSceneTy* sc) {
         for (const auto& pb : sc->ptex) bound |= (&m - mats.data()) == ptrdiff_t(pb.geomID);
         if (!bound) m.flags &= ~kMaterialUsesPtex;  // no texture bound: keep the material's base colour
     }
+    // 2D base-colour images: materials without Ptex sample theirs at the hit's uvs
+    if (sc->d_textures) cudaFree(sc->d_textures);
+    sc->d_textures = nullptr;
+    {
+        size_t n = 0;
+        for (const auto& tb : sc->textures) n += tb.rgba.size();
+        if (n) {
+            cudaError_t e = cudaMalloc(&sc->d_textures, n * sizeof(float));
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(textures)");
+            std::vector<float> all;
+            all.reserve(n);
+            for (const auto& tb : sc->textures) {
+                if (tb.geomID < mats.size() && !(mats[tb.geomID].flags & kMaterialUsesPtex)) {
+                    MaterialDev& m = mats[tb.geomID];
+                    const uint64_t p = reinterpret_cast<uint64_t>(static_cast<float*>(sc->d_textures) + all.size());
+                    m.flags |= kMaterialUsesTexture;
+                    m.tex_lo = uint32_t(p);
+                    m.tex_hi = uint32_t(p >> 32);
+                    m.tex_width = tb.width;
+                    m.tex_height = tb.height;
+                }
+                all.insert(all.end(), tb.rgba.begin(), tb.rgba.end());
+            }
+            e = cudaMemcpy(sc->d_textures, all.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_fail(e, "uploading textures");
+        }
+    }
     // material classes of the attached meshes (shader x Ptex x transparency, as the path tracer sorts them)
     {
         uint32_t seen = 0;
         for (const MeshInput& mi : sc->meshes) {
             const MaterialDev& m = mats[mi.geomID < mats.size() ? mi.geomID : 0];
             const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
-            seen |= 1u << (shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u));
+            seen |= 1u << (shader * 4u + ((m.flags & kMaterialTextured) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u));
         }
         bool ptex = false;
-        for (const auto& m : mats) ptex |= (m.flags & kMaterialUsesPtex) != 0;
+        for (const auto& m : mats) ptex |= (m.flags & kMaterialTextured) != 0;
         sc->class_mask = seen;
         sc->sort_hint_ptex = ptex;
+        sc->tex2d = false;
+        for (const auto& m : mats) sc->tex2d |= (m.flags & kMaterialUsesTexture) != 0;
         uint32_t mask = 0;
         tree_classes(sc, mask, ptex);
         sc->sort_hint = (ptex || __builtin_popcount(mask) > 1) ? 1u : 0u;
@@ -383,6 +420,7 @@ PtScene scene_view(const SelSceneTy* sc) {
         ps.hi[a] = sc->info.bounds_hi[a];
     }
     ps.ray_sort = sc->dev->ray_sort ? 1u : 0u;
+    ps.tex2d = sc->tex2d ? 1u : 0u;
     return ps;
 }
 
@@ -645,6 +683,36 @@ int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const S
     q.z = make_float3(light->z[0], light->z[1], light->z[2]);
     q.radiance = make_float3(light->radiance[0], light->radiance[1], light->radiance[2]);
     scene->light_sets[lightSetIndex].push_back(q);
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_set_texture(SelScene scene, unsigned int geomID, const float* data, unsigned int width,
+                          unsigned int height, unsigned int channels) {
+    if (!scene || (width && height && !data)) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
+    if (channels != 1 && channels != 3 && channels != 4)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "channels must be 1, 3 or 4");
+    if (width > 16384 || height > 16384) return fail(SEL_ERR_INVALID_ARGUMENT, "width and height must be at most 16384");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    auto& list = scene->textures;
+    for (size_t i = 0; i < list.size(); ++i)
+        if (list[i].geomID == geomID) {
+            list.erase(list.begin() + ptrdiff_t(i));
+            break;
+        }
+    if (width && height) {
+        SelSceneTy::TextureBinding tb;
+        tb.geomID = geomID;
+        tb.width = width;
+        tb.height = height;
+        tb.rgba.resize(size_t(width) * height * 4);
+        for (size_t i = 0; i < size_t(width) * height; ++i)
+            for (int c = 0; c < 4; ++c)  // one channel: grey (SampleTextureFloat3 of a Float image)
+                tb.rgba[i * 4 + c] = c < 3 ? data[i * channels + (channels == 1 ? 0 : c)]
+                                           : (channels == 4 ? data[i * 4 + 3] : 1.0f);
+        list.push_back(std::move(tb));
+    }
     scene->shading_dirty = true;
     return SEL_OK;
 }

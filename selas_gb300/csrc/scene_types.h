@@ -17,14 +17,16 @@ struct QuadLight {
 // (SceneLib/ModelResource.h:68-88) plus the geometry's light set and Ptex face range.
 struct MaterialDev {
     int shader;
-    uint32_t flags;      // kMaterialTransparent | kMaterialUsesPtex
+    uint32_t flags;      // kMaterialTransparent | kMaterialUsesPtex | kMaterialUsesTexture
     uint32_t light_set;
     uint32_t ptex_base;  // first face of this geometry in the packed Ptex face table
     float base_color[3];
     float transmittance_color[3];
     float sheen, sheen_tint, clearcoat, clearcoat_gloss, metallic, spec_trans, diffuse_trans, flatness;
     float anisotropic, specular_tint, roughness, scatter_distance, ior;
-    float pad[9];
+    uint32_t tex_lo, tex_hi;        // kMaterialUsesTexture: the base-colour image (float4 texels, row-major)
+    uint32_t tex_width, tex_height;
+    float pad[5];
 };
 static_assert(sizeof(MaterialDev) == 128, "MaterialDev must be 128 bytes");
 
@@ -37,7 +39,7 @@ struct MeshAttrDev {
     const uint32_t* indices;
     const float* normals;
     const float4* tangents;
-    const void* pad;
+    const float2* uvs;  // slot 2
 };
 
 struct ShadeView {
@@ -53,5 +55,7 @@ struct ShadeView {
 
 constexpr uint32_t kMaterialTransparent = 1u;  // DisneySolid with diffTrans or specTrans (BuildModel.cpp:60-65)
 constexpr uint32_t kMaterialUsesPtex = 2u;
+constexpr uint32_t kMaterialUsesTexture = 4u;  // base colour from a 2D image at the hit's uvs (not Ptex)
+constexpr uint32_t kMaterialTextured = kMaterialUsesPtex | kMaterialUsesTexture;
 
 }  // namespace sel

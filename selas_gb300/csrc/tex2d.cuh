@@ -1,0 +1,53 @@
+// Base colour from a 2D image at the hit's uvs: the reference's non-Ptex path of CalculateSurfaceParams
+// (Source/Core/Shading/SurfaceParameters.cpp:186-190,209-213: uvs interpolated from attribute slot 2, else (0, 0);
+// SampleTextureFloat3 / SampleTexture, :60-119, sRGB to linear after filtering; the caller then raises it to 2.2
+// as for Ptex) with TextureFiltering::Triangle at mip level 0 and Repeat wrapping (TextureFiltering.h:30-100).
+// Repeat wraps by the remainder of a signed division, so the texel left of column 0 is the last one of the row
+// above, as in the reference; a texel index before the image's first (the reference reads out of bounds there)
+// takes texel 0.
+#pragma once
+
+#include <cstdint>
+
+#include "scene_types.h"
+#include "vecmath.cuh"
+
+namespace sel {
+
+// SrgbToLinearPrecise (MathLib/ColorSpace.cpp:16-23)
+SEL_HD float srgb_to_linear(float x) { return x <= 0.04045f ? x / 12.92f : powf((x + 0.055f) / (1.0f + 0.055f), 2.4f); }
+
+SEL_HD float3 tex2d_texel(const float4* tex, int w, int h, int s, int t) {
+    s = s % w;
+    t = t % h;
+    int i = t * w + s;
+    i = i < 0 ? 0 : (i > w * h - 1 ? w * h - 1 : i);
+    const float4 c = tex[i];
+    return f3(c.x, c.y, c.z);
+}
+
+// The linear base colour of material m at barycentrics (bu, bv) of triangle `prim` of a mesh with attributes
+// `attr` (null or without uvs: uvs (0, 0)).
+SEL_HD float3 tex2d_base_colour(const MaterialDev& m, const MeshAttrDev* attr, uint32_t prim, float bu, float bv) {
+    float su = 0.0f, sv = 0.0f;
+    if (attr && attr->uvs) {
+        const uint32_t* idx = attr->indices + size_t(prim) * 3;
+        const float2 a = attr->uvs[idx[0]], b = attr->uvs[idx[1]], c = attr->uvs[idx[2]];
+        const float w = 1.0f - bu - bv;
+        su = w * a.x + bu * b.x + bv * c.x;
+        sv = w * a.y + bu * b.y + bv * c.y;
+    }
+    const float4* tex = reinterpret_cast<const float4*>(uint64_t(m.tex_lo) | (uint64_t(m.tex_hi) << 32));
+    const int w = int(m.tex_width), h = int(m.tex_height);
+    const float s = su * float(w) - 0.5f;
+    const float t = sv * float(h) - 0.5f;
+    const int s0 = int(floorf(s)), t0 = int(floorf(t));
+    const float ds = s - float(s0), dt = t - float(t0);
+    const float3 r = (1.0f - ds) * (1.0f - dt) * tex2d_texel(tex, w, h, s0, t0) +
+                     (1.0f - ds) * dt * tex2d_texel(tex, w, h, s0, t0 + 1) +
+                     ds * (1.0f - dt) * tex2d_texel(tex, w, h, s0 + 1, t0) +
+                     ds * dt * tex2d_texel(tex, w, h, s0 + 1, t0 + 1);
+    return f3(srgb_to_linear(r.x), srgb_to_linear(r.y), srgb_to_linear(r.z));
+}
+
+}  // namespace sel

@@ -33,6 +33,7 @@
 #include "radix.cuh"
 #include "scan.cuh"
 #include "shading.cuh"
+#include "tex2d.cuh"
 #include "traverse.cuh"
 
 namespace sel {
@@ -256,19 +257,21 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
     h.pos = f3(org.x + hit.x * dir.x, org.y + hit.x * dir.y, org.z + hit.x * dir.z);
     h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), hit.x));
     float3 base = ld3(m.base_color);
-    if (m.flags & kMaterialUsesPtex) {
+    const MeshAttrDev* attr = geom < P.attr_count ? P.attrs + geom : nullptr;
+    if (m.flags & kMaterialTextured) {
         if constexpr (kPretex) {
             const float4 b = P.st.base[s];
             base = f3(b.x, b.y, b.z);
-        } else {
+        } else if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
             ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
                       hit.y, hit.z, base, pstatus);
             status |= pstatus;
+        } else {
+            base = tex2d_base_colour(m, attr, __float_as_uint(p0.w), hit.y, hit.z);
         }
     }
     h.view = -dir;
-    const MeshAttrDev* attr = geom < P.attr_count ? P.attrs + geom : nullptr;
     float3 fn, ft, fb;
     shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2), [](float3 x) { return x; }, fn, ft,
                   fb, h.bsign);
@@ -581,7 +584,7 @@ __device__ __forceinline__ uint32_t vmaterial_class(const VcmParams& P, uint32_t
     const uint32_t geom = __float_as_uint(__ldg(P.tris + size_t(tri) * 3 + 1).w);
     const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
     const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
-    return 1u + shader * 4u + ((m.flags & kMaterialUsesPtex) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
+    return 1u + shader * 4u + ((m.flags & kMaterialTextured) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
 }
 
 __global__ void k_vclass_reset(uint32_t* counters) {
@@ -639,12 +642,17 @@ __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
         const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1);
         const uint32_t geom = __float_as_uint(p1.w);
         const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
-        if (!(m.flags & kMaterialUsesPtex)) continue;
+        if (!(m.flags & kMaterialTextured)) continue;
         float3 base = ld3(m.base_color);
-        uint32_t pstatus = 0;
-        ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
-                  hit.z, base, pstatus);
-        status |= pstatus;
+        if (m.flags & kMaterialUsesPtex) {
+            uint32_t pstatus = 0;
+            ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
+                      hit.y, hit.z, base, pstatus);
+            status |= pstatus;
+        } else {
+            base = tex2d_base_colour(m, geom < P.attr_count ? P.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
+                                     hit.z);
+        }
         P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
     }
     if (status) atomicOr(P.err, status);

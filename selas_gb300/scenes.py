@@ -193,7 +193,8 @@ class RenderScene:
     camera: dict = field(default_factory=dict)      # position, look_at, up, fov_degrees
     ptex: dict = field(default_factory=dict)        # geomID -> (face rows (n, 8) int32, texels float16)
     ibl: dict = None                                # light (H, W, 3), miss (h, w, 3) or None, rotation, exposure
-    attrs: dict = None                              # geomID -> {"normals": (n, 3), "tangents": (n, 4)}
+    attrs: dict = None                              # geomID -> {"normals": (n, 3), "tangents": (n, 4), "uvs": (n, 2)}
+    textures: dict = None                           # geomID -> 2D base-colour image (h, w, 1 | 3 | 4) floats
 
     def attach_attributes(self, sc) -> None:
         for gid, a in (self.attrs or {}).items():
@@ -201,21 +202,28 @@ class RenderScene:
                 sc.set_vertex_attribute(gid, 0, a["normals"])
             if a.get("tangents") is not None:
                 sc.set_vertex_attribute(gid, 1, a["tangents"])
+            if a.get("uvs") is not None:
+                sc.set_vertex_attribute(gid, 2, a["uvs"])
+        for gid, img in (self.textures or {}).items():
+            sc.set_texture(gid, img)
 
     def attribute_soup(self):
-        """Per-triangle corner normals (n, 9), tangents (n, 12) and flags (1 normals, 2 tangents), in soup()
-        order, for the oracle."""
-        ns, ts, fs = [], [], []
+        """Per-triangle corner normals (n, 9), tangents (n, 12), flags (1 normals, 2 tangents, 4 uvs) and uvs
+        (n, 6), in soup() order, for the oracle."""
+        ns, ts, fs, us = [], [], [], []
         for gid, v, idx in self.geometry.meshes:
             a = (self.attrs or {}).get(gid, {})
-            n, t = a.get("normals"), a.get("tangents")
+            n, t, uv = a.get("normals"), a.get("tangents"), a.get("uvs")
             m = idx.shape[0]
             ns.append(np.asarray(n, np.float32)[idx].reshape(m, 9) if n is not None else np.zeros((m, 9), np.float32))
             ts.append(np.asarray(t, np.float32)[idx].reshape(m, 12) if t is not None else np.zeros((m, 12), np.float32))
-            fs.append(np.full(m, (1 if n is not None else 0) | (2 if t is not None else 0), np.uint8))
+            us.append(np.asarray(uv, np.float32)[idx].reshape(m, 6) if uv is not None else np.zeros((m, 6), np.float32))
+            fs.append(np.full(m, (1 if n is not None else 0) | (2 if t is not None else 0) | (4 if uv is not None else 0),
+                              np.uint8))
         if not ns:
-            return np.zeros((0, 9), np.float32), np.zeros((0, 12), np.float32), np.zeros(0, np.uint8)
-        return np.concatenate(ns), np.concatenate(ts), np.concatenate(fs)
+            return (np.zeros((0, 9), np.float32), np.zeros((0, 12), np.float32), np.zeros(0, np.uint8),
+                    np.zeros((0, 6), np.float32))
+        return np.concatenate(ns), np.concatenate(ts), np.concatenate(fs), np.concatenate(us)
 
     def ptex_tables(self, material_recs=None):
         """Combined face table (rows rebased) and texels of all textured geometries, in geomID order; writes
