@@ -786,12 +786,12 @@ def smooth_spheres(count: int = 4, level: int = 3, seed: int = 0x5E1A5106) -> Re
 # models through assimp (BuildCommon/ImportModel.cpp) into binary model resources; the OBJ reader here stands in
 # for that import for OBJ content.
 # ---------------------------------------------------------------------------------------------------
-def load_obj(text: str):
+def load_obj(text: str, with_uvs: bool = False):
     """Wavefront OBJ text -> list of (material name, vertices (n, 3) f32, indices (m, 3) u32, normals (n, 3) or
-    None), one entry per `usemtl` group in order of first use ("" before any).  Faces may be polygons (fanned
-    from their first corner) with v, v/vt, v//vn or v/vt/vn corners and negative (relative) indices; a group's
-    vertices are its distinct (position, normal) pairs."""
-    pos, nrm = [], []
+    None), one entry per `usemtl` group in order of first use ("" before any); with_uvs appends uvs (n, 2) or
+    None to each entry.  Faces may be polygons (fanned from their first corner) with v, v/vt, v//vn or v/vt/vn
+    corners and negative (relative) indices; a group's vertices are its distinct (position, uv, normal) triples."""
+    pos, nrm, tex = [], [], []
     groups = {}
     order = []
     cur = ""
@@ -809,6 +809,8 @@ def load_obj(text: str):
             pos.append([float(x) for x in parts[1:4]])
         elif tag == "vn":
             nrm.append([float(x) for x in parts[1:4]])
+        elif tag == "vt":
+            tex.append([float(x) for x in parts[1:3]] + [0.0] * max(0, 3 - len(parts)))
         elif tag == "usemtl":
             cur = parts[1] if len(parts) > 1 else ""
         elif tag == "f":
@@ -816,10 +818,11 @@ def load_obj(text: str):
             for c in parts[1:]:
                 f = c.split("/")
                 vi = index(f[0], len(pos))
+                ti = index(f[1], len(tex)) if len(f) > 1 and f[1] else -1
                 ni = index(f[2], len(nrm)) if len(f) > 2 and f[2] else -1
-                if not 0 <= vi < len(pos) or not -1 <= ni < len(nrm):
+                if not 0 <= vi < len(pos) or not -1 <= ni < len(nrm) or not -1 <= ti < len(tex):
                     raise ValueError(f"face corner {c!r} indexes past the vertices read so far")
-                corners.append((vi, ni))
+                corners.append((vi, ni, ti))
             if len(corners) < 3:
                 raise ValueError("a face needs at least three corners")
             if cur not in groups:
@@ -831,6 +834,7 @@ def load_obj(text: str):
                 tris.append((ids[0], ids[k], ids[k + 1]))
     pos_a = np.asarray(pos, np.float32).reshape(-1, 3)
     nrm_a = np.asarray(nrm, np.float32).reshape(-1, 3)
+    tex_a = np.asarray(tex, np.float32).reshape(-1, 2)
     out = []
     for name in order:
         remap, tris = groups[name]
@@ -838,7 +842,11 @@ def load_obj(text: str):
         v = pos_a[[k[0] for k in keys]]
         has_n = all(k[1] >= 0 for k in keys)
         n = nrm_a[[k[1] for k in keys]] if has_n and keys else None
-        out.append((name, np.ascontiguousarray(v), np.asarray(tris, np.uint32).reshape(-1, 3), n))
+        entry = (name, np.ascontiguousarray(v), np.asarray(tris, np.uint32).reshape(-1, 3), n)
+        if with_uvs:
+            has_t = all(k[2] >= 0 for k in keys)
+            entry += (np.ascontiguousarray(tex_a[[k[2] for k in keys]]) if has_t and keys else None,)
+        out.append(entry)
     return out
 
 
@@ -855,7 +863,8 @@ def load_scene_file(path, camera: dict = None, lights: list = (), materials_dir=
     part 0 is the world (the given lights and camera, the file's backgroundIntensity), each distinct model an
     instanced part (its OBJ `usemtl` groups geomIDs 0, 1, ... with the material `<materials_dir>/<name>.json`
     when that file exists, else the default material; `usesPtex` is cleared, since no Ptex texels come with an
-    OBJ), and each subscene file a part instancing its own models (one level of subscenes).  Asset paths are read
+    OBJ; a base colour naming a .hdr image makes it the group's 2D base-colour texture at the OBJ's uvs), and each
+    subscene file a part instancing its own models (one level of subscenes).  Asset paths are read
     relative to the scene file's folder; the image-based light the file names (a .hdr image or a dual-IBL JSON
     file, `load_ibl`) lights the world when the file exists.  Without a camera, one looks at the instanced
     bounds from outside them."""
@@ -871,17 +880,25 @@ def load_scene_file(path, camera: dict = None, lights: list = (), materials_dir=
         key = ("model", asset)
         if key in index_of:
             return index_of[key]
-        geometry, mats, attrs = TriangleScene(), {}, {}
-        for gid, (name, v, idx, n) in enumerate(load_obj((path.parent / asset).read_text())):
+        geometry, mats, attrs, images = TriangleScene(), {}, {}, {}
+        for gid, (name, v, idx, n, uv) in enumerate(load_obj((path.parent / asset).read_text(), with_uvs=True)):
             geometry.add(gid, v, idx)
             f = mat_dir / f"{name}.json"
             if name and f.exists():
-                fields = _material_fields(sel.material_from_json(f.read_text())[0])
+                m, texture = sel.material_from_json(f.read_text())
+                fields = _material_fields(m)
                 fields["usesPtex"] = 0
                 mats[gid] = fields
+                if texture.lower().endswith(".hdr") and (mat_dir / texture).exists():
+                    images[gid] = read_hdr((mat_dir / texture).read_bytes())
+            a = {}
             if n is not None:
-                attrs[gid] = {"normals": n}
-        parts.append(RenderScene(geometry, mats, [], (0.0, 0.0, 0.0), {}, {}, None, attrs or None))
+                a["normals"] = n
+            if uv is not None:
+                a["uvs"] = uv
+            if a:
+                attrs[gid] = a
+        parts.append(RenderScene(geometry, mats, [], (0.0, 0.0, 0.0), {}, {}, None, attrs or None, images or None))
         instances.append([])
         index_of[key] = len(parts) - 1
         return index_of[key]

@@ -188,6 +188,9 @@ def test_load_obj_groups_fans_and_indices():
     assert np.all(top[:, 1] == 1.0) and np.all(gold[3][gold[2][2:].reshape(-1)] == [0, 1, 0])
     floor = scenes.load_obj(FLOOR_OBJ)
     assert floor[0][0] == "Floor" and floor[0][3] is None and floor[0][2].shape == (2, 3)
+    floor_uv = scenes.load_obj(FLOOR_OBJ.replace("vt 0 0", "vt 0 0\nvt 1 0.5"), with_uvs=True)
+    assert floor_uv[0][4].shape == (4, 2) and np.all(floor_uv[0][4] == 0.0)
+    assert scenes.load_obj(CUBE_OBJ, with_uvs=True)[0][4] is None  # v//vn corners carry no uvs
     with pytest.raises(ValueError):
         scenes.load_obj("v 0 0 0\nf 1 2 3\n")
 
@@ -226,6 +229,7 @@ def test_load_scene_file(tmp_path):
     assert cube.materials[1]["usesPtex"] == 0  # no texels come with an OBJ
     assert s.parts[1].materials == {}  # Floor.json does not exist: the default material
     assert s.parts[0].background == pytest.approx((0.2, 0.3, 0.4)) and s.parts[0].lights == lights
+    assert s.parts[1].attrs[0]["uvs"].shape == (4, 2) and s.parts[1].textures is None
     assert set(s.camera) == {"position", "look_at", "up", "fov_degrees"}
 
 
@@ -322,3 +326,15 @@ def test_scene_file_with_dual_ibl(tmp_path):
     assert ibl["rotation"] == pytest.approx(np.pi / 2) and ibl["exposure"] == pytest.approx(2 ** 1.5)
     single = scenes.load_ibl(tmp_path / "sky.hdr")
     assert single["miss"] is None and single["rotation"] == 0.0 and single["exposure"] == 1.0
+
+
+def test_scene_file_with_textured_material(tmp_path):
+    from selas_gb300 import scenes
+    path, lights = _write_scene(tmp_path)
+    img = np.linspace(0.0, 1.0, 8 * 16 * 3, dtype=np.float32).reshape(8, 16, 3)
+    (tmp_path / "floor.hdr").write_bytes(_hdr_bytes(img, True))
+    (tmp_path / "Floor.json").write_text(json.dumps({"baseColor": "floor.hdr", "roughness": 0.8}))
+    s = scenes.load_scene_file(path, lights=lights)
+    floor = s.parts[1]
+    assert floor.materials[0]["roughness"] == np.float32(0.8) and floor.textures[0].shape == (8, 16, 3)
+    assert floor.attrs[0]["uvs"].shape == (4, 2)
