@@ -338,3 +338,29 @@ def test_scene_file_with_textured_material(tmp_path):
     floor = s.parts[1]
     assert floor.materials[0]["roughness"] == np.float32(0.8) and floor.textures[0].shape == (8, 16, 3)
     assert floor.attrs[0]["uvs"].shape == (4, 2)
+
+
+@pytest.mark.gpu
+def test_gpu_textured_scene_file_renders_the_oracles_image(device, tmp_path):
+    """The floor's material file names a .hdr base-colour image sampled at the OBJ's texture coordinates."""
+    import selas_gb300 as sel
+    import oracle
+    from selas_gb300 import scenes
+    path, lights = _write_scene(tmp_path)
+    (tmp_path / "floor.obj").write_text(FLOOR_OBJ.replace("vt 0 0", "vt 0 0\nvt 3 0\nvt 3 3\nvt 0 3")
+                                        .replace("f 1/1 4/1 3/1\nf 1/1 3/1 2/1", "f 1/1 4/4 3/3\nf 1/1 3/3 2/2"))
+    y, x = np.mgrid[0:8, 0:8]
+    img = np.where(((x + y) % 2 == 0)[..., None], [0.9, 0.85, 0.3], [0.15, 0.3, 0.8]).astype(np.float32)
+    (tmp_path / "floor.hdr").write_bytes(_hdr_bytes(img, True))
+    (tmp_path / "Floor.json").write_text(json.dumps({"baseColor": "floor.hdr", "roughness": 0.7}))
+    s = scenes.load_scene_file(path, lights=lights)
+    assert s.parts[1].textures is not None
+    built = s.build(sel, device)
+    gpu = built[0].pt_generate_image(s.sel_camera(sel, 48, 36), sel.pt_settings(8, 6, 0x5E1A5000)).astype(np.float64)
+    s.release(built)
+    cpu = oracle.graph_render(s, 48, 36, 0, 8, seed=0x5E1A5000, max_bounces=6) / 8.0
+    for layer in (0, 1):
+        g, c = gpu[layer], cpu[layer]
+        rel = np.abs(g - c) / np.maximum(np.abs(c), 1e-3 * c.mean())
+        assert np.median(rel) < 1e-4, np.median(rel)
+        assert (rel < 1e-2).mean() > 0.97
