@@ -812,6 +812,17 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     const int trace_grid = grid_for(sms, 1024 / tb);
     const int shade_grid = grid_for(sms, 8);
     const int gen_grid = int((st.capacity + kBlock - 1) / kBlock);
+    // the shading kernel (4 or 5 resident blocks per SM) runs one resident wave of grid-striding blocks, sized by
+    // the occupancy calculator, as VCM's shading kernels do
+    const void* shade_fn = instanced ? (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, true>)
+                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, true>)
+                                                      : reinterpret_cast<const void*>(&k_shade<1, true>))
+                                     : (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, false>)
+                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, false>)
+                                                      : reinterpret_cast<const void*>(&k_shade<1, false>));
+    int shade_blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_blocks, shade_fn, kBlock, 0);
+    const int wave_grid = sms * std::max(shade_blocks, 1);
     auto enqueue = [&](cudaStream_t s) {
         k_batch_begin<<<1, 32, 0, s>>>(P);
         k_generate<<<gen_grid, kBlock, 0, s>>>(P);
@@ -852,13 +863,13 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             if (texture && instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
             else if (texture) k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
             if (instanced) {
-                if (modes == 2u) k_shade<2, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else if (modes == 3u) k_shade<3, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else k_shade<1, true><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                if (modes == 2u) k_shade<2, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else if (modes == 3u) k_shade<3, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else k_shade<1, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
             } else {
-                if (modes == 2u) k_shade<2, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else if (modes == 3u) k_shade<3, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else k_shade<1, false><<<shade_grid, kBlock, 0, s>>>(P, cur, b, q);
+                if (modes == 2u) k_shade<2, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else if (modes == 3u) k_shade<3, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+                else k_shade<1, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
             }
             if (instanced) k_shadow<2, 128><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
