@@ -186,9 +186,10 @@ int sel_occluded1M(SelScene scene, SelRay* rays, unsigned int M, size_t byte_str
  * a real-time loop that cannot risk the device synchronisation cudaMalloc/cudaFree may cause, or code
  * with every byte of HBM budgeted up front.  It has no counterpart in the reference.  The call allocates
  * nothing: it stages records in one fixed array of 65536 SelRayHit records (6 MiB) that every GPU
- * loading the library holds until exit, and rejects M > 65536 with SEL_ERR_INVALID_ARGUMENT.  The first
- * call on a device looks up that array's device address; make that first call before any stream capture.
- * All calls share the array (its contents are whatever the last call left; every call overwrites the
+ * loading the library holds until exit, and rejects M > 65536 with SEL_ERR_INVALID_ARGUMENT.
+ * sel_device_new looks up that array's device address (loading the module that holds it), so the query
+ * itself loads nothing.  Like every query it refuses, with SEL_ERR_INVALID_OPERATION and before any
+ * launch, a scene whose instanced scenes were re-committed after it.  All calls share the array (its contents are whatever the last call left; every call overwrites the
  * records it uses first).  Calls through one SelDevice are serialised; calls through different SelDevice
  * handles on the same GPU that overlap on the GPU race on the array. */
 int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride);

@@ -107,6 +107,9 @@ int sel_device_new(int cuda_device, SelDevice* out_device) {
     for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&dev->qstream[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&dev->d_err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(dev->d_err, 0, sizeof(uint32_t));
+    // The allocation-free query's staging array: resolving its address here loads its module (and so
+    // creates the array) while the device is being set up, not inside the first allocation-free call.
+    if (e == cudaSuccess && resolve_noalloc_staging(dev) != SEL_OK) e = cudaErrorInvalidSymbol;
     if (e != cudaSuccess) {
         if (dev->stream) cudaStreamDestroy(dev->stream);
         for (cudaStream_t q : dev->qstream)

@@ -19,6 +19,7 @@ struct SelDeviceTy {
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT
     bool ray_sort = false;          // SEL_OPTION_RAY_SORT
+    void* noalloc_staging = nullptr;  // device address of sel_intersect1M_noalloc's fixed array on this GPU
     std::mutex mu;
 };
 
@@ -126,4 +127,6 @@ int cuda_fail(cudaError_t e, const char* what);
 int set_device(SelDeviceTy* dev);
 int read_error_word(SelDeviceTy* dev, cudaStream_t s);
 DeviceBvh device_bvh(const SelSceneTy* sc);
+// noalloc.cu: looks up the device address of the fixed staging array on dev's GPU (dev's device current)
+int resolve_noalloc_staging(SelDeviceTy* dev);
 }  // namespace sel

@@ -6,8 +6,6 @@
 // the implicit device synchronisation cudaMalloc/cudaFree may cause, or code that has budgeted every
 // byte of HBM up front.  sel_intersect1M_noalloc is the same query with the staging area in a fixed
 // file-scope __device__ array instead, so the call itself allocates nothing.
-#include <mutex>
-
 #include "capi_internal.h"
 #include "query.h"
 
@@ -21,38 +19,31 @@ constexpr unsigned int kStaticRecords = 65536;  // 6 MiB of SelRayHit records
 // a host-side stand-in under this name; the device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) SelRayHit g_static_rayhits[kStaticRecords];
 
-constexpr int kMaxDevices = 64;
+}  // namespace
 
-struct StaticAddresses {
-    std::mutex mu;
-    void* ptr[kMaxDevices] = {};
-};
+namespace sel {
 
-StaticAddresses& static_addresses() {
-    static StaticAddresses a;
-    return a;
-}
-
-// Device address of the staging array on the current device, resolved once per device.
-int static_staging(int device, SelRayHit** out) {
-    if (device < 0 || device >= kMaxDevices) return fail(SEL_ERR_INVALID_ARGUMENT, "device ordinal out of range");
-    StaticAddresses& a = static_addresses();
-    std::lock_guard<std::mutex> lock(a.mu);
-    if (!a.ptr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_rayhits);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static staging array)");
-        a.ptr[device] = p;
-    }
-    *out = static_cast<SelRayHit*>(a.ptr[device]);
+// Called by sel_device_new with the device current.  With lazy module loading this is where the module
+// holding the array is loaded and the array created, so the query itself neither loads nor allocates.
+// The address belongs to the SelDevice (and to its context): a device handle made after a context reset
+// resolves it again.
+int resolve_noalloc_staging(SelDeviceTy* dev) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_rayhits);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static staging array)");
+    dev->noalloc_staging = p;
     return SEL_OK;
 }
 
-}  // namespace
+}  // namespace sel
 
 extern "C" int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsigned int M, size_t byte_stride) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
+    // A scene whose instanced scenes were re-committed points at their freed trees: refuse it, as every
+    // other query does, before anything is launched.
+    if (!instances_fresh(scene))
+        return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene changed since this scene was committed");
     if (M == 0) return SEL_OK;
     if (!rayhits) return fail(SEL_ERR_INVALID_ARGUMENT, "ray buffer is null");
     if (byte_stride < sizeof(SelRayHit)) return fail(SEL_ERR_INVALID_ARGUMENT, "byte_stride smaller than the record");
@@ -63,8 +54,8 @@ extern "C" int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsig
     if (int rc = set_device(scene->dev)) return rc;
     SelDeviceTy* dev = scene->dev;
     std::lock_guard<std::mutex> dlock(dev->mu);
-    SelRayHit* staging = nullptr;
-    if (int rc = static_staging(dev->cuda_device, &staging)) return rc;
+    SelRayHit* staging = static_cast<SelRayHit*>(dev->noalloc_staging);
+    if (!staging) return fail(SEL_ERR_INVALID_OPERATION, "device has no staging array address");
     const cudaStream_t s = dev->stream;
     // Records are copied in whole, so nothing in the array has to start at zero; strided records are
     // gathered by a pitched copy rather than through a host-side buffer.

@@ -2,7 +2,8 @@
 whose host application owns every byte of HBM, a real-time loop that cannot risk the synchronisation
 cudaMalloc may cause).  It must return exactly what sel_intersect1M returns -- ray queries are compared
 bit for bit everywhere in this suite -- on consecutive calls that reuse its fixed staging array, and
-reject batches larger than that array.  This file is collected last on purpose.
+reject batches larger than that array, refuse a scene whose instanced scenes changed, and leave the
+device's free memory unchanged.  This file is collected last on purpose.
 """
 import ctypes
 
@@ -66,4 +67,48 @@ def test_noalloc_rejects_batches_beyond_its_array(device):
     want = recs[:CAPACITY].copy()
     sc.intersect1M(want)
     assert_hits_equal(full, want)
+    sc.release()
+
+
+def test_noalloc_refuses_a_scene_whose_instanced_scene_changed(device):
+    data = scenes.displaced_icospheres(count=2, level=2, seed=7)
+    leaf = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8)
+    data.attach_to(leaf)
+    leaf.commit()
+    parent = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8)
+    parent.attach_instance(2, leaf, np.eye(4, dtype=np.float32))
+    parent.commit()
+    org, d = scenes.surface_rays(data, 1000, seed=8)
+    recs = sel.make_rayhits(org, d)
+    sel.check(_noalloc(parent, recs))
+    assert (recs["instID0"] == 2).sum() > 100
+    leaf.commit()  # frees the trees the parent's instance records point at
+    recs = sel.make_rayhits(org, d)
+    assert _noalloc(parent, recs) == sel.SEL_ERR_INVALID_OPERATION
+    assert (recs["geomID"] == sel.INVALID_ID).all()  # nothing was traced
+    parent.commit()
+    sel.check(_noalloc(parent, recs))
+    want = sel.make_rayhits(org, d)
+    parent.intersect1M(want)
+    assert_hits_equal(recs, want)
+    parent.release()
+    leaf.release()
+
+
+def test_noalloc_leaves_device_memory_unchanged(device):
+    torch = pytest.importorskip("torch")
+    data = scenes.displaced_icospheres(count=4, level=3, seed=9)
+    sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8)
+    data.attach_to(sc)
+    sc.commit()  # a fresh scene: the host-memory query forms have not allocated its staging buffer
+    batches = [scenes.surface_rays(data, n, seed=10 + n) for n in (CAPACITY, 1000, 30000)]
+    recs = [sel.make_rayhits(o, d) for o, d in batches]
+    sel.check(_noalloc(sc, recs[0]))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for r in recs * 3:
+        sel.check(_noalloc(sc, r))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
     sc.release()
