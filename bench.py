@@ -161,6 +161,12 @@ def cpu_baseline_run(soup, sets, sample: int, steps: int, threads: int):
     return total_q / total_t / 1e6, total_q, total_t
 
 
+def query_config():
+    """The workload of a step, the same for both arms."""
+    return {"workload": WORKLOAD, "queries_per_step": 16777216,
+            "l2": "no flush: ray records (1.2 GB) and BVH exceed the 129 MB L2"}
+
+
 def cpu_desc():
     try:
         import platform
@@ -179,17 +185,18 @@ def run_reference(args):
     data, coherent, incoherent = scenes.ray_query_workload(level=args.level, width=args.width, height=args.width)
     soup = data.soup()
     threads = os.cpu_count() or 1
-    # warm-up (untimed) then K timed bounded-sample steps
-    cpu_baseline_run(soup, [coherent, incoherent], max(1024, args.cpu_sample // 8), max(1, args.warmup), threads)
-    v, q, t = cpu_baseline_run(soup, [coherent, incoherent], args.cpu_sample, args.steps, threads)
+    # warm-up (untimed, on 1/8 of each set) then K timed steps, each the whole workload: every ray of both sets,
+    # closest and any hit (the same 16,777,216 queries a step of the GPU arm runs)
+    full = coherent[0].shape[0]
+    cpu_baseline_run(soup, [coherent, incoherent], max(1024, full // 8), max(1, args.warmup), threads)
+    v, q, t = cpu_baseline_run(soup, [coherent, incoherent], full, args.steps, threads)
     line = {
         "impl": "reference", "metric": "Mrays/s", "value": round(v, 3), "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{args.cpu_sample} rays of each set per step",
-                   "parallelism": "cpu threads"},
+        "config": query_config(),
         "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"{q} queries ({args.cpu_sample} rays x 2 sets x closest+any per step, "
+                         "sample": f"{q} queries (all {full} rays of each set, closest + any hit, per step, "
                                    f"{args.steps} steps) on {cpu_desc()}"},
         "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "Embree 3.2 ships only as Windows/macOS binaries in the reference; the CPU oracle port of the "
@@ -362,6 +369,21 @@ def profile_case(case):
     dev.release()
 
 
+def cornell_cpu_baseline(cornell, spp=4):
+    """The path tracer on the host cores: the oracle port of the reference's EvaluatePath (which traces the
+    reference-compiled path tracer's paths on the same random streams, tests/test_ref_pt.py) over a bounded
+    sample of the Cornell workload (512 x 512 pixels, `spp` of the 64 passes, depth 8), all host threads."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.pt_render(cornell, 64, 64, 0, 1, max_bounces=8, nthreads=threads)  # warm-up
+    t0 = time.perf_counter()
+    oracle.pt_render(cornell, 512, 512, 0, spp, max_bounces=8, nthreads=threads)
+    t = time.perf_counter() - t0
+    return {"value": round(512 * 512 * spp / t, 1), "unit": "paths/s", "cores": threads, "kind": "port",
+            "sample": f"512x512 x {spp} spp of the Cornell workload ({512 * 512 * spp} paths, depth 8) on "
+                      f"{cpu_desc()}, {t:.1f} s"}
+
+
 def render_metrics(sel, scenes, dev, stream, args, room=None):
     """Integrator throughput on both BVH layouts (they return identical hits, so both trace the same paths
     and reach the same image rMSE): the Cornell path tracer (512 x 512, 64 spp, depth 8) and VCM on the room
@@ -393,9 +415,27 @@ def render_metrics(sel, scenes, dev, stream, args, room=None):
         st = sel.pt_settings(64, 8)
         ms = timed(lambda: sel.check(lib.sel_pt_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(st),
                                                                 acc.data_ptr(), sp)), 3)
-        pt[name] = {"ms_per_image": round(ms, 3), "paths_per_s": round(512 * 512 * 64 / (ms * 1e-3), 1)}
+        dev.sync(sp)
+        rays = np.zeros(2, np.uint64)
+        sel.check(lib.sel_scene_last_render_rays(sc.handle, rays.ctypes.data))
+        pt[name] = {"ms_per_image": round(ms, 3), "paths_per_s": round(512 * 512 * 64 / (ms * 1e-3), 1),
+                    "extension_rays": int(rays[0]), "shadow_rays": int(rays[1]),
+                    "mrays_per_s": round(float(rays.sum()) / (ms * 1e-3) / 1e6, 1)}
         sc.release()
     pt["speedup_of_quantised_wide"] = round(pt["quantised_wide8"]["paths_per_s"] / pt["plain_fp32_binary"]["paths_per_s"], 3)
+    # memory roofline of the whole wavefront: algorithmic bytes per extension ray 296 (query 56, hit 24, path state
+    # in and out 128, material record 64, accumulation 24) and per shadow ray 68 (record out 32, query 36) - 364 per
+    # path segment that casts a shadow ray; the Cornell box has no Ptex taps
+    q = pt["quantised_wide8"]
+    alg = q["extension_rays"] * 296 + q["shadow_rays"] * 68
+    peak, peak_kind = measured_peaks()
+    ach = alg / (q["ms_per_image"] * 1e-3) / 1e9
+    pt["roofline"] = {"bound": "hbm", "kernel": "whole path-tracer wavefront (k_extend + k_shade + k_shadow + "
+                      "queue kernels) over one image", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
+                      "frac": round(ach / peak, 5), "peak_source": peak_kind, "algorithmic_bytes_per_image": int(alg),
+                      "traffic": ncu_traffic().get("pt.cornell_image")}
+    if not args.no_cpu_baseline:
+        pt["cpu_baseline"] = cornell_cpu_baseline(cornell)
     out["pt"] = {"workload": "Cornell box, 512x512, 64 spp, max depth 8, one jittered PCG32 sample per pass", **pt}
 
     t0 = time.time()
@@ -681,10 +721,18 @@ def run_ours(args):
         e2e_step()
         e2e_steps = max(2, min(args.steps, 5))
         el = sum(e2e_step() for _ in range(e2e_steps))
+        # the same calls with the records staged through HBM by pipelined copies (SEL_OPTION_ZERO_COPY = 0)
+        dev.set_option(sel.SEL_OPTION_ZERO_COPY, 0)
+        e2e_step()
+        el_staged = sum(e2e_step() for _ in range(e2e_steps))
+        dev.set_option(sel.SEL_OPTION_ZERO_COPY, 1)
         h2d = sum(v.nbytes for v in recs.values())
         e2e = {"value": round(world * queries_per_step * e2e_steps / el / 1e6, 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-               "path": "sel_intersect1M / sel_occluded1M from pinned host memory", "steps": e2e_steps}
+               "path": "sel_intersect1M / sel_occluded1M on records in pinned host memory: the query kernels read "
+                       "the rays and write the hits in place over the host link (SEL_OPTION_ZERO_COPY)",
+               "staged_copies_value": round(world * queries_per_step * e2e_steps / el_staged / 1e6, 3),
+               "steps": e2e_steps}
 
     # roofline of the dominant kernel
     peak, peak_kind = measured_peaks()
@@ -727,11 +775,11 @@ def run_ours(args):
         "metric": "Mrays/s", "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bvh": "8-wide, 8-bit quantised child bounds",
-                   "l2": "no flush: ray records (1.2 GB) and BVH exceed the 129 MB L2",
-                   "parallelism": f"replicas x{world}", "triangles": int(info.triangle_count),
-                   "bvh_nodes": int(info.node_count), "bvh_depth": int(info.max_depth),
-                   "bvh_device_mb": round(info.device_bytes / 2**20, 1), "bvh_build_ms": round(info.build_ms, 1)},
+        "config": query_config(),
+        "parallelism": f"replicas x{world}",
+        "bvh": {"layout": "8-wide, 8-bit quantised child bounds", "triangles": int(info.triangle_count),
+                "nodes": int(info.node_count), "depth": int(info.max_depth),
+                "device_mb": round(info.device_bytes / 2**20, 1), "build_ms": round(info.build_ms, 1)},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,

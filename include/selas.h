@@ -106,9 +106,13 @@ enum {
     SEL_OPTION_MATERIAL_SORT = 2, /* 1 (default): before shading, the integrators order each bounce's hits by
                                      material class and filter Ptex in a kernel of their own when the scene has
                                      Ptex or several material classes; 0: shade in queue order */
-    SEL_OPTION_RAY_SORT = 3       /* 1: the path tracers order each bounce's continuing rays by direction bin
+    SEL_OPTION_RAY_SORT = 3,      /* 1: the path tracers order each bounce's continuing rays by direction bin
                                      (dominant axis and sign) and a Morton code of the origin before tracing
                                      them (PathTracingBatcher.cpp:162-258); 0 (default): queue order */
+    SEL_OPTION_ZERO_COPY = 4      /* 1 (default): the host-memory queries (sel_intersect1M etc.) trace records
+                                     that lie in page-locked host memory the GPU can address (cudaHostAlloc /
+                                     cudaHostRegister) in place, the kernel reading rays and writing hits over
+                                     the host link; 0: always stage them through HBM with pipelined copies */
 };
 int sel_device_set_option(SelDevice device, int option, int value);
 
@@ -236,6 +240,32 @@ int sel_bsdf_evaluate_device(const SelSurface* d_surfaces, const float* d_wo, co
  * flags reflectance[3] wi[3] forwardPdfW reversePdfW mediumPhase extinction[3] uniformsUsed 0. */
 int sel_bsdf_sample_device(const SelSurface* d_surfaces, const float* d_wo, const float* d_u, unsigned int n,
                            float* d_out, void* stream);
+
+/* Shading probes (no counterpart in the reference: diagnostic entry points that run the integrators' own device
+ * functions on given inputs, so that each step can be compared with the reference's function of the same name on
+ * identical inputs).  All take a committed scene without instances; buffers are device memory, work is queued on
+ * `stream`.
+ *
+ * CalculateSurfaceParams + OffsetRayOrigin (Source/Core/Shading/SurfaceParameters.cpp:144-247,403-408) on hits as
+ * RayPick forms them (Source/Applications/Selas/Source/PathTracer.cpp:122-136): d_hits n x 12 floats (position,
+ * Ng, ray direction, u, v, t), d_ids n x 2 (geomID, primID).  d_out n x 40 floats: worldToTangent rows (9),
+ * baseColor (3, after Ptex / 2D image and the power 2.2), transmittanceColor (3), sheen, sheenTint, clearcoat,
+ * clearcoatGloss, metallic, specTrans, diffTrans, flatness, anisotropic, specularTint, roughness, scatterDistance,
+ * ior, relativeIOR, error, shader, materialFlags (eTransparent 1 | eUsesPtex 16), lightSetIndex, the bounce
+ * origin OffsetRayOrigin(-d, 1) (3), the shadow origin OffsetRayOrigin(-d, 0.1) (3), 0. */
+int sel_surface_probe_device(SelScene scene, const float* d_hits, const unsigned int* d_ids, unsigned int n,
+                             float* d_out, void* stream);
+/* NextEventEstimation (Source/Core/Shading/AreaLighting.cpp:113-153,353-373) with its three uniforms given:
+ * d_points n x 6 (position, normal), d_light_sets n, d_u n x 3 (light pick, spherical-rectangle u, v).
+ * d_out n x 9: direction, radiance, distance, pdfW, light index in the set; zeros without a light. */
+int sel_light_probe_device(SelScene scene, const float* d_points, const unsigned int* d_light_sets, const float* d_u,
+                           unsigned int n, float* d_out, void* stream);
+/* The scene's image-based light: Ibl + SphericalToCartesian + SampleIbl(x, y)
+ * (Source/Core/SceneLib/ImageBasedLightResource.cpp:118-151,264-267) for n uniform pairs d_r -> d_samples n x 7
+ * (direction, radiance, pdf); SampleIBlPdf, SampleIbl(wi), SampleIblMiss(wi) (:154-261) for m directions
+ * d_dirs -> d_eval m x 7 (pdf, radiance, miss radiance). */
+int sel_ibl_probe_device(SelScene scene, const float* d_r, unsigned int n, float* d_samples, const float* d_dirs,
+                         unsigned int m, float* d_eval, void* stream);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Shading data of a scene.                                                                          */
@@ -468,6 +498,15 @@ typedef struct SelVcmSettings {
 } SelVcmSettings;
 
 int sel_vcm_settings_defaults(SelVcmSettings* out);
+/* Rays traced by the scene's most recent render (any integrator, any form): out[0] closest-hit (extension)
+ * rays, out[1] any-hit (shadow) rays.  Call once that render's stream has been synchronised.  No reference
+ * counterpart: the measurement counts of the integrators. */
+int sel_scene_last_render_rays(SelScene scene, uint64_t* out);
+/* The per-pass constants of a VCM pass: VCMCommon::CalculateIterationConstants
+ * (Source/Applications/Selas/Source/VCMCommon.cpp:85-112) with vcCount = 1 and iterationIndex = pass + 1, for
+ * base radius radius0, radius alpha and `paths` light paths a pass.  out[5] = vmSearchRadius, vmSearchRadiusSqr,
+ * vmNormalization, vmWeight, vcWeight.  Host computation: needs no GPU. */
+int sel_vcm_pass_constants(float radius0, float alpha, unsigned int paths, unsigned int pass, float* out);
 /* Renders and writes the mean over the passes, [height][width][3] floats in host memory (FP64 sums). */
 int sel_vcm_generate_image(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings, float* out_rgb);
 /* Device form: adds the per-pass sums into d_accum ([height][width][3] doubles in HBM) on `stream` and

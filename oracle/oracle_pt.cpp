@@ -1037,12 +1037,11 @@ bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float
             sv = w * c[1] + u * c[3] + v * c[5];
         }
     }
+    // Repeat (TextureFiltering.h:32-44): `s % w` with s int32 and w uint32 takes the remainder of s converted
+    // to unsigned, so a negative coordinate c reads texel (2^32 + c) mod w.
     auto texel = [&](int s, int tt, int ch) {
-        s = s % t.w;
-        tt = tt % t.h;
-        int i = tt * t.w + s;
-        i = i < 0 ? 0 : (i > t.w * t.h - 1 ? t.w * t.h - 1 : i);
-        return t.rgba[size_t(i) * 4 + ch];
+        const uint32_t ss = uint32_t(s) % uint32_t(t.w), ts = uint32_t(tt) % uint32_t(t.h);
+        return t.rgba[(size_t(ts) * uint32_t(t.w) + ss) * 4 + ch];
     };
     const float s = su * float(t.w) - 0.5f, tt = sv * float(t.h) - 0.5f;
     const int s0 = int(std::floor(s)), t0 = int(std::floor(tt));

@@ -24,6 +24,7 @@ SEL_ERR_DEVICE_LIMIT = 5
 SEL_OPTION_GRAPH_REPLAY = 1
 SEL_OPTION_MATERIAL_SORT = 2
 SEL_OPTION_RAY_SORT = 3
+SEL_OPTION_ZERO_COPY = 4
 SEL_BUILD_HOST, SEL_BUILD_DEVICE = 0, 1
 SEL_BVH_WIDE8_Q8 = 0
 SEL_BVH_BINARY_FP32 = 1
@@ -85,6 +86,11 @@ _SIGNATURES = {
     "sel_occluded1M": [_vp, _vp, _u, _sz],
     "sel_intersect_device": [_vp, _vp, _u, _vp],
     "sel_occluded_device": [_vp, _vp, _u, _vp],
+    "sel_surface_probe_device": [_vp, _vp, _vp, _u, _vp, _vp],
+    "sel_light_probe_device": [_vp, _vp, _vp, _vp, _u, _vp, _vp],
+    "sel_ibl_probe_device": [_vp, _vp, _u, _vp, _vp, _u, _vp, _vp],
+    "sel_vcm_pass_constants": [ctypes.c_float, ctypes.c_float, _u, _u, _vp],
+    "sel_scene_last_render_rays": [_vp, _vp],
 }
 
 

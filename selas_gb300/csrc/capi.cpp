@@ -513,6 +513,9 @@ int sel_device_set_option(SelDevice device, int option, int value) {
         case SEL_OPTION_RAY_SORT:
             device->ray_sort = value != 0;
             return SEL_OK;
+        case SEL_OPTION_ZERO_COPY:
+            device->zero_copy = value != 0;
+            return SEL_OK;
         default:
             return fail(SEL_ERR_INVALID_ARGUMENT, "unknown option");
     }
@@ -546,6 +549,26 @@ static int check_query(SelScene scene) {
     return SEL_OK;
 }
 
+// The device address of `bytes` of host memory at p when the whole range is page-locked memory that the current
+// device can address (cudaHostAlloc / cudaMallocHost / cudaHostRegister under unified addressing): both ends
+// must belong to pinned memory mapped contiguously into the device's address space.
+static bool mapped_host_range(const void* p, size_t bytes, int device, void** dptr) {
+    cudaPointerAttributes a{}, b{};
+    const char* first = static_cast<const char*>(p);
+    const char* last = first + bytes - 1;
+    if (cudaPointerGetAttributes(&a, first) != cudaSuccess || cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+        cudaGetLastError();  // unregistered memory on older runtimes reports an error: not mapped
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+        return false;
+    if (a.device != device || b.device != device) return false;
+    if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) != last - first)
+        return false;
+    *dptr = a.devicePointer;
+    return true;
+}
+
 template <typename Rec, bool kHit>
 static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_stride) {
     if (int rc = check_query(scene)) return rc;
@@ -559,6 +582,17 @@ static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_str
     const size_t bytes = size_t(M) * sizeof(Rec);
     const bool dense = byte_stride == sizeof(Rec);
     cudaError_t e = cudaSuccess;
+    // Records in page-locked host memory the GPU can address (over NVLink-C2C on Grace): the query kernel reads
+    // each ray and writes each hit in place, so only the fields it touches cross the link and no staging buffer
+    // or copy is needed.  Any 16-byte aligned stride that is a multiple of 16 works.
+    void* mapped = nullptr;
+    if (dev->zero_copy && byte_stride % 16 == 0 && (reinterpret_cast<uintptr_t>(recs) & 15u) == 0 &&
+        mapped_host_range(recs, size_t(M - 1) * byte_stride + sizeof(Rec), dev->cuda_device, &mapped)) {
+        e = launch_query_strided(!kHit, device_bvh(scene), mapped, byte_stride, M, dev->d_err, dev->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(dev->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "zero-copy query");
+        return read_error_word(dev, dev->stream);
+    }
     // Large dense batches: chunks pipelined over three streams, so that one chunk's upload, another's
     // traversal and a third's download overlap (the copy engines and the SMs work at once).
     constexpr unsigned kChunk = 1u << 18;

@@ -19,6 +19,7 @@ struct SelDeviceTy {
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT
     bool ray_sort = false;          // SEL_OPTION_RAY_SORT
+    bool zero_copy = true;          // SEL_OPTION_ZERO_COPY
     void* noalloc_staging = nullptr;  // device address of sel_intersect1M_noalloc's fixed array on this GPU
     std::mutex mu;
 };
@@ -52,6 +53,7 @@ struct SelSceneTy {
     void* d_tris = nullptr;
     SelSceneInfo info{};
     void* scratch = nullptr;  // staging buffer of the host-memory query forms
+    const unsigned long long* last_rays = nullptr;  // [closest, any] ray counters of the most recent render
     size_t scratch_bytes = 0;
 
     // shading data (materials indexed by geomID, quad-light sets, background) and its HBM copies

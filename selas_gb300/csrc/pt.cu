@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_shadow(PtParams P)
     static_assert(K != 2 || B == 128, "the instanced stack fills the static shared memory at 128 threads");
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays + 1, (unsigned long long)n);
     uint32_t status = 0;
     for (;;) {
         uint32_t base = 0;
@@ -767,7 +767,7 @@ void pt_layout(PtState& st, Take take, uint32_t paths) {
         st.rhist_off = reinterpret_cast<uint32_t*>(take(4 * (256 * ntiles + 1)));
         st.rscan_tmp = reinterpret_cast<uint32_t*>(take(4 * ((256 * ntiles + 1 + kScanTile - 1) / kScanTile + 1)));
     }
-    st.rays = reinterpret_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+    st.rays = reinterpret_cast<unsigned long long*>(take(2 * sizeof(unsigned long long)));
     st.control = reinterpret_cast<PtControl*>(take(sizeof(PtControl)));
     st.jobs = reinterpret_cast<PtJob*>(take(sizeof(PtJob) * kMaxPtJobs));
     st.capacity = paths;

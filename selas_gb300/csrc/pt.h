@@ -108,7 +108,7 @@ struct PtState {
     float4* sh_d;     // direction, tfar
     float4* sh_c;     // contribution, (job << 28 | pixel) bits
     uint32_t* counters;
-    unsigned long long* rays;  // rays traced (closest + any hit), a running total
+    unsigned long long* rays;  // [0] closest-hit, [1] any-hit rays traced, running totals
     uint32_t* rkeys[2];       // ray sort: keys and the ping-pong partner of the queue
     uint32_t* rvals;
     uint32_t* rhist;          // digit counts per tile and their scan

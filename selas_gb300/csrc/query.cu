@@ -71,6 +71,13 @@ __global__ void __launch_bounds__(kQueryBlock)
 // the lockstep that makes node fetches shared), so the hardware block scheduler does the balancing.
 constexpr int kWideBlocksPerSm = 8;
 
+// Postponed triangle tests in the query kernels: a lane defers its leaf's triangles while fewer than this many
+// lanes of its warp are testing triangles (0: never).
+#ifndef SEL_QUERY_POSTPONE_LANES
+#define SEL_QUERY_POSTPONE_LANES 8
+#endif
+constexpr int kPostponeLanes = SEL_QUERY_POSTPONE_LANES;
+
 template <bool kAnyHit>
 __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm)
     k_query_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris, float4* rays,
@@ -80,7 +87,7 @@ __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm)
     if (i >= n) return;
     QueryHit h;
     uint32_t status = 0;
-    const bool found = trace_wide<kAnyHit>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
+    const bool found = trace_wide<kAnyHit, kPostponeLanes>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
                                            stack_mem + threadIdx.x, kQueryBlock, status);
     if (status) atomicOr(err, status);
     if (found) {
@@ -138,6 +145,13 @@ cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n
 
 cudaError_t launch_occluded(const DeviceBvh& bvh, SelRay* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s) {
     return launch_query<true>(bvh, reinterpret_cast<float4*>(d_rays), sizeof(SelRay) / 16, n, d_err, s);
+}
+
+cudaError_t launch_query_strided(bool any_hit, const DeviceBvh& bvh, void* recs, size_t record_bytes, uint32_t n,
+                                 uint32_t* d_err, cudaStream_t s) {
+    float4* r = static_cast<float4*>(recs);
+    const uint32_t stride = uint32_t(record_bytes / 16);
+    return any_hit ? launch_query<true>(bvh, r, stride, n, d_err, s) : launch_query<false>(bvh, r, stride, n, d_err, s);
 }
 
 }  // namespace sel

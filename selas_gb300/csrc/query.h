@@ -18,5 +18,9 @@ struct DeviceBvh {
 
 cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);
 cudaError_t launch_occluded(const DeviceBvh& bvh, SelRay* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);
+// The same over records `record_bytes` apart (a multiple of 16, at least the record's size), 16-byte aligned,
+// in any memory the device can address (HBM, or page-locked host memory mapped into its address space).
+cudaError_t launch_query_strided(bool any_hit, const DeviceBvh& bvh, void* recs, size_t record_bytes, uint32_t n,
+                                 uint32_t* d_err, cudaStream_t s);
 
 }  // namespace sel

@@ -340,6 +340,7 @@ namespace {
 
 int ensure_pt_state(SelSceneTy* sc, uint32_t paths) {
     if (sc->pt_block && sc->pt_capacity == paths) return SEL_OK;
+    sc->last_rays = nullptr;  // it may point into the block about to be freed
     if (sc->pt_block) cudaFree(sc->pt_block);
     sc->pt_block = nullptr;
     sc->pt_capacity = 0;
@@ -481,6 +482,9 @@ int render_device(SelSceneTy* sc, const SelCamera& camera, const SelPtSettings& 
     const PtState st = pt_state_carve(sc->pt_block, cap);
     const int block = int(settings.traceBlockSize ? settings.traceBlockSize
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
+    sc->last_rays = st.rays;  // this render's ray counts (sel_scene_last_render_rays)
+    if (cudaMemsetAsync(st.rays, 0, 2 * sizeof(unsigned long long), stream) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "ray counters");
     cudaError_t e = pt_render(ps, cam, set, st, d_accum, sc->dev->d_err, stream,
                               sc->dev->graph_replay ? &sc->pt_graph : nullptr, block);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "path tracer launch");
@@ -501,6 +505,9 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
     if (int rc = ensure_pt_state(sc, cap)) return rc;
     const PtScene ps = scene_view(sc);
     const PtState st = pt_state_carve(sc->pt_block, cap);
+    sc->last_rays = st.rays;
+    if (cudaMemsetAsync(st.rays, 0, 2 * sizeof(unsigned long long), stream) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "ray counters");
     PtJob jobs[kMaxPtJobs];
     PtControl ctl;
     std::memset(jobs, 0, sizeof(jobs));
@@ -596,6 +603,7 @@ namespace {
 
 int ensure_vcm_state(SelSceneTy* sc, uint32_t paths, uint32_t max_len) {
     if (sc->vcm_block && sc->vcm_paths == paths && sc->vcm_len == max_len) return SEL_OK;
+    sc->last_rays = nullptr;
     if (sc->vcm_block) cudaFree(sc->vcm_block);
     sc->vcm_block = nullptr;
     sc->vcm_paths = sc->vcm_len = sc->vcm_passes = 0;
@@ -625,6 +633,9 @@ int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSetti
     vcm_lights(sc, set);
     const PtScene ps = scene_view(sc);
     const VcmState st = vcm_state_carve(sc->vcm_block, paths, settings.maxPathLength, kVcmChunk);
+    sc->last_rays = st.rays;
+    if (cudaMemsetAsync(st.rays, 0, 2 * sizeof(unsigned long long), stream) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "ray counters");
     std::vector<VcmConsts> consts;
     for (uint32_t done = 0; done < settings.passes;) {
         const uint32_t n = std::min(kVcmChunk, settings.passes - done);
@@ -795,6 +806,34 @@ int sel_scene_set_background(SelScene scene, float r, float g, float b) {
     scene->background[0] = r;
     scene->background[1] = g;
     scene->background[2] = b;
+    return SEL_OK;
+}
+
+int sel_scene_last_render_rays(SelScene scene, uint64_t* out) {
+    if (!scene || !out) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    out[0] = out[1] = 0;
+    if (!scene->last_rays) return SEL_OK;
+    if (int rc = set_device(scene->dev)) return rc;
+    std::lock_guard<std::mutex> dlock(scene->dev->mu);
+    unsigned long long v[2] = {0, 0};
+    cudaError_t e = cudaMemcpyAsync(v, scene->last_rays, sizeof(v), cudaMemcpyDeviceToHost, scene->dev->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(scene->dev->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "reading the ray counters");
+    out[0] = v[0];
+    out[1] = v[1];
+    return SEL_OK;
+}
+
+int sel_vcm_pass_constants(float radius0, float alpha, unsigned int paths, unsigned int pass, float* out) {
+    if (!out) return fail(SEL_ERR_INVALID_ARGUMENT, "out is null");
+    VcmConsts c;
+    vcm_constants(radius0, alpha, paths, true, pass, c);
+    out[0] = c.radius;
+    out[1] = c.radius2;
+    out[2] = c.vm_norm;
+    out[3] = c.vm_weight;
+    out[4] = c.vc_weight;
     return SEL_OK;
 }
 

@@ -198,7 +198,7 @@ bool admit_one(SelServerTy* S, Job* j) {
             vcm_constants(r0, d.vcm.radiusAlpha, paths, j->vset.merging != 0, d.vcm.firstPass + k, consts[k]);
         // pageable upload: the job's fresh stream has nothing queued but this job's set-up
         vcm_upload_constants(j->vst, consts.data(), d.vcm.passes, s);
-        cudaMemsetAsync(j->vst.rays, 0, sizeof(unsigned long long), s);
+        cudaMemsetAsync(j->vst.rays, 0, 2 * sizeof(unsigned long long), s);
         j->graph.reset(new GraphCache());
         for (auto& ev : j->pass_ev) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
         j->scale = 1.0 / double(d.vcm.passes);
@@ -358,11 +358,11 @@ void finish(SelServerTy* S, Job* j) {
         e = cudaMemcpyAsync(j->result.data(), j->resolved, j->values * sizeof(float), cudaMemcpyDeviceToHost,
                             S->retire_stream);
     if (j->desc.integrator == SEL_INTEGRATOR_VCM && e == cudaSuccess)
-        e = cudaMemcpyAsync(S->h_rays, j->vst.rays, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(S->h_rays, j->vst.rays, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                             S->retire_stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(S->retire_stream);
     if (e != cudaSuccess) worker_error(S, j, e);
-    if (j->desc.integrator == SEL_INTEGRATOR_VCM) S->vcm_rays += *S->h_rays;
+    if (j->desc.integrator == SEL_INTEGRATOR_VCM) S->vcm_rays += S->h_rays[0] + S->h_rays[1];
     cudaFreeAsync(j->d_block, S->retire_stream);
     j->d_block = nullptr;
     if (j->stream) {
@@ -443,13 +443,13 @@ int sel_server_new(SelDevice device, const SelServerConfig* config, SelServer* o
     cudaError_t e = cudaMalloc(&S->pt_block, pt_state_block_bytes(cfg.paths_in_flight));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(server path state)");
     S->pst = pt_state_carve(S->pt_block, cfg.paths_in_flight);
-    e = cudaMemset(S->pst.rays, 0, sizeof(unsigned long long));
+    e = cudaMemset(S->pst.rays, 0, 2 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&S->prio_least, &S->prio_greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&S->pt_stream, cudaStreamNonBlocking, S->prio_greatest);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->retire_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_jobs, sizeof(PtJob) * kMaxPtJobs * kRing);
     if (e == cudaSuccess) e = cudaMallocHost(&S->h_ctl, sizeof(PtControl) * kRing);
-    if (e == cudaSuccess) e = cudaMallocHost(&S->h_rays, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost(&S->h_rays, 2 * sizeof(unsigned long long));
     for (int k = 0; e == cudaSuccess && k < kRing; ++k) e = cudaEventCreateWithFlags(&S->pt_ev[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         cudaFree(S->pt_block);
@@ -552,14 +552,14 @@ int sel_server_wait(SelServer server, uint64_t job_id, float* out, size_t out_fl
 int sel_server_stats(SelServer server, SelServerStats* out) {
     if (!server || !out) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (int rc = set_device(server->dev)) return rc;
-    unsigned long long pt_rays = 0;
-    cudaError_t e = cudaMemcpyAsync(&pt_rays, server->pst.rays, sizeof(pt_rays), cudaMemcpyDeviceToHost,
+    unsigned long long pt_rays[2] = {0, 0};
+    cudaError_t e = cudaMemcpyAsync(pt_rays, server->pst.rays, sizeof(pt_rays), cudaMemcpyDeviceToHost,
                                     server->retire_stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(server->retire_stream);
     if (e != cudaSuccess) return cuda_fail(e, "server statistics");
     std::lock_guard<std::mutex> lock(server->mu);
     *out = server->stats;
-    out->rays = pt_rays + server->vcm_rays;
+    out->rays = pt_rays[0] + pt_rays[1] + server->vcm_rays;
     out->graph_captures = server->pt_graph.captures;
     return SEL_OK;
 }

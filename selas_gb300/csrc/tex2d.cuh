@@ -2,9 +2,9 @@
 // (Source/Core/Shading/SurfaceParameters.cpp:186-190,209-213: uvs interpolated from attribute slot 2, else (0, 0);
 // SampleTextureFloat3 / SampleTexture, :60-119, sRGB to linear after filtering; the caller then raises it to 2.2
 // as for Ptex) with TextureFiltering::Triangle at mip level 0 and Repeat wrapping (TextureFiltering.h:30-100).
-// Repeat wraps by the remainder of a signed division, so the texel left of column 0 is the last one of the row
-// above, as in the reference; a texel index before the image's first (the reference reads out of bounds there)
-// takes texel 0.
+// Repeat takes the remainder of the texel coordinate converted to unsigned, as the reference's `s % w` with an
+// int32 s and a uint32 w does (TextureFiltering.h:32-44): a negative coordinate c reads texel (2^32 + c) mod w,
+// which is the ordinary wrap w + c for the power-of-two sizes images usually have.
 #pragma once
 
 #include <cstdint>
@@ -18,11 +18,8 @@ namespace sel {
 SEL_HD float srgb_to_linear(float x) { return x <= 0.04045f ? x / 12.92f : powf((x + 0.055f) / (1.0f + 0.055f), 2.4f); }
 
 SEL_HD float3 tex2d_texel(const float4* tex, int w, int h, int s, int t) {
-    s = s % w;
-    t = t % h;
-    int i = t * w + s;
-    i = i < 0 ? 0 : (i > w * h - 1 ? w * h - 1 : i);
-    const float4 c = tex[i];
+    const uint32_t ss = uint32_t(s) % uint32_t(w), tt = uint32_t(t) % uint32_t(h);
+    const float4 c = tex[tt * uint32_t(w) + ss];
     return f3(c.x, c.y, c.z);
 }
 

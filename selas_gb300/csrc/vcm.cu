@@ -473,7 +473,7 @@ template <int K, int B>
 __global__ void __launch_bounds__(B, 1024 / B) k_shadow(VcmParams P) {
     __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
     const uint32_t n = P.st.counters[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays + 1, (unsigned long long)n);
     uint32_t status = 0;
     for (;;) {
         uint32_t base = 0;
@@ -1156,7 +1156,7 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.sc = reinterpret_cast<float4*>(take(16 * shadow));
     st.shadow_capacity = uint32_t(shadow);
     st.counters = reinterpret_cast<uint32_t*>(take(4 * 64));
-    st.rays = reinterpret_cast<unsigned long long*>(take(8));
+    st.rays = reinterpret_cast<unsigned long long*>(take(16));
     st.cverts = reinterpret_cast<float4*>(take(16ull * kCamF4 * paths));
     st.pairs = reinterpret_cast<uint2*>(take(8 * nv));
     st.spos = reinterpret_cast<float4*>(take(16 * nv));

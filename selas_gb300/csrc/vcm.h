@@ -56,7 +56,7 @@ struct VcmState {
     uint32_t* counters;   // [0],[1] queue lengths, [2] shadow entries, [3] extend cursor, [4] shadow cursor,
                           // [5] camera-vertex records, [6] connection pairs; [32..47] material-class counts,
                           // [48..63] their scatter cursors
-    unsigned long long* rays;  // rays traced (closest + any hit), a running total
+    unsigned long long* rays;  // [0] closest-hit, [1] any-hit rays traced, running totals
     float4* cverts;       // camera-vertex records of the current bounce, 6 x float4 each
     uint2* pairs;         // (camera-vertex record, light-vertex index) connection pairs of the current bounce
     float4* spos;         // stored-vertex positions in cell order, slot bits in w

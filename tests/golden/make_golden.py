@@ -13,9 +13,23 @@ ptex_golden.npz  - a triangle mesh (icosphere, 320 faces) with 16 x 16 half-floa
                    PtexTriangleFilter (getFilter(f_bspline), zero widths, as SurfaceParameters.cpp:196-206)
                    at seeded (face, u, v) queries including edges, corners and out-of-range faces.
 cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
-                   from the oracle path tracer with MT19937 sampling (oracle/oracle_pt.cpp; each 256-spp chunk
-                   with seeds of its own); the image the
-                   path tracers' rMSE is measured against.  Needs only the oracle (python ... cornell).
+                   from the reference's own path tracer (PathTracer.cpp EvaluatePath, compiled into
+                   oracle/_ref/libref_pt.so) with its MT19937 sampling (each 256-spp chunk with seeds of its own);
+                   the image the path tracers' rMSE is measured against.
+ref_pt_golden.npz - from the reference's own code in oracle/_ref/libref_pt.so (tests/golden/ref_pt.py):
+                   * img_<name>: EvaluatePath images (per-path means, both layers) of the scenes in
+                     tests/ref_scenes.py IMAGES on the GPU's PCG32 streams (stream pass * W * H + pixel);
+                   * deferred_<name>: DeferredPathTracer images (ShadeHitBatch / TraceRayBatch /
+                     TraceOcclusionBatch, one path at a time) of tests/ref_scenes.py DEFERRED on PCG32 streams;
+                   * cornell_mt64: layer 1 of the Cornell scene at 64 x 64, 64 spp with the reference's MT19937
+                     sampling (seed 0x1234): the reference arm of the path tracer's rMSE gate;
+                   * surf_*: CalculateSurfaceParams (+ OffsetRayOrigin) on hits of four scenes (vertex
+                     normals and tangents, Ptex, 2D images with uvs, transparent solids);
+                   * nee_*: NextEventEstimation / LightingPdf with prescribed uniforms over light sets of one
+                     and three quad lights;
+                   * ibl_*: Ibl / SampleIbl / SampleIblMiss / SampleIBlPdf with the densities of
+                     BuildImageBasedLight.cpp;
+                   * vcm_*: VCMCommon::CalculateIterationConstants.
 cornell_vcm_64_ref.npz - the FP64 high-pass vertex connection and merging image of the Cornell scene (64 x 64,
                    4096 passes, path length 10, the default radius) from the oracle VCM (oracle/oracle_vcm.cpp);
                    the image the VCM integrators' rMSE is measured against.  Needs only the oracle
@@ -167,15 +181,15 @@ def make_ptex(seed=0x5E1A5E7E, n_random=6000):
 
 
 def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
-    import oracle
+    import ref_pt
     from selas_gb300 import scenes
-    rs = scenes.cornell_box()
     img = np.zeros((2, size, size, 3), np.float64)
     step = 256
-    for p in range(0, spp, step):
-        # MT19937 engines are seeded per call (seed + pixel): each chunk takes seeds of its own
-        img += oracle.pt_render(rs, size, size, p, min(spp, p + step), max_bounces=8, seed=seed + (p // step) * 65536,
-                                rng="mt")
+    with ref_pt.RefScene(scenes.cornell_box()) as ref:
+        for p in range(0, spp, step):
+            # MT19937 engines are seeded per call (seed + pixel): each chunk takes seeds of its own
+            img += ref.render(size, size, p, min(spp, p + step), max_bounces=8, seed=seed + (p // step) * 65536,
+                              rng="mt")
     img /= spp
     np.savez_compressed(OUT / "cornell_64_ref.npz", image=img.astype(np.float32), spp=spp, seed=seed)
     print("cornell_64_ref.npz: mean radiance", img[1].mean(axis=(0, 1)))
@@ -230,8 +244,116 @@ def make_cornell_deferred(axis=64, size=64, max_bounces=64, seed=0x5E1A5C0D):
     print("cornell_deferred_64_ref.npz: mean radiance", img.mean(axis=(0, 1)))
 
 
+def _hits(rs, n, seed):
+    """n closest hits of rays from the scene's camera position and from points around the scene into random
+    directions: (hits n x 12 = position o + t d in FP32 as RayPick forms it, Ng, d, u, v, t; ids n x 2)."""
+    import oracle
+    import selas_gb300 as sel
+    rng = np.random.default_rng(seed)
+    soup = rs.geometry.soup()
+    lo, hi = rs.geometry.bounds()
+    cam = np.array(rs.camera["position"], np.float32)
+    org = np.where(rng.random((4 * n, 1)) < 0.5, cam, rng.uniform(lo, hi, (4 * n, 3))).astype(np.float32)
+    target = rng.uniform(lo, hi, (4 * n, 3)).astype(np.float32)
+    d = target - org
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    rh = sel.make_rayhits(org, d)
+    oracle.intersect_bruteforce(soup, rh)
+    ok = np.nonzero(rh["geomID"] != sel.INVALID_ID)[0][:n]
+    rh, org, d = rh[ok], org[ok], d[ok]
+    t = rh["tfar"].astype(np.float32)
+    pos = (org + t[:, None] * d).astype(np.float32)
+    hits = np.zeros((ok.size, 12), np.float32)
+    hits[:, 0:3] = pos
+    hits[:, 3:6] = np.stack([rh["Ng_x"], rh["Ng_y"], rh["Ng_z"]], 1)
+    hits[:, 6:9] = d
+    hits[:, 9], hits[:, 10], hits[:, 11] = rh["u"], rh["v"], t
+    ids = np.stack([rh["geomID"], rh["primID"]], 1).astype(np.uint32)
+    return hits, ids
+
+
+def nee_scene():
+    """The Cornell box with light set 0 holding three quad lights (the ceiling light and two tilted wall panels)
+    and light set 1 one small light: NextEventEstimation's uniform pick over a set."""
+    import dataclasses
+    from selas_gb300 import scenes
+    c = scenes.cornell_box()
+    l0 = c.lights[0][1]
+    l1 = dict(position=(10.0, 300.0, 280.0), direction=(1.0, 0.0, 0.0), x=(0.0, 0.0, 90.0), z=(0.0, 60.0, 0.0),
+              radiance=(5.0, 5.0, 8.0))
+    l2 = dict(position=(278.0, 250.0, 550.0), direction=(0.0, -0.6, -0.8), x=(120.0, 0.0, 0.0),
+              z=(0.0, 64.0, -48.0), radiance=(3.0, 6.0, 3.0))
+    l3 = dict(position=(400.0, 554.0, 100.0), direction=(0.0, -1.0, 0.0), x=(40.0, 0.0, 0.0), z=(0.0, 0.0, 30.0),
+              radiance=(30.0, 20.0, 10.0))
+    return dataclasses.replace(c, lights=[(0, l0), (0, l1), (0, l2), (1, l3)])
+
+
+def make_ref_pt(seed=0x5E1A5A11):
+    import ref_pt
+    import ref_scenes
+    from selas_gb300 import scenes
+    out = {}
+    for name, (make, w, h, spp, max_bounces) in ref_scenes.IMAGES.items():
+        with ref_pt.RefScene(make()) as ref:
+            img = ref.render(w, h, 0, spp, max_bounces=max_bounces, seed=ref_scenes.SEED, rng="pcg") / spp
+        out[f"img_{name}"] = img.astype(np.float32)
+        print(f"img_{name}: {w}x{h} x {spp} spp, depth {max_bounces}, mean radiance {img[1].mean():.5f}")
+    for name, (make, w, h, m, max_bounces) in ref_scenes.DEFERRED.items():
+        with ref_pt.RefScene(make()) as ref:
+            img = ref.deferred_render(w, h, m, 0, m * m, max_bounces=max_bounces, seed=ref_scenes.SEED) / (m * m)
+        out[f"deferred_{name}"] = img.astype(np.float32)
+        print(f"deferred_{name}: {w}x{h} x {m * m} samples, at most {max_bounces} segments, mean {img.mean():.5f}")
+    with ref_pt.RefScene(scenes.cornell_box()) as ref:
+        out["cornell_mt64"] = (ref.render(64, 64, 0, 64, max_bounces=8, seed=0x1234, rng="mt")[1] / 64).astype(np.float32)
+    # CalculateSurfaceParams on hits of scenes that exercise each of its branches
+    surf_scenes = {"smooth": scenes.smooth_spheres(), "ibl": ref_scenes.ibl_spheres(0.3),
+                   "textured": ref_scenes.textured_cornell(), "media": ref_scenes.media_cornell()}
+    for k, (name, rs) in enumerate(surf_scenes.items()):
+        hits, ids = _hits(rs, 1000, seed + k)
+        with ref_pt.RefScene(rs) as ref:
+            out[f"surf_{name}_hits"], out[f"surf_{name}_ids"] = hits, ids
+            out[f"surf_{name}_out"] = ref.surface_params(hits, ids)
+        print(f"surf_{name}: {hits.shape[0]} hits")
+    # NextEventEstimation + LightingPdf with prescribed uniforms
+    rng = np.random.default_rng(seed + 10)
+    rs = nee_scene()
+    n = 2000
+    q = np.zeros((n, 6), np.float32)
+    q[:, 0:3] = rng.uniform([1, 1, 1], [555, 553, 555], (n, 3))
+    nrm = rng.normal(size=(n, 3))
+    q[:, 3:6] = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+    sets = rng.integers(0, 3, n).astype(np.uint32)  # set 2 does not exist: no sample
+    u = rng.random((n, 3)).astype(np.float32)
+    u[:16, 0] = np.linspace(0.0, 0.999999, 16)
+    wi = rng.normal(size=(n, 3))
+    wi = (wi / np.linalg.norm(wi, axis=1, keepdims=True)).astype(np.float32)
+    with ref_pt.RefScene(rs) as ref:
+        out["nee_q"], out["nee_sets"], out["nee_u"], out["nee_wi"] = q, sets, u, wi
+        out["nee_out"] = ref.nee(q, sets, u, wi)
+    # the image-based light
+    ibl = scenes.sky_ibl(rotation=0.3, exposure=1.5)
+    rs = ref_scenes.ibl_spheres(0.3)
+    h, w = ibl["light"].shape[:2]
+    r = rng.random((2000, 2)).astype(np.float32)
+    r[:4] = [[0.0, 0.0], [0.999999, 0.999999], [0.5, 0.0], [0.0, 0.5]]
+    dirs = rng.normal(size=(2000, 3))
+    dirs = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32)
+    with ref_pt.RefScene(rs) as ref:
+        smp, rgb, ev, mdf, cdf = ref.ibl(r, dirs, w, h)
+    out.update(ibl_r=r, ibl_sample=smp, ibl_rgb=rgb, ibl_dirs=dirs, ibl_eval=ev, ibl_mdf=mdf, ibl_cdf=cdf)
+    # VCM iteration constants
+    args = np.array([[921600, 1, 0.05, 0.75, 1], [921600, 1, 0.05, 0.75, 256], [4096, 1, 2.5, 0.75, 17],
+                     [4096, 1, 2.5, 0.5, 3], [65536, 1, 0.003, 0.9, 1000]], np.float64)
+    out["vcm_args"] = args
+    out["vcm_out"] = np.stack([ref_pt.vcm_constants(int(a[0]), int(a[1]), a[2], a[3], a[4]) for a in args])
+    np.savez_compressed(OUT / "ref_pt_golden.npz", **out)
+    print("ref_pt_golden.npz:", len(out), "arrays")
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm", "cmj", "deferred"]
+    sys.path.insert(0, str(OUT))
+    sys.path.insert(0, str(OUT.parent))
+    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm", "cmj", "deferred", "ref_pt"]
     if "bsdf" in what:
         make_bsdf()
     if "ptex" in what:
@@ -244,3 +366,5 @@ if __name__ == "__main__":
         make_cmj()
     if "deferred" in what:
         make_cornell_deferred()
+    if "ref_pt" in what:
+        make_ref_pt()

@@ -240,3 +240,37 @@ def test_device_built_bvh_full_size(device, full_workload):
         assert_hits_equal(b, a)
     for sc in built.values():
         sc.release()
+
+
+@pytest.mark.parametrize("stride", [96, 128])
+def test_pinned_records_are_traced_in_place(device, stride):
+    """Records in page-locked host memory (torch pin_memory: cudaHostAlloc) are traced where they lie
+    (SEL_OPTION_ZERO_COPY, the default); pageable records and the option turned off take the staged copies.  All
+    three give bit-identical records, dense and embedded in a larger caller struct, for both query kinds; the
+    bytes around the records are left untouched."""
+    import torch
+    data = scenes.displaced_icospheres(count=8, level=4, seed=31)
+    sc = _scene(device, data, sel.SEL_BVH_WIDE8_Q8)
+    org, d = scenes.surface_rays(data, 300000, seed=32)
+    n = org.shape[0]
+    for fmt, make, query, fields in ((96, sel.make_rayhits, "sel_intersect1M", HIT_FIELDS),
+                                     (48, sel.make_rays, "sel_occluded1M", ("tfar",))):
+        st = stride
+        recs = make(org, d)
+        want = recs.copy()
+        getattr(sel.lib(), query)(sc.handle, want.ctypes.data, n, fmt)  # pageable: staged copies
+        pinned = torch.full((n * st + 64,), 0xA5, dtype=torch.uint8).pin_memory()
+        view = pinned.numpy()
+        body = view[:n * st].reshape(n, st)
+        body[:, :fmt] = recs.view(np.uint8).reshape(n, fmt)
+        for option in (1, 0):
+            device.set_option(sel.SEL_OPTION_ZERO_COPY, option)
+            body[:, :fmt] = recs.view(np.uint8).reshape(n, fmt)
+            sel.check(getattr(sel.lib(), query)(sc.handle, view.ctypes.data, n, st))
+            got = np.ascontiguousarray(body[:, :fmt]).view(recs.dtype).reshape(n)
+            assert_hits_equal(got, want, fields=fields)
+            if st > fmt:
+                assert (body[:, fmt:] == 0xA5).all()
+            assert (view[n * st:] == 0xA5).all()
+        device.set_option(sel.SEL_OPTION_ZERO_COPY, 1)
+    sc.release()

@@ -2,34 +2,20 @@
 SurfaceParameters.cpp:186-213): uvs from vertex attribute slot 2, TextureFiltering::Triangle at mip level 0 with
 Repeat wrapping (TextureFiltering.h:30-100), SrgbToLinearPrecise, then the 2.2 power of every base colour.  The
 GPU and the oracle trace the same PCG32 streams, so their images agree pixel by pixel up to FP32 rounding."""
-import dataclasses
 
 import numpy as np
 import pytest
 
 import oracle
+import ref_scenes
 from selas_gb300 import scenes
 
 SEED = 0x5E1A5000
 
 
-def _checker(n=8):
-    y, x = np.mgrid[0:n, 0:n]
-    a = np.array([0.85, 0.8, 0.2], np.float32)
-    b = np.array([0.1, 0.3, 0.75], np.float32)
-    img = np.where(((x + y) % 2 == 0)[..., None], a, b).astype(np.float32)
-    img[0, 0] = [1.0, 0.0, 0.0]  # one odd texel marks the orientation
-    return img
-
-
-def _textured_cornell():
-    """The Cornell box with a checker image on its floor (geomID 0; uvs 0..2.5, so the image repeats and the
-    filter wraps) and a grey image on the back wall without uvs (every hit samples uv (0, 0))."""
-    c = scenes.cornell_box()
-    v0 = c.geometry.meshes[0][1]
-    uvs = (v0[:, [0, 2]] / 556.0 * 2.5).astype(np.float32)
-    attrs = {0: {"uvs": uvs}}
-    return dataclasses.replace(c, attrs=attrs, textures={0: _checker(), 2: np.full((4, 4, 1), 0.35, np.float32)})
+# the textured Cornell box (checker image on the floor with repeating uvs, a grey image on the back wall without
+# uvs) is shared with the reference pins (tests/ref_scenes.py)
+_textured_cornell = ref_scenes.textured_cornell
 
 
 def _same_paths(gpu, cpu):
