@@ -52,6 +52,12 @@ def parse_args():
     p.add_argument("--vcm-passes", type=int, default=256, help="VCM iterations timed on the quantised BVH")
     p.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving stream (0: skip)")
     p.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrival rate of the serving stream, jobs/s")
+    p.add_argument("--serve-saturated", type=int, default=24,
+                   help="jobs of the stream also submitted all at once (server capacity; 0: skip)")
+    p.add_argument("--serve-serial-sample", type=int, default=0,
+                   help="jobs timed on the serial plain path (0: all; else class means for the rest)")
+    p.add_argument("--serve-only", action="store_true",
+                   help="run only the serving measurement and print its JSON (the full-size stream is run this way)")
     p.add_argument("--terrain-grid", type=int, default=4096, help="instanced terrain heightfield size (0: skip)")
     p.add_argument("--terrain-instances", type=int, default=5000)
     p.add_argument("--terrain-spp", type=int, default=64)
@@ -210,9 +216,13 @@ def serve_metrics(sel, scenes, dev, room, args):
     ray-query icospheres, the VCM room} (resident in HBM), a resolution from {256x256, 512x512, 1024x768,
     1920x1080}, spp (path tracer) or passes (VCM) from {16, 64, 256}, an integrator from {path tracer, VCM}
     and a seeded camera yaw.  Served: submitted at their arrival times to the render server (quantised BVH,
-    shared graph-replayed batches, overlapping VCM jobs).  Serial plain path: the same jobs one after
-    another through sel_pt_generate_image / sel_vcm_generate_image on the binary FP32 BVH with kernel-by-
-    kernel launches; its latencies replay the same arrivals through a FIFO with the measured service times."""
+    shared graph-replayed batches, overlapping VCM jobs).  Saturated: the first `serve_saturated` of the same jobs
+    all submitted at once (closed loop: the server's capacity, not the arrival process).  Serial plain path: the
+    same jobs one after another through sel_pt_generate_image / sel_vcm_generate_image on the binary FP32 BVH with
+    kernel-by-kernel launches; its latencies replay the same arrivals through a FIFO with the measured service
+    times.  With --serve-serial-sample K > 0 only K jobs (seeded pick) run serially and every job's service time
+    is the mean of its class (scene, resolution, spp, integrator) in that sample, else the sample's mean service
+    time per path scaled by the job's paths."""
     rng = np.random.default_rng(0x5E1A5005)
     defs = {"cornell": scenes.cornell_box(), "icospheres": scenes.icosphere_field(), "room": room}
     names = list(defs)
@@ -238,50 +248,72 @@ def serve_metrics(sel, scenes, dev, room, args):
             return sel.pt_job(built[j["scene"]], cam, sel.pt_settings(j["spp"], 8, j["seed"])), cam
         return sel.vcm_job(built[j["scene"]], cam, sel.vcm_settings(j["spp"], 10, j["seed"])), cam
 
-    paths = sum(j["res"][0] * j["res"][1] * j["spp"] * (1 if j["integrator"] == 0 else 2) for j in jobs)
-    # served
-    srv = sel.Server(dev)
-    t0 = time.perf_counter()
-    ids = []
-    for j in jobs:
-        delay = t0 + j["t"] - time.perf_counter()
-        if delay > 0:
-            time.sleep(delay)
-        ids.append(srv.submit(make(j, wide)[0]))
-    served = [srv.wait(i) for i in ids]
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.release()
-    lat = np.array([s.latency_ms for _, s in served])
+    def job_paths(j):
+        return j["res"][0] * j["res"][1] * j["spp"] * (1 if j["integrator"] == 0 else 2)
+
+    def serve(subset, arrivals):
+        srv = sel.Server(dev)
+        t0 = time.perf_counter()
+        ids = []
+        for j in subset:
+            if arrivals:
+                delay = t0 + j["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            ids.append(srv.submit(make(j, wide)[0]))
+        done = [srv.wait(i) for i in ids]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.release()
+        return np.array([s.latency_ms for _, s in done]), wall, st
+
+    paths = sum(job_paths(j) for j in jobs)
+    lat, served_wall, st = serve(jobs, True)
+    sat_jobs = jobs[:max(0, min(args.serve_saturated, len(jobs)))]
+    sat = serve(sat_jobs, False) if sat_jobs else None
     for sc in wide.values():
         sc.release()
     # serial plain path: binary FP32 BVH, no graph replay, one job at a time
     plain = {k: v.build(sel, dev, bvh_kind=sel.SEL_BVH_BINARY_FP32) for k, v in defs.items()}
     warm(plain)
     dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 0)
-    service = []
-    for j in jobs:
+    if args.serve_serial_sample and args.serve_serial_sample < len(jobs):
+        pick = sorted(np.random.default_rng(0x5E1A5006).choice(len(jobs), args.serve_serial_sample, replace=False))
+    else:
+        pick = range(len(jobs))
+    measured = {}
+    for i in pick:
+        j = jobs[i]
         job, cam = make(j, plain)
         t1 = time.perf_counter()
         if j["integrator"] == 0:
             plain[j["scene"]].pt_generate_image(cam, job.pt)
         else:
             plain[j["scene"]].vcm_generate_image(cam, job.vcm)
-        service.append(time.perf_counter() - t1)
+        measured[i] = time.perf_counter() - t1
     dev.set_option(sel.SEL_OPTION_GRAPH_REPLAY, 1)
     for sc in plain.values():
         sc.release()
+    key = lambda j: (j["scene"], j["res"], j["spp"], j["integrator"])
+    by_class = {}
+    for i, sv in measured.items():
+        by_class.setdefault(key(jobs[i]), []).append(sv)
+    per_path = sum(measured.values()) / sum(job_paths(jobs[i]) for i in measured)
+    service = [measured[i] if i in measured else
+               (float(np.mean(by_class[key(j)])) if key(j) in by_class else per_path * job_paths(j))
+               for i, j in enumerate(jobs)]
     finish, lat_serial = 0.0, []
     for j, sv in zip(jobs, service):
         finish = max(finish, j["t"]) + sv
         lat_serial.append(1e3 * (finish - j["t"]))
     lat_serial = np.array(lat_serial)
-    served_wall = wall
-    return {
+    arrival_span = jobs[-1]["t"] if jobs else 0.0
+    out = {
         "workload": f"{len(jobs)} jobs, Poisson arrivals at {args.serve_rate} jobs/s; scene from {{Cornell, ray-query "
                     f"icospheres, VCM room}}, resolution from {{256x256, 512x512, 1024x768, 1920x1080}}, spp/passes from "
                     f"{{16, 64, 256}}, integrator from {{path tracer, VCM}}, seeded camera yaw",
         "jobs_pt": sum(1 for j in jobs if j["integrator"] == 0), "jobs_vcm": sum(1 for j in jobs if j["integrator"] == 1),
+        "arrival_span_s": round(arrival_span, 3),
         "served": {"p50_latency_ms": round(float(np.percentile(lat, 50)), 1),
                    "p99_latency_ms": round(float(np.percentile(lat, 99)), 1),
                    "makespan_s": round(served_wall, 3), "jobs_per_s": round(len(jobs) / served_wall, 3),
@@ -291,10 +323,27 @@ def serve_metrics(sel, scenes, dev, room, args):
                          "p99_latency_ms": round(float(np.percentile(lat_serial, 99)), 1),
                          "makespan_s": round(finish, 3), "busy_s": round(sum(service), 3),
                          "jobs_per_s": round(len(jobs) / finish, 3), "paths_per_s": round(paths / finish, 1),
-                         "mrays_per_s": round(st.rays / finish / 1e6, 1)},
+                         "mrays_per_s": round(st.rays / finish / 1e6, 1),
+                         "service_times": "measured for every job" if len(measured) == len(jobs) else
+                                          f"measured for {len(measured)} jobs, class means for the rest"},
         "throughput_ratio_served_vs_serial_plain": round(finish / served_wall, 3),
+        "regime": ("arrival-bound: the server idles between arrivals, so makespan tracks the arrival span"
+                   if served_wall < 1.2 * arrival_span + 2.0 else
+                   "saturated: jobs arrive faster than they are served, the queue grows and p99 reflects queue growth"),
         "rays_note": "both forms trace the same paths (identical hits, same streams), so they trace the same rays",
     }
+    if sat is not None:
+        sl, sw, sst = sat
+        sat_paths = sum(job_paths(j) for j in sat_jobs)
+        busy = sum(service[:len(sat_jobs)])
+        out["saturated"] = {"jobs": len(sat_jobs), "submitted": "all at t = 0 (closed loop)",
+                            "makespan_s": round(sw, 3), "jobs_per_s": round(len(sat_jobs) / sw, 3),
+                            "paths_per_s": round(sat_paths / sw, 1), "mrays_per_s": round(sst.rays / sw / 1e6, 1),
+                            "p50_latency_ms": round(float(np.percentile(sl, 50)), 1),
+                            "p99_latency_ms": round(float(np.percentile(sl, 99)), 1),
+                            "serial_plain_busy_s": round(busy, 3),
+                            "throughput_ratio_vs_serial_plain": round(busy / sw, 3)}
+    return out
 
 
 def profile_case(case):
@@ -458,8 +507,12 @@ def render_metrics(sel, scenes, dev, stream, args, room=None):
         ms = timed(lambda: sel.check(lib.sel_vcm_render_device(sc.handle, ctypes.byref(cam), ctypes.byref(st),
                                                                  acc.data_ptr(), sp)), 1) if passes else 0.0
         dev.sync(sp)
+        rays = np.zeros(2, np.uint64)
+        sel.check(lib.sel_scene_last_render_rays(sc.handle, rays.ctypes.data))
         vcm[name] = {"passes": passes, "ms_per_pass": round(ms / passes, 3),
-                     "paths_per_s": round(2 * w * h * passes / (ms * 1e-3), 1), "scene_upload_and_build_s": round(build_s, 2)}
+                     "paths_per_s": round(2 * w * h * passes / (ms * 1e-3), 1), "scene_upload_and_build_s": round(build_s, 2),
+                     "extension_rays": int(rays[0]), "shadow_rays": int(rays[1]),
+                     "mrays_per_s": round(float(rays.sum()) / (ms * 1e-3) / 1e6, 1)}
         sc.release()
     vcm["speedup_of_quantised_wide"] = round(vcm["quantised_wide8"]["paths_per_s"] / vcm["plain_fp32_binary"]["paths_per_s"], 3)
 
@@ -799,10 +852,28 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_serving_only(args):
+    """The serving measurement alone (the full-size C5 stream takes many minutes, so it runs on its own)."""
+    from selas_gb300._build import build_library
+    build_library()
+    import selas_gb300 as sel
+    from selas_gb300 import scenes
+    dev = sel.Device(0)
+    t0 = time.time()
+    room = scenes.vcm_room()
+    out = serve_metrics(sel, scenes, dev, room, args)
+    out["room_generation_s"] = round(time.time() - t0, 1)
+    dev.release()
+    print(json.dumps({"serving": out}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.profile_case:
         profile_case(args.profile_case)
+        return
+    if args.serve_only:
+        run_serving_only(args)
         return
     if args.impl == "reference":
         run_reference(args)

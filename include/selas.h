@@ -138,6 +138,16 @@ int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size);
 int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const float* vertices,
                                    size_t vertex_count, size_t vertex_stride_bytes,
                                    const unsigned int* indices, size_t triangle_count);
+/* Replaces rtcNewGeometry(RTC_GEOMETRY_TYPE_QUAD) + index/vertex buffers, the geometry the reference makes for
+ * meshes cooked with four indices per face (Source/Core/SceneLib/ModelResource.cpp:272-281).  indices: 4 per quad.
+ * As in Embree (RTC_GEOMETRY_TYPE_QUAD.3embree3) a quad is the triangles (v0, v1, v3) and (v2, v3, v1); a hit
+ * reports primID = the quad's index, Ng of the triangle hit, and (u, v) of the quad's parametrisation (the second
+ * triangle's (u', v') become (1 - u', 1 - v')), so that p = v0 + u (v1 - v0) + v (v3 - v0) on a planar quad.  Ties
+ * on t between the two triangles of one quad go to the first.  Vertex attributes interpolate bilinearly,
+ * t_uv = (1 - v)((1 - u) t0 + u t1) + v((1 - u) t3 + u t2).  Fewer than 2^31 quads per mesh; quad meshes take no
+ * Ptex texture (the reference filters quad Ptex with the separable bicubic filter, not provided). */
+int sel_scene_attach_quad_mesh(SelScene scene, unsigned int geomID, const float* vertices, size_t vertex_count,
+                               size_t vertex_stride_bytes, const unsigned int* indices, size_t quad_count);
 /* Instances, two levels at most (RTC_MAX_INSTANCE_LEVEL_COUNT = 2): rtcNewGeometry(RTC_GEOMETRY_TYPE_INSTANCE)
  * + rtcSetGeometryInstancedScene + rtcSetGeometryTransform(RTC_FORMAT_FLOAT4X4_COLUMN_MAJOR) +
  * rtcAttachGeometryByID (SubsceneResource.cpp:63-79), and the subscene-instance user geometry whose callbacks

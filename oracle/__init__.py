@@ -57,6 +57,10 @@ def lib() -> ctypes.CDLL:
             "oracle_vcm_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, ctypes.c_uint32, ctypes.c_uint32,
                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_uint64, _i, _vp, _i, _vp, _i, _i, _vp], None),
+            "oracle_vcm_graph_render": ([_i, _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i64, _i, _vp, _vp, _vp, _vp,
+                                         _vp, _vp, _vp, _i, _vp, _vp, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
+                                         ctypes.c_float, ctypes.c_uint64, _i, _i, _i, _vp], None),
         }
         for name, (args, res) in sig.items():
             fn = getattr(_lib, name)
@@ -340,6 +344,47 @@ def graph_render(iscene, width, height, begin, end, max_bounces=8, seed=0x5E1A50
                               L.shape[0], 0, _p(M), _p(MO), _p(R), _p(RO), _p(T), _p(TO), _p(lights), lights.shape[0],
                               _p(sets), sets.shape[0], _p(bg), _p(cam), width, height, begin, end, max_bounces, seed,
                               nthreads or threads(), int(physical_nee), int(deferred), samples_per_axis, _p(out))
+    return out
+
+
+def graph_vcm_render(iscene, width, height, iter_begin, iter_end, bounds, max_len=10, radius0=0.0, alpha=0.75,
+                     seed=0x5E1A5000, nthreads=None, merging=True, strategies=15):
+    """CPU oracle VCM (oracle_vcm.cpp) over an InstancedRenderScene: FP64 per-pixel sums over iterations
+    [iter_begin, iter_end), shape (height, width, 3); bounds: the top scene's world box (lo, hi), the
+    environment's emission disc; lights: the top scene's light set 0."""
+    from selas_gb300.scenes import light_records, material_records
+    set_ibl(iscene.parts[0].ibl)
+    set_attributes(iscene.parts)
+    V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
+    mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
+    for part in iscene.parts:
+        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) + [0])
+        m = material_records(part.materials, count)
+        r, t = part.ptex_tables(m)
+        mats.append(m)
+        mat_off.append(mat_off[-1] + m.shape[0])
+        rows.append(r)
+        row_off.append(row_off[-1] + r.shape[0])
+        tex = t if r.shape[0] else np.zeros(0, np.uint16)
+        texels.append(tex)
+        tex_off.append(tex_off[-1] + tex.size // 3)
+    M = np.ascontiguousarray(np.concatenate(mats))
+    R = np.ascontiguousarray(np.concatenate(rows).astype(np.int32)).reshape(-1, 8)
+    T = np.ascontiguousarray(np.concatenate(texels + [np.zeros(3, np.uint16)]))
+    MO, RO, TO = np.array(mat_off, np.int32), np.array(row_off, np.int32), np.array(tex_off, np.int64)
+    top = iscene.parts[0]
+    lights, sets = light_records(top.lights)
+    lights = lights[int(sets[0][0]):int(sets[0][0] + sets[0][1])] if sets.shape[0] else lights[:0]
+    lights = np.ascontiguousarray(lights)
+    B = np.ascontiguousarray(np.concatenate([np.asarray(bounds[0], np.float32), np.asarray(bounds[1], np.float32)]))
+    c = top.camera
+    cam = np.array(list(c["position"]) + list(c["look_at"]) + list(c["up"]) + [c["fov_degrees"]], np.float32)
+    out = np.zeros((height, width, 3), np.float64)
+    lib().oracle_vcm_graph_render(len(iscene.parts), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(L), _p(I), _p(H),
+                                  _p(Q), L.shape[0], 0, _p(M), _p(MO), _p(R), _p(RO), _p(T), _p(TO), _p(lights),
+                                  lights.shape[0], _p(B), _p(cam), width, height, iter_begin, iter_end, max_len,
+                                  float(radius0), float(alpha), seed, nthreads or threads(), int(merging), strategies,
+                                  _p(out))
     return out
 
 

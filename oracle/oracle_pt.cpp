@@ -402,22 +402,19 @@ void shading_frame(const Scene& sc, const orq::Hit& h, V3& n, V3& t, V3& b) {
         if (it != sc.attrs->first.end()) ai = it->second + h.prim;
     }
     const uint8_t aflags = ai >= 0 ? sc.attrs->flags[size_t(ai)] : 0;
-    auto lerp = [&](float a0, float a1, float a2) {
-        const float w = 1.0f - h.u - h.v;
-        return w * a0 + h.u * a1 + h.v * a2;
-    };
     V3 ngv(h.ng[0], h.ng[1], h.ng[2]);
-    if (aflags & 1u) {
-        const float* c = &sc.attrs->normals[size_t(ai) * 9];
-        ngv = V3(lerp(c[0], c[3], c[6]), lerp(c[1], c[4], c[7]), lerp(c[2], c[5], c[8]));
-    }
+    if (aflags & 1u)
+        ngv = V3(ora::corner_interp(sc.attrs->normals, 3, ai, aflags, h.prim, h.u, h.v, 0),
+                 ora::corner_interp(sc.attrs->normals, 3, ai, aflags, h.prim, h.u, h.v, 1),
+                 ora::corner_interp(sc.attrs->normals, 3, ai, aflags, h.prim, h.u, h.v, 2));
     if (h.l2w[1]) ngv = xvector(h.l2w[1], ngv);
     if (h.l2w[0]) ngv = xvector(h.l2w[0], ngv);
     n = orc::Norm(ngv);
     if (aflags & 2u) {
-        const float* c = &sc.attrs->tangents[size_t(ai) * 12];
-        V3 tl(lerp(c[0], c[4], c[8]), lerp(c[1], c[5], c[9]), lerp(c[2], c[6], c[10]));
-        const float sign = lerp(c[3], c[7], c[11]);
+        V3 tl(ora::corner_interp(sc.attrs->tangents, 4, ai, aflags, h.prim, h.u, h.v, 0),
+              ora::corner_interp(sc.attrs->tangents, 4, ai, aflags, h.prim, h.u, h.v, 1),
+              ora::corner_interp(sc.attrs->tangents, 4, ai, aflags, h.prim, h.u, h.v, 2));
+        const float sign = ora::corner_interp(sc.attrs->tangents, 4, ai, aflags, h.prim, h.u, h.v, 3);
         if (h.l2w[1]) tl = xvector(h.l2w[1], tl);
         if (h.l2w[0]) tl = xvector(h.l2w[0], tl);
         t = tl;
@@ -1022,6 +1019,21 @@ void oracle_set_textures(int n, const uint32_t* keys, const uint32_t* dims, cons
 
 namespace ora {
 
+float corner_interp(const std::vector<float>& arr, int per, int64_t tri, uint8_t flags, uint32_t prim, float u, float v,
+                    int k) {
+    if (!(flags & 8u)) {
+        const float* c = &arr[size_t(tri) * 3 * per];
+        const float w = 1.0f - u - v;
+        return w * c[k] + u * c[per + k] + v * c[2 * per + k];
+    }
+    const int64_t first = tri - int64_t(prim & 1u);  // soup triangle 2q: (v0, v1, v3); 2q + 1: (v2, v3, v1)
+    const float* c0 = &arr[size_t(first) * 3 * per];
+    const float* c1 = &arr[size_t(first + 1) * 3 * per];
+    const float qu = (prim & 1u) ? 1.0f - u : u, qv = (prim & 1u) ? 1.0f - v : v;
+    const float iu = 1.0f - qu, iv = 1.0f - qv;
+    return iv * (iu * c0[k] + qu * c0[per + k]) + qv * (iu * c0[2 * per + k] + qu * c1[k]);
+}
+
 bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]) {
     const auto it = g_tex2d.find((uint64_t(scene) << 32) | geom);
     if (it == g_tex2d.end() || it->second.w <= 0 || it->second.h <= 0) return false;
@@ -1030,11 +1042,10 @@ bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float
     const auto f = g_attrs.first.find((uint64_t(scene) << 32) | geom);
     if (f != g_attrs.first.end() && !g_attrs.uvs.empty()) {
         const int64_t tri = f->second + prim;
-        if ((g_attrs.flags[size_t(tri)] & 4u) != 0) {
-            const float* c = &g_attrs.uvs[size_t(tri) * 6];
-            const float w = 1.0f - u - v;
-            su = w * c[0] + u * c[2] + v * c[4];
-            sv = w * c[1] + u * c[3] + v * c[5];
+        const uint8_t fl = g_attrs.flags[size_t(tri)];
+        if ((fl & 4u) != 0) {
+            su = corner_interp(g_attrs.uvs, 2, tri, fl, prim, u, v, 0);
+            sv = corner_interp(g_attrs.uvs, 2, tri, fl, prim, u, v, 1);
         }
     }
     // Repeat (TextureFiltering.h:32-44): `s % w` with s int32 and w uint32 takes the remainder of s converted
@@ -1081,7 +1092,14 @@ bool index(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene
 
 void frame(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, const float ng[3], float n[3], float t[3],
            float b[3]) {
+    frame_through(scene, geom, prim, u, v, ng, nullptr, nullptr, n, t, b);
+}
+
+void frame_through(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, const float ng[3], const float* l2w0,
+                   const float* l2w1, float n[3], float t[3], float b[3]) {
     orq::Hit h;
+    h.l2w[0] = l2w0;
+    h.l2w[1] = l2w1;
     h.u = u;
     h.v = v;
     h.prim = prim;

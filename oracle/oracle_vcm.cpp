@@ -104,6 +104,9 @@ V3 offset(V3 p, V3 n, float err, V3 dir, float scale) {
 
 struct Scene {
     const void* bvh = nullptr;
+    const void* graph = nullptr;                // instanced scene graph (replaces bvh when set)
+    std::vector<std::vector<Material>> gmats;   // graph: materials of each scene, by geomID
+    std::vector<const orp::Texture*> gptex;     // graph: Ptex of each scene (null: none)
     const orp::Texture* ptex = nullptr;
     std::vector<Material> materials;
     std::vector<Light> lights;  // light set 0
@@ -155,23 +158,29 @@ struct Hit {
     bool transparent;  // material flag eTransparent
 };
 
+// Instanced graphs (ModelDataFromRayIds, SceneResource.cpp:362-378): the hit mesh's scene gives the material,
+// Ptex and vertex attributes; its object-space normal goes through the instances' localToWorld.
 bool make_hit(const Scene& sc, V3 org, V3 dir, Hit& out) {
     orq::Hit h;
     const float o[3] = {org.x, org.y, org.z}, d[3] = {dir.x, dir.y, dir.z};
-    if (!orq::closest(sc.bvh, o, d, 0.0f, 3.402823466e+38f, h)) return false;
-    const Material& m = sc.materials[h.geom < sc.materials.size() ? h.geom : 0];
+    if (sc.graph ? !orq::closest_graph(sc.graph, o, d, 0.0f, 3.402823466e+38f, h)
+                 : !orq::closest(sc.bvh, o, d, 0.0f, 3.402823466e+38f, h))
+        return false;
+    const std::vector<Material>& mats = sc.graph ? sc.gmats[h.scene] : sc.materials;
+    const orp::Texture* ptex = sc.graph ? sc.gptex[h.scene] : sc.ptex;
+    const Material& m = mats[h.geom < mats.size() ? h.geom : 0];
     out.pos = V3(org.x + h.t * dir.x, org.y + h.t * dir.y, org.z + h.t * dir.z);
     out.err = 32.0f * 1.19209e-07f * std::max(std::max(std::fabs(out.pos.x), std::fabs(out.pos.y)),
                                               std::max(std::fabs(out.pos.z), h.t));
     // shading frame, with vertex normals and tangents where the mesh has them (SurfaceParameters.cpp:157-184)
     float fn[3], ft[3], fb[3];
-    ora::frame(0, h.geom, h.prim, h.u, h.v, h.ng, fn, ft, fb);
+    ora::frame_through(h.scene, h.geom, h.prim, h.u, h.v, h.ng, h.l2w[0], h.l2w[1], fn, ft, fb);
     const V3 n(fn[0], fn[1], fn[2]);
     orc::Surf& s = out.s;
     s.t = V3(ft[0], ft[1], ft[2]); s.n = n; s.b = V3(fb[0], fb[1], fb[2]);
     float base[3] = {m.base[0], m.base[1], m.base[2]};
-    if ((m.flags & 2u) && sc.ptex) sc.ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
-    else ora::tex2d(0, h.geom, h.prim, h.u, h.v, base);
+    if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    else ora::tex2d(h.scene, h.geom, h.prim, h.u, h.v, base);
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
     s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
     s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
@@ -258,7 +267,7 @@ bool scatter(Rng& rng, const Hit& h, const Consts& c, PathState& st, bool light_
 bool visible(const Scene& sc, const Hit& h, V3 dir, float tfar) {
     const V3 o = offset(h.pos, h.n, h.err, dir, 0.1f);
     const float oa[3] = {o.x, o.y, o.z}, da[3] = {dir.x, dir.y, dir.z};
-    return !orq::occluded(sc.bvh, oa, da, h.err, tfar);
+    return sc.graph ? !orq::occluded_graph(sc.graph, oa, da, h.err, tfar) : !orq::occluded(sc.bvh, oa, da, h.err, tfar);
 }
 
 // World position -> pixel (inverse of ImageToWorldDirection, GeometryLib/Camera.cpp:56-60).
@@ -323,18 +332,9 @@ void build_grid(Grid& g, const std::vector<LightVertex>& v, uint32_t cells, floa
 
 }  // namespace
 
-extern "C" {
-
-// One VCM render: `iterations` passes, each with width*height light and camera paths.  Inputs as
-// oracle_pt_render (materials: 32-word records per geomID; lights: light set 0 as n x 15 floats; camera:
-// position lookAt up fovDegrees).  out: [height][width][3] doubles, the sum over iterations (divide by
-// `iterations` for the image).  radius0: initial merge radius; alpha: radius reduction; merging 0 turns
-// merging off (bidirectional path tracing with the same connections and weights).
-void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
-                       const float* materials, int n_materials, const float* lights, int n_lights,
-                       const float* camera, uint32_t width, uint32_t height, uint32_t iter_begin, uint32_t iter_end,
-                       uint32_t max_len, float radius0, float alpha, uint64_t seed, int threads,
-                       const int32_t* ptex_rows, int ptex_faces, const uint16_t* ptex_texels, int merging,
+// The passes of a VCM render over a set-up scene (shared by the flat and the instanced entry points).
+static void vcm_passes(Scene& sc, const float* camera, uint32_t width, uint32_t height, uint32_t iter_begin,
+                       uint32_t iter_end, float radius0, float alpha, uint64_t seed, int threads, int merging,
                        int strategies, double* out) {
     // strategies: bit 0 next-event estimation, 1 vertex connection, 2 vertex merging, 3 light tracing (15: all,
     // MIS-weighted, with camera paths hitting the environment); otherwise the enabled strategies are weighted 1
@@ -342,37 +342,6 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
     const bool single = (strategies & 15) != 15;
     const bool use_nee = strategies & 1, use_vc = strategies & 2, use_vm = strategies & 4, use_lt = strategies & 8;
     const bool use_hit = !single || (strategies & 16);
-    Scene sc;
-    sc.bvh = orq::build(verts, prim, geom, ntri);
-    ora::index(prim, geom, nullptr, ntri);
-    orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
-    sc.ptex = tex;
-    sc.max_len = max_len;
-    for (int i = 0; i < n_materials; ++i) sc.materials.push_back(read_material(materials + 32 * i));
-    for (int i = 0; i < n_lights; ++i) {
-        const float* l = lights + 15 * i;
-        sc.lights.push_back({V3(l[0], l[1], l[2]), V3(l[3], l[4], l[5]), V3(l[6], l[7], l[8]), V3(l[9], l[10], l[11]),
-                             V3(l[12], l[13], l[14])});
-    }
-    if (ora::env_present() && ntri > 0) {
-        // the scene's bounding sphere (SceneResource.h:77-78 keeps aaBox and boundingSphere), taken about the
-        // bounding box as for the default merge radius
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int64_t k = 0; k < ntri * 3; ++k)
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = std::min(lo[a], verts[k * 3 + a]);
-                hi[a] = std::max(hi[a], verts[k * 3 + a]);
-            }
-        float d2 = 0.0f;
-        for (int a = 0; a < 3; ++a) {
-            const float e = hi[a] - lo[a];
-            d2 += e * e;
-        }
-        sc.env = true;
-        sc.center = V3(0.5f * (lo[0] + hi[0]), 0.5f * (lo[1] + hi[1]), 0.5f * (lo[2] + hi[2]));
-        sc.radius = 0.5f * std::sqrt(d2);
-        sc.disc_pdf = (1.0f / kPi) * (1.0f / (sc.radius * sc.radius));
-    }
     const uint32_t nq = uint32_t(sc.lights.size());
     const uint32_t n_emitters = nq + (sc.env ? 1u : 0u);
     {  // InitializeRayCastCamera (GeometryLib/Camera.cpp:89-115); the pixel-area image plane uses tan(fov/2)
@@ -728,8 +697,101 @@ void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t*
     }
     for (const auto& img : lt_images)
         for (size_t i = 0; i < img.size(); ++i) out[i] += img[i];
+}
+
+// The environment's emission disc: the bounding sphere of the scene box lo..hi (SceneResource.h:77-78 keeps aaBox
+// and boundingSphere), as for the default merge radius.
+static void env_disc(Scene& sc, const float* lo, const float* hi) {
+    float d2 = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        const float e = hi[a] - lo[a];
+        d2 += e * e;
+    }
+    sc.env = true;
+    sc.center = V3(0.5f * (lo[0] + hi[0]), 0.5f * (lo[1] + hi[1]), 0.5f * (lo[2] + hi[2]));
+    sc.radius = 0.5f * std::sqrt(d2);
+    sc.disc_pdf = (1.0f / kPi) * (1.0f / (sc.radius * sc.radius));
+}
+
+extern "C" {
+
+// One VCM render: `iterations` passes, each with width*height light and camera paths.  Inputs as
+// oracle_pt_render (materials: 32-word records per geomID; lights: light set 0 as n x 15 floats; camera:
+// position lookAt up fovDegrees).  out: [height][width][3] doubles, the sum over iterations (divide by
+// `iterations` for the image).  radius0: initial merge radius; alpha: radius reduction; merging 0 turns
+// merging off (bidirectional path tracing with the same connections and weights).
+void oracle_vcm_render(const float* verts, const uint32_t* prim, const uint32_t* geom, int64_t ntri,
+                       const float* materials, int n_materials, const float* lights, int n_lights,
+                       const float* camera, uint32_t width, uint32_t height, uint32_t iter_begin, uint32_t iter_end,
+                       uint32_t max_len, float radius0, float alpha, uint64_t seed, int threads,
+                       const int32_t* ptex_rows, int ptex_faces, const uint16_t* ptex_texels, int merging,
+                       int strategies, double* out) {
+    Scene sc;
+    sc.bvh = orq::build(verts, prim, geom, ntri);
+    ora::index(prim, geom, nullptr, ntri);
+    orp::Texture* tex = ptex_faces > 0 ? new orp::Texture(ptex_rows, ptex_faces, ptex_texels) : nullptr;
+    sc.ptex = tex;
+    sc.max_len = max_len;
+    for (int i = 0; i < n_materials; ++i) sc.materials.push_back(read_material(materials + 32 * i));
+    for (int i = 0; i < n_lights; ++i) {
+        const float* l = lights + 15 * i;
+        sc.lights.push_back({V3(l[0], l[1], l[2]), V3(l[3], l[4], l[5]), V3(l[6], l[7], l[8]), V3(l[9], l[10], l[11]),
+                             V3(l[12], l[13], l[14])});
+    }
+    if (ora::env_present() && ntri > 0) {
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int64_t k = 0; k < ntri * 3; ++k)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], verts[k * 3 + a]);
+                hi[a] = std::max(hi[a], verts[k * 3 + a]);
+            }
+        env_disc(sc, lo, hi);
+    }
+    vcm_passes(sc, camera, width, height, iter_begin, iter_end, radius0, alpha, seed, threads, merging, strategies, out);
     orq::release(const_cast<void*>(sc.bvh));
     delete tex;
 }
+
+// VCM over an instanced scene graph (two levels): triangles and instances as oracle_graph_render (local-to-world
+// rows), scene s has materials[mat_offsets[s] .. mat_offsets[s+1]) and Ptex faces ptex_rows[row_offsets[s] ..)
+// whose texel offsets are relative to texels + texel_offsets[s]; lights are the top scene's light set 0 and
+// bounds[6] (lo, hi) its world box.  Other arguments as oracle_vcm_render.
+void oracle_vcm_graph_render(int n_scenes, const float* verts, const uint32_t* prim, const uint32_t* geom,
+                             const uint32_t* tri_scene, int64_t ntri, const float* l2w, const uint32_t* inst_id,
+                             const uint32_t* inst_scene, const uint32_t* inst_proto, int64_t ninst, int top,
+                             const float* materials, const int32_t* mat_offsets, const int32_t* ptex_rows,
+                             const int32_t* row_offsets, const uint16_t* texels, const int64_t* texel_offsets,
+                             const float* lights, int n_lights, const float* bounds, const float* camera,
+                             uint32_t width, uint32_t height, uint32_t iter_begin, uint32_t iter_end, uint32_t max_len,
+                             float radius0, float alpha, uint64_t seed, int threads, int merging, int strategies,
+                             double* out) {
+    Scene sc;
+    sc.graph = orq::build_graph(n_scenes, verts, prim, geom, tri_scene, ntri, l2w, inst_id, inst_scene, inst_proto,
+                                ninst, top);
+    ora::index(prim, geom, tri_scene, ntri);
+    std::vector<orp::Texture*> owned;
+    for (int s = 0; s < n_scenes; ++s) {
+        std::vector<Material> mats;
+        for (int i = mat_offsets[s]; i < mat_offsets[s + 1]; ++i) mats.push_back(read_material(materials + 32 * i));
+        if (mats.empty()) mats.push_back(read_material(materials + 32 * mat_offsets[top]));
+        sc.gmats.push_back(mats);
+        const int nf = row_offsets[s + 1] - row_offsets[s];
+        orp::Texture* t = nf > 0 ? new orp::Texture(ptex_rows + 8 * row_offsets[s], nf, texels + 3 * texel_offsets[s])
+                                 : nullptr;
+        owned.push_back(t);
+        sc.gptex.push_back(t);
+    }
+    sc.max_len = max_len;
+    for (int i = 0; i < n_lights; ++i) {
+        const float* l = lights + 15 * i;
+        sc.lights.push_back({V3(l[0], l[1], l[2]), V3(l[3], l[4], l[5]), V3(l[6], l[7], l[8]), V3(l[9], l[10], l[11]),
+                             V3(l[12], l[13], l[14])});
+    }
+    if (ora::env_present()) env_disc(sc, bounds, bounds + 3);
+    vcm_passes(sc, camera, width, height, iter_begin, iter_end, radius0, alpha, seed, threads, merging, strategies, out);
+    orq::release_graph(const_cast<void*>(sc.graph));
+    for (orp::Texture* t : owned) delete t;
+}
+
 
 }  // extern "C"

@@ -74,6 +74,7 @@ _SIGNATURES = {
     "sel_scene_new": [_vp, ctypes.POINTER(_vp)],
     "sel_scene_set_bvh_kind": [_vp, _i],
     "sel_scene_attach_triangle_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
+    "sel_scene_attach_quad_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
     "sel_scene_commit": [_vp],
     "sel_scene_attach_instance": [_vp, _u, _vp, _vp],
     "sel_scene_set_vertex_attribute": [_vp, _u, _u, _vp, _sz, _u],
@@ -173,6 +174,11 @@ class Scene:
         idx = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1, 3)
         check(lib().sel_scene_attach_triangle_mesh(self.handle, geom_id, _ptr(v), v.shape[0], 12, _ptr(idx),
                                                    idx.shape[0]))
+
+    def attach_quad_mesh(self, geom_id: int, vertices: np.ndarray, quads: np.ndarray) -> None:
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        q = np.ascontiguousarray(quads, dtype=np.uint32).reshape(-1, 4)
+        check(lib().sel_scene_attach_quad_mesh(self.handle, geom_id, _ptr(v), v.shape[0], 12, _ptr(q), q.shape[0]))
 
     def attach_instance(self, inst_id: int, instanced: "Scene", local_to_world) -> None:
         """Instance of a committed scene; local_to_world: 4 x 4 (or 3 x 4) affine matrix, row-major maths

@@ -60,7 +60,7 @@ struct Node2 {
 
 struct FlatTri {
     float v[3][3];
-    uint32_t prim, geom;
+    uint32_t prim, geom, kind;
 };
 
 class BinaryBuilder {
@@ -322,7 +322,7 @@ private:
                 std::memcpy(r.v2, t.v[2], 12);
                 r.prim = t.prim;
                 r.geom = t.geom;
-                r.pad = 0;
+                r.kind = t.kind;
                 out_.tris.push_back(r);
             }
             offset += leaf.count;
@@ -405,7 +405,7 @@ std::string emit_binary(const std::vector<Node2>& n2, const std::vector<Prim>& p
         std::memcpy(r.v2, t.v[2], 12);
         r.prim = t.prim;
         r.geom = t.geom;
-        r.pad = 0;
+        r.kind = t.kind;
         out.tris.push_back(r);
     }
     // Renumber reachable internal nodes densely (DFS, left first); a root leaf becomes a node whose
@@ -504,6 +504,7 @@ std::string build_bvh(const std::vector<MeshInput>& meshes, int kind, BuiltBvh& 
             }
             ft.prim = uint32_t(t);
             ft.geom = m.geomID;
+            ft.kind = m.quads ? kTriQuadHalf : kTriPlain;
             tris.push_back(ft);
         }
     }

@@ -741,7 +741,7 @@ std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max
             }
             r.prim = uint32_t(t);
             r.geom = m.geomID;
-            r.pad = 0;
+            r.kind = m.quads ? kTriQuadHalf : kTriPlain;
             soup.push_back(r);
         }
     }

@@ -194,6 +194,33 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
     return SEL_OK;
 }
 
+int sel_scene_attach_quad_mesh(SelScene scene, unsigned int geomID, const float* vertices, size_t vertex_count,
+                               size_t vertex_stride_bytes, const unsigned int* indices, size_t quad_count) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if (quad_count && !indices) return fail(SEL_ERR_INVALID_ARGUMENT, "null buffer");
+    if (quad_count >= (size_t(1) << 31)) return fail(SEL_ERR_INVALID_ARGUMENT, "a quad mesh holds fewer than 2^31 quads");
+    // Embree handles a quad as the triangles (v0, v1, v3) and (v2, v3, v1) (RTC_GEOMETRY_TYPE_QUAD.3embree3):
+    // stored that way, as triangles 2q and 2q + 1 of the mesh
+    std::vector<unsigned int> pairs;
+    try {
+        pairs.resize(quad_count * 6);
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    for (size_t q = 0; q < quad_count; ++q) {
+        const unsigned int* v = indices + 4 * q;
+        unsigned int* t = pairs.data() + 6 * q;
+        t[0] = v[0]; t[1] = v[1]; t[2] = v[3];
+        t[3] = v[2]; t[4] = v[3]; t[5] = v[1];
+    }
+    if (int rc = sel_scene_attach_triangle_mesh(scene, geomID, vertices, vertex_count, vertex_stride_bytes,
+                                                pairs.data(), 2 * quad_count))
+        return rc;
+    std::lock_guard<std::mutex> lock(scene->mu);
+    scene->meshes.back().quads = true;
+    return SEL_OK;
+}
+
 int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld) {
     if (!scene || !instanced || !localToWorld) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (instanced == scene) return fail(SEL_ERR_INVALID_ARGUMENT, "a scene cannot instance itself");
@@ -256,6 +283,18 @@ int sel_interpolate0(SelScene scene, unsigned int geomID, unsigned int primID, f
         const uint32_t n = m.attr_n[slot];
         if (!n) return fail(SEL_ERR_INVALID_OPERATION, "the mesh has no attribute in this slot");
         if (count > n) return fail(SEL_ERR_INVALID_ARGUMENT, "count exceeds the attribute's components");
+        if (m.quads) {
+            // bilinear over the quad (RTC_GEOMETRY_TYPE_QUAD.3embree3): t_uv = (1-v)((1-u) t0 + u t1) + v((1-u) t3 + u t2)
+            if (size_t(primID) * 6 + 5 >= m.indices.size()) return fail(SEL_ERR_INVALID_ARGUMENT, "primID out of range");
+            const uint32_t* t = &m.indices[6 * size_t(primID)];  // (v0, v1, v3), (v2, v3, v1)
+            const float* a0 = &m.attr[slot][size_t(t[0]) * n];
+            const float* a1 = &m.attr[slot][size_t(t[1]) * n];
+            const float* a2 = &m.attr[slot][size_t(t[3]) * n];
+            const float* a3 = &m.attr[slot][size_t(t[2]) * n];
+            const float iu = 1.0f - u, iv = 1.0f - v;
+            for (unsigned int k = 0; k < count; ++k) out[k] = iv * (iu * a0[k] + u * a1[k]) + v * (iu * a3[k] + u * a2[k]);
+            return SEL_OK;
+        }
         if (size_t(primID) * 3 + 2 >= m.indices.size()) return fail(SEL_ERR_INVALID_ARGUMENT, "primID out of range");
         const float* a0 = &m.attr[slot][size_t(m.indices[3 * size_t(primID)]) * n];
         const float* a1 = &m.attr[slot][size_t(m.indices[3 * size_t(primID) + 1]) * n];

@@ -123,6 +123,7 @@ bool instances_fresh(const SelSceneTy* sc);
 int check_deferred_args(SelScene scene, const SelCamera* camera, const SelPtSettings* settings);
 uint32_t deferred_axis(const SelPtSettings& settings);
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings);
+int check_vcm_materials(const SelSceneTy* scene);  // after sync_shading: material tables below 2^56
 void init_camera(const SelCamera& c, PtCamera& out);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);

@@ -31,6 +31,7 @@
 #include "cmj.cuh"
 #include "graph.h"
 #include "ibl.cuh"
+#include "hitref.cuh"
 #include "instance.cuh"
 #include "ptex.cuh"
 #include "radix.cuh"
@@ -175,79 +176,10 @@ bool pt_scene_textured(const PtScene& sc) { return sc.ptex_face_count > 0 || sc.
 
 namespace {
 
-// Instances entered to a hit, as 1 + index in the parent's instance table (0: none).
-__device__ __forceinline__ uint2 inst_indices(const PtScene& sc, const InstHit& h) {
-    const uint32_t a = h.rec[0] ? uint32_t(h.rec[0] - sc.insts) + 1u : 0u;
-    const uint32_t b = h.rec[1] ? uint32_t(h.rec[1] - h.rec[0]->insts) + 1u : 0u;
-    return make_uint2(a, b);
-}
-
-// A hit's leaf record and the shading data of the scene whose mesh was hit: the job's scene, or the scene of
-// the innermost instance entered (ModelDataFromRayIds, SceneResource.cpp:362-378).
-struct HitRef {
-    const float4* tp;
-    const MaterialDev* mats;
-    uint32_t mat_count;
-    uint32_t ptex_count;
-    const void* ptex_faces;
-    const void* ptex_texels;
-    const MeshAttrDev* attrs;
-    uint32_t attr_count;
-    const InstanceRecord* rec0;
-    const InstanceRecord* rec1;
-};
-
+// A hit's leaf record and shading data (hitref.cuh) for path slot s of the wavefront.
 template <bool kInst>
 __device__ __forceinline__ HitRef hit_ref(const PtState& st, const PtScene& S, uint32_t s, uint32_t tri) {
-    HitRef r;
-    r.rec0 = r.rec1 = nullptr;
-    const float4* tris = S.tris;
-    r.mats = S.materials;
-    r.mat_count = S.material_count;
-    r.ptex_faces = S.ptex_faces;
-    r.ptex_texels = S.ptex_texels;
-    r.ptex_count = S.ptex_face_count;
-    r.attrs = S.attrs;
-    r.attr_count = S.attr_count;
-    if (kInst) {
-        const uint2 hi = st.hinst[s];
-        if (hi.x) {
-            r.rec0 = S.insts + (hi.x - 1u);
-            const InstanceRecord* in = r.rec0;
-            if (hi.y) {
-                r.rec1 = r.rec0->insts + (hi.y - 1u);
-                in = r.rec1;
-            }
-            tris = static_cast<const float4*>(in->tris);
-            const ShadeView* v = static_cast<const ShadeView*>(in->shading);
-            r.mats = v->materials;
-            r.mat_count = v->material_count;
-            r.ptex_faces = v->ptex_faces;
-            r.ptex_texels = v->ptex_texels;
-            r.ptex_count = v->ptex_face_count;
-            r.attrs = v->attrs;
-            r.attr_count = v->attr_count;
-        }
-    }
-    r.tp = tris + size_t(tri) * 3;
-    return r;
-}
-
-// World normal of a hit: the object-space normal through the entered instances' local-to-world rows,
-// innermost first (CalculateSurfaceParams transforms Ng by the composed localToWorld,
-// SurfaceParameters.cpp:161-168; not the inverse transpose).
-__device__ __forceinline__ float3 world_normal(const HitRef& r, float3 ng) {
-    const InstanceRecord* recs[2] = {r.rec1, r.rec0};
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        if (!recs[k]) continue;
-        const float4* m = reinterpret_cast<const float4*>(recs[k]->l2w);
-        const float4 r0 = __ldg(m), r1 = __ldg(m + 1), r2 = __ldg(m + 2);
-        float x, y, z;
-        xform_vector(r0, r1, r2, ng.x, ng.y, ng.z, x, y, z);
-        ng = make_float3(x, y, z);
-    }
-    return ng;
+    return hit_ref_of<kInst>(S, kInst ? st.hinst[s] : make_uint2(0u, 0u), tri);
 }
 
 // Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
@@ -294,7 +226,7 @@ __global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_extend(PtParams P,
                                                           h, stack_mem + threadIdx.x, B, status);
                 P.st.hit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
                                     : make_float4(tfar, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
-                P.st.hinst[s] = found ? inst_indices(sc, h) : make_uint2(0u, 0u);
+                P.st.hinst[s] = found ? inst_indices(sc.insts, h) : make_uint2(0u, 0u);
             } else {
                 QueryHit h;
                 const bool found = Tracer<K>::template trace<false>(sc.nodes, sc.tris, q, h, stack_mem + threadIdx.x,

@@ -20,15 +20,32 @@ __device__ __forceinline__ QueryRay load_ray(const float4* rp) {
     return r;
 }
 
+// The hit as Embree reports it.  A quad's triangles are stored as records 2q (v0, v1, v3) and 2q + 1
+// (v2, v3, v1) with kind kTriQuadHalf: primID is q and the second triangle's (u', v') become (1 - u', 1 - v')
+// (RTC_GEOMETRY_TYPE_QUAD.3embree3); Ng is the hit triangle's.
+__device__ __forceinline__ void embree_hit(const float4& p0, const float4& p2, float& u, float& v, uint32_t& prim) {
+    prim = __float_as_uint(p0.w);
+    if (__float_as_uint(p2.w) == kTriQuadHalf) {
+        if (prim & 1u) {
+            u = __fsub_rn(1.0f, u);
+            v = __fsub_rn(1.0f, v);
+        }
+        prim >>= 1;
+    }
+}
+
 __device__ __forceinline__ void store_hit(SelRayHit* rh, const float4* __restrict__ tris, const QueryHit& h) {
     const float4* tp = tris + size_t(h.tri) * 3;
     const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
     const float3 ng = triangle_ng(p0, p1, p2);
+    float u = h.u, v = h.v;
+    uint32_t prim;
+    embree_hit(p0, p2, u, v, prim);
     float* base = reinterpret_cast<float*>(rh);
     base[8] = h.t;  // ray.tfar
     float4* hp = reinterpret_cast<float4*>(base + 12);
-    hp[0] = make_float4(ng.x, ng.y, ng.z, h.u);
-    hp[1] = make_float4(h.v, p0.w, p1.w, __uint_as_float(SEL_INVALID_GEOMETRY_ID));
+    hp[0] = make_float4(ng.x, ng.y, ng.z, u);
+    hp[1] = make_float4(v, __uint_as_float(prim), p1.w, __uint_as_float(SEL_INVALID_GEOMETRY_ID));
     reinterpret_cast<uint32_t*>(base)[20] = SEL_INVALID_GEOMETRY_ID;
 }
 
@@ -36,11 +53,14 @@ __device__ __forceinline__ void store_hit_instanced(SelRayHit* rh, const InstHit
     const float4* tp = h.tris + size_t(h.tri) * 3;
     const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
     const float3 ng = triangle_ng(p0, p1, p2);  // object space of the hit mesh
+    float u = h.u, v = h.v;
+    uint32_t prim;
+    embree_hit(p0, p2, u, v, prim);
     float* base = reinterpret_cast<float*>(rh);
     base[8] = h.t;
     float4* hp = reinterpret_cast<float4*>(base + 12);
-    hp[0] = make_float4(ng.x, ng.y, ng.z, h.u);
-    hp[1] = make_float4(h.v, p0.w, p1.w, __uint_as_float(h.inst[0]));
+    hp[0] = make_float4(ng.x, ng.y, ng.z, u);
+    hp[1] = make_float4(v, __uint_as_float(prim), p1.w, __uint_as_float(h.inst[0]));
     reinterpret_cast<uint32_t*>(base)[20] = h.inst[1];
 }
 
@@ -69,14 +89,10 @@ __global__ void __launch_bounds__(kQueryBlock)
 // (64 registers, 24 KB of shared-memory stacks per block).  A sweep of persistent variants that refill
 // finished lanes from per-warp ray blocks was slower on both coherent and incoherent rays (lanes lose
 // the lockstep that makes node fetches shared), so the hardware block scheduler does the balancing.
+// Postponing a lane's leaf triangles while few lanes of its warp test triangles (Ylitie, Karras, Laine 2017)
+// was slower too at every threshold tried (6, 10, 16 lanes: incoherent closest hit 1,382 / 1,376 / 1,356
+// against 1,418 Mrays/s without), with identical hits.
 constexpr int kWideBlocksPerSm = 8;
-
-// Postponed triangle tests in the query kernels: a lane defers its leaf's triangles while fewer than this many
-// lanes of its warp are testing triangles (0: never).
-#ifndef SEL_QUERY_POSTPONE_LANES
-#define SEL_QUERY_POSTPONE_LANES 8
-#endif
-constexpr int kPostponeLanes = SEL_QUERY_POSTPONE_LANES;
 
 template <bool kAnyHit>
 __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm)
@@ -87,7 +103,7 @@ __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm)
     if (i >= n) return;
     QueryHit h;
     uint32_t status = 0;
-    const bool found = trace_wide<kAnyHit, kPostponeLanes>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
+    const bool found = trace_wide<kAnyHit>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
                                            stack_mem + threadIdx.x, kQueryBlock, status);
     if (status) atomicOr(err, status);
     if (found) {

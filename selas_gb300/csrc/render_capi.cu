@@ -1,4 +1,5 @@
 // C ABI of the scene shading data and of the path-tracer entry points (include/selas.h).
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -185,6 +186,7 @@ static int upload_attrs(SelSceneTy* sc) {
     for (const MeshInput& m : sc->meshes) {
         if (!m.attr_n[0] && !m.attr_n[1] && !has_uvs(m)) continue;
         MeshAttrDev& t = table[m.geomID];
+        t.quads = m.quads ? 1u : 0u;
         t.indices = reinterpret_cast<const uint32_t*>(base + o_idx + ai * 4);
         std::memcpy(host.data() + o_idx + ai * 4, m.indices.data(), m.indices.size() * 4);
         ai += m.indices.size();
@@ -573,10 +575,29 @@ SelVcmSettings default_vcm_settings() {
 
 namespace sel {
 
+// The scene and every scene it instances (directly or below).
+static std::vector<const SelSceneTy*> material_scenes(const SelSceneTy* sc) {
+    std::vector<const SelSceneTy*> out{sc};
+    for (size_t i = 0; i < out.size(); ++i)
+        for (const auto& r : out[i]->referenced)
+            if (std::find(out.begin(), out.end(), r.first) == out.end()) out.push_back(r.first);
+    return out;
+}
+
+// Stored VCM vertices keep their material record's address in 56 bits: checked once the scene's (and its
+// instanced scenes') material tables are in HBM.
+int check_vcm_materials(const SelSceneTy* scene) {
+    for (const SelSceneTy* sc : material_scenes(scene))
+        if (reinterpret_cast<uint64_t>(sc->d_materials) >> 56)
+            return fail(SEL_ERR_INVALID_OPERATION, "material table above the 2^56 address range VCM vertices hold");
+    return SEL_OK;
+}
+
 int check_vcm_args(SelScene scene, const SelCamera* camera, const SelVcmSettings* settings) {
     if (!scene || !camera || !settings) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (!scene->committed) return fail(SEL_ERR_INVALID_OPERATION, "scene not committed");
-    if (scene->d_insts) return fail(SEL_ERR_INVALID_OPERATION, "VCM renders scenes without instances");
+    if (!instances_fresh(scene))
+        return fail(SEL_ERR_INVALID_OPERATION, "an instanced scene changed since this scene was committed");
     if (camera->width == 0 || camera->height == 0 || camera->width > 16384 || camera->height > 16384)
         return fail(SEL_ERR_INVALID_ARGUMENT, "viewport must be 1..16384 in each dimension");
     if (!(camera->fovDegrees > 0.0f && camera->fovDegrees < 180.0f))
@@ -618,6 +639,7 @@ int ensure_vcm_state(SelSceneTy* sc, uint32_t paths, uint32_t max_len) {
 int vcm_render_device(SelSceneTy* sc, const SelCamera& camera, const SelVcmSettings& settings, double* d_accum,
                       cudaStream_t stream) {
     if (int rc = sync_shading(sc)) return rc;
+    if (int rc = check_vcm_materials(sc)) return rc;
     const uint32_t paths = camera.width * camera.height;
     if (int rc = ensure_vcm_state(sc, paths, settings.maxPathLength)) return rc;
     const float radius0 = settings.radius != 0.0f ? settings.radius : vcm_default_radius(sc);
@@ -737,6 +759,9 @@ int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* f
     for (const MeshInput& m : scene->meshes)
         if (m.geomID == geomID) mesh = &m;
     if (!mesh) return fail(SEL_ERR_INVALID_ARGUMENT, "no geometry with this geomID");
+    if (mesh->quads)
+        return fail(SEL_ERR_INVALID_OPERATION,
+                    "Ptex on quad meshes (the separable bicubic filter) is not supported: triangle meshes only");
     if (face_count != mesh->indices.size() / 3)
         return fail(SEL_ERR_INVALID_ARGUMENT, "face_count must equal the geometry's triangle count");
     for (size_t i = 0; i < face_count; ++i) {

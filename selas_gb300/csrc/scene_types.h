@@ -36,10 +36,12 @@ static_assert(sizeof(MaterialDev) == 128, "MaterialDev must be 128 bytes");
 // Vertex attributes of one mesh the shading reads (by geomID): its triangles' vertex indices, shading normals
 // (slot 0, 3 floats per vertex) and tangents (slot 1, xyz + bitangent sign); null where absent.
 struct MeshAttrDev {
-    const uint32_t* indices;
+    const uint32_t* indices;  // 3 per stored triangle (a quad mesh: triangles 2q = (v0, v1, v3), 2q + 1 = (v2, v3, v1))
     const float* normals;
     const float4* tangents;
     const float2* uvs;  // slot 2
+    uint32_t quads;     // 1: a quad mesh, interpolated bilinearly over each quad
+    uint32_t pad;
 };
 
 struct ShadeView {

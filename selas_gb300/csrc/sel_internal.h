@@ -20,8 +20,10 @@ namespace sel {
 struct TriRecord {
     float v0[3]; uint32_t prim;
     float v1[3]; uint32_t geom;
-    float v2[3]; uint32_t pad;
+    float v2[3]; uint32_t kind;  // kTriPlain, or kTriQuadHalf: prim = 2 * quad + half (half 0: v0 v1 v3, 1: v2 v3 v1)
 };
+constexpr uint32_t kTriPlain = 0u;
+constexpr uint32_t kTriQuadHalf = 1u;
 static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 
 // 8-wide node with child boxes quantised to 8 bits per axis (80 bytes = 5 x uint4).
@@ -61,7 +63,8 @@ static_assert(sizeof(BinaryNode) == 64, "BinaryNode must be 64 bytes");
 struct MeshInput {
     uint32_t geomID;
     std::vector<float> vertices;   // xyz packed
-    std::vector<uint32_t> indices; // 3 per triangle
+    std::vector<uint32_t> indices; // 3 per triangle; a quad mesh holds each quad as two triangles (see quads)
+    bool quads = false;            // RTC_GEOMETRY_TYPE_QUAD: triangle 2q is (v0, v1, v3), 2q + 1 is (v2, v3, v1)
     std::vector<float> attr[4];    // per-vertex attributes (sel_scene_set_vertex_attribute), attr_n[slot] floats each
     uint32_t attr_n[4] = {0, 0, 0, 0};
 };

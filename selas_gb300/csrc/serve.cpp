@@ -488,6 +488,8 @@ int sel_server_submit(SelServer server, const SelJob* job, uint64_t* out_job_id)
         std::lock_guard<std::mutex> lock(sc->mu);
         if (int rc = set_device(sc->dev)) return rc;
         if (int rc = sync_shading(sc)) return rc;
+        if (job->integrator == SEL_INTEGRATOR_VCM)
+            if (int rc = check_vcm_materials(sc)) return rc;
     }
     std::unique_ptr<Job> j(new Job());
     j->desc = *job;

@@ -156,6 +156,47 @@ SEL_HD float attr_lerp(float a0, float a1, float a2, float u, float v) {
     return w * a0 + u * a1 + v * a2;
 }
 
+// Where a hit interpolates a mesh's vertex attributes (rtcInterpolate0).  A triangle: corners i0 i1 i2 with
+// weights (1 - u - v, u, v).  A quad of a quad mesh (stored as triangles 2q = (v0, v1, v3) and 2q + 1 =
+// (v2, v3, v1)): its four corners, bilinearly, t_uv = (1 - v)((1 - u) t0 + u t1) + v((1 - u) t3 + u t2)
+// (RTC_GEOMETRY_TYPE_QUAD.3embree3), at the quad's (u, v): the second triangle's (u', v') corrected to
+// (1 - u', 1 - v').
+struct AttrCorners {
+    uint32_t i[4];  // triangle: i0 i1 i2; quad: v0 v1 v2 v3
+    float u, v;
+    bool quad;
+};
+
+SEL_HD AttrCorners attr_corners(const MeshAttrDev* A, uint32_t prim, float u, float v) {
+    AttrCorners c;
+    c.quad = A->quads != 0u;
+    if (!c.quad) {
+        c.i[0] = A->indices[3 * prim];
+        c.i[1] = A->indices[3 * prim + 1];
+        c.i[2] = A->indices[3 * prim + 2];
+        c.i[3] = c.i[2];
+        c.u = u;
+        c.v = v;
+    } else {
+        const uint32_t* t = A->indices + 6 * size_t(prim >> 1);  // (v0, v1, v3), (v2, v3, v1)
+        c.i[0] = t[0];
+        c.i[1] = t[1];
+        c.i[2] = t[3];
+        c.i[3] = t[2];
+        c.u = (prim & 1u) ? 1.0f - u : u;
+        c.v = (prim & 1u) ? 1.0f - v : v;
+    }
+    return c;
+}
+
+// One component of an attribute with `stride` floats per vertex at the corners.
+SEL_HD float attr_at(const AttrCorners& c, const float* a, uint32_t stride, uint32_t k) {
+    if (!c.quad) return attr_lerp(a[stride * c.i[0] + k], a[stride * c.i[1] + k], a[stride * c.i[2] + k], c.u, c.v);
+    const float iu = 1.0f - c.u, iv = 1.0f - c.v;
+    return iv * (iu * a[stride * c.i[0] + k] + c.u * a[stride * c.i[1] + k]) +
+           c.v * (iu * a[stride * c.i[3] + k] + c.u * a[stride * c.i[2] + k]);
+}
+
 // Shading frame of a hit (CalculateSurfaceParams, SurfaceParameters.cpp:157-184): the normal interpolated from
 // the mesh's vertex normals where it has them (else the geometric normal), the tangent from its vertex tangents
 // with b = cross(n, t) x the interpolated sign (returned in `sign`), else an orthonormal basis around n (sign 1).
@@ -164,19 +205,17 @@ template <typename Xf>
 SEL_HD void shading_frame(const MeshAttrDev* A, uint32_t prim, float u, float v, float3 ng, Xf xf, float3& n,
                           float3& t, float3& b, float& sign) {
     float3 nrm = ng;
+    AttrCorners c;
+    if (A) c = attr_corners(A, prim, u, v);
     if (A && A->normals) {
-        const uint32_t i0 = A->indices[3 * prim], i1 = A->indices[3 * prim + 1], i2 = A->indices[3 * prim + 2];
         const float* a = A->normals;
-        nrm = f3(attr_lerp(a[3 * i0], a[3 * i1], a[3 * i2], u, v), attr_lerp(a[3 * i0 + 1], a[3 * i1 + 1], a[3 * i2 + 1], u, v),
-                 attr_lerp(a[3 * i0 + 2], a[3 * i1 + 2], a[3 * i2 + 2], u, v));
+        nrm = f3(attr_at(c, a, 3, 0), attr_at(c, a, 3, 1), attr_at(c, a, 3, 2));
     }
     n = normalize(xf(nrm));
     if (A && A->tangents) {
-        const uint32_t i0 = A->indices[3 * prim], i1 = A->indices[3 * prim + 1], i2 = A->indices[3 * prim + 2];
-        const float4 a0 = A->tangents[i0], a1 = A->tangents[i1], a2 = A->tangents[i2];
-        const float3 tl = f3(attr_lerp(a0.x, a1.x, a2.x, u, v), attr_lerp(a0.y, a1.y, a2.y, u, v),
-                             attr_lerp(a0.z, a1.z, a2.z, u, v));
-        sign = attr_lerp(a0.w, a1.w, a2.w, u, v);
+        const float* a = reinterpret_cast<const float*>(A->tangents);
+        const float3 tl = f3(attr_at(c, a, 4, 0), attr_at(c, a, 4, 1), attr_at(c, a, 4, 2));
+        sign = attr_at(c, a, 4, 3);
         t = xf(tl);
         b = cross(n, t) * sign;
     } else {

@@ -10,6 +10,7 @@
 #include <cstdint>
 
 #include "scene_types.h"
+#include "shading.cuh"
 #include "vecmath.cuh"
 
 namespace sel {
@@ -28,11 +29,10 @@ SEL_HD float3 tex2d_texel(const float4* tex, int w, int h, int s, int t) {
 SEL_HD float3 tex2d_base_colour(const MaterialDev& m, const MeshAttrDev* attr, uint32_t prim, float bu, float bv) {
     float su = 0.0f, sv = 0.0f;
     if (attr && attr->uvs) {
-        const uint32_t* idx = attr->indices + size_t(prim) * 3;
-        const float2 a = attr->uvs[idx[0]], b = attr->uvs[idx[1]], c = attr->uvs[idx[2]];
-        const float w = 1.0f - bu - bv;
-        su = w * a.x + bu * b.x + bv * c.x;
-        sv = w * a.y + bu * b.y + bv * c.y;
+        const AttrCorners c = attr_corners(attr, prim, bu, bv);
+        const float* a = reinterpret_cast<const float*>(attr->uvs);
+        su = attr_at(c, a, 2, 0);
+        sv = attr_at(c, a, 2, 1);
     }
     const float4* tex = reinterpret_cast<const float4*>(uint64_t(m.tex_lo) | (uint64_t(m.tex_hi) << 32));
     const int w = int(m.tex_width), h = int(m.tex_height);

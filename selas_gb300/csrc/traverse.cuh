@@ -211,39 +211,20 @@ __device__ __forceinline__ bool wide_visit(WideState& s, const uint4* __restrict
             }
         }
     }
-    // a group without hit children is empty (its internal-child mask only indexes hit children)
-    s.group = make_uint2(n1.x, new_hits ? (new_hits << 24) | imask : 0u);
+    s.group = make_uint2(n1.x, (new_hits << 24) | imask);
     tbase = n1.y;
     return true;
 }
 
 // One traversal step.  Returns true when the ray is finished (any-hit: on the first hit).
-//
-// Postponed triangle tests (Ylitie, Karras, Laine, "Efficient Incoherent Ray Traversal on GPUs Through
-// Compressed Wide BVHs", HPG 2017, sec. 4): when fewer than kPostpone lanes of the warp are testing triangles
-// and this lane still has nodes to visit, it pushes its remaining triangles as a group of their own (bits 0..23:
-// records tbase + bit; no hit bits, which is what tells it from a node group) and goes on traversing, so that
-// the warp's lanes meet again in the node loop instead of idling while a few lanes test leaves.  A popped
-// triangle group is tested in the next step.  Results do not depend on the order of the tests (smallest t, then
-// smallest key), so every ordering returns the same hit.
-template <bool kAnyHit, int kPostpone = 0>
+template <bool kAnyHit>
 __device__ __forceinline__ bool wide_step(WideState& s, const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                           uint2* stack, int stride, uint32_t& status) {
     uint32_t tmask = 0, tbase = 0;
     if (s.group.y & 0xff000000u) {
         if (!wide_visit<kWideStack>(s, nodes, stack, stride, status, tmask, tbase)) return true;
-    } else if (kPostpone > 0) {  // a postponed triangle group (never set when kPostpone == 0)
-        tmask = s.group.y;
-        tbase = s.group.x;
-        s.group = make_uint2(0u, 0u);
     }
     while (tmask) {
-        if (kPostpone > 0 && (s.group.y & 0xff000000u) && s.sp < kWideStack &&
-            __popc(__activemask()) < kPostpone) {
-            stack[s.sp * stride] = make_uint2(tbase, tmask);
-            ++s.sp;
-            break;
-        }
         const int b = __ffs(tmask) - 1;
         tmask &= tmask - 1u;
         const uint32_t ti = tbase + uint32_t(b);
@@ -273,7 +254,7 @@ __device__ __forceinline__ bool wide_step(WideState& s, const uint4* __restrict_
 }
 
 // Whole-ray form (one thread, one ray).
-template <bool kAnyHit, int kPostpone = 0>
+template <bool kAnyHit>
 __device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
                                            const QueryRay& r, QueryHit& hit, uint2* stack, int stride,
                                            uint32_t& status) {
@@ -283,7 +264,7 @@ __device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, cons
     }
     WideState s;
     wide_init(s, r);
-    while (!wide_step<kAnyHit, kPostpone>(s, nodes, tris, stack, stride, status)) {}
+    while (!wide_step<kAnyHit>(s, nodes, tris, stack, stride, status)) {}
     hit = s.hit;
     return s.hit.tri != 0xffffffffu;
 }

@@ -28,6 +28,7 @@
 
 #include "capi_internal.h"
 #include "graph.h"
+#include "hitref.cuh"
 #include "ibl.cuh"
 #include "ptex.cuh"
 #include "radix.cuh"
@@ -59,6 +60,7 @@ struct VcmParams {
     uint32_t ptex_face_count;
     const MeshAttrDev* attrs;
     uint32_t attr_count;
+    const InstanceRecord* insts;  // the scene's instance table (null: no instances)
     CameraDev cam;
     float image_plane;
     uint32_t width, height, npaths, max_len, slots;
@@ -75,7 +77,7 @@ struct VHit {
     float3 pos, n, view;
     float err, cont, bsign;  // bsign: the shading frame's bitangent sign (b = cross(n, t) x bsign)
     Surface s;
-    uint32_t mat;
+    const MaterialDev* mat;  // the hit mesh's material record (its scene's table: the rendered one or an instance's)
     bool delta, transparent;
 };
 
@@ -93,14 +95,27 @@ constexpr int kVertF4 = 6;
 struct LightVertex {
     float3 pos, n, view, thr, base, t;
     float dvcm, dvc, dvm, bsign;
-    uint32_t len, mat;
+    uint32_t len;
+    const MaterialDev* mat;
 };
+
+// A stored vertex's path length (at most 32) and the address of its material record share two words: the length
+// in bits 0..7 of one with address bits 32..55 above it, address bits 0..31 in the other (device addresses
+// lie below 2^56; the render checks the material tables it hands out).
+__device__ __forceinline__ uint32_t pack_len(uint32_t len, const MaterialDev* m) {
+    return len | (uint32_t(reinterpret_cast<uint64_t>(m) >> 32) << 8);
+}
+__device__ __forceinline__ uint32_t mat_lo(const MaterialDev* m) { return uint32_t(reinterpret_cast<uint64_t>(m)); }
+__device__ __forceinline__ uint32_t unpack_len(uint32_t w) { return w & 0xffu; }
+__device__ __forceinline__ const MaterialDev* unpack_mat(uint32_t len_word, uint32_t lo) {
+    return reinterpret_cast<const MaterialDev*>((uint64_t(len_word >> 8) << 32) | lo);
+}
 
 
 
 __device__ __forceinline__ void store_vertex(float4* v, const VHit& h, const PathState& st) {
-    v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, __uint_as_float(st.len));
-    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(h.mat));
+    v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, __uint_as_float(pack_len(st.len, h.mat)));
+    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(mat_lo(h.mat)));
     v[2] = make_float4(h.view.x, h.view.y, h.view.z, st.dvcm);
     v[3] = make_float4(st.thr.x, st.thr.y, st.thr.z, st.dvc);
     v[4] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, st.dvm);
@@ -111,9 +126,9 @@ __device__ __forceinline__ LightVertex load_vertex(const float4* v) {
     const float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], g = v[5];
     LightVertex lv;
     lv.pos = f3(a.x, a.y, a.z);
-    lv.len = __float_as_uint(a.w);
+    lv.len = unpack_len(__float_as_uint(a.w));
     lv.n = f3(b.x, b.y, b.z);
-    lv.mat = __float_as_uint(b.w);
+    lv.mat = unpack_mat(__float_as_uint(a.w), __float_as_uint(b.w));
     lv.view = f3(c.x, c.y, c.z);
     lv.dvcm = c.w;
     lv.thr = f3(d.x, d.y, d.z);
@@ -245,27 +260,28 @@ __device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const
 
 // Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
 // kPretex: the Ptex base colour was filtered by k_vtexture into P.st.base[s] (material-sorted bounces).
-template <bool kPretex>
+template <bool kPretex, bool kInst>
 __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir, float4 hit, VHit& h,
                           uint32_t& status) {
     const uint32_t tri = __float_as_uint(hit.w);
-    const float4* tp = P.tris + size_t(tri) * 3;
-    const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+    const HitRef hr = hit_ref_of<kInst>(P, kInst ? P.st.phinst[s] : make_uint2(0u, 0u), tri);
+    const float4 p0 = __ldg(hr.tp), p1 = __ldg(hr.tp + 1), p2 = __ldg(hr.tp + 2);
     const uint32_t geom = __float_as_uint(p1.w);
-    const uint32_t mi = geom < P.material_count ? geom : 0;
-    const MaterialDev& m = P.materials[mi];
+    const uint32_t mi = geom < hr.mat_count ? geom : 0;
+    const MaterialDev& m = hr.mats[mi];
     h.pos = f3(org.x + hit.x * dir.x, org.y + hit.x * dir.y, org.z + hit.x * dir.z);
     h.err = 32.0f * 1.19209e-07f * fmaxf(fmaxf(fabsf(h.pos.x), fabsf(h.pos.y)), fmaxf(fabsf(h.pos.z), hit.x));
     float3 base = ld3(m.base_color);
-    const MeshAttrDev* attr = geom < P.attr_count ? P.attrs + geom : nullptr;
+    const MeshAttrDev* attr = geom < hr.attr_count ? hr.attrs + geom : nullptr;
     if (m.flags & kMaterialTextured) {
         if constexpr (kPretex) {
             const float4 b = P.st.base[s];
             base = f3(b.x, b.y, b.z);
         } else if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
-                      hit.y, hit.z, base, pstatus);
+            ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
+                      static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                      hit.z, base, pstatus);
             status |= pstatus;
         } else {
             base = tex2d_base_colour(m, attr, __float_as_uint(p0.w), hit.y, hit.z);
@@ -273,12 +289,12 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
     }
     h.view = -dir;
     float3 fn, ft, fb;
-    shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2), [](float3 x) { return x; }, fn, ft,
-                  fb, h.bsign);
+    shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2),
+                  [&](float3 x) { return kInst ? world_normal(hr, x) : x; }, fn, ft, fb, h.bsign);
     h.s = make_surface_frame(m, ft, fn, fb, h.view, pow3(base, 2.2f));
     h.n = h.s.n;
     h.cont = continuation_probability(h.s);
-    h.mat = mi;
+    h.mat = &m;
     h.delta = m.shader == kDiracTransparent;
     h.transparent = (m.flags & kMaterialTransparent) != 0u;
 }
@@ -458,11 +474,20 @@ __global__ void __launch_bounds__(B, 1024 / B) k_extend(VcmParams P, int cur) {
             QueryRay q;
             q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = 0.0f;
             q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = kFloatMax;
-            QueryHit h;
-            const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B,
-                                                                status);
-            P.st.phit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
-                                 : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+            if constexpr (K == 2) {
+                InstHit h;
+                const bool found = trace_instanced<false>(static_cast<const uint4*>(P.nodes), P.tris, P.insts, q, h,
+                                                          stack_mem + threadIdx.x, B, status);
+                P.st.phit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                     : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+                P.st.phinst[s] = found ? inst_indices(P.insts, h) : make_uint2(0u, 0u);
+            } else {
+                QueryHit h;
+                const bool found = Tracer<K>::template trace<false>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B,
+                                                                    status);
+                P.st.phit[s] = found ? make_float4(h.t, h.u, h.v, __uint_as_float(h.tri))
+                                     : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
+            }
         }
     }
     if (status) atomicOr(P.err, status);
@@ -488,9 +513,16 @@ __global__ void __launch_bounds__(B, 1024 / B) k_shadow(VcmParams P) {
                 QueryRay q;
                 q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
                 q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
-                QueryHit h;
-                if (!Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B, status))
-                    splat(P.accum, __float_as_uint(c.w), f3(c.x, c.y, c.z));
+                bool hit;
+                if constexpr (K == 2) {
+                    InstHit h;
+                    hit = trace_instanced<true>(static_cast<const uint4*>(P.nodes), P.tris, P.insts, q, h,
+                                                stack_mem + threadIdx.x, B, status);
+                } else {
+                    QueryHit h;
+                    hit = Tracer<K>::template trace<true>(P.nodes, P.tris, q, h, stack_mem + threadIdx.x, B, status);
+                }
+                if (!hit) splat(P.accum, __float_as_uint(c.w), f3(c.x, c.y, c.z));
             }
         }
     }
@@ -499,7 +531,7 @@ __global__ void __launch_bounds__(B, 1024 / B) k_shadow(VcmParams P) {
 
 // Light sub-path vertices (EvaluateLightPaths, VCM.cpp:502-561): MIS update, stored vertex, connection to
 // the camera (ConnectLightPathToCamera, VCM.cpp:190-233; tech report sec. 5.3) and scattering.
-template <bool kSorted>
+template <bool kSorted, bool kInst>
 __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const uint32_t* in_queue) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[cur];
@@ -518,7 +550,7 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const 
             const float4 hit = P.st.phit[s];
             if (__float_as_uint(hit.w) != 0xffffffffu) {
                 PathState st = load_path(P, s);
-                make_vhit<kSorted>(P, s, st.org, st.dir, hit, h, status);
+                make_vhit<kSorted, kInst>(P, s, st.org, st.dir, hit, h, status);
                 const float3 seg = h.pos - st.org;
                 const float d2 = dot(seg, seg);
                 const float cos_in = fabsf(dot(h.n, h.view));
@@ -578,11 +610,13 @@ __global__ void __launch_bounds__(kBlock) k_l_shade(VcmParams P, int cur, const 
 // 1 + shader * 4 + 2 (Ptex) + 1 (transparent)), then the Ptex filter of the sorted hits in a kernel of its own,
 // so the shading kernels run one kind of surface per warp and carry no filter code.
 // ---------------------------------------------------------------------------------------------------
+template <bool kInst>
 __device__ __forceinline__ uint32_t vmaterial_class(const VcmParams& P, uint32_t s) {
     const uint32_t tri = __float_as_uint(P.st.phit[s].w);
     if (tri == 0xffffffffu) return 0u;
-    const uint32_t geom = __float_as_uint(__ldg(P.tris + size_t(tri) * 3 + 1).w);
-    const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+    const HitRef hr = hit_ref_of<kInst>(P, kInst ? P.st.phinst[s] : make_uint2(0u, 0u), tri);
+    const uint32_t geom = __float_as_uint(__ldg(hr.tp + 1).w);
+    const MaterialDev& m = hr.mats[geom < hr.mat_count ? geom : 0];
     const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
     return 1u + shader * 4u + ((m.flags & kMaterialTextured) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u);
 }
@@ -591,12 +625,13 @@ __global__ void k_vclass_reset(uint32_t* counters) {
     if (threadIdx.x < 32) counters[32 + threadIdx.x] = 0u;
 }
 
+template <bool kInst>
 __global__ void __launch_bounds__(kBlock) k_vclassify(VcmParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
         const bool valid = e < n;
-        const uint32_t c = valid ? vmaterial_class(P, P.st.queue[cur][e]) : 0xffu;
+        const uint32_t c = valid ? vmaterial_class<kInst>(P, P.st.queue[cur][e]) : 0xffu;
         if (valid) P.st.cls[e] = c;
         const uint32_t peers = __match_any_sync(0xffffffffu, c);
         const uint32_t lane = threadIdx.x & 31u;
@@ -630,6 +665,7 @@ __global__ void __launch_bounds__(kBlock) k_vclass_scatter(VcmParams P, int cur)
     }
 }
 
+template <bool kInst>
 __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
@@ -638,19 +674,20 @@ __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
         const float4 hit = P.st.phit[s];
         const uint32_t tri = __float_as_uint(hit.w);
         if (tri == 0xffffffffu) continue;
-        const float4* tp = P.tris + size_t(tri) * 3;
-        const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1);
+        const HitRef hr = hit_ref_of<kInst>(P, kInst ? P.st.phinst[s] : make_uint2(0u, 0u), tri);
+        const float4 p0 = __ldg(hr.tp), p1 = __ldg(hr.tp + 1);
         const uint32_t geom = __float_as_uint(p1.w);
-        const MaterialDev& m = P.materials[geom < P.material_count ? geom : 0];
+        const MaterialDev& m = hr.mats[geom < hr.mat_count ? geom : 0];
         if (!(m.flags & kMaterialTextured)) continue;
         float3 base = ld3(m.base_color);
         if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_eval(P.ptex_faces, int(P.ptex_face_count), P.ptex_texels, int(m.ptex_base + __float_as_uint(p0.w)),
-                      hit.y, hit.z, base, pstatus);
+            ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
+                      static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                      hit.z, base, pstatus);
             status |= pstatus;
         } else {
-            base = tex2d_base_colour(m, geom < P.attr_count ? P.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
+            base = tex2d_base_colour(m, geom < hr.attr_count ? hr.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
                                      hit.z);
         }
         P.st.base[s] = make_float4(base.x, base.y, base.z, 0.0f);
@@ -754,15 +791,16 @@ constexpr int kCamF4 = 7;
 struct CameraVertex {
     float3 pos, n, view, base, thr, t;
     float err, cont, dvcm, dvc, dvm, bsign;
-    uint32_t mat, pixel, len, transparent;
+    uint32_t pixel, len, transparent;
+    const MaterialDev* mat;
 };
 
 __device__ __forceinline__ void store_camera_vertex(float4* v, const VHit& h, const PathState& st, uint32_t pixel) {
     v[0] = make_float4(h.pos.x, h.pos.y, h.pos.z, h.err);
-    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(h.mat));
+    v[1] = make_float4(h.n.x, h.n.y, h.n.z, __uint_as_float(mat_lo(h.mat)));
     v[2] = make_float4(h.view.x, h.view.y, h.view.z, h.cont);
     v[3] = make_float4(h.s.base_color.x, h.s.base_color.y, h.s.base_color.z, __uint_as_float(pixel));
-    v[4] = make_float4(st.thr.x, st.thr.y, st.thr.z, __uint_as_float(st.len));
+    v[4] = make_float4(st.thr.x, st.thr.y, st.thr.z, __uint_as_float(pack_len(st.len, h.mat)));
     v[5] = make_float4(st.dvcm, st.dvc, st.dvm, __uint_as_float(h.transparent ? 1u : 0u));
     v[6] = make_float4(h.s.t.x, h.s.t.y, h.s.t.z, h.bsign);
 }
@@ -773,13 +811,13 @@ __device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
     cv.pos = f3(a.x, a.y, a.z);
     cv.err = a.w;
     cv.n = f3(b.x, b.y, b.z);
-    cv.mat = __float_as_uint(b.w);
+    cv.mat = unpack_mat(__float_as_uint(e.w), __float_as_uint(b.w));
     cv.view = f3(c.x, c.y, c.z);
     cv.cont = c.w;
     cv.base = f3(d.x, d.y, d.z);
     cv.pixel = __float_as_uint(d.w);
     cv.thr = f3(e.x, e.y, e.z);
-    cv.len = __float_as_uint(e.w);
+    cv.len = unpack_len(__float_as_uint(e.w));
     cv.dvcm = f.x;
     cv.dvc = f.y;
     cv.dvm = f.z;
@@ -789,7 +827,7 @@ __device__ __forceinline__ CameraVertex load_camera_vertex(const float4* v) {
     return cv;
 }
 
-template <bool kSorted>
+template <bool kSorted, bool kInst>
 __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const uint32_t* in_queue) {
     const VcmConsts c = P.st.consts[*P.st.iter];
     const uint32_t n = P.st.counters[cur];
@@ -813,7 +851,7 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const 
             if (__float_as_uint(hit.w) != 0xffffffffu) {
                 hit_ok = true;
                 st = load_path(P, s);
-                make_vhit<kSorted>(P, s, st.org, st.dir, hit, h, status);
+                make_vhit<kSorted, kInst>(P, s, st.org, st.dir, hit, h, status);
                 const float3 seg = h.pos - st.org;
                 const float d2 = dot(seg, seg);
                 const float cos_in = fabsf(dot(h.n, h.view));
@@ -887,7 +925,9 @@ __global__ void __launch_bounds__(kBlock) k_c_shade(VcmParams P, int cur, const 
                     // light vertices of path s that a connection may join (path length bound)
                     const uint32_t lcount = P.st.vcount[s];
                     const float4* lslots = P.st.verts + size_t(s) * P.slots * kVertF4;
-                    while (nvc < lcount && __float_as_uint(lslots[size_t(nvc) * kVertF4].w) + 1 + st.len <= P.max_len) ++nvc;
+                    while (nvc < lcount &&
+                           unpack_len(__float_as_uint(lslots[size_t(nvc) * kVertF4].w)) + 1 + st.len <= P.max_len)
+                        ++nvc;
                 }
             } else if (P.ibl) {
                 // the path leaves the scene: the environment's radiance with the camera-hit weight (ConnectToSkyLight,
@@ -949,12 +989,12 @@ __global__ void __launch_bounds__(kBlock) k_c_connect(VcmParams P) {
             dir = lv.pos - cv.pos;
             const float dist2 = dot(dir, dir), dist = sqrtf(dist2);
             dir = dir * (1.0f / dist);
-            const Surface cs = make_surface_frame(P.materials[cv.mat], cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
+            const Surface cs = make_surface_frame(*cv.mat, cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
                                                   cv.base);
             float cfwd, crev, lfwd, lrev;
             const float3 cf = bsdf_evaluate(cs, cv.view, dir, cfwd, crev);
             if (nonzero(cf)) {
-                const Surface ls = make_surface_frame(P.materials[lv.mat], lv.t, lv.n, cross(lv.n, lv.t) * lv.bsign,
+                const Surface ls = make_surface_frame(*lv.mat, lv.t, lv.n, cross(lv.n, lv.t) * lv.bsign,
                                                       lv.view, lv.base);
                 const float lcont = continuation_probability(ls);
                 const float3 lfa = bsdf_evaluate(ls, -dir, lv.view, lrev, lfwd);
@@ -1044,7 +1084,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_c_merge(VcmParams P) {
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 7);
         if (total == 0) continue;
         const CameraVertex cv = load_camera_vertex(rec);
-        const Surface cs = make_surface_frame(P.materials[cv.mat], cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
+        const Surface cs = make_surface_frame(*cv.mat, cv.t, cv.n, cross(cv.n, cv.t) * cv.bsign, cv.view,
                                               cv.base);
         float3 merged = f3(0.0f);
         // two phases so that the BSDF work runs on full warps: lanes test 32 candidates at a time against
@@ -1057,7 +1097,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_c_merge(VcmParams P) {
             const LightVertex lv = load_vertex(P.st.verts + size_t(vslot) * kVertF4);
             if (cv.len + lv.len > P.max_len) return;
             // the reference merges only between surfaces of the same transparency (VCM.cpp:372-375)
-            const uint32_t lt = (P.materials[lv.mat].flags & kMaterialTransparent) ? 1u : 0u;
+            const uint32_t lt = (lv.mat->flags & kMaterialTransparent) ? 1u : 0u;
             if (cv.transparent != lt) return;
             float fwd, rev;
             const float3 fc = bsdf_evaluate(cs, cv.view, lv.view, fwd, rev);
@@ -1146,6 +1186,7 @@ void vcm_layout(VcmState& st, Take take, uint32_t paths, uint32_t max_len, uint3
     st.plen = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.prng = reinterpret_cast<uint64_t*>(take(8ull * paths));
     st.phit = reinterpret_cast<float4*>(take(16ull * paths));
+    st.phinst = reinterpret_cast<uint2*>(take(8ull * paths));
     st.queue[0] = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.queue[1] = reinterpret_cast<uint32_t*>(take(4ull * paths));
     st.queue_sorted = reinterpret_cast<uint32_t*>(take(4ull * paths));
@@ -1228,6 +1269,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     P.ptex_face_count = sc.ptex_face_count;
     P.attrs = sc.attrs;
     P.attr_count = sc.attr_count;
+    P.insts = sc.insts;
     P.cam.x = make_float3(cam.cam.x[0], cam.cam.x[1], cam.cam.x[2]);
     P.cam.y = make_float3(cam.cam.y[0], cam.cam.y[1], cam.cam.y[2]);
     P.cam.z = make_float3(cam.cam.z[0], cam.cam.z[1], cam.cam.z[2]);
@@ -1281,29 +1323,43 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, kBlock, 0);
         return sms * std::max(blocks, 1);
     };
+    // scenes with instances: the instanced traversal (128-thread blocks, 4 per SM: its 40-entry stacks) and the
+    // shading kernels that read a hit's scene through its instances
+    const bool inst = sc.insts != nullptr;
+    const int inst_grid = sms * 4;
     auto extend = [&](cudaStream_t stream, int cur) {
-        if (sc.bvh_kind != 0) k_extend<1, 128><<<trace_grid, 128, 0, stream>>>(P, cur);
+        if (inst) k_extend<2, 128><<<inst_grid, 128, 0, stream>>>(P, cur);
+        else if (sc.bvh_kind != 0) k_extend<1, 128><<<trace_grid, 128, 0, stream>>>(P, cur);
         else if (tb == 256) k_extend<0, 256><<<trace_grid, 256, 0, stream>>>(P, cur);
         else k_extend<0, 128><<<trace_grid, 128, 0, stream>>>(P, cur);
     };
     auto shadow = [&](cudaStream_t stream) {
-        if (sc.bvh_kind != 0) k_shadow<1, 128><<<trace_grid, 128, 0, stream>>>(P);
+        if (inst) k_shadow<2, 128><<<inst_grid, 128, 0, stream>>>(P);
+        else if (sc.bvh_kind != 0) k_shadow<1, 128><<<trace_grid, 128, 0, stream>>>(P);
         else if (tb == 256) k_shadow<0, 256><<<trace_grid, 256, 0, stream>>>(P);
         else k_shadow<0, 128><<<trace_grid, 128, 0, stream>>>(P);
     };
-    const bool sort = sc.sort_hint != 0;
-    const int l_grid = wave(reinterpret_cast<const void*>(sort ? &k_l_shade<true> : &k_l_shade<false>));
-    const int c_grid = wave(reinterpret_cast<const void*>(sort ? &k_c_shade<true> : &k_c_shade<false>));
+    const bool sort = sc.sort_hint != 0 || inst;
+    const void* l_fn = inst ? reinterpret_cast<const void*>(&k_l_shade<true, true>)
+                            : sort ? reinterpret_cast<const void*>(&k_l_shade<true, false>)
+                                   : reinterpret_cast<const void*>(&k_l_shade<false, false>);
+    const void* c_fn = inst ? reinterpret_cast<const void*>(&k_c_shade<true, true>)
+                            : sort ? reinterpret_cast<const void*>(&k_c_shade<true, false>)
+                                   : reinterpret_cast<const void*>(&k_c_shade<false, false>);
+    const int l_grid = wave(l_fn);
+    const int c_grid = wave(c_fn);
     const int connect_grid = wave(reinterpret_cast<const void*>(&k_c_connect));
     const int merge_grid = wave(reinterpret_cast<const void*>(&k_c_merge));
     // material-class sort and Ptex of a bounce's hits; returns the queue the shading kernel reads
     auto sort_hits = [&](cudaStream_t stream, int cur) -> const uint32_t* {
         if (!sort) return st.queue[cur];
         k_vclass_reset<<<1, 32, 0, stream>>>(st.counters);
-        k_vclassify<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        if (inst) k_vclassify<true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        else k_vclassify<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
         k_vclass_offsets<<<1, 32, 0, stream>>>(st.counters);
         k_vclass_scatter<<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        k_vtexture<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        if (inst) k_vtexture<true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        else k_vtexture<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
         return st.queue_sorted;
     };
     // one pass; identical launches every pass (the pass reads its constants through st.iter)
@@ -1316,8 +1372,9 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
             extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
-            if (sort) k_l_shade<true><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
-            else k_l_shade<false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
+            if (inst) k_l_shade<true, true><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
+            else if (sort) k_l_shade<true, false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
+            else k_l_shade<false, false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
             shadow(stream);
         }
         // hash grid over the stored vertices
@@ -1344,8 +1401,9 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             k_bounce_reset<<<1, 32, 0, stream>>>(st.counters, cur ^ 1);
             extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
-            if (sort) k_c_shade<true><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
-            else k_c_shade<false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
+            if (inst) k_c_shade<true, true><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
+            else if (sort) k_c_shade<true, false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
+            else k_c_shade<false, false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
             k_c_connect<<<connect_grid, kBlock, 0, stream>>>(P);
             k_c_merge<<<merge_grid, kBlock, 0, stream>>>(P);
             shadow(stream);

@@ -44,6 +44,7 @@ struct VcmState {
     uint32_t* plen;       // path length in segments
     uint64_t* prng;       // PCG32 state (the stream is a function of the pass and the slot)
     float4* phit;         // t, u, v, triangle bits (all ones: miss)
+    uint2* phinst;        // instances entered to the hit (scenes with instances: 1 + table index per level)
     uint32_t* queue[2];   // live path slots, ping-pong between bounces
     uint32_t* queue_sorted;  // the current queue ordered by material class (counting sort)
     uint32_t* cls;        // material class of each current queue entry

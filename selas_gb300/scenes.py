@@ -21,10 +21,24 @@ import numpy as np
 @dataclass
 class TriangleScene:
     meshes: list = field(default_factory=list)  # (geom_id, vertices (n,3) f32, indices (m,3) u32)
+    quad_geoms: set = field(default_factory=set)  # geomIDs of quad meshes (their indices hold triangle pairs)
 
     def add(self, geom_id: int, vertices: np.ndarray, indices: np.ndarray) -> None:
         self.meshes.append((int(geom_id), np.ascontiguousarray(vertices, np.float32),
                             np.ascontiguousarray(indices, np.uint32)))
+
+    def add_quads(self, geom_id: int, vertices: np.ndarray, quads: np.ndarray) -> None:
+        """A quad mesh, held as Embree holds it: quad q is the triangles 2q = (v0, v1, v3) and 2q + 1 = (v2, v3, v1)
+        (RTC_GEOMETRY_TYPE_QUAD.3embree3); soup() numbers those triangles 2q and 2q + 1."""
+        q = np.ascontiguousarray(quads, np.uint32).reshape(-1, 4)
+        pairs = np.stack([q[:, 0], q[:, 1], q[:, 3], q[:, 2], q[:, 3], q[:, 1]], 1).reshape(-1, 3)
+        self.add(geom_id, vertices, pairs)
+        self.quad_geoms.add(int(geom_id))
+
+    @staticmethod
+    def quads_of(pairs: np.ndarray) -> np.ndarray:
+        p = np.asarray(pairs).reshape(-1, 6)
+        return np.stack([p[:, 0], p[:, 1], p[:, 3], p[:, 2]], 1)
 
     @property
     def triangle_count(self) -> int:
@@ -41,7 +55,23 @@ class TriangleScene:
 
     def attach_to(self, scene) -> None:
         for gid, v, idx in self.meshes:
-            scene.attach_triangle_mesh(gid, v, idx)
+            if gid in self.quad_geoms:
+                scene.attach_quad_mesh(gid, v, self.quads_of(idx))
+            else:
+                scene.attach_triangle_mesh(gid, v, idx)
+
+    def embree_hits(self, rayhits: np.ndarray) -> None:
+        """Turns hits on the soup's triangles (primID = soup numbering) into what Embree reports: on a quad mesh
+        primID = quad and the second triangle's (u', v') -> (1 - u', 1 - v') in FP32."""
+        if not self.quad_geoms:
+            return
+        hit = rayhits["geomID"] != 0xFFFFFFFF
+        q = hit & np.isin(rayhits["geomID"], np.array(sorted(self.quad_geoms), np.uint32))
+        second = q & (rayhits["primID"] & 1 == 1)
+        one = np.float32(1.0)
+        rayhits["u"][second] = one - rayhits["u"][second]
+        rayhits["v"][second] = one - rayhits["v"][second]
+        rayhits["primID"][q] >>= 1
 
     def bounds(self):
         lo = np.min([m[1].min(axis=0) for m in self.meshes], axis=0)
@@ -208,8 +238,8 @@ class RenderScene:
             sc.set_texture(gid, img)
 
     def attribute_soup(self):
-        """Per-triangle corner normals (n, 9), tangents (n, 12), flags (1 normals, 2 tangents, 4 uvs) and uvs
-        (n, 6), in soup() order, for the oracle."""
+        """Per-triangle corner normals (n, 9), tangents (n, 12), flags (1 normals, 2 tangents, 4 uvs, 8 the
+        triangle is half of a quad) and uvs (n, 6), in soup() order, for the oracle."""
         ns, ts, fs, us = [], [], [], []
         for gid, v, idx in self.geometry.meshes:
             a = (self.attrs or {}).get(gid, {})
@@ -218,8 +248,8 @@ class RenderScene:
             ns.append(np.asarray(n, np.float32)[idx].reshape(m, 9) if n is not None else np.zeros((m, 9), np.float32))
             ts.append(np.asarray(t, np.float32)[idx].reshape(m, 12) if t is not None else np.zeros((m, 12), np.float32))
             us.append(np.asarray(uv, np.float32)[idx].reshape(m, 6) if uv is not None else np.zeros((m, 6), np.float32))
-            fs.append(np.full(m, (1 if n is not None else 0) | (2 if t is not None else 0) | (4 if uv is not None else 0),
-                              np.uint8))
+            fs.append(np.full(m, (1 if n is not None else 0) | (2 if t is not None else 0) | (4 if uv is not None else 0)
+                              | (8 if gid in self.geometry.quad_geoms else 0), np.uint8))
         if not ns:
             return (np.zeros((0, 9), np.float32), np.zeros((0, 12), np.float32), np.zeros(0, np.uint8),
                     np.zeros((0, 6), np.float32))

@@ -128,14 +128,49 @@ def test_gpu_identity_instance_equals_flat_scene(device):
     np.testing.assert_allclose(b, a, rtol=1e-6, atol=1e-9)
 
 
+def _vcm_radius(bounds):
+    lo, hi = bounds
+    return float(0.003 * np.linalg.norm(np.float32(hi) - np.float32(lo)))
+
+
+def test_oracle_identity_instance_vcm_equals_flat_scene():
+    flat, inst = _identity_cornell()
+    lo, hi = flat.geometry.bounds()
+    r = _vcm_radius((lo, hi))
+    a = oracle.vcm_render(flat, 24, 24, 0, 2, max_len=6, radius0=r, seed=SEED)
+    b = oracle.graph_vcm_render(inst, 24, 24, 0, 2, (lo, hi), max_len=6, radius0=r, seed=SEED)
+    np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.gpu
-def test_gpu_vcm_rejects_instanced_scenes(device):
+def test_gpu_instanced_vcm_traces_the_oracles_paths(device):
+    """VCM on the instanced terrain (Ptex instances, two levels): light vertices and camera records keep their
+    material's address, so connections and merges shade with the instance's own material table."""
     import selas_gb300 as sel
-    _, inst = _identity_cornell()
+    s = _terrain()
+    built = s.build(sel, device)
+    info = built[0].info()
+    bounds = (np.float32(info.bounds_lo), np.float32(info.bounds_hi))
+    r = _vcm_radius(bounds) * 4.0
+    gpu = built[0].vcm_generate_image(s.sel_camera(sel, 48, 40), sel.vcm_settings(4, 6, SEED, radius=r))
+    s.release(built)
+    cpu = oracle.graph_vcm_render(s, 48, 40, 0, 4, bounds, max_len=6, radius0=r, seed=SEED) / 4.0
+    _assert_same_paths(gpu.astype(np.float64), cpu)
+
+
+@pytest.mark.gpu
+def test_gpu_identity_instance_vcm_equals_flat_scene(device):
+    import selas_gb300 as sel
+    flat, inst = _identity_cornell()
+    lo, hi = flat.geometry.bounds()
+    r = _vcm_radius((lo, hi))
+    sc = flat.build(sel, device)
+    a = sc.vcm_generate_image(flat.sel_camera(sel, 40, 40), sel.vcm_settings(3, 8, SEED, radius=r)).astype(np.float64)
+    sc.release()
     built = inst.build(sel, device)
-    with pytest.raises(sel.SelError):
-        built[0].vcm_generate_image(inst.sel_camera(sel, 16, 16), sel.vcm_settings(1))
+    b = built[0].vcm_generate_image(inst.sel_camera(sel, 40, 40), sel.vcm_settings(3, 8, SEED, radius=r))
     inst.release(built)
+    np.testing.assert_allclose(b.astype(np.float64), a, rtol=1e-5, atol=1e-8)
 
 
 @pytest.mark.gpu
