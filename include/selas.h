@@ -29,7 +29,8 @@ enum {
     SEL_ERR_OUT_OF_MEMORY = 2,     /* device or host allocation failed                             */
     SEL_ERR_CUDA = 3,              /* a CUDA runtime call failed (text in sel_get_last_error)      */
     SEL_ERR_INVALID_OPERATION = 4, /* e.g. query on a scene that was never committed               */
-    SEL_ERR_DEVICE_LIMIT = 5       /* a kernel hit its iteration cap or stack limit and stopped    */
+    SEL_ERR_DEVICE_LIMIT = 5,      /* a kernel hit its iteration cap or stack limit and stopped    */
+    SEL_ERR_IO = 6                 /* an asset file is missing, unreadable or malformed            */
 };
 
 /* Mirrors RTC_INVALID_GEOMETRY_ID and RTC_MAX_INSTANCE_LEVEL_COUNT (rtcore_common.h:66,72). */
@@ -587,6 +588,80 @@ int sel_server_wait(SelServer server, uint64_t job_id, float* out, size_t out_fl
 int sel_server_stats(SelServer server, SelServerStats* out);
 /* Finishes every queued job, then stops the server. */
 int sel_server_release(SelServer server);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Cooked assets.                                                                                    */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* The reference's cooked asset blobs under <asset_root>/_Assets/<type>/<version>/<name>.bin
+ * (AssetFileUtils::AssetFilePath, Assets/AssetFileUtils.cpp:109-116): SceneResource (version 1539147471),
+ * SubsceneResource (1539551841), ModelResource and ModelGeometryResource (1539636447), Textures (1534887410) and
+ * IBL (1538087123), as SerializeToBinary writes them (IoLib/BinaryStreamSerializer.h:15-32).  Replaces
+ * ReadSceneResource + InitializeSceneResource (SceneLib/SceneResource.cpp:271-315) with its subscenes
+ * (SubsceneResource.cpp:101-160) and models (ModelResource.cpp:432-471). */
+
+/* sel_scene_load_cooked flag: materials that sample Ptex (eUsesPtex) render with their base colour instead of
+ * refusing the scene (the loader reads no .ptx files; bind Ptex with sel_scene_set_ptex on scenes built by hand). */
+#define SEL_COOKED_PTEX_AS_BASE_COLOR 1u
+
+typedef struct SelCookedSceneInfo {
+    uint32_t subscenes;             /* subsceneNames */
+    uint32_t subsceneInstances;
+    uint32_t models;                /* models loaded: each subscene loads its own copy of each model it names */
+    uint32_t modelInstances;        /* over all subscenes */
+    uint32_t meshes;                /* over all loaded models */
+    uint32_t quadMeshes;            /* meshes of 4 indices per face (RTC_GEOMETRY_TYPE_QUAD) */
+    uint64_t faces;                 /* triangles plus quads */
+    uint32_t lights;
+    uint32_t lightSets;             /* lightSetRanges */
+    uint32_t cameras;
+    uint32_t textures;              /* distinct Textures assets the meshes' materials load */
+    uint32_t ptexMeshes;            /* meshes whose material samples Ptex */
+    uint32_t curves;                /* curve geometries of the loaded models (not built: the load is refused) */
+    float backgroundIntensity[4];
+    char ibl[512];                  /* iblName ("" when none) */
+    SelCamera camera;               /* SetupSceneCamera(scene, 0): cameras[0] when valid (fovDegrees > 0, zfar >
+                                       znear), else DefaultCameraSettings; width and height 0 */
+} SelCookedSceneInfo;
+
+/* One mesh of a cooked scene as the reference's loader sets it up (InitializeGeometryUserDatas,
+ * ModelResource.cpp:300-344). */
+typedef struct SelCookedMesh {
+    uint32_t subscene;        /* index into the scene's subsceneNames */
+    uint32_t model;           /* index into that subscene's modelNames */
+    uint32_t mesh;            /* index into the model's meshes: its geomID in the model scene */
+    uint32_t indicesPerFace;  /* 3 or 4 */
+    uint32_t faces;
+    uint32_t materialFlags;   /* MaterialFlags of the resolved material (eTransparent 1, eUsesPtex 16, ...) */
+    SelMaterial material;     /* FindMeshMaterial (ModelResource.cpp:213-229): the model's materials by binary search
+                                 of their sorted name hashes, then the subscene's scene materials, else the default;
+                                 lightSetIndex = the subscene's lightSetIndex */
+    char texture[512];        /* the material's baseColorTexture: a Textures asset name, or a Ptex content path */
+    char name[64];            /* MeshMetaData::name */
+} SelCookedMesh;
+
+/* Parses the scene blob, its subscene blobs and their model and geometry blobs (no device): fills *out_info and
+ * the first `capacity` meshes in load order (subscene, model, mesh).  A missing file or a blob whose offsets or
+ * counts leave the file: SEL_ERR_IO, with the path in the message. */
+int sel_cooked_scene_describe(const char* asset_root, const char* scene_name, SelCookedSceneInfo* out_info,
+                              SelCookedMesh* meshes, unsigned int capacity);
+
+/* Loads a cooked scene into *out_scene, a committed scene of the 8-wide layout:
+ *   top scene:       instance i = subsceneInstances[i], of the scene built for subsceneNames[index];
+ *   subscene scene:  instance j = modelInstances[j], of that subscene's copy of modelNames[index];
+ *   model scene:     geomID k = meshes[k], a triangle or quad mesh with the model's normals (slot 0), tangents
+ *                    (slot 1) and uvs (slot 2), the material FindMeshMaterial resolves (the stored eTransparent
+ *                    flag kept) and, for a non-Ptex material naming a texture, mip 0 of that Textures asset as
+ *                    its base-colour image (read as RGB float triples, as TextureFiltering::Triangle<float3>
+ *                    reads it);
+ * the scene's quad lights in light sets by lightSetRanges, its backgroundIntensity and, when iblName is set, the
+ * IBL asset's light and miss images with its rotation and exposure (the densities are derived again from the
+ * light image).  Queries on *out_scene report instID[0] = i, instID[1] = j and geomID = k, the ids the reference's
+ * Embree scenes report.  Releasing *out_scene releases the subscene and model scenes with it.  Refused with
+ * SEL_ERR_INVALID_OPERATION: models with curves; Ptex materials unless SEL_COOKED_PTEX_AS_BASE_COLOR.
+ * out_info may be null. */
+int sel_scene_load_cooked(SelDevice device, const char* asset_root, const char* scene_name, unsigned int flags,
+                          SelScene* out_scene, SelCookedSceneInfo* out_info);
 
 #ifdef __cplusplus
 }

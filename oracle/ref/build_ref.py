@@ -16,7 +16,9 @@ under tests/golden/ (tests/golden/make_golden.py).
                     Sampler.cpp, which the harness supplies), the SystemLib / IoLib / StringLib / UtilityLib /
                     ThreadingLib files those reference, VCMCommon.cpp, and the Ptex objects above; ray queries go
                     to the oracle's BVH (linked from oracle/liboracle.so) through pt_harness.cpp's Embree shim
-                    (embree_stubs.c aborts on the scene-building entry points, which nothing reaches).
+                    (embree_stubs.c aborts on the scene-building entry points, which nothing reaches);
+                    with cooked_harness.cpp and TextureLib/TextureResource.cpp, the reference's serializer writes
+                    the cooked asset blobs of tests/golden/cooked/ (tests/golden/make_cooked.py).
 
 The reference checkout is found at $SELAS_REFERENCE, else at ../reference beside this repository.
 """
@@ -100,11 +102,11 @@ def build_pt(force=False):
         "StringLib": ["StringUtil"],
         "UtilityLib": ["MurmurHash"],
         "ThreadingLib": ["ThreadLinux"],
-        "TextureLib": ["TextureFiltering"],
+        "TextureLib": ["TextureFiltering", "TextureResource"],
     }
     srcs = [core / d / f"{n}.cpp" for d, ns in names.items() for n in ns]
     srcs += [p for p in sorted((core / "MathLib").glob("*.cpp")) if p.name != "Sampler.cpp"]
-    srcs += [app / "VCMCommon.cpp", HERE / "pt_harness.cpp"]
+    srcs += [app / "VCMCommon.cpp", HERE / "pt_harness.cpp", HERE / "cooked_harness.cpp"]
     inc = [f"-I{core}", f"-I{app}", f"-I{REFERENCE / 'Middleware'}", f"-I{REFERENCE / 'Middleware' / 'ptex' / 'Include'}",
            f"-I{REFERENCE / 'Middleware' / 'embree-latest' / 'include'}", f"-I{oracle_dir}"]
     objs = _compile(srcs, SELAS_FLAGS + ["-DPTEX_STATIC"] + inc, OUT / "obj_pt")

@@ -313,6 +313,18 @@ Error Size(cpointer, uint64&) { std::abort(); }
 }  // namespace File
 Error BuildProcessorContext::AddFileDependency(cpointer) { std::abort(); }
 Error StbImageRead(cpointer, uint, uint, uint&, uint&, uint&, bool&, void*&) { std::abort(); }
+Error StbImageWrite(cpointer, uint, uint, uint, StbImageFormats, void*) { std::abort(); }
+namespace Directory {
+void EnsureDirectoryExists(const char*) { std::abort(); }
+}  // namespace Directory
+
+// The densities the reference's IBL build step stores in a cooked ImageBasedLightResource
+// (BuildImageBasedLight.cpp:24-101, static there): used by cooked_harness.cpp.
+void HarnessIblDensities(Selas::uint width, Selas::uint height, float3* light, IblDensityFunctions* out) {
+    float* intensities = CalculateIntensityMap(width, height, light);
+    CalculateStrataDistributionFunctions(width, height, intensities, out);
+    FreeAligned_(intensities);
+}
 
 }  // namespace Selas
 

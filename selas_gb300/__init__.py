@@ -20,6 +20,7 @@ SEL_ERR_OUT_OF_MEMORY = 2
 SEL_ERR_CUDA = 3
 SEL_ERR_INVALID_OPERATION = 4
 SEL_ERR_DEVICE_LIMIT = 5
+SEL_ERR_IO = 6
 
 SEL_OPTION_GRAPH_REPLAY = 1
 SEL_OPTION_MATERIAL_SORT = 2
@@ -651,3 +652,53 @@ def _scene_set_leaf_size(self, n: int) -> None:
 
 Scene.autotune = _scene_autotune
 Scene.set_leaf_size = _scene_set_leaf_size
+
+
+# ---------------------------------------------------------------------------------------------------
+# Cooked assets (include/selas.h: SelCookedSceneInfo, SelCookedMesh, sel_scene_load_cooked)
+# ---------------------------------------------------------------------------------------------------
+SEL_COOKED_PTEX_AS_BASE_COLOR = 1
+
+
+class SelCookedSceneInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("subscenes", "subsceneInstances", "models", "modelInstances", "meshes",
+                                               "quadMeshes")] + [("faces", ctypes.c_uint64)] + [
+               (n, ctypes.c_uint32) for n in ("lights", "lightSets", "cameras", "textures", "ptexMeshes", "curves")] + [
+               ("backgroundIntensity", ctypes.c_float * 4), ("ibl", ctypes.c_char * 512), ("camera", SelCamera)]
+
+
+class SelCookedMesh(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in ("subscene", "model", "mesh", "indicesPerFace", "faces",
+                                               "materialFlags")] + [
+               ("material", SelMaterial), ("texture", ctypes.c_char * 512), ("name", ctypes.c_char * 64)]
+
+
+register_signatures({
+    "sel_cooked_scene_describe": [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(SelCookedSceneInfo),
+                                  ctypes.POINTER(SelCookedMesh), _u],
+    "sel_scene_load_cooked": [_vp, ctypes.c_char_p, ctypes.c_char_p, _u, ctypes.POINTER(_vp),
+                              ctypes.POINTER(SelCookedSceneInfo)],
+})
+
+
+def cooked_describe(asset_root, scene_name: str):
+    """sel_cooked_scene_describe: (SelCookedSceneInfo, list of SelCookedMesh in load order); needs no device."""
+    info = SelCookedSceneInfo()
+    root, name = str(asset_root).encode(), scene_name.encode()
+    check(lib().sel_cooked_scene_describe(root, name, ctypes.byref(info), None, 0))
+    meshes = (SelCookedMesh * max(info.meshes, 1))()
+    check(lib().sel_cooked_scene_describe(root, name, ctypes.byref(info), meshes, info.meshes))
+    return info, list(meshes[:info.meshes])
+
+
+def load_cooked(device: Device, asset_root, scene_name: str, flags: int = 0):
+    """sel_scene_load_cooked: (committed Scene, SelCookedSceneInfo); releasing the scene releases the subscene and
+    model scenes it instances."""
+    info = SelCookedSceneInfo()
+    h = _vp()
+    check(lib().sel_scene_load_cooked(device.handle, str(asset_root).encode(), scene_name.encode(), flags,
+                                      ctypes.byref(h), ctypes.byref(info)))
+    sc = Scene.__new__(Scene)
+    sc.handle = h
+    sc.device = device
+    return sc, info

@@ -84,6 +84,10 @@ bool instances_fresh(const SelSceneTy* sc) {
     return true;
 }
 
+void adopt_scenes(SelSceneTy* top, const std::vector<SelSceneTy*>& scenes) {
+    top->owned.insert(top->owned.end(), scenes.begin(), scenes.end());
+}
+
 }  // namespace sel
 
 using namespace sel;
@@ -571,7 +575,9 @@ int sel_scene_release(SelScene scene) {
                     scene->d_light_sets, scene->pt_block, scene->d_accum, scene->d_ptex_faces, scene->d_ptex_texels,
                     scene->vcm_block, scene->d_insts, scene->d_view, scene->d_ibl, scene->d_attrs, scene->d_textures})
         if (p) cudaFree(p);
+    std::vector<SelSceneTy*> owned = std::move(scene->owned);
     delete scene;
+    for (auto it = owned.rbegin(); it != owned.rend(); ++it) sel_scene_release(*it);
     return SEL_OK;
 }
 

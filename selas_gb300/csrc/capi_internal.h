@@ -98,6 +98,8 @@ struct SelSceneTy {
     uint32_t vcm_paths = 0, vcm_len = 0, vcm_passes = 0;
     // captured per-batch / per-pass launch graphs of the integrators
     sel::GraphCache pt_graph, vcm_graph;
+    // scenes released with this one, after it (sel_scene_load_cooked: the subscene and model scenes)
+    std::vector<SelSceneTy*> owned;
     std::mutex mu;
 };
 
@@ -109,6 +111,10 @@ struct VcmConsts;
 struct VcmSettings;
 // render_capi.cu
 int sync_shading(SelSceneTy* sc);              // uploads materials, lights, Ptex and the IBL when they changed
+// sel_scene_set_material with the eTransparent flag given instead of derived (cooked materials keep theirs)
+int set_material_flags(SelSceneTy* sc, unsigned int geomID, const SelMaterial& material, bool transparent);
+// capi.cpp: `top` releases `scenes` (created after the scenes they instance) when it is released
+void adopt_scenes(SelSceneTy* top, const std::vector<SelSceneTy*>& scenes);
 // CalculateIntensityMap + CalculateStrataDistributionFunctions (BuildImageBasedLight.cpp:18-107): marginal CDF
 // (height) and conditional CDFs (width x height) of sin(theta) x luma of an RGB latitude-longitude image.
 void ibl_densities(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& mdf, std::vector<float>& cdf);

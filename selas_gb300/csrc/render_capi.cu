@@ -336,6 +336,24 @@ int sync_shading(SelSceneTy* sc) {
     return SEL_OK;
 }
 
+int set_material_flags(SelSceneTy* scene, unsigned int geomID, const SelMaterial& material, bool transparent) {
+    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
+    if (material.shader < SEL_SHADER_DISNEY_THIN || material.shader > SEL_SHADER_DIRAC_TRANSPARENT)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "unknown shader");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    if (scene->materials.size() <= geomID) {
+        MaterialDev unset;
+        std::memset(&unset, 0, sizeof(unset));
+        unset.shader = -1;
+        scene->materials.resize(geomID + 1, unset);
+    }
+    MaterialDev d = to_device(material);
+    d.flags = (d.flags & ~kMaterialTransparent) | (transparent ? kMaterialTransparent : 0u);
+    scene->materials[geomID] = d;
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
 }  // namespace sel
 
 namespace {
@@ -689,19 +707,9 @@ int sel_material_defaults(SelMaterial* out) {
 
 int sel_scene_set_material(SelScene scene, unsigned int geomID, const SelMaterial* material) {
     if (!scene || !material) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
-    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
-    if (material->shader < SEL_SHADER_DISNEY_THIN || material->shader > SEL_SHADER_DIRAC_TRANSPARENT)
-        return fail(SEL_ERR_INVALID_ARGUMENT, "unknown shader");
-    std::lock_guard<std::mutex> lock(scene->mu);
-    if (scene->materials.size() <= geomID) {
-        MaterialDev unset;
-        std::memset(&unset, 0, sizeof(unset));
-        unset.shader = -1;
-        scene->materials.resize(geomID + 1, unset);
-    }
-    scene->materials[geomID] = to_device(*material);
-    scene->shading_dirty = true;
-    return SEL_OK;
+    const bool transparent = material->shader == SEL_SHADER_DISNEY_SOLID &&
+                             (material->diffuseTrans > 0.0f || material->specTrans > 0.0f);
+    return sel::set_material_flags(scene, geomID, *material, transparent);
 }
 
 int sel_scene_add_quad_light(SelScene scene, unsigned int lightSetIndex, const SelQuadLight* light) {

@@ -205,6 +205,8 @@ template <typename Xf>
 SEL_HD void shading_frame(const MeshAttrDev* A, uint32_t prim, float u, float v, float3 ng, Xf xf, float3& n,
                           float3& t, float3& b, float& sign) {
     float3 nrm = ng;
+    // a table entry of a mesh without normals or tangents has no index array either: read no corners then
+    if (A && !A->normals && !A->tangents) A = nullptr;
     AttrCorners c;
     if (A) c = attr_corners(A, prim, u, v);
     if (A && A->normals) {
