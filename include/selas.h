@@ -131,7 +131,9 @@ int sel_scene_set_bvh_kind(SelScene scene, int bvh_kind);
  * builder. */
 enum { SEL_BUILD_HOST = 0, SEL_BUILD_DEVICE = 1 };
 int sel_scene_set_build_mode(SelScene scene, int build_mode);
-/* Triangles per leaf of the device-built 8-wide layout, 1..4 (default 3; the host builder uses 3). */
+/* Triangles per leaf of the device-built 8-wide layout, 1..8 (default 3; the host builder uses 3).  A node's leaf
+ * children hold 32 triangles at most: with leaves above 4, the largest leaves of a node that would hold more
+ * move one level down, each into a node of its own. */
 int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size);
 /* vertices: vertex_count records of 3 floats (x,y,z) every vertex_stride_bytes bytes (>= 12);
  * indices: triangle_count x 3 unsigned ints.  The data is copied; the caller may free it after the
@@ -475,9 +477,9 @@ int sel_render_views_device(SelScene scene, const SelCamera* cameras, unsigned i
                             const SelPtSettings* settings, double* d_accum, void* stream);
 
 /* Autotuner (no reference counterpart).  Renders the given path-tracer workload (timed with CUDA events,
- * after one untimed render per configuration) over BVH layout and leaf size {8-wide quantised with 2, 3, 4
- * triangles per leaf; binary FP32}, wavefront capacity {1,048,576; 4,194,304; 8,388,608 paths} and traversal
- * block size {128, 256 (8-wide only)}; rebuilds the scene with the fastest layout and keeps the fastest
+ * after one untimed render per configuration) over BVH layout and leaf size {8-wide quantised with 2, 3, 4, 8
+ * triangles per leaf; binary FP32 (scenes without instances)}, wavefront capacity {1,048,576; 4,194,304;
+ * 8,388,608 paths} and traversal block size {128, 256 (8-wide only)}; rebuilds the scene with the fastest layout and keeps the fastest
  * capacity and block size as its defaults (used when SelPtSettings leaves them 0).  Images do not depend on
  * any of these choices. */
 typedef struct SelTuneTrial {

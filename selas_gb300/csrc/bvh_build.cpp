@@ -23,7 +23,8 @@ namespace sel {
 namespace {
 
 constexpr int kBins = 32;
-constexpr uint32_t kMaxLeaf = 3;        // triangles per leaf (one wide-node child slot holds <= 3)
+constexpr uint32_t kMaxLeaf = 3;        // triangles per leaf: eight leaf slots stay within a node's 32 records
+static_assert(8 * kMaxLeaf <= kMaxNodeRecords, "a node's leaf children must fit its record mask");
 constexpr int kMedianDepth = 40;        // beyond this depth split at the object median (bounds depth)
 constexpr uint32_t kParallelGrain = 32768;
 
@@ -291,6 +292,7 @@ private:
 
         WideNode node;
         std::memset(&node, 0, sizeof(node));
+        std::memset(node.meta, int(kLeafNone), sizeof(node.meta));
         quantise(nb, slot_child, node);
 
         // internal children: contiguous block in slot order
@@ -313,7 +315,7 @@ private:
             int c = slot_child[s];
             if (c < 0 || !is_leaf(c)) continue;
             const Node2& leaf = n2_[c];
-            node.meta[s] = uint8_t((leaf.count << 5) | offset);
+            node.meta[s] = uint8_t(((leaf.count - 1u) << 5) | offset);
             for (uint32_t k = 0; k < leaf.count; ++k) {
                 const FlatTri& t = tris_[prims_[leaf.first + k].tri];
                 TriRecord r;

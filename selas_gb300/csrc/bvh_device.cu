@@ -1,7 +1,7 @@
 // Device SAH-binned BVH builder: the 8-wide quantised layout of bvh_build.cpp built on the GPU.
 //
 // Same method as the host builder (binned SAH after Wald 2007, 32 bins per axis, leaves of at most 3
-// triangles by default (1..4 selectable), object-median splits beyond depth 40, greedy collapse to 8 children by largest surface area,
+// triangles by default (1..8 selectable), object-median splits beyond depth 40, greedy collapse to 8 children by largest surface area,
 // octant slot assignment and outward 8-bit child-box quantisation after Ylitie, Karras and Laine 2017),
 // organised for the GPU:
 //   1. one thread per triangle: bounds, centroid (box centre, as the host builder);
@@ -28,7 +28,7 @@ namespace sel {
 namespace {
 
 constexpr int kBinsD = 32;
-constexpr uint32_t kMaxLeafLimit = 4;  // 8 leaf slots x 4 triangles fit the 5-bit leaf offsets of WideNode
+constexpr uint32_t kMaxLeafLimit = kMaxLeafRecords;  // leaves beyond a node's 32 records move one level down
 constexpr int kMedianDepthD = 40;
 constexpr uint32_t kSmall = 1024;   // subtrees at or below this many triangles are built by one warp
 constexpr int kWarpStack = 32;
@@ -615,12 +615,26 @@ __global__ void __launch_bounds__(128) k_collapse_gather(Build B, Collapse C, ui
         slot_child[bs] = children[bc];
         done[bc] = true;
     }
-    uint32_t ni = 0, nt = 0;
+    // A node's leaf children hold 32 records at most (the traversal's record mask).  With leaves of more than
+    // 4 triangles eight of them can hold more: the largest leaf (the lowest slot among equals) then becomes an
+    // internal child, a node of its own one level down whose single slot is that leaf, until the rest fit.
+    // Such a demoted leaf is stored as -(child + 2) in the slot table.
+    uint32_t nt = 0;
+    for (int s = 0; s < 8; ++s)
+        if (slot_child[s] >= 0 && is_leaf(B, slot_child[s])) nt += B.nrange[slot_child[s]].y;
+    while (nt > kMaxNodeRecords) {
+        int big = -1;
+        for (int s = 0; s < 8; ++s)
+            if (slot_child[s] >= 0 && is_leaf(B, slot_child[s]) &&
+                (big < 0 || B.nrange[slot_child[s]].y > B.nrange[slot_child[big]].y))
+                big = s;
+        nt -= B.nrange[slot_child[big]].y;
+        slot_child[big] = -(slot_child[big] + 2);
+    }
+    uint32_t ni = 0;
     for (int s = 0; s < 8; ++s) {
         C.slots[size_t(i) * 8 + s] = slot_child[s];
-        if (slot_child[s] < 0) continue;
-        if (is_leaf(B, slot_child[s])) nt += B.nrange[slot_child[s]].y;
-        else ++ni;
+        if (slot_child[s] <= -2 || (slot_child[s] >= 0 && !is_leaf(B, slot_child[s]))) ++ni;
     }
     C.cnt_int[i] = ni;
     C.cnt_tri[i] = nt;
@@ -672,8 +686,11 @@ __global__ void __launch_bounds__(128) k_collapse_emit(Build B, Collapse C, uint
     bool present[8];
     float lo[3][8], hi[3][8];
     float nlo[3] = {INFINITY, INFINITY, INFINITY}, nhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    bool demoted[8];
     for (int s = 0; s < 8; ++s) {
         slot_child[s] = C.slots[size_t(i) * 8 + s];
+        demoted[s] = slot_child[s] <= -2;
+        if (demoted[s]) slot_child[s] = -slot_child[s] - 2;
         present[s] = slot_child[s] >= 0;
         if (!present[s]) continue;
         const float4 l = B.nlo[slot_child[s]], h = B.nhi[slot_child[s]];
@@ -683,6 +700,7 @@ __global__ void __launch_bounds__(128) k_collapse_emit(Build B, Collapse C, uint
     }
     WideNode node;
     memset(&node, 0, sizeof(node));
+    memset(node.meta, int(kLeafNone), sizeof(node.meta));
     for (int a = 0; a < 3; ++a) quantise_axis(a, nlo[a], nhi[a], lo[a], hi[a], present, node);
     node.child_base = next_base + C.off_int[i];
     node.tri_base = tri_base + C.off_tri[i];
@@ -690,14 +708,14 @@ __global__ void __launch_bounds__(128) k_collapse_emit(Build B, Collapse C, uint
     for (int s = 0; s < 8; ++s) {
         const int c = slot_child[s];
         if (c < 0) continue;
-        if (!is_leaf(B, c)) {
+        if (demoted[s] || !is_leaf(B, c)) {
             node.imask |= uint8_t(1u << s);
             C.next[C.off_int[i] + ni] = make_uint2(node.child_base + ni, uint32_t(c));
             ++ni;
             continue;
         }
         const uint2 r = B.nrange[c];
-        node.meta[s] = uint8_t((r.y << 5) | offset);
+        node.meta[s] = uint8_t(((r.y - 1u) << 5) | offset);
         for (uint32_t k = 0; k < r.y; ++k) {
             const uint32_t tri = __float_as_uint(B.plo[B.idx[r.x + k]].w);
             const float4* src = B.soup + size_t(tri) * 3;
@@ -719,7 +737,7 @@ cudaError_t dalloc(T*& p, size_t count) {
 }  // namespace
 
 std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max_leaf, DeviceBuild& out) {
-    if (max_leaf < 1 || max_leaf > kMaxLeafLimit) return "leaf size must lie in 1..4";
+    if (max_leaf < 1 || max_leaf > kMaxLeafLimit) return "leaf size must lie in 1..8";
     std::vector<TriRecord> soup;
     size_t total = 0;
     for (const MeshInput& m : meshes) total += m.indices.size() / 3;
@@ -851,7 +869,9 @@ std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max
     uint32_t* scan_tmp = nullptr;
     uint32_t *cnt_int = nullptr, *cnt_tri = nullptr, *off_int = nullptr, *off_tri = nullptr;
     int* slots = nullptr;
-    const size_t max_wide = n;  // at most one 8-wide node per triangle
+    // 8-wide nodes: each has at least two slots except the single-leaf nodes of demoted leaves (at most one per
+    // five triangles, as only a leaf of five or more is demoted), so at most n + n / 5 + 1 of them
+    const size_t max_wide = max_leaf > 4 ? n + n / 5 + 1 : n;
     take(nodes, max_wide);
     take(tris, n);
     take(lvl_a, max_wide);

@@ -321,7 +321,8 @@ int sel_scene_set_build_mode(SelScene scene, int build_mode) {
 
 int sel_scene_set_leaf_size(SelScene scene, unsigned int leaf_size) {
     if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
-    if (leaf_size < 1 || leaf_size > 4) return fail(SEL_ERR_INVALID_ARGUMENT, "leaf_size must lie in 1..4");
+    if (leaf_size < 1 || leaf_size > kMaxLeafRecords)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "leaf_size must lie in 1..8");
     std::lock_guard<std::mutex> lock(scene->mu);
     scene->leaf_size = leaf_size;
     return SEL_OK;

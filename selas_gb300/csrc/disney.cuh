@@ -541,4 +541,37 @@ SEL_HD float3 bsdf_evaluate(const Surface& s, float3 v, float3 l, float& fwd, fl
     return f3(0.0f);
 }
 
+// The same dispatch for surfaces known to have shader kShader (-1: any), so that a kernel that shades one kind
+// of surface carries only that shader's code.
+template <int kShader>
+SEL_HD bool bsdf_sample_as(const Surface& s, float3 v, const float* u, int& used, BsdfSampleOut& o) {
+    if constexpr (kShader < 0) {
+        return bsdf_sample(s, v, u, used, o);
+    } else {
+        o.flags = 0;
+        o.medium_phase = 0;
+        o.extinction = f3(0.0f);
+        o.reflectance = f3(0.0f);
+        o.wi = f3(0.0f);
+        o.forward_pdf = 0.0f;
+        o.reverse_pdf = 0.0f;
+        if constexpr (kShader == kDisneyThin) return disney::sample(s, v, true, u, used, o);
+        else if constexpr (kShader == kDisneySolid) return disney::sample(s, v, false, u, used, o);
+        else return sample_dirac_transparent(s, v, u, used, o);
+    }
+}
+
+template <int kShader>
+SEL_HD float3 bsdf_evaluate_as(const Surface& s, float3 v, float3 l, float& fwd, float& rev) {
+    if constexpr (kShader < 0) {
+        return bsdf_evaluate(s, v, l, fwd, rev);
+    } else {
+        fwd = 0.0f;
+        rev = 0.0f;
+        if constexpr (kShader == kDisneyThin) return disney::evaluate(s, v, l, true, fwd, rev);
+        else if constexpr (kShader == kDisneySolid) return disney::evaluate(s, v, l, false, fwd, rev);
+        else return f3(0.0f);
+    }
+}
+
 }  // namespace sel

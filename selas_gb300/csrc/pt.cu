@@ -182,11 +182,33 @@ __device__ __forceinline__ HitRef hit_ref(const PtState& st, const PtScene& S, u
     return hit_ref_of<kInst>(S, kInst ? st.hinst[s] : make_uint2(0u, 0u), tri);
 }
 
+// Per-thread traversal stacks of a B-thread block in shared memory (entry k of thread t at k * B + t).  The
+// instanced traversal's 40-entry stacks of a 256-thread block take 80 KB: they live in dynamic shared memory
+// (launched with trace_stack_bytes<K, B>() bytes and the matching MaxDynamicSharedMemorySize attribute); every
+// other stack is a static array.
+template <int K, int B>
+constexpr size_t trace_stack_bytes() {
+    return size_t(Tracer<K>::kDepth) * B * sizeof(typename Tracer<K>::Entry);
+}
+template <int K, int B>
+constexpr bool kDynamicStack = trace_stack_bytes<K, B>() > 48u * 1024u;
+
+template <int K, int B>
+__device__ __forceinline__ typename Tracer<K>::Entry* trace_stack() {
+    if constexpr (kDynamicStack<K, B>) {
+        extern __shared__ __align__(16) unsigned char pt_dynamic_stack[];
+        return reinterpret_cast<typename Tracer<K>::Entry*>(pt_dynamic_stack);
+    } else {
+        __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
+        return stack_mem;
+    }
+}
+
 // Closest hit for the queued paths.  Warps take 32-entry packets from the queue through an atomic cursor,
 // so expensive and cheap rays balance across the GPU.  K = 2: the instanced traversal of the 8-wide layout.
 template <int K, int B>
-__global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_extend(PtParams P, int cur) {
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
+__global__ void __launch_bounds__(B, K == 2 ? 512 / B : 1024 / B) k_extend(PtParams P, int cur) {
+    typename Tracer<K>::Entry* stack_mem = trace_stack<K, B>();
     const uint32_t n = P.st.counters[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays, (unsigned long long)n);
     const uint32_t* queue = P.st.queue[cur];
@@ -305,12 +327,15 @@ __global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
 // the reference's batcher orders hits by (instance, geometry, primitive) before shading
 // (PathTracingBatcher.cpp:221-238,799-825), and hits whose footprints cross the same edges walk the same faces,
 // so a warp's Ptex filter walks stay in step.  Three 8-bit radix passes order the queue by it.
+// The classes are counted as k_classify counts them (the shading kernels find their classes' ranges from it).
 template <bool kInst>
 __global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const uint32_t s = P.st.queue[cur][e];
-        const float4 hit = P.st.hit[s];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t e = base + threadIdx.x;
+        const bool valid = e < n;
+        const uint32_t s = valid ? P.st.queue[cur][e] : 0u;
+        const float4 hit = valid ? P.st.hit[s] : make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(0xffffffffu));
         const uint32_t tri = __float_as_uint(hit.w);
         uint32_t key = 0u;
         if (tri != 0xffffffffu) {
@@ -326,7 +351,10 @@ __global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
                        ptex_region(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count), face, hit.y, hit.z);
             }
         }
-        P.st.rkeys[0][e] = key;
+        const uint32_t c = valid ? key >> 20 : 0xffu;
+        if (valid) P.st.rkeys[0][e] = key;
+        const uint32_t peers = __match_any_sync(0xffffffffu, c);
+        if (valid && (__ffs(peers) - 1) == int(threadIdx.x & 31u)) atomicAdd(&P.st.counters[32 + c], __popc(peers));
     }
 }
 
@@ -367,13 +395,27 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const u
 // integrator out of the kernel).
 // The path tracer's shading at most 96 registers (5 blocks per SM; a few bytes spill): 2 % faster renders of the
 // room than 102 registers.  The deferred and mixed forms keep 4 blocks per SM (their bigger code would spill).
-template <uint32_t kModes, bool kInst>
-__global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams P, int cur, uint32_t bounce, const uint32_t* in_queue) {
-    const uint32_t n = P.st.counters[cur];
+// kShader: the shader of every hit the kernel shades (-1: any).  classes = (c0, c1): the kernel shades the
+// entries of material classes c0..c1 of the class-ordered queue (class counts in counters[32 + c]); c0 < 0: the
+// whole queue.
+template <uint32_t kModes, bool kInst, int kShader>
+__global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams P, int cur, uint32_t bounce,
+                                                                        const uint32_t* in_queue, int2 classes) {
+    uint32_t lo = 0, hi = P.st.counters[cur];
+    if (classes.x >= 0) {
+        uint32_t before = 0, upto = 0;
+        for (int c = 0; c < kPtClasses; ++c) {
+            const uint32_t k = P.st.counters[32 + c];
+            before += c < classes.x ? k : 0u;
+            upto += c <= classes.y ? k : 0u;
+        }
+        lo = before;
+        hi = upto;
+    }
     const int next = cur ^ 1;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    for (uint32_t base = lo + blockIdx.x * blockDim.x; base < hi; base += gridDim.x * blockDim.x) {
         const uint32_t e = base + threadIdx.x;
-        const bool valid = e < n;
+        const bool valid = e < hi;
         bool cont = false, shadow = false, shadow2 = false;
         uint32_t s = 0;
         float4 sh_o = make_float4(0, 0, 0, 0), sh_d = sh_o, sh_c = sh_o;
@@ -440,7 +482,7 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
                 const uint32_t tag = (job << 28) | pixel;
                 if (dot(ls.radiance, f3(1.0f)) > 0.0f) {
                     float fpdf, rpdf;
-                    const float3 refl = bsdf_evaluate(sf, -d, ls.direction, fpdf, rpdf);
+                    const float3 refl = bsdf_evaluate_as<kShader>(sf, -d, ls.direction, fpdf, rpdf);
                     if (deferred) {
                         // weight 1 (DeferredPathTracer.cpp:65-88); the shadow ray starts at tnear 0
                         const float3 smp = 1.0f * refl * ls.radiance * (1.0f / ls.pdf);
@@ -482,7 +524,7 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
                     }
                     if (dot(bg, f3(1.0f)) > 0.0f) {
                         float fpdf, rpdf;
-                        const float3 refl = bsdf_evaluate(sf, -d, sdir, fpdf, rpdf);
+                        const float3 refl = bsdf_evaluate_as<kShader>(sf, -d, sdir, fpdf, rpdf);
                         const float mis = (1.0f * spdf) / (1.0f * spdf + 1.0f * fpdf);
                         const float3 smp = mis * refl * bg * (1.0f / spdf);
                         if (dot(smp, f3(1.0f)) > 0.0f) {
@@ -501,7 +543,7 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
                 for (int k = 0; k < 4; ++k) u4[k] = pcg_float(ahead);
                 int used = 0;
                 BsdfSampleOut bs;
-                const bool ok = bsdf_sample(sf, -d, u4, used, bs);
+                const bool ok = bsdf_sample_as<kShader>(sf, -d, u4, used, bs);
                 for (int k = 0; k < used; ++k) pcg_next(rng);
                 if (!ok) {
                     alive = false;
@@ -589,9 +631,8 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
 }
 
 template <int K, int B>
-__global__ void __launch_bounds__(B, K == 2 ? 4 : 1024 / B) k_shadow(PtParams P) {
-    static_assert(K != 2 || B == 128, "the instanced stack fills the static shared memory at 128 threads");
-    __shared__ typename Tracer<K>::Entry stack_mem[Tracer<K>::kDepth * B];
+__global__ void __launch_bounds__(B, K == 2 ? 512 / B : 1024 / B) k_shadow(PtParams P) {
+    typename Tracer<K>::Entry* stack_mem = trace_stack<K, B>();
     const uint32_t n = P.st.counters[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(P.st.rays + 1, (unsigned long long)n);
     uint32_t status = 0;
@@ -727,13 +768,45 @@ size_t pt_state_block_bytes(uint32_t paths) {
     return total;
 }
 
+template <uint32_t kModes, bool kInst>
+void launch_shade_modes(int shader, int grid, cudaStream_t s, const PtParams& P, int cur, uint32_t b,
+                        const uint32_t* q, int2 classes) {
+    if (shader == 0) k_shade<kModes, kInst, 0><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+    else if (shader == 1) k_shade<kModes, kInst, 1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+    else if (shader == 2) k_shade<kModes, kInst, 2><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+    else k_shade<kModes, kInst, -1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+}
+
+void launch_shade(uint32_t modes, bool inst, int shader, int grid, cudaStream_t s, const PtParams& P, int cur,
+                  uint32_t b, const uint32_t* q, int2 classes) {
+    if (inst) {
+        if (modes == 2u) launch_shade_modes<2, true>(shader, grid, s, P, cur, b, q, classes);
+        else if (modes == 3u) launch_shade_modes<3, true>(shader, grid, s, P, cur, b, q, classes);
+        else launch_shade_modes<1, true>(shader, grid, s, P, cur, b, q, classes);
+    } else {
+        if (modes == 2u) launch_shade_modes<2, false>(shader, grid, s, P, cur, b, q, classes);
+        else if (modes == 3u) launch_shade_modes<3, false>(shader, grid, s, P, cur, b, q, classes);
+        else launch_shade_modes<1, false>(shader, grid, s, P, cur, b, q, classes);
+    }
+}
+
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
-                           bool instanced, bool texture, bool ray_sort, uint64_t batch_paths) {
+                           bool instanced, bool texture, bool ray_sort, uint64_t batch_paths, uint32_t shader_kinds) {
     const bool face_order = sort && texture && !instanced && batch_paths >= kFaceOrderPaths;
-    // 256-thread traversal blocks only for the flat 8-wide layout (its 24-entry stack then fills the 48 KB of
-    // static shared memory; the binary layout's 64-entry and the instanced 40-entry stacks would not fit)
-    const int tb = (trace_block == 256 && bvh_kind == 0 && !instanced) ? 256 : 128;
+    // 256-thread traversal blocks for the 8-wide layout, flat (its 24-entry stacks fill 48 KB of static shared
+    // memory) or instanced (40-entry stacks, 80 KB of dynamic shared memory); the binary layout's 64-entry
+    // stacks stay at 128 threads
+    const int tb = (trace_block == 256 && bvh_kind == 0) ? 256 : 128;
+    constexpr size_t kInstStackBytes = trace_stack_bytes<2, 256>();
+    if (instanced && tb == 256) {
+        cudaError_t e = cudaFuncSetAttribute(k_extend<2, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(kInstStackBytes));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_shadow<2, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(kInstStackBytes));
+        if (e != cudaSuccess) return e;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -746,12 +819,18 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     const int gen_grid = int((st.capacity + kBlock - 1) / kBlock);
     // the shading kernel (4 or 5 resident blocks per SM) runs one resident wave of grid-striding blocks, sized by
     // the occupancy calculator, as VCM's shading kernels do
-    const void* shade_fn = instanced ? (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, true>)
-                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, true>)
-                                                      : reinterpret_cast<const void*>(&k_shade<1, true>))
-                                     : (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, false>)
-                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, false>)
-                                                      : reinterpret_cast<const void*>(&k_shade<1, false>));
+    const void* shade_fn = instanced ? (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, true, -1>)
+                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, true, -1>)
+                                                      : reinterpret_cast<const void*>(&k_shade<1, true, -1>))
+                                     : (modes == 2u ? reinterpret_cast<const void*>(&k_shade<2, false, -1>)
+                                        : modes == 3u ? reinterpret_cast<const void*>(&k_shade<3, false, -1>)
+                                                      : reinterpret_cast<const void*>(&k_shade<1, false, -1>));
+    // shading launches: one kernel for the jobs' single shader over the whole queue; with several shaders and the
+    // class order, one per shader over its classes (1 + shader * 4 .. 4 + shader * 4; the misses, class 0, with
+    // the first); else the kernel for every shader
+    const uint32_t kinds = shader_kinds & 7u;
+    const bool one_kind = kinds != 0u && (kinds & (kinds - 1u)) == 0u;
+    const int single = one_kind ? __builtin_ctz(kinds) : -1;
     int shade_blocks = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&shade_blocks, shade_fn, kBlock, 0);
     const int wave_grid = sms * std::max(shade_blocks, 1);
@@ -761,13 +840,15 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         for (uint32_t b = 0; b < bounces; ++b) {
             const int cur = int(b & 1u);
             k_bounce_reset<<<1, 32, 0, s>>>(st.counters, cur ^ 1);
-            if (instanced) k_extend<2, 128><<<trace_grid, tb, 0, s>>>(P, cur);
+            if (instanced && tb == 256) k_extend<2, 256><<<trace_grid, tb, kInstStackBytes, s>>>(P, cur);
+            else if (instanced) k_extend<2, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             else if (bvh_kind == 0 && tb == 256) k_extend<0, 256><<<trace_grid, tb, 0, s>>>(P, cur);
             else if (bvh_kind == 0) k_extend<0, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             else k_extend<1, 128><<<trace_grid, tb, 0, s>>>(P, cur);
             if (face_order) {
                 // textured scenes, large batches: order by (class, Ptex face, footprint region), three 8-bit
                 // radix passes from the queue to queue_sorted (through rvals)
+                k_class_reset<<<1, 32, 0, s>>>(st.counters);
                 if (instanced) k_sort_keys<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 else k_sort_keys<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
                 const uint32_t ntiles = (st.capacity + kSortTile - 1) / kSortTile;
@@ -794,16 +875,18 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             const uint32_t* q = sort ? st.queue_sorted : st.queue[cur];
             if (texture && instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
             else if (texture) k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
-            if (instanced) {
-                if (modes == 2u) k_shade<2, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else if (modes == 3u) k_shade<3, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else k_shade<1, true><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+            const int2 whole = make_int2(-1, -1);
+            if (one_kind) {
+                launch_shade(modes, instanced, single, wave_grid, s, P, cur, b, q, whole);
+            } else if (sort) {
+                launch_shade(modes, instanced, 0, wave_grid, s, P, cur, b, q, make_int2(0, 4));
+                if (kinds & 2u) launch_shade(modes, instanced, 1, wave_grid, s, P, cur, b, q, make_int2(5, 8));
+                if (kinds & 4u) launch_shade(modes, instanced, 2, wave_grid, s, P, cur, b, q, make_int2(9, 12));
             } else {
-                if (modes == 2u) k_shade<2, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else if (modes == 3u) k_shade<3, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
-                else k_shade<1, false><<<wave_grid, kBlock, 0, s>>>(P, cur, b, q);
+                launch_shade(modes, instanced, -1, wave_grid, s, P, cur, b, q, whole);
             }
-            if (instanced) k_shadow<2, 128><<<trace_grid, tb, 0, s>>>(P);
+            if (instanced && tb == 256) k_shadow<2, 256><<<trace_grid, tb, kInstStackBytes, s>>>(P);
+            else if (instanced) k_shadow<2, 128><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0 && tb == 256) k_shadow<0, 256><<<trace_grid, tb, 0, s>>>(P);
             else if (bvh_kind == 0) k_shadow<0, 128><<<trace_grid, tb, 0, s>>>(P);
             else k_shadow<1, 128><<<trace_grid, tb, 0, s>>>(P);
@@ -834,7 +917,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes, instanced, texture, ray_sort, face_order;
+        uint32_t modes, instanced, texture, ray_sort, face_order, kinds;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -848,6 +931,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.texture = texture ? 1u : 0u;
     key.ray_sort = ray_sort ? 1u : 0u;
     key.face_order = face_order ? 1u : 0u;
+    key.kinds = kinds;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -873,7 +957,8 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     const uint64_t batches = (job.total + st.capacity - 1) / st.capacity;
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
                           trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr,
-                          pt_scene_textured(sc), sc.ray_sort != 0, std::min<uint64_t>(job.total, st.capacity));
+                          pt_scene_textured(sc), sc.ray_sort != 0, std::min<uint64_t>(job.total, st.capacity),
+                          sc.shader_kinds);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -432,6 +432,14 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.ptex_face_count = sc->ptex_face_count;
     for (int i = 0; i < 3; ++i) ps.background[i] = sc->background[i];
     ps.sort_hint = (sc->sort_hint && sc->dev->material_sort) ? 1u : 0u;
+    {
+        uint32_t mask = 0;
+        bool ptex = false;
+        tree_classes(sc, mask, ptex);
+        ps.shader_kinds = 0u;
+        for (uint32_t k = 0; k < 3u; ++k)
+            if ((mask >> (4u * k)) & 15u) ps.shader_kinds |= 1u << k;
+    }
     ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     ps.ibl = static_cast<const IblDev*>(sc->d_ibl);
     ps.attrs = static_cast<const MeshAttrDev*>(sc->d_attrs);
@@ -558,7 +566,7 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
                        sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
-                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0, batch_paths);
+                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0, batch_paths, ps.shader_kinds);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
 }
 
@@ -1064,7 +1072,8 @@ int sel_scene_autotune(SelScene scene, const SelCamera* camera, const SelPtSetti
         int kind;
         uint32_t leaf;
     };
-    const Layout layouts[] = {{SEL_BVH_WIDE8_Q8, 2}, {SEL_BVH_WIDE8_Q8, 3}, {SEL_BVH_WIDE8_Q8, 4}, {SEL_BVH_BINARY_FP32, 3}};
+    const Layout layouts[] = {{SEL_BVH_WIDE8_Q8, 2}, {SEL_BVH_WIDE8_Q8, 3}, {SEL_BVH_WIDE8_Q8, 4}, {SEL_BVH_WIDE8_Q8, 8},
+                              {SEL_BVH_BINARY_FP32, 3}};
     const uint32_t capacities[] = {1u << 20, 1u << 22, 1u << 23};
     const int blocks[] = {128, 256};
     const size_t values = 2ull * camera->width * camera->height * 3;
@@ -1093,8 +1102,8 @@ int sel_scene_autotune(SelScene scene, const SelCamera* camera, const SelPtSetti
         if (sel_scene_commit(scene) != SEL_OK) continue;  // e.g. a tree deeper than a traversal stack
         for (uint32_t cap : capacities)
             for (int block : blocks) {
-                // 256-thread traversal blocks exist for the flat 8-wide layout only
-                if (block == 256 && (L.kind != SEL_BVH_WIDE8_Q8 || !scene->instances.empty())) continue;
+                // 256-thread traversal blocks exist for the 8-wide layout only
+                if (block == 256 && L.kind != SEL_BVH_WIDE8_Q8) continue;
                 SelPtSettings st = *settings;
                 st.pathsInFlight = cap;
                 st.traceBlockSize = uint32_t(block);

@@ -30,7 +30,8 @@ static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 //   origin p (float3), per-axis exponent byte e (scale = 2^(e-127)), internal-child mask imask,
 //   child_base (index of the first internal child; internal children are contiguous in slot order),
 //   tri_base (index of the first triangle; leaf children are contiguous),
-//   meta[8]: leaf slot -> (count << 5) | offset, count in 1..3, offset in 0..23; 0 for internal/empty,
+//   meta[8]: leaf slot -> ((count - 1) << 5) | offset, count in 1..8, offset + count <= 32 (a node's leaf
+//   children hold 32 records at most); kLeafNone (0xff) for internal and empty slots,
 //   qlo/qhi[axis][8]: child box = p + scale * q, rounded outward when built.
 struct WideNode {
     float p[3];
@@ -43,6 +44,9 @@ struct WideNode {
     uint8_t qhi[3][8];
 };
 static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
+constexpr uint32_t kLeafNone = 0xffu;       // WideNode::meta of a slot that is not a leaf
+constexpr uint32_t kMaxNodeRecords = 32u;   // leaf records under one node (the traversal's 32-bit record mask)
+constexpr uint32_t kMaxLeafRecords = 8u;    // records of one leaf slot
 
 // Binary node with FP32 child boxes (64 bytes = 4 x float4):
 //   [c0.lo.x c0.hi.x c0.lo.y c0.hi.y] [c1.lo.x c1.hi.x c1.lo.y c1.hi.y] [c0.lo.z c0.hi.z c1.lo.z c1.hi.z]

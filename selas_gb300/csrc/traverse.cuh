@@ -162,7 +162,7 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t byte) {
 
 // Visits the nearest pending node of s.group (which must have one): pushes the rest of the group, tests the
 // node's eight child boxes, makes its hit internal children the new group and returns the triangles of its
-// hit leaf children as a bit mask over records tbase..tbase+23.  Returns false on stack overflow.
+// hit leaf children as a bit mask over records tbase..tbase+31.  Returns false on stack overflow.
 template <int kDepth>
 __device__ __forceinline__ bool wide_visit(WideState& s, const uint4* __restrict__ nodes, uint2* stack, int stride,
                                            uint32_t& status, uint32_t& tmask, uint32_t& tbase) {
@@ -207,7 +207,7 @@ __device__ __forceinline__ bool wide_visit(WideState& s, const uint4* __restrict
                 new_hits |= 1u << (uint32_t(c) ^ s.oct);
             } else {
                 const uint32_t meta = ((c < 4 ? n1.z : n1.w) >> (8 * byte)) & 0xffu;
-                tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+                if (meta != kLeafNone) tmask |= (0xffu >> (7u - (meta >> 5))) << (meta & 31u);
             }
         }
     }

@@ -180,7 +180,8 @@ def test_untraceable_rays_miss_like_the_bruteforce_definition(device, kind):
     sc.release()
 
 
-@pytest.mark.parametrize("n_spheres,level,leaf", [(1, 0, 3), (3, 2, 3), (8, 4, 3), (8, 4, 1), (8, 4, 2), (8, 4, 4)])
+@pytest.mark.parametrize("n_spheres,level,leaf", [(1, 0, 3), (3, 2, 3), (8, 4, 3), (8, 4, 1), (8, 4, 2), (8, 4, 4),
+                                                   (8, 4, 8), (3, 2, 8)])
 def test_device_built_bvh_matches_bruteforce(device, n_spheres, level, leaf):
     """The 8-wide BVH built by the GPU kernels (SEL_BUILD_DEVICE) answers every query as the definition does,
     from a 20-triangle scene (one warp builds the whole tree) to 80 k triangles (large-task levels first)."""
@@ -202,6 +203,39 @@ def test_device_built_bvh_matches_bruteforce(device, n_spheres, level, leaf):
         sc.occluded1M(rg)
         oracle.occluded_bruteforce(soup, rw)
         assert_hits_equal(rg, rw, fields=("tfar",))
+    sc.release()
+
+
+@pytest.mark.parametrize("leaf", [5, 8])
+def test_device_built_leaves_beyond_a_nodes_records_move_down(device, leaf):
+    """4096 copies of one triangle (and a few jittered ones) cannot be split by position: the tree is all full
+    leaves, so eight of them under one node would hold more than the node's 32 records and the largest move one
+    level down.  Every query still returns the definition's hit, including the tie rule among coincident
+    triangles (smallest t, then geomID and primID)."""
+    rng = np.random.default_rng(12)
+    tri = np.float32([[-1, -1, 0], [1, -1, 0], [0, 1, 0]])
+    copies = np.tile(tri, (4096, 1, 1))
+    jitter = tri[None] + rng.normal(scale=0.05, size=(64, 3, 3)).astype(np.float32)
+    g = scenes.TriangleScene()
+    for gid, block in enumerate((copies, jitter)):
+        g.add(gid, block.reshape(-1, 3), np.arange(block.shape[0] * 3, dtype=np.uint32).reshape(-1, 3))
+    soup = g.soup()
+    sc = sel.Scene(device, sel.SEL_BVH_WIDE8_Q8, sel.SEL_BUILD_DEVICE)
+    sc.set_leaf_size(leaf)
+    g.attach_to(sc)
+    sc.commit()
+    n = 4000
+    org = np.column_stack([rng.uniform(-1.2, 1.2, n), rng.uniform(-1.2, 1.2, n), np.full(n, -5.0)]).astype(np.float32)
+    d = np.column_stack([rng.normal(scale=0.02, size=(n, 2)), np.ones(n)]).astype(np.float32)
+    got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+    sc.intersect1M(got)
+    oracle.intersect_bruteforce(soup, want)
+    assert_hits_equal(got, want)
+    assert (got["geomID"] != 0xFFFFFFFF).mean() > 0.3
+    rg, rw = sel.make_rays(org, d), sel.make_rays(org, d)
+    sc.occluded1M(rg)
+    oracle.occluded_bruteforce(soup, rw)
+    assert_hits_equal(rg, rw, fields=("tfar",))
     sc.release()
 
 
