@@ -412,11 +412,40 @@ typedef struct SelPtexFace {
 int sel_ptex_filter_device(SelDevice device, const SelPtexFace* d_faces, unsigned int nfaces, const uint16_t* d_texels,
                            const float* d_queries, unsigned int n, float* d_out, void* stream);
 
-/* Binds a Ptex texture to geometry geomID (replaces TextureCache::FetchPtex of the per-mesh .ptx,
+/* Binds a Ptex texture to triangle mesh geomID (replaces TextureCache::FetchPtex of the per-mesh .ptx,
  * Source/Core/TextureLib/TextureCache.cpp:168-185): face_count must equal the geometry's triangle count;
- * materials with usesPtex take their base colour from it.  Host arrays, copied. */
+ * materials with usesPtex take their base colour from it.  Host arrays, copied.  A quad mesh: use
+ * sel_scene_set_ptex_quads. */
 int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* faces, size_t face_count,
                        const uint16_t* texels, size_t texel_count);
+
+/* One quad face of a Ptex texture (Ptex FaceInfo of an mt_quad texture): square resolution 2^log2 (all faces of
+ * a mesh share it), texel offset (in texels), neighbouring face across edge i (bottom, right, top, left: edge i
+ * runs from vertex i to vertex i + 1, u along edge 0, v along edge 3 reversed; -1 = boundary) and the
+ * neighbour's edge id for that edge.  40 bytes. */
+typedef struct SelPtexQuadFace {
+    int32_t log2;
+    uint32_t offset;
+    int32_t adjfaces[4];
+    int32_t adjedges[4];
+} SelPtexQuadFace;
+
+/* Binds a Ptex texture to quad mesh geomID: face_count must equal the geometry's quad count (face q is quad q,
+ * sampled at the quad's (u, v) as Embree reports them).  Materials with usesPtex take their base colour from the
+ * separable bicubic filter with B-spline weights that PtexFilter::getFilter(f_bspline) gives a quad texture
+ * (Middleware/ptex/Include/PtexFilters.cpp:116-285,419-441, PtexSeparableFilter.cpp:47-359), with filter
+ * widths 0 as SurfaceParameters.cpp:196-206 evaluates it.  Faces whose texels are all equal, and such faces
+ * amid equal neighbours, take the reader's constant-face forms (flagged here as the Ptex writer flags them).
+ * Host arrays, copied. */
+int sel_scene_set_ptex_quads(SelScene scene, unsigned int geomID, const SelPtexQuadFace* faces, size_t face_count,
+                             const uint16_t* texels, size_t texel_count);
+
+/* The quad filter on device arrays (as sel_ptex_filter_device): d_faces holds nfaces SelPtexQuadFace records,
+ * d_texels half RGB, d_queries n x (face id as int32 bits, u, v); d_out n x 3 (rows of invalid face ids left
+ * untouched).  Needs no scene; asynchronous on `stream`. */
+int sel_ptex_quad_filter_device(SelDevice device, const SelPtexQuadFace* d_faces, unsigned int nfaces,
+                                const uint16_t* d_texels, const float* d_queries, unsigned int n, float* d_out,
+                                void* stream);
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Integrator entry points.                                                                          */

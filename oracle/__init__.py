@@ -33,6 +33,8 @@ def lib() -> ctypes.CDLL:
             "oracle_bsdf_evaluate": ([_vp, _vp, _vp, _i64, _vp], None),
             "oracle_bsdf_sample": ([_vp, _vp, _vp, _i64, _vp], None),
             "oracle_ptex_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
+            "oracle_ptex_quad_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
+            "oracle_set_quad_ptex": ([_i, _vp, _vp, _vp, _vp, _vp], None),
             "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
@@ -189,10 +191,32 @@ def set_textures(parts):
             off += rgba.size
     if not keys:
         lib().oracle_set_textures(0, None, None, None, None)
+    else:
+        k, d = np.asarray(keys, np.uint32), np.asarray(dims, np.uint32)
+        o, r = np.asarray(offs, np.int64), np.ascontiguousarray(np.concatenate(data))
+        lib().oracle_set_textures(len(offs), _p(k), _p(d), _p(o), _p(r))
+    set_quad_ptex(parts)
+
+
+def set_quad_ptex(parts):
+    """Quad-mesh Ptex textures of the next oracle renders: those of the RenderScenes `parts` (scene index =
+    position), face rows (n, 10) and half texels each."""
+    keys, row_offs, rows, tex_offs, texels = [], [0], [], [0], []
+    for si, p in enumerate(parts):
+        tables = p.quad_ptex_tables() if hasattr(p, "quad_ptex_tables") else []
+        for gid, r, t in tables:
+            keys += [si, gid]
+            rows.append(r.reshape(-1))
+            row_offs.append(row_offs[-1] + r.shape[0])
+            texels.append(t.reshape(-1))
+            tex_offs.append(tex_offs[-1] + t.size)
+    if not keys:
+        lib().oracle_set_quad_ptex(0, None, None, None, None, None)
         return
-    k, d = np.asarray(keys, np.uint32), np.asarray(dims, np.uint32)
-    o, r = np.asarray(offs, np.int64), np.ascontiguousarray(np.concatenate(data))
-    lib().oracle_set_textures(len(offs), _p(k), _p(d), _p(o), _p(r))
+    k = np.asarray(keys, np.uint32)
+    ro, to = np.asarray(row_offs, np.int64), np.asarray(tex_offs, np.int64)
+    R, T = np.ascontiguousarray(np.concatenate(rows)), np.ascontiguousarray(np.concatenate(texels))
+    lib().oracle_set_quad_ptex(len(keys) // 2, _p(k), _p(ro), _p(R), _p(to), _p(T))
 
 
 def ibl_sample(ibl, r):
@@ -415,6 +439,16 @@ def instanced_query(scenes, top, rays, any_hit=False, nthreads=None):
     Q = np.array(proto, np.uint32)
     lib().oracle_instanced_query(len(scenes), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(W), _p(I), _p(H), _p(Q),
                                  W.shape[0], top, _p(rays), rays.shape[0], int(any_hit), nthreads or threads())
+
+
+def ptex_quad_eval(faces, texels_u16, queries):
+    """Oracle Ptex quad filter (oracle_ptex_quad.cpp): faces (n, 10), queries (m, 3) = (face bits, u, v) -> (m, 3)."""
+    faces = np.ascontiguousarray(faces, np.int32)
+    texels_u16 = np.ascontiguousarray(texels_u16, np.uint16)
+    queries = np.ascontiguousarray(queries, np.float32)
+    out = np.zeros((queries.shape[0], 3), np.float32)
+    lib().oracle_ptex_quad_eval(_p(faces), faces.shape[0], _p(texels_u16), _p(queries), queries.shape[0], _p(out))
+    return out
 
 
 def ptex_eval(faces, texels_u16, queries):

@@ -24,6 +24,9 @@ void frame_through(uint32_t scene, uint32_t geom, uint32_t prim, float u, float 
 // SurfaceParameters.cpp:186-213 with TextureFiltering::Triangle at level 0, Repeat wrapping, sRGB to linear): uvs
 // from attribute slot 2 ((0, 0) without them).  False when no image is bound.
 bool tex2d(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]);
+// the quad-mesh Ptex bound to (scene, geom) at soup triangle prim (2 * quad + half) with its barycentrics; false
+// when none is bound
+bool quad_ptex(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]);
 
 // One component k of a vertex attribute at a hit, from the soup's corner arrays (`per` floats per corner, three
 // corners per soup triangle): (1 - u - v) a0 + u a1 + v a2 on a triangle; on a quad mesh (flags bit 8, soup

@@ -25,6 +25,7 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <random>
 #include <thread>
 #include <vector>
@@ -439,8 +440,12 @@ void surface_at(const Scene& sc, const orq::Hit& h, V3 pos, V3 dir, SurfHit& o) 
     shading_frame(sc, h, n, t, b);
     s.t = t; s.n = n; s.b = b;
     float base[3] = {m.base[0], m.base[1], m.base[2]};
-    if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
-    else ora::tex2d(sc.graph ? h.scene : 0u, h.geom, h.prim, h.u, h.v, base);
+    if ((m.flags & 2u) && ora::quad_ptex(sc.graph ? h.scene : 0u, h.geom, h.prim, h.u, h.v, base)) {
+    } else if ((m.flags & 2u) && ptex) {
+        ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    } else {
+        ora::tex2d(sc.graph ? h.scene : 0u, h.geom, h.prim, h.u, h.v, base);
+    }
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
     s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
     s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;
@@ -804,6 +809,7 @@ struct Tex2D {
     std::vector<float> rgba;
 };
 static std::map<uint64_t, Tex2D> g_tex2d;
+static std::map<uint64_t, std::unique_ptr<orp::QuadTexture>> g_quad_ptex;  // (scene, geom) -> quad-mesh Ptex
 
 static void index_attrs(const uint32_t* prim, const uint32_t* geom, const uint32_t* tri_scene, int64_t ntri) {
     g_attrs.first.clear();
@@ -1015,9 +1021,30 @@ void oracle_set_textures(int n, const uint32_t* keys, const uint32_t* dims, cons
     }
 }
 
+// Quad-mesh Ptex textures of the following renders: n textures, texture k bound to (scene, geom) = keys[2k],
+// keys[2k + 1], its face rows (10 ints each) rows[row_offsets[k] .. row_offsets[k + 1]) and half RGB texels
+// texels[texel_offsets[k] .. texel_offsets[k + 1]) (in halfs).
+void oracle_set_quad_ptex(int n, const uint32_t* keys, const int64_t* row_offsets, const int32_t* rows,
+                          const int64_t* texel_offsets, const uint16_t* texels) {
+    g_quad_ptex.clear();
+    for (int k = 0; k < n; ++k)
+        g_quad_ptex[(uint64_t(keys[2 * k]) << 32) | keys[2 * k + 1]] = std::make_unique<orp::QuadTexture>(
+            rows + 10 * row_offsets[k], int(row_offsets[k + 1] - row_offsets[k]), texels + texel_offsets[k],
+            size_t(texel_offsets[k + 1] - texel_offsets[k]));
+}
+
 }  // extern "C"
 
 namespace ora {
+
+bool quad_ptex(uint32_t scene, uint32_t geom, uint32_t prim, float u, float v, float rgb[3]) {
+    const auto it = g_quad_ptex.find((uint64_t(scene) << 32) | geom);
+    if (it == g_quad_ptex.end()) return false;
+    // soup triangle 2q + half of quad q: Embree's quad (u, v) is (1 - u, 1 - v) on the second half
+    const bool second = (prim & 1u) != 0u;
+    it->second->eval(int(prim >> 1), second ? 1.0f - u : u, second ? 1.0f - v : v, rgb);
+    return true;
+}
 
 float corner_interp(const std::vector<float>& arr, int per, int64_t tri, uint8_t flags, uint32_t prim, float u, float v,
                     int k) {

@@ -18,4 +18,16 @@ private:
     const uint16_t* texels;
 };
 
+// rows: n x 10 ints (log2, texel offset, adj0..3, adjedge0..3) of a quad-mesh texture; texels: half RGB (copied,
+// with the writer's constant-face flags computed from them).
+class QuadTexture {
+public:
+    QuadTexture(const int32_t* rows, int n, const uint16_t* texels, size_t texel_count);
+    ~QuadTexture();
+    bool eval(int face, float u, float v, float* out) const;
+
+private:
+    void* state;
+};
+
 }  // namespace orp

@@ -179,8 +179,12 @@ bool make_hit(const Scene& sc, V3 org, V3 dir, Hit& out) {
     orc::Surf& s = out.s;
     s.t = V3(ft[0], ft[1], ft[2]); s.n = n; s.b = V3(fb[0], fb[1], fb[2]);
     float base[3] = {m.base[0], m.base[1], m.base[2]};
-    if ((m.flags & 2u) && ptex) ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
-    else ora::tex2d(h.scene, h.geom, h.prim, h.u, h.v, base);
+    if ((m.flags & 2u) && ora::quad_ptex(h.scene, h.geom, h.prim, h.u, h.v, base)) {
+    } else if ((m.flags & 2u) && ptex) {
+        ptex->eval(int(m.ptex_base + h.prim), h.u, h.v, base);
+    } else {
+        ora::tex2d(h.scene, h.geom, h.prim, h.u, h.v, base);
+    }
     s.baseColor = V3(std::pow(base[0], 2.2f), std::pow(base[1], 2.2f), std::pow(base[2], 2.2f));
     s.transmittanceColor = V3(m.trans[0], m.trans[1], m.trans[2]);
     s.sheen = m.sheen; s.sheenTint = m.sheenTint; s.clearcoat = m.clearcoat; s.clearcoatGloss = m.clearcoatGloss;

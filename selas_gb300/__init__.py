@@ -328,6 +328,8 @@ register_signatures({
     "sel_pt_generate_image": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp],
     "sel_ptex_filter_device": [_vp, _vp, _u, _vp, _vp, _u, _vp, _vp],
     "sel_scene_set_ptex": [_vp, _u, _vp, _sz, _vp, _sz],
+    "sel_scene_set_ptex_quads": [_vp, _u, _vp, _sz, _vp, _sz],
+    "sel_ptex_quad_filter_device": [_vp, _vp, _u, _vp, _vp, _u, _vp, _vp],
     "sel_pt_render_device": [_vp, ctypes.POINTER(SelCamera), ctypes.POINTER(SelPtSettings), _vp, _vp],
     "sel_vcm_settings_defaults": [ctypes.POINTER(SelVcmSettings)],
     "sel_device_set_option": [_vp, ctypes.c_int, ctypes.c_int],
@@ -497,10 +499,12 @@ def _scene_vcm_generate_image(self, cam: SelCamera, settings: SelVcmSettings) ->
 
 
 def _scene_set_ptex(self, geom_id: int, rows: np.ndarray, texels: np.ndarray) -> None:
-    """Binds per-face Ptex texels (rows: (n, 8) int32 SelPtexFace records; texels: float16 RGB)."""
+    """Binds per-face Ptex texels (rows: (n, 8) int32 SelPtexFace records of a triangle mesh, or (n, 10) int32
+    SelPtexQuadFace records of a quad mesh; texels: float16 RGB)."""
     r = np.ascontiguousarray(rows, np.int32)
     t = np.ascontiguousarray(np.asarray(texels, np.float16).view(np.uint16))
-    check(lib().sel_scene_set_ptex(self.handle, geom_id, r.ctypes.data, r.shape[0], t.ctypes.data, t.size))
+    fn = lib().sel_scene_set_ptex_quads if r.shape[1] == 10 else lib().sel_scene_set_ptex
+    check(fn(self.handle, geom_id, r.ctypes.data, r.shape[0], t.ctypes.data, t.size))
 
 
 Scene.set_ptex = _scene_set_ptex

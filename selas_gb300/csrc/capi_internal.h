@@ -70,7 +70,8 @@ struct SelSceneTy {
     bool shading_dirty = true;
     struct PtexBinding {
         uint32_t geomID;
-        std::vector<SelPtexFace> faces;
+        bool quads = false;               // sel_scene_set_ptex_quads: faces hold PtexQuadFace records
+        std::vector<SelPtexFace> faces;   // 32-byte face records (triangle faces or quad faces)
         std::vector<uint16_t> texels;
     };
     std::vector<PtexBinding> ptex;
@@ -113,6 +114,8 @@ struct VcmSettings;
 int sync_shading(SelSceneTy* sc);              // uploads materials, lights, Ptex and the IBL when they changed
 // sel_scene_set_material with the eTransparent flag given instead of derived (cooked materials keep theirs)
 int set_material_flags(SelSceneTy* sc, unsigned int geomID, const SelMaterial& material, bool transparent);
+// The Ptex writer's constant and constant-neighbourhood flags of `count` PtexQuadFace records (ptex_quad.cuh)
+void flag_constant_quads(void* records, size_t count, const uint16_t* texels);
 // capi.cpp: `top` releases `scenes` (created after the scenes they instance) when it is released
 void adopt_scenes(SelSceneTy* top, const std::vector<SelSceneTy*>& scenes);
 // CalculateIntensityMap + CalculateStrataDistributionFunctions (BuildImageBasedLight.cpp:18-107): marginal CDF

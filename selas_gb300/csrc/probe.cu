@@ -9,6 +9,7 @@
 #include "ibl.cuh"
 #include "pt.h"
 #include "ptex.cuh"
+#include "ptex_quad.cuh"
 #include "shading.cuh"
 #include "tex2d.cuh"
 
@@ -38,8 +39,8 @@ __global__ void k_surface_probe(PtScene S, const float* __restrict__ hits, const
     float3 base = ld3(m.base_color);
     if (m.flags & kMaterialUsesPtex) {
         uint32_t status = 0;
-        ptex_eval(static_cast<const PtexFace*>(S.ptex_faces), int(S.ptex_face_count),
-                  static_cast<const __half*>(S.ptex_texels), int(m.ptex_base + prim), u, v, base, status);
+        ptex_material_eval(m, S.ptex_faces, int(S.ptex_face_count), static_cast<const __half*>(S.ptex_texels), prim, u,
+                           v, base, status);
         if (status) atomicOr(err, status);
     } else if (m.flags & kMaterialUsesTexture) {
         base = tex2d_base_colour(m, attr, prim, u, v);

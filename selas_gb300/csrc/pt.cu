@@ -34,6 +34,7 @@
 #include "hitref.cuh"
 #include "instance.cuh"
 #include "ptex.cuh"
+#include "ptex_quad.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
 #include "tex2d.cuh"
@@ -345,7 +346,10 @@ __global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
             const uint32_t geom = __float_as_uint(p1.w);
             const MaterialDev& m = r.mats[geom < r.mat_count ? geom : 0];
             key = class_of(m) << 20;
-            if (m.flags & kMaterialUsesPtex) {
+            if (m.flags & kMaterialPtexQuad) {  // the quad's face; no footprint region
+                const int face = int(m.ptex_base + (__float_as_uint(p0.w) >> 1));
+                key |= (uint32_t(face) & 0x1ffffu) << 3;
+            } else if (m.flags & kMaterialUsesPtex) {
                 const int face = int(m.ptex_base + __float_as_uint(p0.w));
                 key |= ((uint32_t(face) & 0x1ffffu) << 3) |
                        ptex_region(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count), face, hit.y, hit.z);
@@ -378,9 +382,8 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const u
         float3 base = ld3(m.base_color);
         if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_eval(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count),
-                      static_cast<const __half*>(r.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
-                      hit.z, base, pstatus);
+            ptex_material_eval(m, r.ptex_faces, int(r.ptex_count), static_cast<const __half*>(r.ptex_texels),
+                               __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
             status |= pstatus;
         } else {
             base = tex2d_base_colour(m, geom < r.attr_count ? r.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
@@ -768,13 +771,22 @@ size_t pt_state_block_bytes(uint32_t paths) {
     return total;
 }
 
+// Shader-specific kernels for the solid and Dirac shaders of single-integrator batches; thin surfaces and mixed
+// batches take the kernel for every shader (each specialisation is compiled once per integrator and instancing).
 template <uint32_t kModes, bool kInst>
 void launch_shade_modes(int shader, int grid, cudaStream_t s, const PtParams& P, int cur, uint32_t b,
                         const uint32_t* q, int2 classes) {
-    if (shader == 0) k_shade<kModes, kInst, 0><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
-    else if (shader == 1) k_shade<kModes, kInst, 1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
-    else if (shader == 2) k_shade<kModes, kInst, 2><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
-    else k_shade<kModes, kInst, -1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+    if constexpr (kModes != 3u) {
+        if (shader == 1) {
+            k_shade<kModes, kInst, 1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+            return;
+        }
+        if (shader == 2) {
+            k_shade<kModes, kInst, 2><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
+            return;
+        }
+    }
+    k_shade<kModes, kInst, -1><<<grid, kBlock, 0, s>>>(P, cur, b, q, classes);
 }
 
 void launch_shade(uint32_t modes, bool inst, int shader, int grid, cudaStream_t s, const PtParams& P, int cur,
@@ -827,7 +839,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
                                                       : reinterpret_cast<const void*>(&k_shade<1, false, -1>));
     // shading launches: one kernel for the jobs' single shader over the whole queue; with several shaders and the
     // class order, one per shader over its classes (1 + shader * 4 .. 4 + shader * 4; the misses, class 0, with
-    // the first); else the kernel for every shader
+    // the thin shader's); else the kernel for every shader
     const uint32_t kinds = shader_kinds & 7u;
     const bool one_kind = kinds != 0u && (kinds & (kinds - 1u)) == 0u;
     const int single = one_kind ? __builtin_ctz(kinds) : -1;
@@ -879,7 +891,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             if (one_kind) {
                 launch_shade(modes, instanced, single, wave_grid, s, P, cur, b, q, whole);
             } else if (sort) {
-                launch_shade(modes, instanced, 0, wave_grid, s, P, cur, b, q, make_int2(0, 4));
+                launch_shade(modes, instanced, -1, wave_grid, s, P, cur, b, q, make_int2(0, 4));
                 if (kinds & 2u) launch_shade(modes, instanced, 1, wave_grid, s, P, cur, b, q, make_int2(5, 8));
                 if (kinds & 4u) launch_shade(modes, instanced, 2, wave_grid, s, P, cur, b, q, make_int2(9, 12));
             } else {

@@ -9,6 +9,7 @@
 #include "capi_internal.h"
 #include "ibl.cuh"
 #include "pt.h"
+#include "ptex_quad.cuh"
 #include "vcm.h"
 
 using namespace sel;
@@ -253,13 +254,25 @@ int sync_shading(SelSceneTy* sc) {
         const uint32_t face_base = uint32_t(faces.size());
         const uint32_t texel_base = uint32_t(texels.size() / 3);
         for (SelPtexFace f : pb.faces) {
-            f.offset += texel_base;
-            for (int e = 0; e < 3; ++e)
-                if (f.adjfaces[e] >= 0) f.adjfaces[e] += int32_t(face_base);
+            if (pb.quads) {
+                PtexQuadFace q;
+                std::memcpy(&q, &f, sizeof(q));
+                q.offset += texel_base;
+                for (int e = 0; e < 4; ++e)
+                    if (q.adj[e] >= 0) q.adj[e] += int32_t(face_base);
+                std::memcpy(&f, &q, sizeof(q));
+            } else {
+                f.offset += texel_base;
+                for (int e = 0; e < 3; ++e)
+                    if (f.adjfaces[e] >= 0) f.adjfaces[e] += int32_t(face_base);
+            }
             faces.push_back(f);
         }
         texels.insert(texels.end(), pb.texels.begin(), pb.texels.end());
-        if (pb.geomID < mats.size()) mats[pb.geomID].ptex_base = face_base;
+        if (pb.geomID < mats.size()) {
+            mats[pb.geomID].ptex_base = face_base;
+            mats[pb.geomID].flags = (mats[pb.geomID].flags & ~kMaterialPtexQuad) | (pb.quads ? kMaterialPtexQuad : 0u);
+        }
     }
     for (auto& m : mats) {
         bool bound = false;
@@ -334,6 +347,59 @@ int sync_shading(SelSceneTy* sc) {
     }
     sc->shading_dirty = false;
     return SEL_OK;
+}
+
+// The Ptex writer's face flags for a quad-mesh texture (PtexWriter.cpp:814-816,996-1075, clamp borders, no
+// subfaces): a face whose texels all have the same bits is constant; a constant face is neighbourhood-constant
+// when, around each of its vertices (clockwise, and counter-clockwise from a boundary), every face is constant
+// with the same value.  The filter applies a constant face through its kernel weight and returns a
+// neighbourhood-constant face's value directly, as the reader does.
+void flag_constant_quads(void* records, size_t count, const uint16_t* texels) {
+    PtexQuadFace* faces = static_cast<PtexQuadFace*>(records);
+    for (size_t i = 0; i < count; ++i) {
+        PtexQuadFace& f = faces[i];
+        const size_t n = size_t(1) << (2 * (f.log2_flags & 0xffu));
+        const uint16_t* d = texels + size_t(f.offset) * 3;
+        bool c = true;
+        for (size_t i = 1; i < n && c; ++i) c = std::memcmp(d, d + 3 * i, 6) == 0;
+        if (c) f.log2_flags |= kQuadConstant;
+    }
+    const int n = int(count);
+    auto edge = [&](int f, int e) { return int((faces[f].adjedge >> (8 * e)) & 3u); };
+    for (int faceid = 0; faceid < n; ++faceid) {
+        PtexQuadFace& f = faces[faceid];
+        if (!(f.log2_flags & kQuadConstant)) continue;
+        const uint16_t* cd = texels + size_t(f.offset) * 3;
+        auto same = [&](int a) {
+            return (faces[a].log2_flags & kQuadConstant) && std::memcmp(cd, texels + size_t(faces[a].offset) * 3, 6) == 0;
+        };
+        bool is_const = true;
+        for (int eid = 0; is_const && eid < 4; ++eid) {
+            int afid = f.adj[eid], aeid = edge(faceid, eid);
+            int count = 0;
+            while (afid != faceid && afid >= 0 && ++count < 10) {
+                if (!same(afid)) { is_const = false; break; }
+                const int next = (aeid + 1) % 4;
+                const int nf = faces[afid].adj[next];
+                aeid = edge(afid, next);
+                afid = nf;
+            }
+            if (afid < 0 && is_const) {
+                aeid = (aeid + 3) % 4;
+                afid = f.adj[aeid];
+                aeid = edge(faceid, aeid);
+                count = 0;
+                while (afid != faceid && afid >= 0 && ++count < 10) {
+                    if (!same(afid)) { is_const = false; break; }
+                    const int prev = (aeid + 3) % 4;
+                    const int nf = faces[afid].adj[prev];
+                    aeid = edge(afid, prev);
+                    afid = nf;
+                }
+            }
+        }
+        if (is_const) f.log2_flags |= kQuadNbConstant;
+    }
 }
 
 int set_material_flags(SelSceneTy* scene, unsigned int geomID, const SelMaterial& material, bool transparent) {
@@ -776,8 +842,7 @@ int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* f
         if (m.geomID == geomID) mesh = &m;
     if (!mesh) return fail(SEL_ERR_INVALID_ARGUMENT, "no geometry with this geomID");
     if (mesh->quads)
-        return fail(SEL_ERR_INVALID_OPERATION,
-                    "Ptex on quad meshes (the separable bicubic filter) is not supported: triangle meshes only");
+        return fail(SEL_ERR_INVALID_OPERATION, "a quad mesh takes its Ptex texture through sel_scene_set_ptex_quads");
     if (face_count != mesh->indices.size() / 3)
         return fail(SEL_ERR_INVALID_ARGUMENT, "face_count must equal the geometry's triangle count");
     for (size_t i = 0; i < face_count; ++i) {
@@ -794,6 +859,54 @@ int sel_scene_set_ptex(SelScene scene, unsigned int geomID, const SelPtexFace* f
     SelSceneTy::PtexBinding pb;
     pb.geomID = geomID;
     pb.faces.assign(faces, faces + face_count);
+    pb.texels.assign(texels, texels + texel_count);
+    for (auto& existing : scene->ptex)
+        if (existing.geomID == geomID) {
+            existing = std::move(pb);
+            scene->shading_dirty = true;
+            return SEL_OK;
+        }
+    scene->ptex.push_back(std::move(pb));
+    scene->shading_dirty = true;
+    return SEL_OK;
+}
+
+int sel_scene_set_ptex_quads(SelScene scene, unsigned int geomID, const SelPtexQuadFace* faces, size_t face_count,
+                             const uint16_t* texels, size_t texel_count) {
+    if (!scene || (face_count && !faces) || (texel_count && !texels)) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
+    if (geomID >= kMaxGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 65536");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    const MeshInput* mesh = nullptr;
+    for (const MeshInput& m : scene->meshes)
+        if (m.geomID == geomID) mesh = &m;
+    if (!mesh) return fail(SEL_ERR_INVALID_ARGUMENT, "no geometry with this geomID");
+    if (!mesh->quads) return fail(SEL_ERR_INVALID_OPERATION, "the geometry is not a quad mesh: use sel_scene_set_ptex");
+    if (face_count != mesh->indices.size() / 6)
+        return fail(SEL_ERR_INVALID_ARGUMENT, "face_count must equal the geometry's quad count");
+    std::vector<PtexQuadFace> q(face_count);
+    for (size_t i = 0; i < face_count; ++i) {
+        const SelPtexQuadFace& f = faces[i];
+        if (f.log2 < 0 || f.log2 > 12) return fail(SEL_ERR_INVALID_ARGUMENT, "face log2 resolution out of range");
+        if (f.log2 != faces[0].log2) return fail(SEL_ERR_INVALID_ARGUMENT, "all faces must share one resolution");
+        const uint64_t need = uint64_t(f.offset) + (uint64_t(1) << (2 * f.log2));
+        if (need * 3 > texel_count) return fail(SEL_ERR_INVALID_ARGUMENT, "face texels exceed the texel array");
+        q[i].log2_flags = uint32_t(f.log2);
+        q[i].offset = f.offset;
+        q[i].adjedge = 0;
+        q[i].pad = 0;
+        for (int e = 0; e < 4; ++e) {
+            if (f.adjfaces[e] >= int64_t(face_count) || f.adjfaces[e] < -1 || f.adjedges[e] < 0 || f.adjedges[e] > 3)
+                return fail(SEL_ERR_INVALID_ARGUMENT, "adjacency out of range");
+            q[i].adj[e] = f.adjfaces[e];
+            q[i].adjedge |= uint32_t(f.adjedges[e]) << (8 * e);
+        }
+    }
+    sel::flag_constant_quads(q.data(), q.size(), texels);
+    SelSceneTy::PtexBinding pb;
+    pb.geomID = geomID;
+    pb.quads = true;
+    pb.faces.resize(face_count);
+    if (face_count) std::memcpy(pb.faces.data(), q.data(), face_count * sizeof(PtexQuadFace));
     pb.texels.assign(texels, texels + texel_count);
     for (auto& existing : scene->ptex)
         if (existing.geomID == geomID) {

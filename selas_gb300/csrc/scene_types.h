@@ -59,5 +59,6 @@ constexpr uint32_t kMaterialTransparent = 1u;  // DisneySolid with diffTrans or 
 constexpr uint32_t kMaterialUsesPtex = 2u;
 constexpr uint32_t kMaterialUsesTexture = 4u;  // base colour from a 2D image at the hit's uvs (not Ptex)
 constexpr uint32_t kMaterialTextured = kMaterialUsesPtex | kMaterialUsesTexture;
+constexpr uint32_t kMaterialPtexQuad = 8u;  // with kMaterialUsesPtex: the geometry's texture is a quad-mesh texture
 
 }  // namespace sel

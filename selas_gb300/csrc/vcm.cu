@@ -31,6 +31,7 @@
 #include "hitref.cuh"
 #include "ibl.cuh"
 #include "ptex.cuh"
+#include "ptex_quad.cuh"
 #include "radix.cuh"
 #include "scan.cuh"
 #include "shading.cuh"
@@ -259,7 +260,8 @@ __device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const
 }
 
 // Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
-// kPretex: the Ptex base colour was filtered by k_vtexture into P.st.base[s] (material-sorted bounces).
+// kPretex: the Ptex base colour was filtered by k_vtexture into P.st.base[s] (material-sorted bounces).  Scenes
+// with Ptex always take the sorted bounces, so the unsorted form samples 2D images only.
 template <bool kPretex, bool kInst>
 __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir, float4 hit, VHit& h,
                           uint32_t& status) {
@@ -277,13 +279,7 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
         if constexpr (kPretex) {
             const float4 b = P.st.base[s];
             base = f3(b.x, b.y, b.z);
-        } else if (m.flags & kMaterialUsesPtex) {
-            uint32_t pstatus = 0;
-            ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
-                      static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
-                      hit.z, base, pstatus);
-            status |= pstatus;
-        } else {
+        } else if (!(m.flags & kMaterialUsesPtex)) {
             base = tex2d_base_colour(m, attr, __float_as_uint(p0.w), hit.y, hit.z);
         }
     }
@@ -682,9 +678,8 @@ __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
         float3 base = ld3(m.base_color);
         if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
-                      static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
-                      hit.z, base, pstatus);
+            ptex_material_eval(m, hr.ptex_faces, int(hr.ptex_count), static_cast<const __half*>(hr.ptex_texels),
+                               __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
             status |= pstatus;
         } else {
             base = tex2d_base_colour(m, geom < hr.attr_count ? hr.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
@@ -1339,7 +1334,8 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         else if (tb == 256) k_shadow<0, 256><<<trace_grid, 256, 0, stream>>>(P);
         else k_shadow<0, 128><<<trace_grid, 128, 0, stream>>>(P);
     };
-    const bool sort = sc.sort_hint != 0 || inst;
+    // Ptex is filtered by the sort's texture pass only: scenes with Ptex always sort
+    const bool sort = sc.sort_hint != 0 || inst || sc.ptex_face_count > 0;
     const void* l_fn = inst ? reinterpret_cast<const void*>(&k_l_shade<true, true>)
                             : sort ? reinterpret_cast<const void*>(&k_l_shade<true, false>)
                                    : reinterpret_cast<const void*>(&k_l_shade<false, false>);

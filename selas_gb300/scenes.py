@@ -261,6 +261,8 @@ class RenderScene:
         rows, texels, base_face, base_texel = [], [], 0, 0
         for gid in sorted(self.ptex):
             r, t = self.ptex[gid]
+            if np.asarray(r).shape[1] == 10:  # quad-mesh textures: quad_ptex_tables
+                continue
             r = np.array(r, np.int32, copy=True)
             r[:, 1] += base_texel
             adj = r[:, 2:5]
@@ -274,6 +276,11 @@ class RenderScene:
         if not rows:
             return np.zeros((0, 8), np.int32), np.zeros(3, np.uint16)
         return np.ascontiguousarray(np.concatenate(rows)), np.ascontiguousarray(np.concatenate(texels))
+
+    def quad_ptex_tables(self):
+        """The quad-mesh Ptex textures: [(geomID, rows (n, 10) int32, texels uint16)]."""
+        return [(gid, np.ascontiguousarray(r, np.int32), np.ascontiguousarray(np.asarray(t, np.float16).view(np.uint16)))
+                for gid, (r, t) in sorted(self.ptex.items()) if np.asarray(r).shape[1] == 10]
 
     def build(self, sel_module, device, bvh_kind=0, build_mode=None):
         """Creates and commits a selas_gb300 Scene with this content."""
@@ -385,19 +392,19 @@ def light_records(lights: list):
 def triangle_adjacency(faces: np.ndarray):
     """Ptex FaceInfo adjacency of a triangle mesh: edge i of a face runs from vertex i to vertex i+1;
     adj[f, i] = neighbouring face across that edge (-1 on a boundary), adjedge[f, i] = the neighbour's edge
-    index for the same edge."""
+    index for the same edge.  Faces of k vertices give k edges each (a quad mesh: edges 0..3)."""
     f = np.asarray(faces, np.int64)
-    n = f.shape[0]
-    a = np.concatenate([f[:, 0], f[:, 1], f[:, 2]])
-    b = np.concatenate([f[:, 1], f[:, 2], f[:, 0]])
-    face_of = np.tile(np.arange(n), 3)
-    edge_of = np.repeat(np.arange(3), n)
+    n, k = f.shape
+    a = np.concatenate([f[:, i] for i in range(k)])
+    b = np.concatenate([f[:, (i + 1) % k] for i in range(k)])
+    face_of = np.tile(np.arange(n), k)
+    edge_of = np.repeat(np.arange(k), n)
     lo, hi = np.minimum(a, b), np.maximum(a, b)
     key = lo * (int(f.max()) + 1) + hi
     order = np.argsort(key, kind="stable")
     ks = key[order]
-    adj = np.full((n, 3), -1, np.int32)
-    adjedge = np.zeros((n, 3), np.int32)
+    adj = np.full((n, k), -1, np.int32)
+    adjedge = np.zeros((n, k), np.int32)
     same = np.nonzero(ks[1:] == ks[:-1])[0]
     for i in same:  # manifold edges appear exactly twice
         p, q = order[i], order[i + 1]
@@ -436,6 +443,92 @@ def ptex_faces(faces: np.ndarray, log2: int):
     table[:, 2:5] = adj
     table[:, 5:8] = adjedge
     return table
+
+
+def ptex_quad_faces(quads: np.ndarray, log2: int):
+    """Face table rows (log2, texel offset, adj0..3, adjedge0..3) as int32, one per quad (Ptex quad faces: edge i
+    from vertex i to vertex i+1, u along edge 0, v along edge 3 reversed)."""
+    n = quads.shape[0]
+    adj, adjedge = triangle_adjacency(quads)
+    table = np.zeros((n, 10), np.int32)
+    table[:, 0] = log2
+    table[:, 1] = np.arange(n, dtype=np.int64) * (1 << (2 * log2))
+    table[:, 2:6] = adj
+    table[:, 6:10] = adjedge
+    return table
+
+
+def quad_cube(m: int = 3):
+    """A cube of side 2 whose faces are m x m quads, outward-facing: (vertices (n, 3), quads (6 m^2, 4)); its
+    eight corners have valence 3, every other vertex 4."""
+    index = {}
+    verts, quads = [], []
+
+    def vid(p):
+        key = tuple(np.round(p, 6))
+        if key not in index:
+            index[key] = len(verts)
+            verts.append(p)
+        return index[key]
+
+    for axis in range(3):
+        for sign in (1.0, -1.0):
+            n = np.zeros(3)
+            n[axis] = sign
+            a = np.zeros(3)
+            a[(axis + 1) % 3] = 1.0
+            b = np.cross(n, a)
+            for i in range(m):
+                for j in range(m):
+                    s0, s1 = -1 + 2 * i / m, -1 + 2 * (i + 1) / m
+                    t0, t1 = -1 + 2 * j / m, -1 + 2 * (j + 1) / m
+                    quads.append([vid(n + s0 * a + t0 * b), vid(n + s1 * a + t0 * b), vid(n + s1 * a + t1 * b),
+                                  vid(n + s0 * a + t1 * b)])
+    return np.array(verts, np.float32), np.array(quads, np.uint32)
+
+
+def quad_fan(k: int = 5):
+    """k quads around one interior vertex of valence k (centre, spoke midpoints, rim points), a disc with a
+    boundary: (vertices, quads)."""
+    verts = [[0.0, 0.0, 0.0]]
+    for i in range(k):
+        a = 2 * np.pi * i / k
+        verts.append([np.cos(a), 0.0, np.sin(a)])
+        b = 2 * np.pi * (i + 0.5) / k
+        verts.append([1.5 * np.cos(b), 0.0, 1.5 * np.sin(b)])
+    quads = [[0, 1 + 2 * i, 2 + 2 * i, 1 + 2 * ((i + 1) % k)] for i in range(k)]
+    return np.array(verts, np.float32), np.array(quads, np.uint32)
+
+
+def quad_textured_cubes(count: int = 4, m: int = 3, log2: int = 3, seed: int = 0x5E1A5F10) -> RenderScene:
+    """Quad-mesh cubes of m x m quads a side (corner valence 3) with per-face Ptex value noise (2^log2 texels a
+    side, the separable bicubic filter), rotated and scaled on a quad floor, a five-quad fan (interior valence 5)
+    with its own Ptex, one 2 x 2 quad light and a dim background."""
+    rng = np.random.default_rng(seed)
+    v0, q0 = quad_cube(m)
+    g = TriangleScene()
+    mats, ptex = {}, {}
+    for i in range(count):
+        a = rng.uniform(0, 2 * np.pi)
+        rot = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+        size = rng.uniform(0.5, 1.0)
+        centre = np.array([rng.uniform(-3.5, 3.5), size, rng.uniform(-2.0, 2.0)])
+        g.add_quads(i, (v0 @ rot.T * size + centre).astype(np.float32), q0)
+        mats[i] = dict(shader=1, lightSetIndex=0, roughness=float(rng.uniform(0.2, 0.9)),
+                       metallic=float(rng.random() < 0.3), ior=1.5, usesPtex=1)
+        ptex[i] = (ptex_quad_faces(q0, log2), value_noise_texels(q0.shape[0], log2, seed + 31 * i))
+    fv, fq = quad_fan(5)
+    gid = count
+    g.add_quads(gid, (fv * 1.2 + np.array([0.0, 0.01, 3.0])).astype(np.float32), fq)
+    mats[gid] = dict(shader=1, lightSetIndex=0, roughness=0.6, ior=1.5, usesPtex=1)
+    ptex[gid] = (ptex_quad_faces(fq, 4), value_noise_texels(fq.shape[0], 4, seed + 7))
+    floor = np.array([[-20, 0, -20], [-20, 0, 20], [20, 0, 20], [20, 0, -20]], np.float32)
+    g.add_quads(count + 1, floor, np.array([[0, 1, 2, 3]], np.uint32))
+    mats[count + 1] = dict(shader=1, lightSetIndex=0, baseColor=(0.6, 0.6, 0.6), roughness=0.7, ior=1.5)
+    light = dict(position=(0.0, 6.0, 0.0), direction=(0.0, -1.0, 0.0), x=(2.0, 0.0, 0.0), z=(0.0, 0.0, 2.0),
+                 radiance=(20.0, 18.0, 15.0))
+    cam = dict(position=(0.0, 4.0, -9.0), look_at=(0.0, 0.8, 0.0), up=(0.0, 1.0, 0.0), fov_degrees=55.0)
+    return RenderScene(g, mats, [(0, light)], (0.1, 0.1, 0.12), cam, ptex=ptex)
 
 
 def textured_spheres(count: int = 6, level: int = 3, log2: int = 4, seed: int = 0x5E1A5F00) -> RenderScene:

@@ -12,6 +12,9 @@ ptex_golden.npz  - a triangle mesh (icosphere, 320 faces) with 16 x 16 half-floa
                    face and Ptex adjacency, written with the vendored Ptex 2.2 writer and filtered by its
                    PtexTriangleFilter (getFilter(f_bspline), zero widths, as SurfaceParameters.cpp:196-206)
                    at seeded (face, u, v) queries including edges, corners and out-of-range faces.
+ptex_quad_golden.npz - quad meshes (a cube of 3 x 3 quads a side: corner valence 3; fans of 5 and 6 quads around
+                   one vertex, with a boundary) at 1 x 1 to 16 x 16 texels per face, filtered by the vendored Ptex's
+                   separable bicubic filter with B-spline weights (getFilter(f_bspline) on mt_quad, zero widths).
 cornell_64_ref.npz - the FP64 high-spp image of the Cornell scene (64 x 64, 4096 spp, depth 8, background 0)
                    from the reference's own path tracer (PathTracer.cpp EvaluatePath, compiled into
                    oracle/_ref/libref_pt.so) with its MT19937 sampling (each 256-spp chunk with seeds of its own);
@@ -178,6 +181,62 @@ def make_ptex(seed=0x5E1A5E7E, n_random=6000):
         assert lib.ref_ptex_eval(path, queries.ctypes.data, queries.shape[0], out.ctypes.data) == 0
     np.savez_compressed(OUT / "ptex_golden.npz", faces=faces, texels=tex_u16, queries=queries, out=out)
     print("ptex_golden.npz:", queries.shape[0], "queries over", nf, "faces")
+
+
+# (mesh, log2, constant) of the quad-mesh Ptex golden: the cube's corners have valence 3, its other vertices 4; the
+# fans have one interior vertex of valence 5 and 6 and a boundary.  Small faces (log2 0..2) take the filter's wide-
+# kernel branches; 1 x 1 faces are constant faces.  constant: the first 27 faces of the cube (half of it) hold one
+# colour, so the writer flags constant faces and constant neighbourhoods among them.
+QUAD_PTEX_CASES = (("cube", 0, False), ("cube", 1, False), ("cube", 2, False), ("cube", 3, False), ("cube", 4, False),
+                   ("fan5", 3, False), ("fan6", 2, False), ("cube", 2, True))
+
+
+def quad_ptex_mesh(name):
+    from selas_gb300 import scenes
+    return {"cube": lambda: scenes.quad_cube(3), "fan5": lambda: scenes.quad_fan(5),
+            "fan6": lambda: scenes.quad_fan(6)}[name]()
+
+
+def make_ptex_quad(seed=0x5E1A5E7F, n_random=2500):
+    """ptex_quad_golden.npz: for each case k, faces_k / texels_k / queries_k / out_k, the vendored Ptex's
+    bicubic B-spline filter on a quad mesh (the separable filter) as Selas calls it."""
+    import tempfile
+    from selas_gb300 import scenes
+    lib = ctypes.CDLL(str(ROOT / "oracle" / "_ref" / "libref_ptex.so"))
+    vp = ctypes.c_void_p
+    lib.ref_ptex_write_quad.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, vp]
+    lib.ref_ptex_eval.argtypes = [ctypes.c_char_p, vp, ctypes.c_int, vp]
+    rng = np.random.default_rng(seed)
+    arrays = {}
+    for k, (mesh, log2, constant) in enumerate(QUAD_PTEX_CASES):
+        _, quads = quad_ptex_mesh(mesh)
+        nf = quads.shape[0]
+        faces = scenes.ptex_quad_faces(quads, log2)
+        tex_u16 = np.ascontiguousarray(scenes.value_noise_texels(nf, log2, seed + k).view(np.uint16))
+        if constant:
+            per_face = tex_u16.reshape(nf, -1, 3)
+            per_face[:27] = np.float16([0.3, 0.6, 0.2]).view(np.uint16)
+        f = rng.integers(0, nf, n_random)
+        q = [np.stack([f, rng.random(n_random), rng.random(n_random)], 1)]
+        special = []
+        for face in rng.integers(0, nf, 30):
+            for u, v in ((0, 0), (1, 0), (0, 1), (1, 1), (0.5, 0), (0, 0.5), (1, 0.5), (0.5, 1), (0.5, 0.5),
+                         (1e-4, 0.3), (0.3, 0.9999), (0.02, 0.97), (0.97, 0.03), (1.2, -0.1), (-0.3, 0.5)):
+                special.append((face, u, v))
+        special += [(-1, 0.3, 0.3), (nf, 0.3, 0.3)]
+        q.append(np.array(special, np.float64))
+        q = np.concatenate(q)
+        queries = np.zeros((q.shape[0], 3), np.float32)
+        queries[:, 0] = q[:, 0].astype(np.int32).view(np.float32)
+        queries[:, 1:] = q[:, 1:]
+        out = np.zeros((q.shape[0], 3), np.float32)
+        with tempfile.TemporaryDirectory() as d:
+            path = (Path(d) / "quads.ptx").as_posix().encode()
+            assert lib.ref_ptex_write_quad(path, faces.ctypes.data, nf, tex_u16.ctypes.data) == 0
+            assert lib.ref_ptex_eval(path, queries.ctypes.data, queries.shape[0], out.ctypes.data) == 0
+        arrays.update({f"faces_{k}": faces, f"texels_{k}": tex_u16, f"queries_{k}": queries, f"out_{k}": out})
+    np.savez_compressed(OUT / "ptex_quad_golden.npz", **arrays)
+    print("ptex_quad_golden.npz:", len(QUAD_PTEX_CASES), "textures")
 
 
 def make_cornell(spp=4096, size=64, seed=0x5E1A5C0B):
@@ -353,11 +412,13 @@ def make_ref_pt(seed=0x5E1A5A11):
 if __name__ == "__main__":
     sys.path.insert(0, str(OUT))
     sys.path.insert(0, str(OUT.parent))
-    what = sys.argv[1:] or ["bsdf", "ptex", "cornell", "vcm", "cmj", "deferred", "ref_pt"]
+    what = sys.argv[1:] or ["bsdf", "ptex", "ptex_quad", "cornell", "vcm", "cmj", "deferred", "ref_pt"]
     if "bsdf" in what:
         make_bsdf()
     if "ptex" in what:
         make_ptex()
+    if "ptex_quad" in what:
+        make_ptex_quad()
     if "cornell" in what:
         make_cornell()
     if "vcm" in what:
