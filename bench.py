@@ -61,7 +61,7 @@ def parse_args():
     p.add_argument("--terrain-grid", type=int, default=4096, help="instanced terrain heightfield size (0: skip)")
     p.add_argument("--terrain-instances", type=int, default=5000)
     p.add_argument("--terrain-spp", type=int, default=64)
-    p.add_argument("--profile-case", choices=["query", "build", "pt", "vcm", "deferred", "instanced", "all"],
+    p.add_argument("--profile-case", choices=["query", "build", "pt", "pt_cornell", "vcm", "deferred", "instanced", "all"],
                    help="run one bounded case for an ncu capture (no timing, no JSON line) and exit")
     return p.parse_args()
 
@@ -375,6 +375,13 @@ def profile_case(case):
             data.attach_to(sc)
             sc.commit()
             sc.release()
+    if case == "pt_cornell":
+        # the path-tracer roofline workload (Cornell box, 512 x 512, depth 8) at 4 of its 64 spp, one batch of
+        # 1,048,576 paths: each sample is the same work, so the image's DRAM traffic is 16 x this capture's
+        rs = scenes.cornell_box()
+        sc = rs.build(sel, dev)
+        sc.pt_generate_image(rs.sel_camera(sel, 512, 512), sel.pt_settings(4, 8))
+        sc.release()
     if case in ("pt", "vcm", "all"):
         room = scenes.vcm_room(icospheres=8)
         sc = room.build(sel, dev)
@@ -529,7 +536,7 @@ def render_metrics(sel, scenes, dev, stream, args, room=None):
     tuned_ms = timed(render, 3)
     b = res.best
     out["autotune"] = {"workload": "room path tracer, 512x512, 16 spp, depth 8",
-                       "space": "8-wide leaf {2,3,4} | binary; capacity {1M, 4M, 8M} paths; traversal block {128, 256}",
+                       "space": "8-wide leaf {2,3,4,8} | binary; capacity {1M, 4M, 8M} paths; traversal block {128, 256}",
                        "trials": int(res.trials), "tuning_s": round(tune_s, 2),
                        "best": {"bvh": "8-wide quantised" if b.bvh_kind == 0 else "binary FP32", "leaf": int(b.leaf_size),
                                 "paths_in_flight": int(b.paths_in_flight), "trace_block": int(b.trace_block)},
@@ -647,9 +654,11 @@ def instanced_metrics(sel, scenes, dev, stream, args):
            "autotune": {"workload": "one view 960x540, 4 spp", "trials": int(res.trials), "tuning_s": round(tune_s, 2),
                         "best": {"leaf": int(b_.leaf_size), "paths_in_flight": int(b_.paths_in_flight),
                                  "trace_block": int(b_.trace_block), "ms": round(b_.ms, 3)},
-                        "space": "8-wide leaf {2,3,4} (a leaf slot's count field has 3 bits, so leaves of 8 are "
-                                 "not offered); capacity {1M, 4M, 8M}; traversal block 128 (the instanced stack "
-                                 "fills the static shared memory at 128 threads)"}}
+                        "space": "8-wide leaf {2,3,4,8}; capacity {1M, 4M, 8M}; traversal block {128, 256} (the "
+                                 "256-thread instanced traversal keeps its stacks in dynamic shared memory)",
+                        "points": [{"leaf": int(t.leaf_size), "paths_in_flight": int(t.paths_in_flight),
+                                    "trace_block": int(t.trace_block), "ms": round(t.ms, 3)}
+                                   for t in (res.trial[i] for i in range(res.trials))]}}
     terrain.release(built)
     del acc
     torch.cuda.empty_cache()

@@ -328,8 +328,9 @@ __global__ void __launch_bounds__(kBlock) k_class_scatter(PtParams P, int cur) {
 // the reference's batcher orders hits by (instance, geometry, primitive) before shading
 // (PathTracingBatcher.cpp:221-238,799-825), and hits whose footprints cross the same edges walk the same faces,
 // so a warp's Ptex filter walks stay in step.  Three 8-bit radix passes order the queue by it.
-// The classes are counted as k_classify counts them (the shading kernels find their classes' ranges from it).
-template <bool kInst>
+// kCount: the classes are counted as k_classify counts them (per-shader shading kernels find their classes'
+// ranges from the counts; a batch with one shader shades the whole queue and needs none).
+template <bool kInst, bool kCount>
 __global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -355,16 +356,20 @@ __global__ void __launch_bounds__(kBlock) k_sort_keys(PtParams P, int cur) {
                        ptex_region(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count), face, hit.y, hit.z);
             }
         }
-        const uint32_t c = valid ? key >> 20 : 0xffu;
         if (valid) P.st.rkeys[0][e] = key;
-        const uint32_t peers = __match_any_sync(0xffffffffu, c);
-        if (valid && (__ffs(peers) - 1) == int(threadIdx.x & 31u)) atomicAdd(&P.st.counters[32 + c], __popc(peers));
+        if constexpr (kCount) {
+            const uint32_t c = valid ? key >> 20 : 0xffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, c);
+            if (valid && (__ffs(peers) - 1) == int(threadIdx.x & 31u)) atomicAdd(&P.st.counters[32 + c], __popc(peers));
+        }
     }
 }
 
 // Ptex base colour of the sorted paths whose hit material is textured (SurfaceParameters.cpp:196-206): a
 // kernel of its own keeps the filter's code out of the shading kernel.
-template <bool kInst>
+// kQuad: the batch has quad-mesh Ptex; without it the quad filter (a function call) stays out of the kernel, whose
+// triangle filter would otherwise lose registers to the call.
+template <bool kInst, bool kQuad>
 __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const uint32_t* in_queue) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
@@ -382,8 +387,13 @@ __global__ void __launch_bounds__(kBlock) k_texture(PtParams P, int cur, const u
         float3 base = ld3(m.base_color);
         if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_material_eval(m, r.ptex_faces, int(r.ptex_count), static_cast<const __half*>(r.ptex_texels),
-                               __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
+            if (kQuad && (m.flags & kMaterialPtexQuad))
+                ptex_material_eval(m, r.ptex_faces, int(r.ptex_count), static_cast<const __half*>(r.ptex_texels),
+                                   __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
+            else
+                ptex_eval(static_cast<const PtexFace*>(r.ptex_faces), int(r.ptex_count),
+                          static_cast<const __half*>(r.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                          hit.z, base, pstatus);
             status |= pstatus;
         } else {
             base = tex2d_base_colour(m, geom < r.attr_count ? r.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
@@ -804,7 +814,8 @@ void launch_shade(uint32_t modes, bool inst, int shader, int grid, cudaStream_t 
 
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block, uint32_t modes,
-                           bool instanced, bool texture, bool ray_sort, uint64_t batch_paths, uint32_t shader_kinds) {
+                           bool instanced, bool texture, bool ray_sort, uint64_t batch_paths, uint32_t shader_kinds,
+                           bool quad_ptex) {
     const bool face_order = sort && texture && !instanced && batch_paths >= kFaceOrderPaths;
     // 256-thread traversal blocks for the 8-wide layout, flat (its 24-entry stacks fill 48 KB of static shared
     // memory) or instanced (40-entry stacks, 80 KB of dynamic shared memory); the binary layout's 64-entry
@@ -860,9 +871,14 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             if (face_order) {
                 // textured scenes, large batches: order by (class, Ptex face, footprint region), three 8-bit
                 // radix passes from the queue to queue_sorted (through rvals)
-                k_class_reset<<<1, 32, 0, s>>>(st.counters);
-                if (instanced) k_sort_keys<true><<<shade_grid, kBlock, 0, s>>>(P, cur);
-                else k_sort_keys<false><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                if (one_kind) {
+                    if (instanced) k_sort_keys<true, false><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                    else k_sort_keys<false, false><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                } else {
+                    k_class_reset<<<1, 32, 0, s>>>(st.counters);
+                    if (instanced) k_sort_keys<true, true><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                    else k_sort_keys<false, true><<<shade_grid, kBlock, 0, s>>>(P, cur);
+                }
                 const uint32_t ntiles = (st.capacity + kSortTile - 1) / kSortTile;
                 uint32_t* kin = st.rkeys[0];
                 uint32_t* kout = st.rkeys[1];
@@ -885,8 +901,10 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
             }
             // Ptex base colours of the hits (the shading kernel reads them), in shading order
             const uint32_t* q = sort ? st.queue_sorted : st.queue[cur];
-            if (texture && instanced) k_texture<true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
-            else if (texture) k_texture<false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
+            if (texture && instanced && quad_ptex) k_texture<true, true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
+            else if (texture && instanced) k_texture<true, false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
+            else if (texture && quad_ptex) k_texture<false, true><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
+            else if (texture) k_texture<false, false><<<shade_grid, kBlock, 0, s>>>(P, cur, q);
             const int2 whole = make_int2(-1, -1);
             if (one_kind) {
                 launch_shade(modes, instanced, single, wave_grid, s, P, cur, b, q, whole);
@@ -929,7 +947,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
         int kind, sms;
         uint32_t bounces, sort;
         int tb;
-        uint32_t modes, instanced, texture, ray_sort, face_order, kinds;
+        uint32_t modes, instanced, texture, ray_sort, face_order, kinds, quad_ptex;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -944,6 +962,7 @@ cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtSt
     key.ray_sort = ray_sort ? 1u : 0u;
     key.face_order = face_order ? 1u : 0u;
     key.kinds = kinds;
+    key.quad_ptex = quad_ptex ? 1u : 0u;
     return replay(graphs, &key, sizeof(key), stream, batches, enqueue);
 }
 
@@ -970,7 +989,7 @@ cudaError_t pt_render(const PtScene& sc, const PtCamera& cam, const PtSettings& 
     return pt_run_batches(sc.bvh_kind, set.max_bounces, sc.sort_hint != 0, st, d_err, batches, stream, graphs,
                           trace_block, set.mode == kPtModeDeferred ? 2u : 1u, sc.insts != nullptr,
                           pt_scene_textured(sc), sc.ray_sort != 0, std::min<uint64_t>(job.total, st.capacity),
-                          sc.shader_kinds);
+                          sc.shader_kinds, sc.ptex_quads != 0);
 }
 
 cudaError_t pt_resolve(const double* d_accum, uint32_t values, double scale, float* d_out, cudaStream_t stream) {

@@ -45,6 +45,7 @@ struct PtScene {
     uint32_t ray_sort;            // 1: sort each bounce's continuing rays (SEL_OPTION_RAY_SORT)
     uint32_t tex2d;               // 1: a material takes its base colour from a 2D image (kMaterialUsesTexture)
     uint32_t shader_kinds;        // bit s: a material of the scene or the scenes it instances has shader s
+    uint32_t ptex_quads;          // 1: a quad mesh of the scene or the scenes it instances has a Ptex texture
 };
 
 // RayCastCameraSettings (GeometryLib/Camera.h:24-42) as InitializeRayCastCamera computes it.
@@ -134,9 +135,10 @@ PtState pt_state_carve(void* block, uint32_t paths);
 cudaError_t pt_run_batches(int bvh_kind, uint32_t bounces, bool sort, const PtState& st, uint32_t* d_err,
                            uint64_t batches, cudaStream_t stream, GraphCache* graphs, int trace_block = 128,
                            uint32_t modes = 1u, bool instanced = false, bool texture = true, bool ray_sort = false,
-                           uint64_t batch_paths = 0, uint32_t shader_kinds = 7u);
+                           uint64_t batch_paths = 0, uint32_t shader_kinds = 7u, bool quad_ptex = true);
 // `ray_sort`: order each bounce's continuing rays by (direction bin, origin cell) before tracing them.
 // `texture`: a job's hits may need Ptex (see pt_scene_textured); the Ptex kernel runs only then.
+// `quad_ptex`: a job's scene has quad-mesh Ptex (the Ptex kernel compiled with the quad filter runs only then).
 // `shader_kinds`: bit s set when a job's scene has a material of shader s.  Shading runs a kernel compiled for
 // one shader: over the whole queue when the jobs have one kind of shader, else per shader over its classes of
 // the class-ordered queue (without the class order: one kernel for every shader).

@@ -217,6 +217,15 @@ static int upload_attrs(SelSceneTy* sc) {
     return SEL_OK;
 }
 
+// A quad-mesh Ptex texture bound in the scene or the scenes its instances reference.
+bool tree_has_quad_ptex(const SelSceneTy* sc) {
+    for (const auto& pb : sc->ptex)
+        if (pb.quads) return true;
+    for (const auto& r : sc->referenced)
+        if (tree_has_quad_ptex(r.first)) return true;
+    return false;
+}
+
 // Material classes (bit shader * 4 + Ptex * 2 + transparent) and Ptex use of a scene and the scenes its
 // instances reference.
 void tree_classes(const SelSceneTy* sc, uint32_t& mask, bool& ptex) {
@@ -505,6 +514,7 @@ PtScene scene_view(const SelSceneTy* sc) {
         ps.shader_kinds = 0u;
         for (uint32_t k = 0; k < 3u; ++k)
             if ((mask >> (4u * k)) & 15u) ps.shader_kinds |= 1u << k;
+        ps.ptex_quads = tree_has_quad_ptex(sc) ? 1u : 0u;
     }
     ps.insts = static_cast<const InstanceRecord*>(sc->d_insts);
     ps.ibl = static_cast<const IblDev*>(sc->d_ibl);
@@ -632,7 +642,8 @@ int render_views_device(SelSceneTy* sc, const SelCamera* cams, uint32_t count, c
                                                   : (sc->tuned_trace_block ? sc->tuned_trace_block : 128u));
     e = pt_run_batches(ps.bvh_kind, settings.maxBounces, ps.sort_hint != 0, st, sc->dev->d_err, batches, stream,
                        sc->dev->graph_replay ? &sc->pt_graph : nullptr, block, mode == kPtModeDeferred ? 2u : 1u,
-                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0, batch_paths, ps.shader_kinds);
+                       ps.insts != nullptr, pt_scene_textured(ps), ps.ray_sort != 0, batch_paths, ps.shader_kinds,
+                       ps.ptex_quads != 0);
     return e == cudaSuccess ? SEL_OK : cuda_fail(e, "multi-view render launch");
 }
 

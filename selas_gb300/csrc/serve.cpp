@@ -286,7 +286,7 @@ bool pt_round(SelServerTy* S) {
     }
     cudaMemcpyAsync(S->pst.jobs, table, sizeof(PtJob) * kMaxPtJobs, cudaMemcpyHostToDevice, S->pt_stream);
     cudaMemcpyAsync(S->pst.control, &c, sizeof(PtControl), cudaMemcpyHostToDevice, S->pt_stream);
-    bool sort = false, instanced = false, texture = false, ray_sort = false;
+    bool sort = false, instanced = false, texture = false, ray_sort = false, quad_ptex = false;
     uint32_t modes = 0, shader_kinds = 0;
     for (int k = 0; k < kMaxPtJobs; ++k)
         if (S->slots[k]) {
@@ -295,13 +295,14 @@ bool pt_round(SelServerTy* S) {
             texture |= pt_scene_textured(S->slots[k]->scene);
             ray_sort |= S->slots[k]->scene.ray_sort != 0;
             shader_kinds |= S->slots[k]->scene.shader_kinds;
+            quad_ptex |= S->slots[k]->scene.ptex_quads != 0;
             modes |= S->slots[k]->desc.integrator == SEL_INTEGRATOR_DEFERRED ? 2u : 1u;
         }
     // rounds per batch: the largest maxBounces of the jobs in the slots (at most config.max_bounces)
     uint64_t batch_paths = 0;
     for (int k = 0; k < kMaxPtJobs; ++k) batch_paths += c.quota[k];
     cudaError_t e = pt_run_batches(0, bounces, sort, S->pst, S->dev->d_err, 1, S->pt_stream, &S->pt_graph, 128,
-                                   modes, instanced, texture, ray_sort, batch_paths, shader_kinds);
+                                   modes, instanced, texture, ray_sort, batch_paths, shader_kinds, quad_ptex);
     for (int k = 0; k < kMaxPtJobs; ++k) {
         Job* j = S->slots[k];
         if (!j || c.quota[k] == 0) continue;

@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(kBlock) k_vclass_scatter(VcmParams P, int cur)
     }
 }
 
-template <bool kInst>
+template <bool kInst, bool kQuad>
 __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
@@ -678,8 +678,13 @@ __global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
         float3 base = ld3(m.base_color);
         if (m.flags & kMaterialUsesPtex) {
             uint32_t pstatus = 0;
-            ptex_material_eval(m, hr.ptex_faces, int(hr.ptex_count), static_cast<const __half*>(hr.ptex_texels),
-                               __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
+            if (kQuad && (m.flags & kMaterialPtexQuad))
+                ptex_material_eval(m, hr.ptex_faces, int(hr.ptex_count), static_cast<const __half*>(hr.ptex_texels),
+                                   __float_as_uint(p0.w), hit.y, hit.z, base, pstatus);
+            else
+                ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
+                          static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                          hit.z, base, pstatus);
             status |= pstatus;
         } else {
             base = tex2d_base_colour(m, geom < hr.attr_count ? hr.attrs + geom : nullptr, __float_as_uint(p0.w), hit.y,
@@ -1336,6 +1341,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     };
     // Ptex is filtered by the sort's texture pass only: scenes with Ptex always sort
     const bool sort = sc.sort_hint != 0 || inst || sc.ptex_face_count > 0;
+    const bool quads = sc.ptex_quads != 0;
     const void* l_fn = inst ? reinterpret_cast<const void*>(&k_l_shade<true, true>)
                             : sort ? reinterpret_cast<const void*>(&k_l_shade<true, false>)
                                    : reinterpret_cast<const void*>(&k_l_shade<false, false>);
@@ -1354,8 +1360,10 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         else k_vclassify<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
         k_vclass_offsets<<<1, 32, 0, stream>>>(st.counters);
         k_vclass_scatter<<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        if (inst) k_vtexture<true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        else k_vtexture<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        if (inst && quads) k_vtexture<true, true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        else if (inst) k_vtexture<true, false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        else if (quads) k_vtexture<false, true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+        else k_vtexture<false, false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
         return st.queue_sorted;
     };
     // one pass; identical launches every pass (the pass reads its constants through st.iter)
@@ -1408,7 +1416,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     };
     struct Key {
         VcmParams P;
-        int kind, sms, radix_passes, sort, tb;
+        int kind, sms, radix_passes, sort, tb, quads;
     } key;
     std::memset(&key, 0, sizeof(key));
     std::memcpy(&key.P, &P, sizeof(P));
@@ -1417,6 +1425,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
     key.sms = sms;
     key.radix_passes = radix_passes;
     key.sort = sort ? 1 : 0;
+    key.quads = quads ? 1 : 0;
     return replay(graphs, &key, sizeof(key), stream, passes, enqueue);
 }
 
