@@ -163,6 +163,16 @@ int sel_scene_attach_quad_mesh(SelScene scene, unsigned int geomID, const float*
  * while `scene` uses it (releasing it fails while a committed scene instances it); committing it again
  * requires committing `scene` again.  Scenes with instances use the SEL_BVH_WIDE8_Q8 layout. */
 int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld);
+/* Round B-spline curves: rtcNewGeometry(RTC_GEOMETRY_TYPE_ROUND_BSPLINE_CURVE) + the index buffer (RTC_FORMAT_UINT,
+ * one entry per segment) + the vertex buffer (RTC_FORMAT_FLOAT4: x, y, z, radius) (ModelResource.cpp:300-332).
+ * Segment k is the uniform cubic B-spline of points indices[k] .. indices[k] + 3, swept by a sphere whose radius
+ * follows the same spline.  Embree's curve intersector is closed, so hits are defined here: the segment is cut
+ * at u = j / 8 into round cones (the union of spheres of linearly interpolated centre and radius between its
+ * pieces' end spheres); a hit reports t, u = the touching sphere's parameter along the segment, v = 0, Ng = hit
+ * point - that sphere's centre (object space), primID = k.  Scenes with curves use the 8-wide layout and are
+ * traversed by the instanced traversal.  points: point_count x 4 floats; data copied. */
+int sel_scene_attach_curve_mesh(SelScene scene, unsigned int geomID, const float* points, size_t point_count,
+                                const unsigned int* indices, size_t segment_count);
 int sel_scene_commit(SelScene scene);
 /* Per-vertex attributes: rtcSetGeometryVertexAttributeCount + rtcSetSharedGeometryBuffer(
  * RTC_BUFFER_TYPE_VERTEX_ATTRIBUTE, slot, RTC_FORMAT_FLOAT<components>) (ModelResource.cpp:183-197).  Slot 0..3
@@ -648,7 +658,7 @@ typedef struct SelCookedSceneInfo {
     uint32_t cameras;
     uint32_t textures;              /* distinct Textures assets the meshes' materials load */
     uint32_t ptexMeshes;            /* meshes whose material samples Ptex */
-    uint32_t curves;                /* curve geometries of the loaded models (not built: the load is refused) */
+    uint32_t curves;                /* curve geometries of the loaded models */
     float backgroundIntensity[4];
     char ibl[512];                  /* iblName ("" when none) */
     SelCamera camera;               /* SetupSceneCamera(scene, 0): cameras[0] when valid (fovDegrees > 0, zfar >
@@ -688,8 +698,10 @@ int sel_cooked_scene_describe(const char* asset_root, const char* scene_name, Se
  * the scene's quad lights in light sets by lightSetRanges, its backgroundIntensity and, when iblName is set, the
  * IBL asset's light and miss images with its rotation and exposure (the densities are derived again from the
  * light image).  Queries on *out_scene report instID[0] = i, instID[1] = j and geomID = k, the ids the reference's
- * Embree scenes report.  Releasing *out_scene releases the subscene and model scenes with it.  Refused with
- * SEL_ERR_INVALID_OPERATION: models with curves; Ptex materials unless SEL_COOKED_PTEX_AS_BASE_COLOR.
+ * Embree scenes report.  A model's curves (InitializeCurves, ModelResource.cpp:300-332) follow its meshes as
+ * geomIDs meshes + c, round B-spline curves (sel_scene_attach_curve_mesh) with the material of the model's
+ * curveModelName.  Releasing *out_scene releases the subscene and model scenes with it.  Refused with
+ * SEL_ERR_INVALID_OPERATION: Ptex materials unless SEL_COOKED_PTEX_AS_BASE_COLOR.
  * out_info may be null. */
 int sel_scene_load_cooked(SelDevice device, const char* asset_root, const char* scene_name, unsigned int flags,
                           SelScene* out_scene, SelCookedSceneInfo* out_info);

@@ -34,7 +34,9 @@ def lib() -> ctypes.CDLL:
             "oracle_bsdf_sample": ([_vp, _vp, _vp, _i64, _vp], None),
             "oracle_ptex_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
             "oracle_ptex_quad_eval": ([_vp, _i, _vp, _vp, _i64, _vp], None),
+            "oracle_curve_hits": ([_vp, _vp, _i64, ctypes.c_uint32, _vp, _i64, _i], None),
             "oracle_set_quad_ptex": ([_i, _vp, _vp, _vp, _vp, _vp], None),
+            "oracle_set_curves": ([_i, _vp, _vp, _vp, _vp, _vp], None),
             "oracle_pt_render": ([_vp, _vp, _vp, _i64, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.c_uint64, _i, _i, _vp, _i, _vp, _i, _vp], None),
@@ -77,6 +79,14 @@ def threads() -> int:
 
 def _p(a: np.ndarray) -> int:
     return a.ctypes.data
+
+
+def curve_hits(points, indices, geom_id: int, records: np.ndarray) -> None:
+    """Brute-force round B-spline curve hits (oracle_curve.cpp) of one curve geometry, in place: RTCRayHit
+    records (closest hit; a nearer curve hit replaces the record's) or RTCRay records (any hit)."""
+    p = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+    i = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    lib().oracle_curve_hits(_p(p), _p(i), i.size, geom_id, _p(records), records.shape[0], records.dtype.itemsize)
 
 
 def intersect_bruteforce(soup, rayhits: np.ndarray, nthreads: int | None = None) -> None:
@@ -196,6 +206,37 @@ def set_textures(parts):
         o, r = np.asarray(offs, np.int64), np.ascontiguousarray(np.concatenate(data))
         lib().oracle_set_textures(len(offs), _p(k), _p(d), _p(o), _p(r))
     set_quad_ptex(parts)
+    set_curves(parts)
+
+
+def set_curves(parts):
+    """Round B-spline curve geometries of the next oracle renders: those of the RenderScenes `parts` (scene index =
+    position; RenderScene.curves, geomID -> (points (n, 4), segment first points)), traced beside each scene's
+    triangles (oracle_curve.cpp)."""
+    keys, pt_offs, pts, idx_offs, idx = [], [0], [], [0], []
+    for si, p in enumerate(parts):
+        for gid, (cp, ci) in sorted((getattr(p, "curves", None) or {}).items()):
+            cp = np.ascontiguousarray(cp, np.float32).reshape(-1, 4)
+            ci = np.ascontiguousarray(ci, np.uint32).reshape(-1)
+            keys += [si, gid]
+            pts.append(cp)
+            pt_offs.append(pt_offs[-1] + cp.shape[0])
+            idx.append(ci)
+            idx_offs.append(idx_offs[-1] + ci.size)
+    if not keys:
+        lib().oracle_set_curves(0, None, None, None, None, None)
+        return
+    k = np.asarray(keys, np.uint32)
+    po, io = np.asarray(pt_offs, np.int64), np.asarray(idx_offs, np.int64)
+    P, I = np.ascontiguousarray(np.concatenate(pts)), np.ascontiguousarray(np.concatenate(idx))
+    lib().oracle_set_curves(len(keys) // 2, _p(k), _p(po), _p(P), _p(io), _p(I))
+
+
+def _material_count(render_scene, geom):
+    """Material records a flat render needs: every geomID of its triangles, curves and materials."""
+    ids = [int(geom.max()) if geom.size else 0] + list(render_scene.materials.keys())
+    ids += list((getattr(render_scene, "curves", None) or {}).keys())
+    return 1 + max(ids)
 
 
 def set_quad_ptex(parts):
@@ -246,7 +287,7 @@ def pt_render(render_scene, width, height, pass_begin, pass_end, max_bounces=8, 
     set_ibl(getattr(render_scene, "ibl", None))
     set_attributes([render_scene])
     verts, prim, geom = render_scene.geometry.soup()
-    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    mats = material_records(render_scene.materials, _material_count(render_scene, geom))
     rows, texels = render_scene.ptex_tables(mats)
     lights, sets = light_records(render_scene.lights)
     bg = np.array(render_scene.background, np.float32)
@@ -270,7 +311,7 @@ def deferred_render(render_scene, width, height, sample_begin, sample_end, sampl
     set_ibl(getattr(render_scene, "ibl", None))
     set_attributes([render_scene])
     verts, prim, geom = render_scene.geometry.soup()
-    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    mats = material_records(render_scene.materials, _material_count(render_scene, geom))
     rows, texels = render_scene.ptex_tables(mats)
     lights, sets = light_records(render_scene.lights)
     bg = np.array(render_scene.background, np.float32)
@@ -329,6 +370,7 @@ def _graph_arrays(scenes):
 def graph_intersect(scenes, top, rayhits, nthreads=None):
     """The render oracle's per-scene-BVH instanced traversal (closest hit; instIDs are not written)."""
     V, P, G, O, L, I, H, Q = _graph_arrays(scenes)
+    set_curves([])  # triangles only: no curves left from an earlier render
     lib().oracle_graph_intersect(len(scenes), _p(V), _p(P), _p(G), _p(O), V.shape[0], _p(L), _p(I), _p(H), _p(Q),
                                  L.shape[0], top, _p(rayhits), rayhits.shape[0], nthreads or threads())
 
@@ -344,7 +386,8 @@ def graph_render(iscene, width, height, begin, end, max_bounces=8, seed=0x5E1A50
     V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
     mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
     for part in iscene.parts:
-        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) + [0])
+        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) +
+                        list((getattr(part, "curves", None) or {}).keys()) + [0])
         m = material_records(part.materials, count)
         r, t = part.ptex_tables(m)
         mats.append(m)
@@ -382,7 +425,8 @@ def graph_vcm_render(iscene, width, height, iter_begin, iter_end, bounds, max_le
     V, P, G, O, L, I, H, Q = _graph_arrays(iscene.graph())
     mats, mat_off, rows, row_off, texels, tex_off = [], [0], [], [0], [], [0]
     for part in iscene.parts:
-        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) + [0])
+        count = 1 + max([gid for gid, _, _ in part.geometry.meshes] + list(part.materials.keys()) +
+                        list((getattr(part, "curves", None) or {}).keys()) + [0])
         m = material_records(part.materials, count)
         r, t = part.ptex_tables(m)
         mats.append(m)
@@ -473,7 +517,7 @@ def vcm_render(render_scene, width, height, iter_begin, iter_end, max_len=10, ra
     set_attributes([render_scene])
     set_ibl(getattr(render_scene, "ibl", None))
     verts, prim, geom = render_scene.geometry.soup()
-    mats = material_records(render_scene.materials, int(geom.max()) + 1)
+    mats = material_records(render_scene.materials, _material_count(render_scene, geom))
     rows, texels = render_scene.ptex_tables(mats)
     lights, sets = light_records(render_scene.lights)
     lights0 = np.ascontiguousarray(lights[sets[0, 0]:sets[0, 0] + sets[0, 1]]) if sets.shape[0] else lights[:0]

@@ -27,6 +27,8 @@
 #include <thread>
 #include <vector>
 
+#include "oracle_curve.h"
+
 namespace {
 
 struct Ray {
@@ -552,7 +554,19 @@ bool closest(const void* h, const float* org, const float* dir, float tnear, flo
     r.tnear = tnear;
     r.tfar = tfar;
     Best best;
-    if (!trace<false>(bvh, r, best)) return false;
+    const bool tri = !bvh.nodes.empty() && trace<false>(bvh, r, best);
+    float ct, cu;
+    uint32_t cp, cg;
+    if (orcv::closest(0, org, dir, tnear, tri ? best.t : tfar, ct, cu, out.ng, cp, cg) &&
+        (!tri || ct < best.t || ((uint64_t(cg) << 32) | cp) < best.key)) {  // a curve of the scene (oracle_curve.cpp)
+        out.t = ct;
+        out.u = cu;
+        out.v = 0.0f;
+        out.prim = cp;
+        out.geom = cg;
+        return true;
+    }
+    if (!tri) return false;
     const Tri& t = bvh.tris[size_t(best.tri)];
     out.t = best.t;
     out.u = best.u;
@@ -573,7 +587,7 @@ bool occluded(const void* h, const float* org, const float* dir, float tnear, fl
     r.tnear = tnear;
     r.tfar = tfar;
     Best best;
-    return trace<true>(bvh, r, best);
+    return (!bvh.nodes.empty() && trace<true>(bvh, r, best)) || orcv::occluded(0, org, dir, tnear, tfar);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -601,6 +615,9 @@ struct Graph {
 struct GBest {
     float t = 0, u = 0, v = 0;
     const Tri* tri = nullptr;
+    bool curve = false;  // the best hit is a curve's (cng, cprim, cgeom)
+    float cng[3] = {0, 0, 0};
+    uint32_t cprim = 0, cgeom = 0;
     uint64_t inst = ~0ull, key = ~0ull;
     uint32_t scene = 0;
     const float* l2w[2] = {nullptr, nullptr};
@@ -612,6 +629,8 @@ void scene_bounds(Graph& G, uint32_t s, std::vector<int>& done) {
     GScene& S = G.scenes[s];
     S.bounds.reset();
     if (S.bvh && !S.bvh->nodes.empty()) S.bounds.grow(S.bvh->nodes[0].box);
+    Box cb;
+    if (orcv::bounds(s, cb.lo, cb.hi)) S.bounds.grow(cb);
     for (GInst& in : S.insts) {
         scene_bounds(G, in.proto, done);
         const Box& pb = G.scenes[in.proto].bounds;
@@ -652,6 +671,7 @@ void gclosest(const Graph& G, uint32_t s, const float* o, const float* d, float 
                 tfar = b.t;
                 best.t = b.t; best.u = b.u; best.v = b.v;
                 best.tri = &S.bvh->tris[size_t(b.tri)];
+                best.curve = false;
                 best.inst = cur;
                 best.key = k;
                 best.scene = s;
@@ -659,6 +679,26 @@ void gclosest(const Graph& G, uint32_t s, const float* o, const float* d, float 
                 best.l2w[1] = nullptr;
                 ++best.updates;
             }
+        }
+    }
+    float ct, cu, cng[3];
+    uint32_t cp, cg;
+    if (orcv::closest(s, o, d, tnear, tfar, ct, cu, cng, cp, cg)) {  // the scene's curves (oracle_curve.cpp)
+        const uint64_t k = (uint64_t(cg) << 32) | cp;
+        if (ct < tfar || cur < best.inst || (cur == best.inst && k < best.key)) {
+            tfar = ct;
+            best.t = ct; best.u = cu; best.v = 0.0f;
+            best.tri = nullptr;
+            best.curve = true;
+            std::memcpy(best.cng, cng, 12);
+            best.cprim = cp;
+            best.cgeom = cg;
+            best.inst = cur;
+            best.key = k;
+            best.scene = s;
+            best.l2w[0] = chain0;
+            best.l2w[1] = nullptr;
+            ++best.updates;
         }
     }
     if (level >= 2) return;
@@ -687,6 +727,7 @@ bool goccluded(const Graph& G, uint32_t s, const float* o, const float* d, float
         Best b;
         if (trace<true>(*S.bvh, r, b)) return true;
     }
+    if (orcv::occluded(s, o, d, tnear, tfar)) return true;
     if (level >= 2) return false;
     for (const GInst& in : S.insts) {
         float tmin;
@@ -739,13 +780,19 @@ bool closest_graph(const void* g, const float* org, const float* dir, float tnea
     if (untraceable(org, dir)) return false;
     GBest best;
     gclosest(G, G.top, org, dir, tnear, tfar, ~0ull, 0, nullptr, best);
-    if (!best.tri) return false;
+    if (!best.tri && !best.curve) return false;
     out.t = best.t;
     out.u = best.u;
     out.v = best.v;
-    normal(*best.tri, out.ng);
-    out.prim = best.tri->prim;
-    out.geom = best.tri->geom;
+    if (best.curve) {
+        std::memcpy(out.ng, best.cng, 12);
+        out.prim = best.cprim;
+        out.geom = best.cgeom;
+    } else {
+        normal(*best.tri, out.ng);
+        out.prim = best.tri->prim;
+        out.geom = best.tri->geom;
+    }
     out.scene = best.scene;
     out.l2w[0] = best.l2w[0];
     out.l2w[1] = best.l2w[1];

@@ -76,6 +76,7 @@ _SIGNATURES = {
     "sel_scene_set_bvh_kind": [_vp, _i],
     "sel_scene_attach_triangle_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
     "sel_scene_attach_quad_mesh": [_vp, _u, _vp, _sz, _sz, _vp, _sz],
+    "sel_scene_attach_curve_mesh": [_vp, _u, _vp, _sz, _vp, _sz],
     "sel_scene_commit": [_vp],
     "sel_scene_attach_instance": [_vp, _u, _vp, _vp],
     "sel_scene_set_vertex_attribute": [_vp, _u, _u, _vp, _sz, _u],
@@ -180,6 +181,13 @@ class Scene:
         v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
         q = np.ascontiguousarray(quads, dtype=np.uint32).reshape(-1, 4)
         check(lib().sel_scene_attach_quad_mesh(self.handle, geom_id, _ptr(v), v.shape[0], 12, _ptr(q), q.shape[0]))
+
+    def attach_curve_mesh(self, geom_id: int, points: np.ndarray, indices: np.ndarray) -> None:
+        """Round B-spline curves: points (n, 4) = (x, y, z, radius), indices (k,) = first control point of each
+        segment."""
+        p = np.ascontiguousarray(points, np.float32).reshape(-1, 4)
+        i = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        check(lib().sel_scene_attach_curve_mesh(self.handle, geom_id, _ptr(p), p.shape[0], _ptr(i), i.size))
 
     def attach_instance(self, inst_id: int, instanced: "Scene", local_to_world) -> None:
         """Instance of a committed scene; local_to_world: 4 x 4 (or 3 x 4) affine matrix, row-major maths

@@ -506,7 +506,7 @@ std::string build_bvh(const std::vector<MeshInput>& meshes, int kind, BuiltBvh& 
             }
             ft.prim = uint32_t(t);
             ft.geom = m.geomID;
-            ft.kind = m.quads ? kTriQuadHalf : kTriPlain;
+            ft.kind = m.quads ? kTriQuadHalf : (m.curves ? kTriCurve : kTriPlain);
             tris.push_back(ft);
         }
     }

@@ -759,7 +759,7 @@ std::string build_wide_device(const std::vector<MeshInput>& meshes, uint32_t max
             }
             r.prim = uint32_t(t);
             r.geom = m.geomID;
-            r.kind = m.quads ? kTriQuadHalf : kTriPlain;
+            r.kind = m.quads ? kTriQuadHalf : (m.curves ? kTriCurve : kTriPlain);
             soup.push_back(r);
         }
     }

@@ -179,6 +179,8 @@ int sel_scene_attach_triangle_mesh(SelScene scene, unsigned int geomID, const fl
     std::lock_guard<std::mutex> lock(scene->mu);
     for (const MeshInput& m : scene->meshes)
         if (m.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
+    for (const SelSceneTy::CurveInput& c : scene->curves)
+        if (c.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
     for (const SelSceneTy::InstanceInput& ii : scene->instances)
         if (ii.instID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already used by an instance");
     MeshInput m;
@@ -225,6 +227,41 @@ int sel_scene_attach_quad_mesh(SelScene scene, unsigned int geomID, const float*
     return SEL_OK;
 }
 
+int sel_scene_attach_curve_mesh(SelScene scene, unsigned int geomID, const float* points, size_t point_count,
+                                const unsigned int* indices, size_t segment_count) {
+    if (!scene) return fail(SEL_ERR_INVALID_ARGUMENT, "scene is null");
+    if ((point_count && !points) || (segment_count && !indices)) return fail(SEL_ERR_INVALID_ARGUMENT, "null buffer");
+    if (geomID >= kInstanceGeom) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID must be below 0xFFFFFFFE");
+    if (segment_count >= (size_t(1) << 31)) return fail(SEL_ERR_INVALID_ARGUMENT, "fewer than 2^31 segments");
+    for (size_t k = 0; k < segment_count; ++k)
+        if (size_t(indices[k]) + 3 >= point_count)
+            return fail(SEL_ERR_INVALID_ARGUMENT, "a segment's four control points run past the point array");
+    for (size_t i = 0; i < 4 * point_count; ++i)
+        if (!std::isfinite(points[i])) return fail(SEL_ERR_INVALID_ARGUMENT, "non-finite control point");
+    for (size_t i = 0; i < point_count; ++i)
+        if (points[4 * i + 3] < 0.0f) return fail(SEL_ERR_INVALID_ARGUMENT, "negative curve radius");
+    std::lock_guard<std::mutex> lock(scene->mu);
+    for (const MeshInput& m : scene->meshes)
+        if (m.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
+    for (const SelSceneTy::CurveInput& c : scene->curves)
+        if (c.geomID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already attached");
+    for (const SelSceneTy::InstanceInput& ii : scene->instances)
+        if (ii.instID == geomID) return fail(SEL_ERR_INVALID_ARGUMENT, "geomID already used by an instance");
+    for (const SelSceneTy::TextureBinding& t : scene->textures)
+        if (t.geomID == geomID) return fail(SEL_ERR_INVALID_OPERATION, "a texture is bound to this geomID; curves take none");
+    SelSceneTy::CurveInput c;
+    c.geomID = geomID;
+    try {
+        c.points.assign(points, points + 4 * point_count);
+        c.indices.assign(indices, indices + segment_count);
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    scene->curves.push_back(std::move(c));
+    scene->committed = false;
+    return SEL_OK;
+}
+
 int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene instanced, const float* localToWorld) {
     if (!scene || !instanced || !localToWorld) return fail(SEL_ERR_INVALID_ARGUMENT, "null argument");
     if (instanced == scene) return fail(SEL_ERR_INVALID_ARGUMENT, "a scene cannot instance itself");
@@ -244,6 +281,8 @@ int sel_scene_attach_instance(SelScene scene, unsigned int instID, SelScene inst
     std::lock_guard<std::mutex> lock(scene->mu);
     for (const MeshInput& mi : scene->meshes)
         if (mi.geomID == instID) return fail(SEL_ERR_INVALID_ARGUMENT, "instID already used by a mesh");
+    for (const SelSceneTy::CurveInput& c : scene->curves)
+        if (c.geomID == instID) return fail(SEL_ERR_INVALID_ARGUMENT, "instID already used by a curve geometry");
     for (const SelSceneTy::InstanceInput& o : scene->instances)
         if (o.instID == instID) return fail(SEL_ERR_INVALID_ARGUMENT, "instID already attached");
     scene->instances.push_back(ii);
@@ -412,6 +451,12 @@ int finish_instances(SelSceneTy* scene, uint32_t levels, uint32_t below) {
         if (e != cudaSuccess) return cuda_fail(e, "instance table");
         scene->info.triangle_count -= n;
         scene->info.device_bytes += n * sizeof(InstanceRecord);
+    } else if (!scene->curves.empty()) {
+        // curve segments are intersected by the instanced traversal only: a scene with curves and no instances
+        // takes it through an instance table of one unused record
+        cudaError_t e = cudaMalloc(&scene->d_insts, sizeof(InstanceRecord));
+        if (e == cudaSuccess) e = cudaMemset(scene->d_insts, 0, sizeof(InstanceRecord));
+        if (e != cudaSuccess) return cuda_fail(e, "instance table");
     }
     scene->inst_levels = levels;
     for (auto& r : scene->referenced) --r.first->instanced_by;
@@ -427,6 +472,64 @@ int finish_instances(SelSceneTy* scene, uint32_t levels, uint32_t below) {
 }
 
 int commit_geometry(SelSceneTy* scene);
+
+// The build's stand-in for a curve geometry: per segment a box "triangle" (lo, hi, lo), the box of its four
+// control points grown by their largest radius (the B-spline and its radius stay inside their hull).
+MeshInput curve_boxes(const SelSceneTy::CurveInput& c) {
+    MeshInput m;
+    m.geomID = c.geomID;
+    m.curves = true;
+    m.vertices.reserve(c.indices.size() * 6);
+    m.indices.reserve(c.indices.size() * 3);
+    for (size_t k = 0; k < c.indices.size(); ++k) {
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, r = 0.0f;
+        for (int j = 0; j < 4; ++j) {
+            const float* p = &c.points[4 * (size_t(c.indices[k]) + j)];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], p[a]);
+                hi[a] = std::max(hi[a], p[a]);
+            }
+            r = std::max(r, p[3]);
+        }
+        for (int a = 0; a < 3; ++a) {
+            const float pad = r + (std::fabs(lo[a]) + std::fabs(hi[a]) + r) * std::ldexp(1.0f, -20);
+            lo[a] = std::nextafter(lo[a] - pad, -INFINITY);
+            hi[a] = std::nextafter(hi[a] + pad, INFINITY);
+        }
+        const uint32_t v = uint32_t(m.vertices.size() / 3);
+        m.vertices.insert(m.vertices.end(), {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]});
+        m.indices.insert(m.indices.end(), {v, v + 1, v});
+    }
+    return m;
+}
+
+// After the build: the segments' control points appended to the leaf records and each curve record pointed at
+// its own (curve.cu).
+int finish_curves(SelSceneTy* scene) {
+    std::vector<float> data;
+    std::vector<uint32_t> geoms, bases;
+    size_t nseg = 0;
+    for (const SelSceneTy::CurveInput& c : scene->curves) nseg += c.indices.size();
+    try {
+        data.reserve(nseg * 16);
+        for (const SelSceneTy::CurveInput& c : scene->curves) {
+            geoms.push_back(c.geomID);
+            bases.push_back(uint32_t(data.size() / 16));
+            for (uint32_t first : c.indices)
+                data.insert(data.end(), c.points.begin() + 4 * size_t(first), c.points.begin() + 4 * (size_t(first) + 4));
+        }
+    } catch (const std::bad_alloc&) {
+        return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+    void* tris = scene->d_tris;
+    const uint64_t records = scene->info.triangle_count;
+    cudaError_t e = attach_curve_data(&tris, records, data.data(), nseg, geoms.data(), bases.data(),
+                                      uint32_t(geoms.size()));
+    if (e != cudaSuccess) return cuda_fail(e, "curve segment data");
+    scene->d_tris = tris;
+    scene->info.device_bytes += nseg * 64;
+    return SEL_OK;
+}
 
 }  // namespace
 
@@ -445,9 +548,26 @@ extern "C" int sel_scene_commit(SelScene scene) {
         }
         scene->meshes.push_back(std::move(mesh));  // the instance records, for the duration of the build
     }
+    // curve geometries enter the build as boxes, one per segment (their records are finished afterwards)
+    const size_t mesh_count = scene->meshes.size();
+    if (!scene->curves.empty()) {
+        if (scene->kind != SEL_BVH_WIDE8_Q8) {
+            if (has_instances) scene->meshes.pop_back();
+            return fail(SEL_ERR_INVALID_OPERATION, "scenes with curves need the SEL_BVH_WIDE8_Q8 layout");
+        }
+        try {
+            for (const SelSceneTy::CurveInput& c : scene->curves) scene->meshes.push_back(curve_boxes(c));
+        } catch (const std::bad_alloc&) {
+            scene->meshes.resize(mesh_count);
+            if (has_instances) scene->meshes.pop_back();
+            return fail(SEL_ERR_OUT_OF_MEMORY, "host allocation failed");
+        }
+    }
     scene->committed = false;
     int rc = commit_geometry(scene);
+    scene->meshes.resize(mesh_count);
     if (has_instances) scene->meshes.pop_back();
+    if (rc == SEL_OK && !scene->curves.empty()) rc = finish_curves(scene);
     if (rc == SEL_OK) rc = finish_instances(scene, levels, below);
     if (rc != SEL_OK) {
         scene->committed = false;

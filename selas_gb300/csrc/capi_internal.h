@@ -32,6 +32,14 @@ struct SelSceneTy {
     uint32_t tuned_paths_in_flight = 0; // sel_scene_autotune's choices (0: built-in defaults)
     uint32_t tuned_trace_block = 0;
     std::vector<sel::MeshInput> meshes;
+    // round B-spline curve geometries (sel_scene_attach_curve_mesh): control points (x, y, z, radius) and the
+    // first control point of each segment
+    struct CurveInput {
+        uint32_t geomID;
+        std::vector<float> points;
+        std::vector<uint32_t> indices;
+    };
+    std::vector<CurveInput> curves;
     // instances of other committed scenes (sel_scene_attach_instance): id, instanced scene, transforms
     struct InstanceInput {
         uint32_t instID;
@@ -116,6 +124,10 @@ int sync_shading(SelSceneTy* sc);              // uploads materials, lights, Pte
 int set_material_flags(SelSceneTy* sc, unsigned int geomID, const SelMaterial& material, bool transparent);
 // The Ptex writer's constant and constant-neighbourhood flags of `count` PtexQuadFace records (ptex_quad.cuh)
 void flag_constant_quads(void* records, size_t count, const uint16_t* texels);
+// curve.cu: replaces *d_tris (`records` leaf records) by a copy followed by the segments' control points (nseg x
+// 16 floats) and points each kTriCurve record at its segment (geoms[k] / bases[k]: geomID and first segment)
+cudaError_t attach_curve_data(void** d_tris, uint64_t records, const float* data, size_t nseg, const uint32_t* geoms,
+                              const uint32_t* bases, uint32_t ngeoms);
 // capi.cpp: `top` releases `scenes` (created after the scenes they instance) when it is released
 void adopt_scenes(SelSceneTy* top, const std::vector<SelSceneTy*>& scenes);
 // CalculateIntensityMap + CalculateStrataDistributionFunctions (BuildImageBasedLight.cpp:18-107): marginal CDF

@@ -62,7 +62,7 @@ constexpr uint32_t kFlagTransparent = 1u, kFlagUsesPtex = 16u;  // MaterialFlags
 // indicesPerFace, nameHash (u32 each), name FixedString64.
 constexpr size_t kMesh = 92, kMeshName = 28;
 // ModelResourceData (ModelResource.h:125-149)
-constexpr size_t kModelVertexCount = 24, kModelMaterials = 168,
+constexpr size_t kModelVertexCount = 24, kModelCurveVertexCount = 28, kModelCurveName = 32, kModelMaterials = 168,
                  kModelMaterialHashes = 200, kModelMeshes = 232, kModelCurves = 264, kModelSize = 296;
 // ModelGeometryData (ModelResource.h:151-170): eight u64 sizes (index, faceIndex, position, normals, tangents, uvs,
 // curveIndex, curveVertex), then the eight arrays (file offsets) in the same order.
@@ -221,6 +221,10 @@ struct Model {
     std::vector<Material> materials;
     std::vector<Mesh> meshes;
     uint64_t curves = 0;
+    std::vector<std::pair<uint32_t, uint32_t>> curve_ranges;  // CurveMetaData: (indexOffset, indexCount)
+    uint32_t curve_material = 0;                              // curveModelName (a material name hash)
+    uint32_t curve_vertex_count = 0;
+    size_t curve_indices = 0, curve_vertices = 0;             // offsets in the geometry blob
     Blob geometry;
     size_t indices = 0, positions = 0, normals = 0, tangents = 0, uvs = 0;  // offsets (0: absent)
     uint64_t index_count = 0;
@@ -285,7 +289,12 @@ Model load_model(const std::string& root, const std::string& name) {
             throw BlobError{b.path + ": mesh " + x.name + " index count is not a multiple of its face size"};
         m.meshes.push_back(x);
     }
-    m.curves = b.carray(kModelCurves, 8, "curves").first;
+    const auto curves = b.carray(kModelCurves, 8, "curves");
+    m.curves = curves.first;
+    for (uint64_t i = 0; i < curves.first; ++i)  // CurveMetaData (ModelResource.h:107-111): indexOffset, indexCount
+        m.curve_ranges.emplace_back(b.get<uint32_t>(curves.second + 8 * i), b.get<uint32_t>(curves.second + 8 * i + 4));
+    m.curve_vertex_count = b.get<uint32_t>(kModelCurveVertexCount);
+    m.curve_material = b.get<uint32_t>(kModelCurveName);
 
     m.geometry = read_blob(root, kModelGeometryType, kModelVersion, name);
     const Blob& g = m.geometry;
@@ -313,6 +322,19 @@ Model load_model(const std::string& root, const std::string& name) {
         for (uint32_t k = 0; k < x.index_count; ++k)
             if (g.get<uint32_t>(m.indices + 4 * (size_t(x.index_offset) + k)) >= nv)
                 throw BlobError{g.path + ": mesh " + x.name + " indexes past the vertex array"};
+    }
+    // curves (InitializeCurves, ModelResource.cpp:300-332): one index per segment into the float4 control points
+    if (m.curves) {
+        const uint64_t ncv = m.curve_vertex_count;
+        if (sizes[6] % 4 || sizes[7] != ncv * 16) throw BlobError{g.path + ": curve array sizes"};
+        m.curve_indices = g.array(kGeomPtrs + 48, sizes[6] / 4, 4, "curveIndices");
+        m.curve_vertices = g.array(kGeomPtrs + 56, ncv, 16, "curveVertices");
+        for (const auto& c : m.curve_ranges) {
+            if (uint64_t(c.first) + c.second > sizes[6] / 4) throw BlobError{g.path + ": a curve indexes past curveIndices"};
+            for (uint32_t k = 0; k < c.second; ++k)
+                if (uint64_t(g.get<uint32_t>(m.curve_indices + 4 * (size_t(c.first) + k))) + 3 >= ncv)
+                    throw BlobError{g.path + ": a curve segment runs past curveVertices"};
+        }
     }
     return m;
 }
@@ -558,6 +580,25 @@ int build_model(SelDevice dev, const Subscene& sub, const Model& m, const Materi
             if ((rc = sel_scene_set_texture(sc, unsigned(k), t.rgb.data(), t.width, t.height, 3))) return rc;
         }
     }
+    // curve c as geomID meshes + c, with the material of the model's curveModelName and no texture
+    // (InitializeGeometryUserDatas, ModelResource.cpp:346-363)
+    for (size_t c = 0; c < m.curve_ranges.size(); ++c) {
+        const auto& range = m.curve_ranges[c];
+        std::vector<uint32_t> idx(range.second);
+        if (!idx.empty()) std::memcpy(idx.data(), base + m.curve_indices + 4 * size_t(range.first), 4 * idx.size());
+        const uint32_t lo = idx.empty() ? 0u : *std::min_element(idx.begin(), idx.end());
+        const uint32_t hi = idx.empty() ? 0u : *std::max_element(idx.begin(), idx.end()) + 4u;
+        for (uint32_t& i : idx) i -= lo;
+        std::vector<float> pts(size_t(hi - lo) * 4);
+        if (!pts.empty()) std::memcpy(pts.data(), base + m.curve_vertices + 16 * size_t(lo), 4 * pts.size());
+        const unsigned geom = unsigned(m.meshes.size() + c);
+        int rc = sel_scene_attach_curve_mesh(sc, geom, pts.data(), hi - lo, idx.data(), idx.size());
+        if (rc) return rc;
+        const Material& mat = find_mesh_material(m, sub, m.curve_material, fallback);
+        SelMaterial sm = to_sel(mat, uint32_t(sub.light_set));
+        sm.usesPtex = 0u;
+        if ((rc = sel::set_material_flags(sc, geom, sm, (mat.flags & kFlagTransparent) != 0u))) return rc;
+    }
     return sel_scene_commit(sc);
 }
 
@@ -696,9 +737,6 @@ int sel_scene_load_cooked(SelDevice device, const char* asset_root, const char* 
         const SceneAssets s = load_assets(asset_root, scene_name);
         SelCookedSceneInfo info;
         fill_info(s, &info);
-        if (info.curves)
-            return fail(SEL_ERR_INVALID_OPERATION, "the scene's models hold curves (RTC_GEOMETRY_TYPE_ROUND_BSPLINE_CURVE), "
-                                                   "which this loader does not build");
         const Material fallback = default_material();
         const std::vector<MeshRow> rows = mesh_rows(s, fallback);
         std::map<std::string, int> tex;

@@ -86,4 +86,17 @@ __device__ __forceinline__ float3 world_normal(const HitRef& r, float3 ng) {
     return ng;
 }
 
+// Object-space geometric normal of a hit on leaf record tp (words p0, p1, p2): the triangle's, or for a curve
+// segment the normal at (t, u) of the world ray (o, d) taken into the hit mesh's space through the entered
+// instances, outermost first, as the instanced traversal takes it (curve.cuh).
+__device__ __forceinline__ float3 record_ng(const float4* tp, const float4& p0, const float4& p1, const float4& p2,
+                                            const InstanceRecord* rec0, const InstanceRecord* rec1, float3 o, float3 d,
+                                            float t, float u) {
+    if (__float_as_uint(p2.w) != kTriCurve) return triangle_ng(p0, p1, p2);
+    float ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+    if (rec0) inst_apply(rec0, ox, oy, oz, dx, dy, dz);
+    if (rec1) inst_apply(rec1, ox, oy, oz, dx, dy, dz);
+    return curve_ng(curve_points(tp, p0), ox, oy, oz, dx, dy, dz, t, u);
+}
+
 }  // namespace sel

@@ -14,6 +14,7 @@
 // (instID[0], instID[1], geomID, primID), so the result does not depend on the tree shapes.
 #pragma once
 
+#include "curve.cuh"
 #include "traverse.cuh"
 
 namespace sel {
@@ -174,7 +175,15 @@ __device__ __forceinline__ bool inst_step(InstState& s, uint2* stack, int stride
             break;
         }
         float t, u, v;
-        if (watertight_intersect(s.w.wt, s.w.ox, s.w.oy, s.w.oz, p0, p1, p2, s.w.tnear, s.w.tfar, t, u, v)) {
+        bool hit;
+        if (__float_as_uint(p2.w) == kTriCurve) {  // a round B-spline curve segment (curve.cuh)
+            v = 0.0f;
+            hit = curve_intersect(curve_points(tp, p0), s.w.ox, s.w.oy, s.w.oz, s.w.dx, s.w.dy, s.w.dz, s.w.tnear,
+                                  s.w.tfar, t, u);
+        } else {
+            hit = watertight_intersect(s.w.wt, s.w.ox, s.w.oy, s.w.oz, p0, p1, p2, s.w.tnear, s.w.tfar, t, u, v);
+        }
+        if (hit) {
             if (kAnyHit) {
                 inst_record_hit(s, t, u, v, ti);
                 return true;

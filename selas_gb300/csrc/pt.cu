@@ -467,7 +467,9 @@ __global__ void __launch_bounds__(kBlock, kModes == 1u ? 5 : 4) k_shade(PtParams
                 const MeshAttrDev* attr = geom < hr.attr_count ? hr.attrs + geom : nullptr;
                 float3 fn, ft, fb;
                 float fsign;
-                shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2),
+                const float3 ng = kInst ? record_ng(hr.tp, p0, p1, p2, hr.rec0, hr.rec1, o, d, hit.x, hit.y)
+                                        : triangle_ng(p0, p1, p2);
+                shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, ng,
                               [&](float3 x) { return kInst ? world_normal(hr, x) : x; }, fn, ft, fb, fsign);
                 // RayPick error bound (PathTracer.cpp:134-136)
                 const float err = 32.0f * 1.19209e-07f *

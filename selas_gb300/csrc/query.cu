@@ -2,6 +2,7 @@
 // launchers.  One thread per ray; each thread keeps its traversal stack in shared memory.
 #include "query.h"
 
+#include "hitref.cuh"
 #include "instance.cuh"
 #include "traverse.cuh"
 
@@ -52,7 +53,15 @@ __device__ __forceinline__ void store_hit(SelRayHit* rh, const float4* __restric
 __device__ __forceinline__ void store_hit_instanced(SelRayHit* rh, const InstHit& h) {
     const float4* tp = h.tris + size_t(h.tri) * 3;
     const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
-    const float3 ng = triangle_ng(p0, p1, p2);  // object space of the hit mesh
+    // object space of the hit mesh (a curve segment's from the ray, curve.cuh)
+    float3 ng;
+    if (__float_as_uint(p2.w) == kTriCurve) {
+        const float* ray = reinterpret_cast<const float*>(rh);
+        ng = record_ng(tp, p0, p1, p2, h.rec[0], h.rec[1], make_float3(ray[0], ray[1], ray[2]),
+                       make_float3(ray[4], ray[5], ray[6]), h.t, h.u);
+    } else {
+        ng = triangle_ng(p0, p1, p2);
+    }
     float u = h.u, v = h.v;
     uint32_t prim;
     embree_hit(p0, p2, u, v, prim);
@@ -91,7 +100,9 @@ __global__ void __launch_bounds__(kQueryBlock)
 // the lockstep that makes node fetches shared), so the hardware block scheduler does the balancing.
 // Postponing a lane's leaf triangles while few lanes of its warp test triangles (Ylitie, Karras, Laine 2017)
 // was slower too at every threshold tried (6, 10, 16 lanes: incoherent closest hit 1,382 / 1,376 / 1,356
-// against 1,418 Mrays/s without), with identical hits.
+// against 1,418 Mrays/s without), with identical hits.  So was prefetching, before each step's leaf tests, the
+// lines of its leaf records and of the node the next step visits (prefetch.global.L1 / .L2): incoherent closest
+// hit 1,417 against 1,431 Mrays/s, and the Cornell box's path tracer 11 % slower.
 constexpr int kWideBlocksPerSm = 8;
 
 template <bool kAnyHit>

@@ -70,6 +70,14 @@ int upload(void*& dst, const T* src, size_t count) {
 
 namespace sel {
 
+// One past the largest geomID of the scene's meshes and curves: the size of its per-geomID material table.
+static uint32_t geom_limit(const SelSceneTy* sc) {
+    uint32_t n = 0;
+    for (const MeshInput& m : sc->meshes) n = m.geomID + 1 > n ? m.geomID + 1 : n;
+    for (const SelSceneTy::CurveInput& c : sc->curves) n = c.geomID + 1 > n ? c.geomID + 1 : n;
+    return n;
+}
+
 void ibl_densities(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& mdf, std::vector<float>& cdf) {
     mdf.assign(height, 0.0f);
     cdf.assign(size_t(width) * height, 0.0f);
@@ -244,8 +252,7 @@ int sync_shading(SelSceneTy* sc) {
         sc->sort_hint = (ptex || __builtin_popcount(mask) > 1) ? 1u : 0u;
         return SEL_OK;
     }
-    uint32_t max_geom = 0;
-    for (const MeshInput& m : sc->meshes) max_geom = m.geomID + 1 > max_geom ? m.geomID + 1 : max_geom;
+    const uint32_t max_geom = geom_limit(sc);
     if (max_geom > kMaxGeom) return fail(SEL_ERR_INVALID_OPERATION, "rendering needs geomIDs below 65536");
     std::vector<MaterialDev> mats(max_geom ? max_geom : 1, to_device(default_material()));
     for (size_t i = 0; i < sc->materials.size() && i < mats.size(); ++i)
@@ -318,11 +325,13 @@ int sync_shading(SelSceneTy* sc) {
     // material classes of the attached meshes (shader x Ptex x transparency, as the path tracer sorts them)
     {
         uint32_t seen = 0;
-        for (const MeshInput& mi : sc->meshes) {
-            const MaterialDev& m = mats[mi.geomID < mats.size() ? mi.geomID : 0];
+        auto see = [&](uint32_t geomID) {
+            const MaterialDev& m = mats[geomID < mats.size() ? geomID : 0];
             const uint32_t shader = uint32_t(m.shader) < 3u ? uint32_t(m.shader) : 0u;
             seen |= 1u << (shader * 4u + ((m.flags & kMaterialTextured) ? 2u : 0u) + ((m.flags & kMaterialTransparent) ? 1u : 0u));
-        }
+        };
+        for (const MeshInput& mi : sc->meshes) see(mi.geomID);
+        for (const SelSceneTy::CurveInput& c : sc->curves) see(c.geomID);
         bool ptex = false;
         for (const auto& m : mats) ptex |= (m.flags & kMaterialTextured) != 0;
         sc->class_mask = seen;
@@ -496,8 +505,7 @@ PtScene scene_view(const SelSceneTy* sc) {
     ps.bvh_kind = sc->info.bvh_kind == SEL_BVH_WIDE8_Q8 ? 0 : 1;
     ps.tris = static_cast<const float4*>(sc->d_tris);
     ps.materials = static_cast<const MaterialDev*>(sc->d_materials);
-    uint32_t max_geom = 0;
-    for (const MeshInput& m : sc->meshes) max_geom = m.geomID + 1 > max_geom ? m.geomID + 1 : max_geom;
+    const uint32_t max_geom = geom_limit(sc);
     ps.material_count = max_geom ? max_geom : 1;
     ps.lights = static_cast<const QuadLight*>(sc->d_lights);
     ps.light_sets = static_cast<const uint2*>(sc->d_light_sets);
@@ -821,6 +829,9 @@ int sel_scene_set_texture(SelScene scene, unsigned int geomID, const float* data
         return fail(SEL_ERR_INVALID_ARGUMENT, "channels must be 1, 3 or 4");
     if (width > 16384 || height > 16384) return fail(SEL_ERR_INVALID_ARGUMENT, "width and height must be at most 16384");
     std::lock_guard<std::mutex> lock(scene->mu);
+    for (const SelSceneTy::CurveInput& c : scene->curves)
+        if (c.geomID == geomID && width && height)
+            return fail(SEL_ERR_INVALID_OPERATION, "curves take no texture (they have no uvs)");
     auto& list = scene->textures;
     for (size_t i = 0; i < list.size(); ++i)
         if (list[i].geomID == geomID) {

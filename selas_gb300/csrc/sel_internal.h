@@ -24,6 +24,9 @@ struct TriRecord {
 };
 constexpr uint32_t kTriPlain = 0u;
 constexpr uint32_t kTriQuadHalf = 1u;
+// a round B-spline curve segment (curve.cuh): v0.x / v0.y hold the byte offset from the record to its four
+// control points; while the BVH is built, v0 / v1 are the corners of the segment's box
+constexpr uint32_t kTriCurve = 2u;
 static_assert(sizeof(TriRecord) == 48, "TriRecord must be 48 bytes");
 
 // 8-wide node with child boxes quantised to 8 bits per axis (80 bytes = 5 x uint4).
@@ -69,6 +72,7 @@ struct MeshInput {
     std::vector<float> vertices;   // xyz packed
     std::vector<uint32_t> indices; // 3 per triangle; a quad mesh holds each quad as two triangles (see quads)
     bool quads = false;            // RTC_GEOMETRY_TYPE_QUAD: triangle 2q is (v0, v1, v3), 2q + 1 is (v2, v3, v1)
+    bool curves = false;           // box triangles (lo, hi, lo) standing for curve segments (kTriCurve records)
     std::vector<float> attr[4];    // per-vertex attributes (sel_scene_set_vertex_attribute), attr_n[slot] floats each
     uint32_t attr_n[4] = {0, 0, 0, 0};
 };

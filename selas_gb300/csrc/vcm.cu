@@ -285,7 +285,9 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
     }
     h.view = -dir;
     float3 fn, ft, fb;
-    shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, triangle_ng(p0, p1, p2),
+    const float3 ng = kInst ? record_ng(hr.tp, p0, p1, p2, hr.rec0, hr.rec1, org, dir, hit.x, hit.y)
+                            : triangle_ng(p0, p1, p2);
+    shading_frame(attr, __float_as_uint(p0.w), hit.y, hit.z, ng,
                   [&](float3 x) { return kInst ? world_normal(hr, x) : x; }, fn, ft, fb, h.bsign);
     h.s = make_surface_frame(m, ft, fn, fb, h.view, pow3(base, 2.2f));
     h.n = h.s.n;

@@ -225,6 +225,7 @@ class RenderScene:
     ibl: dict = None                                # light (H, W, 3), miss (h, w, 3) or None, rotation, exposure
     attrs: dict = None                              # geomID -> {"normals": (n, 3), "tangents": (n, 4), "uvs": (n, 2)}
     textures: dict = None                           # geomID -> 2D base-colour image (h, w, 1 | 3 | 4) floats
+    curves: dict = None                             # geomID -> (control points (n, 4), segment first points (k,))
 
     def attach_attributes(self, sc) -> None:
         for gid, a in (self.attrs or {}).items():
@@ -286,6 +287,8 @@ class RenderScene:
         """Creates and commits a selas_gb300 Scene with this content."""
         sc = sel_module.Scene(device, bvh_kind, build_mode)
         self.geometry.attach_to(sc)
+        for gid, (pts, idx) in sorted((self.curves or {}).items()):
+            sc.attach_curve_mesh(gid, pts, idx)
         self.attach_attributes(sc)
         for gid, m in self.materials.items():
             sc.set_material(gid, sel_module.material(**m))
@@ -531,6 +534,28 @@ def quad_textured_cubes(count: int = 4, m: int = 3, log2: int = 3, seed: int = 0
     return RenderScene(g, mats, [(0, light)], (0.1, 0.1, 0.12), cam, ptex=ptex)
 
 
+def curve_strands(strands: int = 24, points: int = 6, length: float = 2.0, root: float = 0.06, tip: float = 0.015,
+                  seed: int = 0x5E1A5C01):
+    """Hair-like strands for round B-spline curves, laid out as the reference's curve model builder lays out a
+    strand of m control points (CDisneySceneBuildProcessor.cpp:177-220): the first and last points repeated, radii
+    from `root` to `tip` along the strand, m - 1 segments starting at consecutive points.  Returns (points (n, 4)
+    x, y, z, radius; indices (segments,))."""
+    rng = np.random.default_rng(seed)
+    pts, idx = [], []
+    for _ in range(strands):
+        base = np.array([rng.uniform(-1.5, 1.5), 0.0, rng.uniform(-1.0, 1.0)])
+        bend = rng.normal(scale=0.4, size=3)
+        cps = [base + np.array([0.0, length * k / (points - 1), 0.0]) + bend * (k / (points - 1)) ** 2
+               for k in range(points)]
+        widths = [root + (tip - root) * k / (points - 1) for k in range(points)]
+        first = len(pts)
+        pts.append(list(cps[0]) + [root])
+        pts += [list(c) + [w] for c, w in zip(cps, widths)]
+        pts.append(list(cps[-1]) + [tip])
+        idx += [first + k for k in range(points - 1)]
+    return np.array(pts, np.float32), np.array(idx, np.uint32)
+
+
 def textured_spheres(count: int = 6, level: int = 3, log2: int = 4, seed: int = 0x5E1A5F00) -> RenderScene:
     """A few displaced icospheres with per-face Ptex value-noise base colour (16 x 16 FP16 RGB by default)
     on a grey floor, under one 2 x 2 quad light and a dim background."""
@@ -687,6 +712,8 @@ class InstancedRenderScene:
             if p.geometry.meshes:
                 p.geometry.attach_to(sc)
                 p.attach_attributes(sc)
+            for gid, (pts, idx) in sorted((getattr(p, "curves", None) or {}).items()):
+                sc.attach_curve_mesh(gid, pts, idx)
             for gid, m in p.materials.items():
                 sc.set_material(gid, sel_module.material(**m))
             for ls, l in p.lights:

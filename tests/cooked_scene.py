@@ -16,7 +16,11 @@ What the scenes exercise:
     which shading samples mip 0); walls with normals, tangents and uvs, the box model without attributes;
   * "cornell_sky": the same subscenes under an image-based light (an IBL blob with the reference's densities);
   * "cornell_ptex": a subscene whose material samples Ptex (eUsesPtex), which the loader refuses unless asked to
-    render such materials with their base colour.
+    render such materials with their base colour;
+  * "cornell_hair": the Cornell subscenes plus a third whose model holds a plate mesh and two round B-spline
+    curves (CurveMetaData ranges over one shared curve vertex array, the material named by curveModelName and
+    found among the subscene's scene materials), loaded as geomIDs after the model's meshes
+    (InitializeCurves, ModelResource.cpp:300-332).
 """
 from __future__ import annotations
 
@@ -157,6 +161,31 @@ def _box_model():
                 materials={})
 
 
+def _strands_model():
+    """A plate (one triangle mesh of two triangles) and hair strands as two curves over one curve vertex array:
+    the first three strands' segments, then the rest (indices into the shared array, as the build writes them)."""
+    pts, idx = scenes.curve_strands(strands=8, seed=0x5E1A5C07)
+    per = idx.size // 8
+    plate = np.float32([[-2, 0, -1.5], [2, 0, -1.5], [2, 0, 1.5], [-2, 0, 1.5]])
+    return dict(positions=plate, normals=None, tangents=None, uvs=None, indices=np.uint32([0, 2, 1, 0, 3, 2]),
+                meshes=[dict(name="plate", material="plate", indicesPerFace=3, indexOffset=0, indexCount=6,
+                             vertexOffset=0, vertexCount=4)],
+                materials={"plate": material(base=(0.2, 0.2, 0.25), roughness=0.8, metallic=0.0)},
+                curves=[(0, 3 * per), (3 * per, idx.size - 3 * per)], curve_indices=idx, curve_vertices=pts,
+                curve_material="hair")
+
+
+def curve_geometry(model):
+    """The model's curves as the loader attaches them: [(geomID, control points, segment first points)], each
+    curve's points cut to the range its segments use."""
+    out = []
+    for c, (off, count) in enumerate(model.get("curves", [])):
+        idx = model["curve_indices"][off:off + count]
+        lo, hi = int(idx.min()), int(idx.max()) + 4
+        out.append((len(model["meshes"]) + c, model["curve_vertices"][lo:hi], (idx - lo).astype(np.uint32)))
+    return out
+
+
 def _checker_texture():
     n = 8
     y, x = np.mgrid[0:n, 0:n]
@@ -181,6 +210,9 @@ def cooked_cornell():
                       materials=[("box_paint", box_paint)]),
         "room_ptex": dict(light_set=0, models=["walls"], instances=[(0, np.eye(4, dtype=np.float32))],
                           materials=[("green", material(base=(0.12, 0.45, 0.15), texture="ptex/walls", ptex=True))]),
+        "hairy": dict(light_set=0, models=["strands"],
+                      instances=[(0, _affine((70, 70, 70), 25.0, (170.0, 0.5, 110.0)))],
+                      materials=[("hair", material(base=(0.45, 0.3, 0.15), roughness=0.35, metallic=0.1))]),
     }
     light = dict(type=0, position=(278.0, 554.0, 279.5), direction=(0.0, -1.0, 0.0), x=(130.0, 0.0, 0.0),
                  z=(0.0, 0.0, 105.0), radiance=(17.0, 12.0, 4.0))
@@ -191,9 +223,12 @@ def cooked_cornell():
                       lights=[light], ranges=[(0, 1)], cameras=[camera])
     scenes_ = {"cornell": base_scene,
                "cornell_sky": dict(copy.deepcopy(base_scene), ibl="sky", background=(0.0, 0.0, 0.0, 1.0)),
-               "cornell_ptex": dict(copy.deepcopy(base_scene), subscenes=["room_ptex", "props"])}
+               "cornell_ptex": dict(copy.deepcopy(base_scene), subscenes=["room_ptex", "props"]),
+               "cornell_hair": dict(copy.deepcopy(base_scene), subscenes=["room", "props", "hairy"],
+                                    instances=base_scene["instances"] + [(2, _affine())])}
     sky = scenes.sky_ibl(width=32, height=16, miss_size=(16, 8))
-    return dict(scenes=scenes_, subscenes=subscenes, models={"walls": _wall_model(), "box": _box_model()},
+    return dict(scenes=scenes_, subscenes=subscenes,
+                models={"walls": _wall_model(), "box": _box_model(), "strands": _strands_model()},
                 textures={"checker": _checker_texture()},
                 ibls={"sky": dict(light=sky["light"], miss=sky["miss"], rotation=float(sky.get("rotation", 0.0)),
                                   exposure=float(sky.get("exposure", 1.0)))})
@@ -280,9 +315,13 @@ def instanced_scene(assets, scene_name):
                     attrs[k] = a
                 if m["texture"] and not m["flags"] & E_USES_PTEX:
                     textures[k] = assets["textures"][m["texture"]]["mips"][0]
+            curves = {}
+            for gid, pts, idx in curve_geometry(model):
+                curves[gid] = (pts, idx)
+                mats[gid] = _sel_material(find_mesh_material(model, sub, model["curve_material"]), sub["light_set"])
             model_part.append(len(parts))
             parts.append(scenes.RenderScene(g, mats, [], (0.0, 0.0, 0.0), {}, attrs=attrs or None,
-                                            textures=textures or None))
+                                            textures=textures or None, curves=curves or None))
             instances.append([])
         for j, (index, m) in enumerate(sub["instances"]):
             instances[sub_part[si]].append((j, model_part[index], np.asarray(m, np.float32)))

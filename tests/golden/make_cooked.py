@@ -93,16 +93,22 @@ def write_all(assets, root: Path):
         nrm, tan, uvs = (None if m[k] is None else np.ascontiguousarray(m[k], np.float32)
                          for k in ("normals", "tangents", "uvs"))
         idx = np.ascontiguousarray(m["indices"], np.uint32)
+        curves = np.ascontiguousarray(np.array(m.get("curves", []), np.uint32).reshape(-1, 2))
+        cidx = np.ascontiguousarray(m.get("curve_indices", np.zeros(0)), np.uint32)
+        cpts = np.ascontiguousarray(m.get("curve_vertices", np.zeros((0, 4))), np.float32)
+        cname = cs.name_hash(m["curve_material"]) if "curve_material" in m else 0
         assert L.ref_cooked_write_model(r, name.encode(), pos.shape[0], _p(pos), _p(nrm), _p(tan), _p(uvs), idx.size,
                                         _p(idx), _p(words), _strings([x["name"] for x in m["meshes"]]),
-                                        len(m["meshes"]), _p(hashes), _p(ints), _p(floats), tex, len(pairs), 0, None,
-                                        0, None, 0, None, 0) == 0
+                                        len(m["meshes"]), _p(hashes), _p(ints), _p(floats), tex, len(pairs), cname,
+                                        _p(curves) if curves.size else None, curves.shape[0],
+                                        _p(cidx) if cidx.size else None, cidx.size,
+                                        _p(cpts) if cpts.size else None, cpts.shape[0]) == 0
         counts = np.zeros(6, np.uint64)
         back_words = np.zeros_like(words)
         back_idx = np.zeros_like(idx)
         assert L.ref_cooked_read_model(r, name.encode(), _p(counts), _p(back_words), words.shape[0], _p(back_idx),
                                        idx.size) == 0
-        assert list(counts[:5]) == [len(m["meshes"]), len(pairs), 0, pos.shape[0], idx.size], counts
+        assert list(counts[:5]) == [len(m["meshes"]), len(pairs), curves.shape[0], pos.shape[0], idx.size], counts
         assert counts[5] == (0 if uvs is None else uvs.size * 4)
         np.testing.assert_array_equal(back_words, words)
         np.testing.assert_array_equal(back_idx, idx)

@@ -33,7 +33,7 @@ def _sel_fields(m):
                     m.clearcoatGloss, m.specTrans, m.diffuseTrans, m.flatness, m.ior, m.scatterDistance]))
 
 
-@pytest.mark.parametrize("name", ["cornell", "cornell_sky", "cornell_ptex"])
+@pytest.mark.parametrize("name", ["cornell", "cornell_sky", "cornell_ptex", "cornell_hair"])
 def test_describe_matches_the_description(name):
     info, meshes = sel.cooked_describe(ROOT, name)
     sd = ASSETS["scenes"][name]
@@ -41,7 +41,9 @@ def test_describe_matches_the_description(name):
     assert info.subscenes == len(sd["subscenes"]) and info.subsceneInstances == len(sd["instances"])
     assert info.models == sum(len(s["models"]) for s in subs)
     assert info.modelInstances == sum(len(s["instances"]) for s in subs)
-    assert (info.lights, info.lightSets, info.cameras, info.curves) == (1, 1, 1, 0)
+    curves = sum(len(ASSETS["models"][m].get("curves", [])) for s in subs for m in s["models"])
+    assert (info.lights, info.lightSets, info.cameras, info.curves) == (1, 1, 1, curves)
+    assert curves == (2 if name == "cornell_hair" else 0)
     assert list(info.backgroundIntensity) == list(np.float32(sd["background"]))
     assert info.ibl.decode() == sd["ibl"]
     cam = sd["cameras"][0]
@@ -192,7 +194,42 @@ def test_gpu_cooked_scene_equals_the_scene_built_by_hand(device):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cornell", "cornell_sky"])
+def test_gpu_cooked_curves_report_the_reference_ids(device):
+    """The hair subscene's curves load as geomIDs 1 and 2 of the strands model (after its plate mesh), with the
+    material curveModelName names; every query field equals that of the same graph built by hand."""
+    sc, info = sel.load_cooked(device, ROOT, "cornell_hair")
+    iscene = cs.instanced_scene(ASSETS, "cornell_hair")
+    built = iscene.build(sel, device)
+    try:
+        rng = np.random.default_rng(4)
+        n = 20000
+        org = np.tile(np.float32(info.camera.position), (n, 1))
+        # half the rays aimed near the strands' control points (world space), half over the region around them
+        model, (_, l2w) = ASSETS["models"]["strands"], ASSETS["subscenes"]["hairy"]["instances"][0]
+        cp = model["curve_vertices"][:, :3] @ np.asarray(l2w)[:3, :3].T + np.asarray(l2w)[:3, 3]
+        near = cp[rng.integers(0, cp.shape[0], n // 2)] + rng.normal(scale=3.0, size=(n // 2, 3))
+        target = np.concatenate([near, rng.uniform([60, 0, 30], [280, 160, 190], size=(n - n // 2, 3))])
+        target = target.astype(np.float32)
+        d = (target - org).astype(np.float32)
+        got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
+        sc.intersect1M(got)
+        built[0].intersect1M(want)
+        for f in ("geomID", "primID", "instID0", "instID1", "tfar", "u", "v", "Ng_x", "Ng_y", "Ng_z"):
+            np.testing.assert_array_equal(got[f], want[f], err_msg=f)
+        hair = got["instID0"] == 2
+        assert set(np.unique(got["geomID"][hair])) == {0, 1, 2}
+        assert (got["v"][hair & (got["geomID"] > 0)] == 0).all()
+        cam = _camera(info, 48, 40)
+        a = sc.pt_generate_image(cam, sel.pt_settings(4, 6, SEED))
+        b = built[0].pt_generate_image(cam, sel.pt_settings(4, 6, SEED))
+        np.testing.assert_array_equal(a, b)
+    finally:
+        iscene.release(built)
+        sc.release()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cornell", "cornell_sky", "cornell_hair"])
 def test_gpu_cooked_scene_traces_the_oracles_paths(device, name):
     sc, info = sel.load_cooked(device, ROOT, name)
     try:
