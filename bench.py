@@ -791,8 +791,10 @@ def run_ours(args):
         h2d = sum(v.nbytes for v in recs.values())
         e2e = {"value": round(world * queries_per_step * e2e_steps / el / 1e6, 3), "unit": "Mrays/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
-               "path": "sel_intersect1M / sel_occluded1M on records in pinned host memory: the query kernels read "
-                       "the rays and write the hits in place over the host link (SEL_OPTION_ZERO_COPY)",
+               "path": "sel_intersect1M / sel_occluded1M on records in pinned host memory: incoherent batches are "
+                       "traced in place, the query kernels reading rays and writing hits over the host link; large "
+                       "batches of coherent rays are staged through HBM by full-duplex copies pipelined over four "
+                       "streams (SEL_OPTION_ZERO_COPY)",
                "staged_copies_value": round(world * queries_per_step * e2e_steps / el_staged / 1e6, 3),
                "steps": e2e_steps}
 

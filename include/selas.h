@@ -113,7 +113,10 @@ enum {
     SEL_OPTION_ZERO_COPY = 4      /* 1 (default): the host-memory queries (sel_intersect1M etc.) trace records
                                      that lie in page-locked host memory the GPU can address (cudaHostAlloc /
                                      cudaHostRegister) in place, the kernel reading rays and writing hits over
-                                     the host link; 0: always stage them through HBM with pipelined copies */
+                                     the host link, except batches of more than 524,288 records whose rays
+                                     run nearly parallel record to record (camera rays: their traversal is
+                                     too short to hide the link, so full-duplex staged copies are faster);
+                                     0: always stage them through HBM with pipelined copies */
 };
 int sel_device_set_option(SelDevice device, int option, int value);
 

@@ -108,7 +108,7 @@ int sel_device_new(int cuda_device, SelDevice* out_device) {
     dev->cuda_device = cuda_device;
     if (int rc = set_device(dev)) { delete dev; return rc; }
     e = cudaStreamCreateWithFlags(&dev->stream, cudaStreamNonBlocking);
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&dev->qstream[k], cudaStreamNonBlocking);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&dev->qstream[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&dev->d_err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(dev->d_err, 0, sizeof(uint32_t));
     // The allocation-free query's staging array: resolving its address here loads its module (and so
@@ -735,6 +735,29 @@ static bool mapped_host_range(const void* p, size_t bytes, int device, void** dp
     return true;
 }
 
+// Whether a batch's rays run nearly parallel from one record to the next (camera rays in pixel order): sampled
+// pairs of neighbouring records, directions within about 2.5 degrees.  Such rays traverse so fast that moving
+// the records over the host link is the whole cost, and the copy engines' full-duplex staging moves them
+// fastest; incoherent rays traverse long enough to hide the link's latency, and the query kernel reads and
+// writes them in place.
+static bool coherent_batch(const void* recs, size_t byte_stride, unsigned int M) {
+    constexpr unsigned kPairs = 256;
+    if (M < 2) return false;
+    const unsigned pairs = std::min(M - 1, kPairs);
+    const size_t step = size_t(M - 1) / pairs;
+    const char* base = static_cast<const char*>(recs);
+    unsigned close = 0;
+    for (unsigned k = 0; k < pairs; ++k) {
+        const float* a = reinterpret_cast<const float*>(base + size_t(k) * step * byte_stride) + 4;
+        const float* b = reinterpret_cast<const float*>(base + (size_t(k) * step + 1) * byte_stride) + 4;
+        const double d = double(a[0]) * b[0] + double(a[1]) * b[1] + double(a[2]) * b[2];
+        const double n = std::sqrt((double(a[0]) * a[0] + double(a[1]) * a[1] + double(a[2]) * a[2]) *
+                                   (double(b[0]) * b[0] + double(b[1]) * b[1] + double(b[2]) * b[2]));
+        if (n > 0.0 && d > 0.999 * n) ++close;
+    }
+    return 2 * close > pairs;
+}
+
 template <typename Rec, bool kHit>
 static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_stride) {
     if (int rc = check_query(scene)) return rc;
@@ -750,26 +773,29 @@ static int host_query(SelScene scene, Rec* recs, unsigned int M, size_t byte_str
     cudaError_t e = cudaSuccess;
     // Records in page-locked host memory the GPU can address (over NVLink-C2C on Grace): the query kernel reads
     // each ray and writes each hit in place, so only the fields it touches cross the link and no staging buffer
-    // or copy is needed.  Any 16-byte aligned stride that is a multiple of 16 works.
+    // or copy is needed.  Any 16-byte aligned stride that is a multiple of 16 works.  Large dense batches of
+    // coherent rays take the staged pipeline below instead (coherent_batch).
+    constexpr unsigned kChunk = 1u << 18;
+    const bool staged_pipeline = dense && M > 2 * kChunk;
     void* mapped = nullptr;
     if (dev->zero_copy && byte_stride % 16 == 0 && (reinterpret_cast<uintptr_t>(recs) & 15u) == 0 &&
+        !(staged_pipeline && coherent_batch(recs, byte_stride, M)) &&
         mapped_host_range(recs, size_t(M - 1) * byte_stride + sizeof(Rec), dev->cuda_device, &mapped)) {
         e = launch_query_strided(!kHit, device_bvh(scene), mapped, byte_stride, M, dev->d_err, dev->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(dev->stream);
         if (e != cudaSuccess) return cuda_fail(e, "zero-copy query");
         return read_error_word(dev, dev->stream);
     }
-    // Large dense batches: chunks pipelined over three streams, so that one chunk's upload, another's
-    // traversal and a third's download overlap (the copy engines and the SMs work at once).
-    constexpr unsigned kChunk = 1u << 18;
-    if (dense && M > 2 * kChunk) {
-        if (int rc = ensure_scratch(scene, 3 * size_t(kChunk) * sizeof(Rec))) return rc;
+    // Large dense batches: chunks pipelined over four streams, so that uploads, traversals and downloads of
+    // different chunks overlap (the copy engines move both directions at once while the SMs traverse).
+    if (staged_pipeline) {
+        if (int rc = ensure_scratch(scene, 4 * size_t(kChunk) * sizeof(Rec))) return rc;
         Rec* slots = static_cast<Rec*>(scene->scratch);
         const DeviceBvh bvh = device_bvh(scene);
         for (unsigned c0 = 0, c = 0; c0 < M && e == cudaSuccess; c0 += kChunk, ++c) {
             const unsigned n = std::min(kChunk, M - c0);
-            cudaStream_t q = dev->qstream[c % 3];
-            Rec* d = slots + size_t(c % 3) * kChunk;
+            cudaStream_t q = dev->qstream[c % 4];
+            Rec* d = slots + size_t(c % 4) * kChunk;
             e = cudaMemcpyAsync(d, recs + c0, size_t(n) * sizeof(Rec), cudaMemcpyHostToDevice, q);
             if (e != cudaSuccess) break;
             e = kHit ? launch_intersect(bvh, reinterpret_cast<SelRayHit*>(d), n, dev->d_err, q)

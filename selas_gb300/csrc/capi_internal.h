@@ -14,7 +14,7 @@
 struct SelDeviceTy {
     int cuda_device = 0;
     cudaStream_t stream = nullptr;  // internal stream for the host-memory entry points
-    cudaStream_t qstream[3] = {nullptr, nullptr, nullptr};  // pipelined host-memory queries (chunk k on k % 3)
+    cudaStream_t qstream[4] = {nullptr, nullptr, nullptr, nullptr};  // pipelined host-memory queries (chunk k on k % 4)
     uint32_t* d_err = nullptr;      // kernel error word (iteration cap / stack overflow bits)
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT

@@ -102,7 +102,8 @@ __global__ void __launch_bounds__(kQueryBlock)
 // was slower too at every threshold tried (6, 10, 16 lanes: incoherent closest hit 1,382 / 1,376 / 1,356
 // against 1,418 Mrays/s without), with identical hits.  So was prefetching, before each step's leaf tests, the
 // lines of its leaf records and of the node the next step visits (prefetch.global.L1 / .L2): incoherent closest
-// hit 1,417 against 1,431 Mrays/s, and the Cornell box's path tracer 11 % slower.
+// hit 1,417 against 1,431 Mrays/s, and the Cornell box's path tracer 11 % slower.  Node loads marked L2
+// evict_last (createpolicy + ld.global.nc.L2::cache_hint) left every set unchanged (1,432 against 1,431).
 constexpr int kWideBlocksPerSm = 8;
 
 template <bool kAnyHit>
