@@ -109,7 +109,11 @@ enum {
                                      Ptex or several material classes; 0: shade in queue order */
     SEL_OPTION_RAY_SORT = 3,      /* 1: the path tracers order each bounce's continuing rays by direction bin
                                      (dominant axis and sign) and a Morton code of the origin before tracing
-                                     them (PathTracingBatcher.cpp:162-258); 0 (default): queue order */
+                                     them (PathTracingBatcher.cpp:162-258), and the queries trace batches of
+                                     at least 1,048,576 records in HBM (8-wide layout, no instances) in the
+                                     order of the direction's octant and a Morton code of the origin, unless
+                                     the batch's neighbouring rays run nearly parallel; 0 (default): queue
+                                     and record order */
     SEL_OPTION_ZERO_COPY = 4      /* 1 (default): the host-memory queries (sel_intersect1M etc.) trace records
                                      that lie in page-locked host memory the GPU can address (cudaHostAlloc /
                                      cudaHostRegister) in place, the kernel reading rays and writing hits over

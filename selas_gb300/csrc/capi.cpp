@@ -73,6 +73,11 @@ DeviceBvh device_bvh(const SelSceneTy* sc) {
     b.tris = static_cast<const float4*>(sc->d_tris);
     b.tri_count = uint32_t(sc->info.triangle_count);
     b.insts = static_cast<const InstanceRecord*>(sc->d_insts);
+    for (int a = 0; a < 3; ++a) {
+        b.lo[a] = sc->info.bounds_lo[a];
+        b.hi[a] = sc->info.bounds_hi[a];
+    }
+    b.order_rays = sc->dev->ray_sort;
     return b;
 }
 
@@ -114,6 +119,14 @@ int sel_device_new(int cuda_device, SelDevice* out_device) {
     // The allocation-free query's staging array: resolving its address here loads its module (and so
     // creates the array) while the device is being set up, not inside the first allocation-free call.
     if (e == cudaSuccess && resolve_noalloc_staging(dev) != SEL_OK) e = cudaErrorInvalidSymbol;
+    // The ray-order scratch of large queries is stream-ordered (cudaMallocAsync from the device's default pool):
+    // the pool keeps freed memory for the next query instead of returning it at every synchronisation.
+    if (e == cudaSuccess) {
+        cudaMemPool_t pool = nullptr;
+        e = cudaDeviceGetDefaultMemPool(&pool, cuda_device);
+        uint64_t keep = ~uint64_t(0);
+        if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e != cudaSuccess) {
         if (dev->stream) cudaStreamDestroy(dev->stream);
         for (cudaStream_t q : dev->qstream)

@@ -162,6 +162,29 @@ def test_full_size_workload(device, full_workload):
     binary.release()
 
 
+def test_ordered_large_batches_return_the_same_records(device, full_workload):
+    """SEL_OPTION_RAY_SORT: a batch of 4 M incoherent rays in HBM is traced in the order of its octant / Morton
+    keys (through an index, the records staying in place) and returns every record bit for bit as in record order;
+    the coherent batch is left in its order by the device-side gate and agrees too."""
+    pytest.importorskip("torch")
+    data, coherent, incoherent = full_workload
+    wide = _scene(device, data, sel.SEL_BVH_WIDE8_Q8)
+    try:
+        for org, d in (incoherent, coherent):
+            plain = _trace_device(wide, org, d)
+            plain_occ = _trace_device(wide, org, d, any_hit=True)
+            device.set_option(sel.SEL_OPTION_RAY_SORT, 1)
+            try:
+                ordered = _trace_device(wide, org, d)
+                ordered_occ = _trace_device(wide, org, d, any_hit=True)
+            finally:
+                device.set_option(sel.SEL_OPTION_RAY_SORT, 0)
+            assert_hits_equal(ordered, plain)
+            assert np.array_equal(ordered_occ.view(np.uint8), plain_occ.view(np.uint8))
+    finally:
+        wide.release()
+
+
 @pytest.mark.parametrize("kind", KINDS)
 def test_untraceable_rays_miss_like_the_bruteforce_definition(device, kind):
     data = scenes.displaced_icospheres(count=5, level=3, seed=11)
