@@ -768,7 +768,7 @@ def run_ours(args):
             np.copyto(host[k], recs[k])
         lib = sel.lib()
 
-        def e2e_step():
+        def e2e_step(per_set):
             el = 0.0
             for k in host:
                 np.copyto(host[k], recs[k])  # restage outside the timed calls
@@ -777,26 +777,41 @@ def run_ours(args):
                     sel.check(lib.sel_intersect1M(wide.handle, host[k].ctypes.data, counts[k], 96))
                 else:
                     sel.check(lib.sel_occluded1M(wide.handle, host[k].ctypes.data, counts[k], 48))
-                el += time.perf_counter() - t_0
+                dt = time.perf_counter() - t_0
+                per_set.setdefault(k, []).append(dt)
+                el += dt
             return el
 
-        e2e_step()
-        e2e_steps = max(2, min(args.steps, 5))
-        el = sum(e2e_step() for _ in range(e2e_steps))
+        # the first calls on freshly pinned buffers run up to 2.5x slower (the host link's address translation
+        # warms up over the 1.2 GB of records), so several untimed steps precede the timed ones
+        e2e_warmup = max(3, args.warmup)
+        for _ in range(e2e_warmup):
+            e2e_step({})
+        # host-link throughput varies from step to step (the host memory is shared with the other GPUs of the
+        # node), so the value is taken at the median step and the mean is reported beside it
+        e2e_steps = max(5, min(args.steps, 9))
+        sets_auto, sets_staged = {}, {}
+        steps_auto = [e2e_step(sets_auto) for _ in range(e2e_steps)]
         # the same calls with the records staged through HBM by pipelined copies (SEL_OPTION_ZERO_COPY = 0)
         dev.set_option(sel.SEL_OPTION_ZERO_COPY, 0)
-        e2e_step()
-        el_staged = sum(e2e_step() for _ in range(e2e_steps))
+        for _ in range(e2e_warmup):
+            e2e_step({})
+        steps_staged = [e2e_step(sets_staged) for _ in range(e2e_steps)]
         dev.set_option(sel.SEL_OPTION_ZERO_COPY, 1)
+        med_ms = lambda d: {k: round(1e3 * statistics.median(v), 3) for k, v in d.items()}
         h2d = sum(v.nbytes for v in recs.values())
-        e2e = {"value": round(world * queries_per_step * e2e_steps / el / 1e6, 3), "unit": "Mrays/s",
+        rate = lambda sec: round(world * queries_per_step / sec / 1e6, 3)
+        e2e = {"value": rate(statistics.median(steps_auto)), "unit": "Mrays/s",
+               "mean_value": rate(statistics.mean(steps_auto)),
+               "step_ms": [round(1e3 * t, 3) for t in steps_auto],
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(h2d),
                "path": "sel_intersect1M / sel_occluded1M on records in pinned host memory: incoherent batches are "
                        "traced in place, the query kernels reading rays and writing hits over the host link; large "
                        "batches of coherent rays are staged through HBM by full-duplex copies pipelined over four "
                        "streams (SEL_OPTION_ZERO_COPY)",
-               "staged_copies_value": round(world * queries_per_step * e2e_steps / el_staged / 1e6, 3),
-               "steps": e2e_steps}
+               "staged_copies_value": rate(statistics.median(steps_staged)),
+               "per_set_ms": med_ms(sets_auto), "staged_per_set_ms": med_ms(sets_staged),
+               "steps": e2e_steps, "warmup_steps": e2e_warmup}
 
     # roofline of the dominant kernel
     peak, peak_kind = measured_peaks()

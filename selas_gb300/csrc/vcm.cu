@@ -260,8 +260,9 @@ __device__ __forceinline__ void store_path(const VcmParams& P, uint32_t s, const
 }
 
 // Surface at a stored closest hit of the ray (org, dir) (CalculateSurfaceParams as the path tracer uses it).
-// kPretex: the Ptex base colour was filtered by k_vtexture into P.st.base[s] (material-sorted bounces).  Scenes
-// with Ptex always take the sorted bounces, so the unsorted form samples 2D images only.
+// kPretex: the base colour of textured hits was filtered or sampled by k_vtexture into P.st.base[s] (every bounce
+// of a material-sorted pass or of a scene with quad-mesh Ptex); otherwise the shading kernel filters triangle Ptex
+// and samples 2D images itself (the plain form: SEL_OPTION_MATERIAL_SORT 0).
 template <bool kPretex, bool kInst>
 __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir, float4 hit, VHit& h,
                           uint32_t& status) {
@@ -279,7 +280,13 @@ __device__ void make_vhit(const VcmParams& P, uint32_t s, float3 org, float3 dir
         if constexpr (kPretex) {
             const float4 b = P.st.base[s];
             base = f3(b.x, b.y, b.z);
-        } else if (!(m.flags & kMaterialUsesPtex)) {
+        } else if (m.flags & kMaterialUsesPtex) {
+            uint32_t pstatus = 0;
+            ptex_eval(static_cast<const PtexFace*>(hr.ptex_faces), int(hr.ptex_count),
+                      static_cast<const __half*>(hr.ptex_texels), int(m.ptex_base + __float_as_uint(p0.w)), hit.y,
+                      hit.z, base, pstatus);
+            status |= pstatus;
+        } else {
             base = tex2d_base_colour(m, attr, __float_as_uint(p0.w), hit.y, hit.z);
         }
     }
@@ -664,11 +671,11 @@ __global__ void __launch_bounds__(kBlock) k_vclass_scatter(VcmParams P, int cur)
 }
 
 template <bool kInst, bool kQuad>
-__global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur) {
+__global__ void __launch_bounds__(kBlock) k_vtexture(VcmParams P, int cur, const uint32_t* queue) {
     const uint32_t n = P.st.counters[cur];
     uint32_t status = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-        const uint32_t s = P.st.queue_sorted[e];
+        const uint32_t s = queue[e];
         const float4 hit = P.st.phit[s];
         const uint32_t tri = __float_as_uint(hit.w);
         if (tri == 0xffffffffu) continue;
@@ -1341,32 +1348,39 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
         else if (tb == 256) k_shadow<0, 256><<<trace_grid, 256, 0, stream>>>(P);
         else k_shadow<0, 128><<<trace_grid, 128, 0, stream>>>(P);
     };
-    // Ptex is filtered by the sort's texture pass only: scenes with Ptex always sort
-    const bool sort = sc.sort_hint != 0 || inst || sc.ptex_face_count > 0;
+    // Textures are filtered by the texture pass (k_vtexture) over the sorted queue when the hits are sorted; the
+    // plain form (SEL_OPTION_MATERIAL_SORT 0) filters triangle Ptex inline in queue order, and quad-mesh Ptex, which
+    // only the texture pass evaluates, over the queue in its own order
+    const bool sort = sc.sort_hint != 0 || inst;
     const bool quads = sc.ptex_quads != 0;
+    const bool pretex = sort || quads;
     const void* l_fn = inst ? reinterpret_cast<const void*>(&k_l_shade<true, true>)
-                            : sort ? reinterpret_cast<const void*>(&k_l_shade<true, false>)
-                                   : reinterpret_cast<const void*>(&k_l_shade<false, false>);
+                            : pretex ? reinterpret_cast<const void*>(&k_l_shade<true, false>)
+                                     : reinterpret_cast<const void*>(&k_l_shade<false, false>);
     const void* c_fn = inst ? reinterpret_cast<const void*>(&k_c_shade<true, true>)
-                            : sort ? reinterpret_cast<const void*>(&k_c_shade<true, false>)
-                                   : reinterpret_cast<const void*>(&k_c_shade<false, false>);
+                            : pretex ? reinterpret_cast<const void*>(&k_c_shade<true, false>)
+                                     : reinterpret_cast<const void*>(&k_c_shade<false, false>);
     const int l_grid = wave(l_fn);
     const int c_grid = wave(c_fn);
     const int connect_grid = wave(reinterpret_cast<const void*>(&k_c_connect));
     const int merge_grid = wave(reinterpret_cast<const void*>(&k_c_merge));
     // material-class sort and Ptex of a bounce's hits; returns the queue the shading kernel reads
     auto sort_hits = [&](cudaStream_t stream, int cur) -> const uint32_t* {
-        if (!sort) return st.queue[cur];
-        k_vclass_reset<<<1, 32, 0, stream>>>(st.counters);
-        if (inst) k_vclassify<true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        else k_vclassify<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        k_vclass_offsets<<<1, 32, 0, stream>>>(st.counters);
-        k_vclass_scatter<<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        if (inst && quads) k_vtexture<true, true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        else if (inst) k_vtexture<true, false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        else if (quads) k_vtexture<false, true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        else k_vtexture<false, false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
-        return st.queue_sorted;
+        if (!pretex) return st.queue[cur];
+        const uint32_t* q = st.queue[cur];
+        if (sort) {
+            k_vclass_reset<<<1, 32, 0, stream>>>(st.counters);
+            if (inst) k_vclassify<true><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            else k_vclassify<false><<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            k_vclass_offsets<<<1, 32, 0, stream>>>(st.counters);
+            k_vclass_scatter<<<shade_grid, kBlock, 0, stream>>>(P, cur);
+            q = st.queue_sorted;
+        }
+        if (inst && quads) k_vtexture<true, true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+        else if (inst) k_vtexture<true, false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+        else if (quads) k_vtexture<false, true><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+        else k_vtexture<false, false><<<shade_grid, kBlock, 0, stream>>>(P, cur, q);
+        return q;
     };
     // one pass; identical launches every pass (the pass reads its constants through st.iter)
     auto enqueue = [&](cudaStream_t stream) {
@@ -1379,7 +1393,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
             if (inst) k_l_shade<true, true><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
-            else if (sort) k_l_shade<true, false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
+            else if (pretex) k_l_shade<true, false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
             else k_l_shade<false, false><<<l_grid, kBlock, 0, stream>>>(P, cur, q);
             shadow(stream);
         }
@@ -1408,7 +1422,7 @@ cudaError_t vcm_run_passes(const PtScene& sc, const VcmCamera& cam, const VcmSet
             extend(stream, cur);
             const uint32_t* q = sort_hits(stream, cur);
             if (inst) k_c_shade<true, true><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
-            else if (sort) k_c_shade<true, false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
+            else if (pretex) k_c_shade<true, false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
             else k_c_shade<false, false><<<c_grid, kBlock, 0, stream>>>(P, cur, q);
             k_c_connect<<<connect_grid, kBlock, 0, stream>>>(P);
             k_c_merge<<<merge_grid, kBlock, 0, stream>>>(P);
