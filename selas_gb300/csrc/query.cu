@@ -107,7 +107,10 @@ __global__ void __launch_bounds__(kQueryBlock)
 // hit 1,417 against 1,431 Mrays/s, and the Cornell box's path tracer 11 % slower.  Node loads marked L2
 // evict_last (createpolicy + ld.global.nc.L2::cache_hint) left every set unchanged (1,432 against 1,431).
 // Nine blocks per SM (56 registers, a few bytes spilled) help the any-hit kernel (incoherent 2,069 against
-// 2,026 Mrays/s) and slow the closest-hit one (1,363 against 1,433), so each takes its own.
+// 2,026 Mrays/s) and slow the closest-hit one (1,363 against 1,433), so each takes its own.  The any-hit kernel
+// tests each step's leaf triangles with the whole warp (trace_wide_warp: incoherent 2,147 against 2,068, coherent
+// 14,660 against 14,200); for closest hit the shuffles, slots and key loads cost what the fuller warps save
+// (incoherent 1,416 against 1,434, coherent 7,780 against 8,240), so it keeps one lane per ray.
 template <bool kAnyHit>
 constexpr int kWideBlocksPerSm = kAnyHit ? 9 : 8;
 
@@ -117,11 +120,20 @@ __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm<kAnyHit>)
                  uint32_t record_float4s, uint32_t n, uint32_t* err) {
     __shared__ uint2 stack_mem[kWideStack * kQueryBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const bool valid = i < n;
     QueryHit h;
     uint32_t status = 0;
-    const bool found = trace_wide<kAnyHit>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
-                                           stack_mem + threadIdx.x, kQueryBlock, status);
+    bool found;
+    if constexpr (kAnyHit) {  // the warp tests its leaf triangles together; lanes past the batch stay to help
+        QueryRay r{};
+        if (valid) r = load_ray(rays + size_t(i) * record_float4s);
+        found = trace_wide_warp<true>(nodes, tris, valid, r, h, stack_mem + threadIdx.x, kQueryBlock, nullptr,
+                                      status);
+    } else {
+        if (!valid) return;
+        found = trace_wide<false>(nodes, tris, load_ray(rays + size_t(i) * record_float4s), h,
+                                  stack_mem + threadIdx.x, kQueryBlock, status);
+    }
     if (status) atomicOr(err, status);
     if (found) {
         if (kAnyHit)
@@ -190,12 +202,21 @@ __global__ void __launch_bounds__(kQueryBlock, kWideBlocksPerSm<kAnyHit>)
                          const uint32_t* ctl, uint32_t* err) {
     __shared__ uint2 stack_mem[kWideStack * kQueryBlock];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t r = ctl[0] ? order[i] : i;
+    const bool valid = i < n;
+    const uint32_t r = !valid ? 0u : (ctl[0] ? order[i] : i);
     QueryHit h;
     uint32_t status = 0;
-    const bool found = trace_wide<kAnyHit>(nodes, tris, load_ray(rays + size_t(r) * record_float4s), h,
-                                           stack_mem + threadIdx.x, kQueryBlock, status);
+    bool found;
+    if constexpr (kAnyHit) {
+        QueryRay ray{};
+        if (valid) ray = load_ray(rays + size_t(r) * record_float4s);
+        found = trace_wide_warp<true>(nodes, tris, valid, ray, h, stack_mem + threadIdx.x, kQueryBlock, nullptr,
+                                      status);
+    } else {
+        if (!valid) return;
+        found = trace_wide<false>(nodes, tris, load_ray(rays + size_t(r) * record_float4s), h,
+                                  stack_mem + threadIdx.x, kQueryBlock, status);
+    }
     if (status) atomicOr(err, status);
     if (found) {
         if (kAnyHit)

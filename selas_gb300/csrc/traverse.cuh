@@ -269,6 +269,133 @@ __device__ __forceinline__ bool trace_wide(const uint4* __restrict__ nodes, cons
     return s.hit.tri != 0xffffffffu;
 }
 
+// Warp-cooperative form (one ray per lane, all 32 lanes of the warp together, finished and idle lanes included):
+// each step every lane with a pending node visits it, then the warp tests the leaf triangles those visits exposed
+// together, 32 (ray, triangle) pairs a round, each lane testing one pair with its owner's ray taken by shuffles.
+// Incoherent rays leave most lanes of the one-lane form idle during leaf tests (9 of 32 active per instruction);
+// here the tests run on full warps.  The owner takes its candidates in the one-lane form's order (ascending
+// record index within a step) under the same rule (t < tfar, or t == tfar and a smaller (geomID, primID)), and a
+// candidate's t, u, v do not depend on the tfar it was tested against, so the hits are the same bits.
+// slots: this warp's 32 result slots in shared memory (closest hit only; any hit needs none).  The query kernels
+// use this form for any hit only: for closest hit it measured no faster than the one-lane form.
+struct CoopSlot {
+    float t, u, v;
+    uint32_t ti;
+};
+
+template <bool kAnyHit>
+__device__ __forceinline__ bool trace_wide_warp(const uint4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                bool valid, const QueryRay& r, QueryHit& hit, uint2* stack,
+                                                int stride, CoopSlot* slots, uint32_t& status) {
+    const uint32_t lane = threadIdx.x & 31u;
+    WideState s;
+    wide_init(s, r);
+    bool done = !valid || ray_untraceable(r);
+    while (__any_sync(0xffffffffu, !done)) {
+        uint32_t tmask = 0, tbase = 0;
+        if (!done && (s.group.y & 0xff000000u)) {
+            if (!wide_visit<kWideStack>(s, nodes, stack, stride, status, tmask, tbase)) {
+                done = true;
+                tmask = 0;
+            }
+        }
+        // pairs: lane L owns pairs [excl, incl) of the warp's concatenation, its set tmask bits in ascending order
+        const uint32_t cnt = __popc(tmask);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= uint32_t(o)) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        const uint32_t excl = incl - cnt;
+        const uint32_t kpack = uint32_t(s.wt.kx) | (uint32_t(s.wt.ky) << 2) | (uint32_t(s.wt.kz) << 4);
+        for (uint32_t r0 = 0; r0 < total; r0 += 32) {
+            const uint32_t j = r0 + lane;
+            uint32_t owner = 0;  // the first lane whose inclusive end exceeds j
+#pragma unroll
+            for (uint32_t step = 16; step >= 1; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xffffffffu, incl, owner + step - 1);
+                if (e <= j) owner += step;
+            }
+            const uint32_t o_mask = __shfl_sync(0xffffffffu, tmask, owner);
+            const uint32_t o_base = __shfl_sync(0xffffffffu, tbase, owner);
+            const uint32_t o_excl = __shfl_sync(0xffffffffu, excl, owner);
+            const uint32_t kp = __shfl_sync(0xffffffffu, kpack, owner);
+            Watertight w;
+            w.kx = int(kp & 3u);
+            w.ky = int((kp >> 2) & 3u);
+            w.kz = int((kp >> 4) & 3u);
+            w.sx = __shfl_sync(0xffffffffu, s.wt.sx, owner);
+            w.sy = __shfl_sync(0xffffffffu, s.wt.sy, owner);
+            w.sz = __shfl_sync(0xffffffffu, s.wt.sz, owner);
+            const float rox = __shfl_sync(0xffffffffu, s.ox, owner);
+            const float roy = __shfl_sync(0xffffffffu, s.oy, owner);
+            const float roz = __shfl_sync(0xffffffffu, s.oz, owner);
+            const float rtn = __shfl_sync(0xffffffffu, s.tnear, owner);
+            const float rtf = __shfl_sync(0xffffffffu, s.tfar, owner);
+            bool got = false;
+            float t = 0.0f, u = 0.0f, v = 0.0f;
+            uint32_t ti = 0xffffffffu;
+            const uint32_t bit = j < total ? __fns(o_mask, 0u, int(j - o_excl) + 1) : 0xffffffffu;
+            if (bit < 32u) {
+                ti = o_base + bit;
+                const float4* tp = tris + size_t(ti) * 3;
+                const float4 p0 = __ldg(tp), p1 = __ldg(tp + 1), p2 = __ldg(tp + 2);
+                got = watertight_intersect(w, rox, roy, roz, p0, p1, p2, rtn, rtf, t, u, v);
+            }
+            // this lane's own pairs in the round: [a, b) of the concatenation
+            const uint32_t a = excl > r0 ? excl : r0;
+            const uint32_t b = incl < r0 + 32 ? incl : r0 + 32;
+            if constexpr (kAnyHit) {
+                const uint32_t hits = __ballot_sync(0xffffffffu, got);
+                if (!done && a < b) {
+                    const uint32_t span = b - a;
+                    const uint32_t mine = (hits >> (a - r0)) & (span >= 32 ? 0xffffffffu : ((1u << span) - 1u));
+                    if (mine) {
+                        s.hit.tri = 0u;  // occluded: only the fact of a hit is reported
+                        done = true;
+                    }
+                }
+            } else {
+                slots[lane] = CoopSlot{t, u, v, got ? ti : 0xffffffffu};
+                __syncwarp();
+                for (uint32_t q = a; q < b; ++q) {
+                    const CoopSlot c = slots[q - r0];
+                    if (c.ti == 0xffffffffu || c.t > s.tfar) continue;
+                    const float4* cp = tris + size_t(c.ti) * 3;
+                    const uint64_t key = (uint64_t(__float_as_uint(__ldg(&cp[1].w))) << 32) |
+                                         uint64_t(__float_as_uint(__ldg(&cp[0].w)));
+                    if (c.t < s.tfar || key < s.best_key) {
+                        s.tfar = c.t;
+                        s.best_key = key;
+                        s.hit.t = c.t;
+                        s.hit.u = c.u;
+                        s.hit.v = c.v;
+                        s.hit.tri = c.ti;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (!done) {
+            if (++s.iters > kIterationCap) {
+                status |= kErrIterationCap;
+                done = true;
+            } else if (!(s.group.y & 0xff000000u)) {
+                if (s.sp == 0) {
+                    done = true;
+                } else {
+                    --s.sp;
+                    s.group = stack[s.sp * stride];
+                }
+            }
+        }
+    }
+    hit = s.hit;
+    return valid && s.hit.tri != 0xffffffffu;
+}
+
 // ---------------------------------------------------------------------------------------------------
 // Binary FP32 BVH (the plain GPU path): classic stack traversal, nearer child first.
 // `stack` points at this thread's first int entry; entries are `stride` ints apart.
