@@ -110,7 +110,9 @@ __global__ void __launch_bounds__(kQueryBlock)
 // 2,026 Mrays/s) and slow the closest-hit one (1,363 against 1,433), so each takes its own.  The any-hit kernel
 // tests each step's leaf triangles with the whole warp (trace_wide_warp: incoherent 2,147 against 2,068, coherent
 // 14,660 against 14,200); for closest hit the shuffles, slots and key loads cost what the fuller warps save
-// (incoherent 1,416 against 1,434, coherent 7,780 against 8,240), so it keeps one lane per ray.
+// (incoherent 1,416 against 1,434, coherent 7,780 against 8,240), so it keeps one lane per ray.  Choosing per
+// step (each lane its own triangles unless one lane holds 1.5x more pairs than the warp's rounds) was slower
+// still (1,402 and 7,780): the warp-synchronous loop itself costs the closest-hit kernel.
 template <bool kAnyHit>
 constexpr int kWideBlocksPerSm = kAnyHit ? 9 : 8;
 
