@@ -29,7 +29,9 @@ def test_small_scene_matches_bruteforce(device, kind):
     soup = data.soup()
     sc = _scene(device, data, kind)
     cam = scenes.camera_basis([0.0, 70.0, -170.0], [0.0, 40.0, 0.0], [0.0, 1.0, 0.0], 60.0, 96, 96)
-    for org, d in (scenes.primary_rays(cam), scenes.surface_rays(data, 8000, seed=5)):
+    # 8,003 surface rays: the last warp has lanes past the batch, which the any-hit kernel's warp-wide leaf tests
+    # keep as helpers
+    for org, d in (scenes.primary_rays(cam), scenes.surface_rays(data, 8003, seed=5)):
         got, want = sel.make_rayhits(org, d), sel.make_rayhits(org, d)
         sc.intersect1M(got)
         oracle.intersect_bruteforce(soup, want)
