@@ -511,6 +511,25 @@ __global__ void __launch_bounds__(B, 1024 / B) k_shadow(VcmParams P) {
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const uint32_t e = base + (threadIdx.x & 31u);
+        // 8-wide layout: the packet's lanes test their leaf triangles together (trace_wide_warp): passes 1.2 % faster
+        // on the room at 1280 x 720 (20.54 against 20.79 ms).  The path tracer's shadow kernel, whose packets can mix
+        // jobs' scenes, measured 3 % slower this way on the Cornell box and keeps one lane per ray.
+        if constexpr (K == 0) {
+            float4 c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (e < n) c = P.st.sc[e];
+            const bool live = c.x != 0.0f || c.y != 0.0f || c.z != 0.0f;
+            QueryRay q{};
+            if (live) {
+                const float4 o = P.st.so[e], d = P.st.sd[e];
+                q.ox = o.x; q.oy = o.y; q.oz = o.z; q.tnear = o.w;
+                q.dx = d.x; q.dy = d.y; q.dz = d.z; q.tfar = d.w;
+            }
+            QueryHit h;
+            const bool hit = trace_wide_warp<true>(static_cast<const uint4*>(P.nodes), P.tris, live, q, h,
+                                                   stack_mem + threadIdx.x, B, nullptr, status);
+            if (live && !hit) splat(P.accum, __float_as_uint(c.w), f3(c.x, c.y, c.z));
+            continue;
+        }
         if (e < n) {
             const float4 c = P.st.sc[e];
             if (c.x != 0.0f || c.y != 0.0f || c.z != 0.0f) {
