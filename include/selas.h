@@ -231,7 +231,9 @@ int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsigned int M, 
 /* Device-memory forms: d_rayhits / d_rays point to HBM, work is queued on `stream` (void* holding a
  * cudaStream_t, NULL = default stream) and the call returns without waiting.  Replace the packet
  * queries rtcIntersect8 / rtcOccluded8 of Source/Applications/Selas/Source/DeferredPathTracer.cpp:191,267
- * for whole ray batches.  Use sel_device_sync to wait and collect kernel errors. */
+ * for whole ray batches.  Use sel_device_sync to wait and collect kernel errors.  With SEL_OPTION_RAY_SORT,
+ * batches of 1,048,576 records or more take stream-ordered scratch (cudaMallocAsync / cudaFreeAsync from the
+ * device's default memory pool, 16 bytes a record) for their key sort; otherwise the calls allocate nothing. */
 int sel_intersect_device(SelScene scene, SelRayHit* d_rayhits, unsigned int n, void* stream);
 int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* stream);
 
