@@ -94,6 +94,9 @@ const char* sel_get_last_error(void);
 /* Device lifetime.  Replaces rtcNewDevice / rtcReleaseDevice (rtcore_device.h; called at           */
 /* Source/Applications/Selas/Source/main.cpp:99).  cuda_device selects the GPU.                      */
 /* ------------------------------------------------------------------------------------------------ */
+/* Also sets the release threshold of that GPU's default memory pool (this process's, shared with any other
+ * cudaMallocAsync user in it) to keep freed memory, so the stream-ordered scratch of ordered queries is reused
+ * instead of returned to the driver at every synchronisation. */
 int sel_device_new(int cuda_device, SelDevice* out_device);
 int sel_device_release(SelDevice device);
 /* Waits for `stream` and returns SEL_ERR_DEVICE_LIMIT if any kernel of this device raised its error
