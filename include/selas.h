@@ -94,9 +94,6 @@ const char* sel_get_last_error(void);
 /* Device lifetime.  Replaces rtcNewDevice / rtcReleaseDevice (rtcore_device.h; called at           */
 /* Source/Applications/Selas/Source/main.cpp:99).  cuda_device selects the GPU.                      */
 /* ------------------------------------------------------------------------------------------------ */
-/* Also sets the release threshold of that GPU's default memory pool (this process's, shared with any other
- * cudaMallocAsync user in it) to keep freed memory, so the stream-ordered scratch of ordered queries is reused
- * instead of returned to the driver at every synchronisation. */
 int sel_device_new(int cuda_device, SelDevice* out_device);
 int sel_device_release(SelDevice device);
 /* Waits for `stream` and returns SEL_ERR_DEVICE_LIMIT if any kernel of this device raised its error
@@ -235,8 +232,8 @@ int sel_intersect1M_noalloc(SelScene scene, SelRayHit* rayhits, unsigned int M, 
  * cudaStream_t, NULL = default stream) and the call returns without waiting.  Replace the packet
  * queries rtcIntersect8 / rtcOccluded8 of Source/Applications/Selas/Source/DeferredPathTracer.cpp:191,267
  * for whole ray batches.  Use sel_device_sync to wait and collect kernel errors.  With SEL_OPTION_RAY_SORT,
- * batches of 1,048,576 records or more take stream-ordered scratch (cudaMallocAsync / cudaFreeAsync from the
- * device's default memory pool, 16 bytes a record) for their key sort; otherwise the calls allocate nothing. */
+ * batches of 1,048,576 records or more take stream-ordered scratch for their key sort (16 bytes a record, from a
+ * memory pool the SelDevice owns and keeps filled); otherwise the calls allocate nothing. */
 int sel_intersect_device(SelScene scene, SelRayHit* d_rayhits, unsigned int n, void* stream);
 int sel_occluded_device(SelScene scene, SelRay* d_rays, unsigned int n, void* stream);
 

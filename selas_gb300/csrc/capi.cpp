@@ -78,6 +78,7 @@ DeviceBvh device_bvh(const SelSceneTy* sc) {
         b.hi[a] = sc->info.bounds_hi[a];
     }
     b.order_rays = sc->dev->ray_sort;
+    b.pool = sc->dev->order_pool;
     return b;
 }
 
@@ -119,15 +120,19 @@ int sel_device_new(int cuda_device, SelDevice* out_device) {
     // The allocation-free query's staging array: resolving its address here loads its module (and so
     // creates the array) while the device is being set up, not inside the first allocation-free call.
     if (e == cudaSuccess && resolve_noalloc_staging(dev) != SEL_OK) e = cudaErrorInvalidSymbol;
-    // The ray-order scratch of large queries is stream-ordered (cudaMallocAsync from the device's default pool):
-    // the pool keeps freed memory for the next query instead of returning it at every synchronisation.
+    // The ray-order scratch of large queries is stream-ordered, from a pool of the device's own that keeps freed
+    // memory for the next query instead of returning it at every synchronisation.
     if (e == cudaSuccess) {
-        cudaMemPool_t pool = nullptr;
-        e = cudaDeviceGetDefaultMemPool(&pool, cuda_device);
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = cuda_device;
+        e = cudaMemPoolCreate(&dev->order_pool, &props);
         uint64_t keep = ~uint64_t(0);
-        if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e == cudaSuccess) e = cudaMemPoolSetAttribute(dev->order_pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     if (e != cudaSuccess) {
+        if (dev->order_pool) cudaMemPoolDestroy(dev->order_pool);
         if (dev->stream) cudaStreamDestroy(dev->stream);
         for (cudaStream_t q : dev->qstream)
             if (q) cudaStreamDestroy(q);
@@ -149,6 +154,7 @@ int sel_device_release(SelDevice device) {
         cudaStreamDestroy(q);
     }
     cudaFree(device->d_err);
+    if (device->order_pool) cudaMemPoolDestroy(device->order_pool);  // released once its last block is freed
     delete device;
     return SEL_OK;
 }

@@ -16,6 +16,7 @@ struct SelDeviceTy {
     cudaStream_t stream = nullptr;  // internal stream for the host-memory entry points
     cudaStream_t qstream[4] = {nullptr, nullptr, nullptr, nullptr};  // pipelined host-memory queries (chunk k on k % 4)
     uint32_t* d_err = nullptr;      // kernel error word (iteration cap / stack overflow bits)
+    cudaMemPool_t order_pool = nullptr;  // stream-ordered scratch of ordered queries (keeps freed memory)
     bool graph_replay = true;       // SEL_OPTION_GRAPH_REPLAY
     bool material_sort = true;      // SEL_OPTION_MATERIAL_SORT
     bool ray_sort = false;          // SEL_OPTION_RAY_SORT

@@ -236,7 +236,8 @@ cudaError_t launch_query_ordered(const DeviceBvh& bvh, float4* d_rays, uint32_t 
     const size_t hist = size_t(256) * ntiles;
     const size_t words = 4 * size_t(n) + hist + (hist + 1) + scan_scratch_words(hist + 1) + 1;
     uint32_t* mem = nullptr;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&mem), words * 4, s);
+    cudaError_t e = bvh.pool ? cudaMallocFromPoolAsync(reinterpret_cast<void**>(&mem), words * 4, bvh.pool, s)
+                             : cudaMallocAsync(reinterpret_cast<void**>(&mem), words * 4, s);
     if (e != cudaSuccess) return e;
     uint32_t* keys[2] = {mem, mem + n};
     uint32_t* vals[2] = {mem + 2 * size_t(n), mem + 3 * size_t(n)};

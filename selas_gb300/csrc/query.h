@@ -16,6 +16,7 @@ struct DeviceBvh {
     const InstanceRecord* insts = nullptr;  // instance table of a scene with instances (8-wide layout only)
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // scene bounds (ray ordering keys)
     bool order_rays = false;  // SEL_OPTION_RAY_SORT: large incoherent batches in HBM are traced in key order
+    cudaMemPool_t pool = nullptr;  // the device's pool for the ordering scratch
 };
 
 cudaError_t launch_intersect(const DeviceBvh& bvh, SelRayHit* d_rays, uint32_t n, uint32_t* d_err, cudaStream_t s);
